@@ -1,0 +1,111 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Loaded by tests/, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
+``--impl reference`` legs of bench.py -- never by the GPU library.  The oracle
+restates the reference's calcNewDay/routing in C (wg_oracle.c); ``build()``
+compiles it with ``make`` into ``oracle/_build``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_build", "libwg_oracle.so")
+_lib = None
+
+_STATIC_FIELDS = [
+    ("ncell", ctypes.c_int32), ("nband", ctypes.c_int32), ("river_velo_opt", ctypes.c_int32),
+    ("pad0", ctypes.c_int32), ("default_velocity", ctypes.c_double),
+    ("lct_albedo", ctypes.c_void_p), ("lct_albedo_snow", ctypes.c_void_p), ("lct_ddf", ctypes.c_void_p),
+    ("lct_lai_a", ctypes.c_void_p), ("lct_lai_b", ctypes.c_void_p), ("lct_initial_days", ctypes.c_void_p),
+    ("area_km2", ctypes.c_void_p), ("lat_deg", ctypes.c_void_p), ("contfreq", ctypes.c_void_p),
+    ("lct", ctypes.c_void_p), ("built_up", ctypes.c_void_p), ("smax", ctypes.c_void_p),
+    ("lai_max", ctypes.c_void_p), ("gw_factor", ctypes.c_void_p), ("rg_max", ctypes.c_void_p),
+    ("texture", ctypes.c_void_p), ("ldd", ctypes.c_void_p), ("aindex", ctypes.c_void_p),
+    ("elev", ctypes.c_void_p), ("param", ctypes.c_void_p),
+    ("loc_lake", ctypes.c_void_p), ("loc_wetl", ctypes.c_void_p), ("glo_wetl", ctypes.c_void_p),
+    ("glo_lake", ctypes.c_void_p), ("glo_res", ctypes.c_void_p),
+    ("lake_area", ctypes.c_void_p), ("res_area", ctypes.c_void_p), ("stor_cap", ctypes.c_void_p),
+    ("mean_outflow", ctypes.c_void_p), ("mean_demand", ctypes.c_void_p), ("res_type", ctypes.c_void_p),
+    ("start_month", ctypes.c_void_p),
+    ("river_length", ctypes.c_void_p), ("river_slope", ctypes.c_void_p), ("roughness", ctypes.c_void_p),
+    ("bankfull", ctypes.c_void_p), ("downstream", ctypes.c_void_p), ("rout_order", ctypes.c_void_p),
+]
+
+_STATE_ORDER = ["canopy", "soil", "snow", "snow_band", "lai_days", "lai_status", "lai_precsum",
+                "gw", "river", "loclake", "locwetl", "glolake", "glowetl", "res",
+                "rf_loclake", "rf_locwetl", "rf_glolake", "rf_glowetl", "rf_res", "k_release",
+                "laf", "laf_prev", "fswb_next", "laf_started"]
+
+
+class _Static(ctypes.Structure):
+    _fields_ = _STATIC_FIELDS
+
+
+class _State(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_void_p) for f in _STATE_ORDER]
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(_LIB):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(_LIB)
+        _lib.wgo_init_state.argtypes = [ctypes.POINTER(_Static), ctypes.POINTER(_State)]
+        _lib.wgo_run.argtypes = [ctypes.POINTER(_Static), ctypes.POINTER(_State), ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                 ctypes.c_void_p, ctypes.c_int]
+        _lib.wgo_bottom_width.argtypes = [ctypes.c_double]
+        _lib.wgo_bottom_width.restype = ctypes.c_double
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Oracle:
+    """One region simulated by the CPU restatement; state arrays live in ``self.state``."""
+
+    def __init__(self, region):
+        from watergap2_gb300.region import empty_state
+        self.region = region
+        self._keep = []
+        st = _Static()
+        st.ncell, st.nband = region.ncell, region.nband
+        st.river_velo_opt, st.default_velocity = region.river_velo_opt, region.default_velocity
+        for name, ctype in _STATIC_FIELDS[5:]:
+            a = region.arrays[name]
+            self._keep.append(a)
+            setattr(st, name, a.ctypes.data)
+        self._static = st
+        self.state = empty_state(region.ncell, region.nband)
+        self._cstate = _State()
+        for f in _STATE_ORDER:
+            setattr(self._cstate, f, self.state[f].ctypes.data)
+        rc = lib().wgo_init_state(ctypes.byref(self._static), ctypes.byref(self._cstate))
+        if rc:
+            raise RuntimeError(f"wgo_init_state failed: {rc}")
+
+    def run(self, doy0, P, T, S, discharge=False, balance=False, nthreads=1):
+        P, T, S = (np.ascontiguousarray(x, np.float32) for x in (P, T, S))
+        nd = P.shape[0]
+        assert P.shape == (nd, self.region.ncell)
+        q = np.zeros((nd, self.region.ncell)) if discharge else None
+        b = np.zeros((nd, 6)) if balance else None
+        rc = lib().wgo_run(ctypes.byref(self._static), ctypes.byref(self._cstate), int(doy0), nd,
+                           _ptr(P), _ptr(T), _ptr(S), _ptr(q) if q is not None else None,
+                           _ptr(b) if b is not None else None, int(nthreads))
+        if rc:
+            raise RuntimeError(f"wgo_run failed: {rc}")
+        return q, b

@@ -1,0 +1,179 @@
+"""Run the reference's own code (oracle/_ref/wg_ref_harness) on a synthetic region.
+
+TEST INFRASTRUCTURE ONLY, and usable only where the reference sources exist
+(the build container): the harness is compiled from them by ``make ref``.  It
+writes the region as the input files the reference reads (big-endian UNF grids,
+LAI_22.DAT, LCT_22.DAT, a parameter JSON), runs the harness over ``ndays`` and
+returns the dumped state.  The reference always has 67,420 grid cells (def.h:10);
+the region occupies the first ``ncell`` of them and the rest are marked
+non-continental.
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+from watergap2_gb300.region import NPARAM, PARAM_JSON_KEYS
+
+NG = 67420
+REF_BANDS = 100
+_HERE = os.path.dirname(os.path.abspath(__file__))
+HARNESS = os.path.join(_HERE, "_ref", "wg_ref_harness")
+SNAP_FIELDS = ["canopy", "soil", "snow", "lai_days", "lai_status", "lai_precsum", "gw", "river", "loclake",
+               "locwetl", "glolake", "glowetl", "res", "rf_loclake", "rf_locwetl", "rf_glolake", "rf_glowetl",
+               "rf_res", "k_release", "laf", "laf_prev", "rs", "gwr"]
+
+
+def available() -> bool:
+    return os.path.exists(HARNESS)
+
+
+def build() -> bool:
+    src = os.environ.get("WG_REFERENCE_SOURCE", "/root/reference/source")
+    if not os.path.isdir(src):
+        return False
+    subprocess.run(["make", "-s", "-C", _HERE, "-j8", "ref", f"REF={src}"], check=True)
+    return True
+
+
+def _unf(path, arr, dt):
+    np.asarray(arr).astype(dt).astype(np.dtype(dt).newbyteorder(">")).tofile(path)
+
+
+def _full(values, dtype, fill=0):
+    out = np.full(NG, fill, dtype)
+    out[: values.shape[0]] = values
+    return out
+
+
+def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000):
+    n = region.ncell
+    if n > NG:
+        raise ValueError("region larger than the reference grid")
+    reg = region if region.nband == REF_BANDS else region.with_bands(REF_BANDS)
+    resopt = int(np.any(region.res_area > 0))
+    os.makedirs(os.path.join(d, "G_RES"), exist_ok=True)
+    rows = region.row.astype(np.int16)
+    cols = region.col.astype(np.int16)
+    # geometry (geo.init, source/geo.cpp:7-81)
+    area_rows = np.zeros(360, np.float32)
+    area_rows[rows - 1] = region.area_km2.astype(np.float32)
+    _unf(f"{d}/GAREA.UNF0", area_rows, np.float32)
+    _unf(f"{d}/GR.UNF2", _full(rows, np.int16, 1), np.int16)
+    _unf(f"{d}/GC.UNF2", _full(cols, np.int16, 1), np.int16)
+    _unf(f"{d}/GCRC.UNF4", np.zeros(360 * 720, np.int32), np.int32)
+    _unf(f"{d}/GCONTFREQ.UNF0", _full(region.contfreq, np.float32), np.float32)
+    f32 = lambda name: _full(region.arrays[name], np.float32)
+    _unf(f"{d}/G_LOCLAK.UNF0", f32("loc_lake"), np.float32)
+    _unf(f"{d}/G_GLOLAK.UNF0", f32("glo_lake"), np.float32)
+    _unf(f"{d}/G_LOCWET.UNF0", f32("loc_wetl"), np.float32)
+    _unf(f"{d}/G_GLOWET.UNF0", f32("glo_wetl"), np.float32)
+    _unf(f"{d}/G_LOCRES.UNF0", np.zeros(NG, np.float32), np.float32)
+    _unf(f"{d}/G_RES/G_RES_FRAC.UNF0", f32("glo_res"), np.float32)
+    _unf(f"{d}/G_RES/G_RES_2000.UNF0", f32("glo_res"), np.float32)
+    _unf(f"{d}/G_LAKAREA.UNF0", f32("lake_area"), np.float32)
+    _unf(f"{d}/G_RESAREA.UNF0", f32("res_area"), np.float32)
+    _unf(f"{d}/G_REGLAKE.UNF0", np.zeros(NG, np.float32), np.float32)
+    _unf(f"{d}/G_REG_LAKE.UNF1", np.zeros(NG, np.int8), np.int8)
+    _unf(f"{d}/G_OUTFLOW_CELL_ASSIGNMENT.UNF4", np.zeros(NG, np.int32), np.int32)
+    down = _full(region.downstream.astype(np.int32) + 1, np.int32)     # 1-based, 0 = outlet
+    down[down < 0] = 0
+    _unf(f"{d}/G_OUTFLC.UNF4", down, np.int32)
+    _unf(f"{d}/G_RES_TYPE.UNF1", _full(region.res_type, np.int8, 2), np.int8)
+    _unf(f"{d}/G_START_YEAR.UNF4", np.full(NG, 1900, np.int32), np.int32)
+    _unf(f"{d}/G_START_MONTH.UNF1", _full(region.start_month, np.int8, 1), np.int8)
+    _unf(f"{d}/G_MEAN_OUTFLOW.UNF0", _full(region.extras["mean_outflow_km3_month"], np.float32), np.float32)
+    _unf(f"{d}/G_STORAGE_CAPACITY.UNF0", f32("stor_cap"), np.float32)
+    _unf(f"{d}/G_NUs_1971_2000.UNF0", np.zeros(NG, np.float32), np.float32)
+    _unf(f"{d}/G_ALLOC_COEFF.5.UNF0", np.zeros(NG * 5, np.float32), np.float32)
+    _unf(f"{d}/G_RIVER_LENGTH.UNF0", _full(region.extras["river_length_file"], np.float32, 50.0), np.float32)
+    _unf(f"{d}/G_RIVERSLOPE.UNF0", _full(region.river_slope, np.float32, 1e-3), np.float32)
+    _unf(f"{d}/G_ROUGHNESS.UNF0", _full(region.roughness, np.float32, 0.03), np.float32)
+    _unf(f"{d}/G_BANKFULL.UNF0", _full(region.bankfull, np.float32, 1.0), np.float32)
+    # routing order: G_ROUT_ORDER[cell] = 1-based position; padding cells come last
+    pos = np.empty(NG, np.int32)
+    pos[region.rout_order] = np.arange(n, dtype=np.int32) + 1
+    pos[n:] = np.arange(n, NG, dtype=np.int32) + 1
+    _unf(f"{d}/G_ROUT_ORDER.UNF4", pos, np.int32)
+    ldd = _full(region.ldd, np.int8, 5)
+    _unf(f"{d}/G_LDD_2.UNF1", ldd, np.int8)
+    # land-cover tables (LAI_22.DAT: lai.cpp:110-149, LCT_22.DAT: daily.cpp:1925-1959)
+    tb = region.lct_tables
+    with open(f"{d}/LAI_22.DAT", "w") as f:
+        f.write("# synthetic LAI table\n")
+        for i in range(18):
+            f.write(f"{i + 1} {float(tb['lai'][i])!r} {float(tb['fdp'][i])!r} {float(tb['rfep'][i])!r} "
+                    f"{int(tb['initial_days'][i])} {float(tb['kc_min'][i])!r} {float(tb['kc_max'][i])!r}\n")
+    with open(f"{d}/LCT_22.DAT", "w") as f:
+        f.write("# synthetic land-cover table\n")
+        for i in range(18):
+            f.write(f"{i + 1} {float(tb['rooting'][i])!r} {float(tb['albedo'][i])!r} "
+                    f"{float(tb['albedo_snow'][i])!r} {float(tb['ddf'][i])!r} {float(tb['emissivity'][i])!r}\n")
+    par = region.arrays["param"].reshape(NPARAM, n)
+    obj = {}
+    for k, key in enumerate(PARAM_JSON_KEYS):
+        full = np.ones(NG)
+        full[:n] = par[k]
+        obj[key] = [float(x) for x in full]
+    with open(f"{d}/params.json", "w") as f:
+        json.dump(obj, f)
+    with open(f"{d}/config.txt", "w") as f:
+        f.write(f"routing {d}/ROUTING.DAT\nend_of_head\n")
+    # raw arrays the harness sets directly
+    region.lct.astype(np.uint8).tofile(f"{d}/c_lct.bin")
+    region.built_up.astype(np.float32).tofile(f"{d}/c_built_up.bin")
+    region.smax.astype(np.float32).tofile(f"{d}/c_smax.bin")
+    region.lai_max.astype(np.float32).tofile(f"{d}/c_lai_max.bin")
+    region.gw_factor.astype(np.float32).tofile(f"{d}/c_gw_factor.bin")
+    region.rg_max.astype(np.int16).tofile(f"{d}/c_rg_max.bin")
+    region.texture.astype(np.int8).tofile(f"{d}/c_texture.bin")
+    region.aindex.astype(np.int16).tofile(f"{d}/c_aindex.bin")
+    reg.elev.astype(np.int16).tofile(f"{d}/c_elev.bin")
+    np.asarray(stations, np.int32).tofile(f"{d}/c_stations.bin")
+    np.ascontiguousarray(P, np.float32).tofile(f"{d}/f_prec.bin")
+    np.ascontiguousarray(T, np.float32).tofile(f"{d}/f_temp.bin")
+    np.ascontiguousarray(S, np.float32).tofile(f"{d}/f_swrad.bin")
+    with open(f"{d}/meta.txt", "w") as f:
+        f.write(f"{n} {P.shape[0]} {doy0} {year0} {resopt} {region.river_velo_opt} {len(stations)} {len(snapshots)}\n")
+    with open(f"{d}/snapshots.txt", "w") as f:
+        f.write(" ".join(str(int(s)) for s in snapshots) + "\n")
+
+
+def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None):
+    """Run the reference harness; returns dict(lai_a, lai_b, bottom_width, snapshots=[{field: array}],
+    discharge=[ndays, nstation], stations=...)."""
+    if not available():
+        raise RuntimeError("reference harness not built (make -C oracle ref)")
+    ndays = P.shape[0]
+    n = region.ncell
+    if stations is None:
+        outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+        stations = outl[:40]
+    stations = np.asarray(stations, np.int32)
+    snapshots = list(snapshots or [ndays])
+    tmp = workdir or tempfile.mkdtemp(prefix="wg_ref_")
+    write_case(region, tmp, P, T, S, doy0, stations, snapshots)
+    out = os.path.join(tmp, "out.bin")
+    subprocess.run([HARNESS, tmp, out], check=True, stdout=subprocess.DEVNULL)
+    raw = np.fromfile(out, np.float64)
+    o = 0
+    res = {"lai_a": raw[o:o + 18].copy(), "lai_b": raw[o + 18:o + 36].copy()}
+    o += 36
+    res["bottom_width"] = raw[o:o + n].copy(); o += n
+    o += n   # land fraction before the first annualInit (unused)
+    snaps = []
+    for _ in snapshots:
+        snap = {}
+        for f in SNAP_FIELDS:
+            snap[f] = raw[o:o + n].copy(); o += n
+        bands = raw[o:o + REF_BANDS * n].reshape(REF_BANDS, n).T.copy(); o += REF_BANDS * n
+        snap["snow_band"] = bands
+        snaps.append(snap)
+    res["snapshots"] = snaps
+    res["discharge"] = raw[o:o + ndays * len(stations)].reshape(ndays, len(stations)).copy()
+    res["stations"] = stations
+    return res

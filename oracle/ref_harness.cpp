@@ -1,0 +1,230 @@
+// ref_harness.cpp -- drives the reference's own daily.cpp / routing.cpp object
+// code over a synthetic region, the way integrate_wghm_ does
+// (source/integrateWGHM.cpp:280-800), and dumps the resulting state.
+//
+// TEST INFRASTRUCTURE ONLY.  Built from the reference sources by
+// oracle/Makefile (target "ref") into oracle/_ref/; it exists in the build
+// container only and pins the C restatement (wg_oracle.c) to the reference.
+//
+// Inputs (directory argv[1], written by oracle/ref_case.py): the UNF grids
+// read by geo.init and routing.init, LAI_22.DAT, LCT_22.DAT, params.json,
+// config.txt, plus raw little-endian arrays for what the harness sets directly.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <sstream>
+#include <string>
+#include <vector>
+#include <array>
+#include <algorithm>
+#include <initializer_list>
+#include <type_traits>
+#include <iomanip>
+#include <set>
+#include <list>
+#include <functional>
+// The harness needs write access to a few members the reference keeps private
+// (laiClass::G_LAImax, calibParamClass::calibParamJson, LAI state for the dump).
+#define private public
+#define protected public
+#include "globals.h"
+#include "calib_param.h"
+#include "json11.hpp"
+#undef private
+#undef protected
+
+calibParamClass calibParam;   // defined in watergap.cpp in the reference, which the harness replaces
+
+template <class T>
+static std::vector<T> read_raw(const std::string &path, size_t count) {
+  std::vector<T> v(count);
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f) { fprintf(stderr, "harness: cannot open %s\n", path.c_str()); exit(2); }
+  if (fread(v.data(), sizeof(T), count, f) != count) { fprintf(stderr, "harness: short read %s\n", path.c_str()); exit(2); }
+  fclose(f);
+  return v;
+}
+
+static void write_raw(FILE *f, const double *p, size_t n) { fwrite(p, sizeof(double), n, f); }
+
+int main(int argc, char **argv) {
+  if (argc < 3) { fprintf(stderr, "usage: %s <case dir> <out file>\n", argv[0]); return 1; }
+  std::string dir = argv[1];
+  int ncase, ndays, doy0, year0, resopt, velo, nstation, nsnap;
+  {
+    std::ifstream m(dir + "/meta.txt");
+    m >> ncase >> ndays >> doy0 >> year0 >> resopt >> velo >> nstation >> nsnap;
+    if (!m) { fprintf(stderr, "harness: bad meta.txt\n"); return 2; }
+  }
+  std::vector<int> snap_days(nsnap);
+  {
+    std::ifstream m(dir + "/snapshots.txt");
+    for (int i = 0; i < nsnap; i++) m >> snap_days[i];
+  }
+
+  // options of the hot path (integrateWGHM.cpp / option.cpp defaults, then the configs' switches)
+  options.input_dir = dir; options.output_dir = dir; options.routing_dir = dir; options.climate_dir = dir;
+  options.water_use_dir = dir; options.land_cover_dir = dir;
+  options.basin = 1; options.fileEndianType = 2; options.grid_store = 0; options.grid_store_TypeForStorages = 0;
+  options.day_store = 0; options.cloud = 2; options.intercept = 1; options.calc_albedo = 0;
+  options.rout_prepare = 0; options.timeStepCheckFlag = 0; options.riverveloOpt = velo; options.time_series = 1;
+  options.subtract_use = 0; options.use_alloc = 0; options.delayedUseSatisfaction = 0; options.petOpt = 0;
+  options.clclOpt = 0; options.permaOpt = 0; options.resOpt = resopt; options.landCoverOpt = 0; options.use_kc = 0;
+  options.statcorrOpt = 0; options.aridareaOpt = 0; options.fractionalRoutingOpt = 0; options.riverEvapoOpt = 0;
+  options.aggrNUsGloLakResOpt = 0; options.climate_spatial_resolution = 0; options.resYearOpt = 0;
+  options.resYearReference = 2000; options.resYearFirstToUse = 1900; options.resYearLastToUse = 2010;
+  options.antNatOpt = 0; options.resNUsMeanYearFirst = 1971; options.resNUsMeanYearLast = 2000;
+  options.glacierOpt = 0; options.calc_wtemp = 0; options.start_year = year0; options.end_year = year0;
+  options.init_years = 0; options.time_step = 1; options.outLAImax = 0;
+
+  ConfigFile cfg(dir + "/config.txt", year0, 1, "OL");
+
+  geo.init(dir, 2);
+  auto lct = read_raw<unsigned char>(dir + "/c_lct.bin", ncase);
+  auto built = read_raw<float>(dir + "/c_built_up.bin", ncase);
+  auto smax = read_raw<float>(dir + "/c_smax.bin", ncase);
+  auto laimax = read_raw<float>(dir + "/c_lai_max.bin", ncase);
+  auto fg = read_raw<float>(dir + "/c_gw_factor.bin", ncase);
+  auto rg = read_raw<short>(dir + "/c_rg_max.bin", ncase);
+  auto tex = read_raw<signed char>(dir + "/c_texture.bin", ncase);
+  auto aind = read_raw<short>(dir + "/c_aindex.bin", ncase);
+  auto elev = read_raw<short>(dir + "/c_elev.bin", (size_t)ncase * 101);
+  auto stations = read_raw<int>(dir + "/c_stations.bin", nstation);
+  for (int n = 0; n < ng; n++) {
+    land.G_landCover[n] = n < ncase ? (char)lct[n] : 1;
+    land.G_built_up[n] = n < ncase ? built[n] : 0.f;
+    G_aindex[n] = n < ncase ? aind[n] : 0;
+    G_toBeCalculated[n] = 1;
+  }
+
+  // cell-specific calibration parameters: the JSON object calibParamClass::getValue reads
+  {
+    std::ifstream f(dir + "/params.json");
+    std::stringstream ss; ss << f.rdbuf();
+    std::string err;
+    calibParam.calibParamJson = json11::Json::parse(ss.str(), err);
+    if (!err.empty()) { fprintf(stderr, "harness: json: %s\n", err.c_str()); return 2; }
+  }
+
+  WghmStateFile wghmState(ng, 31);
+  AdditionalOutputInputFile additionalOutIn;
+  SnowInElevationFile snowIO;
+
+  cbasin.cellNum.clear();
+  for (int i = 0; i < nstation; i++) cbasin.cellNum.push_back(stations[i] + 1);
+  cbasin.numberOfCalibBasins = 0;
+
+  lai.init(dir, dir, land.G_landCover, additionalOutIn, calibParam);
+  for (int n = 0; n < ncase; n++) lai.G_LAImax[n] = laimax[n];
+  dailyWaterBalance.init(dir, nstation);
+  routing.init(nstation, cfg, wghmState, additionalOutIn);
+  routing.initLakeDepthActive(calibParam);
+  routing.initWetlDepthActive(calibParam);
+  routing.initFractionStatus();
+  routing.setStoragesToZero();
+  routing.setLakeWetlToMaximum(options.start_year);
+  for (int n = 0; n < ng; n++) {
+    dailyWaterBalance.G_gammaHBV[n] = calibParam.getValue(P_GAMRUN_C, n);
+    dailyWaterBalance.G_cellCorrFact[n] = calibParam.getValue(P_CFA, n);
+    routing.G_statCorrFact[n] = calibParam.getValue(P_CFS, n);
+  }
+  dailyWaterBalance.setStoragesToZero();
+  for (int n = 0; n < ng; n++) {
+    maxSoilWaterCap.G_Smax[n] = n < ncase ? smax[n] : 0.f;
+    GW.setgwFactor(n, n < ncase ? fg[n] : 0.f);
+    GW.setRgmax(n, n < ncase ? rg[n] : 0);
+    GW.G_texture[n] = n < ncase ? tex[n] : 0;
+    for (int e = 0; e < 101; e++) dailyWaterBalance.G_Elevation(n, e) = n < ncase ? elev[(size_t)n * 101 + e] : 0;
+  }
+
+  FILE *out = fopen(argv[2], "wb");
+  if (!out) { fprintf(stderr, "harness: cannot write %s\n", argv[2]); return 2; }
+  // the LAI factors the reference derived (checked against the restatement's inputs)
+  {
+    std::vector<double> la(18), lb(18);
+    for (int i = 0; i < 18; i++) { la[i] = lai.lai_factor_a[i]; lb[i] = lai.lai_factor_b[i]; }
+    write_raw(out, la.data(), 18); write_raw(out, lb.data(), 18);
+    std::vector<double> g(ncase);
+    for (int n = 0; n < ncase; n++) g[n] = routing.G_riverBottomWidth[n];
+    write_raw(out, g.data(), ncase);
+    for (int n = 0; n < ncase; n++) g[n] = routing.G_landAreaFrac[n];
+    write_raw(out, g.data(), ncase);
+  }
+
+  const short first_day_in_month[12] = {1, 32, 60, 91, 121, 152, 182, 213, 244, 274, 305, 335};
+  const short last_day_in_month[12] = {30, 58, 89, 119, 150, 180, 211, 242, 272, 303, 333, 364};
+  auto P = read_raw<float>(dir + "/f_prec.bin", (size_t)ndays * ncase);
+  auto T = read_raw<float>(dir + "/f_temp.bin", (size_t)ndays * ncase);
+  auto S = read_raw<float>(dir + "/f_swrad.bin", (size_t)ndays * ncase);
+  std::vector<double> q((size_t)ndays * nstation, 0.0);
+
+  int year = year0;
+  int doy = doy0;
+  int snap_i = 0;
+  bool year_started = false;
+  for (int d = 0; d < ndays; d++) {
+    if (!year_started || doy == 1) {
+      dailyWaterBalance.annualInit();
+      routing.annualInit(year, 1, additionalOutIn);
+      year_started = true;
+    }
+    int month = 0;
+    while (month < 11 && doy >= first_day_in_month[month + 1]) month++;
+    short day_in_month = (short)(doy - first_day_in_month[month] + 1);
+    for (int n = 0; n < ncase; n++) {
+      climateYear.G_precipitation_d365(n, doy - 1) = P[(size_t)d * ncase + n];
+      climateYear.G_temperature_d365(n, doy - 1) = T[(size_t)d * ncase + n];
+      climateYear.G_shortwave_d365(n, doy - 1) = S[(size_t)d * ncase + n];
+    }
+    for (int n = 0; n < ng; ++n)
+      if (geo.G_contcell[n])
+        dailyWaterBalance.calcNewDay((short)doy, (short)month, day_in_month, last_day_in_month[month], (short)year, n,
+                                     wghmState, additionalOutIn, snowIO, 0, calibParam);
+    routing.routing((short)year, (short)doy, (short)month, day_in_month, last_day_in_month[month], wghmState,
+                    additionalOutIn, 0, calibParam);
+    routing.updateLandAreaFrac(additionalOutIn);
+    for (int b = 0; b < nstation; b++) q[(size_t)d * nstation + b] = routing.dailyRiverDischarge(b, doy - 1);
+    if (snap_i < nsnap && snap_days[snap_i] == d + 1) {
+      // state snapshot after day d+1, fixed field order (read by oracle/ref_case.py)
+      std::vector<double> g(ncase);
+#define DUMP(expr) do { for (int n = 0; n < ncase; n++) g[n] = (double)(expr); write_raw(out, g.data(), ncase); } while (0)
+      DUMP(dailyWaterBalance.G_canopyWaterContent[n]);
+      DUMP(dailyWaterBalance.G_soilWaterContent[n]);
+      DUMP(dailyWaterBalance.G_snow[n]);
+      DUMP(lai.G_days_since_start[n]);
+      DUMP(lai.G_GrowingStatus[n]);
+      DUMP(lai.G_PrecSum[n]);
+      DUMP(routing.G_groundwaterStorage[n]);
+      DUMP(routing.G_riverStorage[n]);
+      DUMP(routing.G_locLakeStorage[n]);
+      DUMP(routing.G_locWetlStorage[n]);
+      DUMP(routing.G_gloLakeStorage[n]);
+      DUMP(routing.G_gloWetlStorage[n]);
+      DUMP(routing.G_gloResStorage[n]);
+      DUMP(routing.G_locLakeAreaReductionFactor[n]);
+      DUMP(routing.G_locWetlAreaReductionFactor[n]);
+      DUMP(routing.G_gloLakeEvapoReductionFactor[n]);
+      DUMP(routing.G_gloWetlAreaReductionFactor[n]);
+      DUMP(routing.G_gloResEvapoReductionFactor[n]);
+      DUMP(routing.K_release[n]);
+      DUMP(routing.G_landAreaFrac[n]);
+      DUMP(routing.G_landAreaFracPrevTimestep[n]);
+      DUMP(dailyWaterBalance.G_dailyLocalSurfaceRunoff[n]);
+      DUMP(dailyWaterBalance.G_dailyGwRecharge[n]);
+      for (int e = 1; e <= 100; e++) DUMP(dailyWaterBalance.G_SnowInElevation(n, e));
+#undef DUMP
+      snap_i++;
+    }
+    doy = doy % 365 + 1;
+    if (doy == 1) year++;
+  }
+  write_raw(out, q.data(), q.size());
+  fclose(out);
+  return 0;
+}

@@ -1,0 +1,117 @@
+/*
+ * wg_oracle.h -- CPU restatement of the WaterGAP2 daily step (oracle).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker for the GPU library, never a
+ * part of it: only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline
+ * leg load it.  It restates, in plain C and cell by cell, the reference's
+ *   dailyWaterBalanceClass::calcNewDay   (source/daily.cpp:94-1257)
+ *   laiClass::getDailyLai / dailyLai_*    (source/lai.cpp:152-293)
+ *   dailyWaterBalanceClass::calc_ext_rad  (source/daily.cpp:2398-2449)
+ *   routingClass::routing                 (source/routing.cpp:1629-4520, 5034-5188)
+ *   routingClass::updateLandAreaFrac      (source/routing.cpp:5343-5352)
+ *   routingClass::getRiverVelocity / getNewRiverVelocity (source/routing.cpp:7274-7341)
+ * for the option set of the hot path (time_series=1, cloud=2, petOpt=0,
+ * intercept=1, use_kc=0, calc_albedo=0, clclOpt=0, subtract_use=0,
+ * fractionalRoutingOpt=0, aridareaOpt=0, riverEvapoOpt=0, statcorrOpt=0,
+ * use_alloc=0, glacierOpt=0, calc_wtemp=0, riverveloOpt 0/1/2).
+ *
+ * Parity pin: in the build container this restatement is compared with the
+ * reference's own daily.cpp/routing.cpp object code, linked into a harness
+ * (oracle/ref_harness.cpp); the comparison produced the golden fixtures in
+ * tests/golden/.  All arithmetic keeps the reference's expression order and
+ * is compiled with -ffp-contract=off so that x86 and Arm agree.
+ */
+#ifndef WG_ORACLE_H
+#define WG_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Calibration parameters, in the order of eCalibParam (source/calib_param.h:72-101). */
+enum {
+  WGO_P_GAMRUN_C = 0, WGO_P_CFA, WGO_P_CFS, WGO_M_ROOT_D, WGO_M_RIVRGH_C, WGO_P_LAK_D,
+  WGO_P_WET_D, WGO_P_SWOUTF_C, WGO_M_EVAREDEX, WGO_M_NETRAD, WGO_P_PTC_HUM, WGO_P_PTC_ARI,
+  WGO_P_PET_MXDY, WGO_P_MCWH, WGO_M_LAI, WGO_P_T_SNOWFZ, WGO_P_T_SNOWMT, WGO_M_DEGDAY_F,
+  WGO_P_T_GRADNT, WGO_M_GW_F, WGO_M_RG_MAX, WGO_P_PCRITGWA, WGO_P_GWOUTF_C, WGO_M_NETABSSW,
+  WGO_M_NETABSGW, WGO_M_PREC, WGO_NPARAM
+};
+
+/* Static description of a region: all arrays are caller-owned, length ncell
+ * unless stated.  Value types follow the reference's storage types. */
+typedef struct {
+  int32_t ncell;
+  int32_t nband;            /* snow elevation bands (reference: 100)            */
+  int32_t river_velo_opt;   /* options.riverveloOpt: 0 constant, 1 inflow-, 2 storage-based */
+  int32_t pad0;
+  double  default_velocity; /* routingClass::defaultRiverVelocity [km/d]       */
+  /* land-cover tables, 18 entries (LCT_22.DAT, LAI_22.DAT)                    */
+  const double  *lct_albedo, *lct_albedo_snow, *lct_ddf;
+  const float   *lct_lai_a, *lct_lai_b;     /* 0.1*fdp, (1-fdp)*rfep (float)  */
+  const int16_t *lct_initial_days;
+  /* geometry                                                                  */
+  const double  *area_km2;    /* geo.areaOfCellByArrayPos                      */
+  const double  *lat_deg;     /* -(G_row/2 - 90.25)                             */
+  const double  *contfreq;    /* geo.G_contfreq [%]                            */
+  /* land                                                                      */
+  const uint8_t *lct;         /* land.G_landCover, 1..18                       */
+  const float   *built_up;    /* land.G_built_up                               */
+  const float   *smax;        /* maxSoilWaterCap.G_Smax [mm]                   */
+  const float   *lai_max;     /* laiClass::G_LAImax                            */
+  const float   *gw_factor;   /* GW.getgwFactor                                 */
+  const int16_t *rg_max;      /* GW.getRgmax (x100)                            */
+  const int8_t  *texture;     /* GW.G_texture                                   */
+  const int8_t  *ldd;         /* G_LDD (sign: <0 inland sink)                  */
+  const int16_t *aindex;      /* G_aindex (1 arid, 0 humid)                    */
+  const int16_t *elev;        /* [ncell*(nband+1)]: [0] mean, [1..] bands asc  */
+  const double  *param;       /* [WGO_NPARAM*ncell] calibParam values           */
+  /* surface water bodies                                                      */
+  const double  *loc_lake, *loc_wetl, *glo_wetl, *glo_lake, *glo_res; /* [%]  */
+  const double  *lake_area, *res_area;   /* km2 (outflow cell)                 */
+  const double  *stor_cap;    /* km3                                           */
+  const double  *mean_outflow;/* m3/s (after routing.init conversion)          */
+  const double  *mean_demand; /* m3/s                                          */
+  const int8_t  *res_type;    /* 1 irrigation, 2 other                         */
+  const int8_t  *start_month; /* 1..12                                          */
+  /* river                                                                     */
+  const double  *river_length;/* km, already x contfreq/100                    */
+  const double  *river_slope, *roughness, *bankfull; /* as read (float values) */
+  /* topology                                                                  */
+  const int32_t *downstream;  /* 0-based, -1 outlet / sink                      */
+  const int32_t *rout_order;  /* cells in processing order (G_routingCell-1)   */
+} wgo_static;
+
+/* Dynamic state, caller-owned, updated in place. */
+typedef struct {
+  double *canopy, *soil, *snow /* G_snow */, *snow_band /* [ncell*nband] */;
+  int32_t *lai_days, *lai_status; double *lai_precsum;
+  double *gw, *river, *loclake, *locwetl, *glolake, *glowetl, *res;
+  double *rf_loclake, *rf_locwetl, *rf_glolake, *rf_glowetl, *rf_res;
+  double *k_release;
+  double *laf, *laf_prev, *fswb_next; int32_t *laf_started;
+} wgo_state;
+
+/* Initial state as set by setStoragesToZero + setLakeWetlToMaximum +
+ * initFractionStatus + annualInit (first year) of the reference. */
+int wgo_init_state(const wgo_static *s, wgo_state *st);
+
+/* Run ndays consecutive days starting at day-of-year doy0 (1..365, wraps).
+ * Forcing is day-major float [ndays*ncell] (precipitation mm, temperature C,
+ * shortwave W/m2).  Optional outputs (may be NULL):
+ *   discharge [ndays*ncell]  transported volume per cell and day [km3/d]
+ *   balance   [ndays*6]      storage total, P in, E out, Q out (outlets+sinks),
+ *                            sum of per-cell closure residuals, max |residual|
+ * nthreads > 1 runs the vertical pass with OpenMP (routing stays serial, as in
+ * the reference). */
+int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays,
+            const float *prec, const float *temp, const float *swrad,
+            double *discharge, double *balance, int nthreads);
+
+/* Derived river bottom width [m] (routing.cpp:490-495), exposed for tests. */
+double wgo_bottom_width(double bankfull);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

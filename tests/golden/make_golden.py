@@ -1,0 +1,63 @@
+"""Regenerate the golden fixtures from the reference's own code.
+
+Runs only where the reference sources are present (the build container): it
+builds oracle/_ref/wg_ref_harness from them (oracle/Makefile, target "ref"),
+runs each case below through the reference's calcNewDay/routing, and stores
+the inputs together with the reference's outputs, so that the tests can check
+the C restatement -- and through it the GPU library -- on any machine.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import ref_case  # noqa: E402
+from watergap2_gb300 import synthetic as sy  # noqa: E402
+from watergap2_gb300.region import save_npz  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+# name -> (region factory, days, first day of year, snapshot days)
+CASES = {
+    "region16_365d": (lambda: sy.region_64x64(seed=1, size=16), 365, 1, [1, 180, 365]),
+    "region64_30d": (lambda: sy.region_64x64(seed=1), 30, 1, [30]),
+    "swb_velo1_200d": (lambda: sy.region_small_swb(seed=21), 200, 20, [100, 200]),
+    "swb_velo2_120d": (lambda: sy.region_small_swb(seed=5, ny=16, nx=32, river_velo_opt=2), 120, 300, [120]),
+}
+
+
+def main(names=None):
+    if not ref_case.available():
+        if not ref_case.build():
+            raise SystemExit("reference sources not found; cannot regenerate fixtures")
+    for name, (make, nd, doy0, snaps) in CASES.items():
+        if names and name not in names:
+            continue
+        region = make()
+        P, T, S = sy.forcing(region, nd, doy0=doy0)
+        outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+        stations = outl[:24]
+        res = ref_case.run(region, P, T, S, doy0=doy0, stations=stations, snapshots=snaps)
+        extra = dict(P=P, T=T, S=S, doy0=np.array(doy0), stations=res["stations"], snap_days=np.array(snaps),
+                     discharge=res["discharge"])
+        rep = ref_case.REF_BANDS // region.nband
+        for i, snap in enumerate(res["snapshots"]):
+            bands = snap.pop("snow_band")
+            # replicated bands must agree with each other; keep one per band
+            b = bands.reshape(region.ncell, region.nband, rep)
+            assert np.array_equal(b, np.repeat(b[:, :, :1], rep, axis=2))
+            extra[f"s{i}_snow_band"] = b[:, :, 0].copy()
+            for k, v in snap.items():
+                extra[f"s{i}_{k}"] = v
+        path = os.path.join(HERE, f"{name}.npz")
+        save_npz(region, path, **extra)
+        print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
