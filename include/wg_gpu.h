@@ -1,0 +1,162 @@
+/*
+ * wg_gpu.h -- C ABI of the GB300 WaterGAP2 daily step (libwg_gpu.so).
+ *
+ * The library replaces, for one region held on one GPU, the per-day hot path
+ * of the reference:
+ *   dailyWaterBalanceClass::calcNewDay   source/daily.h:24, daily.cpp:94-1541
+ *   routingClass::routing                source/routing.h:44-45, routing.cpp:1629-5244
+ *   routingClass::updateLandAreaFrac     source/routing.h:46, routing.cpp:5343-5352
+ * together with the state set-up the reference performs before its day loop
+ * (setStoragesToZero, setLakeWetlToMaximum, initFractionStatus, annualInit:
+ * source/daily.cpp:1882-1894, routing.cpp:748-848, 979-1205, 5647-5716).
+ *
+ * Conventions: plain pointers and sizes only; every entry point returns a
+ * wg_status (no exceptions, no process exit).  Host buffers are owned by the
+ * caller; device buffers are owned by the context.  A context is bound to one
+ * CUDA device and one stream and is not thread-safe.  Device-side faults of
+ * the library's own kernels (an exceeded wait, an inconsistent topology) come
+ * back as status codes, never as traps.
+ *
+ * Option set (the reference's optionClass, source/option.h): time_series=1,
+ * cloud=2, petOpt=0, intercept=1, use_kc=0, calc_albedo=0, clclOpt=0,
+ * subtract_use=0, use_alloc=0, fractionalRoutingOpt=0, aridareaOpt=0,
+ * riverEvapoOpt=0, statcorrOpt=0, glacierOpt=0, calc_wtemp=0, antNatOpt=0,
+ * resYearOpt=0, riverveloOpt 0/1/2.  Other option values are out of scope and
+ * rejected with WG_ERR_UNSUPPORTED.
+ */
+#ifndef WG_GPU_H
+#define WG_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  WG_OK = 0,
+  WG_ERR_INVALID = 1,      /* bad argument or size                                 */
+  WG_ERR_UNSUPPORTED = 2,  /* option outside the supported set                      */
+  WG_ERR_CUDA = 3,         /* CUDA runtime error (see wg_last_error)                */
+  WG_ERR_NOMEM = 4,        /* device allocation failed                              */
+  WG_ERR_TOPOLOGY = 5,     /* drainage network has a cycle or a bad index           */
+  WG_ERR_TIMEOUT = 6,      /* a device-side wait exceeded its iteration limit       */
+  WG_ERR_DEVICE = 7        /* no usable sm_103a device                               */
+} wg_status;
+
+/* Number of calibration parameters (eCalibParam, source/calib_param.h:72-101). */
+#define WG_NPARAM 26
+#define WG_NLCT 18
+
+/* Static description of a region (host pointers, read once by wg_create).
+ * Field types follow the reference's storage types; the parameter block is
+ * [WG_NPARAM][ncell] in eCalibParam order. */
+typedef struct wg_region {
+  int32_t ncell;
+  int32_t nband;            /* snow elevation bands (the reference fixes 100)        */
+  int32_t river_velo_opt;   /* options.riverveloOpt                                   */
+  int32_t pad0;
+  double default_velocity;  /* routingClass::defaultRiverVelocity [km/d]              */
+  const double *lct_albedo, *lct_albedo_snow, *lct_ddf;        /* [18] LCT_22.DAT    */
+  const float *lct_lai_a, *lct_lai_b;                           /* [18] laiClass      */
+  const int16_t *lct_initial_days;                              /* [18] LAI_22.DAT    */
+  const double *area_km2, *lat_deg, *contfreq;
+  const uint8_t *lct;
+  const float *built_up, *smax, *lai_max, *gw_factor;
+  const int16_t *rg_max;
+  const int8_t *texture, *ldd;
+  const int16_t *aindex;
+  const int16_t *elev;                                          /* [ncell*(nband+1)]  */
+  const double *param;                                          /* [26*ncell]         */
+  const double *loc_lake, *loc_wetl, *glo_wetl, *glo_lake, *glo_res;   /* [%]         */
+  const double *lake_area, *res_area, *stor_cap, *mean_outflow, *mean_demand;
+  const int8_t *res_type, *start_month;
+  const double *river_length, *river_slope, *roughness, *bankfull;
+  const int32_t *downstream;   /* 0-based downstream cell, -1 at outlets and sinks   */
+  const int32_t *rout_order;   /* reference routing order (G_routingCell - 1)          */
+} wg_region;
+
+/* Host view of the dynamic state (caller-owned arrays, length ncell unless noted;
+ * snow_band is [ncell*nband], cell-major). */
+typedef struct wg_state_view {
+  double *canopy, *soil, *snow, *snow_band;
+  int32_t *lai_days, *lai_status;
+  double *lai_precsum;
+  double *gw, *river, *loclake, *locwetl, *glolake, *glowetl, *res;
+  double *rf_loclake, *rf_locwetl, *rf_glolake, *rf_glowetl, *rf_res;
+  double *k_release;
+  double *laf, *laf_prev, *fswb_next;
+  int32_t *laf_started;
+} wg_state_view;
+
+typedef struct wg_options {
+  int32_t device;          /* CUDA device ordinal                                     */
+  int32_t max_days;        /* capacity of the device forcing buffer, in days          */
+  int32_t nstation;        /* cells whose daily discharge is recorded                 */
+  int32_t record_balance;  /* 1: keep per-cell water-balance accumulators             */
+  const int32_t *stations; /* [nstation] cell indices                                  */
+  uint64_t stream;         /* cudaStream_t to use (0 = the context's own stream)      */
+} wg_options;
+
+typedef struct wg_ctx wg_ctx;
+
+/* Create a context: copies the region to the device in schedule order, builds
+ * the drainage topology, and sets the reference's start-of-run state.
+ * Replaces dailyWaterBalanceClass::init/setStoragesToZero and routingClass::init/
+ * setStoragesToZero/setLakeWetlToMaximum/initFractionStatus/annualInit
+ * (source/daily.cpp:1566-1894, routing.cpp:131-1205, 5647-5716). */
+wg_status wg_create(const wg_region *region, const wg_options *opt, wg_ctx **out);
+wg_status wg_destroy(wg_ctx *ctx);
+
+/* Copy the state host->device / device->host (the reference's setStorages and
+ * its wghmState writes: source/daily.cpp:1896-1924, routing.cpp:851-882, 5001-5020). */
+wg_status wg_set_state(wg_ctx *ctx, const wg_state_view *state);
+wg_status wg_get_state(wg_ctx *ctx, wg_state_view *state);
+
+/* Copy ndays of day-major forcing [ndays*ncell] (precipitation mm, temperature C,
+ * shortwave W/m2; the reference's climateYear.G_*_d365 floats, climateYear.h:12-15)
+ * into forcing slots [day0, day0+ndays) of the device buffer. */
+wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec,
+                            const float *temp, const float *swrad);
+
+/* One day, the reference's call granularity: the vertical balance of every cell
+ * (the OpenMP calcNewDay loop, source/integrateWGHM.cpp:767-783) for day of year
+ * doy (1..365) from forcing slot fday ... */
+wg_status wg_step_vertical(wg_ctx *ctx, int32_t doy, int32_t fday);
+/* ... then routing through the drainage tree and the land-area-fraction update
+ * (source/integrateWGHM.cpp:797-798).  Discharge of the stations is recorded at
+ * output slot oday. */
+wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday);
+
+/* ndays consecutive days in one persistent launch (days pipelined along the
+ * drainage depth); identical results to ndays calls of the two entry points
+ * above.  Forcing slots fday0.., discharge output slots from fday0 too. */
+wg_status wg_run_days(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays);
+
+/* Daily discharge (transported volume, km3/d) of the stations, [ndays*nstation],
+ * for output slots [day0, day0+ndays). */
+wg_status wg_get_discharge(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out);
+
+/* Water balance: out[0] total storage [km3] (land storages over the land fraction
+ * plus all surface-water and groundwater storages), out[1..4] accumulated
+ * inflow (precipitation), evaporation, outflow at outlets and sinks, and clamp
+ * corrections since the last wg_reset_balance, out[5] the largest per-cell
+ * closure residual relative to the cell's throughput.  Sums are compensated FP64. */
+wg_status wg_get_balance(wg_ctx *ctx, double out[6]);
+wg_status wg_reset_balance(wg_ctx *ctx);
+
+/* Wait for the context's stream. */
+wg_status wg_synchronize(wg_ctx *ctx);
+
+/* Information: number of drainage levels (longest flow path + 1), kernel
+ * launches issued so far, and the last CUDA error string. */
+int32_t wg_num_levels(const wg_ctx *ctx);
+int64_t wg_launch_count(const wg_ctx *ctx);
+const char *wg_last_error(const wg_ctx *ctx);
+const char *wg_status_string(wg_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

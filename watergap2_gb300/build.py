@@ -1,0 +1,62 @@
+"""Build recipe of the in-tree CUDA library ``_build/libwg_gpu.so`` (sm_103a only).
+
+Compiled with nvcc directly (no cmake): the two translation units in parallel,
+then one shared library.  ``--fmad=false`` keeps the arithmetic of the FP64
+path in the reference's expression order (no contraction into FMA), and the
+host code is compiled with ``-ffp-contract=off`` so that x86 and Arm hosts
+produce the same constants.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libwg_gpu.so")
+SOURCES = ["wg_kernels.cu", "wg_capi.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def flags(extra=()):
+    return [*ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
+            "-I", os.path.join(HERE, "..", "include"), *extra]
+
+
+def build(verbose: bool = False, ptxas_info: bool = False) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    cc = nvcc()
+    procs = []
+    objs = []
+    for src in SOURCES:
+        obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
+        objs.append(obj)
+        extra = ["-Xptxas", "-v"] if ptxas_info and src.endswith(".cu") else []
+        x = ["-x", "cu"] if src.endswith(".cpp") else []
+        cmd = [cc, *flags(extra), *x, "-c", os.path.join(CSRC, src), "-o", obj]
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    for cmd, p in procs:
+        out, _ = p.communicate()
+        if verbose or ptxas_info:
+            print(out)
+        if p.returncode:
+            raise RuntimeError(f"nvcc failed ({' '.join(cmd)}):\n{out}")
+    link = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode:
+        raise RuntimeError(f"link failed:\n{r.stdout}")
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+    print(build(verbose=True, ptxas_info="-v" in sys.argv))

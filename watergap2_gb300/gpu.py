@@ -1,0 +1,216 @@
+"""ctypes binding of the C ABI of ``_build/libwg_gpu.so`` (include/wg_gpu.h).
+
+``Model`` mirrors the reference's pair of day-step objects for one region on one
+GB300: ``step_vertical`` is the whole-grid counterpart of
+``dailyWaterBalanceClass::calcNewDay`` (source/daily.h:24), ``step_routing`` of
+``routingClass::routing`` + ``updateLandAreaFrac`` (source/routing.h:44-46), and
+``run_days`` runs many days in one persistent launch.  There is no CPU fallback:
+if the library or a GPU is missing, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .region import FIELDS, STATE_FIELDS, Region, empty_state
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libwg_gpu.so")
+
+WG_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported option", 3: "CUDA error", 4: "out of device memory",
+          5: "invalid drainage topology", 6: "device wait exceeded its limit", 7: "no usable device"}
+
+# exported entry points of include/wg_gpu.h
+SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_upload_forcing", "wg_step_vertical",
+           "wg_step_routing", "wg_run_days", "wg_get_discharge", "wg_get_balance", "wg_reset_balance",
+           "wg_synchronize", "wg_num_levels", "wg_launch_count", "wg_last_error", "wg_status_string")
+
+
+class WgError(RuntimeError):
+    pass
+
+
+class _Region(ctypes.Structure):
+    _fields_ = [("ncell", ctypes.c_int32), ("nband", ctypes.c_int32), ("river_velo_opt", ctypes.c_int32),
+                ("pad0", ctypes.c_int32), ("default_velocity", ctypes.c_double)] + \
+               [(name, ctypes.c_void_p) for name, _, _ in FIELDS]
+
+
+class _StateView(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name, _, _ in STATE_FIELDS]
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("max_days", ctypes.c_int32), ("nstation", ctypes.c_int32),
+                ("record_balance", ctypes.c_int32), ("stations", ctypes.c_void_p), ("stream", ctypes.c_uint64)]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise WgError(f"{path} is missing: build it with watergap2_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+    lib.wg_create.argtypes = [ctypes.POINTER(_Region), ctypes.POINTER(_Options), ctypes.POINTER(vp)]
+    lib.wg_destroy.argtypes = [vp]
+    lib.wg_set_state.argtypes = [vp, ctypes.POINTER(_StateView)]
+    lib.wg_get_state.argtypes = [vp, ctypes.POINTER(_StateView)]
+    lib.wg_upload_forcing.argtypes = [vp, i32, i32, vp, vp, vp]
+    lib.wg_step_vertical.argtypes = [vp, i32, i32]
+    lib.wg_step_routing.argtypes = [vp, i32, i32]
+    lib.wg_run_days.argtypes = [vp, i32, i32, i32]
+    lib.wg_get_discharge.argtypes = [vp, i32, i32, vp]
+    lib.wg_get_balance.argtypes = [vp, vp]
+    lib.wg_reset_balance.argtypes = [vp]
+    lib.wg_synchronize.argtypes = [vp]
+    lib.wg_num_levels.argtypes = [vp]
+    lib.wg_num_levels.restype = i32
+    lib.wg_launch_count.argtypes = [vp]
+    lib.wg_launch_count.restype = i64
+    lib.wg_last_error.argtypes = [vp]
+    lib.wg_last_error.restype = ctypes.c_char_p
+    lib.wg_status_string.argtypes = [ctypes.c_int]
+    lib.wg_status_string.restype = ctypes.c_char_p
+    for name in ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_upload_forcing", "wg_step_vertical",
+                 "wg_step_routing", "wg_run_days", "wg_get_discharge", "wg_get_balance", "wg_reset_balance",
+                 "wg_synchronize"):
+        getattr(lib, name).restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+class Model:
+    """One region resident on one GPU."""
+
+    def __init__(self, region: Region, max_days: int = 366, stations=None, record_balance: bool = False,
+                 device: int = 0):
+        self.lib = load_library()
+        self.region = region
+        self._keep = []
+        r = _Region()
+        r.ncell, r.nband, r.river_velo_opt = region.ncell, region.nband, region.river_velo_opt
+        r.default_velocity = region.default_velocity
+        for name, _, _ in FIELDS:
+            a = region.arrays[name]
+            self._keep.append(a)
+            setattr(r, name, a.ctypes.data)
+        self.stations = np.ascontiguousarray(
+            np.nonzero(region.downstream < 0)[0] if stations is None else stations, np.int32)
+        o = _Options()
+        o.device, o.max_days, o.nstation = device, int(max_days), int(self.stations.size)
+        o.record_balance = int(bool(record_balance))
+        o.stations = self.stations.ctypes.data
+        o.stream = 0
+        self.max_days = int(max_days)
+        h = ctypes.c_void_p()
+        self._check(self.lib.wg_create(ctypes.byref(r), ctypes.byref(o), ctypes.byref(h)), "wg_create", None)
+        self.h = h
+
+    def _check(self, rc, what, h="self"):
+        if rc != WG_OK:
+            msg = ""
+            if h is not None and getattr(self, "h", None):
+                msg = self.lib.wg_last_error(self.h).decode()
+            raise WgError(f"{what}: {STATUS.get(rc, rc)} {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.wg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_levels(self) -> int:
+        return int(self.lib.wg_num_levels(self.h))
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.wg_launch_count(self.h))
+
+    def upload_forcing(self, day0: int, P, T, S):
+        P, T, S = (np.ascontiguousarray(x, np.float32) for x in (P, T, S))
+        nd = P.shape[0]
+        self._check(self.lib.wg_upload_forcing(self.h, int(day0), nd, _ptr(P), _ptr(T), _ptr(S)), "upload_forcing")
+
+    def step_vertical(self, doy: int, fday: int):
+        self._check(self.lib.wg_step_vertical(self.h, int(doy), int(fday)), "step_vertical")
+
+    def step_routing(self, doy: int, oday: int):
+        self._check(self.lib.wg_step_routing(self.h, int(doy), int(oday)), "step_routing")
+
+    def run_days(self, doy0: int, fday0: int, ndays: int):
+        self._check(self.lib.wg_run_days(self.h, int(doy0), int(fday0), int(ndays)), "run_days")
+
+    def synchronize(self):
+        self._check(self.lib.wg_synchronize(self.h), "synchronize")
+
+    def discharge(self, day0: int, ndays: int) -> np.ndarray:
+        out = np.zeros((ndays, self.stations.size))
+        self._check(self.lib.wg_get_discharge(self.h, int(day0), int(ndays), _ptr(out)), "get_discharge")
+        return out
+
+    def balance(self) -> np.ndarray:
+        out = np.zeros(6)
+        self._check(self.lib.wg_get_balance(self.h, _ptr(out)), "get_balance")
+        return out
+
+    def reset_balance(self):
+        self._check(self.lib.wg_reset_balance(self.h), "reset_balance")
+
+    def get_state(self) -> dict:
+        st = empty_state(self.region.ncell, self.region.nband)
+        v = _StateView()
+        for k, a in st.items():
+            setattr(v, k, a.ctypes.data)
+        self._check(self.lib.wg_get_state(self.h, ctypes.byref(v)), "get_state")
+        return st
+
+    def set_state(self, st: dict):
+        v = _StateView()
+        keep = []
+        for name, dt, _ in STATE_FIELDS:
+            a = np.ascontiguousarray(st[name], dt)
+            keep.append(a)
+            setattr(v, name, a.ctypes.data)
+        self._check(self.lib.wg_set_state(self.h, ctypes.byref(v)), "set_state")
+
+    def run(self, doy0: int, P, T, S, per_day: bool = False, chunk: int | None = None):
+        """Convenience: upload forcing and simulate len(P) days from day-of-year doy0;
+        returns station discharge [ndays, nstation]."""
+        nd = P.shape[0]
+        chunk = chunk or self.max_days
+        qs = []
+        done = 0
+        doy = doy0
+        while done < nd:
+            k = min(chunk, nd - done, self.max_days)
+            self.upload_forcing(0, P[done:done + k], T[done:done + k], S[done:done + k])
+            if per_day:
+                for d in range(k):
+                    dd = (doy - 1 + d) % 365 + 1
+                    self.step_vertical(dd, d)
+                    self.step_routing(dd, d)
+            else:
+                self.run_days(doy, 0, k)
+            qs.append(self.discharge(0, k))
+            done += k
+            doy = (doy - 1 + k) % 365 + 1
+        return np.concatenate(qs) if qs else np.zeros((0, self.stations.size))
