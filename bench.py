@@ -1,0 +1,333 @@
+"""Benchmark of the WaterGAP2 daily step on GB300 (cell-days/s).
+
+Workload (the largest single-GPU configuration the metric is quoted on): the
+plain FP64 global 0.5-degree grid, 67,420 land cells with local lakes,
+wetlands, 300 global lakes and 1,200 reservoirs, D8 drainage with ~6,000
+outlets; seeded synthetic inputs (no dataset).  One step = one simulated year
+(365 days) of the whole grid, i.e. 24.6 M cell-days; the default 10 timed
+steps are the 10-year run (246.1 M cell-days).
+
+  value  device-resident: forcing for all years is in HBM before timing; each
+         step is one persistent launch of the day-pipelined kernel (wg_run_days).
+  e2e    through the C ABI with host buffers: every step copies that year's
+         forcing from pinned host memory (wg_upload_forcing) and reads the
+         outlet discharge back (wg_get_discharge).
+  --impl reference  the reference's CPU algorithm (the oracle port of
+         daily.cpp/routing.cpp) on the host cores, same metric.
+
+Run:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-days/s on 1 GB300 (plain FP64 vs batched FP32 ensemble) at stated error"
+DAYS_PER_STEP = 365
+# algorithmic HBM bytes per cell-day of a day-by-day FP64 implementation with the
+# water bodies of this workload: vertical 224 + routing 96 + water bodies ~4
+BYTES_PER_CELL_DAY = 324.0
+
+
+def _forcing_block(args):
+    seed, y = args
+    from watergap2_gb300 import synthetic as sy
+    region = sy.region_global()
+    return sy.forcing(region, DAYS_PER_STEP, seed=seed, doy0=1, day_offset=y * DAYS_PER_STEP)
+
+
+def make_forcing(nyears, seed=2, procs=None):
+    """Forcing for nyears independent years, generated in parallel (spawned workers,
+    before any CUDA context exists)."""
+    procs = procs or min(nyears, os.cpu_count() or 1)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        blocks = pool.map(_forcing_block, [(seed, y) for y in range(nyears)])
+    P = np.concatenate([b[0] for b in blocks])
+    T = np.concatenate([b[1] for b in blocks])
+    S = np.concatenate([b[2] for b in blocks])
+    return P, T, S
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            out, _ = self.proc.communicate(timeout=10)
+            self.lines = [l for l in out.splitlines() if l.strip()]
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_sample(region, ndays, threads):
+    """The oracle port over ndays of the workload; returns (cell-days/s, seconds)."""
+    from oracle import Oracle
+    from watergap2_gb300 import synthetic as sy
+    P, T, S = sy.forcing(region, ndays, seed=2, doy0=1)
+    o = Oracle(region)
+    t0 = time.perf_counter()
+    o.run(1, P, T, S, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return region.ncell * ndays / dt, dt
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU algorithm on the host cores."""
+    if rank != 0:
+        return
+    from watergap2_gb300 import synthetic as sy
+    region = sy.region_global()
+    threads = os.cpu_count() or 1
+    sample_days = int(os.environ.get("WG_REF_SAMPLE_DAYS", "20"))
+    for _ in range(args.warmup):
+        cpu_sample(region, max(2, sample_days // 4), threads)
+    vals, secs = [], 0.0
+    for _ in range(args.steps):
+        v, dt = cpu_sample(region, sample_days, threads)
+        vals.append(v)
+        secs += dt
+    value = statistics.median(vals)
+    ms = 1000.0 * region.ncell * DAYS_PER_STEP / value
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-days/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "global 0.5-degree grid, 67,420 cells, lakes/wetlands/reservoirs, FP64",
+                   "days_per_step": DAYS_PER_STEP, "ncell": region.ncell},
+        "cpu_baseline": {"value": value, "unit": "cell-days/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample_days} days x {region.ncell} cells per step, vertical pass on "
+                                   f"{threads} OpenMP threads, routing serial as in the reference"},
+        "e2e": {"value": value, "unit": "cell-days/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def fp64_peak_tflops():
+    from watergap2_gb300 import gpu
+    return gpu.measure_fp64_peak()
+
+
+def run_gpu(args, rank, world):
+    import torch
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    region = sy.region_global()
+    nyears = args.warmup + args.steps
+    P, T, S = args.forcing
+    stream = torch.cuda.Stream(device=local)
+    model = Model(region, max_days=nyears * DAYS_PER_STEP, device=local, stream=stream.cuda_stream)
+    nst = model.stations.size
+
+    # ---- value: device-resident forcing, one persistent launch per simulated year
+    model.upload_forcing(0, P, T, S)
+    model.synchronize()
+    doy = 1
+    for w in range(args.warmup):
+        model.run_days(doy, w * DAYS_PER_STEP, DAYS_PER_STEP)
+    model.synchronize()
+    launches0 = model.launch_count
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    per_step = []
+    with ClockSampler(local) as clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for k in range(args.steps):
+            e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e_a.record(stream)
+            model.run_days(doy, (args.warmup + k) * DAYS_PER_STEP, DAYS_PER_STEP)
+            e_b.record(stream)
+            per_step.append((e_a, e_b))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        model.synchronize()
+        if dist:
+            dist.barrier()
+    gpu_launches = model.launch_count - launches0
+    elapsed_ms = ev0.elapsed_time(ev1)
+    launch_ms = [a.elapsed_time(b) for a, b in per_step]
+    if dist:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    cell_days = region.ncell * DAYS_PER_STEP * args.steps
+    value = cell_days * world / (elapsed_ms / 1000.0)
+    q_dev = model.discharge((args.warmup + args.steps - 1) * DAYS_PER_STEP, DAYS_PER_STEP)
+
+    # ---- e2e: same metric through the C ABI with host buffers (pinned), copies timed
+    e2e_model = Model(region, max_days=DAYS_PER_STEP, device=local, stream=stream.cuda_stream)
+    pin = [torch.empty((nyears * DAYS_PER_STEP, region.ncell), dtype=torch.float32, pin_memory=True)
+           for _ in range(3)]
+    for t_, a in zip(pin, (P, T, S)):
+        t_.numpy()[:] = a
+    hostq = torch.empty((DAYS_PER_STEP, nst), dtype=torch.float64, pin_memory=True).numpy()
+    Pn, Tn, Sn = (t_.numpy() for t_ in pin)
+    for w in range(args.warmup):
+        sl = slice(w * DAYS_PER_STEP, (w + 1) * DAYS_PER_STEP)
+        e2e_model.upload_forcing(0, Pn[sl], Tn[sl], Sn[sl])
+        e2e_model.run_days(1, 0, DAYS_PER_STEP)
+        e2e_model.discharge_into(0, DAYS_PER_STEP, hostq)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        sl = slice((args.warmup + k) * DAYS_PER_STEP, (args.warmup + k + 1) * DAYS_PER_STEP)
+        e2e_model.upload_forcing(0, Pn[sl], Tn[sl], Sn[sl])
+        e2e_model.run_days(1, 0, DAYS_PER_STEP)
+        e2e_model.discharge_into(0, DAYS_PER_STEP, hostq)   # synchronises
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = cell_days * world / e2e_s
+    same = bool(np.array_equal(hostq, q_dev))
+    h2d = 3 * DAYS_PER_STEP * region.ncell * 4
+    d2h = DAYS_PER_STEP * nst * 8
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peaks, peak_kind = measured_peaks()
+    mean_launch_s = statistics.mean(launch_ms) / 1000.0
+    achieved = BYTES_PER_CELL_DAY * region.ncell * DAYS_PER_STEP / mean_launch_s / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "pipeline_fp64_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("dram_bytes_per_cell_day")
+        if traffic is not None:
+            traffic = traffic * region.ncell * DAYS_PER_STEP
+    fp64 = None
+    try:
+        peak64 = fp64_peak_tflops()
+        fpath = os.path.join(ROOT, "profiles", "pipeline_fp64_flops.json")
+        if os.path.exists(fpath):
+            with open(fpath) as f:
+                fl = json.load(f).get("fp64_flops_per_cell_day")
+            ach64 = fl * region.ncell * DAYS_PER_STEP / mean_launch_s / 1e12
+            fp64 = {"achieved": ach64, "peak": peak64, "unit": "TFLOP/s", "frac": ach64 / peak64,
+                    "flops_per_cell_day": fl, "peak_kind": "measured (DFMA loop)"}
+        else:
+            fp64 = {"peak": peak64, "unit": "TFLOP/s", "peak_kind": "measured (DFMA loop)"}
+    except Exception as exc:   # diagnostics only
+        fp64 = {"error": str(exc)}
+    cpu_threads = os.cpu_count() or 1
+    cpu_days = int(os.environ.get("WG_CPU_SAMPLE_DAYS", "20"))
+    cpu_val, cpu_s = cpu_sample(region, cpu_days, cpu_threads)
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-days/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators)",
+        "config": {"workload": "global 0.5-degree grid, 67,420 cells, lakes/wetlands/reservoirs, FP64, "
+                               "1 step = 365 days (10 steps = the 10-year run)",
+                   "ncell": region.ncell, "days_per_step": DAYS_PER_STEP, "levels": model.num_levels,
+                   "stations": int(nst), "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (295 MB of forcing read per step)"},
+        "gpu_launches": int(gpu_launches),
+        "e2e": {"value": e2e_value, "unit": "cell-days/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "matches_device_run": same},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": achieved / peaks.get("hbm_gbs"), "traffic": traffic,
+                     "peak_kind": peak_kind, "bytes_per_cell_day": BYTES_PER_CELL_DAY,
+                     "kernel": "k_pipeline<true>", "mean_launch_ms": 1000 * mean_launch_s},
+        "fp64": fp64,
+        "cpu_baseline": {"value": cpu_val, "unit": "cell-days/s", "cores": cpu_threads, "kind": "port",
+                         "sample": f"{cpu_days} days of the same grid ({region.ncell * cpu_days} cell-days, "
+                                   f"{cpu_s:.1f} s), vertical pass on {cpu_threads} OpenMP threads, routing serial"},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    # forcing first (spawned workers), then CUDA
+    args.forcing = make_forcing(args.warmup + args.steps)
+    run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

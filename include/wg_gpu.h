@@ -149,6 +149,10 @@ wg_status wg_reset_balance(wg_ctx *ctx);
 /* Wait for the context's stream. */
 wg_status wg_synchronize(wg_ctx *ctx);
 
+/* Diagnostic: FP64 fused-multiply-add throughput of a device in TFLOP/s, from a
+ * loop of independent DFMA chains (the FP64 ceiling of the plain FP64 path). */
+wg_status wg_measure_fp64_peak(int32_t device, double *tflops);
+
 /* Information: number of drainage levels (longest flow path + 1), kernel
  * launches issued so far, and the last CUDA error string. */
 int32_t wg_num_levels(const wg_ctx *ctx);

@@ -26,7 +26,8 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported option", 3: "CUDA erro
 # exported entry points of include/wg_gpu.h
 SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_upload_forcing", "wg_step_vertical",
            "wg_step_routing", "wg_run_days", "wg_get_discharge", "wg_get_balance", "wg_reset_balance",
-           "wg_synchronize", "wg_num_levels", "wg_launch_count", "wg_last_error", "wg_status_string")
+           "wg_synchronize", "wg_num_levels", "wg_launch_count", "wg_last_error", "wg_status_string",
+           "wg_measure_fp64_peak")
 
 
 class WgError(RuntimeError):
@@ -78,6 +79,8 @@ def load_library(path: str = LIB_PATH):
     lib.wg_launch_count.restype = i64
     lib.wg_last_error.argtypes = [vp]
     lib.wg_last_error.restype = ctypes.c_char_p
+    lib.wg_measure_fp64_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.wg_measure_fp64_peak.restype = ctypes.c_int
     lib.wg_status_string.argtypes = [ctypes.c_int]
     lib.wg_status_string.restype = ctypes.c_char_p
     for name in ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_upload_forcing", "wg_step_vertical",
@@ -88,6 +91,16 @@ def load_library(path: str = LIB_PATH):
     return lib
 
 
+def measure_fp64_peak(device: int = 0) -> float:
+    """FP64 FMA throughput of the device in TFLOP/s (a dependent-chain-free DFMA loop)."""
+    lib = load_library()
+    v = ctypes.c_double(0.0)
+    rc = lib.wg_measure_fp64_peak(int(device), ctypes.byref(v))
+    if rc != WG_OK:
+        raise WgError(f"wg_measure_fp64_peak: {STATUS.get(rc, rc)}")
+    return float(v.value)
+
+
 def _ptr(a):
     return a.ctypes.data if a is not None else None
 
@@ -96,7 +109,7 @@ class Model:
     """One region resident on one GPU."""
 
     def __init__(self, region: Region, max_days: int = 366, stations=None, record_balance: bool = False,
-                 device: int = 0):
+                 device: int = 0, stream: int = 0):
         self.lib = load_library()
         self.region = region
         self._keep = []
@@ -113,7 +126,7 @@ class Model:
         o.device, o.max_days, o.nstation = device, int(max_days), int(self.stations.size)
         o.record_balance = int(bool(record_balance))
         o.stations = self.stations.ctypes.data
-        o.stream = 0
+        o.stream = int(stream)
         self.max_days = int(max_days)
         h = ctypes.c_void_p()
         self._check(self.lib.wg_create(ctypes.byref(r), ctypes.byref(o), ctypes.byref(h)), "wg_create", None)
@@ -164,6 +177,12 @@ class Model:
 
     def discharge(self, day0: int, ndays: int) -> np.ndarray:
         out = np.zeros((ndays, self.stations.size))
+        self._check(self.lib.wg_get_discharge(self.h, int(day0), int(ndays), _ptr(out)), "get_discharge")
+        return out
+
+    def discharge_into(self, day0: int, ndays: int, out: np.ndarray) -> np.ndarray:
+        """Like discharge() but into a caller-provided (e.g. pinned) float64 array."""
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size >= ndays * self.stations.size
         self._check(self.lib.wg_get_discharge(self.h, int(day0), int(ndays), _ptr(out)), "get_discharge")
         return out
 

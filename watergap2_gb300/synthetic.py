@@ -422,24 +422,35 @@ def region_small_swb(seed: int = 21, nband: int = 5, ny: int = 24, nx: int = 48,
 
 def forcing(region: Region, ndays: int, seed: int = 2, doy0: int = 1, day_offset: int = 0):
     """Day-major float32 forcing [ndays, ncell]: precipitation (mm), temperature (C),
-    shortwave (W/m2).  ``day_offset`` selects a window of a longer series so that a
-    long run can be generated year by year."""
+    shortwave (W/m2).  Day g of the series (g = day_offset + d) belongs to block
+    g // 365, which has its own generator keyed by (seed, block), so a long run can
+    be generated piecewise and every piece is the same wherever it is cut."""
     n = region.ncell
     lat = region.lat_deg
     P = np.empty((ndays, n), np.float32)
     T = np.empty((ndays, n), np.float32)
     S = np.empty((ndays, n), np.float32)
     hemi = np.where(lat >= 0, 1.0, -1.0)
-    tmean = 10.0 + 14.0 * (1.0 - np.abs(lat) / 45.0) if region.name == "region_global" else np.full(n, 10.0)
-    for d in range(ndays):
-        g = day_offset + d
-        rng = np.random.default_rng((seed, g))
+    if region.name == "region_global":
+        tmean = 10.0 + 14.0 * (1.0 - np.abs(lat) / 45.0)
+    else:
+        tmean = np.full(n, 10.0)
+    swamp = np.clip(np.abs(lat) / 30.0, 0.3, 1.0) * hemi
+    g0, g1 = day_offset, day_offset + ndays
+    for blk in range(g0 // 365, (g1 - 1) // 365 + 1):
+        rng = np.random.default_rng((seed, blk))
+        u = rng.uniform(size=(365, n))
+        amount = rng.gamma(0.8, 8.0, (365, n))
+        noise_t = rng.normal(0.0, 3.0, (365, n))
+        noise_s = rng.normal(0.0, 10.0, (365, n))
+        lo, hi = max(g0, blk * 365), min(g1, (blk + 1) * 365)
+        k = np.arange(lo, hi)
+        j = k - blk * 365                      # row within the block
+        d = k - day_offset                     # row within the output
         doy = (doy0 - 1 + d) % 365 + 1
-        wet = rng.uniform(size=n) >= 0.6
-        amount = rng.gamma(0.8, 8.0, n)
-        P[d] = np.where(wet, amount, 0.0)
-        season = np.sin(2 * np.pi * doy / 365.0) * hemi
-        T[d] = tmean + 12.0 * season + rng.normal(0.0, 3.0, n)
-        sw = 175.0 + 125.0 * np.sin(2 * np.pi * (doy - 80) / 365.0) * hemi * np.clip(np.abs(lat) / 30.0, 0.3, 1.0)
-        S[d] = np.clip(sw + rng.normal(0.0, 10.0, n), 50.0, 300.0)
+        P[d] = np.where(u[j] >= 0.6, amount[j], 0.0)
+        season = np.sin(2 * np.pi * doy / 365.0)[:, None] * hemi[None, :]
+        T[d] = tmean[None, :] + 12.0 * season + noise_t[j]
+        sw = 175.0 + 125.0 * np.sin(2 * np.pi * (doy - 80) / 365.0)[:, None] * swamp[None, :]
+        S[d] = np.clip(sw + noise_s[j], 50.0, 300.0)
     return P, T, S
