@@ -136,7 +136,7 @@ def run_reference(args, rank, world):
     from watergap2_gb300 import synthetic as sy
     region = sy.region_global()
     threads = os.cpu_count() or 1
-    sample_days = int(os.environ.get("WG_REF_SAMPLE_DAYS", "20"))
+    sample_days = int(os.environ.get("WG_REF_SAMPLE_DAYS", "120"))
     for _ in range(args.warmup):
         cpu_sample(region, max(2, sample_days // 4), threads)
     vals, secs = [], 0.0
@@ -283,7 +283,7 @@ def run_gpu(args, rank, world):
     except Exception as exc:   # diagnostics only
         fp64 = {"error": str(exc)}
     cpu_threads = os.cpu_count() or 1
-    cpu_days = int(os.environ.get("WG_CPU_SAMPLE_DAYS", "20"))
+    cpu_days = int(os.environ.get("WG_CPU_SAMPLE_DAYS", "1000"))
     cpu_val, cpu_s = cpu_sample(region, cpu_days, cpu_threads)
     line = {
         "metric": METRIC, "value": value, "unit": "cell-days/s", "n_gpus": world, "steps": args.steps,
@@ -312,8 +312,29 @@ def run_gpu(args, rank, world):
         dist.destroy_process_group()
 
 
+def run_profile_case(days: int = 120, warm_days: int = 30):
+    """A short, self-contained case for ncu: the global grid, one warm-up launch of
+    warm_days, then one launch of `days` days (forcing + state > L2).  Capture the
+    second launch: ncu -k regex:k_pipeline -s 1 -c 1 python bench.py --profile"""
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_global()
+    P, T, S = sy.forcing(region, warm_days + days, seed=2, doy0=1)
+    m = Model(region, max_days=warm_days + days)
+    m.upload_forcing(0, P, T, S)
+    m.run_days(1, 0, warm_days)
+    m.synchronize()
+    t0 = time.perf_counter()
+    m.run_days(1 + warm_days, warm_days, days)
+    m.synchronize()
+    dt = time.perf_counter() - t0
+    print(json.dumps({"profile_case": "global grid", "ncell": region.ncell, "days": days,
+                      "seconds": dt, "cell_days_per_s": region.ncell * days / dt}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--profile", action="store_true", help="run the short ncu case and exit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -321,6 +342,9 @@ def main():
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.profile:
+        run_profile_case()
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
