@@ -184,12 +184,15 @@ def run_gpu(args, rank, world):
     model = Model(region, max_days=nyears * DAYS_PER_STEP, device=local, stream=stream.cuda_stream)
     nst = model.stations.size
 
-    # ---- value: device-resident forcing, one persistent launch per simulated year
+    # ---- value: device-resident forcing.  The whole nyears-year run is one
+    # day-pipelined wavefront; each step is one call covering 365 wavefront steps,
+    # so after the warm-up every timed call routes exactly 365 days of every cell.
+    ndays = nyears * DAYS_PER_STEP
     model.upload_forcing(0, P, T, S)
     model.synchronize()
-    doy = 1
-    for w in range(args.warmup):
-        model.run_days(doy, w * DAYS_PER_STEP, DAYS_PER_STEP)
+    total_steps = model.num_steps(ndays)
+    assert args.warmup * DAYS_PER_STEP >= model.num_levels - 1, "warm-up must fill the wavefront"
+    model.run_steps(1, 0, ndays, 0, args.warmup * DAYS_PER_STEP)
     model.synchronize()
     launches0 = model.launch_count
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -200,9 +203,10 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
         ev0.record(stream)
         for k in range(args.steps):
+            t0 = (args.warmup + k) * DAYS_PER_STEP
             e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e_a.record(stream)
-            model.run_days(doy, (args.warmup + k) * DAYS_PER_STEP, DAYS_PER_STEP)
+            model.run_steps(1, 0, ndays, t0, t0 + DAYS_PER_STEP)
             e_b.record(stream)
             per_step.append((e_a, e_b))
         ev1.record(stream)
@@ -213,46 +217,55 @@ def run_gpu(args, rank, world):
     gpu_launches = model.launch_count - launches0
     elapsed_ms = ev0.elapsed_time(ev1)
     launch_ms = [a.elapsed_time(b) for a, b in per_step]
+    model.run_steps(1, 0, ndays, nyears * DAYS_PER_STEP, total_steps)   # drain (untimed)
+    model.synchronize()
     if dist:
         t = torch.tensor([elapsed_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed_ms = float(t.item())
     cell_days = region.ncell * DAYS_PER_STEP * args.steps
     value = cell_days * world / (elapsed_ms / 1000.0)
-    q_dev = model.discharge((args.warmup + args.steps - 1) * DAYS_PER_STEP, DAYS_PER_STEP)
+    lag = model.num_levels - 1
+    q_dev = model.discharge(0, ndays)
 
-    # ---- e2e: same metric through the C ABI with host buffers (pinned), copies timed
-    e2e_model = Model(region, max_days=DAYS_PER_STEP, device=local, stream=stream.cuda_stream)
-    pin = [torch.empty((nyears * DAYS_PER_STEP, region.ncell), dtype=torch.float32, pin_memory=True)
-           for _ in range(3)]
+    # ---- e2e: the same run through the C ABI with host buffers: every step copies
+    # that year's forcing from pinned host memory and reads back the outlet
+    # discharge of the 365 days the step completed
+    del model
+    e2e_model = Model(region, max_days=ndays, device=local, stream=stream.cuda_stream)
+    pin = [torch.empty((ndays, region.ncell), dtype=torch.float32, pin_memory=True) for _ in range(3)]
     for t_, a in zip(pin, (P, T, S)):
         t_.numpy()[:] = a
-    hostq = torch.empty((DAYS_PER_STEP, nst), dtype=torch.float64, pin_memory=True).numpy()
     Pn, Tn, Sn = (t_.numpy() for t_ in pin)
+    hostq = torch.empty((DAYS_PER_STEP, nst), dtype=torch.float64, pin_memory=True).numpy()
+
+    def e2e_step(k):
+        sl = slice(k * DAYS_PER_STEP, (k + 1) * DAYS_PER_STEP)
+        e2e_model.upload_forcing(k * DAYS_PER_STEP, Pn[sl], Tn[sl], Sn[sl])
+        e2e_model.run_steps(1, 0, ndays, k * DAYS_PER_STEP, (k + 1) * DAYS_PER_STEP)
+        d0 = max(0, (k + 1) * DAYS_PER_STEP - lag - DAYS_PER_STEP)
+        e2e_model.discharge_into(d0, DAYS_PER_STEP, hostq)   # synchronises
+
     for w in range(args.warmup):
-        sl = slice(w * DAYS_PER_STEP, (w + 1) * DAYS_PER_STEP)
-        e2e_model.upload_forcing(0, Pn[sl], Tn[sl], Sn[sl])
-        e2e_model.run_days(1, 0, DAYS_PER_STEP)
-        e2e_model.discharge_into(0, DAYS_PER_STEP, hostq)
+        e2e_step(w)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(args.steps):
-        sl = slice((args.warmup + k) * DAYS_PER_STEP, (args.warmup + k + 1) * DAYS_PER_STEP)
-        e2e_model.upload_forcing(0, Pn[sl], Tn[sl], Sn[sl])
-        e2e_model.run_days(1, 0, DAYS_PER_STEP)
-        e2e_model.discharge_into(0, DAYS_PER_STEP, hostq)   # synchronises
+        e2e_step(args.warmup + k)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    e2e_model.run_steps(1, 0, ndays, nyears * DAYS_PER_STEP, total_steps)
+    same = bool(np.array_equal(e2e_model.discharge(0, ndays), q_dev))
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e_value = cell_days * world / e2e_s
-    same = bool(np.array_equal(hostq, q_dev))
     h2d = 3 * DAYS_PER_STEP * region.ncell * 4
     d2h = DAYS_PER_STEP * nst * 8
+    num_levels = e2e_model.num_levels
 
     if rank != 0:
         if dist:
@@ -290,8 +303,8 @@ def run_gpu(args, rank, world):
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators)",
         "config": {"workload": "global 0.5-degree grid, 67,420 cells, lakes/wetlands/reservoirs, FP64, "
-                               "1 step = 365 days (10 steps = the 10-year run)",
-                   "ncell": region.ncell, "days_per_step": DAYS_PER_STEP, "levels": model.num_levels,
+                               "1 step = 365 days of every cell (10 steps = the 10-year run)",
+                   "ncell": region.ncell, "days_per_step": DAYS_PER_STEP, "levels": num_levels,
                    "stations": int(nst), "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (295 MB of forcing read per step)"},
         "gpu_launches": int(gpu_launches),
@@ -300,7 +313,7 @@ def run_gpu(args, rank, world):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                      "frac": achieved / peaks.get("hbm_gbs"), "traffic": traffic,
                      "peak_kind": peak_kind, "bytes_per_cell_day": BYTES_PER_CELL_DAY,
-                     "kernel": "k_pipeline<true>", "mean_launch_ms": 1000 * mean_launch_s},
+                     "kernel": "k_vertical_ahead + k_pipeline (one step)", "mean_step_ms": 1000 * mean_launch_s},
         "fp64": fp64,
         "cpu_baseline": {"value": cpu_val, "unit": "cell-days/s", "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_days} days of the same grid ({region.ncell * cpu_days} cell-days, "
@@ -312,23 +325,28 @@ def run_gpu(args, rank, world):
         dist.destroy_process_group()
 
 
-def run_profile_case(days: int = 120, warm_days: int = 30):
-    """A short, self-contained case for ncu: the global grid, one warm-up launch of
-    warm_days, then one launch of `days` days (forcing + state > L2).  Capture the
-    second launch: ncu -k regex:k_pipeline -s 1 -c 1 python bench.py --profile"""
+def run_profile_case(days: int = 120, warm_days: int = 200):
+    """A short, self-contained case for ncu: the global grid, a warm-up call that
+    fills the day-pipelined wavefront (warm_days steps), then one call of `days`
+    steady-state steps (one k_vertical_ahead and one k_pipeline launch; forcing and
+    state exceed L2).  Capture the second call's kernels:
+      ncu -k regex:k_pipeline -s 1 -c 1 python bench.py --profile"""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global()
-    P, T, S = sy.forcing(region, warm_days + days, seed=2, doy0=1)
-    m = Model(region, max_days=warm_days + days)
+    nd = warm_days + days
+    P, T, S = sy.forcing(region, nd, seed=2, doy0=1)
+    m = Model(region, max_days=nd)
     m.upload_forcing(0, P, T, S)
-    m.run_days(1, 0, warm_days)
+    m.run_steps(1, 0, nd, 0, warm_days)
     m.synchronize()
     t0 = time.perf_counter()
-    m.run_days(1 + warm_days, warm_days, days)
+    m.run_steps(1, 0, nd, warm_days, warm_days + days)
     m.synchronize()
     dt = time.perf_counter() - t0
-    print(json.dumps({"profile_case": "global grid", "ncell": region.ncell, "days": days,
+    m.run_steps(1, 0, nd, warm_days + days, m.num_steps(nd))
+    m.synchronize()
+    print(json.dumps({"profile_case": "global grid, steady-state wavefront", "ncell": region.ncell, "steps": days,
                       "seconds": dt, "cell_days_per_s": region.ncell * days / dt}))
 
 

@@ -97,6 +97,17 @@ typedef struct wg_options {
   int32_t record_balance;  /* 1: keep per-cell water-balance accumulators             */
   const int32_t *stations; /* [nstation] cell indices                                  */
   uint64_t stream;         /* cudaStream_t to use (0 = the context's own stream)      */
+  int32_t precision;       /* 0: FP64 state and fluxes (the reference's arithmetic);
+                              1: FP32 state and fluxes, FP64 confluence and balance sums */
+  int32_t members;         /* ensemble members sharing the forcing (>1 needs precision 1);
+                              each member is an independent model state, as one
+                              process per member in the reference's data assimilation
+                              (source/enKF2wghmState.cpp:17-121)                       */
+  const float *member_prec_factor;   /* [members] precipitation multiplier, or NULL   */
+  const float *member_gamma_factor;  /* [members] multiplier on P_GAMRUN_C, or NULL   */
+  int32_t block_threads;   /* 64, 128 or 256 threads per block; 0 = 256               */
+  int32_t ring_days;       /* days of vertical outputs buffered between the vertical
+                              balance run ahead and routing; 0 = as many as fit in 2 GB */
 } wg_options;
 
 typedef struct wg_ctx wg_ctx;
@@ -113,6 +124,11 @@ wg_status wg_destroy(wg_ctx *ctx);
  * its wghmState writes: source/daily.cpp:1896-1924, routing.cpp:851-882, 5001-5020). */
 wg_status wg_set_state(wg_ctx *ctx, const wg_state_view *state);
 wg_status wg_get_state(wg_ctx *ctx, wg_state_view *state);
+
+/* The same for one member of an ensemble context (member 0 is what wg_get_state
+ * and wg_set_state address). */
+wg_status wg_set_member_state(wg_ctx *ctx, int32_t member, const wg_state_view *state);
+wg_status wg_get_member_state(wg_ctx *ctx, int32_t member, wg_state_view *state);
 
 /* Copy ndays of day-major forcing [ndays*ncell] (precipitation mm, temperature C,
  * shortwave W/m2; the reference's climateYear.G_*_d365 floats, climateYear.h:12-15)
@@ -134,8 +150,17 @@ wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday);
  * above.  Forcing slots fday0.., discharge output slots from fday0 too. */
 wg_status wg_run_days(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays);
 
-/* Daily discharge (transported volume, km3/d) of the stations, [ndays*nstation],
- * for output slots [day0, day0+ndays). */
+/* A run of ndays days is a wavefront of ndays + levels - 1 steps (step t routes
+ * day t - offset(cell) of every cell).  wg_run_steps executes steps [t_begin,
+ * t_end) of such a run, so a long run can be split over several calls (for
+ * example one call per simulated year) without draining the wavefront between
+ * them; the results equal one wg_run_days call.  The state is only consistent
+ * (all cells on the same day) after the last step. */
+wg_status wg_run_steps(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin, int32_t t_end);
+int32_t wg_run_num_steps(const wg_ctx *ctx, int32_t ndays);
+
+/* Daily discharge (transported volume, km3/d) of the stations,
+ * [ndays][nstation][members], for output slots [day0, day0+ndays). */
 wg_status wg_get_discharge(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out);
 
 /* Water balance: out[0] total storage [km3] (land storages over the land fraction
@@ -145,6 +170,11 @@ wg_status wg_get_discharge(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out
  * closure residual relative to the cell's throughput.  Sums are compensated FP64. */
 wg_status wg_get_balance(wg_ctx *ctx, double out[6]);
 wg_status wg_reset_balance(wg_ctx *ctx);
+
+/* Launch shape of the persistent kernels: threads per block (64/128/256) and
+ * blocks (0 = as many as fit on the device at once).  Used by the autotuner. */
+wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks);
+wg_status wg_get_launch_shape(const wg_ctx *ctx, int32_t *threads, int32_t *blocks, int32_t *max_blocks);
 
 /* Wait for the context's stream. */
 wg_status wg_synchronize(wg_ctx *ctx);

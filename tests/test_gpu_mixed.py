@@ -1,0 +1,72 @@
+"""Mixed precision (FP32 state and fluxes, FP64 confluence and balance sums) and
+the batched ensemble, against the FP64 path on the same inputs.
+
+Error measure for discharge: largest |Q32 - Q64| over all outlets and days,
+relative to that outlet's largest FP64 discharge (so that near-zero flows of
+dry days do not dominate).  Bound: 1e-5 relative on outlet discharge for the
+FP32 paths (the ensemble's stated error bound).
+"""
+import numpy as np
+import pytest
+
+from helpers import max_rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _outlet_rel_err(q32, q64):
+    scale = np.maximum(np.abs(q64).max(axis=0), 1e-30)
+    return float(np.max(np.abs(q32 - q64) / scale))
+
+
+def test_fp32_global_one_year_discharge_error():
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_global()
+    P, T, S = sy.forcing(region, 365, doy0=1)
+    q64 = Model(region, max_days=365).run(1, P, T, S)
+    q32 = Model(region, max_days=365, precision="fp32").run(1, P, T, S)
+    err = _outlet_rel_err(q32, q64)
+    print(f"FP32 vs FP64 outlet discharge, max error relative to outlet peak: {err:.2e}")
+    assert err <= 1e-5, err
+
+
+def test_fp32_mass_balance_closes_in_fp64_sums():
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_small_swb(seed=14)
+    P, T, S = sy.forcing(region, 365, doy0=1)
+    m = Model(region, max_days=365, record_balance=True, precision="fp32")
+    s0 = m.balance()[0]
+    m.run(1, P, T, S)
+    total, pin, evap, out, leak, worst = m.balance()
+    resid = (total - s0) - (pin - evap - out + leak)
+    # FP32 state: closure is limited by FP32 rounding of the storages, the sums are FP64
+    assert abs(resid) <= 1e-5 * max(total, pin), (resid, total, pin)
+
+
+def test_ensemble_members_match_single_runs():
+    """Members with factor 1 equal the single FP32 run bit for bit; a member with a
+    precipitation factor equals a single FP32 run on scaled forcing."""
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_small_swb(seed=16)
+    nd = 60
+    P, T, S = sy.forcing(region, nd, doy0=90)
+    M = 64
+    pf = np.ones(M, np.float32)
+    pf[5] = np.float32(1.3)
+    gf = np.ones(M, np.float32)
+    ens = Model(region, max_days=nd, precision="fp32", members=M, prec_factor=pf, gamma_factor=gf)
+    qe = ens.run(90, P, T, S)                       # [nd, nst, M]
+    single = Model(region, max_days=nd, precision="fp32")
+    qs = single.run(90, P, T, S)
+    assert np.array_equal(qe[:, :, 0], qs)
+    assert np.array_equal(qe[:, :, 63], qs)
+    scaled = Model(region, max_days=nd, precision="fp32")
+    qsc = scaled.run(90, (P.astype(np.float32) * np.float32(1.3)).astype(np.float32), T, S)
+    assert np.array_equal(qe[:, :, 5], qsc)
+    st = ens.get_state(member=5)
+    st2 = scaled.get_state()
+    for k in ("soil", "river", "gw", "loclake"):
+        assert np.array_equal(st[k], st2[k]), k

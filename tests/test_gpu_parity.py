@@ -152,3 +152,38 @@ def test_mass_balance_closes_every_cell():
     resid = (total - s0) - (pin - evap - out + leak)
     assert abs(resid) <= 1e-12 * max(total, pin), (resid, total, pin)
     assert worst <= 1e-12, worst
+
+
+def test_split_steps_equal_one_launch():
+    """A run split into several wg_run_steps calls (wavefront not drained between
+    them) equals one wg_run_days call bit for bit."""
+    from watergap2_gb300 import synthetic as sy
+    region = sy.region_small_swb(seed=15)
+    nd = 150
+    P, T, S = sy.forcing(region, nd, doy0=250)
+    a = _model(region, max_days=nd, stations=np.arange(region.ncell))
+    a.upload_forcing(0, P, T, S)
+    a.run_days(250, 0, nd)
+    b = _model(region, max_days=nd, stations=np.arange(region.ncell))
+    b.upload_forcing(0, P, T, S)
+    total = b.num_steps(nd)
+    cuts = [0, 7, 40, 41, 100, total]
+    for t0, t1 in zip(cuts[:-1], cuts[1:]):
+        b.run_steps(250, 0, nd, t0, t1)
+    assert np.array_equal(a.discharge(0, nd), b.discharge(0, nd))
+    for k, v in a.get_state().items():
+        assert np.array_equal(v, b.get_state()[k]), k
+
+
+def test_small_ring_equals_large_ring():
+    """The vertical balance run ahead in chunks of a few days gives the same results."""
+    from watergap2_gb300 import synthetic as sy
+    region = sy.region_64x64(seed=6, size=24)
+    P, T, S = sy.forcing(region, 100, doy0=30)
+    a = _model(region, max_days=100)
+    qa = a.run(30, P, T, S)
+    b = _model(region, max_days=100, ring_days=9)
+    qb = b.run(30, P, T, S)
+    assert np.array_equal(qa, qb)
+    for k, v in a.get_state().items():
+        assert np.array_equal(v, b.get_state()[k]), k

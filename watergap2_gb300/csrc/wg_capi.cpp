@@ -8,14 +8,15 @@
 //   setStoragesToZero / setLakeWetlToMaximum  (daily.cpp:1882-1894, routing.cpp:790-848, 5647-5716)
 //   initFractionStatus / annualInit (routing.cpp:748-765, 979-1205)
 // Constants the reference recomputes each day from per-cell inputs are
-// evaluated here once, with the reference's expressions, so that the device
-// sees the identical double values.
+// evaluated here once, with the reference's expressions, in the precision of
+// the context (FP64, or FP32 for the mixed-precision and ensemble paths).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -65,7 +66,6 @@ wg_status reference_rout_order(int n, const int32_t *down, std::vector<int32_t> 
   std::vector<int32_t> frontier, next;
   for (int i = 0; i < n; ++i)
     if (cnt[i] == 0) frontier.push_back(i);
-  std::vector<char> listed(n, 0);
   while (!frontier.empty()) {
     std::sort(frontier.begin(), frontier.end());
     next.clear();
@@ -135,25 +135,57 @@ wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, 
   return WG_OK;
 }
 
+// Per-cell constants in cell order, double precision (converted to the context's
+// precision on upload).
+struct HostConsts {
+  std::vector<uint32_t> flags;
+  std::vector<int32_t> ext_row, station;
+  std::vector<int16_t> init_days, band_el;
+  std::vector<int8_t> start_month;
+  // one vector per DevCellsT field of type R
+#define WG_RFIELDS(X)                                                                                            \
+  X(cfa) X(inv_cfa) X(mprec) X(alpha) X(pet_mxdy) X(mnetrad) X(mcwh) X(t_snowfz) X(t_snowmt) X(pcritgwa) X(gamma) \
+  X(albedo) X(albedo_snow) X(ddf_m) X(lai_min) X(lai_max) X(smax) X(inv_smax) X(fg) X(rgmax) X(built_up)         \
+  X(t_gradnt) X(elev0) X(area) X(area_f) X(gw_e) X(gw_ik) X(gw_ome) X(sw_k) X(sw_e) X(sw_ik) X(sw_ome) X(evx)    \
+  X(a6) X(ll100) X(maxs_ll) X(inv_maxs_ll) X(lw100) X(maxs_lw) X(inv_maxs_lw) X(la6) X(maxs_gl) X(inv_maxs_gl)  \
+  X(ra6) X(rcap) X(inv_rcap) X(rcap01) X(inv_rcap085) X(c_ratio) X(c4) X(one_m_c4) X(prov_rel) X(gw100)         \
+  X(maxs_gw) X(inv_maxs_gw) X(bw) X(inv_mr) X(sqrt_slope) X(inv_len) X(rlen)
+#define X(f) std::vector<double> f;
+  WG_RFIELDS(X)
+#undef X
+  std::vector<double> band_dt;   // [ncell][nband]
+  std::vector<double> ext, inv_s0;
+  int nrow = 0;
+};
+
+inline double safe_inv(double x) { return x != 0. ? 1. / x : 0.; }
+
 }  // namespace
 
+// One context: all device buffers of one region in one precision.
 struct wg_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  int n = 0, nband = 0, max_days = 0, nstation = 0;
+  int n = 0, nband = 0, max_days = 0, nstation = 0, members = 1, precision = 0;
+  int threads = 256, blocks_fused = 0, blocks_route = 0;
   Topology topo;
-  DevCells cells{};
-  DevState state{};
-  DevVert vert{};
+  DevCellsT<double> cd{};
+  DevStateT<double> sd{};
+  DevVertT<double> vd{};
+  DevCellsT<float> cf{};
+  DevStateT<float> sf{};
+  DevVertT<float> vf{};
+  DevRingT<double> rd{};
+  DevRingT<float> rf{};
   DevForcing forcing{};
   DevBalance balance{};
+  DevMembers mem{};
   DevSync sync{};
   double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
   float *staging = nullptr;
   int32_t *d_cell_of_slot = nullptr;
   int staging_days = 0;
-  int blocks_fused = 0, blocks_route = 0;
   int64_t launches = 0;
   std::vector<void *> allocs;
   std::string err;
@@ -169,6 +201,7 @@ struct wg_ctx {
     allocs.push_back(p);
     return (T *)p;
   }
+  size_t nstate() const { return (size_t)n * members; }
 };
 
 namespace {
@@ -179,11 +212,11 @@ wg_status cuda_fail(wg_ctx *ctx, cudaError_t e, const char *what) {
   return e == cudaErrorMemoryAllocation ? WG_ERR_NOMEM : WG_ERR_CUDA;
 }
 
-// upload a per-cell host array (cell order) into slot order
-template <class T>
-const T *upload_slots(wg_ctx *ctx, const std::vector<T> &by_cell, wg_status &st) {
+// upload a per-cell host array (cell order) into slot order, converting to T
+template <class T, class S>
+const T *upload_slots(wg_ctx *ctx, const std::vector<S> &by_cell, wg_status &st) {
   std::vector<T> by_slot(by_cell.size());
-  for (size_t s = 0; s < by_slot.size(); ++s) by_slot[s] = by_cell[ctx->topo.cell_of_slot[s]];
+  for (size_t s = 0; s < by_slot.size(); ++s) by_slot[s] = (T)by_cell[ctx->topo.cell_of_slot[s]];
   T *d = ctx->alloc<T>(by_slot.size());
   if (!d) { st = WG_ERR_NOMEM; return nullptr; }
   cudaError_t e = cudaMemcpy(d, by_slot.data(), by_slot.size() * sizeof(T), cudaMemcpyHostToDevice);
@@ -191,82 +224,156 @@ const T *upload_slots(wg_ctx *ctx, const std::vector<T> &by_cell, wg_status &st)
   return d;
 }
 
-template <class T>
-const T *upload_raw(wg_ctx *ctx, const std::vector<T> &v, wg_status &st) {
-  T *d = ctx->alloc<T>(v.size());
+template <class T, class S>
+const T *upload_raw(wg_ctx *ctx, const std::vector<S> &v, wg_status &st) {
+  std::vector<T> c(v.begin(), v.end());
+  T *d = ctx->alloc<T>(c.size());
   if (!d) { st = WG_ERR_NOMEM; return nullptr; }
-  cudaError_t e = cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMemcpy(d, c.data(), c.size() * sizeof(T), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) st = cuda_fail(ctx, e, "upload");
   return d;
 }
 
 // band-major slot layout of a cell-major [ncell][nb] array
-template <class T>
-std::vector<T> bands_to_slots(const wg_ctx *ctx, const T *cellmajor, int nb) {
+template <class T, class S>
+std::vector<T> bands_to_slots(const wg_ctx *ctx, const S *cellmajor, int nb) {
   const int n = ctx->n;
   std::vector<T> out((size_t)n * nb);
   for (int s = 0; s < n; ++s) {
     const int c = ctx->topo.cell_of_slot[s];
-    for (int b = 0; b < nb; ++b) out[(size_t)b * n + s] = cellmajor[(size_t)c * nb + b];
+    for (int b = 0; b < nb; ++b) out[(size_t)b * n + s] = (T)cellmajor[(size_t)c * nb + b];
   }
   return out;
 }
 
-struct HostState {
-  std::vector<double> canopy, soil, snow, band, precsum, gw, river, loclake, locwetl, glolake, glowetl, res;
-  std::vector<double> rf_loclake, rf_locwetl, rf_glolake, rf_glowetl, rf_res, k_release, laf, laf_prev, fswb_next;
-  std::vector<int32_t> days, status, started;
-};
+template <class R>
+wg_status upload_cells(wg_ctx *ctx, const HostConsts &h, DevCellsT<R> &c, double default_velocity, int velo_opt) {
+  wg_status st = WG_OK;
+  c.n = ctx->n;
+  c.nband = ctx->nband;
+  c.velo_opt = velo_opt;
+  c.nrow = h.nrow;
+  c.default_velocity = (R)default_velocity;
+  c.invB = (R)(1.0 / ctx->nband);
+  c.nlevel = ctx->topo.nlevel;
+  c.nstation = ctx->nstation;
+  c.flags = upload_slots<uint32_t>(ctx, h.flags, st);
+  c.ext_row = upload_slots<int32_t>(ctx, h.ext_row, st);
+  c.station = upload_slots<int32_t>(ctx, h.station, st);
+  c.init_days = upload_slots<int16_t>(ctx, h.init_days, st);
+  c.start_month = upload_slots<int8_t>(ctx, h.start_month, st);
+#define X(f) c.f = upload_slots<R>(ctx, h.f, st);
+  WG_RFIELDS(X)
+#undef X
+  c.band_dt = upload_raw<R>(ctx, bands_to_slots<double>(ctx, h.band_dt.data(), ctx->nband), st);
+  c.band_el = upload_raw<int16_t>(ctx, bands_to_slots<int16_t>(ctx, h.band_el.data(), ctx->nband), st);
+  c.ext_rad = upload_raw<R>(ctx, h.ext, st);
+  c.inv_s0 = upload_raw<R>(ctx, h.inv_s0, st);
+  std::vector<int32_t> off_slot(ctx->n);
+  for (int s = 0; s < ctx->n; ++s) off_slot[s] = ctx->topo.offset[ctx->topo.cell_of_slot[s]];
+  c.offset = upload_raw<int32_t>(ctx, off_slot, st);
+  c.level_start = upload_raw<int32_t>(ctx, ctx->topo.level_start, st);
+  c.up_ptr = upload_raw<int32_t>(ctx, ctx->topo.up_ptr, st);
+  c.up_idx = upload_raw<int32_t>(ctx, ctx->topo.up_idx, st);
+  return st;
+}
 
-#define WG_STATE_FIELDS(X)                                                                                     \
-  X(canopy) X(soil) X(snow) X(lai_precsum) X(gw) X(river) X(loclake) X(locwetl) X(glolake) X(glowetl) X(res) \
+#define WG_STATE_R(X)                                                                                               \
+  X(canopy) X(soil) X(snow) X(lai_precsum) X(gw) X(river) X(loclake) X(locwetl) X(glolake) X(glowetl) X(res)      \
   X(rf_loclake) X(rf_locwetl) X(rf_glolake) X(rf_glowetl) X(rf_res) X(k_release) X(laf) X(laf_prev) X(fswb_next)
+#define WG_STATE_I(X) X(lai_days) X(lai_status) X(laf_started)
 
-wg_status copy_state(wg_ctx *ctx, const wg_state_view *v, bool to_device) {
-  const int n = ctx->n, B = ctx->nband;
+template <class R>
+wg_status alloc_state(wg_ctx *ctx, DevStateT<R> &s, DevVertT<R> &v) {
+  const size_t N = ctx->nstate();
+#define X(f) s.f = ctx->alloc<R>(N); if (!s.f) return WG_ERR_NOMEM;
+  WG_STATE_R(X)
+#undef X
+#define X(f) s.f = ctx->alloc<int32_t>(N); if (!s.f) return WG_ERR_NOMEM;
+  WG_STATE_I(X)
+#undef X
+  s.snow_band = ctx->alloc<R>(N * ctx->nband);
+  if (!s.snow_band) return WG_ERR_NOMEM;
+  const int n = ctx->n;
+  v.rs = ctx->alloc<R>(n); v.gwr = ctx->alloc<R>(n); v.transfer = ctx->alloc<R>(n); v.owp = ctx->alloc<R>(n);
+  v.owpet = ctx->alloc<R>(n); v.land_in = ctx->alloc<R>(n); v.land_evap = ctx->alloc<R>(n);
+  v.land_leak = ctx->alloc<R>(n);
+  return v.land_leak ? WG_OK : WG_ERR_NOMEM;
+}
+
+// Copy one member's state between host arrays (cell order, double) and the device.
+template <class R>
+wg_status copy_state(wg_ctx *ctx, const DevStateT<R> &s, const wg_state_view *v, int member, bool to_device) {
+  const int n = ctx->n, B = ctx->nband, M = ctx->members;
+  const size_t N = ctx->nstate();
   const auto &c2s = ctx->topo.cell_of_slot;
-  std::vector<double> tmp(n);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  // gather/scatter the member's values with a strided 2D copy (member innermost)
+  std::vector<R> tmp(n);
   std::vector<int32_t> itmp(n);
-  cudaError_t e = cudaSuccess;
-  auto dbl = [&](double *host, double *dev) {
+  auto xfer = [&](void *host_slots, void *dev, size_t elem) {
+    if (e != cudaSuccess) return;
+    char *base = (char *)dev + (size_t)member * elem;
+    if (to_device)
+      e = cudaMemcpy2D(base, elem * M, host_slots, elem, elem, n, cudaMemcpyHostToDevice);
+    else
+      e = cudaMemcpy2D(host_slots, elem, base, elem * M, elem, n, cudaMemcpyDeviceToHost);
+  };
+  auto dbl = [&](double *host, R *dev) {
     if (!host) return;
     if (to_device) {
-      for (int s = 0; s < n; ++s) tmp[s] = host[c2s[s]];
-      e = e ? e : cudaMemcpy(dev, tmp.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+      for (int q = 0; q < n; ++q) tmp[q] = (R)host[c2s[q]];
+      xfer(tmp.data(), dev, sizeof(R));
     } else {
-      e = e ? e : cudaMemcpy(tmp.data(), dev, n * sizeof(double), cudaMemcpyDeviceToHost);
-      for (int s = 0; s < n; ++s) host[c2s[s]] = tmp[s];
+      xfer(tmp.data(), dev, sizeof(R));
+      for (int q = 0; q < n; ++q) host[c2s[q]] = (double)tmp[q];
     }
   };
   auto i32 = [&](int32_t *host, int32_t *dev) {
     if (!host) return;
     if (to_device) {
-      for (int s = 0; s < n; ++s) itmp[s] = host[c2s[s]];
-      e = e ? e : cudaMemcpy(dev, itmp.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice);
+      for (int q = 0; q < n; ++q) itmp[q] = host[c2s[q]];
+      xfer(itmp.data(), dev, sizeof(int32_t));
     } else {
-      e = e ? e : cudaMemcpy(itmp.data(), dev, n * sizeof(int32_t), cudaMemcpyDeviceToHost);
-      for (int s = 0; s < n; ++s) host[c2s[s]] = itmp[s];
+      xfer(itmp.data(), dev, sizeof(int32_t));
+      for (int q = 0; q < n; ++q) host[c2s[q]] = itmp[q];
     }
   };
-  cudaStreamSynchronize(ctx->stream);
-#define X(f) dbl(v->f, ctx->state.f);
-  WG_STATE_FIELDS(X)
+#define X(f) dbl(v->f, s.f);
+  WG_STATE_R(X)
 #undef X
-  i32(v->lai_days, ctx->state.lai_days);
-  i32(v->lai_status, ctx->state.lai_status);
-  i32(v->laf_started, ctx->state.laf_started);
+#define X(f) i32(v->f, s.f);
+  WG_STATE_I(X)
+#undef X
   if (v->snow_band) {
-    std::vector<double> b((size_t)n * B);
-    if (to_device) {
-      b = bands_to_slots(ctx, v->snow_band, B);
-      e = e ? e : cudaMemcpy(ctx->state.snow_band, b.data(), b.size() * sizeof(double), cudaMemcpyHostToDevice);
-    } else {
-      e = e ? e : cudaMemcpy(b.data(), ctx->state.snow_band, b.size() * sizeof(double), cudaMemcpyDeviceToHost);
-      for (int s = 0; s < n; ++s)
-        for (int k = 0; k < B; ++k) v->snow_band[(size_t)c2s[s] * B + k] = b[(size_t)k * n + s];
+    for (int b = 0; b < B; ++b) {
+      R *dev = s.snow_band + (size_t)b * N;
+      if (to_device) {
+        for (int q = 0; q < n; ++q) tmp[q] = (R)v->snow_band[(size_t)c2s[q] * B + b];
+        xfer(tmp.data(), dev, sizeof(R));
+      } else {
+        xfer(tmp.data(), dev, sizeof(R));
+        for (int q = 0; q < n; ++q) v->snow_band[(size_t)c2s[q] * B + b] = (double)tmp[q];
+      }
     }
   }
   return cuda_fail(ctx, e, to_device ? "set_state" : "get_state");
+}
+
+wg_status state_io(wg_ctx *ctx, const wg_state_view *v, int member, bool to_device) {
+  if (member < 0 || member >= ctx->members) return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  return ctx->precision == 0 ? copy_state(ctx, ctx->sd, v, member, to_device)
+                             : copy_state(ctx, ctx->sf, v, member, to_device);
+}
+
+void fill_fastmath_tables(double e2[64], double lf[129], double inv[129]) {
+  for (int j = 0; j < 64; ++j) e2[j] = exp2((double)j / 64.0);
+  for (int j = 0; j <= 128; ++j) {
+    const double F = 1.0 + j / 128.0;
+    lf[j] = log(F);
+    inv[j] = 1.0 / F;
+  }
 }
 
 }  // namespace
@@ -296,7 +403,11 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   *out = nullptr;
   if (r->ncell <= 0 || r->nband <= 0 || r->nband > 256 || opt->max_days <= 0) return WG_ERR_INVALID;
   if (r->river_velo_opt < 0 || r->river_velo_opt > 2) return WG_ERR_UNSUPPORTED;
+  if (opt->precision < 0 || opt->precision > 1) return WG_ERR_UNSUPPORTED;
+  if (opt->members < 1 || (opt->members > 1 && opt->precision != 1)) return WG_ERR_UNSUPPORTED;
   if (opt->nstation < 0 || (opt->nstation > 0 && !opt->stations)) return WG_ERR_INVALID;
+  if (opt->block_threads != 0 && opt->block_threads != 64 && opt->block_threads != 128 && opt->block_threads != 256)
+    return WG_ERR_INVALID;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
     if (r->lct[i] < 1 || r->lct[i] > WG_NLCT) return WG_ERR_INVALID;
@@ -304,45 +415,47 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
       if (r->res_type[i] != 1 && r->res_type[i] != 2) return WG_ERR_INVALID;
       if (!(r->mean_outflow[i] > 0.) || r->start_month[i] < 1 || r->start_month[i] > 12) return WG_ERR_INVALID;
     }
+    if (!(r->river_length[i] > 0.)) return WG_ERR_INVALID;
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= opt->device) return WG_ERR_DEVICE;
-  wg_ctx *ctx = new wg_ctx();
+  std::unique_ptr<wg_ctx> ctx(new wg_ctx());
   ctx->device = opt->device;
   ctx->n = n;
   ctx->nband = B;
   ctx->max_days = opt->max_days;
   ctx->nstation = opt->nstation;
-  wg_status st = WG_OK;
-  cudaError_t e = cudaSetDevice(opt->device);
-  if (e != cudaSuccess) { delete ctx; return WG_ERR_DEVICE; }
+  ctx->members = opt->members;
+  ctx->precision = opt->precision;
+  ctx->threads = opt->block_threads ? opt->block_threads : 256;
+  if (cudaSetDevice(opt->device) != cudaSuccess) return WG_ERR_DEVICE;
   if (opt->stream) {
     ctx->stream = (cudaStream_t)opt->stream;
   } else {
-    e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { delete ctx; return WG_ERR_CUDA; }
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return WG_ERR_CUDA;
     ctx->own_stream = true;
   }
-  st = build_topology(n, r->downstream, r->rout_order, ctx->topo);
-  if (st != WG_OK) { delete ctx; return st; }
+  wg_status st = build_topology(n, r->downstream, r->rout_order, ctx->topo);
+  if (st != WG_OK) return st;
+  {
+    double e2[64], lf[129], inv[129];
+    fill_fastmath_tables(e2, lf, inv);
+    st = cuda_fail(ctx.get(), upload_fastmath_tables(e2, lf, inv), "fastmath tables");
+    if (st != WG_OK) return st;
+  }
 
-  // ----- per-cell constants, cell order (names as in DevCells)
+  // ----- per-cell constants in cell order, with the reference's expressions
   auto P = [&](int k, int i) { return r->param[(size_t)k * n + i]; };
   enum { GAMRUN = 0, CFA = 1, RIVRGH = 4, LAK_D = 5, WET_D = 6, SWOUTF = 7, EVAREDEX = 8, NETRAD = 9, PTC_HUM = 10,
          PTC_ARI = 11, PET_MXDY = 12, MCWH = 13, T_SNOWFZ = 15, T_SNOWMT = 16, DEGDAY = 17, T_GRADNT = 18,
          PCRITGWA = 21, GWOUTF = 22, PREC = 25 };
-  std::vector<uint32_t> flags(n);
-  std::vector<int32_t> ext_row(n), station(n, -1);
-  std::vector<int16_t> init_days(n);
-  std::vector<int8_t> start_month(n);
-  std::vector<double> area(n), a6(n), albedo(n), albedo_snow(n), ddf_m(n), lai_min(n), lai_max(n), mprec(n),
-      alpha(n), pet_mxdy(n), mnetrad(n), mcwh(n), t_snowfz(n), t_snowmt(n), pcritgwa(n), gamma(n), cfa(n), smax(n),
-      fg(n), rgmax(n), built_up(n), t_gradnt(n), elev0(n), gw_e(n), gw_ik(n), gw_ome(n), sw_k(n), sw_e(n), sw_ik(n),
-      sw_ome(n), evx(n), ll100(n), maxs_ll(n), lw100(n), maxs_lw(n), la6(n), maxs_gl(n), ra6(n), rcap(n), rcap01(n),
-      rcap085(n), c_ratio(n), c4(n), one_m_c4(n), prov_rel(n), gw100(n), maxs_gw(n), ll(n), lw(n), gwet(n), bw(n),
-      inv_mr(n), sqrt_slope(n), rlen(n);
-  std::vector<double> band_dt((size_t)n * B);
-  std::vector<int16_t> band_el((size_t)n * B);
+  HostConsts h;
+  h.flags.resize(n); h.ext_row.resize(n); h.station.assign(n, -1); h.init_days.resize(n); h.start_month.resize(n);
+#define X(f) h.f.assign(n, 0.);
+  WG_RFIELDS(X)
+#undef X
+  h.band_dt.resize((size_t)n * B);
+  h.band_el.resize((size_t)n * B);
   std::vector<double> lats;
   for (int i = 0; i < n; ++i) {
     const int lct = r->lct[i];
@@ -358,143 +471,141 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     if (r->glo_wetl[i] > 0) f |= F_GLOWETL;
     if (r->res_type[i] == 1) f |= F_RES_IRRIG;
     if (r->downstream[i] < 0) f |= F_OUTLET;
-    flags[i] = f;
+    {
+      const double l0 = (r->contfreq[i] - (r->glo_lake[i] + r->glo_wetl[i] + r->loc_lake[i] + r->loc_wetl[i] +
+                                           r->glo_res[i]));
+      if ((f & (F_LOCLAKE | F_LOCWETL | F_GLOLAKE | F_RES | F_GLOWETL)) || !(l0 > 0.)) f |= F_VINLINE;
+    }
+    h.flags[i] = f;
     const double ar = r->area_km2[i];
-    area[i] = ar;
-    a6[i] = ar / 1000000.;
-    albedo[i] = r->lct_albedo[lct - 1];
-    albedo_snow[i] = r->lct_albedo_snow[lct - 1];
-    ddf_m[i] = P(DEGDAY, i) * r->lct_ddf[lct - 1];
+    h.area[i] = ar;
+    h.area_f[i] = ar * 1e-8;
+    h.a6[i] = ar / 1000000.;
+    h.albedo[i] = r->lct_albedo[lct - 1];
+    h.albedo_snow[i] = r->lct_albedo_snow[lct - 1];
+    h.ddf_m[i] = P(DEGDAY, i) * r->lct_ddf[lct - 1];
     const float lmin = r->lct_lai_a[lct - 1] + r->lct_lai_b[lct - 1] * r->lai_max[i];   // lai.cpp:154 (float)
-    lai_min[i] = lmin;
-    lai_max[i] = r->lai_max[i];
-    init_days[i] = r->lct_initial_days[lct - 1];
-    mprec[i] = P(PREC, i);
-    alpha[i] = (r->aindex[i] == 1) ? P(PTC_ARI, i) : P(PTC_HUM, i);
-    pet_mxdy[i] = P(PET_MXDY, i);
-    mnetrad[i] = P(NETRAD, i);
-    mcwh[i] = P(MCWH, i);
-    t_snowfz[i] = P(T_SNOWFZ, i);
-    t_snowmt[i] = P(T_SNOWMT, i);
-    pcritgwa[i] = P(PCRITGWA, i);
-    gamma[i] = P(GAMRUN, i);
-    cfa[i] = P(CFA, i);
-    smax[i] = r->smax[i];
-    fg[i] = r->gw_factor[i];
-    rgmax[i] = r->rg_max[i] / 100.;
-    built_up[i] = r->built_up[i];
-    t_gradnt[i] = P(T_GRADNT, i);
+    h.lai_min[i] = lmin;
+    h.lai_max[i] = r->lai_max[i];
+    h.init_days[i] = r->lct_initial_days[lct - 1];
+    h.mprec[i] = P(PREC, i);
+    h.alpha[i] = (r->aindex[i] == 1) ? P(PTC_ARI, i) : P(PTC_HUM, i);
+    h.pet_mxdy[i] = P(PET_MXDY, i);
+    h.mnetrad[i] = P(NETRAD, i);
+    h.mcwh[i] = P(MCWH, i);
+    h.t_snowfz[i] = P(T_SNOWFZ, i);
+    h.t_snowmt[i] = P(T_SNOWMT, i);
+    h.pcritgwa[i] = P(PCRITGWA, i);
+    h.gamma[i] = P(GAMRUN, i);
+    h.cfa[i] = P(CFA, i);
+    h.inv_cfa[i] = safe_inv(P(CFA, i));
+    h.smax[i] = r->smax[i];
+    h.inv_smax[i] = safe_inv((double)r->smax[i]);
+    h.fg[i] = r->gw_factor[i];
+    h.rgmax[i] = r->rg_max[i] / 100.;
+    h.built_up[i] = r->built_up[i];
+    h.t_gradnt[i] = P(T_GRADNT, i);
     const int16_t *el = r->elev + (size_t)i * (B + 1);
-    elev0[i] = el[0];
+    h.elev0[i] = el[0];
     for (int b = 0; b < B; ++b) {
-      band_dt[(size_t)i * B + b] = (el[b + 1] - el[0]) * P(T_GRADNT, i);
-      band_el[(size_t)i * B + b] = el[b + 1];
+      h.band_dt[(size_t)i * B + b] = (el[b + 1] - el[0]) * P(T_GRADNT, i);
+      h.band_el[(size_t)i * B + b] = el[b + 1];
     }
     const double kg = P(GWOUTF, i);
-    gw_e[i] = exp(-1. * kg);
-    gw_ik[i] = 1. / kg;
-    gw_ome[i] = 1. - exp(-1. * kg);
+    h.gw_e[i] = exp(-1. * kg);
+    h.gw_ik[i] = 1. / kg;
+    h.gw_ome[i] = 1. - exp(-1. * kg);
     const double ks = P(SWOUTF, i);
-    sw_k[i] = ks;
-    sw_e[i] = exp(-1. * ks);
-    sw_ik[i] = 1. / ks;
-    sw_ome[i] = 1. - exp(-1. * ks);
-    evx[i] = P(EVAREDEX, i) * 3.32193;
+    h.sw_k[i] = ks;
+    h.sw_e[i] = exp(-1. * ks);
+    h.sw_ik[i] = 1. / ks;
+    h.sw_ome[i] = 1. - exp(-1. * ks);
+    h.evx[i] = P(EVAREDEX, i) * 3.32193;
     const double lakeDepth = P(LAK_D, i) * 0.001, wetlDepth = P(WET_D, i) * 0.001;
-    ll[i] = r->loc_lake[i];
-    lw[i] = r->loc_wetl[i];
-    gwet[i] = r->glo_wetl[i];
-    ll100[i] = r->loc_lake[i] / 100.;
-    maxs_ll[i] = ((r->loc_lake[i]) / 100.) * ar * lakeDepth;
-    lw100[i] = r->loc_wetl[i] / 100.;
-    maxs_lw[i] = ((r->loc_wetl[i]) / 100.) * ar * wetlDepth;
-    la6[i] = r->lake_area[i] / 1000000.;
-    maxs_gl[i] = (r->lake_area[i]) * lakeDepth;
-    ra6[i] = r->res_area[i] / 1000000.;
-    rcap[i] = r->stor_cap[i];
-    rcap01[i] = r->stor_cap[i] * 0.1;
-    rcap085[i] = r->stor_cap[i] * 0.85;
+    h.ll100[i] = r->loc_lake[i] / 100.;
+    h.maxs_ll[i] = ((r->loc_lake[i]) / 100.) * ar * lakeDepth;
+    h.inv_maxs_ll[i] = safe_inv(h.maxs_ll[i]);
+    h.lw100[i] = r->loc_wetl[i] / 100.;
+    h.maxs_lw[i] = ((r->loc_wetl[i]) / 100.) * ar * wetlDepth;
+    h.inv_maxs_lw[i] = safe_inv(h.maxs_lw[i]);
+    h.la6[i] = r->lake_area[i] / 1000000.;
+    h.maxs_gl[i] = (r->lake_area[i]) * lakeDepth;
+    h.inv_maxs_gl[i] = safe_inv(h.maxs_gl[i]);
+    h.ra6[i] = r->res_area[i] / 1000000.;
+    h.rcap[i] = r->stor_cap[i];
+    h.inv_rcap[i] = safe_inv(r->stor_cap[i]);
+    h.rcap01[i] = r->stor_cap[i] * 0.1;
+    h.inv_rcap085[i] = safe_inv(r->stor_cap[i] * 0.85);
     if (r->res_area[i] > 0.) {
-      c_ratio[i] = r->stor_cap[i] / (r->mean_outflow[i] * 31536000. / 1000000000.);
-      c4[i] = (4. * c_ratio[i] * c_ratio[i]);
-      one_m_c4[i] = (1.0 - ((4. * c_ratio[i] * c_ratio[i])));
+      h.c_ratio[i] = r->stor_cap[i] / (r->mean_outflow[i] * 31536000. / 1000000000.);
+      h.c4[i] = (4. * h.c_ratio[i] * h.c_ratio[i]);
+      h.one_m_c4[i] = (1.0 - ((4. * h.c_ratio[i] * h.c_ratio[i])));
       if (r->res_type[i] == 1) {
         // net use is out of scope: the downstream monthly demand is 0 (routing.cpp:2961-2983)
         const double monthlyUse = 0.0;
         if (r->mean_demand[i] >= 0.5 * r->mean_outflow[i])
-          prov_rel[i] = r->mean_outflow[i] / 2. * (1. + monthlyUse / r->mean_demand[i]);
+          h.prov_rel[i] = r->mean_outflow[i] / 2. * (1. + monthlyUse / r->mean_demand[i]);
         else
-          prov_rel[i] = r->mean_outflow[i] + monthlyUse - r->mean_demand[i];
+          h.prov_rel[i] = r->mean_outflow[i] + monthlyUse - r->mean_demand[i];
       } else {
-        prov_rel[i] = r->mean_outflow[i];
+        h.prov_rel[i] = r->mean_outflow[i];
       }
     }
-    start_month[i] = r->start_month[i];
-    gw100[i] = r->glo_wetl[i] / 100.;
-    maxs_gw[i] = ((r->glo_wetl[i]) / 100.) * ar * wetlDepth;
+    h.start_month[i] = r->start_month[i];
+    h.gw100[i] = r->glo_wetl[i] / 100.;
+    h.maxs_gw[i] = ((r->glo_wetl[i]) / 100.) * ar * wetlDepth;
+    h.inv_maxs_gw[i] = safe_inv(h.maxs_gw[i]);
     double bf = r->bankfull[i];                       // routing.cpp:488-495
     if (bf < 0.05) bf = 0.05;
-    bw[i] = 2.71 * pow(bf, 0.557) - 2.0 * 2.0 * (0.349 * pow(bf, 0.341));
-    inv_mr[i] = 1. / (P(RIVRGH, i) * r->roughness[i]);
-    sqrt_slope[i] = pow(r->river_slope[i], 0.5);
-    rlen[i] = r->river_length[i];
-    // latitude row of the extraterrestrial-radiation table
+    h.bw[i] = 2.71 * pow(bf, 0.557) - 2.0 * 2.0 * (0.349 * pow(bf, 0.341));
+    h.inv_mr[i] = 1. / (P(RIVRGH, i) * r->roughness[i]);
+    h.sqrt_slope[i] = pow(r->river_slope[i], 0.5);
+    h.rlen[i] = r->river_length[i];
+    h.inv_len[i] = 1. / r->river_length[i];
     auto it = std::find(lats.begin(), lats.end(), r->lat_deg[i]);
-    if (it == lats.end()) { lats.push_back(r->lat_deg[i]); ext_row[i] = (int32_t)lats.size() - 1; }
-    else ext_row[i] = (int32_t)(it - lats.begin());
+    if (it == lats.end()) { lats.push_back(r->lat_deg[i]); h.ext_row[i] = (int32_t)lats.size() - 1; }
+    else h.ext_row[i] = (int32_t)(it - lats.begin());
   }
   for (int k = 0; k < opt->nstation; ++k) {
     const int cidx = opt->stations[k];
-    if (cidx < 0 || cidx >= n) { delete ctx; return WG_ERR_INVALID; }
-    station[cidx] = k;
+    if (cidx < 0 || cidx >= n) return WG_ERR_INVALID;
+    h.station[cidx] = k;
   }
-  const int nrow = (int)lats.size();
-  std::vector<double> ext((size_t)365 * nrow);
+  h.nrow = (int)lats.size();
+  h.ext.resize((size_t)365 * h.nrow);
+  h.inv_s0.resize((size_t)365 * h.nrow);
   for (int d = 1; d <= 365; ++d)
-    for (int k = 0; k < nrow; ++k) ext[(size_t)(d - 1) * nrow + k] = calc_ext_rad((short)d, lats[k]);
-
-  DevCells &c = ctx->cells;
-  c.n = n;
-  c.nband = B;
-  c.velo_opt = r->river_velo_opt;
-  c.nrow = nrow;
-  c.default_velocity = r->default_velocity;
-  c.nlevel = ctx->topo.nlevel;
-  c.nstation = opt->nstation;
-#define UP(field) c.field = upload_slots(ctx, field, st);
-  UP(flags) UP(ext_row) UP(init_days) UP(start_month) UP(station) UP(area) UP(a6) UP(albedo) UP(albedo_snow)
-  UP(ddf_m) UP(lai_min) UP(lai_max) UP(mprec) UP(alpha) UP(pet_mxdy) UP(mnetrad) UP(mcwh) UP(t_snowfz)
-  UP(t_snowmt) UP(pcritgwa) UP(gamma) UP(cfa) UP(smax) UP(fg) UP(rgmax) UP(built_up) UP(t_gradnt) UP(elev0)
-  UP(gw_e) UP(gw_ik) UP(gw_ome) UP(sw_k) UP(sw_e) UP(sw_ik) UP(sw_ome) UP(evx) UP(ll100) UP(maxs_ll) UP(lw100)
-  UP(maxs_lw) UP(la6) UP(maxs_gl) UP(ra6) UP(rcap) UP(rcap01) UP(rcap085) UP(c_ratio) UP(c4) UP(one_m_c4)
-  UP(prov_rel) UP(gw100) UP(maxs_gw) UP(ll) UP(lw) UP(gwet) UP(bw) UP(inv_mr) UP(sqrt_slope) UP(rlen)
-#undef UP
-  c.band_dt = upload_raw(ctx, bands_to_slots(ctx, band_dt.data(), B), st);
-  c.band_el = upload_raw(ctx, bands_to_slots(ctx, band_el.data(), B), st);
-  c.ext_rad = upload_raw(ctx, ext, st);
-  std::vector<int32_t> off_slot(n);
-  for (int s = 0; s < n; ++s) off_slot[s] = ctx->topo.offset[ctx->topo.cell_of_slot[s]];
-  c.offset = upload_raw(ctx, off_slot, st);
-  c.level_start = upload_raw(ctx, ctx->topo.level_start, st);
-  c.up_ptr = upload_raw(ctx, ctx->topo.up_ptr, st);
-  c.up_idx = upload_raw(ctx, ctx->topo.up_idx, st);
-  ctx->d_cell_of_slot = (int32_t *)upload_raw(ctx, ctx->topo.cell_of_slot, st);
-  if (st != WG_OK) { wg_destroy(ctx); return st; }
+    for (int k = 0; k < h.nrow; ++k) {
+      const double e = calc_ext_rad((short)d, lats[k]);
+      h.ext[(size_t)(d - 1) * h.nrow + k] = e;
+      h.inv_s0[(size_t)(d - 1) * h.nrow + k] = safe_inv((0.25 + 0.5) * e);
+    }
+  st = ctx->precision == 0 ? upload_cells(ctx.get(), h, ctx->cd, r->default_velocity, r->river_velo_opt)
+                           : upload_cells(ctx.get(), h, ctx->cf, r->default_velocity, r->river_velo_opt);
+  ctx->d_cell_of_slot = (int32_t *)upload_raw<int32_t>(ctx.get(), ctx->topo.cell_of_slot, st);
+  if (st != WG_OK) return st;
 
   // ----- dynamic buffers
-  DevState &s = ctx->state;
-#define AL(f, T) s.f = ctx->alloc<T>(n);
-  AL(canopy, double) AL(soil, double) AL(snow, double) AL(lai_days, int32_t) AL(lai_status, int32_t)
-  AL(lai_precsum, double) AL(gw, double) AL(river, double) AL(loclake, double) AL(locwetl, double)
-  AL(glolake, double) AL(glowetl, double) AL(res, double) AL(rf_loclake, double) AL(rf_locwetl, double)
-  AL(rf_glolake, double) AL(rf_glowetl, double) AL(rf_res, double) AL(k_release, double) AL(laf, double)
-  AL(laf_prev, double) AL(fswb_next, double) AL(laf_started, int32_t)
-#undef AL
-  s.snow_band = ctx->alloc<double>((size_t)n * B);
-  DevVert &v = ctx->vert;
-  v.rs = ctx->alloc<double>(n); v.gwr = ctx->alloc<double>(n); v.transfer = ctx->alloc<double>(n);
-  v.owp = ctx->alloc<double>(n); v.owpet = ctx->alloc<double>(n); v.land_in = ctx->alloc<double>(n);
-  v.land_evap = ctx->alloc<double>(n); v.land_leak = ctx->alloc<double>(n);
+  st = ctx->precision == 0 ? alloc_state(ctx.get(), ctx->sd, ctx->vd) : alloc_state(ctx.get(), ctx->sf, ctx->vf);
+  if (st != WG_OK) return st;
+  const size_t N = ctx->nstate();
+  {
+    // ring of vertical outputs: as many days as fit in ~2 GB, at least 8, at most max_days
+    const size_t elem = ctx->precision == 0 ? sizeof(double) : sizeof(float);
+    const size_t budget = opt->ring_days > 0 ? (size_t)opt->ring_days : ((size_t)2 << 30) / (2 * elem * N);
+    const int ring = (int)std::max<size_t>(8, std::min<size_t>(budget, (size_t)ctx->max_days));
+    if (ctx->precision == 0) {
+      ctx->rd.ring_days = ring;
+      ctx->rd.rs = ctx->alloc<double>((size_t)ring * N);
+      ctx->rd.gwr = ctx->alloc<double>((size_t)ring * N);
+      if (!ctx->rd.gwr) return WG_ERR_NOMEM;
+    } else {
+      ctx->rf.ring_days = ring;
+      ctx->rf.rs = ctx->alloc<float>((size_t)ring * N);
+      ctx->rf.gwr = ctx->alloc<float>((size_t)ring * N);
+      if (!ctx->rf.gwr) return WG_ERR_NOMEM;
+    }
+  }
   float *fb = ctx->alloc<float>((size_t)3 * ctx->max_days * n);
   ctx->forcing.prec = fb;
   ctx->forcing.temp = fb ? fb + (size_t)ctx->max_days * n : nullptr;
@@ -502,27 +613,37 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   ctx->forcing.max_days = ctx->max_days;
   ctx->staging_days = std::min(ctx->max_days, 32);
   ctx->staging = ctx->alloc<float>((size_t)ctx->staging_days * n);
-  ctx->outq = ctx->alloc<double>((size_t)2 * n);
-  ctx->qst = ctx->alloc<double>((size_t)ctx->max_days * std::max(1, ctx->nstation));
-  ctx->balance.acc = ctx->alloc<double>((size_t)10 * n);
+  ctx->outq = ctx->alloc<double>((size_t)2 * N);
+  ctx->qst = ctx->alloc<double>((size_t)ctx->max_days * std::max(1, ctx->nstation) * ctx->members);
   ctx->balance.enabled = opt->record_balance ? 1 : 0;
-  ctx->vol0 = ctx->alloc<double>(n);
-  ctx->partial = ctx->alloc<double>((size_t)8 * ((n + 255) / 256));
+  ctx->balance.acc = ctx->alloc<double>(ctx->balance.enabled ? (size_t)10 * N : 1);
+  ctx->vol0 = ctx->alloc<double>(N);
+  ctx->partial = ctx->alloc<double>((size_t)8 * ((N + 255) / 256));
   ctx->sync.counter = ctx->alloc<unsigned int>(1);
   ctx->sync.error = ctx->alloc<int>(1);
-  if (!s.snow_band || !v.land_leak || !fb || !ctx->staging || !ctx->outq || !ctx->qst || !ctx->balance.acc ||
-      !ctx->vol0 || !ctx->partial || !ctx->sync.counter || !ctx->sync.error || !s.laf_started) {
-    wg_destroy(ctx);
+  float *mf = ctx->alloc<float>((size_t)2 * ctx->members);
+  if (!fb || !ctx->staging || !ctx->outq || !ctx->qst || !ctx->balance.acc || !ctx->vol0 || !ctx->partial ||
+      !ctx->sync.counter || !ctx->sync.error || !mf)
     return WG_ERR_NOMEM;
+  {
+    std::vector<float> fac(2 * ctx->members, 1.0f);
+    for (int k = 0; k < ctx->members; ++k) {
+      if (opt->member_prec_factor) fac[k] = opt->member_prec_factor[k];
+      if (opt->member_gamma_factor) fac[ctx->members + k] = opt->member_gamma_factor[k];
+    }
+    cudaMemcpy(mf, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice);
+    ctx->mem.members = ctx->members;
+    ctx->mem.prec_factor = mf;
+    ctx->mem.gamma_factor = mf + ctx->members;
   }
   cudaMemset(ctx->sync.error, 0, sizeof(int));
-  cudaMemset(ctx->outq, 0, (size_t)2 * n * sizeof(double));
-  cudaMemset(ctx->qst, 0, (size_t)ctx->max_days * std::max(1, ctx->nstation) * sizeof(double));
+  cudaMemset(ctx->outq, 0, (size_t)2 * N * sizeof(double));
+  cudaMemset(ctx->qst, 0, (size_t)ctx->max_days * std::max(1, ctx->nstation) * ctx->members * sizeof(double));
 
   // ----- start-of-run state, cell order (the reference's set-up sequence; see file header)
-  std::vector<double> z(n, 0.), one(n, 1.), rf_res(n, 0.), kr(n, 0.1), loclake(n), locwetl(n), glolake(n), glowetl(n),
-      resv(n), laf(n), fswb(n), bands((size_t)n * B, 0.), river(n, 0.);
-  std::vector<int32_t> iz(n, 0);
+  std::vector<double> zeros(n, 0.), ones(n, 1.), kr(n, 0.1), loclake(n), locwetl(n), glolake(n), glowetl(n),
+      resv(n), laf(n), fswb(n), bands((size_t)n * B, 0.), river(n, 0.), rfres(n, 0.);
+  std::vector<int32_t> izero(n, 0);
   for (int i = 0; i < n; ++i) {
     const double ar = r->area_km2[i];
     const double lakeDepth = P(LAK_D, i) * 0.001, wetlDepth = P(WET_D, i) * 0.001;
@@ -542,47 +663,34 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     }
   }
   wg_state_view init{};
-  init.canopy = z.data();
-  std::vector<double> z2(n, 0.), z3(n, 0.), z4(n, 0.), z5(n, 0.);
-  init.soil = z2.data();
-  init.snow = z3.data();
-  init.snow_band = bands.data();
-  std::vector<int32_t> iz2(n, 0);
-  init.lai_days = iz.data();
-  init.lai_status = iz2.data();
-  init.lai_precsum = z4.data();
-  init.gw = z5.data();
-  init.river = river.data();
-  init.loclake = loclake.data();
-  init.locwetl = locwetl.data();
-  init.glolake = glolake.data();
-  init.glowetl = glowetl.data();
-  init.res = resv.data();
-  std::vector<double> o1(n, 1.), o2(n, 1.), o3(n, 1.), o4(n, 1.);
-  init.rf_loclake = o1.data();
-  init.rf_locwetl = o2.data();
-  init.rf_glolake = o3.data();
-  init.rf_glowetl = o4.data();
-  init.rf_res = rf_res.data();
-  init.k_release = kr.data();
-  init.laf = laf.data();
-  std::vector<double> lp(n, 0.);
-  init.laf_prev = lp.data();
-  init.fswb_next = fswb.data();
-  std::vector<int32_t> started(n, 0);
-  init.laf_started = started.data();
-  st = copy_state(ctx, &init, true);
-  if (st != WG_OK) { wg_destroy(ctx); return st; }
-  ctx->blocks_fused = std::min(pipeline_max_blocks(true), (n + 255) / 256);
-  ctx->blocks_route = std::min(pipeline_max_blocks(false), (n + 255) / 256);
+  init.canopy = zeros.data(); init.soil = zeros.data(); init.snow = zeros.data(); init.snow_band = bands.data();
+  init.lai_days = izero.data(); init.lai_status = izero.data(); init.lai_precsum = zeros.data();
+  init.gw = zeros.data(); init.river = river.data(); init.loclake = loclake.data(); init.locwetl = locwetl.data();
+  init.glolake = glolake.data(); init.glowetl = glowetl.data(); init.res = resv.data();
+  init.rf_loclake = ones.data(); init.rf_locwetl = ones.data(); init.rf_glolake = ones.data();
+  init.rf_glowetl = ones.data(); init.rf_res = rfres.data(); init.k_release = kr.data();
+  init.laf = laf.data(); init.laf_prev = zeros.data(); init.fswb_next = fswb.data(); init.laf_started = izero.data();
+  for (int m = 0; m < ctx->members; ++m) {
+    st = state_io(ctx.get(), &init, m, true);
+    if (st != WG_OK) return st;
+  }
+  const bool ens = ctx->members > 1;
+  const int th = ctx->threads;
+  const int need = (int)std::min<size_t>((N + th - 1) / th, (size_t)1 << 30);
+  if (ctx->precision == 0) {
+    ctx->blocks_fused = std::min(pipeline_max_blocks<double>(true, ens, th), need);
+    ctx->blocks_route = std::min(pipeline_max_blocks<double>(false, ens, th), need);
+  } else {
+    ctx->blocks_fused = std::min(pipeline_max_blocks<float>(true, ens, th), need);
+    ctx->blocks_route = std::min(pipeline_max_blocks<float>(false, ens, th), need);
+  }
   if (ctx->blocks_fused <= 0 || ctx->blocks_route <= 0) {
     ctx->err = "cooperative launch not possible";
-    wg_destroy(ctx);
     return WG_ERR_DEVICE;
   }
-  st = wg_reset_balance(ctx);
-  if (st != WG_OK) { wg_destroy(ctx); return st; }
-  *out = ctx;
+  st = wg_reset_balance(ctx.get());
+  if (st != WG_OK) return st;
+  *out = ctx.release();
   return WG_OK;
 }
 
@@ -596,24 +704,23 @@ wg_status wg_destroy(wg_ctx *ctx) {
 
 wg_status wg_set_state(wg_ctx *ctx, const wg_state_view *v) {
   if (!ctx || !v) return WG_ERR_INVALID;
-  cudaSetDevice(ctx->device);
-  return copy_state(ctx, v, true);
+  return state_io(ctx, v, 0, true);
 }
 
 wg_status wg_get_state(wg_ctx *ctx, wg_state_view *v) {
   if (!ctx || !v) return WG_ERR_INVALID;
-  cudaSetDevice(ctx->device);
-  return copy_state(ctx, v, false);
+  return state_io(ctx, v, 0, false);
 }
 
-}  // extern "C"
-
-namespace wg {
-cudaError_t launch_gather_forcing(const float *src, float *dst, const int32_t *cell_of_slot, int n, int ndays,
-                                  cudaStream_t st);
+wg_status wg_set_member_state(wg_ctx *ctx, int32_t member, const wg_state_view *v) {
+  if (!ctx || !v) return WG_ERR_INVALID;
+  return state_io(ctx, v, member, true);
 }
 
-extern "C" {
+wg_status wg_get_member_state(wg_ctx *ctx, int32_t member, wg_state_view *v) {
+  if (!ctx || !v) return WG_ERR_INVALID;
+  return state_io(ctx, v, member, false);
+}
 
 wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec, const float *temp,
                             const float *swrad) {
@@ -640,31 +747,69 @@ wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const floa
 
 wg_status wg_step_vertical(wg_ctx *ctx, int32_t doy, int32_t fday) {
   if (!ctx || doy < 1 || doy > 365 || fday < 0 || fday >= ctx->max_days) return WG_ERR_INVALID;
+  if (ctx->members != 1) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
   ctx->launches++;
-  return cuda_fail(ctx, launch_vertical(ctx->cells, ctx->state, ctx->vert, ctx->forcing, doy, fday, ctx->stream),
-                   "step_vertical");
+  cudaError_t e = ctx->precision == 0
+                      ? launch_vertical(ctx->cd, ctx->sd, ctx->vd, ctx->forcing, doy, fday, ctx->stream)
+                      : launch_vertical(ctx->cf, ctx->sf, ctx->vf, ctx->forcing, doy, fday, ctx->stream);
+  return cuda_fail(ctx, e, "step_vertical");
 }
 
 wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday) {
   if (!ctx || doy < 1 || doy > 365 || oday < 0 || oday >= ctx->max_days) return WG_ERR_INVALID;
+  if (ctx->members != 1) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
   ctx->launches++;
-  return cuda_fail(ctx,
-                   launch_pipeline(false, ctx->cells, ctx->state, ctx->vert, ctx->forcing, ctx->balance, ctx->sync,
-                                   ctx->outq, ctx->qst, doy, 0, oday, 1, ctx->blocks_route, ctx->stream),
-                   "step_routing");
+  cudaError_t e = ctx->precision == 0
+                      ? launch_pipeline(false, ctx->cd, ctx->sd, ctx->vd, ctx->forcing, ctx->mem, ctx->balance,
+                                        ctx->rd, ctx->sync, ctx->outq, ctx->qst, doy, 0, oday, 1, 0, ctx->topo.nlevel,
+                                        ctx->blocks_route, ctx->threads, ctx->stream)
+                      : launch_pipeline(false, ctx->cf, ctx->sf, ctx->vf, ctx->forcing, ctx->mem, ctx->balance,
+                                        ctx->rf, ctx->sync, ctx->outq, ctx->qst, doy, 0, oday, 1, 0, ctx->topo.nlevel,
+                                        ctx->blocks_route, ctx->threads, ctx->stream);
+  return cuda_fail(ctx, e, "step_routing");
 }
 
-wg_status wg_run_days(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays) {
-  if (!ctx || doy0 < 1 || doy0 > 365 || fday0 < 0 || ndays <= 0 || fday0 + ndays > ctx->max_days)
-    return WG_ERR_INVALID;
+}  // extern "C"
+
+// Steps [t_b, t_e) of the day-pipelined wavefront of a run of ndays days: for each
+// chunk of at most ring_days steps, the vertical balance of the cells without water
+// bodies runs ahead (one launch), then the routing wavefront (one cooperative launch).
+template <class R>
+static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
+                                const DevRingT<R> &ring, int doy0, int fday0, int ndays, int t_b, int t_e) {
+  for (int a = t_b; a < t_e; a += ring.ring_days) {
+    const int b = std::min(t_e, a + ring.ring_days);
+    cudaError_t e = launch_vertical_ahead(c, s, ctx->forcing, ctx->mem, ctx->balance, ring, doy0, fday0, ndays, a, b,
+                                          ctx->stream);
+    ctx->launches++;
+    if (e == cudaSuccess)
+      e = launch_pipeline(true, c, s, v, ctx->forcing, ctx->mem, ctx->balance, ring, ctx->sync, ctx->outq, ctx->qst,
+                          doy0, fday0, fday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->stream);
+    ctx->launches++;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "run_steps");
+  }
+  return WG_OK;
+}
+
+extern "C" {
+
+wg_status wg_run_steps(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin, int32_t t_end) {
+  if (!ctx || doy0 < 1 || doy0 > 365 || fday0 < 0 || ndays <= 0 || fday0 + ndays > ctx->max_days) return WG_ERR_INVALID;
+  const int total = ndays + ctx->topo.nlevel - 1;
+  if (t_begin < 0 || t_end > total || t_begin > t_end) return WG_ERR_INVALID;
+  if (t_begin == t_end) return WG_OK;
   cudaSetDevice(ctx->device);
-  ctx->launches++;
-  return cuda_fail(ctx,
-                   launch_pipeline(true, ctx->cells, ctx->state, ctx->vert, ctx->forcing, ctx->balance, ctx->sync,
-                                   ctx->outq, ctx->qst, doy0, fday0, fday0, ndays, ctx->blocks_fused, ctx->stream),
-                   "run_days");
+  return ctx->precision == 0 ? run_steps_impl(ctx, ctx->cd, ctx->sd, ctx->vd, ctx->rd, doy0, fday0, ndays, t_begin, t_end)
+                             : run_steps_impl(ctx, ctx->cf, ctx->sf, ctx->vf, ctx->rf, doy0, fday0, ndays, t_begin, t_end);
+}
+
+int32_t wg_run_num_steps(const wg_ctx *ctx, int32_t ndays) { return ctx ? ndays + ctx->topo.nlevel - 1 : 0; }
+
+wg_status wg_run_days(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays) {
+  if (!ctx) return WG_ERR_INVALID;
+  return wg_run_steps(ctx, doy0, fday0, ndays, 0, ndays + ctx->topo.nlevel - 1);
 }
 
 wg_status wg_synchronize(wg_ctx *ctx) {
@@ -687,26 +832,35 @@ wg_status wg_get_discharge(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out
   if (ctx->nstation == 0 || ndays == 0) return WG_OK;
   wg_status st = wg_synchronize(ctx);
   if (st != WG_OK) return st;
+  const size_t per_day = (size_t)ctx->nstation * ctx->members;
   return cuda_fail(ctx,
-                   cudaMemcpy(out, ctx->qst + (size_t)day0 * ctx->nstation,
-                              (size_t)ndays * ctx->nstation * sizeof(double), cudaMemcpyDeviceToHost),
+                   cudaMemcpy(out, ctx->qst + (size_t)day0 * per_day, (size_t)ndays * per_day * sizeof(double),
+                              cudaMemcpyDeviceToHost),
                    "get_discharge");
 }
 
 wg_status wg_reset_balance(wg_ctx *ctx) {
   if (!ctx) return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
-  cudaError_t e = cudaMemsetAsync(ctx->balance.acc, 0, (size_t)10 * ctx->n * sizeof(double), ctx->stream);
-  if (e == cudaSuccess) e = launch_volume(ctx->cells, ctx->state, ctx->vol0, ctx->stream);
+  cudaError_t e = cudaSuccess;
+  if (ctx->balance.enabled)
+    e = cudaMemsetAsync(ctx->balance.acc, 0, (size_t)10 * ctx->nstate() * sizeof(double), ctx->stream);
+  if (e == cudaSuccess)
+    e = ctx->precision == 0 ? launch_volume(ctx->cd, ctx->sd, ctx->members, ctx->vol0, ctx->stream)
+                            : launch_volume(ctx->cf, ctx->sf, ctx->members, ctx->vol0, ctx->stream);
   ctx->launches++;
   return cuda_fail(ctx, e, "reset_balance");
 }
 
 wg_status wg_get_balance(wg_ctx *ctx, double out[6]) {
   if (!ctx || !out) return WG_ERR_INVALID;
+  if (!ctx->balance.enabled) return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
   int nb = 0;
-  cudaError_t e = launch_balance_sum(ctx->cells, ctx->state, ctx->balance, ctx->vol0, ctx->partial, &nb, ctx->stream);
+  cudaError_t e = ctx->precision == 0 ? launch_balance_sum(ctx->cd, ctx->sd, ctx->members, ctx->balance, ctx->vol0,
+                                                           ctx->partial, &nb, ctx->stream)
+                                      : launch_balance_sum(ctx->cf, ctx->sf, ctx->members, ctx->balance, ctx->vol0,
+                                                           ctx->partial, &nb, ctx->stream);
   ctx->launches++;
   if (e != cudaSuccess) return cuda_fail(ctx, e, "get_balance");
   std::vector<double> part((size_t)nb * 8);
@@ -725,6 +879,30 @@ wg_status wg_get_balance(wg_ctx *ctx, double out[6]) {
   }
   for (int k = 0; k < 5; ++k) out[k] = sum[k] + comp[k];
   out[5] = mx;
+  return WG_OK;
+}
+
+wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks) {
+  if (!ctx || (threads != 64 && threads != 128 && threads != 256) || blocks < 0) return WG_ERR_INVALID;
+  const bool ens = ctx->members > 1;
+  const int maxb = ctx->precision == 0 ? pipeline_max_blocks<double>(true, ens, threads)
+                                       : pipeline_max_blocks<float>(true, ens, threads);
+  const int maxr = ctx->precision == 0 ? pipeline_max_blocks<double>(false, ens, threads)
+                                       : pipeline_max_blocks<float>(false, ens, threads);
+  const int need = (int)std::min<size_t>((ctx->nstate() + threads - 1) / threads, (size_t)1 << 30);
+  if (maxb <= 0 || maxr <= 0) return WG_ERR_DEVICE;
+  ctx->threads = threads;
+  ctx->blocks_fused = std::min(blocks > 0 ? std::min(blocks, maxb) : maxb, need);
+  ctx->blocks_route = std::min(blocks > 0 ? std::min(blocks, maxr) : maxr, need);
+  return WG_OK;
+}
+
+wg_status wg_get_launch_shape(const wg_ctx *ctx, int32_t *threads, int32_t *blocks, int32_t *max_blocks) {
+  if (!ctx || !threads || !blocks || !max_blocks) return WG_ERR_INVALID;
+  *threads = ctx->threads;
+  *blocks = ctx->blocks_fused;
+  *max_blocks = ctx->precision == 0 ? pipeline_max_blocks<double>(true, ctx->members > 1, ctx->threads)
+                                    : pipeline_max_blocks<float>(true, ctx->members > 1, ctx->threads);
   return WG_OK;
 }
 

@@ -1,26 +1,31 @@
 // wg_kernels.cu -- kernels of the GB300 WaterGAP2 daily step (sm_103a).
 //
-//  k_vertical      one thread per cell: calcNewDay for one day (daily.cpp:94-1257).
+//  k_vertical      one thread per cell: calcNewDay for one day (daily.cpp:94-1257),
+//                  the reference's per-day call granularity.
 //  k_pipeline      persistent cooperative kernel: routing through the drainage
-//                  tree as a wavefront over drainage levels; with FUSED it also
-//                  runs the vertical balance and pipelines days, so that cell n
-//                  computes day d at step d + offset(n) (offset = longest path -
-//                  distance to the outlet).  Every upstream cell of n then has
-//                  offset(n)-1 and delivers day d's outflow exactly one step
-//                  earlier through a two-slot buffer; the only synchronisation
-//                  is one grid barrier per step.
-//  k_balance_sum   compensated (Neumaier) FP64 reduction of the balance terms.
+//                  tree as a wavefront over drainage levels.  With FUSED it also
+//                  runs the vertical balance and pipelines days: cell n computes
+//                  day d at step d + offset(n), offset = longest flow path -
+//                  distance of n to its outlet.  Every upstream cell of n then
+//                  has offset(n) - 1 and delivers day d's outflow exactly one step
+//                  earlier through a two-slot buffer, so one grid barrier per step
+//                  is the only synchronisation and every step keeps all cells busy.
+//                  With ENS the cells carry `members` independent states
+//                  (ensemble members), innermost in memory.
+//  k_volume / k_balance_sum   compensated (Neumaier) FP64 water-balance sums.
 //
-// The grid barrier spins with an iteration limit: on timeout it raises the
-// context's error word and every block returns (no trap, no endless wait).
+// Precision: R = double is the plain FP64 path; R = float keeps state and
+// fluxes in FP32 while confluence sums, the outflow buffer and all balance
+// sums stay FP64.  The grid barrier spins with an iteration limit: on timeout
+// it raises the context's error word and every block returns (no trap).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <algorithm>
 
 #include "wg_device.h"
-#include "wg_physics.cuh"
 #include "wg_kernels.h"
+#include "wg_physics.cuh"
 
 namespace wg {
 
@@ -69,9 +74,8 @@ __device__ __forceinline__ void neumaier_add(double *acc, size_t k_sum, size_t k
   acc[k_comp] = c;
 }
 
-__device__ __forceinline__ void record_balance(const DevBalance &b, int n, int i, double in, double evap, double up,
-                                               double out, double leak) {
-  const size_t N = (size_t)n;
+__device__ __forceinline__ void record_balance(const DevBalance &b, size_t N, size_t i, double in, double evap,
+                                               double up, double out, double leak) {
   neumaier_add(b.acc, 0 * N + i, 5 * N + i, in);
   neumaier_add(b.acc, 1 * N + i, 6 * N + i, evap);
   neumaier_add(b.acc, 2 * N + i, 7 * N + i, out);
@@ -79,98 +83,242 @@ __device__ __forceinline__ void record_balance(const DevBalance &b, int n, int i
   neumaier_add(b.acc, 4 * N + i, 9 * N + i, leak);
 }
 
-__global__ void __launch_bounds__(256) k_vertical(DevCells c, DevState s, DevVert v, DevForcing f, int doy, int fday) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.n) return;
-  const size_t fo = (size_t)fday * c.n + i;
-  const double ext = c.ext_rad[(size_t)(doy - 1) * c.nrow + c.ext_row[i]];
-  VOut o;
-  vertical_cell(c, s, i, (double)f.prec[fo], (double)f.temp[fo], (double)f.swrad[fo], ext, o);
-  v.rs[i] = o.rs; v.gwr[i] = o.gwr; v.transfer[i] = o.transfer; v.owp[i] = o.owp; v.owpet[i] = o.owpet;
-  v.land_in[i] = o.land_in; v.land_evap[i] = o.land_evap; v.land_leak[i] = o.land_leak;
+template <class R>
+__device__ __forceinline__ RState<R> load_rstate(const DevStateT<R> &s, size_t i, uint32_t fl) {
+  RState<R> r;
+  r.gw = s.gw[i];
+  r.river = s.river[i];
+  r.loclake = (fl & F_LOCLAKE) ? s.loclake[i] : R(0);
+  r.rf_loclake = (fl & F_LOCLAKE) ? s.rf_loclake[i] : R(0);
+  r.locwetl = (fl & F_LOCWETL) ? s.locwetl[i] : R(0);
+  r.rf_locwetl = (fl & F_LOCWETL) ? s.rf_locwetl[i] : R(0);
+  r.glolake = (fl & F_GLOLAKE) ? s.glolake[i] : R(0);
+  r.rf_glolake = (fl & F_GLOLAKE) ? s.rf_glolake[i] : R(0);
+  r.glowetl = (fl & F_GLOWETL) ? s.glowetl[i] : R(0);
+  r.rf_glowetl = (fl & F_GLOWETL) ? s.rf_glowetl[i] : R(0);
+  r.res = (fl & F_RES) ? s.res[i] : R(0);
+  r.rf_res = (fl & F_RES) ? s.rf_res[i] : R(0);
+  r.k_release = (fl & F_RES) ? s.k_release[i] : R(0);
+  return r;
 }
 
-template <bool FUSED>
-__global__ void __launch_bounds__(256) k_pipeline(DevCells c, DevState s, DevVert v, DevForcing f, DevBalance b,
-                                                  DevSync sync, double *outq, double *qst, int doy0, int fday0,
-                                                  int oday0, int ndays) {
+// Store only what the cell's water bodies can have changed.
+template <class R>
+__device__ __forceinline__ void store_rstate(const DevStateT<R> &s, size_t i, const RState<R> &r, uint32_t fl) {
+  s.gw[i] = r.gw;
+  s.river[i] = r.river;
+  if (fl & F_LOCLAKE) { s.loclake[i] = r.loclake; s.rf_loclake[i] = r.rf_loclake; }
+  if (fl & F_LOCWETL) { s.locwetl[i] = r.locwetl; s.rf_locwetl[i] = r.rf_locwetl; }
+  if (fl & F_GLOLAKE) { s.glolake[i] = r.glolake; s.rf_glolake[i] = r.rf_glolake; }
+  if (fl & F_GLOWETL) { s.glowetl[i] = r.glowetl; s.rf_glowetl[i] = r.rf_glowetl; }
+  if (fl & F_RES) { s.res[i] = r.res; s.rf_res[i] = r.rf_res; s.k_release[i] = r.k_release; }
+}
+
+// One cell-day of the vertical balance on state index si (slot s).
+template <class R>
+__device__ __forceinline__ void vertical_at(const DevCellsT<R> &c, const DevStateT<R> &st, size_t N, int s,
+                                            size_t si, int doy, R Pin, R gamma_soil, float Tf, float SWf,
+                                            VOut<R> &o) {
+  const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
+  const R ext = c.ext_rad[ti], inv_s0 = c.inv_s0[ti];
+  R canopy = st.canopy[si], soil = st.soil[si], gsnow = st.snow[si], psum = st.lai_precsum[si];
+  int days = st.lai_days[si], status = st.lai_status[si];
+  const R laf = st.laf[si];
+  const R prev = (st.laf_started[si] == 1) ? st.laf_prev[si] : laf;   // daily.cpp:159-169
+  vertical_cell<R>(c, s, gamma_soil, canopy, soil, gsnow, st.snow_band + si, N, days, status, psum, laf, prev, Pin,
+                   Tf, SWf, ext, inv_s0, o);
+  st.canopy[si] = canopy; st.soil[si] = soil; st.snow[si] = gsnow; st.lai_precsum[si] = psum;
+  st.lai_days[si] = days; st.lai_status[si] = status;
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_vertical(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
+                                                  int doy, int fday) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.n) return;
+  const size_t fo = (size_t)fday * c.n + s;
+  VOut<R> o;
+  vertical_at<R>(c, st, (size_t)c.n, s, (size_t)s, doy, R(f.prec[fo]), c.gamma[s], f.temp[fo], f.swrad[fo], o);
+  v.rs[s] = o.rs; v.gwr[s] = o.gwr; v.transfer[s] = o.transfer; v.owp[s] = o.owp; v.owpet[s] = o.owpet;
+  v.land_in[s] = o.land_in; v.land_evap[s] = o.land_evap; v.land_leak[s] = o.land_leak;
+}
+
+// Vertical balance ahead of routing for the cells whose land fraction and open-water
+// fluxes do not depend on routing (no water body): each thread takes one
+// (cell, member) through the days the pipeline steps [t_b, t_e) will route, with
+// the vertical state in registers, and leaves surface runoff and recharge in the
+// ring buffer.  Results equal the in-wavefront computation: the vertical balance of
+// such a cell reads nothing routing writes.
+template <class R, bool ENS>
+__global__ void __launch_bounds__(256) k_vertical_ahead(DevCellsT<R> c, DevStateT<R> st, DevForcing f,
+                                                        DevMembers mem, DevBalance b, DevRingT<R> ring, int doy0,
+                                                        int fday0, int ndays, int t_b, int t_e) {
   const int n = c.n;
-  const int nsteps = ndays + c.nlevel - 1;
-  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gstride = gridDim.x * blockDim.x;
-  for (int t = 0; t < nsteps; ++t) {
+  const int M = ENS ? mem.members : 1;
+  const size_t N = (size_t)n * M;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int s = ENS ? (int)(i / M) : (int)i;
+  const int mm = ENS ? (int)(i - (size_t)s * M) : 0;
+  if (c.flags[s] & F_VINLINE) return;
+  const int off = c.offset[s];
+  const int d0 = max(0, t_b - off), d1 = min(ndays, t_e - off);
+  if (d0 >= d1) return;
+  R canopy = st.canopy[i], soil = st.soil[i], gsnow = st.snow[i], psum = st.lai_precsum[i];
+  int days = st.lai_days[i], status = st.lai_status[i];
+  const R laf = st.laf[i];   // constant for these cells (no water body)
+  R pf = R(1), gam = c.gamma[s];
+  if (ENS) {
+    pf = R(mem.prec_factor[mm]);
+    gam *= R(mem.gamma_factor[mm]);
+  }
+  double acc_in = 0., acc_ev = 0., acc_lk = 0.;
+  const double land_f = (double)c.area_f[s] * (double)laf;
+  for (int d = d0; d < d1; ++d) {
+    const int doy = (doy0 - 1 + d) % 365 + 1;
+    const size_t fo = (size_t)(fday0 + d) * n + s;
+    const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
+    VOut<R> o;
+    vertical_cell<R>(c, s, gam, canopy, soil, gsnow, st.snow_band + i, N, days, status, psum, laf, laf,
+                     R(f.prec[fo]) * pf, f.temp[fo], f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o);
+    const size_t ri = (size_t)(d % ring.ring_days) * N + i;
+    ring.rs[ri] = o.rs;
+    ring.gwr[ri] = o.gwr;
+    if (b.enabled) {
+      acc_in += (double)o.land_in * land_f;
+      acc_ev += (double)o.land_evap * land_f;
+      acc_lk += (double)o.land_leak * land_f;
+    }
+  }
+  st.canopy[i] = canopy; st.soil[i] = soil; st.snow[i] = gsnow; st.lai_precsum[i] = psum;
+  st.lai_days[i] = days; st.lai_status[i] = status;
+  if (b.enabled) {
+    neumaier_add(b.acc, 0 * N + i, 5 * N + i, acc_in);
+    neumaier_add(b.acc, 1 * N + i, 6 * N + i, acc_ev);
+    neumaier_add(b.acc, 4 * N + i, 9 * N + i, acc_lk);
+  }
+}
+
+template <class R, bool FUSED, bool ENS>
+__global__ void __launch_bounds__(256) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
+                                                  DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
+                                                  double *outq, double *qst, int doy0, int fday0, int oday0,
+                                                  int ndays, int t_b, int t_e) {
+  const int n = c.n;
+  const int M = ENS ? mem.members : 1;
+  const size_t N = (size_t)n * M;
+  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gstride = (long long)gridDim.x * blockDim.x;
+  for (int t = t_b; t < t_e; ++t) {
     const int lo_off = max(0, t - ndays + 1), hi_off = min(c.nlevel - 1, t);
     if (lo_off <= hi_off) {
-      const int lo = c.level_start[lo_off], hi = c.level_start[hi_off + 1];
-      double *q_now = outq + (size_t)(t & 1) * n;
-      const double *q_prev = outq + (size_t)((t + 1) & 1) * n;
-      // slot i always belongs to thread i mod gstride, so a cell's state is read and
-      // written by one thread; only upstream outflows cross threads (read via L2)
-      int r0 = (gtid - lo) % gstride;
+      const long long lo = (long long)c.level_start[lo_off] * M, hi = (long long)c.level_start[hi_off + 1] * M;
+      double *q_now = outq + (size_t)(t & 1) * N;
+      const double *q_prev = outq + (size_t)((t + 1) & 1) * N;
+      // state index i always belongs to thread i mod gstride, so a cell's state is read
+      // and written by one thread; only upstream outflows cross threads (read via L2)
+      long long r0 = (gtid - lo) % gstride;
       if (r0 < 0) r0 += gstride;
-      for (int i = lo + r0; i < hi; i += gstride) {
-        const int d = t - c.offset[i];
+      for (long long i = lo + r0; i < hi; i += gstride) {
+        const int s = ENS ? (int)(i / M) : (int)i;
+        const int mm = ENS ? (int)(i - (long long)s * M) : 0;
+        const size_t si = (size_t)i;
+        const int d = t - c.offset[s];
         const int doy = (doy0 - 1 + d) % 365 + 1;
         const int month = month_of(doy);
-        VOut o;
-        if (FUSED) {
-          const size_t fo = (size_t)(fday0 + d) * n + i;
-          const double ext = c.ext_rad[(size_t)(doy - 1) * c.nrow + c.ext_row[i]];
-          vertical_cell(c, s, i, (double)f.prec[fo], (double)f.temp[fo], (double)f.swrad[fo], ext, o);
+        const uint32_t fl = c.flags[s];
+        VOut<R> o;
+        if (FUSED && !(fl & F_VINLINE)) {
+          const size_t ri = (size_t)(d % ring.ring_days) * N + si;
+          o.rs = ring.rs[ri];
+          o.gwr = ring.gwr[ri];
+          o.transfer = R(0); o.owp = R(0); o.owpet = R(0);
+          o.land_in = R(0); o.land_evap = R(0); o.land_leak = R(0);   // accounted ahead
+        } else if (FUSED) {
+          const size_t fo = (size_t)(fday0 + d) * n + s;
+          R Pin = R(f.prec[fo]);
+          R gam = c.gamma[s];
+          if (ENS) {
+            Pin *= R(mem.prec_factor[mm]);
+            gam *= R(mem.gamma_factor[mm]);
+          }
+          vertical_at<R>(c, st, N, s, si, doy, Pin, gam, f.temp[fo], f.swrad[fo], o);
         } else {
-          o.rs = v.rs[i]; o.gwr = v.gwr[i]; o.transfer = v.transfer[i]; o.owp = v.owp[i]; o.owpet = v.owpet[i];
-          o.land_in = v.land_in[i]; o.land_evap = v.land_evap[i]; o.land_leak = v.land_leak[i];
+          o.rs = v.rs[s]; o.gwr = v.gwr[s]; o.transfer = v.transfer[s]; o.owp = v.owp[s]; o.owpet = v.owpet[s];
+          o.land_in = v.land_in[s]; o.land_evap = v.land_evap[s]; o.land_leak = v.land_leak[s];
         }
-        // upstream inflow: the reference sums pushes in routing order (routing.cpp:3955-3958)
+        // upstream inflow, summed in FP64 in the reference's push order (routing.cpp:3955-3958)
         double up = 0.;
-        const int u0 = c.up_ptr[i], u1 = c.up_ptr[i + 1];
-        for (int k = u0; k < u1; ++k) up += __ldcg(q_prev + c.up_idx[k]);
-        RTerms rt;
-        const double land_f = c.area[i] * (s.laf[i] / 100.) / 1000000.;
-        const double tv = routing_cell(c, s, i, doy, month, o, up, rt);
-        q_now[i] = tv;
-        if (b.enabled)
-          record_balance(b, n, i, o.land_in * land_f + rt.p_ow, o.land_evap * land_f + rt.e_ow, up, tv,
-                         o.land_leak * land_f + rt.leak);
-        fraction_update(c, s, i);
-        const int st = c.station[i];
-        if (st >= 0) qst[(size_t)(oday0 + d) * c.nstation + st] = tv;
+        const int u0 = c.up_ptr[s], u1 = c.up_ptr[s + 1];
+        for (int k = u0; k < u1; ++k) up += __ldcg(q_prev + (size_t)c.up_idx[k] * M + mm);
+        const R laf = st.laf[si], laf_prev = st.laf_prev[si];
+        RState<R> rs = load_rstate(st, si, fl);
+        RTerms<R> rt;
+        const R tv = routing_cell<R>(c, s, rs, doy, month, laf, laf_prev, o, up, rt);
+        store_rstate(st, si, rs, fl);
+        q_now[si] = (double)tv;
+        if (b.enabled) {
+          const double land_f = (double)c.area_f[s] * (double)laf;
+          record_balance(b, N, si, (double)o.land_in * land_f + (double)rt.p_ow,
+                         (double)o.land_evap * land_f + (double)rt.e_ow, up, (double)tv,
+                         (double)o.land_leak * land_f + (double)rt.leak);
+        }
+        // land-area fraction for the next day (routing.cpp:5034-5188, 5343-5352)
+        R next = laf;
+        if (fl & (F_LOCLAKE | F_LOCWETL | F_GLOWETL)) {
+          R fswb = st.fswb_next[si];
+          next = fraction_next<R>(fl, rs, c.ll100[s], c.lw100[s], c.gw100[s], laf, fswb);
+          st.fswb_next[si] = fswb;
+          st.laf[si] = next;
+        }
+        st.laf_prev[si] = laf;
+        st.laf_started[si] = 1;
+        const int stn = c.station[s];
+        if (stn >= 0) qst[((size_t)(oday0 + d) * c.nstation + stn) * M + mm] = (double)tv;
       }
     }
-    if (t + 1 < nsteps) {
-      if (!grid_barrier(sync, (unsigned)t)) return;
+    if (t + 1 < t_e) {
+      if (!grid_barrier(sync, (unsigned)(t - t_b))) return;
     }
   }
 }
 
-// Volume of the state of slot i [km3]: land storages (mm of the land fraction they
-// were last rescaled to) plus groundwater and surface-water storages.
-__device__ __forceinline__ double cell_volume(const DevCells &c, const DevState &s, int i) {
+// Volume of the state at index i (slot s) [km3]: land storages (mm of the land
+// fraction they were last rescaled to) plus groundwater and surface-water storages.
+template <class R>
+__device__ __forceinline__ double cell_volume(const DevCellsT<R> &c, const DevStateT<R> &st, size_t N, int s,
+                                              size_t i) {
   double snow = 0.;
-  for (int e = 0; e < c.nband; ++e) snow += s.snow_band[(size_t)e * c.n + i];
+  for (int e = 0; e < c.nband; ++e) snow += (double)st.snow_band[(size_t)e * N + i];
   snow /= (double)c.nband;
-  const double laf = s.laf_started[i] ? s.laf_prev[i] : s.laf[i];
-  const double f = c.area[i] * (laf / 100.) / 1000000.;
-  return (s.canopy[i] + snow + s.soil[i]) * f + s.gw[i] + s.river[i] + s.loclake[i] + s.locwetl[i] + s.glolake[i] +
-         s.glowetl[i] + s.res[i];
+  const double laf = st.laf_started[i] ? (double)st.laf_prev[i] : (double)st.laf[i];
+  const double f = (double)c.area[s] * (laf / 100.) / 1000000.;
+  return ((double)st.canopy[i] + snow + (double)st.soil[i]) * f + (double)st.gw[i] + (double)st.river[i] +
+         (double)st.loclake[i] + (double)st.locwetl[i] + (double)st.glolake[i] + (double)st.glowetl[i] +
+         (double)st.res[i];
 }
 
-__global__ void k_volume(DevCells c, DevState s, double *vol) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < c.n) vol[i] = cell_volume(c, s, i);
+template <class R>
+__global__ void k_volume(DevCellsT<R> c, DevStateT<R> st, int M, double *vol) {
+  const size_t N = (size_t)c.n * M;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) vol[i] = cell_volume<R>(c, st, N, (int)(i / M), i);
 }
 
-// Block-level Neumaier reduction; out[blockIdx.x*8 + k] partial sums of
-//   0 storage, 1 in, 2 evap, 3 outlet out, 4 leak, 5 max relative cell residual
-__global__ void __launch_bounds__(256) k_balance_sum(DevCells c, DevState s, DevBalance b, const double *vol0,
-                                                     double *partial) {
+// Block-level Neumaier reduction; partial[blockIdx.x*8 + k] sums of
+//   0 storage, 1 in, 2 evap, 3 outflow at outlets and sinks, 4 leak,
+//   5 largest closure residual of a cell relative to its throughput.
+template <class R>
+__global__ void __launch_bounds__(256) k_balance_sum(DevCellsT<R> c, DevStateT<R> st, int M, DevBalance b,
+                                                     const double *vol0, double *partial) {
   __shared__ double sh[6][256];
-  __shared__ double shc[6][256];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ double shc[5][256];
+  const size_t N = (size_t)c.n * M;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   double val[6] = {0, 0, 0, 0, 0, 0};
-  if (i < c.n) {
-    const size_t N = (size_t)c.n;
-    const double vnow = cell_volume(c, s, i);
+  if (i < N) {
+    const int s = (int)(i / M);
+    const double vnow = cell_volume<R>(c, st, N, s, i);
     const double in = b.acc[0 * N + i] + b.acc[5 * N + i];
     const double ev = b.acc[1 * N + i] + b.acc[6 * N + i];
     const double out = b.acc[2 * N + i] + b.acc[7 * N + i];
@@ -179,16 +327,14 @@ __global__ void __launch_bounds__(256) k_balance_sum(DevCells c, DevState s, Dev
     val[0] = vnow;
     val[1] = in;
     val[2] = ev;
-    val[3] = (c.flags[i] & F_OUTLET) ? out : 0.;
+    val[3] = (c.flags[s] & F_OUTLET) ? out : 0.;
     val[4] = lk;
     const double resid = (vnow - vol0[i]) - (in - ev + up - out + lk);
     const double scale = fmax(fmax(fabs(vnow), fabs(vol0[i])), fmax(fmax(in, ev), fmax(up, out)));
     val[5] = scale > 0. ? fabs(resid) / scale : 0.;
   }
-  for (int k = 0; k < 6; ++k) {
-    sh[k][threadIdx.x] = val[k];
-    shc[k][threadIdx.x] = 0.;
-  }
+  for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = val[k];
+  for (int k = 0; k < 5; ++k) shc[k][threadIdx.x] = 0.;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) {
@@ -219,6 +365,13 @@ __global__ void k_gather_forcing(const float *__restrict__ src, float *__restric
 }
 
 // ---------------------------------------------------------------- launchers
+cudaError_t upload_fastmath_tables(const double exp2_tab[64], const double logF_tab[129], const double invF_tab[129]) {
+  cudaError_t e = cudaMemcpyToSymbol(fm::g_exp2_tab, exp2_tab, 64 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(fm::g_logF_tab, logF_tab, 129 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(fm::g_invF_tab, invF_tab, 129 * sizeof(double));
+  return e;
+}
+
 cudaError_t launch_gather_forcing(const float *src, float *dst, const int32_t *cell_of_slot, int n, int ndays,
                                   cudaStream_t st) {
   const size_t total = (size_t)n * ndays;
@@ -228,45 +381,89 @@ cudaError_t launch_gather_forcing(const float *src, float *dst, const int32_t *c
   return cudaGetLastError();
 }
 
-cudaError_t launch_vertical(const DevCells &c, const DevState &s, const DevVert &v, const DevForcing &f, int doy,
-                            int fday, cudaStream_t st) {
+template <class R>
+cudaError_t launch_vertical(const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v, const DevForcing &f,
+                            int doy, int fday, cudaStream_t st) {
   const int threads = 256, blocks = (c.n + threads - 1) / threads;
-  k_vertical<<<blocks, threads, 0, st>>>(c, s, v, f, doy, fday);
+  k_vertical<R><<<blocks, threads, 0, st>>>(c, s, v, f, doy, fday);
   return cudaGetLastError();
 }
 
-int pipeline_max_blocks(bool fused) {
+template <class R>
+cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, const DevForcing &f,
+                                  const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring, int doy0,
+                                  int fday0, int ndays, int t_b, int t_e, cudaStream_t st) {
+  const size_t N = (size_t)c.n * mem.members;
+  const int threads = 256, blocks = (int)((N + threads - 1) / threads);
+  if (mem.members > 1)
+    k_vertical_ahead<R, true><<<blocks, threads, 0, st>>>(c, s, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e);
+  else
+    k_vertical_ahead<R, false><<<blocks, threads, 0, st>>>(c, s, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e);
+  return cudaGetLastError();
+}
+
+template <class R>
+static const void *pipeline_fn(bool fused, bool ens) {
+  if (ens) return (const void *)k_pipeline<R, true, true>;
+  return fused ? (const void *)k_pipeline<R, true, false> : (const void *)k_pipeline<R, false, false>;
+}
+
+template <class R>
+int pipeline_max_blocks(bool fused, bool ens, int threads) {
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (fused) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pipeline<true>, 256, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pipeline<false>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pipeline_fn<R>(fused, ens), threads, 0);
   return per * nsm;
 }
 
-cudaError_t launch_pipeline(bool fused, const DevCells &c, const DevState &s, const DevVert &v, const DevForcing &f,
-                            const DevBalance &b, const DevSync &sync, double *outq, double *qst, int doy0, int fday0,
-                            int oday0, int ndays, int blocks, cudaStream_t st) {
+template <class R>
+cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
+                            const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
+                            const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
+                            int t_b, int t_e, int blocks, int threads, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(sync.counter, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
-  void *args[] = {(void *)&c, (void *)&s, (void *)&v, (void *)&f, (void *)&b, (void *)&sync, (void *)&outq,
-                  (void *)&qst, (void *)&doy0, (void *)&fday0, (void *)&oday0, (void *)&ndays};
-  const void *fn = fused ? (const void *)k_pipeline<true> : (const void *)k_pipeline<false>;
-  return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(256), args, 0, st);
+  void *args[] = {(void *)&c,    (void *)&s,    (void *)&v,     (void *)&f,     (void *)&mem,   (void *)&b,
+                  (void *)&ring, (void *)&sync, (void *)&outq,  (void *)&qst,   (void *)&doy0,  (void *)&fday0,
+                  (void *)&oday0, (void *)&ndays, (void *)&t_b, (void *)&t_e};
+  const bool ens = mem.members > 1;
+  return cudaLaunchCooperativeKernel(pipeline_fn<R>(fused, ens), dim3(blocks), dim3(threads), args, 0, st);
 }
 
-cudaError_t launch_volume(const DevCells &c, const DevState &s, double *vol, cudaStream_t st) {
-  const int threads = 256, blocks = (c.n + threads - 1) / threads;
-  k_volume<<<blocks, threads, 0, st>>>(c, s, vol);
+template <class R>
+cudaError_t launch_volume(const DevCellsT<R> &c, const DevStateT<R> &s, int M, double *vol, cudaStream_t st) {
+  const size_t N = (size_t)c.n * M;
+  const int threads = 256, blocks = (int)((N + threads - 1) / threads);
+  k_volume<R><<<blocks, threads, 0, st>>>(c, s, M, vol);
   return cudaGetLastError();
 }
 
-cudaError_t launch_balance_sum(const DevCells &c, const DevState &s, const DevBalance &b, const double *vol0,
-                               double *partial, int *nblocks, cudaStream_t st) {
-  const int threads = 256, blocks = (c.n + threads - 1) / threads;
+template <class R>
+cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int M, const DevBalance &b,
+                               const double *vol0, double *partial, int *nblocks, cudaStream_t st) {
+  const size_t N = (size_t)c.n * M;
+  const int threads = 256, blocks = (int)((N + threads - 1) / threads);
   *nblocks = blocks;
-  k_balance_sum<<<blocks, threads, 0, st>>>(c, s, b, vol0, partial);
+  k_balance_sum<R><<<blocks, threads, 0, st>>>(c, s, M, b, vol0, partial);
   return cudaGetLastError();
 }
+
+#define WG_INSTANTIATE(R)                                                                                          \
+  template cudaError_t launch_vertical<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,        \
+                                          const DevForcing &, int, int, cudaStream_t);                             \
+  template int pipeline_max_blocks<R>(bool, bool, int);                                                           \
+  template cudaError_t launch_pipeline<R>(bool, const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,  \
+                                          const DevForcing &, const DevMembers &, const DevBalance &,             \
+                                          const DevRingT<R> &, const DevSync &, double *, double *, int, int,     \
+                                          int, int, int, int, int, int, cudaStream_t);                            \
+  template cudaError_t launch_vertical_ahead<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevForcing &,   \
+                                                const DevMembers &, const DevBalance &, const DevRingT<R> &, int,  \
+                                                int, int, int, int, cudaStream_t);                                 \
+  template cudaError_t launch_volume<R>(const DevCellsT<R> &, const DevStateT<R> &, int, double *, cudaStream_t); \
+  template cudaError_t launch_balance_sum<R>(const DevCellsT<R> &, const DevStateT<R> &, int, const DevBalance &,  \
+                                             const double *, double *, int *, cudaStream_t);
+WG_INSTANTIATE(double)
+WG_INSTANTIATE(float)
 
 }  // namespace wg

@@ -5,13 +5,26 @@
 #include "wg_device.h"
 
 namespace wg {
-cudaError_t launch_vertical(const DevCells &c, const DevState &s, const DevVert &v, const DevForcing &f, int doy,
-                            int fday, cudaStream_t st);
-int pipeline_max_blocks(bool fused);
-cudaError_t launch_pipeline(bool fused, const DevCells &c, const DevState &s, const DevVert &v, const DevForcing &f,
-                            const DevBalance &b, const DevSync &sync, double *outq, double *qst, int doy0, int fday0,
-                            int oday0, int ndays, int blocks, cudaStream_t st);
-cudaError_t launch_volume(const DevCells &c, const DevState &s, double *vol, cudaStream_t st);
-cudaError_t launch_balance_sum(const DevCells &c, const DevState &s, const DevBalance &b, const double *vol0,
-                               double *partial, int *nblocks, cudaStream_t st);
+cudaError_t upload_fastmath_tables(const double exp2_tab[64], const double logF_tab[129], const double invF_tab[129]);
+cudaError_t launch_gather_forcing(const float *src, float *dst, const int32_t *cell_of_slot, int n, int ndays,
+                                  cudaStream_t st);
+template <class R>
+cudaError_t launch_vertical(const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v, const DevForcing &f,
+                            int doy, int fday, cudaStream_t st);
+template <class R>
+int pipeline_max_blocks(bool fused, bool ens, int threads);
+template <class R>
+cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
+                            const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
+                            const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
+                            int t_b, int t_e, int blocks, int threads, cudaStream_t st);
+template <class R>
+cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, const DevForcing &f,
+                                  const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring, int doy0,
+                                  int fday0, int ndays, int t_b, int t_e, cudaStream_t st);
+template <class R>
+cudaError_t launch_volume(const DevCellsT<R> &c, const DevStateT<R> &s, int M, double *vol, cudaStream_t st);
+template <class R>
+cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int M, const DevBalance &b,
+                               const double *vol0, double *partial, int *nblocks, cudaStream_t st);
 }  // namespace wg

@@ -7,11 +7,17 @@
 // fraction_update: the land-area-fraction update of routing.cpp:5034-5188 and
 //                updateLandAreaFrac (routing.cpp:5343-5352).
 //
-// Expression order follows the reference term by term (the library is built
-// with --fmad=false), so that results differ from the reference only where
-// CUDA's exp/pow round differently from the host libm.
+// Templated on the arithmetic type R of state and fluxes: double for the plain
+// FP64 path, float for the mixed-precision and ensemble paths (whose confluence
+// sums and balance sums stay FP64; see wg_kernels.cu).  The control flow is the
+// reference's, branch for branch.  To spend as few instructions as possible on
+// GB300's slow FP64 pipe, divisions by per-cell constants are replaced by
+// products with reciprocals prepared on the host, repeated divisors are inverted
+// once, pow(T,4) is two squarings and exp/log/pow come from wg_fastmath.cuh; each
+// of these changes a result by a few ulp at most, far inside the 1e-10 bound.
 #pragma once
 #include "wg_device.h"
+#include "wg_fastmath.cuh"
 
 namespace wg {
 
@@ -26,21 +32,38 @@ __device__ __forceinline__ int month_of(int doy) {
   return m;
 }
 
+template <class R> struct M;
+template <> struct M<double> {
+  static __device__ __forceinline__ double exp(double x) { return fm::exp(x); }
+  static __device__ __forceinline__ double pow(double x, double y) { return fm::pow(x, y); }
+  static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+  static __device__ __forceinline__ double fabs_(double x) { return fabs(x); }
+};
+template <> struct M<float> {
+  static __device__ __forceinline__ float exp(float x) { return expf(x); }
+  static __device__ __forceinline__ float pow(float x, float y) { return (x > 0.f) ? powf(x, y) : 0.f; }
+  static __device__ __forceinline__ float rcp(float x) { return 1.0f / x; }
+  static __device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
+};
+
+template <class R>
 struct VOut {
-  double rs, gwr, transfer, owp, owpet;
-  double land_in, land_evap, land_leak;
+  R rs, gwr, transfer, owp, owpet;
+  R land_in, land_evap, land_leak;
 };
 
 // laiClass::dailyLai_growing (lai.cpp:179-241)
-__device__ __forceinline__ double lai_growing(int &days, int init, int &status, bool evergreen, bool arid,
-                                              double lmin, double lmax, double &psum, double prec) {
+template <class R>
+__device__ __forceinline__ R lai_growing(int &days, int init, int &status, bool evergreen, bool arid, R lmin, R lmax,
+                                         R &psum, R prec) {
+  const R inv30 = R(1.0 / 30.0);
   if (status == 0) {
     if (days >= init) {
       days++;
       psum += prec;
-      if (psum > 40.) {
+      if (psum > R(40.)) {
         if (days >= init + 30) { days = init + 30; status = 1; }
-        return (lmin + (lmax - lmin) * (days - init) / 30.);
+        return lmin + (lmax - lmin) * R(days - init) * inv30;
       }
       days = init;
       return lmin;
@@ -52,24 +75,25 @@ __device__ __forceinline__ double lai_growing(int &days, int init, int &status, 
   if (days <= 30) {
     days--;
     if (evergreen) status = 0;
-    if (days <= 0) { days = 0; status = 0; psum = 0.; }
-    return (lmax - (lmax - lmin) * (30 - days) / 30.);
+    if (days <= 0) { days = 0; status = 0; psum = R(0); }
+    return lmax - (lmax - lmin) * R(30 - days) * inv30;
   }
-  if (arid && (prec < 0.5)) days--;
+  if (arid && (prec < R(0.5))) days--;
   else days = 30 + init;
   return lmax;
 }
 
 // laiClass::dailyLai_nogrowing (lai.cpp:243-293)
-__device__ __forceinline__ double lai_nogrowing(int &days, int init, int &status, double lmin, double lmax,
-                                                double &psum, double prec) {
+template <class R>
+__device__ __forceinline__ R lai_nogrowing(int &days, int init, int &status, R lmin, R lmax, R &psum, R prec) {
+  const R inv30 = R(1.0 / 30.0);
   if (status == 0) {
     if (days > init) {
       days++;
       psum += prec;
-      if (psum > 40.) {
+      if (psum > R(40.)) {
         if (days >= init + 30) { days = init + 30; status = 1; }
-        return (lmin + (lmax - lmin) * (days - init) / 30.);
+        return lmin + (lmax - lmin) * R(days - init) * inv30;
       }
       days = init;
       return lmin;
@@ -79,97 +103,100 @@ __device__ __forceinline__ double lai_nogrowing(int &days, int init, int &status
   }
   if (days <= 30) {
     days--;
-    if (days <= 0) { days = 0; status = 0; psum = 0.; }
-    return (lmax - (lmax - lmin) * (30 - days) / 30.);
+    if (days <= 0) { days = 0; status = 0; psum = R(0); }
+    return lmax - (lmax - lmin) * R(30 - days) * inv30;
   }
   days--;
   return lmax;
 }
 
-// dailyWaterBalanceClass::calcNewDay for slot i (daily.cpp:94-1257).
-__device__ __forceinline__ void vertical_cell(const DevCells &c, const DevState &s, int i, double P, double T,
-                                              double SW, double ext_rad, VOut &o) {
-  const int n = c.n, B = c.nband;
-  const uint32_t fl = c.flags[i];
-  const double landAreaFrac = s.laf[i];
-  const double prevLAF = (s.laf_started[i] == 1) ? s.laf_prev[i] : landAreaFrac;   // daily.cpp:159-169
-  const double cfa = c.cfa[i];
-  const bool arid = (fl & F_ARID) != 0;
-  double transfer = 0.;
+// dailyWaterBalanceClass::calcNewDay for one cell (daily.cpp:94-1257).
+//   c, s        : per-cell constants and the cell's slot
+//   gamma_soil  : runoff exponent (P_GAMRUN_C, times a member's factor in an ensemble)
+//   canopy ...  : the cell's state, read and written through references
+//   band        : the cell's snow bands, band[e * bstride]
+//   Pin         : precipitation (times a member's factor in an ensemble)
+template <class R>
+__device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R gamma_soil, R &canopy, R &soil,
+                                              R &gsnow, R *band, size_t bstride, int &days, int &status, R &psum,
+                                              R landAreaFrac, R prevLAF, R Pin, float Tf, float SWf, R ext_rad,
+                                              R inv_s0, VOut<R> &o) {
+  typedef M<R> m;
+  const int B = c.nband;
+  const R invB = c.invB;
+  const uint32_t flags = c.flags[s];
+  const bool arid = (flags & F_ARID) != 0;
+  R transfer = R(0);
+  const R cfa = c.cfa[s];
+  R dailyPrec = c.mprec[s] * Pin;                                 // daily.cpp:248
+  const R T = R(Tf);
+  const R temp2 = T + R(237.3);
+  const R inv_t2 = m::rcp(temp2);
+  const R e_s = R(0.6108) * m::exp(R(17.27) * T * inv_t2);
+  const R alpha = c.alpha[s], maxDailyPET = c.pet_mxdy[s];
+  const R a_c = arid ? R(1.35) : R(1.00), b_c = arid ? R(-0.35) : R(0.00);
 
-  double dailyPrec = c.mprec[i] * P;                           // daily.cpp:248
-  const double dailyTempC = T;
-  const double temp2 = dailyTempC + 237.3;
-  const double e_s = 0.6108 * exp(17.27 * dailyTempC / temp2);
-  const double alpha = c.alpha[i], maxDailyPET = c.pet_mxdy[i];
-  const double a_c = arid ? 1.35 : 1.00, b_c = arid ? -0.35 : 0.00;
-
-  // LAI state machine (lai.cpp:152-177)
-  int days = s.lai_days[i], status = s.lai_status[i];
-  double psum = s.lai_precsum[i];
-  double dailyLai;
-  if (dailyTempC > 8.)
-    dailyLai = lai_growing(days, c.init_days[i], status, (fl & F_EVERGREEN) != 0, arid, c.lai_min[i], c.lai_max[i],
-                           psum, dailyPrec);
+  // LAI state machine (lai.cpp:152-177); the temperature tests use the float input
+  R dailyLai;
+  if (Tf > 8.f)
+    dailyLai = lai_growing<R>(days, c.init_days[s], status, (flags & F_EVERGREEN) != 0, arid, c.lai_min[s], c.lai_max[s],
+                              psum, dailyPrec);
   else
-    dailyLai = lai_nogrowing(days, c.init_days[i], status, c.lai_min[i], c.lai_max[i], psum, dailyPrec);
-  s.lai_days[i] = days;
-  s.lai_status[i] = status;
-  s.lai_precsum[i] = psum;
+    dailyLai = lai_nogrowing<R>(days, c.init_days[s], status, c.lai_min[s], c.lai_max[s], psum, dailyPrec);
 
-  const double albedo = (s.snow[i] > 3.) ? c.albedo_snow[i] : c.albedo[i];          // daily.cpp:366-379
-  const double lat_heat = (dailyTempC > 0) ? 2.501 - 0.002361 * dailyTempC : 2.835;  // daily.cpp:382-387
-  const double solar_rad_0 = (0.25 + 0.5) * ext_rad;
-  const double conv = 0.0864 / lat_heat;
-  const double solar_rad = conv * SW;
-  double solar_fraction;                                                             // daily.cpp:430-448
-  if (ext_rad == 0.) solar_fraction = 0.;
-  else solar_fraction = solar_rad / solar_rad_0;
-  if (solar_fraction > 1.) solar_fraction = 1.;
-  const double ff = a_c * solar_fraction + b_c;
-  const double net_emissivity = -0.02 + 0.261 * exp(-0.000777 * dailyTempC * dailyTempC);
-  const double temp_K = dailyTempC + 273.2;
-  const double net_lw = (-ff * net_emissivity * 0.000000004903 * pow(temp_K, 4.)) / lat_heat;
-  const double net_sw = solar_rad * (1. - albedo);
-  const double net_rad = c.mnetrad[i] * (net_sw + net_lw);
-  const double ow_net_rad = solar_rad * (1. - 0.08) + net_lw;
-  const double inc_svp = 4098. * e_s / (temp2 * temp2);                             // daily.cpp:484-532
-  const double gamma = (0.0016286 * 101.3) / lat_heat;
-  const double dailyPET = (net_rad <= 0.) ? 0. : alpha * (inc_svp * net_rad) / (inc_svp + gamma);
-  const double owPET = (ow_net_rad <= 0.) ? 0. : alpha * (inc_svp * ow_net_rad) / (inc_svp + gamma);
+  const R albedo = (gsnow > R(3.)) ? c.albedo_snow[s] : c.albedo[s];                 // daily.cpp:366-379
+  const R lat_heat = (Tf > 0.f) ? R(2.501) - R(0.002361) * T : R(2.835);      // daily.cpp:382-387
+  const R rlh = m::rcp(lat_heat);
+  const R solar_rad = R(0.0864) * rlh * R(SWf);
+  R solar_fraction = (ext_rad == R(0)) ? R(0) : solar_rad * inv_s0;          // daily.cpp:430-448
+  if (solar_fraction > R(1.)) solar_fraction = R(1.);
+  const R ff = a_c * solar_fraction + b_c;
+  const R net_emissivity = R(-0.02) + R(0.261) * m::exp(R(-0.000777) * T * T);
+  const R tK = T + R(273.2);
+  const R tK2 = tK * tK;
+  const R net_lw = (-ff * net_emissivity * R(0.000000004903) * (tK2 * tK2)) * rlh;
+  const R net_rad = c.mnetrad[s] * (solar_rad * (R(1.) - albedo) + net_lw);
+  const R ow_net_rad = solar_rad * R(1. - 0.08) + net_lw;
+  const R inc_svp = R(4098.) * e_s * (inv_t2 * inv_t2);                     // daily.cpp:484-532
+  const R gamma = R(0.0016286 * 101.3) * rlh;
+  const R apet = alpha * inc_svp * m::rcp(inc_svp + gamma);
+  const R dailyPET = (net_rad <= R(0)) ? R(0) : apet * net_rad;
+  const R owPET = (ow_net_rad <= R(0)) ? R(0) : apet * ow_net_rad;
   o.owp = dailyPrec;
   o.owpet = owPET;
 
-  double lsc = 0., initialStorage = 0.;
-  double canopyEvapo = 0., prec_to_soil = 0., soilPET = 0., snowEvapo = 0., effPrec = 0.;
-  double immediate = 0., dailyAET = 0., runoff = 0., total = 0., gwr = 0., pot = 0.;
-  double overflow = 0., neg_land_aet = 0., cellAET = 0., gwr_route = 0., leak = 0.;
+  R lsc = R(0), initialStorage = R(0);
+  R canopyEvapo = R(0), prec_to_soil = R(0), soilPET = R(0), snowEvapo = R(0), effPrec = R(0);
+  R immediate = R(0), dailyAET = R(0), runoff = R(0), total = R(0), gwr = R(0), pot = R(0);
+  R overflow = R(0), neg_land_aet = R(0), cellAET = R(0), gwr_route = R(0), leak = R(0);
+  const bool land = landAreaFrac > R(0.);
+  // prevLAF / landAreaFrac; exactly 1 while the land fraction does not change
+  const R ratio = !land ? R(0) : (prevLAF == landAreaFrac ? R(1) : prevLAF / landAreaFrac);
 
   // interception (daily.cpp:825-895)
-  double canopy = s.canopy[i];
-  if (landAreaFrac <= 0.) {
+  if (!land) {
     transfer = canopy;
-    canopy = 0.;
+    canopy = R(0);
   } else {
-    canopy *= prevLAF / landAreaFrac;
-    if (fabs(canopy) <= WG_MIN_STOR_VOL) canopy = 0.;
+    canopy *= ratio;
+    if (m::fabs_(canopy) <= R(WG_MIN_STOR_VOL)) canopy = R(0);
     initialStorage = canopy;
-    if (dailyLai > 0.00001) {
-      const double maxcs = c.mcwh[i] * dailyLai;
-      const double deficiency = maxcs - canopy;
+    if (dailyLai > R(0.00001)) {
+      const R maxcs = c.mcwh[s] * dailyLai;
+      const R deficiency = maxcs - canopy;
       if (dailyPrec < deficiency) {
         canopy += dailyPrec;
-        prec_to_soil = 0.;
+        prec_to_soil = R(0);
       } else {
         canopy = maxcs;
         prec_to_soil = dailyPrec - deficiency;
       }
-      const double cwc = canopy;
-      canopyEvapo = dailyPET * pow((cwc / maxcs), 0.66666666);
+      const R cwc = canopy;
+      canopyEvapo = dailyPET * m::pow(cwc / maxcs, R(0.66666666));
       if (canopyEvapo > cwc) {
         canopyEvapo = cwc;
         soilPET = dailyPET - cwc;
-        canopy = 0.0;
+        canopy = R(0);
       } else {
         canopy -= canopyEvapo;
         soilPET = dailyPET - canopyEvapo;
@@ -180,119 +207,110 @@ __device__ __forceinline__ void vertical_cell(const DevCells &c, const DevState 
     }
     lsc += canopy - initialStorage;
   }
-  s.canopy[i] = canopy;
-  if (soilPET < 0.) soilPET = 0.0;
+  if (soilPET < R(0)) soilPET = R(0);
 
   // snow in elevation bands (daily.cpp:897-1062)
-  double tempElevMax = 0., snowChange = 0., gsnow = 0.;
+  R tempElevMax = R(0), snowChange = R(0), gs = R(0);
   int thresh = 0;
-  const double t_snowfz = c.t_snowfz[i], t_snowmt = c.t_snowmt[i], ddf_m = c.ddf_m[i];
+  const R t_snowfz = c.t_snowfz[s], t_snowmt = c.t_snowmt[s], ddf_m = c.ddf_m[s];
   for (int e = 0; e < B; ++e) {
-    const size_t k = (size_t)e * n + i;
-    double sb = s.snow_band[k];
-    double temp_elev = dailyTempC - c.band_dt[k];
-    if (landAreaFrac <= 0.) {
-      transfer += sb / (double)B;
-      sb = 0.;
-      gsnow = 0.;
+    R sb = band[e * bstride];
+    R temp_elev = T - c.band_dt[(size_t)e * c.n + s];
+    if (!land) {
+      transfer += sb * invB;
+      sb = R(0);
+      gs = R(0);
     } else {
-      double effBefore, melt = 0.;
-      sb = sb * prevLAF / landAreaFrac;
-      if (fabs(sb) <= WG_MIN_STOR_VOL) sb = 0.;
+      R effBefore, melt = R(0);
+      sb *= ratio;
+      if (m::fabs_(sb) <= R(WG_MIN_STOR_VOL)) sb = R(0);
       initialStorage = sb;
-      if (sb > 1000.) {
-        if (thresh == 0.) thresh = c.band_el[k];
-        else if (thresh > 0.) temp_elev = dailyTempC - ((thresh - c.elev0[i]) * c.t_gradnt[i]);
+      if (sb > R(1000.)) {
+        if (thresh == 0) thresh = c.band_el[(size_t)e * c.n + s];
+        else if (thresh > 0) temp_elev = T - (R(thresh) - c.elev0[s]) * c.t_gradnt[s];
       }
       if (temp_elev <= t_snowfz) {
-        effBefore = 0.;
+        effBefore = R(0);
         sb += prec_to_soil;
         if (sb > soilPET) {
           sb -= soilPET;
           snowEvapo += soilPET;
         } else {
           snowEvapo += sb;
-          sb = 0.;
+          sb = R(0);
         }
       } else {
         effBefore = prec_to_soil;
       }
-      if (temp_elev > t_snowmt) {
-        if (!(sb < 0.)) {
-          melt = ddf_m * (temp_elev - t_snowmt);
-          if (melt > sb) {
-            melt = sb;
-            sb = 0.;
-          } else {
-            sb -= melt;
-          }
+      if (temp_elev > t_snowmt && !(sb < R(0))) {
+        melt = ddf_m * (temp_elev - t_snowmt);
+        if (melt > sb) {
+          melt = sb;
+          sb = R(0);
+        } else {
+          sb -= melt;
         }
       }
       snowChange += sb - initialStorage;
       if (e == 0) tempElevMax = temp_elev;
-      gsnow += sb;
+      gs += sb;
       effPrec += effBefore + melt;
     }
-    s.snow_band[k] = sb;
+    band[e * bstride] = sb;
   }
-  if (landAreaFrac > 0.) {
-    gsnow /= (double)B;
-    effPrec /= (double)B;
-    snowEvapo /= (double)B;
-    snowChange /= (double)B;
+  if (land) {
+    gs *= invB;
+    effPrec *= invB;
+    snowEvapo *= invB;
+    snowChange *= invB;
     lsc += snowChange;
   }
-  s.snow[i] = gsnow;
+  gsnow = gs;
 
   // immediate runoff from built-up area (daily.cpp:1068-1071)
-  const double bu = c.built_up[i];
-  if (bu > 0.) {
-    immediate = 0.5 * effPrec * bu;
+  if (c.built_up[s] > R(0)) {
+    immediate = R(0.5) * effPrec * c.built_up[s];
     effPrec -= immediate;
   }
 
   // soil, AET, runoff, groundwater recharge (daily.cpp:1080-1239)
-  double soil = s.soil[i];
-  if (landAreaFrac <= 0.) {
+  if (!land) {
     transfer += soil;
     transfer *= cfa;
-    soil = 0.;
+    soil = R(0);
   } else {
-    const double Smax = c.smax[i];
-    soil *= prevLAF / landAreaFrac;
+    const R Smax = c.smax[s];
+    soil *= ratio;
     initialStorage = soil;
-    overflow = 0;
     if (soil > Smax) {
       overflow = soil - Smax;
       soil = Smax;
     }
     if (tempElevMax > t_snowfz) {
-      if (Smax > 0.) {
-        const double sat = soil / Smax;
-        runoff = effPrec * pow(sat, c.gamma[i]);
-        if (soilPET > (maxDailyPET - canopyEvapo) * sat) dailyAET = (maxDailyPET - canopyEvapo) * sat;
-        else dailyAET = soilPET;
+      if (Smax > R(0)) {
+        const R sat = soil * c.inv_smax[s];
+        runoff = effPrec * m::pow(sat, gamma_soil);
+        const R lim = (maxDailyPET - canopyEvapo) * sat;
+        dailyAET = (soilPET > lim) ? lim : soilPET;
         soil += effPrec - dailyAET - runoff;
-        if (fabs(soil) <= WG_MIN_STOR_VOL) soil = 0.;
-        effPrec = 0.;
-        if (soil < 0.) {
+        if (m::fabs_(soil) <= R(WG_MIN_STOR_VOL)) soil = R(0);
+        effPrec = R(0);
+        if (soil < R(0)) {
           dailyAET += soil;
-          soil = 0.;
+          soil = R(0);
         }
         runoff *= cfa;
         immediate *= cfa;
-        const double rgmax = c.rgmax[i], fg = c.fg[i];
-        if (rgmax < (fg * runoff)) gwr = rgmax;
-        else gwr = fg * runoff;
+        const R fgr = c.fg[s] * runoff;
+        gwr = (c.rgmax[s] < fgr) ? c.rgmax[s] : fgr;
         // the reference's inland-sink test here reads a grid nothing fills (globals.cpp:8),
-        // so the arid rule applies by land cover and texture alone
-        if ((fl & F_ARID_GW) && (dailyPrec <= c.pcritgwa[i])) {
+        // so the arid rule applies by aridity and texture alone
+        if ((flags & F_ARID_GW) && (dailyPrec <= c.pcritgwa[s])) {
           pot = gwr;
-          gwr = 0.;
+          gwr = R(0);
         }
         runoff -= pot;
-        pot /= cfa;
-        soil += pot;
+        soil += pot * c.inv_cfa[s];
         if (soil > Smax) {
           overflow += soil - Smax;
           soil = Smax;
@@ -304,28 +322,27 @@ __device__ __forceinline__ void vertical_cell(const DevCells &c, const DevState 
       overflow *= cfa;
       effPrec *= cfa;
       total += overflow + effPrec;
-      dailyAET = 0.;
+      dailyAET = R(0);
       leak -= cfa * immediate;   // built-up runoff is dropped in this branch
     }
     gwr_route = gwr;   // G_dailyGwRecharge (daily.cpp:1232)
     lsc += soil - initialStorage;
-    cellAET = lsc * (cfa - 1.0) - dailyPrec * (cfa - 1.0) + (dailyAET + canopyEvapo + snowEvapo) * cfa;
-    if (cellAET < 0.) {
+    cellAET = (lsc - dailyPrec) * (cfa - R(1.0)) + (dailyAET + canopyEvapo + snowEvapo) * cfa;
+    if (cellAET < R(0)) {
       neg_land_aet = cellAET;
-      cellAET = 0.;
+      cellAET = R(0);
     }
   }
   // surface runoff (daily.cpp:1244-1257)
-  if (neg_land_aet < 0.) total = total + neg_land_aet;
-  if (total < 0.) {
+  if (neg_land_aet < R(0)) total = total + neg_land_aet;
+  if (total < R(0)) {
     leak -= total;
-    total = 0.;
+    total = R(0);
   }
-  if ((total - gwr) < 0.) {
+  if ((total - gwr) < R(0)) {
     soil += total - gwr;
     gwr = total;
   }
-  s.soil[i] = soil;
   o.rs = total - gwr;
   o.gwr = gwr_route;
   o.transfer = transfer;
@@ -334,186 +351,178 @@ __device__ __forceinline__ void vertical_cell(const DevCells &c, const DevState 
   o.land_leak = leak;
 }
 
+template <class R>
 struct RTerms {
-  double p_ow, e_ow, leak;
+  R p_ow, e_ow, leak;
+};
+
+// Routing state of one cell (surface water and groundwater storages).
+template <class R>
+struct RState {
+  R gw, river, loclake, locwetl, glolake, glowetl, res;
+  R rf_loclake, rf_locwetl, rf_glolake, rf_glowetl, rf_res, k_release;
 };
 
 // getRiverVelocity / getNewRiverVelocity (routing.cpp:7274-7341)
-__device__ __forceinline__ double river_velocity(const DevCells &c, int i, double riverInflow, double S) {
-  const double bw = c.bw[i];
-  double v;
+template <class R>
+__device__ __forceinline__ R river_velocity(const DevCellsT<R> &c, int s, R riverInflow, R S) {
+  typedef M<R> m;
+  const R bw = c.bw[s];
+  R depth, csa;
   if (c.velo_opt == 1) {
-    const double Q = (riverInflow * 1000. * 1000. * 1000.) / (60. * 60. * 24.);
-    const double depth = 0.349 * pow(Q, 0.341);
-    const double csa = depth * (2.0 * depth + bw);
-    const double wp = bw + 2.0 * depth * sqrt(5.0);
-    const double hr = csa / wp;
-    v = c.inv_mr[i] * pow(hr, (2. / 3.)) * c.sqrt_slope[i];
+    const R Q = riverInflow * R(1.0e9 / 86400.);
+    depth = R(0.349) * m::pow(Q, R(0.341));
+    csa = depth * (R(2.0) * depth + bw);
   } else {
-    const double csa = (S / c.rlen[i]) * 1000000.;
-    const double depth = -bw / 4.0 + sqrt(bw * bw / 16.0 + 0.5 * csa);
-    const double wp = bw + 2.0 * depth * sqrt(5.0);
-    const double hr = csa / wp;
-    v = c.inv_mr[i] * pow(hr, (2. / 3.)) * c.sqrt_slope[i];
+    csa = (S * c.inv_len[s]) * R(1000000.);
+    depth = -bw * R(0.25) + sqrt(bw * bw * R(1.0 / 16.0) + R(0.5) * csa);
   }
-  v = v * 86.4;
-  return (v < 0.00001) ? 0.00001 : v;
+  const R wp = bw + R(2.0 * 2.23606797749979) * depth;   // 2 sqrt(5)
+  const R hr = csa / wp;
+  const R v = c.inv_mr[s] * m::pow(hr, R(2. / 3.)) * c.sqrt_slope[s] * R(86.4);
+  return (v < R(0.00001)) ? R(0.00001) : v;
 }
 
 // One cell of routingClass::routing (routing.cpp:1835-4520) given the vertical
-// outputs and the summed upstream inflow; returns transportedVolume.
-__device__ __forceinline__ double routing_cell(const DevCells &c, const DevState &s, int i, int doy, int month,
-                                               const VOut &v, double inflow_up, RTerms &rt) {
-  const uint32_t fl = c.flags[i];
-  const double cellArea = c.area[i];
-  const double cfa = c.cfa[i];
-  const double laf = s.laf[i];
-  rt.p_ow = 0.; rt.e_ow = 0.; rt.leak = 0.;
-  double dlsr;
-  if (laf <= 0.) dlsr = v.transfer * cellArea / 1000000. * s.laf_prev[i] / 100.;
-  else dlsr = v.rs * cellArea / 1000000. * laf / 100.;
+// outputs and the summed upstream inflow (FP64 for every precision); returns the
+// transported volume.
+template <class R>
+__device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R> &st, int doy, int month, R laf,
+                                          R laf_prev, const VOut<R> &v, double inflow_up, RTerms<R> &rt) {
+  typedef M<R> m;
+  const uint32_t fl = c.flags[s];
+  const R cfa = c.cfa[s];
+  rt.p_ow = R(0); rt.e_ow = R(0); rt.leak = R(0);
+  const R f_land = c.area_f[s] * laf;
+  R dlsr = (laf <= R(0)) ? v.transfer * c.area_f[s] * laf_prev : v.rs * f_land;
   // groundwater (routing.cpp:2061-2200)
-  const double gw0 = s.gw[i];
-  const double netGWin = v.gwr * cellArea * (laf / 100.) / 1000000.;
-  double gw = gw0 * c.gw_e[i] + c.gw_ik[i] * netGWin * c.gw_ome[i];
-  if (fabs(gw) <= WG_MIN_STOR_VOL) gw = 0.;
-  double gw_runoff = gw0 - gw + netGWin;
-  if (gw_runoff <= 0.) {
-    gw_runoff = 0.;
+  const R gw0 = st.gw;
+  const R netGWin = v.gwr * f_land;
+  R gw = gw0 * c.gw_e[s] + c.gw_ik[s] * netGWin * c.gw_ome[s];
+  if (m::fabs_(gw) <= R(WG_MIN_STOR_VOL)) gw = R(0);
+  R gw_runoff = gw0 - gw + netGWin;
+  if (gw_runoff <= R(0)) {
+    gw_runoff = R(0);
     gw = gw0 + netGWin;
-    if (fabs(gw) <= WG_MIN_STOR_VOL) gw = 0.;
+    if (m::fabs_(gw) <= R(WG_MIN_STOR_VOL)) gw = R(0);
   }
-  s.gw[i] = gw;
-  double inflow;
-  if (!(fl & F_SINK)) {
-    inflow = dlsr;
-    inflow += gw_runoff;
-  } else {
-    if (laf == 0.) dlsr = v.transfer * cellArea / 1000000. * s.laf_prev[i] / 100.;
-    else dlsr = v.rs * cellArea / 1000000. * laf / 100.;
-    inflow = dlsr + gw_runoff;
-  }
-  const double owp = v.owp, owpet = v.owpet;
-  double outflow = 0.;
-  const double a6 = c.a6[i];
+  st.gw = gw;
+  R inflow = dlsr + gw_runoff;
+  const R owp = v.owp, owpet = v.owpet;
+  R outflow = R(0);
+  const R a6 = c.a6[s];
 
   if (fl & F_LOCLAKE) {  // local lake (routing.cpp:2318-2490)
-    const double S0 = s.loclake[i], maxS = c.maxs_ll[i], rf = s.rf_loclake[i], p100 = c.ll100[i];
-    double evapo = ((1.0 - cfa) * owp * rf) + (cfa * (owpet * rf));
-    if (evapo < 0.) evapo = 0.;
-    const double pin = (owp * rf) * a6 * p100;
-    const double TI = inflow + pin;
-    const double PETgwr = evapo * a6 * p100;
-    double PETgwrMax = S0 + maxS + TI;
-    const double avail = PETgwrMax;
-    if (PETgwrMax < 0.) PETgwrMax = 0.;
-    double S;
+    const R S0 = st.loclake, maxS = c.maxs_ll[s], rf = st.rf_loclake;
+    R evapo = (R(1.0) - cfa) * owp * rf + cfa * owpet * rf;
+    if (evapo < R(0)) evapo = R(0);
+    const R pin = owp * rf * a6 * c.ll100[s];
+    const R TI = inflow + pin;
+    const R PETgwr = evapo * a6 * c.ll100[s];
+    R PETgwrMax = S0 + maxS + TI;
+    const R avail = PETgwrMax;
+    if (PETgwrMax < R(0)) PETgwrMax = R(0);
+    R S;
     if (PETgwr > PETgwrMax) {
-      S = (-1.) * maxS;
+      S = -maxS;
       rt.e_ow += avail;
     } else {
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
     }
     rt.p_ow += pin;
-    if (S0 > 0.) {
-      outflow = c.sw_k[i] * S0 * pow((S0 / maxS), 1.5);
-      if (S <= 0.) outflow = 0;
+    if (S0 > R(0)) {
+      outflow = c.sw_k[s] * S0 * m::pow(S0 * c.inv_maxs_ll[s], R(1.5));
+      if (S <= R(0)) outflow = R(0);
       else if (outflow > S) outflow = S;
-    } else outflow = 0.;
+    } else outflow = R(0);
     S -= outflow;
-    if (fabs(S) <= WG_MIN_STOR_VOL) S = 0.;
+    if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     if (S > maxS) {
-      outflow += (S - maxS);
+      outflow += S - maxS;
       S = maxS;
     }
     inflow = outflow;
-    double r = 1. - pow(fabs(S - maxS) / (2. * maxS), c.evx[i]);
-    if (r < 0.) r = 0.;
-    if (r > 1.) r = 1.;
-    s.loclake[i] = S;
-    s.rf_loclake[i] = r;
+    R r = R(1.) - m::pow(m::fabs_(S - maxS) * (R(0.5) * c.inv_maxs_ll[s]), c.evx[s]);
+    st.loclake = S;
+    st.rf_loclake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
   }
   if (fl & F_LOCWETL) {  // local wetland (routing.cpp:2495-2617)
-    const double S0 = s.locwetl[i], maxS = c.maxs_lw[i], rf = s.rf_locwetl[i], p100 = c.lw100[i];
-    double evapo = ((1.0 - cfa) * owp * rf) + (cfa * (owpet * rf));
-    if (evapo < 0.) evapo = 0.;
-    const double pin = (owp * rf * a6 * p100);
-    const double TI = inflow + pin;
-    const double PETgwr = evapo * a6 * p100;
-    const double PETgwrMax = S0 + TI;
-    double S;
+    const R S0 = st.locwetl, maxS = c.maxs_lw[s], rf = st.rf_locwetl;
+    R evapo = (R(1.0) - cfa) * owp * rf + cfa * owpet * rf;
+    if (evapo < R(0)) evapo = R(0);
+    const R pin = owp * rf * a6 * c.lw100[s];
+    const R TI = inflow + pin;
+    const R PETgwr = evapo * a6 * c.lw100[s];
+    const R PETgwrMax = S0 + TI;
+    R S;
     if (PETgwr > PETgwrMax) {
-      S = 0.;
+      S = R(0);
       rt.e_ow += PETgwrMax;
     } else {
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
     }
     rt.p_ow += pin;
-    if (fabs(S) <= WG_MIN_STOR_VOL) S = 0.;
-    if (S > 0.) {
-      outflow = c.sw_k[i] * S * pow((S / maxS), 2.5);
+    if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
+    if (S > R(0)) {
+      outflow = c.sw_k[s] * S * m::pow(S * c.inv_maxs_lw[s], R(2.5));
       if (outflow > S) outflow = S;
-    } else outflow = 0.;
+    } else outflow = R(0);
     S -= outflow;
     if (S > maxS) {
-      outflow += (S - maxS);
+      outflow += S - maxS;
       S = maxS;
     }
     inflow = outflow;
-    double r = 1. - pow(fabs(S - maxS) / (maxS), c.evx[i]);
-    if (r < 0.) r = 0.;
-    if (r > 1.) r = 1.;
-    s.locwetl[i] = S;
-    s.rf_locwetl[i] = r;
+    R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_maxs_lw[s], c.evx[s]);
+    st.locwetl = S;
+    st.rf_locwetl = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
   }
-  inflow += inflow_up;   // routing.cpp:2623-2624
+  inflow = R((double)inflow + inflow_up);   // routing.cpp:2623-2624
   if (fl & F_GLOLAKE) {  // global lake (routing.cpp:2630-2804)
-    const double S0 = s.glolake[i], maxS = c.maxs_gl[i], rf = s.rf_glolake[i], la6 = c.la6[i];
-    double evapo = ((1.0 - cfa) * owp) + (cfa * owpet * rf);
-    if (evapo < 0.) evapo = 0.;
-    const double pin = (owp * la6);
-    const double TI = inflow + pin;
-    const double PU = evapo * la6;
-    const double PUmax = TI + maxS + S0;
+    const R S0 = st.glolake, maxS = c.maxs_gl[s], rf = st.rf_glolake;
+    R evapo = (R(1.0) - cfa) * owp + cfa * owpet * rf;
+    if (evapo < R(0)) evapo = R(0);
+    const R pin = owp * c.la6[s];
+    const R TI = inflow + pin;
+    const R PU = evapo * c.la6[s];
+    const R PUmax = TI + maxS + S0;
     rt.p_ow += pin;
-    double S;
+    R S;
     if (PU > PUmax) {
-      S = (-1.) * maxS;
-      outflow = 0.;
+      S = -maxS;
+      outflow = R(0);
       rt.e_ow += PUmax;
     } else {
-      S = S0 * c.sw_e[i] + c.sw_ik[i] * (TI - PU) * c.sw_ome[i];
+      S = S0 * c.sw_e[s] + c.sw_ik[s] * (TI - PU) * c.sw_ome[s];
       outflow = TI + S0 - S - PU;
       if (S > maxS) {
-        outflow += (S - maxS);
+        outflow += S - maxS;
         S = maxS;
       }
-      if (outflow < 0.) {
-        outflow = 0.;
+      if (outflow < R(0)) {
+        outflow = R(0);
         S = S0 + TI - PU;
       }
       rt.e_ow += PU;
     }
-    if (fabs(S) <= WG_MIN_STOR_VOL) S = 0.;
+    if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     inflow = outflow;
-    double r = 1. - pow(fabs(S - maxS) / (2. * maxS), c.evx[i]);
-    if (r < 0.) r = 0.;
-    if (r > 1.) r = 1.;
-    s.glolake[i] = S;
-    s.rf_glolake[i] = r;
+    R r = R(1.) - m::pow(m::fabs_(S - maxS) * (R(0.5) * c.inv_maxs_gl[s]), c.evx[s]);
+    st.glolake = S;
+    st.rf_glolake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
   }
   if (fl & F_RES) {  // reservoir (routing.cpp:2807-3082)
-    const double S0 = s.res[i], maxS = c.rcap[i], rf = s.rf_res[i], ra6 = c.ra6[i];
-    double evapo = ((1.0 - cfa) * owp) + (cfa * (owpet * rf));
-    if (evapo < 0.) evapo = 0.;
-    const double pin = (owp * ra6);
-    const double TI = inflow + pin;
-    const double PETgwr = evapo * ra6;
-    const double PETgwrMax = S0 + TI;
+    const R S0 = st.res, maxS = c.rcap[s], rf = st.rf_res;
+    R evapo = (R(1.0) - cfa) * owp + cfa * owpet * rf;
+    if (evapo < R(0)) evapo = R(0);
+    const R pin = owp * c.ra6[s];
+    const R TI = inflow + pin;
+    const R PETgwr = evapo * c.ra6[s];
+    const R PETgwrMax = S0 + TI;
     rt.p_ow += pin;
-    double S;
+    R S;
     if (PETgwr > PETgwrMax) {
       S = S0 + TI - PETgwrMax;
       rt.e_ow += PETgwrMax;
@@ -521,109 +530,97 @@ __device__ __forceinline__ double routing_cell(const DevCells &c, const DevState
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
     }
-    if (fabs(S) <= WG_MIN_STOR_VOL) S = 0.;
-    double K = s.k_release[i];
-    if (month == c.start_month[i] - 1 && doy == c_first_day_in_month[month]) {
-      if (S < c.rcap01[i]) K = 0.1;
-      else K = S / c.rcap085[i];
-      s.k_release[i] = K;
+    if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
+    R K = st.k_release;
+    if (month == c.start_month[s] - 1 && doy == c_first_day_in_month[month]) {
+      K = (S < c.rcap01[s]) ? R(0.1) : S * c.inv_rcap085[s];
+      st.k_release = K;
     }
-    const double prov_rel = c.prov_rel[i];
-    double release;
-    if (c.c_ratio[i] >= 0.5) release = K * prov_rel;
-    else release = (c.c4[i] * K * prov_rel) + (c.one_m_c4[i] * inflow * 1000000000. / (24. * 3600.));
-    if (S >= c.rcap01[i]) outflow = release * (24. * 3600.) / 1000000000.;
-    else outflow = 0.1 * release * (24. * 3600.) / 1000000000.;
-    if (outflow < 0.) outflow = 0.;
+    R release;
+    if (c.c_ratio[s] >= R(0.5)) release = K * c.prov_rel[s];
+    else release = c.c4[s] * K * c.prov_rel[s] + c.one_m_c4[s] * inflow * R(1.0e9 / 86400.);
+    outflow = ((S >= c.rcap01[s]) ? release : R(0.1) * release) * R(86400. / 1.0e9);
+    if (outflow < R(0)) outflow = R(0);
     S -= outflow;
     if (S > maxS) {
-      outflow += (S - maxS);
+      outflow += S - maxS;
       S = maxS;
     }
-    if (S < 0.) {
+    if (S < R(0)) {
       outflow += S;
-      S = 0.;
+      S = R(0);
     }
     inflow = outflow;
-    double r = 1. - pow(fabs(S - maxS) / maxS, 2.81383);
-    if (r < 0.) r = 0.;
-    if (r > 1.) r = 1.;
-    s.res[i] = S;
-    s.rf_res[i] = r;
+    R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_rcap[s], R(2.81383));
+    st.res = S;
+    st.rf_res = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
   }
   if (fl & F_GLOWETL) {  // global wetland (routing.cpp:3178-3297)
-    const double S0 = s.glowetl[i], maxS = c.maxs_gw[i], rf = s.rf_glowetl[i], p100 = c.gw100[i];
-    double evapo = ((1.0 - cfa) * (owp * rf)) + (cfa * (owpet * rf));
-    if (evapo < 0.) evapo = 0.;
-    const double pin = (owp * rf * a6 * p100);
-    const double TI = inflow + pin;
-    const double PETgwr = evapo * a6 * p100;
-    const double PETgwrMax = TI + S0;
+    const R S0 = st.glowetl, maxS = c.maxs_gw[s], rf = st.rf_glowetl;
+    R evapo = (R(1.0) - cfa) * owp * rf + cfa * owpet * rf;
+    if (evapo < R(0)) evapo = R(0);
+    const R pin = owp * rf * a6 * c.gw100[s];
+    const R TI = inflow + pin;
+    const R PETgwr = evapo * a6 * c.gw100[s];
+    const R PETgwrMax = TI + S0;
     rt.p_ow += pin;
-    double S;
+    R S;
     if (PETgwr > PETgwrMax) {
-      S = 0.;
-      outflow = 0.;
+      S = R(0);
+      outflow = R(0);
       rt.e_ow += PETgwrMax;
     } else {
-      S = S0 * c.sw_e[i] + c.sw_ik[i] * (TI - PETgwr) * c.sw_ome[i];
+      S = S0 * c.sw_e[s] + c.sw_ik[s] * (TI - PETgwr) * c.sw_ome[s];
       outflow = TI + S0 - S - PETgwr;
       rt.e_ow += PETgwr;
     }
     if (S > maxS) {
-      outflow += (S - maxS);
+      outflow += S - maxS;
       S = maxS;
     }
-    if (fabs(S) <= WG_MIN_STOR_VOL) S = 0.;
+    if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     inflow = outflow;
-    double r = 1. - pow(fabs(S - maxS) / maxS, c.evx[i]);
-    if (r < 0.) r = 0.;
-    if (r > 1.) r = 1.;
-    s.glowetl[i] = S;
-    s.rf_glowetl[i] = r;
+    R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_maxs_gw[s], c.evx[s]);
+    st.glowetl = S;
+    st.rf_glowetl = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
   }
   // river (routing.cpp:3385-3514)
-  const double S0 = s.river[i];
-  double velocity;
-  if (c.velo_opt == 0) velocity = c.default_velocity;
-  else velocity = river_velocity(c, i, inflow, S0);
-  const double K = velocity / c.rlen[i];
-  const double eK = exp(-1. * K);
-  const double maxUse = inflow + (K * S0 * eK) / (1. - eK);
-  double S, transported;
-  if (0. > maxUse) {
-    S = 0.;
+  const R S0 = st.river;
+  const R velocity = (c.velo_opt == 0) ? c.default_velocity : river_velocity<R>(c, s, inflow, S0);
+  const R K = velocity * c.inv_len[s];
+  const R eK = m::exp(-K);
+  const R omeK = R(1.) - eK;
+  R S, transported;
+  if (inflow * omeK + K * S0 * eK < R(0)) {   // sign of RivEvapoRemUseMax (routing.cpp:3444-3449)
+    const R maxUse = inflow + K * S0 * eK / omeK;
+    S = R(0);
     transported = inflow + S0 - maxUse;
   } else {
-    S = S0 * eK + (1. / K) * (inflow - 0.) * (1. - eK);
-    if (fabs(S) <= WG_MIN_STOR_VOL) S = 0.;
-    transported = inflow + S0 - S - 0.;
+    S = S0 * eK + inflow * omeK / K;
+    if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
+    transported = inflow + S0 - S;
   }
-  if (transported < 0.) {
+  if (transported < R(0)) {
     rt.leak -= transported;
-    transported = 0.;
+    transported = R(0);
   }
-  s.river[i] = S;
+  st.river = S;
   return transported;
 }
 
-// Land-area fraction for the next day (routing.cpp:5034-5188, 5343-5352).
-__device__ __forceinline__ void fraction_update(const DevCells &c, const DevState &s, int i) {
-  const uint32_t fl = c.flags[i];
-  double fLocLake = 0., fLocWet = 0., fGloWet = 0.;
-  if ((fl & F_LOCLAKE) && (s.rf_loclake[i] > 0.)) fLocLake = (s.rf_loclake[i] * c.ll[i] / 100.);
-  if ((fl & F_LOCWETL) && (s.rf_locwetl[i] > 0.)) fLocWet = (s.rf_locwetl[i] * c.lw[i] / 100.);
-  if ((fl & F_GLOWETL) && (s.rf_glowetl[i] > 0.)) fGloWet = (s.rf_glowetl[i] * c.gwet[i] / 100.);
-  const double fswb = s.fswb_next[i];
-  const double next = fLocLake + fLocWet + fGloWet;
-  s.fswb_next[i] = next;
-  const double changePct = next * 100. - fswb * 100.0;
-  const double laf = s.laf[i];
-  double lafNext = laf - (changePct + (0. * 100.));
-  if (lafNext < 0.) lafNext = 0.;
-  s.laf_started[i] = 1;
-  s.laf_prev[i] = laf;
-  s.laf[i] = lafNext;
+// Land-area fraction for the next day (routing.cpp:5034-5188, 5343-5352); returns
+// the new land fraction and updates fswb_next.
+template <class R>
+__device__ __forceinline__ R fraction_next(uint32_t fl, const RState<R> &s, R ll100, R lw100, R gw100, R laf,
+                                           R &fswb_next) {
+  R f = R(0);
+  if ((fl & F_LOCLAKE) && s.rf_loclake > R(0)) f += s.rf_loclake * ll100;
+  if ((fl & F_LOCWETL) && s.rf_locwetl > R(0)) f += s.rf_locwetl * lw100;
+  if ((fl & F_GLOWETL) && s.rf_glowetl > R(0)) f += s.rf_glowetl * gw100;
+  const R changePct = (f - fswb_next) * R(100.);
+  fswb_next = f;
+  const R next = laf - changePct;
+  return next < R(0) ? R(0) : next;
 }
 
 }  // namespace wg

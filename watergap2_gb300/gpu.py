@@ -24,10 +24,11 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported option", 3: "CUDA erro
           5: "invalid drainage topology", 6: "device wait exceeded its limit", 7: "no usable device"}
 
 # exported entry points of include/wg_gpu.h
-SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_upload_forcing", "wg_step_vertical",
-           "wg_step_routing", "wg_run_days", "wg_get_discharge", "wg_get_balance", "wg_reset_balance",
-           "wg_synchronize", "wg_num_levels", "wg_launch_count", "wg_last_error", "wg_status_string",
-           "wg_measure_fp64_peak")
+SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_member_state",
+           "wg_get_member_state", "wg_upload_forcing", "wg_step_vertical", "wg_step_routing", "wg_run_days",
+           "wg_get_discharge", "wg_get_balance", "wg_reset_balance", "wg_synchronize", "wg_launch_shape",
+           "wg_get_launch_shape", "wg_num_levels", "wg_launch_count", "wg_last_error", "wg_status_string",
+           "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps")
 
 
 class WgError(RuntimeError):
@@ -46,7 +47,10 @@ class _StateView(ctypes.Structure):
 
 class _Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("max_days", ctypes.c_int32), ("nstation", ctypes.c_int32),
-                ("record_balance", ctypes.c_int32), ("stations", ctypes.c_void_p), ("stream", ctypes.c_uint64)]
+                ("record_balance", ctypes.c_int32), ("stations", ctypes.c_void_p), ("stream", ctypes.c_uint64),
+                ("precision", ctypes.c_int32), ("members", ctypes.c_int32), ("member_prec_factor", ctypes.c_void_p),
+                ("member_gamma_factor", ctypes.c_void_p), ("block_threads", ctypes.c_int32),
+                ("ring_days", ctypes.c_int32)]
 
 
 _lib = None
@@ -65,10 +69,18 @@ def load_library(path: str = LIB_PATH):
     lib.wg_destroy.argtypes = [vp]
     lib.wg_set_state.argtypes = [vp, ctypes.POINTER(_StateView)]
     lib.wg_get_state.argtypes = [vp, ctypes.POINTER(_StateView)]
+    lib.wg_set_member_state.argtypes = [vp, i32, ctypes.POINTER(_StateView)]
+    lib.wg_get_member_state.argtypes = [vp, i32, ctypes.POINTER(_StateView)]
+    lib.wg_launch_shape.argtypes = [vp, i32, i32]
+    lib.wg_get_launch_shape.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]
     lib.wg_upload_forcing.argtypes = [vp, i32, i32, vp, vp, vp]
     lib.wg_step_vertical.argtypes = [vp, i32, i32]
     lib.wg_step_routing.argtypes = [vp, i32, i32]
     lib.wg_run_days.argtypes = [vp, i32, i32, i32]
+    lib.wg_run_steps.argtypes = [vp, i32, i32, i32, i32, i32]
+    lib.wg_run_steps.restype = ctypes.c_int
+    lib.wg_run_num_steps.argtypes = [vp, i32]
+    lib.wg_run_num_steps.restype = i32
     lib.wg_get_discharge.argtypes = [vp, i32, i32, vp]
     lib.wg_get_balance.argtypes = [vp, vp]
     lib.wg_reset_balance.argtypes = [vp]
@@ -83,9 +95,10 @@ def load_library(path: str = LIB_PATH):
     lib.wg_measure_fp64_peak.restype = ctypes.c_int
     lib.wg_status_string.argtypes = [ctypes.c_int]
     lib.wg_status_string.restype = ctypes.c_char_p
-    for name in ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_upload_forcing", "wg_step_vertical",
-                 "wg_step_routing", "wg_run_days", "wg_get_discharge", "wg_get_balance", "wg_reset_balance",
-                 "wg_synchronize"):
+    for name in ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_member_state",
+                 "wg_get_member_state", "wg_upload_forcing", "wg_step_vertical", "wg_step_routing", "wg_run_days",
+                 "wg_get_discharge", "wg_get_balance", "wg_reset_balance", "wg_synchronize", "wg_launch_shape",
+                 "wg_get_launch_shape"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -109,7 +122,8 @@ class Model:
     """One region resident on one GPU."""
 
     def __init__(self, region: Region, max_days: int = 366, stations=None, record_balance: bool = False,
-                 device: int = 0, stream: int = 0):
+                 device: int = 0, stream: int = 0, precision: str = "fp64", members: int = 1,
+                 prec_factor=None, gamma_factor=None, block_threads: int = 0, ring_days: int = 0):
         self.lib = load_library()
         self.region = region
         self._keep = []
@@ -127,6 +141,16 @@ class Model:
         o.record_balance = int(bool(record_balance))
         o.stations = self.stations.ctypes.data
         o.stream = int(stream)
+        o.precision = {"fp64": 0, "fp32": 1}[precision]
+        o.members = int(members)
+        self.members = int(members)
+        self.precision = precision
+        self._pf = None if prec_factor is None else np.ascontiguousarray(prec_factor, np.float32)
+        self._gf = None if gamma_factor is None else np.ascontiguousarray(gamma_factor, np.float32)
+        o.member_prec_factor = self._pf.ctypes.data if self._pf is not None else None
+        o.member_gamma_factor = self._gf.ctypes.data if self._gf is not None else None
+        o.block_threads = int(block_threads)
+        o.ring_days = int(ring_days)
         self.max_days = int(max_days)
         h = ctypes.c_void_p()
         self._check(self.lib.wg_create(ctypes.byref(r), ctypes.byref(o), ctypes.byref(h)), "wg_create", None)
@@ -172,11 +196,20 @@ class Model:
     def run_days(self, doy0: int, fday0: int, ndays: int):
         self._check(self.lib.wg_run_days(self.h, int(doy0), int(fday0), int(ndays)), "run_days")
 
+    def run_steps(self, doy0: int, fday0: int, ndays: int, t_begin: int, t_end: int):
+        self._check(self.lib.wg_run_steps(self.h, int(doy0), int(fday0), int(ndays), int(t_begin), int(t_end)),
+                    "run_steps")
+
+    def num_steps(self, ndays: int) -> int:
+        return int(self.lib.wg_run_num_steps(self.h, int(ndays)))
+
     def synchronize(self):
         self._check(self.lib.wg_synchronize(self.h), "synchronize")
 
     def discharge(self, day0: int, ndays: int) -> np.ndarray:
-        out = np.zeros((ndays, self.stations.size))
+        """[ndays, nstation] (single member) or [ndays, nstation, members]."""
+        shape = (ndays, self.stations.size) if self.members == 1 else (ndays, self.stations.size, self.members)
+        out = np.zeros(shape)
         self._check(self.lib.wg_get_discharge(self.h, int(day0), int(ndays), _ptr(out)), "get_discharge")
         return out
 
@@ -194,22 +227,31 @@ class Model:
     def reset_balance(self):
         self._check(self.lib.wg_reset_balance(self.h), "reset_balance")
 
-    def get_state(self) -> dict:
+    def get_state(self, member: int = 0) -> dict:
         st = empty_state(self.region.ncell, self.region.nband)
         v = _StateView()
         for k, a in st.items():
             setattr(v, k, a.ctypes.data)
-        self._check(self.lib.wg_get_state(self.h, ctypes.byref(v)), "get_state")
+        self._check(self.lib.wg_get_member_state(self.h, int(member), ctypes.byref(v)), "get_state")
         return st
 
-    def set_state(self, st: dict):
+    def set_state(self, st: dict, member: int = 0):
         v = _StateView()
         keep = []
         for name, dt, _ in STATE_FIELDS:
             a = np.ascontiguousarray(st[name], dt)
             keep.append(a)
             setattr(v, name, a.ctypes.data)
-        self._check(self.lib.wg_set_state(self.h, ctypes.byref(v)), "set_state")
+        self._check(self.lib.wg_set_member_state(self.h, int(member), ctypes.byref(v)), "set_state")
+
+    def launch_shape(self, threads: int | None = None, blocks: int | None = None):
+        """Set (threads, blocks) of the persistent kernels if given; return (threads, blocks, max_blocks)."""
+        if threads is not None:
+            self._check(self.lib.wg_launch_shape(self.h, int(threads), int(blocks or 0)), "launch_shape")
+        t, b, mb = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self._check(self.lib.wg_get_launch_shape(self.h, ctypes.byref(t), ctypes.byref(b), ctypes.byref(mb)),
+                    "get_launch_shape")
+        return t.value, b.value, mb.value
 
     def run(self, doy0: int, P, T, S, per_day: bool = False, chunk: int | None = None):
         """Convenience: upload forcing and simulate len(P) days from day-of-year doy0;
