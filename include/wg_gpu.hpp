@@ -1,0 +1,120 @@
+// wg_gpu.hpp -- C++ host side above the C ABI (include/wg_gpu.h).
+//
+// wg::Context owns one wg_ctx (RAII, exceptions instead of status codes).
+// wg::DailyWaterBalanceGpu and wg::RoutingGpu are drop-in stand-ins for the
+// reference's singletons `dailyWaterBalance` and `routing` inside
+// integrate_wghm_ (source/integrateWGHM.cpp:755-799): the same method names and
+// argument meaning as
+//   dailyWaterBalanceClass::calcNewDay(day, month, day_in_month, last_day_in_month,
+//                                      year, n, wghmState, additionalOutIn,
+//                                      snow_in_elevation, readinstatus, calParam)
+//                                      (source/daily.h:24)
+//   routingClass::routing(year, day, month, day_in_month, last_day_in_month,
+//                         wghmState, additionalOutIn, readinstatus, calParam)
+//                         (source/routing.h:44-45)
+//   routingClass::updateLandAreaFrac(additionalOutIn)  (source/routing.h:46)
+// The reference calls calcNewDay once per cell from an OpenMP loop; here the
+// first call of a day runs the whole grid and the other calls of that day
+// return at once, so the loop can stay as it is.  The state-file arguments are
+// accepted as templates (the reference's types) and not touched: the GPU keeps
+// the state, and Context::state() copies it out when the caller writes files.
+#ifndef WG_GPU_HPP
+#define WG_GPU_HPP
+
+#include <atomic>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "wg_gpu.h"
+
+namespace wg {
+
+class Error : public std::runtime_error {
+ public:
+  Error(wg_status s, const std::string &what) : std::runtime_error(what), status(s) {}
+  wg_status status;
+};
+
+class Context {
+ public:
+  Context(const wg_region &region, const wg_options &opt) {
+    check(wg_create(&region, &opt, &ctx_), "wg_create");
+  }
+  ~Context() {
+    if (ctx_) wg_destroy(ctx_);
+  }
+  Context(const Context &) = delete;
+  Context &operator=(const Context &) = delete;
+
+  wg_ctx *get() const { return ctx_; }
+  int levels() const { return wg_num_levels(ctx_); }
+
+  void upload_forcing(int day0, int ndays, const float *prec, const float *temp, const float *swrad) {
+    check(wg_upload_forcing(ctx_, day0, ndays, prec, temp, swrad), "wg_upload_forcing");
+  }
+  void step_vertical(int doy, int fday) { check(wg_step_vertical(ctx_, doy, fday), "wg_step_vertical"); }
+  void step_routing(int doy, int oday) { check(wg_step_routing(ctx_, doy, oday), "wg_step_routing"); }
+  void run_days(int doy0, int fday0, int ndays) { check(wg_run_days(ctx_, doy0, fday0, ndays), "wg_run_days"); }
+  void synchronize() { check(wg_synchronize(ctx_), "wg_synchronize"); }
+  void state(wg_state_view &out) { check(wg_get_state(ctx_, &out), "wg_get_state"); }
+  void set_state(const wg_state_view &in) { check(wg_set_state(ctx_, &in), "wg_set_state"); }
+  void discharge(int day0, int ndays, double *out) {
+    check(wg_get_discharge(ctx_, day0, ndays, out), "wg_get_discharge");
+  }
+
+  void check(wg_status s, const char *what) const {
+    if (s != WG_OK)
+      throw Error(s, std::string(what) + ": " + wg_status_string(s) + (ctx_ ? std::string(" ") + wg_last_error(ctx_) : ""));
+  }
+
+ private:
+  wg_ctx *ctx_ = nullptr;
+};
+
+// Stand-in for dailyWaterBalanceClass in the day loop.  The caller uploads the
+// day's forcing (Context::upload_forcing, slot fday) before the cell loop.
+class DailyWaterBalanceGpu {
+ public:
+  explicit DailyWaterBalanceGpu(Context &c) : ctx_(c) {}
+  void set_forcing_slot(int fday) { fday_ = fday; }
+
+  template <class WghmStateFile, class AdditionalOutputInputFile, class SnowInElevationFile, class CalibParam>
+  void calcNewDay(const short day, const short /*month*/, const short /*day_in_month*/,
+                  const short /*last_day_in_month*/, const short /*year*/, const int /*n*/, WghmStateFile &,
+                  AdditionalOutputInputFile &, SnowInElevationFile &, const short /*readinstatus*/, CalibParam &) {
+    // whole grid on the first call of the day; the remaining calls are no-ops
+    int prev = last_day_.load();
+    if (prev != day && last_day_.compare_exchange_strong(prev, day)) ctx_.step_vertical(day, fday_);
+  }
+
+ private:
+  Context &ctx_;
+  int fday_ = 0;
+  std::atomic<int> last_day_{-1};
+};
+
+// Stand-in for routingClass in the day loop.
+class RoutingGpu {
+ public:
+  explicit RoutingGpu(Context &c) : ctx_(c) {}
+  void set_output_slot(int oday) { oday_ = oday; }
+
+  template <class WghmStateFile, class AdditionalOutputInputFile, class CalibParam>
+  void routing(const short /*year*/, short day, short /*month*/, const short /*day_in_month*/,
+               const short /*last_day_in_month*/, WghmStateFile &, AdditionalOutputInputFile &,
+               const short /*readinstatus*/, CalibParam &) {
+    ctx_.step_routing(day, oday_);
+  }
+  // the land-area-fraction update is part of step_routing (routing.cpp:5034-5188)
+  template <class AdditionalOutputInputFile>
+  void updateLandAreaFrac(AdditionalOutputInputFile &) {}
+
+ private:
+  Context &ctx_;
+  int oday_ = 0;
+};
+
+}  // namespace wg
+
+#endif

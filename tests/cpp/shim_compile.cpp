@@ -1,0 +1,25 @@
+// Compiles the C++ host side (include/wg_gpu.hpp) against the C ABI and links
+// libwg_gpu.so; runs only calls that need no GPU.
+#include <cstdio>
+#include <cstring>
+
+#include "wg_gpu.hpp"
+
+struct FakeStateFile {};
+struct FakeCalib {};
+
+int main() {
+  // status strings and argument checks work without a device
+  if (std::strcmp(wg_status_string(WG_OK), "ok") != 0) return 1;
+  if (wg_create(nullptr, nullptr, nullptr) != WG_ERR_INVALID) return 2;
+  wg_region r{};
+  wg_options o{};
+  try {
+    wg::Context c(r, o);   // ncell = 0 -> WG_ERR_INVALID before any device call
+    return 3;
+  } catch (const wg::Error &e) {
+    if (e.status != WG_ERR_INVALID) return 4;
+  }
+  std::printf("ok\n");
+  return 0;
+}
