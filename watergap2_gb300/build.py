@@ -54,7 +54,22 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode:
         raise RuntimeError(f"link failed:\n{r.stdout}")
+    build_synth()
     return LIB
+
+
+SYNTH_LIB = os.path.join(OUT, "libwg_synth.so")
+
+
+def build_synth() -> str:
+    """Host-only generator helpers (no CUDA): priority-flood + D8 for large grids."""
+    os.makedirs(OUT, exist_ok=True)
+    cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+           os.path.join(CSRC, "wg_synth.cpp"), "-o", SYNTH_LIB]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode:
+        raise RuntimeError(f"g++ failed:\n{r.stdout}")
+    return SYNTH_LIB
 
 
 if __name__ == "__main__":

@@ -360,6 +360,41 @@ wg_status copy_state(wg_ctx *ctx, const DevStateT<R> &s, const wg_state_view *v,
   return cuda_fail(ctx, e, to_device ? "set_state" : "get_state");
 }
 
+// The same host state (cell order) into every member, one copy per field.
+template <class R>
+wg_status broadcast_state(wg_ctx *ctx, const DevStateT<R> &s, const wg_state_view *v) {
+  const int n = ctx->n, B = ctx->nband, M = ctx->members;
+  const size_t N = ctx->nstate();
+  const auto &c2s = ctx->topo.cell_of_slot;
+  cudaError_t e = cudaSuccess;
+  std::vector<R> tmp(N);
+  std::vector<int32_t> itmp(N);
+  auto dbl = [&](const double *host, R *dev) {
+    if (e != cudaSuccess) return;
+    for (int q = 0; q < n; ++q)
+      for (int m = 0; m < M; ++m) tmp[(size_t)q * M + m] = (R)host[c2s[q]];
+    e = cudaMemcpy(dev, tmp.data(), N * sizeof(R), cudaMemcpyHostToDevice);
+  };
+  auto i32 = [&](const int32_t *host, int32_t *dev) {
+    if (e != cudaSuccess) return;
+    for (int q = 0; q < n; ++q)
+      for (int m = 0; m < M; ++m) itmp[(size_t)q * M + m] = host[c2s[q]];
+    e = cudaMemcpy(dev, itmp.data(), N * sizeof(int32_t), cudaMemcpyHostToDevice);
+  };
+#define X(f) dbl(v->f, s.f);
+  WG_STATE_R(X)
+#undef X
+#define X(f) i32(v->f, s.f);
+  WG_STATE_I(X)
+#undef X
+  for (int b = 0; b < B && e == cudaSuccess; ++b) {
+    for (int q = 0; q < n; ++q)
+      for (int m = 0; m < M; ++m) tmp[(size_t)q * M + m] = (R)v->snow_band[(size_t)c2s[q] * B + b];
+    e = cudaMemcpy(s.snow_band + (size_t)b * N, tmp.data(), N * sizeof(R), cudaMemcpyHostToDevice);
+  }
+  return cuda_fail(ctx, e, "initial state");
+}
+
 wg_status state_io(wg_ctx *ctx, const wg_state_view *v, int member, bool to_device) {
   if (member < 0 || member >= ctx->members) return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
@@ -670,10 +705,8 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   init.rf_loclake = ones.data(); init.rf_locwetl = ones.data(); init.rf_glolake = ones.data();
   init.rf_glowetl = ones.data(); init.rf_res = rfres.data(); init.k_release = kr.data();
   init.laf = laf.data(); init.laf_prev = zeros.data(); init.fswb_next = fswb.data(); init.laf_started = izero.data();
-  for (int m = 0; m < ctx->members; ++m) {
-    st = state_io(ctx.get(), &init, m, true);
-    if (st != WG_OK) return st;
-  }
+  st = ctx->precision == 0 ? broadcast_state(ctx.get(), ctx->sd, &init) : broadcast_state(ctx.get(), ctx->sf, &init);
+  if (st != WG_OK) return st;
   const bool ens = ctx->members > 1;
   const int th = ctx->threads;
   const int need = (int)std::min<size_t>((N + th - 1) / th, (size_t)1 << 30);

@@ -36,17 +36,20 @@ LDD_STEP = {1: (1, -1), 2: (1, 0), 3: (1, 1), 4: (0, -1), 6: (0, 1), 7: (-1, -1)
 STEP_LDD = {v: k for k, v in LDD_STEP.items()}
 
 
-def cell_area_km2(row: np.ndarray) -> np.ndarray:
-    """Area of a 0.5-degree cell in grid row ``row`` (1-based, north to south), float32."""
-    lat_n = np.radians(90.0 - (row - 1) * 0.5)
-    lat_s = np.radians(90.0 - row * 0.5)
-    a = EARTH_R_KM ** 2 * np.radians(0.5) * (np.sin(lat_n) - np.sin(lat_s))
+def cell_area_km2(row: np.ndarray, res: float = 0.5) -> np.ndarray:
+    """Area of a res-degree cell in grid row ``row`` (1-based, north to south), float32."""
+    lat_n = np.radians(90.0 - (row - 1) * res)
+    lat_s = np.radians(90.0 - row * res)
+    a = EARTH_R_KM ** 2 * np.radians(res) * (np.sin(lat_n) - np.sin(lat_s))
     return np.abs(a).astype(np.float32)
 
 
-def row_latitude(row: np.ndarray) -> np.ndarray:
-    """Latitude used by calc_ext_rad: -(G_row/2 - 90.25) (source/daily.cpp:2423)."""
-    return -(row.astype(np.float64) / 2.0 - 90.25)
+def row_latitude(row: np.ndarray, res: float = 0.5) -> np.ndarray:
+    """Cell-centre latitude; for 0.5 degrees the reference's -(G_row/2 - 90.25)
+    (source/daily.cpp:2423), which only exists for that grid."""
+    if res == 0.5:
+        return -(row.astype(np.float64) / 2.0 - 90.25)
+    return 90.0 - (row.astype(np.float64) - 0.5) * res
 
 
 def fractal_field(shape, beta: float, rng: np.random.Generator) -> np.ndarray:
@@ -81,10 +84,35 @@ def _neighbours(r, c, ny, nx, wrap):
             yield rr, cc, dr, dc
 
 
-def flood_and_d8(dem: np.ndarray, land: np.ndarray, seeds: np.ndarray, wrap: bool):
+def _synth_lib():
+    import ctypes
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libwg_synth.so")
+    if not os.path.exists(path):
+        return None
+    lib = ctypes.CDLL(path)
+    lib.wg_synth_flood_d8.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    lib.wg_synth_flood_d8.restype = ctypes.c_int
+    return lib
+
+
+def flood_and_d8(dem: np.ndarray, land: np.ndarray, seeds: np.ndarray, wrap: bool, native: bool | None = None):
     """Priority-flood pit filling from the seed cells, then D8 steepest descent on
-    the filled surface.  Returns ldd codes (5 at seeds, 1-9 elsewhere, 0 off-land)."""
+    the filled surface.  Returns ldd codes (5 at seeds, 1-9 elsewhere, 0 off-land).
+    Uses the compiled helper (libwg_synth.so, same algorithm) when present."""
     ny, nx = dem.shape
+    lib = _synth_lib() if native is not False else None
+    if lib is not None:
+        d = np.ascontiguousarray(dem, np.float64)
+        la = np.ascontiguousarray(land, np.uint8)
+        se = np.ascontiguousarray(seeds, np.uint8).copy()
+        ldd = np.zeros((ny, nx), np.int8)
+        rc = lib.wg_synth_flood_d8(ny, nx, d.ctypes.data, la.ctypes.data, se.ctypes.data, int(bool(wrap)),
+                                   ldd.ctypes.data)
+        if rc:
+            raise RuntimeError("cell without a downhill neighbour after pit filling")
+        return ldd, None
     eps = 1e-6
     filled = np.full(dem.shape, np.inf)
     done = np.zeros(dem.shape, bool)
@@ -193,7 +221,7 @@ def _upstream_cells(downstream: np.ndarray, order: np.ndarray) -> np.ndarray:
 
 
 def _build_region(name, rows, cols, gr, gc, ldd_grid, index_grid, dem_m, coastal, rng, nband, swb, river_velo_opt,
-                  wrap=False):
+                  wrap=False, res=0.5):
     """rows/cols: global 1-based 0.5-degree position; gr/gc: 0-based position in ldd_grid."""
     ncell = rows.shape[0]
     tabs = _lct_tables(np.random.default_rng(7))
@@ -213,8 +241,8 @@ def _build_region(name, rows, cols, gr, gc, ldd_grid, index_grid, dem_m, coastal
     order = rout_order_from(downstream)
     acc = _upstream_cells(downstream, order)
 
-    area = cell_area_km2(rows).astype(np.float64)
-    lat = row_latitude(rows)
+    area = cell_area_km2(rows, res).astype(np.float64)
+    lat = row_latitude(rows, res)
     contfreq = np.where(coastal, np.round(rng.uniform(40.0, 100.0, ncell), 1), 100.0).astype(np.float32)
     contfreq = contfreq.astype(np.float64)
     lct = rng.integers(1, NLCT + 1, ncell).astype(np.uint8)
@@ -305,7 +333,7 @@ def _build_region(name, rows, cols, gr, gc, ldd_grid, index_grid, dem_m, coastal
         lake_area[:] = np.where(glo_lake > 0, (glo_lake / 100.0 * area).astype(np.float32), 0.0)
         res_area[:] = np.where(glo_res > 0, np.maximum(res_area, 0.0), 0.0)
 
-    raw_len = rng.uniform(30.0, 80.0, ncell).astype(np.float32).astype(np.float64)
+    raw_len = (rng.uniform(30.0, 80.0, ncell) * (res / 0.5)).astype(np.float32).astype(np.float64)
     river_length = raw_len * (contfreq / 100.)          # routing.cpp:480-482
     river_slope = np.exp(rng.uniform(math.log(1e-5), math.log(1e-2), ncell)).astype(np.float32).astype(np.float64)
     rough_hi = 0.1 if swb is not None else 0.05
@@ -362,8 +390,9 @@ def region_64x64(seed: int = 1, nband: int = 5, row0: int = 60, col0: int = 300,
 
 def region_global(seed: int = 11, nband: int = 5, nland: int = 67420, n_outlets: int = 6000,
                   n_sinks: int = 60, swb=(2023, 1348, 300, 1200), river_velo_opt: int = 1,
-                  shape=(360, 720)) -> Region:
-    """Global 0.5-degree grid with a seeded land mask (default 67,420 land cells)."""
+                  shape=(360, 720), name: str = "region_global") -> Region:
+    """Global 0.5-degree grid with a seeded land mask (default 67,420 land cells).
+    With another shape the grid spacing is 180/ny degrees."""
     rng = np.random.default_rng(seed)
     ny, nx = shape
     mask_f = fractal_field((ny, nx), 3.2, rng)
@@ -405,10 +434,20 @@ def region_global(seed: int = 11, nband: int = 5, nland: int = 67420, n_outlets:
     rr, cc = np.nonzero(land)
     index = -np.ones((ny, nx), np.int64)
     index[rr, cc] = np.arange(rr.size)
-    reg = _build_region("region_global", (rr + 1).astype(np.int64), (cc + 1).astype(np.int64), rr, cc, ldd, index,
+    reg = _build_region(name, (rr + 1).astype(np.int64), (cc + 1).astype(np.int64), rr, cc, ldd, index,
                         dem[rr, cc], coastal[rr, cc], np.random.default_rng(seed + 2), nband, swb,
-                        river_velo_opt, wrap=True)
+                        river_velo_opt, wrap=True, res=180.0 / ny)
     return reg
+
+
+def region_5min(seed: int = 41, nband: int = 5, nland: int = 2_200_000, shape=(2160, 4320)) -> Region:
+    """Fine global grid: 2160 x 4320 cells of 5 arc-minutes, ~2.2 M land cells, the
+    global generators at 9x the water-body counts.  The reference cannot run it
+    (its geometry is fixed to 0.5 degrees, def.h:10, geo.h:25)."""
+    k = 9
+    return region_global(seed=seed, nband=nband, nland=nland, n_outlets=6000 * k, n_sinks=60 * k,
+                         swb=(int(0.03 * nland), int(0.02 * nland), 300 * k, 1200 * k), shape=shape,
+                         name="region_5min")
 
 
 def region_small_swb(seed: int = 21, nband: int = 5, ny: int = 24, nx: int = 48,
@@ -431,7 +470,7 @@ def forcing(region: Region, ndays: int, seed: int = 2, doy0: int = 1, day_offset
     T = np.empty((ndays, n), np.float32)
     S = np.empty((ndays, n), np.float32)
     hemi = np.where(lat >= 0, 1.0, -1.0)
-    if region.name == "region_global":
+    if region.name in ("region_global", "region_5min"):
         tmean = 10.0 + 14.0 * (1.0 - np.abs(lat) / 45.0)
     else:
         tmean = np.full(n, 10.0)
