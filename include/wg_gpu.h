@@ -171,6 +171,18 @@ wg_status wg_get_discharge(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out
 wg_status wg_get_balance(wg_ctx *ctx, double out[6]);
 wg_status wg_reset_balance(wg_ctx *ctx);
 
+/* The same sums as wg_get_balance, for callers that cannot allocate device
+ * memory after set-up -- for example a data-assimilation driver that runs its
+ * cycles inside CUDA stream capture, or a process whose free device memory is
+ * held by another framework's allocator.  No counterpart in the reference (it
+ * has no balance check).  Allocates nothing: the per-block partial sums go to a
+ * fixed 4 MiB device array inside the library, which limits the context to
+ * 16,777,216 states (cells x members); larger contexts get WG_ERR_INVALID and a
+ * message in wg_last_error.  The first call on a device looks up the array's
+ * device address (make it before any stream capture).  All calls share the
+ * array: calls that overlap on the GPU race.  Needs record_balance. */
+wg_status wg_get_balance_noalloc(wg_ctx *ctx, double out[6]);
+
 /* Launch shape of the persistent kernels: threads per block (64/128/256) and
  * blocks (0 = as many as fit on the device at once).  Used by the autotuner. */
 wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks);

@@ -915,6 +915,26 @@ wg_status wg_get_balance(wg_ctx *ctx, double out[6]) {
   return WG_OK;
 }
 
+wg_status wg_get_balance_noalloc(wg_ctx *ctx, double out[6]) {
+  if (!ctx || !out) return WG_ERR_INVALID;
+  if (!ctx->balance.enabled) return WG_ERR_INVALID;
+  if ((int64_t)ctx->nstate() > noalloc_max_states()) {
+    ctx->err = "wg_get_balance_noalloc: " + std::to_string(ctx->nstate()) + " states exceed its fixed scratch of " +
+               std::to_string(noalloc_max_states()) + " states";
+    return WG_ERR_INVALID;
+  }
+  cudaSetDevice(ctx->device);
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  cudaError_t e = ctx->precision == 0
+                      ? balance_noalloc(ctx->device, ctx->cd, ctx->sd, ctx->members, ctx->balance, ctx->vol0,
+                                        ctx->stream, out)
+                      : balance_noalloc(ctx->device, ctx->cf, ctx->sf, ctx->members, ctx->balance, ctx->vol0,
+                                        ctx->stream, out);
+  ctx->launches += 2;
+  return cuda_fail(ctx, e, "get_balance_noalloc");
+}
+
 wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks) {
   if (!ctx || (threads != 64 && threads != 128 && threads != 256) || blocks < 0) return WG_ERR_INVALID;
   const bool ens = ctx->members > 1;

@@ -27,4 +27,9 @@ cudaError_t launch_volume(const DevCellsT<R> &c, const DevStateT<R> &s, int M, d
 template <class R>
 cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int M, const DevBalance &b,
                                const double *vol0, double *partial, int *nblocks, cudaStream_t st);
+// wg_noalloc.cu: the balance sums with their scratch in a fixed device array
+int64_t noalloc_max_states();
+template <class R>
+cudaError_t balance_noalloc(int device, const DevCellsT<R> &c, const DevStateT<R> &s, int M, const DevBalance &b,
+                            const double *vol0, cudaStream_t st, double out[6]);
 }  // namespace wg

@@ -28,7 +28,7 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_get_member_state", "wg_upload_forcing", "wg_step_vertical", "wg_step_routing", "wg_run_days",
            "wg_get_discharge", "wg_get_balance", "wg_reset_balance", "wg_synchronize", "wg_launch_shape",
            "wg_get_launch_shape", "wg_num_levels", "wg_launch_count", "wg_last_error", "wg_status_string",
-           "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps")
+           "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc")
 
 
 class WgError(RuntimeError):
@@ -84,6 +84,8 @@ def load_library(path: str = LIB_PATH):
     lib.wg_get_discharge.argtypes = [vp, i32, i32, vp]
     lib.wg_get_balance.argtypes = [vp, vp]
     lib.wg_reset_balance.argtypes = [vp]
+    lib.wg_get_balance_noalloc.argtypes = [vp, vp]
+    lib.wg_get_balance_noalloc.restype = ctypes.c_int
     lib.wg_synchronize.argtypes = [vp]
     lib.wg_num_levels.argtypes = [vp]
     lib.wg_num_levels.restype = i32
@@ -222,6 +224,12 @@ class Model:
     def balance(self) -> np.ndarray:
         out = np.zeros(6)
         self._check(self.lib.wg_get_balance(self.h, _ptr(out)), "get_balance")
+        return out
+
+    def balance_noalloc(self) -> np.ndarray:
+        """wg_get_balance_noalloc: the balance sums without any device allocation."""
+        out = np.zeros(6)
+        self._check(self.lib.wg_get_balance_noalloc(self.h, _ptr(out)), "get_balance_noalloc")
         return out
 
     def reset_balance(self):
