@@ -38,6 +38,24 @@ DAYS_PER_STEP = 365
 # algorithmic HBM bytes per cell-day of a day-by-day FP64 implementation with the
 # water bodies of this workload: vertical 224 + routing 96 + water bodies ~4
 BYTES_PER_CELL_DAY = 324.0
+# of which the wavefront kernel k_pipeline moves: routing 96 + water bodies 4 +
+# the vertical balance of the cells with water bodies (7.2 % of the cells x 224)
+WAVEFRONT_BYTES_PER_CELL_DAY = 116.2
+
+
+def profile_figures(path=os.path.join(ROOT, "profiles", "fp64_global_wavefront_kernels.md")):
+    """The '- name kernel: value' lines of the committed ncu summary."""
+    out = {}
+    if os.path.exists(path):
+        for line in open(path):
+            line = line.strip()
+            if line.startswith("- ") and ":" in line:
+                k, v = line[2:].rsplit(":", 1)
+                try:
+                    out[k.strip()] = float(v)
+                except ValueError:
+                    pass
+    return out
 
 
 def _forcing_block(args):
@@ -160,6 +178,81 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+ENS_MEMBERS = 256
+ENS_DAYS = 730
+
+
+def outlet_errors(q_test, q_ref):
+    """Per-outlet discharge error of q_test against q_ref ([days, outlets]):
+    mean error |mean q - mean ref| / mean ref, and daily error max |q - ref| over
+    the days relative to the outlet's peak reference discharge."""
+    scale = np.maximum(np.abs(q_ref).max(axis=0), 1e-30)
+    daily = np.abs(q_test - q_ref).max(axis=0) / scale
+    mean = np.abs(q_test.mean(axis=0) - q_ref.mean(axis=0)) / np.maximum(np.abs(q_ref.mean(axis=0)), 1e-30)
+    return {"mean_err_max": float(mean.max()), "daily_err_median": float(np.median(daily)),
+            "daily_err_q99": float(np.quantile(daily, 0.99)), "daily_err_max": float(daily.max())}
+
+
+def run_ensemble(args, region, P, T, S, stream, local, plain_value):
+    """Batched ensemble: ENS_MEMBERS members of the global grid over ENS_DAYS days in
+    one day-pipelined wavefront (FP32 state, FP64 confluence and balance sums),
+    launch shape and chunk length from the autotuner, the whole run captured in one
+    CUDA graph and replayed.  Members: precipitation x lognormal(0, 0.3), runoff
+    coefficient gamma x U(0.7, 1.3), each from its own seed; member 0 unperturbed.
+    Discharge error: members 0 and 1 of the first replay against FP64 runs of the
+    same inputs."""
+    import torch
+    from watergap2_gb300.gpu import Model
+    M, nd = ENS_MEMBERS, ENS_DAYS
+    P, T, S = P[:nd], T[:nd], S[:nd]
+    pf = np.array([np.exp(np.random.default_rng((7, m)).normal(0.0, 0.3)) for m in range(M)], np.float32)
+    gf = np.array([np.random.default_rng((8, m)).uniform(0.7, 1.3) for m in range(M)], np.float32)
+    pf[0] = gf[0] = 1.0
+    ens = Model(region, max_days=nd, device=local, stream=stream.cuda_stream, precision="fp32", members=M,
+                prec_factor=pf, gamma_factor=gf)
+    ens.upload_forcing(0, P, T, S)
+    total = ens.num_steps(nd)
+    lag = ens.num_levels - 1
+    tune = ens.autotune(1, 0, nd, lag, 64)
+    ens.graph_capture(1, 0, nd, 0, total)
+    # first replay: from the initial state, checked against FP64
+    ens.graph_launch()
+    ens.synchronize()
+    nst = ens.stations.size
+    q_m = np.empty((2, nd, nst))
+    for d0 in range(0, nd, 73):
+        q = ens.discharge(d0, min(73, nd - d0))            # [days, stations, members]
+        q_m[:, d0:d0 + q.shape[0]] = np.moveaxis(q[:, :, :2], 2, 0)
+        del q
+    errors = {}
+    for m in (0, 1):
+        reg = region if gf[m] == 1.0 else region.with_param("P_GAMRUN_C", region.param("P_GAMRUN_C") * float(gf[m]))
+        ref = Model(reg, max_days=nd, device=local, stream=stream.cuda_stream)
+        q64 = ref.run(1, (P * pf[m]).astype(np.float32), T, S)
+        del ref
+        errors[f"member{m}"] = dict(outlet_errors(q_m[m], q64), prec_factor=float(pf[m]), gamma_factor=float(gf[m]))
+    for _ in range(max(0, args.warmup - 1)):
+        ens.graph_launch()
+    ens.synchronize()
+    l0 = ens.launch_count
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    reps = max(1, min(args.steps, 3))
+    for _ in range(reps):
+        ens.graph_launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ens.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    value = M * region.ncell * nd / (ms / 1000.0)
+    return {"metric": "member-cell-days/s", "value": value, "members": M, "days": nd, "ncell": region.ncell,
+            "ms_per_run": ms, "runs_timed": reps, "gpu_launches": int(ens.launch_count - l0),
+            "dtype": "f32 state, f64 sums", "vs_plain_fp64": value / plain_value, "autotune": tune,
+            "graph": "whole run (all launch pairs) captured once, replayed per run",
+            "discharge_error_vs_fp64": errors}
+
+
 def fp64_peak_tflops():
     from watergap2_gb300 import gpu
     return gpu.measure_fp64_peak()
@@ -195,6 +288,7 @@ def run_gpu(args, rank, world):
     model.run_steps(1, 0, ndays, 0, args.warmup * DAYS_PER_STEP)
     model.synchronize()
     launches0 = model.launch_count
+    model.kernel_timing(True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     per_step = []
     with ClockSampler(local) as clocks:
@@ -215,6 +309,9 @@ def run_gpu(args, rank, world):
         if dist:
             dist.barrier()
     gpu_launches = model.launch_count - launches0
+    kernel_ms = model.kernel_times()
+    model.kernel_timing(False)
+    vinline_frac = model.vinline_fraction()
     elapsed_ms = ev0.elapsed_time(ev1)
     launch_ms = [a.elapsed_time(b) for a, b in per_step]
     model.run_steps(1, 0, ndays, nyears * DAYS_PER_STEP, total_steps)   # drain (untimed)
@@ -239,12 +336,24 @@ def run_gpu(args, rank, world):
     Pn, Tn, Sn = (t_.numpy() for t_ in pin)
     hostq = torch.empty((DAYS_PER_STEP, nst), dtype=torch.float64, pin_memory=True).numpy()
 
-    def e2e_step(k):
+    phases = []   # per timed step: CUDA-event ms of upload and run, host ms of the whole step
+
+    def e2e_step(k, record=False):
         sl = slice(k * DAYS_PER_STEP, (k + 1) * DAYS_PER_STEP)
+        h0 = time.perf_counter()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)] if record else None
+        if record:
+            ev[0].record(stream)
         e2e_model.upload_forcing(k * DAYS_PER_STEP, Pn[sl], Tn[sl], Sn[sl])
+        if record:
+            ev[1].record(stream)
         e2e_model.run_steps(1, 0, ndays, k * DAYS_PER_STEP, (k + 1) * DAYS_PER_STEP)
+        if record:
+            ev[2].record(stream)
         d0 = max(0, (k + 1) * DAYS_PER_STEP - lag - DAYS_PER_STEP)
         e2e_model.discharge_into(d0, DAYS_PER_STEP, hostq)   # synchronises
+        if record:
+            phases.append((ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), 1e3 * (time.perf_counter() - h0)))
 
     for w in range(args.warmup):
         e2e_step(w)
@@ -253,7 +362,7 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(args.steps):
-        e2e_step(args.warmup + k)
+        e2e_step(args.warmup + k, record=True)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_model.run_steps(1, 0, ndays, nyears * DAYS_PER_STEP, total_steps)
@@ -267,32 +376,36 @@ def run_gpu(args, rank, world):
     d2h = DAYS_PER_STEP * nst * 8
     num_levels = e2e_model.num_levels
 
+    del e2e_model
+    ensemble = None
+    if rank == 0 and not os.environ.get("WG_BENCH_NO_ENSEMBLE"):
+        ensemble = run_ensemble(args, region, P, T, S, stream, local, value)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
     peaks, peak_kind = measured_peaks()
-    mean_launch_s = statistics.mean(launch_ms) / 1000.0
-    achieved = BYTES_PER_CELL_DAY * region.ncell * DAYS_PER_STEP / mean_launch_s / 1e9
+    # dominant kernel: the wavefront kernel k_pipeline (one launch per timed step),
+    # its device time from the CUDA events the library records around it
+    pipe_ms = kernel_ms["wavefront_ms"] / kernel_ms["launch_pairs"]
+    va_ms = kernel_ms["vertical_ahead_ms"] / kernel_ms["launch_pairs"]
+    launch_cell_days = region.ncell * DAYS_PER_STEP
+    achieved = WAVEFRONT_BYTES_PER_CELL_DAY * launch_cell_days / (pipe_ms / 1000.0) / 1e9
+    figs = profile_figures()
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "pipeline_fp64_traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get("dram_bytes_per_cell_day")
-        if traffic is not None:
-            traffic = traffic * region.ncell * DAYS_PER_STEP
+    if "traffic_bytes_per_cell_day k_pipeline" in figs:
+        traffic = figs["traffic_bytes_per_cell_day k_pipeline"] * launch_cell_days
     fp64 = None
     try:
         peak64 = fp64_peak_tflops()
-        fpath = os.path.join(ROOT, "profiles", "pipeline_fp64_flops.json")
-        if os.path.exists(fpath):
-            with open(fpath) as f:
-                fl = json.load(f).get("fp64_flops_per_cell_day")
-            ach64 = fl * region.ncell * DAYS_PER_STEP / mean_launch_s / 1e12
-            fp64 = {"achieved": ach64, "peak": peak64, "unit": "TFLOP/s", "frac": ach64 / peak64,
-                    "flops_per_cell_day": fl, "peak_kind": "measured (DFMA loop)"}
-        else:
-            fp64 = {"peak": peak64, "unit": "TFLOP/s", "peak_kind": "measured (DFMA loop)"}
+        fp64 = {"peak": peak64, "unit": "TFLOP/s", "peak_kind": "measured (DFMA loop)"}
+        for kname, ms, cd in (("k_pipeline", pipe_ms, launch_cell_days),
+                              ("k_vertical_ahead", va_ms, launch_cell_days * (1.0 - vinline_frac))):
+            fl = figs.get(f"fp64_flops_per_cell_day {kname}")
+            if fl is not None:
+                ach = fl * cd / (ms / 1000.0) / 1e12
+                fp64[kname] = {"achieved": ach, "frac": ach / peak64, "flops_per_cell_day": fl,
+                               "launch_ms": ms, "pipe_busy_ncu": figs.get(f"fp64_pipe_busy {kname}")}
     except Exception as exc:   # diagnostics only
         fp64 = {"error": str(exc)}
     cpu_threads = os.cpu_count() or 1
@@ -309,12 +422,18 @@ def run_gpu(args, rank, world):
                    "l2": "inputs larger than L2 (295 MB of forcing read per step)"},
         "gpu_launches": int(gpu_launches),
         "e2e": {"value": e2e_value, "unit": "cell-days/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "matches_device_run": same},
+                "matches_device_run": same,
+                "phases_ms": {"upload": statistics.mean(p[0] for p in phases),
+                              "run": statistics.mean(p[1] for p in phases),
+                              "step_host": statistics.mean(p[2] for p in phases)}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                      "frac": achieved / peaks.get("hbm_gbs"), "traffic": traffic,
-                     "peak_kind": peak_kind, "bytes_per_cell_day": BYTES_PER_CELL_DAY,
-                     "kernel": "k_vertical_ahead + k_pipeline (one step)", "mean_step_ms": 1000 * mean_launch_s},
+                     "peak_kind": peak_kind, "kernel": "k_pipeline (wavefront, 365 steps per launch)",
+                     "algorithmic_bytes_per_cell_day": WAVEFRONT_BYTES_PER_CELL_DAY, "launch_ms": pipe_ms,
+                     "limiter": "FP64 pipe (see fp64), not HBM",
+                     "vertical_ahead_launch_ms": va_ms},
         "fp64": fp64,
+        "ensemble": ensemble,
         "cpu_baseline": {"value": cpu_val, "unit": "cell-days/s", "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_days} days of the same grid ({region.ncell * cpu_days} cell-days, "
                                    f"{cpu_s:.1f} s), vertical pass on {cpu_threads} OpenMP threads, routing serial"},

@@ -105,7 +105,9 @@ typedef struct wg_options {
                               (source/enKF2wghmState.cpp:17-121)                       */
   const float *member_prec_factor;   /* [members] precipitation multiplier, or NULL   */
   const float *member_gamma_factor;  /* [members] multiplier on P_GAMRUN_C, or NULL   */
-  int32_t block_threads;   /* 64, 128 or 256 threads per block; 0 = 256               */
+  int32_t block_threads;   /* threads per block, a multiple of 32 up to 512; 0 = one   */
+                           /* block per SM for one member (256 if that does not fit),  */
+                           /* 256 for ensembles                                        */
   int32_t ring_days;       /* days of vertical outputs buffered between the vertical
                               balance run ahead and routing; 0 = as many as fit in 2 GB */
 } wg_options;
@@ -183,10 +185,66 @@ wg_status wg_reset_balance(wg_ctx *ctx);
  * array: calls that overlap on the GPU race.  Needs record_balance. */
 wg_status wg_get_balance_noalloc(wg_ctx *ctx, double out[6]);
 
-/* Launch shape of the persistent kernels: threads per block (64/128/256) and
- * blocks (0 = as many as fit on the device at once).  Used by the autotuner. */
+/* Launch shape of the persistent kernels: threads per block (a multiple of 32
+ * up to 512) and blocks (0 = as many as fit on the device at once).  Used by
+ * the autotuner. */
 wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks);
 wg_status wg_get_launch_shape(const wg_ctx *ctx, int32_t *threads, int32_t *blocks, int32_t *max_blocks);
+
+/* Replace calibration parameter k of every cell (cell order; eCalibParam index,
+ * source/calib_param.h:72-101): 0 = P_GAMRUN_C (runoff coefficient gamma),
+ * 1 = P_CFA (areal correction factor); other k give WG_ERR_UNSUPPORTED, values
+ * must be positive.  Replaces the reference's calibration loop changing gamma
+ * and the correction factor between simulation runs
+ * (calibGammaClass::findNewGamma, source/calibration.cpp:266-636;
+ * integrateWGHM.cpp:414-417). */
+wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values);
+
+/* Device snapshot of the model state (storages, snow bands, LAI state, land
+ * fractions, the wavefront's outflow buffer and the balance sums): save, and
+ * restore as often as needed -- e.g. the start state of each calibration run,
+ * or a forecast state of data assimilation.  One snapshot per context; the
+ * autotuner uses the same one.  No counterpart in the reference (it re-reads
+ * state files). */
+wg_status wg_save_snapshot(wg_ctx *ctx);
+wg_status wg_restore_snapshot(wg_ctx *ctx);
+
+/* Kernel timing: with enable != 0, wg_run_steps records CUDA events on the
+ * context's stream around each launch of the vertical-ahead kernel and of the
+ * wavefront kernel; wg_get_kernel_times synchronises and returns the summed
+ * device time of each since the last call (or since enabling), and the number
+ * of launch pairs.  Launches inside a captured graph are not timed. */
+wg_status wg_kernel_timing(wg_ctx *ctx, int32_t enable);
+wg_status wg_get_kernel_times(wg_ctx *ctx, double *vertical_ahead_ms, double *wavefront_ms, int32_t *launch_pairs);
+
+/* Wavefront steps per launch pair of wg_run_steps (one vertical-ahead launch,
+ * then one cooperative wavefront launch): 1 .. the ring capacity
+ * (wg_options.ring_days); 0 = the ring capacity.  No counterpart in the
+ * reference (it has no day pipelining). */
+wg_status wg_set_chunk_steps(wg_ctx *ctx, int32_t steps);
+int32_t wg_get_chunk_steps(const wg_ctx *ctx);
+
+/* Autotuner: times wg_run_steps(doy0, fday0, ndays, t_begin, t_begin + trial_steps)
+ * for each launch shape -- threads per block 64/128/256/512 (for an ensemble,
+ * the members of one cell that share a block) and chunk steps 8, 16, ... up to
+ * the ring capacity -- restoring the model state from a device snapshot before
+ * each trial and after the last, and keeps the fastest shape.  The state, the
+ * balance sums and the wavefront buffers are as before the call; station
+ * discharge of the trial days is overwritten.  No counterpart in the reference. */
+typedef struct wg_tune_result {
+  int32_t threads, blocks, chunk_steps, trials;
+  double ms_per_step;   /* of the chosen shape, on the trial steps */
+} wg_tune_result;
+wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin,
+                      int32_t trial_steps, wg_tune_result *out);
+
+/* Capture wg_run_steps(doy0, fday0, ndays, t_begin, t_end) -- every launch of
+ * the run, the cooperative wavefront launches included -- into a CUDA graph of
+ * the context (replacing an earlier one), and replay it on the context's stream
+ * with wg_graph_launch.  Each replay runs the same steps again on the state it
+ * finds.  No counterpart in the reference. */
+wg_status wg_graph_capture(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin, int32_t t_end);
+wg_status wg_graph_launch(wg_ctx *ctx);
 
 /* Wait for the context's stream. */
 wg_status wg_synchronize(wg_ctx *ctx);

@@ -1,0 +1,94 @@
+"""Run-time tools of a context: chunk length, autotuner (device snapshot of the
+state around its trials) and CUDA-graph replay of a run.  None of them may
+change a result: the FP64 path gives the same bits under every launch shape and
+chunk length, and a replayed graph the same bits as the direct calls."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _region_and_forcing(seed, nd, doy0=1):
+    from watergap2_gb300 import synthetic as sy
+    region = sy.region_small_swb(seed=seed)
+    return region, sy.forcing(region, nd, doy0=doy0)
+
+
+def test_chunk_steps_do_not_change_results():
+    from watergap2_gb300.gpu import Model
+    region, (P, T, S) = _region_and_forcing(21, 90)
+    ref = Model(region, max_days=90)
+    q_ref = ref.run(1, P, T, S)
+    for steps in (1, 7, 16):
+        m = Model(region, max_days=90)
+        assert m.chunk_steps(steps) == steps
+        assert np.array_equal(m.run(1, P, T, S), q_ref)
+
+
+def test_autotune_leaves_state_and_results_unchanged():
+    from watergap2_gb300.gpu import Model
+    nd = 120
+    region, (P, T, S) = _region_and_forcing(22, nd)
+    plain = Model(region, max_days=nd, record_balance=True)
+    plain.upload_forcing(0, P, T, S)
+    total = plain.num_steps(nd)
+    plain.run_steps(1, 0, nd, 0, 40)
+    plain.run_steps(1, 0, nd, 40, total)
+    q_ref, b_ref = plain.discharge(0, nd), plain.balance()
+
+    m = Model(region, max_days=nd, record_balance=True)
+    m.upload_forcing(0, P, T, S)
+    m.run_steps(1, 0, nd, 0, 40)
+    st_before = m.get_state()
+    res = m.autotune(1, 0, nd, 40, 32)
+    assert res["trials"] >= 4 and res["threads"] in (64, 128, 256, 512) and res["chunk_steps"] >= 1
+    st_after = m.get_state()
+    for k in st_before:
+        assert np.array_equal(st_before[k], st_after[k]), k
+    m.run_steps(1, 0, nd, 40, total)
+    assert np.array_equal(m.discharge(0, nd), q_ref)
+    assert np.array_equal(m.balance(), b_ref)
+
+
+def test_graph_replay_equals_direct_calls():
+    from watergap2_gb300.gpu import Model
+    nd = 60
+    region, (P, T, S) = _region_and_forcing(23, nd, doy0=100)
+    direct = Model(region, max_days=nd)
+    direct.upload_forcing(0, P, T, S)
+    total = direct.num_steps(nd)
+    direct.run_steps(100, 0, nd, 0, total)
+    q1 = direct.discharge(0, nd)
+    direct.run_steps(100, 0, nd, 0, total)          # a second pass from the state the first left
+    q2 = direct.discharge(0, nd)
+
+    g = Model(region, max_days=nd)
+    g.upload_forcing(0, P, T, S)
+    g.chunk_steps(16)                               # several launch pairs in the graph
+    n0 = g.launch_count
+    g.graph_capture(100, 0, nd, 0, total)
+    assert g.launch_count == n0                     # captured, not run
+    g.graph_launch()
+    assert np.array_equal(g.discharge(0, nd), q1)
+    g.graph_launch()
+    assert np.array_equal(g.discharge(0, nd), q2)
+    assert g.launch_count - n0 == 2 * 2 * -(-total // 16)
+
+
+def test_ensemble_autotune_and_graph():
+    """Ensemble: tuned shape and graph replay give the same bits as the default shape."""
+    from watergap2_gb300.gpu import Model
+    nd, M = 45, 48
+    region, (P, T, S) = _region_and_forcing(24, nd, doy0=150)
+    pf = np.exp(np.random.default_rng(5).normal(0.0, 0.3, M)).astype(np.float32)
+    ref = Model(region, max_days=nd, precision="fp32", members=M, prec_factor=pf)
+    q_ref = ref.run(150, P, T, S)
+
+    m = Model(region, max_days=nd, precision="fp32", members=M, prec_factor=pf)
+    m.upload_forcing(0, P, T, S)
+    total = m.num_steps(nd)
+    res = m.autotune(150, 0, nd, 0, min(total, 24))
+    assert res["trials"] >= 4
+    m.graph_capture(150, 0, nd, 0, total)
+    m.graph_launch()
+    assert np.array_equal(m.discharge(0, nd), q_ref)

@@ -1,6 +1,6 @@
 """Build recipe of the in-tree CUDA library ``_build/libwg_gpu.so`` (sm_103a only).
 
-Compiled with nvcc directly (no cmake): the two translation units in parallel,
+Compiled with nvcc directly (no cmake): every translation unit in parallel,
 then one shared library.  ``--fmad=false`` keeps the arithmetic of the FP64
 path in the reference's expression order (no contraction into FMA), and the
 host code is compiled with ``-ffp-contract=off`` so that x86 and Arm hosts
@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libwg_gpu.so")
-SOURCES = ["wg_kernels.cu", "wg_capi.cpp", "wg_peak.cu", "wg_noalloc.cu"]
+SOURCES = ["wg_kernels.cu", "wg_capi.cpp", "wg_peak.cu", "wg_noalloc.cu", "wg_tune.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

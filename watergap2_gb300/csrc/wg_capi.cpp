@@ -16,11 +16,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
 
 #include "../../include/wg_gpu.h"
+#include "wg_ctx.h"
 #include "wg_device.h"
 #include "wg_kernels.h"
 
@@ -45,15 +47,6 @@ double calc_ext_rad(short day, double lat_deg) {
                               cos(theta) * cos(declination_angle) * sin(omega_s)));
 }
 
-struct Topology {
-  std::vector<int32_t> rout_pos;      // position of each cell in the reference routing order
-  std::vector<int32_t> offset;        // per cell: pipeline step offset
-  std::vector<int32_t> cell_of_slot;  // slot -> cell
-  std::vector<int32_t> slot_of_cell;  // cell -> slot
-  std::vector<int32_t> level_start;   // [nlevel+1]
-  std::vector<int32_t> up_ptr, up_idx;// slot space
-  int32_t nlevel = 0;
-};
 
 // Routing order of the reference (rout_prepare.cpp:834-886): Kahn passes, each pass
 // numbering the cells without pending inflow in index order.
@@ -79,7 +72,19 @@ wg_status reference_rout_order(int n, const int32_t *down, std::vector<int32_t> 
   return (int)order.size() == n ? WG_OK : WG_ERR_TOPOLOGY;
 }
 
-wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, Topology &t) {
+// Slot order.  The day-pipelined kernel maps slot i to thread i (mod the grid),
+// so a warp runs the 32 cells of 32 consecutive slots in lock step, and every cell
+// is busy in every step of the steady state.  Cells are therefore grouped by work
+// class (cls: cells of one class run the same branches -- above all, cells with a
+// water body also run the vertical balance inside the wavefront), within a class
+// by offset and then routing order (so that a warp's cells mostly compute the same
+// day and read forcing and ring rows contiguously).  The warps of each class are
+// then spread evenly over the slot range, so that each block -- one per SM by
+// default -- holds its share of every class and no SM waits on the others at the
+// step barrier.  The order of slots changes nothing in the results: each cell's
+// inputs are addressed through its slot, and inflows are summed in the upstream
+// lists' routing order.
+wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, const uint32_t *cls, Topology &t) {
   for (int i = 0; i < n; ++i)
     if (down[i] < -1 || down[i] >= n || down[i] == i) return WG_ERR_TOPOLOGY;
   std::vector<int32_t> order;
@@ -108,19 +113,38 @@ wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, 
   t.nlevel = dmax + 1;
   t.offset.resize(n);
   for (int i = 0; i < n; ++i) t.offset[i] = dmax - depth[i];
-  // slots: by offset, ties in routing order (a stable bucket pass over the routing order)
   t.level_start.assign(t.nlevel + 1, 0);
   for (int i = 0; i < n; ++i) t.level_start[t.offset[i] + 1]++;
   for (int l = 0; l < t.nlevel; ++l) t.level_start[l + 1] += t.level_start[l];
-  std::vector<int32_t> fill(t.level_start.begin(), t.level_start.end() - 1);
+  std::vector<int32_t> seq(order);
+  std::stable_sort(seq.begin(), seq.end(), [&](int a, int b) {
+    const uint32_t ca = cls ? cls[a] : 0u, cb = cls ? cls[b] : 0u;
+    if (ca != cb) return ca < cb;
+    return t.offset[a] < t.offset[b];
+  });
+  const int W = (n + 31) / 32;
+  const int wfull = n / 32;   // a partial last warp stays last, so that every full warp stays aligned
+  std::vector<uint32_t> wcls(W);
+  std::map<uint32_t, int> count;
+  for (int w = 0; w < W; ++w) {
+    wcls[w] = cls ? cls[seq[(size_t)w * 32]] : 0u;
+    if (w < wfull) count[wcls[w]]++;
+  }
+  std::map<uint32_t, int> seen;
+  std::vector<std::pair<double, int>> key(wfull);
+  for (int w = 0; w < wfull; ++w) key[w] = {(seen[wcls[w]]++ + 0.5) / count[wcls[w]], w};
+  std::stable_sort(key.begin(), key.end());
+  std::vector<int32_t> worder(W);
+  for (int k = 0; k < wfull; ++k) worder[k] = key[k].second;
+  if (W > wfull) worder[W - 1] = W - 1;
   t.cell_of_slot.resize(n);
   t.slot_of_cell.resize(n);
-  for (int k = 0; k < n; ++k) {
-    const int c = order[k];
-    const int s = fill[t.offset[c]]++;
-    t.cell_of_slot[s] = c;
-    t.slot_of_cell[c] = s;
-  }
+  int slot = 0;
+  for (int k = 0; k < W; ++k)
+    for (int j = worder[k] * 32; j < std::min(n, worder[k] * 32 + 32); ++j) {
+      t.cell_of_slot[slot] = seq[j];
+      t.slot_of_cell[seq[j]] = slot++;
+    }
   // upstream lists in slot space, each in routing order (the order of the reference's pushes)
   t.up_ptr.assign(n + 1, 0);
   for (int i = 0; i < n; ++i)
@@ -133,6 +157,27 @@ wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, 
     if (down[c] >= 0) t.up_idx[pos[t.slot_of_cell[down[c]]]++] = t.slot_of_cell[c];
   }
   return WG_OK;
+}
+
+// Water-body flags of cell i and F_VINLINE (the vertical balance runs inside the
+// wavefront: a water body, or no land left outside the water bodies).
+uint32_t water_flags(const wg_region *r, int i) {
+  uint32_t f = 0;
+  if (r->loc_lake[i] > 0.) f |= F_LOCLAKE;
+  if (r->loc_wetl[i] > 0.) f |= F_LOCWETL;
+  if (r->lake_area[i] > 0.) f |= F_GLOLAKE;
+  if (r->res_area[i] > 0.) f |= F_RES;
+  if (r->glo_wetl[i] > 0) f |= F_GLOWETL;
+  const double l0 =
+      (r->contfreq[i] - (r->glo_lake[i] + r->glo_wetl[i] + r->loc_lake[i] + r->loc_wetl[i] + r->glo_res[i]));
+  if (f || !(l0 > 0.)) f |= F_VINLINE;
+  return f;
+}
+
+// Work class for the slot order: the branches a cell takes in the wavefront.
+uint32_t work_class(const wg_region *r, int i) {
+  const uint32_t f = water_flags(r, i);
+  return (f & F_VINLINE) ? (f | (r->res_type[i] == 1 ? F_RES_IRRIG : 0u)) : 0u;
 }
 
 // Per-cell constants in cell order, double precision (converted to the context's
@@ -162,47 +207,6 @@ inline double safe_inv(double x) { return x != 0. ? 1. / x : 0.; }
 
 }  // namespace
 
-// One context: all device buffers of one region in one precision.
-struct wg_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  int n = 0, nband = 0, max_days = 0, nstation = 0, members = 1, precision = 0;
-  int threads = 256, blocks_fused = 0, blocks_route = 0;
-  Topology topo;
-  DevCellsT<double> cd{};
-  DevStateT<double> sd{};
-  DevVertT<double> vd{};
-  DevCellsT<float> cf{};
-  DevStateT<float> sf{};
-  DevVertT<float> vf{};
-  DevRingT<double> rd{};
-  DevRingT<float> rf{};
-  DevForcing forcing{};
-  DevBalance balance{};
-  DevMembers mem{};
-  DevSync sync{};
-  double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
-  float *staging = nullptr;
-  int32_t *d_cell_of_slot = nullptr;
-  int staging_days = 0;
-  int64_t launches = 0;
-  std::vector<void *> allocs;
-  std::string err;
-
-  ~wg_ctx() {
-    for (void *p : allocs) cudaFree(p);
-    if (own_stream && stream) cudaStreamDestroy(stream);
-  }
-  template <class T>
-  T *alloc(size_t count) {
-    void *p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) return nullptr;
-    allocs.push_back(p);
-    return (T *)p;
-  }
-  size_t nstate() const { return (size_t)n * members; }
-};
 
 namespace {
 
@@ -210,6 +214,24 @@ wg_status cuda_fail(wg_ctx *ctx, cudaError_t e, const char *what) {
   if (e == cudaSuccess) return WG_OK;
   if (ctx) ctx->err = std::string(what) + ": " + cudaGetErrorString(e);
   return e == cudaErrorMemoryAllocation ? WG_ERR_NOMEM : WG_ERR_CUDA;
+}
+
+bool valid_block_threads(int threads) { return threads >= 32 && threads <= kMaxBlockThreads && threads % 32 == 0; }
+
+// Single-member contexts: one block per SM holding an equal share of the cells
+// (whole warps), so that every SM carries the same work between step barriers;
+// 256 when the cells do not fit one block per SM or the block does not fit an SM.
+int default_block_threads(wg_ctx *ctx) {
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+  if (nsm <= 0) return 256;
+  const size_t per_sm = (ctx->nstate() + nsm - 1) / nsm;
+  if (per_sm > (size_t)kMaxBlockThreads) return 256;
+  const int th = std::max(64, (int)((per_sm + 31) / 32 * 32));
+  const int need = (int)((ctx->nstate() + th - 1) / th);
+  const int fits = ctx->precision == 0 ? pipeline_max_blocks<double>(true, false, th)
+                                       : pipeline_max_blocks<float>(true, false, th);
+  return fits >= need ? th : 256;
 }
 
 // upload a per-cell host array (cell order) into slot order, converting to T
@@ -278,10 +300,6 @@ wg_status upload_cells(wg_ctx *ctx, const HostConsts &h, DevCellsT<R> &c, double
   return st;
 }
 
-#define WG_STATE_R(X)                                                                                               \
-  X(canopy) X(soil) X(snow) X(lai_precsum) X(gw) X(river) X(loclake) X(locwetl) X(glolake) X(glowetl) X(res)      \
-  X(rf_loclake) X(rf_locwetl) X(rf_glolake) X(rf_glowetl) X(rf_res) X(k_release) X(laf) X(laf_prev) X(fswb_next)
-#define WG_STATE_I(X) X(lai_days) X(lai_status) X(laf_started)
 
 template <class R>
 wg_status alloc_state(wg_ctx *ctx, DevStateT<R> &s, DevVertT<R> &v) {
@@ -413,6 +431,27 @@ void fill_fastmath_tables(double e2[64], double lf[129], double inv[129]) {
 
 }  // namespace
 
+namespace {
+template <class R>
+wg_status set_calib_param(wg_ctx *ctx, const DevCellsT<R> &c, int32_t k, const double *values) {
+  const int n = ctx->n;
+  std::vector<R> a(n), b(n);
+  for (int s = 0; s < n; ++s) {
+    const double v = values[ctx->topo.cell_of_slot[s]];
+    a[s] = (R)v;
+    b[s] = (R)safe_inv(v);
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (k == 0) {
+    if (e == cudaSuccess) e = cudaMemcpy((R *)c.gamma, a.data(), n * sizeof(R), cudaMemcpyHostToDevice);
+  } else {
+    if (e == cudaSuccess) e = cudaMemcpy((R *)c.cfa, a.data(), n * sizeof(R), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy((R *)c.inv_cfa, b.data(), n * sizeof(R), cudaMemcpyHostToDevice);
+  }
+  return cuda_fail(ctx, e, "set_calib_param");
+}
+}  // namespace
+
 extern "C" {
 
 const char *wg_status_string(wg_status s) {
@@ -441,7 +480,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->precision < 0 || opt->precision > 1) return WG_ERR_UNSUPPORTED;
   if (opt->members < 1 || (opt->members > 1 && opt->precision != 1)) return WG_ERR_UNSUPPORTED;
   if (opt->nstation < 0 || (opt->nstation > 0 && !opt->stations)) return WG_ERR_INVALID;
-  if (opt->block_threads != 0 && opt->block_threads != 64 && opt->block_threads != 128 && opt->block_threads != 256)
+  if (opt->block_threads != 0 && !valid_block_threads(opt->block_threads))
     return WG_ERR_INVALID;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
@@ -470,7 +509,9 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return WG_ERR_CUDA;
     ctx->own_stream = true;
   }
-  wg_status st = build_topology(n, r->downstream, r->rout_order, ctx->topo);
+  std::vector<uint32_t> cls(n);
+  for (int i = 0; i < n; ++i) cls[i] = work_class(r, i);
+  wg_status st = build_topology(n, r->downstream, r->rout_order, cls.data(), ctx->topo);
   if (st != WG_OK) return st;
   {
     double e2[64], lf[129], inv[129];
@@ -499,18 +540,9 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     if (r->aindex[i] == 1 && r->texture[i] < 21) f |= F_ARID_GW;
     if (r->ldd[i] < 0) f |= F_SINK;
     if (lct <= 2) f |= F_EVERGREEN;
-    if (r->loc_lake[i] > 0.) f |= F_LOCLAKE;
-    if (r->loc_wetl[i] > 0.) f |= F_LOCWETL;
-    if (r->lake_area[i] > 0.) f |= F_GLOLAKE;
-    if (r->res_area[i] > 0.) f |= F_RES;
-    if (r->glo_wetl[i] > 0) f |= F_GLOWETL;
+    f |= water_flags(r, i);
     if (r->res_type[i] == 1) f |= F_RES_IRRIG;
     if (r->downstream[i] < 0) f |= F_OUTLET;
-    {
-      const double l0 = (r->contfreq[i] - (r->glo_lake[i] + r->glo_wetl[i] + r->loc_lake[i] + r->loc_wetl[i] +
-                                           r->glo_res[i]));
-      if ((f & (F_LOCLAKE | F_LOCWETL | F_GLOLAKE | F_RES | F_GLOWETL)) || !(l0 > 0.)) f |= F_VINLINE;
-    }
     h.flags[i] = f;
     const double ar = r->area_km2[i];
     h.area[i] = ar;
@@ -625,9 +657,13 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (st != WG_OK) return st;
   const size_t N = ctx->nstate();
   {
-    // ring of vertical outputs: as many days as fit in ~2 GB, at least 8, at most max_days
+    // ring of vertical outputs: as many days as fit in 8 GB or an eighth of the free
+    // device memory, whichever is less; at least 8, at most max_days
     const size_t elem = ctx->precision == 0 ? sizeof(double) : sizeof(float);
-    const size_t budget = opt->ring_days > 0 ? (size_t)opt->ring_days : ((size_t)2 << 30) / (2 * elem * N);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = (size_t)16 << 30;
+    const size_t ring_bytes = std::min<size_t>((size_t)8 << 30, free_b / 8);
+    const size_t budget = opt->ring_days > 0 ? (size_t)opt->ring_days : ring_bytes / (2 * elem * N);
     const int ring = (int)std::max<size_t>(8, std::min<size_t>(budget, (size_t)ctx->max_days));
     if (ctx->precision == 0) {
       ctx->rd.ring_days = ring;
@@ -708,6 +744,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   st = ctx->precision == 0 ? broadcast_state(ctx.get(), ctx->sd, &init) : broadcast_state(ctx.get(), ctx->sf, &init);
   if (st != WG_OK) return st;
   const bool ens = ctx->members > 1;
+  if (!opt->block_threads && !ens) ctx->threads = default_block_threads(ctx.get());
   const int th = ctx->threads;
   const int need = (int)std::min<size_t>((N + th - 1) / th, (size_t)1 << 30);
   if (ctx->precision == 0) {
@@ -812,15 +849,20 @@ wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday) {
 template <class R>
 static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
                                 const DevRingT<R> &ring, int doy0, int fday0, int ndays, int t_b, int t_e) {
-  for (int a = t_b; a < t_e; a += ring.ring_days) {
-    const int b = std::min(t_e, a + ring.ring_days);
+  const int chunk = (ctx->chunk_steps > 0 && ctx->chunk_steps <= ring.ring_days) ? ctx->chunk_steps : ring.ring_days;
+  for (int a = t_b; a < t_e; a += chunk) {
+    const int b = std::min(t_e, a + chunk);
+    cudaEvent_t *ev = ctx->timing ? ctx->timing_events() : nullptr;
+    if (ev) cudaEventRecord(ev[0], ctx->stream);
     cudaError_t e = launch_vertical_ahead(c, s, ctx->forcing, ctx->mem, ctx->balance, ring, doy0, fday0, ndays, a, b,
-                                          ctx->stream);
+                                          ctx->blocks_fused, ctx->threads, ctx->stream);
     ctx->launches++;
+    if (ev) cudaEventRecord(ev[1], ctx->stream);
     if (e == cudaSuccess)
       e = launch_pipeline(true, c, s, v, ctx->forcing, ctx->mem, ctx->balance, ring, ctx->sync, ctx->outq, ctx->qst,
                           doy0, fday0, fday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->stream);
     ctx->launches++;
+    if (ev) cudaEventRecord(ev[2], ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "run_steps");
   }
   return WG_OK;
@@ -935,8 +977,18 @@ wg_status wg_get_balance_noalloc(wg_ctx *ctx, double out[6]) {
   return cuda_fail(ctx, e, "get_balance_noalloc");
 }
 
+
+wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values) {
+  if (!ctx || !values) return WG_ERR_INVALID;
+  if (k != 0 && k != 1) return WG_ERR_UNSUPPORTED;
+  for (int i = 0; i < ctx->n; ++i)
+    if (!(values[i] > 0.) || !std::isfinite(values[i])) return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  return ctx->precision == 0 ? set_calib_param(ctx, ctx->cd, k, values) : set_calib_param(ctx, ctx->cf, k, values);
+}
+
 wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks) {
-  if (!ctx || (threads != 64 && threads != 128 && threads != 256) || blocks < 0) return WG_ERR_INVALID;
+  if (!ctx || !valid_block_threads(threads) || blocks < 0) return WG_ERR_INVALID;
   const bool ens = ctx->members > 1;
   const int maxb = ctx->precision == 0 ? pipeline_max_blocks<double>(true, ens, threads)
                                        : pipeline_max_blocks<float>(true, ens, threads);

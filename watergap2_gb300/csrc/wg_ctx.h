@@ -1,0 +1,104 @@
+// wg_ctx.h -- the library's context (struct wg_ctx of include/wg_gpu.h) and the
+// host-side topology; shared by the C ABI (wg_capi.cpp) and the run-time tools
+// (wg_tune.cpp: snapshot, autotuner, CUDA graphs).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/wg_gpu.h"
+#include "wg_device.h"
+
+using wg::DevBalance;
+using wg::DevCellsT;
+using wg::DevForcing;
+using wg::DevMembers;
+using wg::DevRingT;
+using wg::DevStateT;
+using wg::DevSync;
+using wg::DevVertT;
+
+// Drainage topology and slot order of one region (built once by wg_create).
+struct Topology {
+  std::vector<int32_t> rout_pos;      // position of each cell in the reference routing order
+  std::vector<int32_t> offset;        // per cell: pipeline step offset
+  std::vector<int32_t> cell_of_slot;  // slot -> cell
+  std::vector<int32_t> slot_of_cell;  // cell -> slot
+  std::vector<int32_t> level_start;   // [nlevel+1]
+  std::vector<int32_t> up_ptr, up_idx;// slot space
+  int32_t nlevel = 0;
+};
+
+// The mutable per-state arrays of DevStateT (besides snow_band).
+#define WG_STATE_R(X)                                                                                               \
+  X(canopy) X(soil) X(snow) X(lai_precsum) X(gw) X(river) X(loclake) X(locwetl) X(glolake) X(glowetl) X(res)      \
+  X(rf_loclake) X(rf_locwetl) X(rf_glolake) X(rf_glowetl) X(rf_res) X(k_release) X(laf) X(laf_prev) X(fswb_next)
+#define WG_STATE_I(X) X(lai_days) X(lai_status) X(laf_started)
+
+struct Snapshot;   // wg_tune.cpp
+
+// One context: all device buffers of one region in one precision.
+struct wg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int n = 0, nband = 0, max_days = 0, nstation = 0, members = 1, precision = 0;
+  int threads = 256, blocks_fused = 0, blocks_route = 0;
+  Topology topo;
+  DevCellsT<double> cd{};
+  DevStateT<double> sd{};
+  DevVertT<double> vd{};
+  DevCellsT<float> cf{};
+  DevStateT<float> sf{};
+  DevVertT<float> vf{};
+  DevRingT<double> rd{};
+  DevRingT<float> rf{};
+  DevForcing forcing{};
+  DevBalance balance{};
+  DevMembers mem{};
+  DevSync sync{};
+  double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
+  float *staging = nullptr;
+  int32_t *d_cell_of_slot = nullptr;
+  int staging_days = 0;
+  int64_t launches = 0;
+  std::vector<void *> allocs;
+  std::string err;
+  int chunk_steps = 0;                     // steps per (vertical-ahead, wavefront) launch pair
+  Snapshot *snap = nullptr;                // device copy of the mutable state (autotuner)
+  cudaGraph_t graph = nullptr;             // wg_graph_capture
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_launches = 0;                  // kernels in the captured graph
+  bool timing = false;                     // CUDA events around each launch pair of wg_run_steps
+  std::vector<cudaEvent_t> tev;            // 3 per recorded launch pair
+  size_t tev_used = 0;
+  cudaEvent_t *timing_events() {           // the next three events of the pool
+    if (tev_used + 3 > tev.size())
+      for (int k = 0; k < 3; ++k) {
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        tev.push_back(e);
+      }
+    cudaEvent_t *p = tev.data() + tev_used;
+    tev_used += 3;
+    return p;
+  }
+
+  ~wg_ctx() {
+    release_tools();
+    for (void *p : allocs) cudaFree(p);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+  }
+  template <class T>
+  T *alloc(size_t count) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) return nullptr;
+    allocs.push_back(p);
+    return (T *)p;
+  }
+  size_t nstate() const { return (size_t)n * members; }
+  int ring_days() const { return precision == 0 ? rd.ring_days : rf.ring_days; }
+  void release_tools();   // snapshot and graph (wg_tune.cpp)
+};

@@ -151,57 +151,57 @@ __global__ void __launch_bounds__(256) k_vertical(DevCellsT<R> c, DevStateT<R> s
 // ring buffer.  Results equal the in-wavefront computation: the vertical balance of
 // such a cell reads nothing routing writes.
 template <class R, bool ENS>
-__global__ void __launch_bounds__(256) k_vertical_ahead(DevCellsT<R> c, DevStateT<R> st, DevForcing f,
+__global__ void __launch_bounds__(kMaxBlockThreads) k_vertical_ahead(DevCellsT<R> c, DevStateT<R> st, DevForcing f,
                                                         DevMembers mem, DevBalance b, DevRingT<R> ring, int doy0,
                                                         int fday0, int ndays, int t_b, int t_e) {
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const size_t N = (size_t)n * M;
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  const int s = ENS ? (int)(i / M) : (int)i;
-  const int mm = ENS ? (int)(i - (size_t)s * M) : 0;
-  if (c.flags[s] & F_VINLINE) return;
-  const int off = c.offset[s];
-  const int d0 = max(0, t_b - off), d1 = min(ndays, t_e - off);
-  if (d0 >= d1) return;
-  R canopy = st.canopy[i], soil = st.soil[i], gsnow = st.snow[i], psum = st.lai_precsum[i];
-  int days = st.lai_days[i], status = st.lai_status[i];
-  const R laf = st.laf[i];   // constant for these cells (no water body)
-  R pf = R(1), gam = c.gamma[s];
-  if (ENS) {
-    pf = R(mem.prec_factor[mm]);
-    gam *= R(mem.gamma_factor[mm]);
-  }
-  double acc_in = 0., acc_ev = 0., acc_lk = 0.;
-  const double land_f = (double)c.area_f[s] * (double)laf;
-  for (int d = d0; d < d1; ++d) {
-    const int doy = (doy0 - 1 + d) % 365 + 1;
-    const size_t fo = (size_t)(fday0 + d) * n + s;
-    const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
-    VOut<R> o;
-    vertical_cell<R>(c, s, gam, canopy, soil, gsnow, st.snow_band + i, N, days, status, psum, laf, laf,
-                     R(f.prec[fo]) * pf, f.temp[fo], f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o);
-    const size_t ri = (size_t)(d % ring.ring_days) * N + i;
-    ring.rs[ri] = o.rs;
-    ring.gwr[ri] = o.gwr;
-    if (b.enabled) {
-      acc_in += (double)o.land_in * land_f;
-      acc_ev += (double)o.land_evap * land_f;
-      acc_lk += (double)o.land_leak * land_f;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+    const int s = ENS ? (int)(i / M) : (int)i;
+    const int mm = ENS ? (int)(i - (size_t)s * M) : 0;
+    if (c.flags[s] & F_VINLINE) continue;
+    const int off = c.offset[s];
+    const int d0 = max(0, t_b - off), d1 = min(ndays, t_e - off);
+    if (d0 >= d1) continue;
+    R canopy = st.canopy[i], soil = st.soil[i], gsnow = st.snow[i], psum = st.lai_precsum[i];
+    int days = st.lai_days[i], status = st.lai_status[i];
+    const R laf = st.laf[i];   // constant for these cells (no water body)
+    R pf = R(1), gam = c.gamma[s];
+    if (ENS) {
+      pf = R(mem.prec_factor[mm]);
+      gam *= R(mem.gamma_factor[mm]);
     }
-  }
-  st.canopy[i] = canopy; st.soil[i] = soil; st.snow[i] = gsnow; st.lai_precsum[i] = psum;
-  st.lai_days[i] = days; st.lai_status[i] = status;
-  if (b.enabled) {
-    neumaier_add(b.acc, 0 * N + i, 5 * N + i, acc_in);
-    neumaier_add(b.acc, 1 * N + i, 6 * N + i, acc_ev);
-    neumaier_add(b.acc, 4 * N + i, 9 * N + i, acc_lk);
+    double acc_in = 0., acc_ev = 0., acc_lk = 0.;
+    const double land_f = (double)c.area_f[s] * (double)laf;
+    for (int d = d0; d < d1; ++d) {
+      const int doy = (doy0 - 1 + d) % 365 + 1;
+      const size_t fo = (size_t)(fday0 + d) * n + s;
+      const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
+      VOut<R> o;
+      vertical_cell<R>(c, s, gam, canopy, soil, gsnow, st.snow_band + i, N, days, status, psum, laf, laf,
+                       R(f.prec[fo]) * pf, f.temp[fo], f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o);
+      const size_t ri = (size_t)(d % ring.ring_days) * N + i;
+      ring.rs[ri] = o.rs;
+      ring.gwr[ri] = o.gwr;
+      if (b.enabled) {
+        acc_in += (double)o.land_in * land_f;
+        acc_ev += (double)o.land_evap * land_f;
+        acc_lk += (double)o.land_leak * land_f;
+      }
+    }
+    st.canopy[i] = canopy; st.soil[i] = soil; st.snow[i] = gsnow; st.lai_precsum[i] = psum;
+    st.lai_days[i] = days; st.lai_status[i] = status;
+    if (b.enabled) {
+      neumaier_add(b.acc, 0 * N + i, 5 * N + i, acc_in);
+      neumaier_add(b.acc, 1 * N + i, 6 * N + i, acc_ev);
+      neumaier_add(b.acc, 4 * N + i, 9 * N + i, acc_lk);
+    }
   }
 }
 
 template <class R, bool FUSED, bool ENS>
-__global__ void __launch_bounds__(256) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
+__global__ void __launch_bounds__(kMaxBlockThreads) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
                                                   double *outq, double *qst, int doy0, int fday0, int oday0,
                                                   int ndays, int t_b, int t_e) {
@@ -211,20 +211,17 @@ __global__ void __launch_bounds__(256) k_pipeline(DevCellsT<R> c, DevStateT<R> s
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gstride = (long long)gridDim.x * blockDim.x;
   for (int t = t_b; t < t_e; ++t) {
-    const int lo_off = max(0, t - ndays + 1), hi_off = min(c.nlevel - 1, t);
-    if (lo_off <= hi_off) {
-      const long long lo = (long long)c.level_start[lo_off] * M, hi = (long long)c.level_start[hi_off + 1] * M;
+    if (t - c.nlevel + 1 < ndays) {   // some cell still has a day to compute
       double *q_now = outq + (size_t)(t & 1) * N;
       const double *q_prev = outq + (size_t)((t + 1) & 1) * N;
       // state index i always belongs to thread i mod gstride, so a cell's state is read
       // and written by one thread; only upstream outflows cross threads (read via L2)
-      long long r0 = (gtid - lo) % gstride;
-      if (r0 < 0) r0 += gstride;
-      for (long long i = lo + r0; i < hi; i += gstride) {
+      for (long long i = gtid; i < (long long)N; i += gstride) {
         const int s = ENS ? (int)(i / M) : (int)i;
         const int mm = ENS ? (int)(i - (long long)s * M) : 0;
         const size_t si = (size_t)i;
         const int d = t - c.offset[s];
+        if (d < 0 || d >= ndays) continue;   // this cell's wavefront has not reached it yet / is done
         const int doy = (doy0 - 1 + d) % 365 + 1;
         const int month = month_of(doy);
         const uint32_t fl = c.flags[s];
@@ -378,9 +375,7 @@ cudaError_t launch_vertical(const DevCellsT<R> &c, const DevStateT<R> &s, const 
 template <class R>
 cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, const DevForcing &f,
                                   const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring, int doy0,
-                                  int fday0, int ndays, int t_b, int t_e, cudaStream_t st) {
-  const size_t N = (size_t)c.n * mem.members;
-  const int threads = 256, blocks = (int)((N + threads - 1) / threads);
+                                  int fday0, int ndays, int t_b, int t_e, int blocks, int threads, cudaStream_t st) {
   if (mem.members > 1)
     k_vertical_ahead<R, true><<<blocks, threads, 0, st>>>(c, s, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e);
   else
@@ -414,7 +409,19 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
                   (void *)&ring, (void *)&sync, (void *)&outq,  (void *)&qst,   (void *)&doy0,  (void *)&fday0,
                   (void *)&oday0, (void *)&ndays, (void *)&t_b, (void *)&t_e};
   const bool ens = mem.members > 1;
-  return cudaLaunchCooperativeKernel(pipeline_fn<R>(fused, ens), dim3(blocks), dim3(threads), args, 0, st);
+  // cooperative (all blocks resident, or the launch fails) through the launch
+  // attribute, which stream capture records into a graph kernel node
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, pipeline_fn<R>(fused, ens), args);
 }
 
 template <class R>
@@ -445,7 +452,7 @@ cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int
                                           int, int, int, int, int, int, cudaStream_t);                            \
   template cudaError_t launch_vertical_ahead<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevForcing &,   \
                                                 const DevMembers &, const DevBalance &, const DevRingT<R> &, int,  \
-                                                int, int, int, int, cudaStream_t);                                 \
+                                                int, int, int, int, int, int, cudaStream_t);                       \
   template cudaError_t launch_volume<R>(const DevCellsT<R> &, const DevStateT<R> &, int, double *, cudaStream_t); \
   template cudaError_t launch_balance_sum<R>(const DevCellsT<R> &, const DevStateT<R> &, int, const DevBalance &,  \
                                              const double *, double *, int *, cudaStream_t);

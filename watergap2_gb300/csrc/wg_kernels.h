@@ -5,6 +5,8 @@
 #include "wg_device.h"
 
 namespace wg {
+// Largest block of the day-pipelined kernels (k_pipeline, k_vertical_ahead).
+constexpr int kMaxBlockThreads = 512;
 cudaError_t upload_fastmath_tables(const double exp2_tab[64], const double logF_tab[129], const double invF_tab[129]);
 cudaError_t launch_gather_forcing(const float *src, float *dst, const int32_t *cell_of_slot, int n, int ndays,
                                   cudaStream_t st);
@@ -21,7 +23,7 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
 template <class R>
 cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, const DevForcing &f,
                                   const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring, int doy0,
-                                  int fday0, int ndays, int t_b, int t_e, cudaStream_t st);
+                                  int fday0, int ndays, int t_b, int t_e, int blocks, int threads, cudaStream_t st);
 template <class R>
 cudaError_t launch_volume(const DevCellsT<R> &c, const DevStateT<R> &s, int M, double *vol, cudaStream_t st);
 template <class R>

@@ -1,0 +1,271 @@
+// wg_tune.cpp -- run-time tools of a context: a device snapshot of the mutable
+// state, the launch-shape autotuner, and CUDA-graph capture of a run.
+//
+// The reference has no counterpart (its day loop is OpenMP over cells); these
+// exist for the batched paths: an ensemble of hundreds of members in one
+// persistent wavefront, whose best block size (members of one cell per block)
+// and chunk length (wavefront steps per vertical-ahead/wavefront launch pair)
+// depend on the member count and the device, is tuned once and then replayed
+// as one graph launch per run.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "wg_ctx.h"
+#include "wg_kernels.h"
+
+using namespace wg;
+
+// Device copy of everything a run mutates: the state arrays, the snow bands,
+// the two-slot outflow buffer of the wavefront and the balance accumulators.
+// (The ring of vertical outputs holds nothing between calls: each chunk's
+// vertical-ahead launch fills exactly the days its wavefront launch reads.)
+struct Snapshot {
+  std::vector<std::pair<void *, size_t>> fields;   // (device array, bytes)
+  char *buf = nullptr;
+  size_t bytes = 0;
+};
+
+namespace {
+
+wg_status fail(wg_ctx *ctx, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return WG_OK;
+  ctx->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? WG_ERR_NOMEM : WG_ERR_CUDA;
+}
+
+template <class R>
+void list_fields(wg_ctx *ctx, const DevStateT<R> &s, Snapshot &sn) {
+  const size_t N = ctx->nstate();
+#define X(f) sn.fields.push_back({(void *)s.f, N * sizeof(R)});
+  WG_STATE_R(X)
+#undef X
+#define X(f) sn.fields.push_back({(void *)s.f, N * sizeof(int32_t)});
+  WG_STATE_I(X)
+#undef X
+  sn.fields.push_back({(void *)s.snow_band, N * ctx->nband * sizeof(R)});
+  sn.fields.push_back({(void *)ctx->outq, 2 * N * sizeof(double)});
+  if (ctx->balance.enabled) sn.fields.push_back({(void *)ctx->balance.acc, 10 * N * sizeof(double)});
+}
+
+wg_status snapshot_save(wg_ctx *ctx) {
+  if (!ctx->snap) {
+    Snapshot *sn = new Snapshot();
+    if (ctx->precision == 0) list_fields(ctx, ctx->sd, *sn);
+    else list_fields(ctx, ctx->sf, *sn);
+    for (auto &f : sn->fields) sn->bytes += (f.second + 255) / 256 * 256;
+    cudaError_t e = cudaMalloc((void **)&sn->buf, sn->bytes);
+    if (e != cudaSuccess) {
+      delete sn;
+      return fail(ctx, e, "snapshot");
+    }
+    ctx->snap = sn;
+  }
+  size_t off = 0;
+  for (auto &f : ctx->snap->fields) {
+    cudaError_t e = cudaMemcpyAsync(ctx->snap->buf + off, f.first, f.second, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, e, "snapshot");
+    off += (f.second + 255) / 256 * 256;
+  }
+  return WG_OK;
+}
+
+wg_status snapshot_restore(wg_ctx *ctx) {
+  if (!ctx->snap) return WG_ERR_INVALID;
+  size_t off = 0;
+  for (auto &f : ctx->snap->fields) {
+    cudaError_t e = cudaMemcpyAsync(f.first, ctx->snap->buf + off, f.second, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, e, "restore");
+    off += (f.second + 255) / 256 * 256;
+  }
+  return WG_OK;
+}
+
+}  // namespace
+
+void wg_ctx::release_tools() {
+  for (cudaEvent_t e : tev) cudaEventDestroy(e);
+  tev.clear();
+  tev_used = 0;
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  if (graph) cudaGraphDestroy(graph);
+  graph_exec = nullptr;
+  graph = nullptr;
+  if (snap) {
+    cudaFree(snap->buf);
+    delete snap;
+    snap = nullptr;
+  }
+}
+
+extern "C" {
+
+wg_status wg_save_snapshot(wg_ctx *ctx) {
+  if (!ctx) return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  wg_status st = snapshot_save(ctx);
+  return st != WG_OK ? st : wg_synchronize(ctx);
+}
+
+wg_status wg_restore_snapshot(wg_ctx *ctx) {
+  if (!ctx) return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  wg_status st = snapshot_restore(ctx);
+  return st != WG_OK ? st : wg_synchronize(ctx);
+}
+
+wg_status wg_kernel_timing(wg_ctx *ctx, int32_t enable) {
+  if (!ctx) return WG_ERR_INVALID;
+  ctx->timing = enable != 0;
+  ctx->tev_used = 0;
+  return WG_OK;
+}
+
+wg_status wg_get_kernel_times(wg_ctx *ctx, double *vertical_ahead_ms, double *wavefront_ms, int32_t *launch_pairs) {
+  if (!ctx || !vertical_ahead_ms || !wavefront_ms || !launch_pairs) return WG_ERR_INVALID;
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  double va = 0., wf = 0.;
+  for (size_t k = 0; k + 3 <= ctx->tev_used; k += 3) {
+    float a = 0.f, b = 0.f;
+    if (cudaEventElapsedTime(&a, ctx->tev[k], ctx->tev[k + 1]) != cudaSuccess ||
+        cudaEventElapsedTime(&b, ctx->tev[k + 1], ctx->tev[k + 2]) != cudaSuccess)
+      return fail(ctx, cudaGetLastError(), "kernel times");
+    va += a;
+    wf += b;
+  }
+  *vertical_ahead_ms = va;
+  *wavefront_ms = wf;
+  *launch_pairs = (int32_t)(ctx->tev_used / 3);
+  ctx->tev_used = 0;
+  return WG_OK;
+}
+
+wg_status wg_set_chunk_steps(wg_ctx *ctx, int32_t steps) {
+  if (!ctx || steps < 0 || steps > ctx->ring_days()) return WG_ERR_INVALID;
+  ctx->chunk_steps = steps;
+  return WG_OK;
+}
+
+int32_t wg_get_chunk_steps(const wg_ctx *ctx) {
+  if (!ctx) return 0;
+  return (ctx->chunk_steps > 0 && ctx->chunk_steps <= ctx->ring_days()) ? ctx->chunk_steps : ctx->ring_days();
+}
+
+wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin,
+                      int32_t trial_steps, wg_tune_result *out) {
+  if (!ctx || !out || trial_steps <= 0) return WG_ERR_INVALID;
+  const int total = ndays + ctx->topo.nlevel - 1;
+  if (t_begin < 0 || t_begin + trial_steps > total) return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  const int th0 = ctx->threads, ch0 = ctx->chunk_steps;
+  int32_t bl0 = 0, mb0 = 0, tmp = 0;
+  wg_get_launch_shape(ctx, &tmp, &bl0, &mb0);
+  wg_status st = snapshot_save(ctx);
+  if (st != WG_OK) return st;
+  // candidates: block sizes 64..512 (for ensembles: members of one cell per block,
+  // or whole cells per block when a cell has fewer members), chunk lengths 8..ring
+  std::vector<int> ths = {64, 128, 256, 512};
+  std::vector<int> chs;
+  for (int c = 8; c <= ctx->ring_days(); c *= 2) chs.push_back(c);
+  if (chs.empty() || chs.back() != ctx->ring_days()) chs.push_back(ctx->ring_days());
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 1e300;
+  int best_th = th0, best_ch = ch0, trials = 0;
+  for (int th : ths) {
+    if (wg_launch_shape(ctx, th, 0) != WG_OK) continue;   // does not fit the device
+    for (int ch : chs) {
+      if (ch > trial_steps && ch != chs.front()) continue;   // a chunk longer than the trial says nothing
+      ctx->chunk_steps = ch;
+      st = snapshot_restore(ctx);
+      if (st != WG_OK) break;
+      cudaEventRecord(e0, ctx->stream);
+      st = wg_run_steps(ctx, doy0, fday0, ndays, t_begin, t_begin + trial_steps);
+      cudaEventRecord(e1, ctx->stream);
+      if (st != WG_OK) break;
+      st = wg_synchronize(ctx);
+      if (st != WG_OK) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ++trials;
+      if (ms < best) {
+        best = ms;
+        best_th = th;
+        best_ch = ch;
+      }
+    }
+    if (st != WG_OK) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  wg_status st2 = snapshot_restore(ctx);
+  if (st == WG_OK) st = st2;
+  if (st == WG_OK) st = wg_synchronize(ctx);
+  if (st != WG_OK || trials == 0) {
+    wg_launch_shape(ctx, th0, bl0);
+    ctx->chunk_steps = ch0;
+    return st != WG_OK ? st : WG_ERR_UNSUPPORTED;
+  }
+  wg_launch_shape(ctx, best_th, 0);
+  ctx->chunk_steps = best_ch;
+  out->threads = best_th;
+  int32_t mb = 0;
+  wg_get_launch_shape(ctx, &tmp, &out->blocks, &mb);
+  out->chunk_steps = best_ch;
+  out->ms_per_step = best / trial_steps;
+  out->trials = trials;
+  return WG_OK;
+}
+
+wg_status wg_graph_capture(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin, int32_t t_end) {
+  if (!ctx) return WG_ERR_INVALID;
+  const int total = ndays + ctx->topo.nlevel - 1;
+  if (doy0 < 1 || doy0 > 365 || fday0 < 0 || ndays <= 0 || fday0 + ndays > ctx->max_days || t_begin < 0 ||
+      t_end > total || t_begin >= t_end)
+    return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  ctx->graph_exec = nullptr;
+  ctx->graph = nullptr;
+  const int64_t l0 = ctx->launches;
+  const bool timing = ctx->timing;
+  ctx->timing = false;   // no timing events inside the graph
+  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    ctx->timing = timing;
+    return fail(ctx, e, "graph capture");
+  }
+  st = wg_run_steps(ctx, doy0, fday0, ndays, t_begin, t_end);
+  ctx->timing = timing;
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->graph_launches = (int)(ctx->launches - l0);
+  ctx->launches = l0;   // captured, not run
+  if (st != WG_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess) return fail(ctx, e, "graph capture");
+  e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(ctx, e, "graph instantiate");
+  }
+  ctx->graph = g;
+  return WG_OK;
+}
+
+wg_status wg_graph_launch(wg_ctx *ctx) {
+  if (!ctx || !ctx->graph_exec) return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  ctx->launches += ctx->graph_launches;
+  return fail(ctx, cudaGraphLaunch(ctx->graph_exec, ctx->stream), "graph launch");
+}
+
+}  // extern "C"

@@ -28,7 +28,10 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_get_member_state", "wg_upload_forcing", "wg_step_vertical", "wg_step_routing", "wg_run_days",
            "wg_get_discharge", "wg_get_balance", "wg_reset_balance", "wg_synchronize", "wg_launch_shape",
            "wg_get_launch_shape", "wg_num_levels", "wg_launch_count", "wg_last_error", "wg_status_string",
-           "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc")
+           "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc",
+           "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
+           "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
+           "wg_get_kernel_times")
 
 
 class WgError(RuntimeError):
@@ -43,6 +46,11 @@ class _Region(ctypes.Structure):
 
 class _StateView(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name, _, _ in STATE_FIELDS]
+
+
+class _TuneResult(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int32), ("blocks", ctypes.c_int32), ("chunk_steps", ctypes.c_int32),
+                ("trials", ctypes.c_int32), ("ms_per_step", ctypes.c_double)]
 
 
 class _Options(ctypes.Structure):
@@ -95,12 +103,26 @@ def load_library(path: str = LIB_PATH):
     lib.wg_last_error.restype = ctypes.c_char_p
     lib.wg_measure_fp64_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     lib.wg_measure_fp64_peak.restype = ctypes.c_int
+    lib.wg_kernel_timing.argtypes = [vp, i32]
+    lib.wg_get_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(i32)]
+    lib.wg_set_calib_param.argtypes = [vp, i32, vp]
+    lib.wg_save_snapshot.argtypes = [vp]
+    lib.wg_restore_snapshot.argtypes = [vp]
+    lib.wg_set_chunk_steps.argtypes = [vp, i32]
+    lib.wg_get_chunk_steps.argtypes = [vp]
+    lib.wg_get_chunk_steps.restype = i32
+    lib.wg_autotune.argtypes = [vp, i32, i32, i32, i32, i32, ctypes.POINTER(_TuneResult)]
+    lib.wg_graph_capture.argtypes = [vp, i32, i32, i32, i32, i32]
+    lib.wg_graph_launch.argtypes = [vp]
     lib.wg_status_string.argtypes = [ctypes.c_int]
     lib.wg_status_string.restype = ctypes.c_char_p
     for name in ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_member_state",
                  "wg_get_member_state", "wg_upload_forcing", "wg_step_vertical", "wg_step_routing", "wg_run_days",
                  "wg_get_discharge", "wg_get_balance", "wg_reset_balance", "wg_synchronize", "wg_launch_shape",
-                 "wg_get_launch_shape"):
+                 "wg_get_launch_shape", "wg_set_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
+                 "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
+                 "wg_get_kernel_times"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -260,6 +282,58 @@ class Model:
         self._check(self.lib.wg_get_launch_shape(self.h, ctypes.byref(t), ctypes.byref(b), ctypes.byref(mb)),
                     "get_launch_shape")
         return t.value, b.value, mb.value
+
+    def set_calib_param(self, name: str, values):
+        """wg_set_calib_param for P_GAMRUN_C or P_CFA, values per cell."""
+        k = {"P_GAMRUN_C": 0, "P_CFA": 1}[name]
+        v = np.ascontiguousarray(values, np.float64)
+        assert v.shape == (self.region.ncell,)
+        self._check(self.lib.wg_set_calib_param(self.h, k, _ptr(v)), "set_calib_param")
+
+    def vinline_fraction(self) -> float:
+        """Fraction of cells whose vertical balance runs inside the wavefront (a water
+        body, or no land outside the water bodies) -- the rule of wg_create."""
+        r = self.region
+        wb = (r.loc_lake > 0) | (r.loc_wetl > 0) | (r.lake_area > 0) | (r.res_area > 0) | (r.glo_wetl > 0)
+        l0 = r.contfreq - (r.glo_lake + r.glo_wetl + r.loc_lake + r.loc_wetl + r.glo_res)
+        return float(np.mean(wb | ~(l0 > 0)))
+
+    def kernel_timing(self, enable: bool = True):
+        self._check(self.lib.wg_kernel_timing(self.h, int(bool(enable))), "kernel_timing")
+
+    def kernel_times(self) -> dict:
+        """Summed device ms of the vertical-ahead and wavefront launches since the last call."""
+        a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+        self._check(self.lib.wg_get_kernel_times(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)),
+                    "get_kernel_times")
+        return {"vertical_ahead_ms": a.value, "wavefront_ms": b.value, "launch_pairs": n.value}
+
+    def save_snapshot(self):
+        self._check(self.lib.wg_save_snapshot(self.h), "save_snapshot")
+
+    def restore_snapshot(self):
+        self._check(self.lib.wg_restore_snapshot(self.h), "restore_snapshot")
+
+    def chunk_steps(self, steps: int | None = None) -> int:
+        """Set the wavefront steps per launch pair if given (0 = ring capacity); return the value in use."""
+        if steps is not None:
+            self._check(self.lib.wg_set_chunk_steps(self.h, int(steps)), "set_chunk_steps")
+        return int(self.lib.wg_get_chunk_steps(self.h))
+
+    def autotune(self, doy0: int, fday0: int, ndays: int, t_begin: int, trial_steps: int) -> dict:
+        """wg_autotune: pick threads per block and chunk steps on a trial window; state unchanged."""
+        r = _TuneResult()
+        self._check(self.lib.wg_autotune(self.h, int(doy0), int(fday0), int(ndays), int(t_begin), int(trial_steps),
+                                         ctypes.byref(r)), "autotune")
+        return {"threads": r.threads, "blocks": r.blocks, "chunk_steps": r.chunk_steps, "trials": r.trials,
+                "ms_per_step": r.ms_per_step}
+
+    def graph_capture(self, doy0: int, fday0: int, ndays: int, t_begin: int, t_end: int):
+        self._check(self.lib.wg_graph_capture(self.h, int(doy0), int(fday0), int(ndays), int(t_begin), int(t_end)),
+                    "graph_capture")
+
+    def graph_launch(self):
+        self._check(self.lib.wg_graph_launch(self.h), "graph_launch")
 
     def run(self, doy0: int, P, T, S, per_day: bool = False, chunk: int | None = None):
         """Convenience: upload forcing and simulate len(P) days from day-of-year doy0;

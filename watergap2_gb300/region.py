@@ -113,6 +113,18 @@ class Region:
     def param(self, name: str) -> np.ndarray:
         return self.arrays["param"].reshape(NPARAM, self.ncell)[PARAM[name]]
 
+    def with_param(self, name: str, values) -> "Region":
+        """The same region with calibration parameter ``name`` replaced (per cell)."""
+        arrays = dict(self.arrays)
+        p = self.arrays["param"].copy()
+        p.reshape(NPARAM, self.ncell)[PARAM[name]] = values
+        arrays["param"] = p
+        out = dataclasses.replace(self, arrays=arrays)
+        for k in ("lct_tables", "extras"):
+            if k in self.__dict__:
+                out.__dict__[k] = self.__dict__[k]
+        return out
+
     def with_bands(self, nband: int) -> "Region":
         """The same region with each band replicated so that the total band count is
         ``nband`` (a multiple of the current count); band order stays ascending."""
