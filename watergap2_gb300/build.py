@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libwg_gpu.so")
-SOURCES = ["wg_kernels.cu", "wg_capi.cpp", "wg_peak.cu", "wg_noalloc.cu", "wg_tune.cpp"]
+SOURCES = ["wg_kernels.cu", "wg_capi.cpp", "wg_peak.cu", "wg_noalloc.cu", "wg_tune.cpp", "wg_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
