@@ -1,5 +1,5 @@
-"""The C ABI library: builds, loads and exports every entry point of include/wg_gpu.h
-(no GPU calls)."""
+"""The C ABI library: builds, loads and exports every entry point declared in
+include/*.h (no GPU calls)."""
 import ctypes
 import os
 import re
@@ -8,11 +8,13 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "wg_gpu.h")
+MLP_HEADER = os.path.join(ROOT, "include", "wg_mlp.h")
+PATTERN = r"^\s*(?:wg_status|int32_t|int64_t|const char \*)\s*(wg_\w+)\s*\("
 
 
-def declared_symbols():
-    text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:wg_status|int32_t|int64_t|const char \*)\s*(wg_\w+)\s*\(", text, re.M)))
+def declared_symbols(header=HEADER):
+    text = open(header).read()
+    return sorted(set(re.findall(PATTERN, text, re.M)))
 
 
 @pytest.fixture(scope="module")
@@ -29,8 +31,13 @@ def test_header_declares_entry_points():
 
 
 def test_library_exports_every_declared_symbol(lib):
-    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    missing = [s for s in declared_symbols() + declared_symbols(MLP_HEADER) if not hasattr(lib, s)]
     assert not missing, missing
+
+
+def test_mlp_header_declares_its_entry_points():
+    syms = declared_symbols(MLP_HEADER)
+    assert {"wg_mlp_create", "wg_mlp_forward", "wg_mlp_gradient", "wg_mlp_train"} <= set(syms)
 
 
 def test_python_binding_covers_header():
