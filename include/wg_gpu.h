@@ -200,6 +200,10 @@ wg_status wg_get_launch_shape(const wg_ctx *ctx, int32_t *threads, int32_t *bloc
  * integrateWGHM.cpp:414-417). */
 wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values);
 
+/* Replace the per-member precipitation and gamma factors of an ensemble
+ * (as wg_options.member_prec_factor / member_gamma_factor; NULL = all 1). */
+wg_status wg_set_member_factors(wg_ctx *ctx, const float *prec_factor, const float *gamma_factor);
+
 /* Device snapshot of the model state (storages, snow bands, LAI state, land
  * fractions, the wavefront's outflow buffer and the balance sums): save, and
  * restore as often as needed -- e.g. the start state of each calibration run,

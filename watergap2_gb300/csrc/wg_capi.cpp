@@ -978,6 +978,22 @@ wg_status wg_get_balance_noalloc(wg_ctx *ctx, double out[6]) {
 }
 
 
+wg_status wg_set_member_factors(wg_ctx *ctx, const float *prec_factor, const float *gamma_factor) {
+  if (!ctx) return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  const int M = ctx->members;
+  std::vector<float> fac(2 * (size_t)M, 1.0f);
+  for (int k = 0; k < M; ++k) {
+    if (prec_factor) fac[k] = prec_factor[k];
+    if (gamma_factor) fac[M + k] = gamma_factor[k];
+    if (!(fac[k] >= 0.f) || !(fac[M + k] > 0.f)) return WG_ERR_INVALID;
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy((float *)ctx->mem.prec_factor, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice);
+  return cuda_fail(ctx, e, "set_member_factors");
+}
+
 wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values) {
   if (!ctx || !values) return WG_ERR_INVALID;
   if (k != 0 && k != 1) return WG_ERR_UNSUPPORTED;

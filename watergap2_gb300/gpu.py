@@ -31,7 +31,7 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc",
            "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
-           "wg_get_kernel_times")
+           "wg_get_kernel_times", "wg_set_member_factors")
 
 
 class WgError(RuntimeError):
@@ -107,6 +107,7 @@ def load_library(path: str = LIB_PATH):
     lib.wg_get_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                         ctypes.POINTER(i32)]
     lib.wg_set_calib_param.argtypes = [vp, i32, vp]
+    lib.wg_set_member_factors.argtypes = [vp, vp, vp]
     lib.wg_save_snapshot.argtypes = [vp]
     lib.wg_restore_snapshot.argtypes = [vp]
     lib.wg_set_chunk_steps.argtypes = [vp, i32]
@@ -122,7 +123,7 @@ def load_library(path: str = LIB_PATH):
                  "wg_get_discharge", "wg_get_balance", "wg_reset_balance", "wg_synchronize", "wg_launch_shape",
                  "wg_get_launch_shape", "wg_set_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
                  "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
-                 "wg_get_kernel_times"):
+                 "wg_get_kernel_times", "wg_set_member_factors"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -307,6 +308,13 @@ class Model:
         self._check(self.lib.wg_get_kernel_times(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)),
                     "get_kernel_times")
         return {"vertical_ahead_ms": a.value, "wavefront_ms": b.value, "launch_pairs": n.value}
+
+    def set_member_factors(self, prec_factor=None, gamma_factor=None):
+        pf = None if prec_factor is None else np.ascontiguousarray(prec_factor, np.float32)
+        gf = None if gamma_factor is None else np.ascontiguousarray(gamma_factor, np.float32)
+        for a in (pf, gf):
+            assert a is None or a.shape == (self.members,)
+        self._check(self.lib.wg_set_member_factors(self.h, _ptr(pf), _ptr(gf)), "set_member_factors")
 
     def save_snapshot(self):
         self._check(self.lib.wg_save_snapshot(self.h), "save_snapshot")
