@@ -10,6 +10,7 @@ class FakeProblem:
     def __init__(self, a, b, target):
         self.a, self.b, self.target_q = a, b, target
         self.static = np.zeros((a.size, 9), np.float32)
+        self.pvol = np.full(a.size, 20.0)
         self.calls = 0
         self.call_seconds = 0.0
 
@@ -99,3 +100,12 @@ def test_learned_driver_falls_back_when_proposals_do_not_help():
     missed_first = cal.rel_err(p.simulate(np.ones(50), np.ones(50)), p.target_q) >= cal.TOL
     assert res["fallback"][missed_first].all()
     assert (err < cal.TOL).mean() > 0.9
+
+
+def test_secant_refinement_without_network_beats_bisection_on_a_smooth_model():
+    p = _problem(n=200, seed=3)
+    bis = cal.calibrate_bisection(p)
+    p2 = _problem(n=200, seed=3)
+    sec = cal.calibrate_learned(p2, None)
+    assert (cal.rel_err(sec["q"], p2.target_q) < cal.TOL).mean() >= (cal.rel_err(bis["q"], p.target_q) < cal.TOL).mean() - 0.01
+    assert sec["calls"].mean() < bis["calls"].mean()

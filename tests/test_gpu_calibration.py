@@ -12,8 +12,10 @@ pytestmark = pytest.mark.gpu
 def test_learned_calibration_needs_fewer_model_calls():
     from watergap2_gb300.calibration import run_workload
     out = run_workload(nbasin=80, lo=20, hi=400, ndays=730, epochs=60, seed=17)
-    bis, lrn = out["bisection"], out["learned"]
-    print({k: out[k] for k in ("basins", "cells", "training_runs", "train_loss")}, bis, lrn)
+    bis, lrn, sec = out["bisection"], out["learned"], out["secant_without_network"]
+    print({k: out[k] for k in ("basins", "cells", "training_runs", "train_loss")}, bis, sec, lrn)
     assert bis["within_1pct"] >= 0.9
     assert lrn["within_1pct"] >= bis["within_1pct"] - 0.02
     assert lrn["calls_per_basin_mean"] < 0.8 * bis["calls_per_basin_mean"]
+    # the network's own share of the gain: its first step beats the reference's first move
+    assert lrn["calls_per_basin_mean"] < sec["calls_per_basin_mean"]

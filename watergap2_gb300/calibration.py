@@ -40,6 +40,7 @@ class Problem:
     true_gamma: np.ndarray
     true_cfa: np.ndarray
     ndays: int
+    pvol: np.ndarray = None   # [nbasin] mean precipitation volume per day over the basin
     calls: int = 0
     call_seconds: float = 0.0
 
@@ -82,12 +83,23 @@ def basin_statics(basins, P, T, S) -> np.ndarray:
                      mean(r.lai_max.astype(float)) / 6.0, mean(wb), mean(arid), mean(sw) / 300.0], axis=1)
 
 
-def step_inputs(static, gamma, cfa, q, q_target) -> np.ndarray:
-    """Network inputs of one proposal: statics, the current point, and the log
-    ratio of target to current discharge."""
-    ratio = np.clip(np.log(np.maximum(q_target, 1e-30) / np.maximum(q, 1e-30)), -5.0, 5.0)
-    return np.concatenate([static, np.stack([np.log(gamma) / np.log(50.0), np.log(cfa), ratio], axis=1)],
-                          axis=1).astype(np.float32)
+def basin_precip_volume(basins, P) -> np.ndarray:
+    """Mean daily precipitation volume of each basin (mm x km2 x 1e-6 = km3), the
+    scale of its discharge."""
+    r = basins.region
+    v = P.mean(axis=0)[basins.source_cell].astype(np.float64) * r.area_km2.astype(np.float64) * 1e-6
+    return np.bincount(basins.basin_of_cell, weights=v)
+
+
+def step_inputs(static, gamma, cfa, q, q_target, pvol) -> np.ndarray:
+    """Network inputs of one proposal: statics, the current point, the runoff
+    ratios of the current and of the target discharge, and their log ratio."""
+    qc, qt = np.maximum(q, 1e-30), np.maximum(q_target, 1e-30)
+    ratio = np.clip(np.log(qt / qc), -5.0, 5.0)
+    rc = np.clip(np.log(qc / pvol), -10.0, 2.0) / 5.0
+    rt = np.clip(np.log(qt / pvol), -10.0, 2.0) / 5.0
+    dyn = np.stack([np.log(gamma) / np.log(50.0), np.log(cfa), ratio, rc, rt], axis=1)
+    return np.concatenate([static, dyn], axis=1).astype(np.float32)
 
 
 def rel_err(q, q_target):
@@ -197,35 +209,62 @@ def calibrate_bisection(prob: Problem, gamma0=1.0, max_calls=60):
 
 
 # --------------------------------------------------------- learned proposals
-def calibrate_learned(prob: Problem, net, gamma0=1.0, max_proposals=3, max_calls=60):
-    """Start at (gamma0, 1).  The network proposes (dlog gamma, dlog CFA) from the
-    basin statics, the current point and log(Qtarget / Q); the plain model runs
-    every proposal.  Within 1 %: done.  Closer than the current point: it
-    becomes the current point, and the network proposes again (at most
-    max_proposals times).  Not closer, or proposals used up: the basin falls
-    back to bisection started from its current point."""
+def _secant(pts, q_target):
+    """Next (gamma, CFA) from the last two points, secant in (log gamma, log Q / CFA)
+    (discharge scales with CFA); gamma beyond its range goes to the limit and CFA
+    takes the remaining factor.  None when the two points do not define a slope."""
+    (g1, c1, q1), (g2, c2, q2) = pts[-2], pts[-1]
+    if q1 <= 0 or q2 <= 0 or g1 == g2:
+        return None
+    x1, x2 = np.log(g1), np.log(g2)
+    y1, y2 = np.log(q1 / c1), np.log(q2 / c2)
+    m = (y2 - y1) / (x2 - x1)
+    if not np.isfinite(m) or abs(m) < 1e-6:
+        return None
+    yt = np.log(q_target / c2)
+    x3 = x2 + (yt - y2) / m
+    lo, hi = np.log(GAMMA_LO), np.log(GAMMA_HI)
+    if lo <= x3 <= hi:
+        return float(np.exp(x3)), c2
+    xb = min(max(x3, lo), hi)
+    q_b = np.exp(y2 + m * (xb - x2)) * c2       # predicted discharge at the limit, CFA c2
+    return float(np.exp(xb)), float(np.clip(c2 * q_target / q_b, CFA_LO, CFA_HI))
+
+
+def calibrate_learned(prob: Problem, net=None, gamma0=1.0, max_refine=4, max_calls=60):
+    """Start at (gamma0, 1).  First step: the network's proposal (dlog gamma,
+    dlog CFA) from the basin statics, the current point and the target -- or,
+    without a network, the reference's first move (gamma to the limit on the side
+    of the error).  Then secant steps on the plain model's own responses.  Every
+    point is a plain-model run; within 1 %: done.  A step that does not bring the
+    basin closer, or max_refine secant steps without success: the basin falls
+    back to bisection started from its best point."""
     n = prob.nbasin
     tq = prob.target_q
-    cur_g, cur_c = np.full(n, float(gamma0)), np.ones(n)
-    cur_q = prob.simulate(cur_g, cur_c)
+    pvol = prob.pvol if prob.pvol is not None else np.ones(n)
+    g0, c0 = np.full(n, float(gamma0)), np.ones(n)
+    q0 = prob.simulate(g0, c0)
     calls = np.ones(n, np.int64)
-    q_final = cur_q.copy()
-    done = rel_err(cur_q, tq) < TOL
+    q_final = q0.copy()
+    pts = [[(g0[i], 1.0, q0[i])] for i in range(n)]
+    best = [0] * n
+    done = rel_err(q0, tq) < TOL
     fallback = np.zeros(n, bool)
-    proposals = np.zeros(n, np.int64)
+    refine = np.zeros(n, np.int64)
     bis = [None] * n
-    nxt_g, nxt_c = cur_g.copy(), cur_c.copy()
+    nxt_g, nxt_c = g0.copy(), c0.copy()
+    # first step for every basin not yet within 1 %
+    first = ~done
+    if net is not None and first.any():
+        y = net.forward(step_inputs(prob.static[first], g0[first], c0[first], q0[first], tq[first],
+                                    pvol[first]))[:, :2]
+        nxt_g[first] = np.clip(g0[first] * np.exp(y[:, 0]), GAMMA_LO, GAMMA_HI)
+        nxt_c[first] = np.clip(c0[first] * np.exp(y[:, 1]), CFA_LO, CFA_HI)
+    else:
+        nxt_g[first] = np.where(q0[first] > tq[first], GAMMA_HI, GAMMA_LO)
     for _ in range(max_calls):
         if done.all():
             break
-        prop = ~done & ~fallback
-        if prop.any():
-            y = net.forward(step_inputs(prob.static[prop], cur_g[prop], cur_c[prop], cur_q[prop], tq[prop]))[:, :2]
-            nxt_g[prop] = np.clip(cur_g[prop] * np.exp(y[:, 0]), GAMMA_LO, GAMMA_HI)
-            nxt_c[prop] = np.clip(cur_c[prop] * np.exp(y[:, 1]), CFA_LO, CFA_HI)
-            proposals[prop] += 1
-        for i in np.nonzero(~done & fallback)[0]:
-            nxt_g[i], nxt_c[i] = bis[i].gamma, bis[i].cfa
         active = ~done
         q = prob.simulate(nxt_g, nxt_c)
         calls[active] += 1
@@ -235,25 +274,32 @@ def calibrate_learned(prob: Problem, net, gamma0=1.0, max_proposals=3, max_calls
             if fallback[i]:
                 bis[i].update(q[i], tq[i])
                 done[i] = err[i] < TOL or bis[i].done
+                if not done[i]:
+                    nxt_g[i], nxt_c[i] = bis[i].gamma, bis[i].cfa
                 continue
+            pts[i].append((nxt_g[i], nxt_c[i], q[i]))
             if err[i] < TOL:
                 done[i] = True
                 continue
-            improved = err[i] < rel_err(cur_q[i], tq[i])
-            if improved:
-                cur_g[i], cur_c[i], cur_q[i] = nxt_g[i], nxt_c[i], q[i]
-            if not improved or proposals[i] >= max_proposals:
+            gb, cb, qb = pts[i][best[i]]
+            if err[i] < rel_err(qb, tq[i]):
+                best[i] = len(pts[i]) - 1
+            nxt = _secant(pts[i], tq[i]) if refine[i] < max_refine else None
+            if nxt is None or (err[i] >= rel_err(qb, tq[i]) and len(pts[i]) > 2):
+                gb, cb, qb = pts[i][best[i]]
                 fallback[i] = True
-                b = Bisection(cur_g[i])
-                b.cfa = cur_c[i]
-                b.update(cur_q[i], tq[i])     # the start point's run is already known
-                bis[i] = b
-                done[i] = b.done
-                q_final[i] = cur_q[i]
-    final_g = np.array([bis[i].gamma if fallback[i] else nxt_g[i] for i in range(n)])
-    final_c = np.array([bis[i].cfa if fallback[i] else nxt_c[i] for i in range(n)])
-    return {"gamma": final_g, "cfa": final_c, "calls": calls, "fallback": fallback, "proposals": proposals,
-            "q": q_final}
+                bis[i] = Bisection(gb)
+                bis[i].cfa = cb
+                bis[i].update(qb, tq[i])     # the start point's run is already known
+                q_final[i] = qb
+                done[i] = bis[i].done
+                nxt_g[i], nxt_c[i] = bis[i].gamma, bis[i].cfa
+            else:
+                refine[i] += 1
+                nxt_g[i], nxt_c[i] = nxt
+    final_g = np.array([bis[i].gamma if fallback[i] else pts[i][-1][0] for i in range(n)])
+    final_c = np.array([bis[i].cfa if fallback[i] else pts[i][-1][1] for i in range(n)])
+    return {"gamma": final_g, "cfa": final_c, "calls": calls, "fallback": fallback, "q": q_final}
 
 
 # ------------------------------------------------------------- the workload
@@ -296,7 +342,7 @@ def training_runs(basins, P_src, T_src, S_src, ndays, launches_a=20, launches_b=
     return np.concatenate(G, 1), np.concatenate(C, 1), np.concatenate(Q, 1)
 
 
-def training_pairs(static, G, C, Q, pairs_per_basin=400, seed=62):
+def training_pairs(static, pvol, G, C, Q, pairs_per_basin=400, seed=62):
     """(inputs, steps): from run r1 of a basin to run r2 of the same basin, the
     step (dlog gamma, dlog CFA) given log(Q_r2 / Q_r1)."""
     rng = np.random.default_rng(seed)
@@ -306,7 +352,7 @@ def training_pairs(static, G, C, Q, pairs_per_basin=400, seed=62):
     r2 = rng.integers(0, R, bi.size)
     ok = (r1 != r2) & (Q[bi, r1] > 0) & (Q[bi, r2] > 0)
     bi, r1, r2 = bi[ok], r1[ok], r2[ok]
-    x = step_inputs(static[bi], G[bi, r1], C[bi, r1], Q[bi, r1], Q[bi, r2])
+    x = step_inputs(static[bi], G[bi, r1], C[bi, r1], Q[bi, r1], Q[bi, r2], pvol[bi])
     y = np.stack([np.log(G[bi, r2] / G[bi, r1]), np.log(C[bi, r2] / C[bi, r1])], 1).astype(np.float32)
     return x, y
 
@@ -333,12 +379,13 @@ def run_workload(nbasin=1000, lo=20, hi=20000, ndays=730, seed=71, device=0, epo
     bs = bmod.cut_basins(src_region, nbasin=nbasin, lo=lo, hi=hi, seed=seed)
     P, T, S = sy.forcing(src_region, ndays, seed=seed + 1, doy0=1)
     static = basin_statics(bs, P, T, S)
+    pvol = basin_precip_volume(bs, P)
     say(f"basins: {bs.nbasin}, cells {bs.region.ncell}")
     # training set: 200 runs per basin (25 launches x 8 members)
     t0 = time.perf_counter()
     G, C, Q = training_runs(bs, P, T, S, ndays, device=device)
     t_runs = time.perf_counter() - t0
-    x, y = training_pairs(static, G, C, Q)
+    x, y = training_pairs(static, pvol, G, C, Q)
     say(f"training runs: {G.shape[1]} per basin in {t_runs:.1f} s; pairs {x.shape[0]}")
     t0 = time.perf_counter()
     net = Mlp(device=device, seed=seed)
@@ -353,13 +400,14 @@ def run_workload(nbasin=1000, lo=20, hi=20000, ndays=730, seed=71, device=0, epo
     upload_basin_forcing(model, bs, P, T, S)
     model.save_snapshot()
     prob = Problem(basins=bs, model=model, static=static, target_q=np.zeros(bs.nbasin), true_gamma=g_true,
-                   true_cfa=c_true, ndays=ndays)
+                   true_cfa=c_true, ndays=ndays, pvol=pvol)
     prob.target_q = prob.simulate(g_true, c_true)
     out = {"basins": int(bs.nbasin), "cells": int(bs.region.ncell),
            "basin_cells": {"min": int(bs.sizes.min()), "mean": float(bs.sizes.mean()), "max": int(bs.sizes.max())},
            "days_per_call": ndays, "training_runs": int(G.size), "training_pairs": int(x.shape[0]),
            "training_runs_s": t_runs, "train_s": t_train, "train_loss": loss}
     for name, fn in (("bisection", lambda: calibrate_bisection(prob)),
+                     ("secant_without_network", lambda: calibrate_learned(prob, None)),
                      ("learned", lambda: calibrate_learned(prob, net))):
         prob.calls, prob.call_seconds = 0, 0.0
         t0 = time.perf_counter()
