@@ -25,6 +25,8 @@ from __future__ import annotations
 import heapq
 import math
 
+import os
+
 import numpy as np
 
 from .region import NLCT, NPARAM, PARAM, Region
@@ -493,3 +495,62 @@ def forcing(region: Region, ndays: int, seed: int = 2, doy0: int = 1, day_offset
         sw = 175.0 + 125.0 * np.sin(2 * np.pi * (doy - 80) / 365.0)[:, None] * swamp[None, :]
         S[d] = np.clip(sw + noise_s[j], 50.0, 300.0)
     return P, T, S
+
+
+def _forcing_chunk(args):
+    """Worker of forcing_parallel: cells [c0, c1) of year block blk into shared memory."""
+    from multiprocessing import shared_memory
+    name, n, c0, c1, seed, blk, lat, tmean_global = args
+    shm = shared_memory.SharedMemory(name=name)
+    try:
+        out = np.ndarray((3, 365, n), np.float32, buffer=shm.buf)
+        m = c1 - c0
+        rng = np.random.default_rng((seed, blk, c0))
+        u = rng.uniform(size=(365, m))
+        amount = rng.gamma(0.8, 8.0, (365, m))
+        noise_t = rng.normal(0.0, 3.0, (365, m))
+        noise_s = rng.normal(0.0, 10.0, (365, m))
+        hemi = np.where(lat >= 0, 1.0, -1.0)
+        tmean = 10.0 + 14.0 * (1.0 - np.abs(lat) / 45.0) if tmean_global else np.full(m, 10.0)
+        swamp = np.clip(np.abs(lat) / 30.0, 0.3, 1.0) * hemi
+        doy = np.arange(1, 366)
+        out[0, :, c0:c1] = np.where(u >= 0.6, amount, 0.0)
+        season = np.sin(2 * np.pi * doy / 365.0)[:, None] * hemi[None, :]
+        out[1, :, c0:c1] = tmean[None, :] + 12.0 * season + noise_t
+        sw = 175.0 + 125.0 * np.sin(2 * np.pi * (doy - 80) / 365.0)[:, None] * swamp[None, :]
+        out[2, :, c0:c1] = np.clip(sw + noise_s, 50.0, 300.0)
+    finally:
+        shm.close()
+
+
+def forcing_year_parallel(region: Region, year: int, seed: int = 2, procs: int | None = None, chunk: int = 65536,
+                          consume=None):
+    """One year (day-of-year 1..365) of forcing [3, 365, ncell] float32 for large
+    grids: the distributions of forcing(), with cells split into chunks that
+    spawned workers generate in parallel into shared memory, each chunk from its
+    own generator keyed by (seed, year, first cell).  The same numbers for any
+    worker count.  With consume, the shared array is handed to consume(array)
+    instead of being copied out (for grids whose year of forcing is many GB);
+    call from a script whose main module can be re-imported (spawned workers)."""
+    import multiprocessing as mp
+    from multiprocessing import shared_memory
+    n = region.ncell
+    shm = shared_memory.SharedMemory(create=True, size=3 * 365 * n * 4)
+    try:
+        lat = region.lat_deg
+        glob = region.name in ("region_global", "region_5min")
+        jobs = [(shm.name, n, c0, min(n, c0 + chunk), seed, year, lat[c0:min(n, c0 + chunk)], glob)
+                for c0 in range(0, n, chunk)]
+        with mp.get_context("spawn").Pool(procs or min(len(jobs), os.cpu_count() or 1)) as pool:
+            pool.map(_forcing_chunk, jobs)
+        view = np.ndarray((3, 365, n), np.float32, buffer=shm.buf)
+        if consume is not None:
+            consume(view)
+            out = None
+        else:
+            out = view.copy()
+        del view
+    finally:
+        shm.close()
+        shm.unlink()
+    return out
