@@ -217,6 +217,8 @@ def _secant(pts, q_target):
     if q1 <= 0 or q2 <= 0 or g1 == g2:
         return None
     x1, x2 = np.log(g1), np.log(g2)
+    if x1 == x2:
+        return None
     y1, y2 = np.log(q1 / c1), np.log(q2 / c2)
     m = (y2 - y1) / (x2 - x1)
     if not np.isfinite(m) or abs(m) < 1e-6:
