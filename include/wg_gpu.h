@@ -137,6 +137,15 @@ wg_status wg_get_member_state(wg_ctx *ctx, int32_t member, wg_state_view *state)
  * into forcing slots [day0, day0+ndays) of the device buffer. */
 wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec,
                             const float *temp, const float *swrad);
+/* The same upload on the context's copy stream, overlapped with runs already
+ * queued: it waits only for earlier uploads, and later runs and steps wait for
+ * it.  The caller guarantees that the days it writes are not read by runs still
+ * in flight (e.g. next year's forcing while this year runs) and keeps pinned
+ * source arrays unchanged until the next wg_synchronize.  No counterpart in the
+ * reference (it reads each year's forcing before the year's day loop,
+ * climateYear.cpp:38-79). */
+wg_status wg_upload_forcing_async(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec, const float *temp,
+                                  const float *swrad);
 
 /* One day, the reference's call granularity: the vertical balance of every cell
  * (the OpenMP calcNewDay loop, source/integrateWGHM.cpp:767-783) for day of year

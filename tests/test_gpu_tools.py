@@ -92,3 +92,25 @@ def test_ensemble_autotune_and_graph():
     m.graph_capture(150, 0, nd, 0, total)
     m.graph_launch()
     assert np.array_equal(m.discharge(0, nd), q_ref)
+
+
+def test_overlapped_uploads_give_the_same_run():
+    """Year-by-year forcing on the copy stream, each year uploaded while the
+    previous one runs, equals the run with all forcing uploaded first."""
+    from watergap2_gb300.gpu import Model
+    region, (P, T, S) = _region_and_forcing(25, 3 * 365)
+    ref = Model(region, max_days=3 * 365)
+    ref.upload_forcing(0, P, T, S)
+    total = ref.num_steps(3 * 365)
+    ref.run_steps(1, 0, 3 * 365, 0, total)
+    q_ref = ref.discharge(0, 3 * 365)
+
+    m = Model(region, max_days=3 * 365)
+    m.upload_forcing(0, P[:365], T[:365], S[:365])
+    for y in range(3):
+        m.run_steps(1, 0, 3 * 365, 365 * y, 365 * (y + 1))
+        if y < 2:
+            sl = slice(365 * (y + 1), 365 * (y + 2))
+            m.upload_forcing(365 * (y + 1), P[sl], T[sl], S[sl], overlap=True)
+    m.run_steps(1, 0, 3 * 365, 3 * 365, total)
+    assert np.array_equal(m.discharge(0, 3 * 365), q_ref)

@@ -84,7 +84,65 @@ wg_status reference_rout_order(int n, const int32_t *down, std::vector<int32_t> 
 // step barrier.  The order of slots changes nothing in the results: each cell's
 // inputs are addressed through its slot, and inflows are summed in the upstream
 // lists' routing order.
-wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, const uint32_t *cls, Topology &t) {
+// Warp placement for the single-member wavefront layout: blocks of
+// cell_warps warps of cells plus one idle warp (warps_per_block in all).  Warp
+// w of a block issues on SM sub-partition w % 4, and the FP64 work between two
+// step barriers is the sum over a sub-partition's warps, so the one idle warp
+// leaves one sub-partition per block with fewer warps; a water-body warp
+// (about three times the FP64 work of a plain one) goes there, and plain warps
+// fill the rest.  Greedy: each water-body warp to the sub-partition whose
+// predicted load (its water-body warps plus one per remaining position) is
+// lowest; plain warps keep their class-sorted order.  The partial last warp
+// stays at the last position so that slots stay dense.
+void place_warps(const std::vector<int32_t> &seq, const uint32_t *cls, int n, const WarpLayout &lay,
+                 std::vector<int32_t> &worder) {
+  const int W = (n + 31) / 32, wfull = n / 32, cw = lay.cell_warps;
+  // positions p = block * cw + weff, p < W; sub-partition of each
+  std::vector<int> smsp(W);
+  for (int p = 0; p < W; ++p) {
+    const int weff = p % cw;
+    const int w = weff < lay.idle_warp ? weff : weff + 1;
+    smsp[p] = w & 3;
+  }
+  const int nbucket = ((W + cw - 1) / cw) * 4;
+  std::vector<std::vector<int>> free_pos(nbucket);
+  for (int p = wfull - 1; p >= 0; --p) free_pos[(p / cw) * 4 + smsp[p]].push_back(p);   // ascending when popped
+  std::vector<int> heavy_cost(nbucket, 0);
+  std::vector<int> heavy, light;
+  for (int w = 0; w < wfull; ++w) {
+    bool h = false;
+    for (int j = w * 32; j < w * 32 + 32 && !h; ++j) h = cls && cls[seq[j]] != 0u;
+    (h ? heavy : light).push_back(w);
+  }
+  const int kHeavy = 3;
+  std::vector<int> placed(wfull, -1);
+  std::vector<uint8_t> used(W, 0);
+  for (int w : heavy) {
+    int best = -1;
+    long long best_load = 0;
+    for (int b = 0; b < nbucket; ++b) {
+      if (free_pos[b].empty()) continue;
+      const long long load = heavy_cost[b] + kHeavy + (long long)(free_pos[b].size() - 1);
+      if (best < 0 || load < best_load) {
+        best = b;
+        best_load = load;
+      }
+    }
+    const int p = free_pos[best].back();
+    free_pos[best].pop_back();
+    heavy_cost[best] += kHeavy;
+    placed[w] = p;
+    used[p] = 1;
+  }
+  size_t li = 0;
+  for (int p = 0; p < wfull; ++p)
+    if (!used[p]) placed[light[li++]] = p;
+  for (int w = 0; w < wfull; ++w) worder[placed[w]] = w;
+  if (W > wfull) worder[W - 1] = W - 1;
+}
+
+wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, const uint32_t *cls,
+                         const WarpLayout *lay, Topology &t) {
   for (int i = 0; i < n; ++i)
     if (down[i] < -1 || down[i] >= n || down[i] == i) return WG_ERR_TOPOLOGY;
   std::vector<int32_t> order;
@@ -130,13 +188,17 @@ wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, 
     wcls[w] = cls ? cls[seq[(size_t)w * 32]] : 0u;
     if (w < wfull) count[wcls[w]]++;
   }
-  std::map<uint32_t, int> seen;
-  std::vector<std::pair<double, int>> key(wfull);
-  for (int w = 0; w < wfull; ++w) key[w] = {(seen[wcls[w]]++ + 0.5) / count[wcls[w]], w};
-  std::stable_sort(key.begin(), key.end());
   std::vector<int32_t> worder(W);
-  for (int k = 0; k < wfull; ++k) worder[k] = key[k].second;
-  if (W > wfull) worder[W - 1] = W - 1;
+  if (lay && lay->idle_warp >= 0) {
+    place_warps(seq, cls, n, *lay, worder);
+  } else {
+    std::map<uint32_t, int> seen;
+    std::vector<std::pair<double, int>> key(wfull);
+    for (int w = 0; w < wfull; ++w) key[w] = {(seen[wcls[w]]++ + 0.5) / count[wcls[w]], w};
+    std::stable_sort(key.begin(), key.end());
+    for (int k = 0; k < wfull; ++k) worder[k] = key[k].second;
+    if (W > wfull) worder[W - 1] = W - 1;
+  }
   t.cell_of_slot.resize(n);
   t.slot_of_cell.resize(n);
   int slot = 0;
@@ -216,22 +278,50 @@ wg_status cuda_fail(wg_ctx *ctx, cudaError_t e, const char *what) {
   return e == cudaErrorMemoryAllocation ? WG_ERR_NOMEM : WG_ERR_CUDA;
 }
 
+// Runs on the context's stream wait for the overlapped forcing uploads.
+void join_uploads(wg_ctx *ctx) {
+  if (ctx->upload_pending) {
+    cudaStreamWaitEvent(ctx->stream, ctx->upload_done, 0);
+    ctx->upload_pending = false;
+  }
+}
+
 bool valid_block_threads(int threads) { return threads >= 32 && threads <= kMaxBlockThreads && threads % 32 == 0; }
 
-// Single-member contexts: one block per SM holding an equal share of the cells
-// (whole warps), so that every SM carries the same work between step barriers;
-// 256 when the cells do not fit one block per SM or the block does not fit an SM.
-int default_block_threads(wg_ctx *ctx) {
+// Single-member contexts: one block per SM with an equal share of the cells in
+// whole warps plus one idle warp (see place_warps), so that every SM and every
+// SM sub-partition carries about the same FP64 work between step barriers.
+// No layout (idle_warp < 0) when the cells do not fit one block per SM or the
+// block does not fit an SM.
+WarpLayout default_layout(wg_ctx *ctx) {
+  WarpLayout lay;
   int nsm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
-  if (nsm <= 0) return 256;
-  const size_t per_sm = (ctx->nstate() + nsm - 1) / nsm;
-  if (per_sm > (size_t)kMaxBlockThreads) return 256;
-  const int th = std::max(64, (int)((per_sm + 31) / 32 * 32));
-  const int need = (int)((ctx->nstate() + th - 1) / th);
-  const int fits = ctx->precision == 0 ? pipeline_max_blocks<double>(true, false, th)
-                                       : pipeline_max_blocks<float>(true, false, th);
-  return fits >= need ? th : 256;
+  if (nsm <= 0) return lay;
+  const long long W = ((long long)ctx->nstate() + 31) / 32;
+  const int cw = (int)std::max<long long>(2, (W + nsm - 1) / nsm);
+  const int wpb = cw + 1;
+  if (wpb * 32 > kMaxBlockThreads) return lay;
+  const int blocks = (int)((W + cw - 1) / cw);
+  const int fits = ctx->precision == 0 ? pipeline_max_blocks<double>(true, false, wpb * 32)
+                                       : pipeline_max_blocks<float>(true, false, wpb * 32);
+  const int fits_r = ctx->precision == 0 ? pipeline_max_blocks<double>(false, false, wpb * 32)
+                                         : pipeline_max_blocks<float>(false, false, wpb * 32);
+  if (fits < blocks || fits_r < blocks) return lay;
+  // the idle warp: the last warp of the sub-partition that has the fewest warps
+  int cnt[4] = {0, 0, 0, 0};
+  for (int w = 0; w < wpb; ++w) cnt[w & 3]++;
+  int sp = 0;
+  for (int k = 1; k < 4; ++k)
+    if (cnt[k] < cnt[sp]) sp = k;
+  int idle = -1;
+  for (int w = 0; w < wpb; ++w)
+    if ((w & 3) == sp) idle = w;
+  lay.cell_warps = cw;
+  lay.idle_warp = idle;
+  lay.blocks = blocks;
+  lay.threads = wpb * 32;
+  return lay;
 }
 
 // upload a per-cell host array (cell order) into slot order, converting to T
@@ -509,9 +599,13 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return WG_ERR_CUDA;
     ctx->own_stream = true;
   }
+  if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->upload_done, cudaEventDisableTiming) != cudaSuccess)
+    return WG_ERR_CUDA;
   std::vector<uint32_t> cls(n);
   for (int i = 0; i < n; ++i) cls[i] = work_class(r, i);
-  wg_status st = build_topology(n, r->downstream, r->rout_order, cls.data(), ctx->topo);
+  if (!opt->block_threads && ctx->members == 1) ctx->layout = default_layout(ctx.get());
+  wg_status st = build_topology(n, r->downstream, r->rout_order, cls.data(), &ctx->layout, ctx->topo);
   if (st != WG_OK) return st;
   {
     double e2[64], lf[129], inv[129];
@@ -744,9 +838,10 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   st = ctx->precision == 0 ? broadcast_state(ctx.get(), ctx->sd, &init) : broadcast_state(ctx.get(), ctx->sf, &init);
   if (st != WG_OK) return st;
   const bool ens = ctx->members > 1;
-  if (!opt->block_threads && !ens) ctx->threads = default_block_threads(ctx.get());
+  if (ctx->layout.idle_warp >= 0) ctx->threads = ctx->layout.threads;
   const int th = ctx->threads;
-  const int need = (int)std::min<size_t>((N + th - 1) / th, (size_t)1 << 30);
+  const int need = ctx->layout.idle_warp >= 0 ? ctx->layout.blocks
+                                              : (int)std::min<size_t>((N + th - 1) / th, (size_t)1 << 30);
   if (ctx->precision == 0) {
     ctx->blocks_fused = std::min(pipeline_max_blocks<double>(true, ens, th), need);
     ctx->blocks_route = std::min(pipeline_max_blocks<double>(false, ens, th), need);
@@ -792,8 +887,8 @@ wg_status wg_get_member_state(wg_ctx *ctx, int32_t member, wg_state_view *v) {
   return state_io(ctx, v, member, false);
 }
 
-wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec, const float *temp,
-                            const float *swrad) {
+static wg_status upload_forcing_on(wg_ctx *ctx, cudaStream_t st, int32_t day0, int32_t ndays, const float *prec,
+                                   const float *temp, const float *swrad) {
   if (!ctx || !prec || !temp || !swrad || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days)
     return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
@@ -804,10 +899,9 @@ wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const floa
     const int nd = std::min(ctx->staging_days, ndays - d);
     for (int k = 0; k < 3; ++k) {
       cudaError_t e = cudaMemcpyAsync(ctx->staging, src[k] + (size_t)d * n, (size_t)nd * n * sizeof(float),
-                                      cudaMemcpyHostToDevice, ctx->stream);
+                                      cudaMemcpyHostToDevice, st);
       if (e == cudaSuccess)
-        e = launch_gather_forcing(ctx->staging, dst[k] + (size_t)(day0 + d) * n, ctx->d_cell_of_slot, n, nd,
-                                  ctx->stream);
+        e = launch_gather_forcing(ctx->staging, dst[k] + (size_t)(day0 + d) * n, ctx->d_cell_of_slot, n, nd, st);
       ctx->launches++;
       if (e != cudaSuccess) return cuda_fail(ctx, e, "upload_forcing");
     }
@@ -815,10 +909,29 @@ wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const floa
   return WG_OK;
 }
 
+wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec, const float *temp,
+                            const float *swrad) {
+  if (!ctx) return WG_ERR_INVALID;
+  join_uploads(ctx);   // after the overlapped uploads, in the order of the calls
+  return upload_forcing_on(ctx, ctx->stream, day0, ndays, prec, temp, swrad);
+}
+
+wg_status wg_upload_forcing_async(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec, const float *temp,
+                                  const float *swrad) {
+  if (!ctx) return WG_ERR_INVALID;
+  wg_status st = upload_forcing_on(ctx, ctx->copy_stream, day0, ndays, prec, temp, swrad);
+  if (st != WG_OK) return st;
+  cudaError_t e = cudaEventRecord(ctx->upload_done, ctx->copy_stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "upload_forcing_async");
+  ctx->upload_pending = true;
+  return WG_OK;
+}
+
 wg_status wg_step_vertical(wg_ctx *ctx, int32_t doy, int32_t fday) {
   if (!ctx || doy < 1 || doy > 365 || fday < 0 || fday >= ctx->max_days) return WG_ERR_INVALID;
   if (ctx->members != 1) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
+  join_uploads(ctx);
   ctx->launches++;
   cudaError_t e = ctx->precision == 0
                       ? launch_vertical(ctx->cd, ctx->sd, ctx->vd, ctx->forcing, doy, fday, ctx->stream)
@@ -830,14 +943,15 @@ wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday) {
   if (!ctx || doy < 1 || doy > 365 || oday < 0 || oday >= ctx->max_days) return WG_ERR_INVALID;
   if (ctx->members != 1) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
+  join_uploads(ctx);
   ctx->launches++;
   cudaError_t e = ctx->precision == 0
                       ? launch_pipeline(false, ctx->cd, ctx->sd, ctx->vd, ctx->forcing, ctx->mem, ctx->balance,
                                         ctx->rd, ctx->sync, ctx->outq, ctx->qst, doy, 0, oday, 1, 0, ctx->topo.nlevel,
-                                        ctx->blocks_route, ctx->threads, ctx->stream)
+                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->stream)
                       : launch_pipeline(false, ctx->cf, ctx->sf, ctx->vf, ctx->forcing, ctx->mem, ctx->balance,
                                         ctx->rf, ctx->sync, ctx->outq, ctx->qst, doy, 0, oday, 1, 0, ctx->topo.nlevel,
-                                        ctx->blocks_route, ctx->threads, ctx->stream);
+                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->stream);
   return cuda_fail(ctx, e, "step_routing");
 }
 
@@ -860,7 +974,8 @@ static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevSta
     if (ev) cudaEventRecord(ev[1], ctx->stream);
     if (e == cudaSuccess)
       e = launch_pipeline(true, c, s, v, ctx->forcing, ctx->mem, ctx->balance, ring, ctx->sync, ctx->outq, ctx->qst,
-                          doy0, fday0, fday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->stream);
+                          doy0, fday0, fday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->layout,
+                          ctx->stream);
     ctx->launches++;
     if (ev) cudaEventRecord(ev[2], ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "run_steps");
@@ -876,6 +991,7 @@ wg_status wg_run_steps(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, 
   if (t_begin < 0 || t_end > total || t_begin > t_end) return WG_ERR_INVALID;
   if (t_begin == t_end) return WG_OK;
   cudaSetDevice(ctx->device);
+  join_uploads(ctx);
   return ctx->precision == 0 ? run_steps_impl(ctx, ctx->cd, ctx->sd, ctx->vd, ctx->rd, doy0, fday0, ndays, t_begin, t_end)
                              : run_steps_impl(ctx, ctx->cf, ctx->sf, ctx->vf, ctx->rf, doy0, fday0, ndays, t_begin, t_end);
 }
@@ -890,7 +1006,8 @@ wg_status wg_run_days(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays) {
 wg_status wg_synchronize(wg_ctx *ctx) {
   if (!ctx) return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
-  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
   int flag = 0;
   e = cudaMemcpy(&flag, ctx->sync.error, sizeof(int), cudaMemcpyDeviceToHost);
@@ -1012,6 +1129,7 @@ wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks) {
                                        : pipeline_max_blocks<float>(false, ens, threads);
   const int need = (int)std::min<size_t>((ctx->nstate() + threads - 1) / threads, (size_t)1 << 30);
   if (maxb <= 0 || maxr <= 0) return WG_ERR_DEVICE;
+  ctx->layout.idle_warp = -1;   // plain mapping (slot i -> thread i mod the grid)
   ctx->threads = threads;
   ctx->blocks_fused = std::min(blocks > 0 ? std::min(blocks, maxb) : maxb, need);
   ctx->blocks_route = std::min(blocks > 0 ? std::min(blocks, maxr) : maxr, need);

@@ -10,6 +10,7 @@
 
 #include "../../include/wg_gpu.h"
 #include "wg_device.h"
+#include "wg_kernels.h"
 
 using wg::DevBalance;
 using wg::DevCellsT;
@@ -19,6 +20,7 @@ using wg::DevRingT;
 using wg::DevStateT;
 using wg::DevSync;
 using wg::DevVertT;
+using wg::WarpLayout;
 
 // Drainage topology and slot order of one region (built once by wg_create).
 struct Topology {
@@ -44,8 +46,12 @@ struct wg_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaStream_t copy_stream = nullptr;      // wg_upload_forcing_async
+  cudaEvent_t upload_done = nullptr;
+  bool upload_pending = false;
   int n = 0, nband = 0, max_days = 0, nstation = 0, members = 1, precision = 0;
   int threads = 256, blocks_fused = 0, blocks_route = 0;
+  WarpLayout layout;                       // single-member wavefront layout (idle_warp < 0: none)
   Topology topo;
   DevCellsT<double> cd{};
   DevStateT<double> sd{};
@@ -90,6 +96,8 @@ struct wg_ctx {
     release_tools();
     for (void *p : allocs) cudaFree(p);
     if (own_stream && stream) cudaStreamDestroy(stream);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+    if (upload_done) cudaEventDestroy(upload_done);
   }
   template <class T>
   T *alloc(size_t count) {

@@ -204,12 +204,20 @@ template <class R, bool FUSED, bool ENS>
 __global__ void __launch_bounds__(kMaxBlockThreads) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
                                                   double *outq, double *qst, int doy0, int fday0, int oday0,
-                                                  int ndays, int t_b, int t_e) {
+                                                  int ndays, int t_b, int t_e, int cell_warps, int idle_warp) {
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const size_t N = (size_t)n * M;
-  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long gstride = (long long)gridDim.x * blockDim.x;
+  // thread -> first state index and stride: plain (i mod the grid), or the
+  // single-member layout with one idle warp per block (cell_warps warps of cells)
+  long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long gstride = (long long)gridDim.x * blockDim.x;
+  if (!ENS && idle_warp >= 0) {
+    const int warp = threadIdx.x >> 5;
+    const int weff = warp - (warp > idle_warp ? 1 : 0);
+    gtid = warp == idle_warp ? (long long)N : ((long long)blockIdx.x * cell_warps + weff) * 32 + (threadIdx.x & 31);
+    gstride = (long long)gridDim.x * cell_warps * 32;
+  }
   for (int t = t_b; t < t_e; ++t) {
     if (t - c.nlevel + 1 < ndays) {   // some cell still has a day to compute
       double *q_now = outq + (size_t)(t & 1) * N;
@@ -402,12 +410,16 @@ template <class R>
 cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
                             const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
                             const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
-                            int t_b, int t_e, int blocks, int threads, cudaStream_t st) {
+                            int t_b, int t_e, int blocks, int threads, const WarpLayout &lay, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(sync.counter, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
+  int cell_warps = lay.cell_warps, idle_warp = mem.members > 1 ? -1 : lay.idle_warp;
+  if (idle_warp >= 0 && (threads != lay.threads || (long long)blocks * cell_warps * 32 < (long long)c.n))
+    idle_warp = -1;   // the layout does not describe this launch: plain mapping
   void *args[] = {(void *)&c,    (void *)&s,    (void *)&v,     (void *)&f,     (void *)&mem,   (void *)&b,
                   (void *)&ring, (void *)&sync, (void *)&outq,  (void *)&qst,   (void *)&doy0,  (void *)&fday0,
-                  (void *)&oday0, (void *)&ndays, (void *)&t_b, (void *)&t_e};
+                  (void *)&oday0, (void *)&ndays, (void *)&t_b, (void *)&t_e, (void *)&cell_warps,
+                  (void *)&idle_warp};
   const bool ens = mem.members > 1;
   // cooperative (all blocks resident, or the launch fails) through the launch
   // attribute, which stream capture records into a graph kernel node
@@ -449,7 +461,7 @@ cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int
   template cudaError_t launch_pipeline<R>(bool, const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,  \
                                           const DevForcing &, const DevMembers &, const DevBalance &,             \
                                           const DevRingT<R> &, const DevSync &, double *, double *, int, int,     \
-                                          int, int, int, int, int, int, cudaStream_t);                            \
+                                          int, int, int, int, int, int, const WarpLayout &, cudaStream_t);        \
   template cudaError_t launch_vertical_ahead<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevForcing &,   \
                                                 const DevMembers &, const DevBalance &, const DevRingT<R> &, int,  \
                                                 int, int, int, int, int, int, cudaStream_t);                       \

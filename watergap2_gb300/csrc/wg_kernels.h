@@ -7,6 +7,16 @@
 namespace wg {
 // Largest block of the day-pipelined kernels (k_pipeline, k_vertical_ahead).
 constexpr int kMaxBlockThreads = 512;
+
+// Thread-to-slot layout of the single-member wavefront: each block runs
+// cell_warps warps of 32 consecutive slots plus one idle warp at warp index
+// idle_warp (idle_warp < 0: plain mapping, slot i on thread i mod the grid).
+struct WarpLayout {
+  int cell_warps = 0;
+  int idle_warp = -1;
+  int blocks = 0;
+  int threads = 0;
+};
 cudaError_t upload_fastmath_tables(const double exp2_tab[64], const double logF_tab[129], const double invF_tab[129]);
 cudaError_t launch_gather_forcing(const float *src, float *dst, const int32_t *cell_of_slot, int n, int ndays,
                                   cudaStream_t st);
@@ -19,7 +29,7 @@ template <class R>
 cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
                             const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
                             const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
-                            int t_b, int t_e, int blocks, int threads, cudaStream_t st);
+                            int t_b, int t_e, int blocks, int threads, const WarpLayout &lay, cudaStream_t st);
 template <class R>
 cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, const DevForcing &f,
                                   const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring, int doy0,

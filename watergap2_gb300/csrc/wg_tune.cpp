@@ -160,8 +160,9 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
   if (t_begin < 0 || t_begin + trial_steps > total) return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
   const int th0 = ctx->threads, ch0 = ctx->chunk_steps;
-  int32_t bl0 = 0, mb0 = 0, tmp = 0;
-  wg_get_launch_shape(ctx, &tmp, &bl0, &mb0);
+  const int bf0 = ctx->blocks_fused, br0 = ctx->blocks_route;
+  const WarpLayout lay0 = ctx->layout;
+  int32_t tmp = 0;
   wg_status st = snapshot_save(ctx);
   if (st != WG_OK) return st;
   // candidates: block sizes 64..512 (for ensembles: members of one cell per block,
@@ -174,9 +175,17 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   double best = 1e300;
-  int best_th = th0, best_ch = ch0, trials = 0;
+  int best_th = -1, best_ch = ch0, trials = 0;   // best_th < 0: the shape the context had
+  auto restore_shape0 = [&]() {
+    ctx->threads = th0;
+    ctx->blocks_fused = bf0;
+    ctx->blocks_route = br0;
+    ctx->layout = lay0;
+  };
+  ths.insert(ths.begin(), -1);
   for (int th : ths) {
-    if (wg_launch_shape(ctx, th, 0) != WG_OK) continue;   // does not fit the device
+    if (th < 0) restore_shape0();                          // first the context's own shape and layout
+    else if (wg_launch_shape(ctx, th, 0) != WG_OK) continue;   // does not fit the device
     for (int ch : chs) {
       if (ch > trial_steps && ch != chs.front()) continue;   // a chunk longer than the trial says nothing
       ctx->chunk_steps = ch;
@@ -205,13 +214,16 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
   if (st == WG_OK) st = st2;
   if (st == WG_OK) st = wg_synchronize(ctx);
   if (st != WG_OK || trials == 0) {
-    wg_launch_shape(ctx, th0, bl0);
+    restore_shape0();
     ctx->chunk_steps = ch0;
     return st != WG_OK ? st : WG_ERR_UNSUPPORTED;
   }
-  wg_launch_shape(ctx, best_th, 0);
+  if (best_th < 0)
+    restore_shape0();
+  else
+    wg_launch_shape(ctx, best_th, 0);
   ctx->chunk_steps = best_ch;
-  out->threads = best_th;
+  out->threads = ctx->threads;
   int32_t mb = 0;
   wg_get_launch_shape(ctx, &tmp, &out->blocks, &mb);
   out->chunk_steps = best_ch;
@@ -229,6 +241,7 @@ wg_status wg_graph_capture(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t nda
   cudaSetDevice(ctx->device);
   wg_status st = wg_synchronize(ctx);
   if (st != WG_OK) return st;
+  ctx->upload_pending = false;   // synchronised: nothing for the graph to wait on
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   ctx->graph_exec = nullptr;

@@ -31,7 +31,7 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc",
            "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
-           "wg_get_kernel_times", "wg_set_member_factors")
+           "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async")
 
 
 class WgError(RuntimeError):
@@ -82,6 +82,7 @@ def load_library(path: str = LIB_PATH):
     lib.wg_launch_shape.argtypes = [vp, i32, i32]
     lib.wg_get_launch_shape.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]
     lib.wg_upload_forcing.argtypes = [vp, i32, i32, vp, vp, vp]
+    lib.wg_upload_forcing_async.argtypes = [vp, i32, i32, vp, vp, vp]
     lib.wg_step_vertical.argtypes = [vp, i32, i32]
     lib.wg_step_routing.argtypes = [vp, i32, i32]
     lib.wg_run_days.argtypes = [vp, i32, i32, i32]
@@ -123,7 +124,7 @@ def load_library(path: str = LIB_PATH):
                  "wg_get_discharge", "wg_get_balance", "wg_reset_balance", "wg_synchronize", "wg_launch_shape",
                  "wg_get_launch_shape", "wg_set_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
                  "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
-                 "wg_get_kernel_times", "wg_set_member_factors"):
+                 "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -152,6 +153,7 @@ class Model:
         self.lib = load_library()
         self.region = region
         self._keep = []
+        self._inflight = []
         r = _Region()
         r.ncell, r.nband, r.river_velo_opt = region.ncell, region.nband, region.river_velo_opt
         r.default_velocity = region.default_velocity
@@ -207,10 +209,17 @@ class Model:
     def launch_count(self) -> int:
         return int(self.lib.wg_launch_count(self.h))
 
-    def upload_forcing(self, day0: int, P, T, S):
+    def upload_forcing(self, day0: int, P, T, S, overlap: bool = False):
+        """Forcing of len(P) days into day slots day0..; with overlap, on the copy
+        stream alongside runs in flight (wg_upload_forcing_async: the days written
+        must not be read by those runs; pinned sources stay unchanged until the
+        next synchronize)."""
         P, T, S = (np.ascontiguousarray(x, np.float32) for x in (P, T, S))
         nd = P.shape[0]
-        self._check(self.lib.wg_upload_forcing(self.h, int(day0), nd, _ptr(P), _ptr(T), _ptr(S)), "upload_forcing")
+        fn = self.lib.wg_upload_forcing_async if overlap else self.lib.wg_upload_forcing
+        if overlap:
+            self._inflight.append((P, T, S))   # alive until the next synchronize
+        self._check(fn(self.h, int(day0), nd, _ptr(P), _ptr(T), _ptr(S)), "upload_forcing")
 
     def step_vertical(self, doy: int, fday: int):
         self._check(self.lib.wg_step_vertical(self.h, int(doy), int(fday)), "step_vertical")
@@ -230,6 +239,7 @@ class Model:
 
     def synchronize(self):
         self._check(self.lib.wg_synchronize(self.h), "synchronize")
+        self._inflight.clear()
 
     def discharge(self, day0: int, ndays: int) -> np.ndarray:
         """[ndays, nstation] (single member) or [ndays, nstation, members]."""
