@@ -209,6 +209,13 @@ wg_status wg_get_launch_shape(const wg_ctx *ctx, int32_t *threads, int32_t *bloc
  * integrateWGHM.cpp:414-417). */
 wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values);
 
+/* Cells the day step runs (cell order, nonzero = run; NULL = all).  A skipped
+ * cell keeps its state and produces no outflow, so skip whole basins only (a
+ * cell and everything upstream of it): the calibration loop drops the basins it
+ * has finished, as the reference runs only the cells of the station being
+ * calibrated (G_toBeCalculated, integrateWGHM.cpp:421-442). */
+wg_status wg_set_active_cells(wg_ctx *ctx, const uint8_t *active);
+
 /* Replace the per-member precipitation and gamma factors of an ensemble
  * (as wg_options.member_prec_factor / member_gamma_factor; NULL = all 1). */
 wg_status wg_set_member_factors(wg_ctx *ctx, const float *prec_factor, const float *gamma_factor);

@@ -18,7 +18,7 @@ class FakeProblem:
     def nbasin(self):
         return self.a.size
 
-    def simulate(self, gamma, cfa):
+    def simulate(self, gamma, cfa, active=None):
         self.calls += 1
         return cfa * self.a / (1.0 + self.b * gamma)
 

@@ -114,3 +114,28 @@ def test_overlapped_uploads_give_the_same_run():
             m.upload_forcing(365 * (y + 1), P[sl], T[sl], S[sl], overlap=True)
     m.run_steps(1, 0, 3 * 365, 3 * 365, total)
     assert np.array_equal(m.discharge(0, 3 * 365), q_ref)
+
+
+def test_inactive_basins_do_not_change_active_ones():
+    """wg_set_active_cells: the basins that run give the same bits as in a full run."""
+    from watergap2_gb300.gpu import Model
+    nd = 90
+    region, (P, T, S) = _region_and_forcing(26, nd)
+    down = region.downstream
+    basin = np.arange(region.ncell)
+    for _ in range(region.ncell):                  # follow each cell to its outlet
+        nxt = np.where(down[basin] >= 0, down[basin], basin)
+        if np.array_equal(nxt, basin):
+            break
+        basin = nxt
+    outlets = np.nonzero(down < 0)[0]
+    keep = np.isin(basin, outlets[::2])
+    full = Model(region, max_days=nd)
+    q_full = full.run(1, P, T, S)
+    part = Model(region, max_days=nd)
+    part.set_active_cells(keep)
+    q_part = part.run(1, P, T, S)
+    run_st = np.isin(full.stations, outlets[::2])
+    assert run_st.any() and (~run_st).any()
+    assert np.array_equal(q_part[:, run_st], q_full[:, run_st])
+    assert not np.array_equal(q_part[:, ~run_st], q_full[:, ~run_st])

@@ -48,11 +48,13 @@ class Problem:
     def nbasin(self) -> int:
         return self.basins.nbasin
 
-    def simulate(self, gamma, cfa) -> np.ndarray:
+    def simulate(self, gamma, cfa, active=None) -> np.ndarray:
         """One plain-model call: every basin with its own (gamma, CFA), from the start
-        state; returns each basin's mean outlet discharge over the evaluation year."""
+        state; returns each basin's mean outlet discharge over the evaluation year.
+        With active (per basin), only those basins run (the others' values are stale)."""
         t0 = time.perf_counter()
         m, b = self.model, self.basins.basin_of_cell
+        m.set_active_cells(None if active is None else np.asarray(active, bool)[b])
         m.restore_snapshot()
         m.set_calib_param("P_GAMRUN_C", np.asarray(gamma, np.float64)[b])
         m.set_calib_param("P_CFA", np.asarray(cfa, np.float64)[b])
@@ -200,7 +202,9 @@ def calibrate_bisection(prob: Problem, gamma0=1.0, max_calls=60):
         active = [i for i in range(n) if not st[i].done]
         if not active:
             break
-        q = prob.simulate(np.array([s.gamma for s in st]), np.array([s.cfa for s in st]))
+        mask = np.zeros(n, bool)
+        mask[active] = True
+        q = prob.simulate(np.array([s.gamma for s in st]), np.array([s.cfa for s in st]), mask)
         for i in active:
             q_final[i] = q[i]
             st[i].update(q[i], prob.target_q[i])
@@ -268,7 +272,7 @@ def calibrate_learned(prob: Problem, net=None, gamma0=1.0, max_refine=4, max_cal
         if done.all():
             break
         active = ~done
-        q = prob.simulate(nxt_g, nxt_c)
+        q = prob.simulate(nxt_g, nxt_c, active)
         calls[active] += 1
         err = rel_err(q, tq)
         for i in np.nonzero(active)[0]:

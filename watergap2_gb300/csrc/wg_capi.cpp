@@ -1111,6 +1111,26 @@ wg_status wg_set_member_factors(wg_ctx *ctx, const float *prec_factor, const flo
   return cuda_fail(ctx, e, "set_member_factors");
 }
 
+wg_status wg_set_active_cells(wg_ctx *ctx, const uint8_t *active) {
+  if (!ctx) return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "set_active_cells");
+  uint8_t *dev = nullptr;
+  if (active) {
+    if (!ctx->d_active) ctx->d_active = ctx->alloc<uint8_t>(ctx->n);
+    if (!ctx->d_active) return WG_ERR_NOMEM;
+    std::vector<uint8_t> by_slot(ctx->n);
+    for (int s = 0; s < ctx->n; ++s) by_slot[s] = active[ctx->topo.cell_of_slot[s]] ? 1 : 0;
+    e = cudaMemcpy(ctx->d_active, by_slot.data(), ctx->n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "set_active_cells");
+    dev = ctx->d_active;
+  }
+  ctx->cd.active = dev;
+  ctx->cf.active = dev;
+  return WG_OK;
+}
+
 wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values) {
   if (!ctx || !values) return WG_ERR_INVALID;
   if (k != 0 && k != 1) return WG_ERR_UNSUPPORTED;

@@ -68,6 +68,7 @@ struct wg_ctx {
   double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
   float *staging = nullptr;
   int32_t *d_cell_of_slot = nullptr;
+  uint8_t *d_active = nullptr;             // wg_set_active_cells (slot order)
   int staging_days = 0;
   int64_t launches = 0;
   std::vector<void *> allocs;

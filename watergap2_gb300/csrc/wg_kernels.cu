@@ -136,7 +136,7 @@ template <class R>
 __global__ void __launch_bounds__(256) k_vertical(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   int doy, int fday) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= c.n) return;
+  if (s >= c.n || (c.active && !c.active[s])) return;
   const size_t fo = (size_t)fday * c.n + s;
   VOut<R> o;
   vertical_at<R>(c, st, (size_t)c.n, s, (size_t)s, doy, R(f.prec[fo]), c.gamma[s], f.temp[fo], f.swrad[fo], o);
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads) k_vertical_ahead(DevCellsT<R
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
     const int s = ENS ? (int)(i / M) : (int)i;
     const int mm = ENS ? (int)(i - (size_t)s * M) : 0;
-    if (c.flags[s] & F_VINLINE) continue;
+    if ((c.flags[s] & F_VINLINE) || (c.active && !c.active[s])) continue;
     const int off = c.offset[s];
     const int d0 = max(0, t_b - off), d1 = min(ndays, t_e - off);
     if (d0 >= d1) continue;
@@ -230,6 +230,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads) k_pipeline(DevCellsT<R> c, D
         const size_t si = (size_t)i;
         const int d = t - c.offset[s];
         if (d < 0 || d >= ndays) continue;   // this cell's wavefront has not reached it yet / is done
+        if (c.active && !c.active[s]) continue;
         const int doy = (doy0 - 1 + d) % 365 + 1;
         const int month = month_of(doy);
         const uint32_t fl = c.flags[s];

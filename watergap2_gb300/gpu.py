@@ -31,7 +31,7 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc",
            "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
-           "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async")
+           "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells")
 
 
 class WgError(RuntimeError):
@@ -109,6 +109,7 @@ def load_library(path: str = LIB_PATH):
                                         ctypes.POINTER(i32)]
     lib.wg_set_calib_param.argtypes = [vp, i32, vp]
     lib.wg_set_member_factors.argtypes = [vp, vp, vp]
+    lib.wg_set_active_cells.argtypes = [vp, vp]
     lib.wg_save_snapshot.argtypes = [vp]
     lib.wg_restore_snapshot.argtypes = [vp]
     lib.wg_set_chunk_steps.argtypes = [vp, i32]
@@ -124,7 +125,8 @@ def load_library(path: str = LIB_PATH):
                  "wg_get_discharge", "wg_get_balance", "wg_reset_balance", "wg_synchronize", "wg_launch_shape",
                  "wg_get_launch_shape", "wg_set_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
                  "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
-                 "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async"):
+                 "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async",
+                 "wg_set_active_cells"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -318,6 +320,12 @@ class Model:
         self._check(self.lib.wg_get_kernel_times(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)),
                     "get_kernel_times")
         return {"vertical_ahead_ms": a.value, "wavefront_ms": b.value, "launch_pairs": n.value}
+
+    def set_active_cells(self, active=None):
+        """wg_set_active_cells: run only the cells where active is true (None: all)."""
+        a = None if active is None else np.ascontiguousarray(np.asarray(active, bool).astype(np.uint8))
+        assert a is None or a.shape == (self.region.ncell,)
+        self._check(self.lib.wg_set_active_cells(self.h, _ptr(a)), "set_active_cells")
 
     def set_member_factors(self, prec_factor=None, gamma_factor=None):
         pf = None if prec_factor is None else np.ascontiguousarray(prec_factor, np.float32)
