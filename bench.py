@@ -519,6 +519,23 @@ def run_fine():
     q64 = models["fp64"].discharge(0, nd)
     q32 = models["fp32"].discharge(0, nd)
     err_q = outlet_errors(q32, q64)
+    # which outlets carry the largest errors: their basins' size and water bodies
+    scale = np.maximum(np.abs(q64).max(axis=0), 1e-30)
+    daily = np.abs(q32 - q64).max(axis=0) / scale
+    mean_e = np.abs(q32.mean(axis=0) - q64.mean(axis=0)) / np.maximum(np.abs(q64.mean(axis=0)), 1e-30)
+    from watergap2_gb300.basins import dfs_order
+    order, tin, tout = dfs_order(region.downstream)
+    st = models["fp64"].stations
+    wb = {"reservoirs": region.res_area > 0, "global_lakes": region.lake_area > 0, "local_lakes": region.loc_lake > 0,
+          "arid": region.aindex == 1}
+    worst = []
+    for j in np.argsort(-mean_e)[:5]:
+        cells = order[tin[st[j]]:tout[st[j]] + 1]
+        worst.append({"basin_cells": int(cells.size), "mean_q": float(q64[:, j].mean()), "mean_err": float(mean_e[j]),
+                      "daily_err": float(daily[j]), **{k: int(v[cells].sum()) for k, v in wb.items()}})
+    err_q["frac_mean_err_above_1e-5"] = float((mean_e > 1e-5).mean())
+    err_q["frac_daily_err_above_1e-5"] = float((daily > 1e-5).mean())
+    err_q["worst_outlets"] = worst
     st64, st32 = models["fp64"].get_state(), models["fp32"].get_state()
     err_s = {}
     for k in ("canopy", "snow", "soil", "gw", "river", "loclake", "locwetl", "glolake", "glowetl", "res"):

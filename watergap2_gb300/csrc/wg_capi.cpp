@@ -887,8 +887,8 @@ wg_status wg_get_member_state(wg_ctx *ctx, int32_t member, wg_state_view *v) {
   return state_io(ctx, v, member, false);
 }
 
-static wg_status upload_forcing_on(wg_ctx *ctx, cudaStream_t st, int32_t day0, int32_t ndays, const float *prec,
-                                   const float *temp, const float *swrad) {
+static wg_status upload_forcing_on(wg_ctx *ctx, cudaStream_t st, float *staging, int32_t day0, int32_t ndays,
+                                   const float *prec, const float *temp, const float *swrad) {
   if (!ctx || !prec || !temp || !swrad || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days)
     return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
@@ -898,10 +898,10 @@ static wg_status upload_forcing_on(wg_ctx *ctx, cudaStream_t st, int32_t day0, i
   for (int d = 0; d < ndays; d += ctx->staging_days) {
     const int nd = std::min(ctx->staging_days, ndays - d);
     for (int k = 0; k < 3; ++k) {
-      cudaError_t e = cudaMemcpyAsync(ctx->staging, src[k] + (size_t)d * n, (size_t)nd * n * sizeof(float),
+      cudaError_t e = cudaMemcpyAsync(staging, src[k] + (size_t)d * n, (size_t)nd * n * sizeof(float),
                                       cudaMemcpyHostToDevice, st);
       if (e == cudaSuccess)
-        e = launch_gather_forcing(ctx->staging, dst[k] + (size_t)(day0 + d) * n, ctx->d_cell_of_slot, n, nd, st);
+        e = launch_gather_forcing(staging, dst[k] + (size_t)(day0 + d) * n, ctx->d_cell_of_slot, n, nd, st);
       ctx->launches++;
       if (e != cudaSuccess) return cuda_fail(ctx, e, "upload_forcing");
     }
@@ -913,13 +913,17 @@ wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const floa
                             const float *swrad) {
   if (!ctx) return WG_ERR_INVALID;
   join_uploads(ctx);   // after the overlapped uploads, in the order of the calls
-  return upload_forcing_on(ctx, ctx->stream, day0, ndays, prec, temp, swrad);
+  return upload_forcing_on(ctx, ctx->stream, ctx->staging, day0, ndays, prec, temp, swrad);
 }
 
 wg_status wg_upload_forcing_async(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec, const float *temp,
                                   const float *swrad) {
   if (!ctx) return WG_ERR_INVALID;
-  wg_status st = upload_forcing_on(ctx, ctx->copy_stream, day0, ndays, prec, temp, swrad);
+  // its own staging buffer: the copy stream is not ordered after uploads on the
+  // context's stream
+  if (!ctx->staging_async) ctx->staging_async = ctx->alloc<float>((size_t)ctx->staging_days * ctx->n);
+  if (!ctx->staging_async) return WG_ERR_NOMEM;
+  wg_status st = upload_forcing_on(ctx, ctx->copy_stream, ctx->staging_async, day0, ndays, prec, temp, swrad);
   if (st != WG_OK) return st;
   cudaError_t e = cudaEventRecord(ctx->upload_done, ctx->copy_stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "upload_forcing_async");

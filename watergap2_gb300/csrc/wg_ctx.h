@@ -67,6 +67,7 @@ struct wg_ctx {
   DevSync sync{};
   double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
   float *staging = nullptr;
+  float *staging_async = nullptr;          // staging of wg_upload_forcing_async
   int32_t *d_cell_of_slot = nullptr;
   uint8_t *d_active = nullptr;             // wg_set_active_cells (slot order)
   int staging_days = 0;

@@ -46,6 +46,36 @@ template <> struct M<float> {
   static __device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
 };
 
+// Comparisons of the day step's hot loops.  On GB300 a double compare issues on
+// the FP64 pipe (2 lanes per SM per clock) like an FMA; these give the same
+// answers for every non-NaN operand from integer instructions on the bit
+// patterns: x >= 0 orders like its bits as a signed integer, x < 0 like the
+// negated magnitude (key below, which maps -0 and +0 to the same key), and a
+// compare with a positive constant needs no key at all.  FP32 compares are
+// cheap and stay as they are.
+template <class R> struct C;
+template <> struct C<double> {
+  static __device__ __forceinline__ long long key(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : (long long)(0x8000000000000000ull - (unsigned long long)b);
+  }
+  static __device__ __forceinline__ bool gt(double a, double b) { return key(a) > key(b); }
+  static __device__ __forceinline__ bool le(double a, double b) { return key(a) <= key(b); }
+  static __device__ __forceinline__ bool lt0(double a) { return key(a) < 0; }
+  // a > c and |a| <= c for a constant c > 0
+  static __device__ __forceinline__ bool gt_c(double a, double c) { return __double_as_longlong(a) > __double_as_longlong(c); }
+  static __device__ __forceinline__ bool abs_le_c(double a, double c) {
+    return (__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFll) <= __double_as_longlong(c);
+  }
+};
+template <> struct C<float> {
+  static __device__ __forceinline__ bool gt(float a, float b) { return a > b; }
+  static __device__ __forceinline__ bool le(float a, float b) { return a <= b; }
+  static __device__ __forceinline__ bool lt0(float a) { return a < 0.f; }
+  static __device__ __forceinline__ bool gt_c(float a, float c) { return a > c; }
+  static __device__ __forceinline__ bool abs_le_c(float a, float c) { return fabsf(a) <= c; }
+};
+
 template <class R>
 struct VOut {
   R rs, gwr, transfer, owp, owpet;
@@ -221,18 +251,19 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
       sb = R(0);
       gs = R(0);
     } else {
+      typedef C<R> cmp;
       R effBefore, melt = R(0);
       sb *= ratio;
-      if (m::fabs_(sb) <= R(WG_MIN_STOR_VOL)) sb = R(0);
+      if (cmp::abs_le_c(sb, R(WG_MIN_STOR_VOL))) sb = R(0);
       initialStorage = sb;
-      if (sb > R(1000.)) {
+      if (cmp::gt_c(sb, R(1000.))) {
         if (thresh == 0) thresh = c.band_el[(size_t)e * c.n + s];
         else if (thresh > 0) temp_elev = T - (R(thresh) - c.elev0[s]) * c.t_gradnt[s];
       }
-      if (temp_elev <= t_snowfz) {
+      if (cmp::le(temp_elev, t_snowfz)) {
         effBefore = R(0);
         sb += prec_to_soil;
-        if (sb > soilPET) {
+        if (cmp::gt(sb, soilPET)) {
           sb -= soilPET;
           snowEvapo += soilPET;
         } else {
@@ -242,9 +273,9 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
       } else {
         effBefore = prec_to_soil;
       }
-      if (temp_elev > t_snowmt && !(sb < R(0))) {
+      if (cmp::gt(temp_elev, t_snowmt) && !cmp::lt0(sb)) {
         melt = ddf_m * (temp_elev - t_snowmt);
-        if (melt > sb) {
+        if (cmp::gt(melt, sb)) {
           melt = sb;
           sb = R(0);
         } else {
