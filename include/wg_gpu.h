@@ -147,6 +147,23 @@ wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const floa
 wg_status wg_upload_forcing_async(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec, const float *temp,
                                   const float *swrad);
 
+/* Forcing straight from the reference's yearly climate files: prec, temp and
+ * swrad each hold one `.365.UNF0` file as read from disk -- big-endian float,
+ * cell-major [ncell][nd_file] (G_GPCC_..., G_TEMP_..., G_SSRD_...; read by
+ * climateYearClass::read_climate_data_daily_per_year, climateYear.cpp:38-79,
+ * through GridUNFAdapter::readGrid, grid_io_adapters.h:91-129).  Days
+ * [d_first, d_first + ndays) of the files go to day slots day0.. .  The raw
+ * bytes are copied to the device as they are; the byte swap and the transpose
+ * to the day-major slot layout run on the GPU.  overlap != 0: on the copy
+ * stream, as wg_upload_forcing_async. */
+wg_status wg_upload_forcing_unf(wg_ctx *ctx, int32_t day0, int32_t nd_file, int32_t d_first, int32_t ndays,
+                                const void *prec, const void *temp, const void *swrad, int32_t overlap);
+
+/* Read `bytes` bytes of a file into dst (e.g. a pinned buffer for
+ * wg_upload_forcing_unf); returns the bytes read, -1 if the file cannot be
+ * opened. */
+int64_t wg_read_unf(const char *path, void *dst, int64_t bytes);
+
 /* One day, the reference's call granularity: the vertical balance of every cell
  * (the OpenMP calcNewDay loop, source/integrateWGHM.cpp:767-783) for day of year
  * doy (1..365) from forcing slot fday ... */

@@ -139,3 +139,24 @@ def test_inactive_basins_do_not_change_active_ones():
     assert run_st.any() and (~run_st).any()
     assert np.array_equal(q_part[:, run_st], q_full[:, run_st])
     assert not np.array_equal(q_part[:, ~run_st], q_full[:, ~run_st])
+
+
+def test_forcing_from_unf_files_equals_day_major_upload(tmp_path):
+    """The reference's yearly climate files (big-endian, cell-major), byte-swapped
+    and transposed on the GPU, give the same run as the day-major upload --
+    straight and overlapped on the copy stream."""
+    from watergap2_gb300 import unf
+    from watergap2_gb300.gpu import Model, read_unf
+    nd = 2 * 365
+    region, (P, T, S) = _region_and_forcing(27, nd)
+    n = region.ncell
+    ref = Model(region, max_days=nd)
+    q_ref = ref.run(1, P, T, S)
+    m = Model(region, max_days=nd)
+    for y in range(2):
+        sl = slice(365 * y, 365 * (y + 1))
+        paths = unf.write_climate_year(str(tmp_path), 2000 + y, P[sl], T[sl], S[sl])
+        raws = [read_unf(paths[k], n * 365 * 4) for k in ("prec", "temp", "swrad")]
+        m.upload_forcing_unf(365 * y, *raws, overlap=(y == 1))
+    m.run_days(1, 0, nd)
+    assert np.array_equal(m.discharge(0, nd), q_ref)

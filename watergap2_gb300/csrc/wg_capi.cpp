@@ -916,6 +916,48 @@ wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const floa
   return upload_forcing_on(ctx, ctx->stream, ctx->staging, day0, ndays, prec, temp, swrad);
 }
 
+wg_status wg_upload_forcing_unf(wg_ctx *ctx, int32_t day0, int32_t nd_file, int32_t d_first, int32_t ndays,
+                                const void *prec, const void *temp, const void *swrad, int32_t overlap) {
+  if (!ctx || !prec || !temp || !swrad || nd_file <= 0 || d_first < 0 || ndays < 0 || d_first + ndays > nd_file ||
+      day0 < 0 || day0 + ndays > ctx->max_days)
+    return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  const int which = overlap ? 1 : 0;
+  const size_t per = (size_t)ctx->n * nd_file;
+  if (ctx->unf_cap[which] < per) {
+    ctx->unf_raw[which] = ctx->alloc<uint32_t>(per);   // freed with the context
+    if (!ctx->unf_raw[which]) return WG_ERR_NOMEM;
+    ctx->unf_cap[which] = per;
+  }
+  if (!overlap) join_uploads(ctx);
+  cudaStream_t st = overlap ? ctx->copy_stream : ctx->stream;
+  const void *src[3] = {prec, temp, swrad};
+  float *dst[3] = {(float *)ctx->forcing.prec, (float *)ctx->forcing.temp, (float *)ctx->forcing.swrad};
+  for (int k = 0; k < 3; ++k) {
+    cudaError_t e = cudaMemcpyAsync(ctx->unf_raw[which], src[k], per * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = launch_unf_forcing(ctx->unf_raw[which], dst[k] + (size_t)day0 * ctx->n, ctx->d_cell_of_slot, ctx->n,
+                             nd_file, d_first, ndays, st);
+    ctx->launches++;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "upload_forcing_unf");
+  }
+  if (overlap) {
+    cudaError_t e = cudaEventRecord(ctx->upload_done, ctx->copy_stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "upload_forcing_unf");
+    ctx->upload_pending = true;
+  }
+  return WG_OK;
+}
+
+int64_t wg_read_unf(const char *path, void *dst, int64_t bytes) {
+  if (!path || !dst || bytes < 0) return -1;
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return -1;
+  const size_t got = std::fread(dst, 1, (size_t)bytes, f);
+  std::fclose(f);
+  return (int64_t)got;
+}
+
 wg_status wg_upload_forcing_async(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec, const float *temp,
                                   const float *swrad) {
   if (!ctx) return WG_ERR_INVALID;

@@ -68,6 +68,8 @@ struct wg_ctx {
   double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
   float *staging = nullptr;
   float *staging_async = nullptr;          // staging of wg_upload_forcing_async
+  uint32_t *unf_raw[2] = {nullptr, nullptr};   // raw file bytes (context stream, copy stream)
+  size_t unf_cap[2] = {0, 0};
   int32_t *d_cell_of_slot = nullptr;
   uint8_t *d_active = nullptr;             // wg_set_active_cells (slot order)
   int staging_days = 0;

@@ -356,6 +356,38 @@ __global__ void k_gather_forcing(const float *__restrict__ src, float *__restric
   }
 }
 
+// Forcing as the reference's yearly files hold it (`.365.UNF0`: big-endian float,
+// cell-major [cell][nd_file], climateYear.cpp:38-79, grid_io_adapters.h:91-129):
+// days [d_first, d_first + nd) of the file into dst [day][slot].  32 x 32 tiles
+// through shared memory: a warp reads 32 days of one cell (contiguous) and writes
+// 32 slots of one day (contiguous); the byte swap is one byte permute.
+__global__ void __launch_bounds__(256) k_unf_forcing(const uint32_t *__restrict__ raw, float *__restrict__ dst,
+                                                     const int32_t *__restrict__ cell_of_slot, int n, int nd_file,
+                                                     int d_first, int nd) {
+  __shared__ float tile[32][33];
+  const int s0 = blockIdx.x * 32, d0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int r = ty; r < 32; r += 8) {
+    const int s = s0 + r, d = d0 + tx;
+    if (s < n && d < nd) {
+      const uint32_t v = raw[(size_t)cell_of_slot[s] * nd_file + d_first + d];
+      tile[r][tx] = __uint_as_float(__byte_perm(v, 0u, 0x0123));
+    }
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int d = d0 + r, s = s0 + tx;
+    if (s < n && d < nd) dst[(size_t)d * n + s] = tile[tx][r];
+  }
+}
+
+cudaError_t launch_unf_forcing(const uint32_t *raw, float *dst, const int32_t *cell_of_slot, int n, int nd_file,
+                               int d_first, int nd, cudaStream_t st) {
+  const dim3 grid((unsigned)((n + 31) / 32), (unsigned)((nd + 31) / 32));
+  k_unf_forcing<<<grid, 256, 0, st>>>(raw, dst, cell_of_slot, n, nd_file, d_first, nd);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- launchers
 cudaError_t upload_fastmath_tables(const double exp2_tab[64], const double logF_tab[129], const double invF_tab[129]) {
   cudaError_t e = cudaMemcpyToSymbol(fm::g_exp2_tab, exp2_tab, 64 * sizeof(double));

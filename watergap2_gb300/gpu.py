@@ -31,7 +31,8 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc",
            "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
-           "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells")
+           "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells",
+           "wg_upload_forcing_unf", "wg_read_unf")
 
 
 class WgError(RuntimeError):
@@ -110,6 +111,9 @@ def load_library(path: str = LIB_PATH):
     lib.wg_set_calib_param.argtypes = [vp, i32, vp]
     lib.wg_set_member_factors.argtypes = [vp, vp, vp]
     lib.wg_set_active_cells.argtypes = [vp, vp]
+    lib.wg_upload_forcing_unf.argtypes = [vp, i32, i32, i32, i32, vp, vp, vp, i32]
+    lib.wg_read_unf.argtypes = [ctypes.c_char_p, vp, i64]
+    lib.wg_read_unf.restype = i64
     lib.wg_save_snapshot.argtypes = [vp]
     lib.wg_restore_snapshot.argtypes = [vp]
     lib.wg_set_chunk_steps.argtypes = [vp, i32]
@@ -126,10 +130,21 @@ def load_library(path: str = LIB_PATH):
                  "wg_get_launch_shape", "wg_set_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
                  "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
                  "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async",
-                 "wg_set_active_cells"):
+                 "wg_set_active_cells", "wg_upload_forcing_unf"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
+
+
+def read_unf(path: str, nbytes: int, out: np.ndarray | None = None) -> np.ndarray:
+    """wg_read_unf: nbytes of a file into out (uint8, e.g. pinned), or a new array."""
+    lib = load_library()
+    buf = np.empty(nbytes, np.uint8) if out is None else out
+    assert buf.nbytes >= nbytes and buf.flags.c_contiguous
+    got = lib.wg_read_unf(path.encode(), buf.ctypes.data, int(nbytes))
+    if got != nbytes:
+        raise WgError(f"wg_read_unf {path}: read {got} of {nbytes} bytes")
+    return buf
 
 
 def measure_fp64_peak(device: int = 0) -> float:
@@ -222,6 +237,21 @@ class Model:
         if overlap:
             self._inflight.append((P, T, S))   # alive until the next synchronize
         self._check(fn(self.h, int(day0), nd, _ptr(P), _ptr(T), _ptr(S)), "upload_forcing")
+
+    def upload_forcing_unf(self, day0: int, prec_raw, temp_raw, swrad_raw, nd_file: int = 365, d_first: int = 0,
+                           ndays: int | None = None, overlap: bool = False):
+        """Days [d_first, d_first + ndays) of three raw `.365.UNF0` files (bytes as read,
+        big-endian cell-major [ncell][nd_file]) into day slots day0.. ."""
+        raws = [np.ascontiguousarray(np.frombuffer(r, np.uint8) if isinstance(r, (bytes, bytearray)) else r)
+                for r in (prec_raw, temp_raw, swrad_raw)]
+        for r in raws:
+            assert r.nbytes == self.region.ncell * nd_file * 4, (r.nbytes, self.region.ncell * nd_file * 4)
+        nd = nd_file - d_first if ndays is None else ndays
+        if overlap:
+            self._inflight.append(tuple(raws))
+        self._check(self.lib.wg_upload_forcing_unf(self.h, int(day0), int(nd_file), int(d_first), int(nd),
+                                                   _ptr(raws[0]), _ptr(raws[1]), _ptr(raws[2]), int(bool(overlap))),
+                    "upload_forcing_unf")
 
     def step_vertical(self, doy: int, fday: int):
         self._check(self.lib.wg_step_vertical(self.h, int(doy), int(fday)), "step_vertical")
