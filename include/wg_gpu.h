@@ -226,6 +226,19 @@ wg_status wg_get_launch_shape(const wg_ctx *ctx, int32_t *threads, int32_t *bloc
  * integrateWGHM.cpp:414-417). */
 wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values);
 
+/* Monthly aggregates of the routing outputs, accumulated by the wavefront
+ * kernel as it routes each cell-day (the reference's monthly output grids,
+ * routing.cpp:3964-4238: G_monthlyRiverAvail, G_monthlyMin/MaxRiverAvail, the
+ * monthly surface-water storage).  nmonths months of an output calendar whose
+ * output day 0 (wg_get_discharge's day 0) is day-of-year doy_day0; 0 months
+ * switches them off.  Enabling (again) zeroes them. */
+wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0);
+/* which: 0 river availability [km3/month] (sum of the daily transported volume),
+ * 1 sum of the day-end surface-water + groundwater storage [km3 x days],
+ * 2 smallest and 3 largest daily transported volume [km3/day];
+ * out [nm][ncell][members], cell order. */
+wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out);
+
 /* Cells the day step runs (cell order, nonzero = run; NULL = all).  A skipped
  * cell keeps its state and produces no outflow, so skip whole basins only (a
  * cell and everything upstream of it): the calibration loop drops the basins it

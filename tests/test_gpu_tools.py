@@ -160,3 +160,35 @@ def test_forcing_from_unf_files_equals_day_major_upload(tmp_path):
         m.upload_forcing_unf(365 * y, *raws, overlap=(y == 1))
     m.run_days(1, 0, nd)
     assert np.array_equal(m.discharge(0, nd), q_ref)
+
+
+def test_monthly_aggregates_match_daily_outputs():
+    """The wavefront's monthly epilogue against the daily outputs: sums of the
+    daily discharge of every cell, their minimum and maximum, and the sum of the
+    day-end surface-water and groundwater storage."""
+    from watergap2_gb300.gpu import Model
+    nd = 75                                            # Jan 1 .. Mar 16: two full months and a part
+    region, (P, T, S) = _region_and_forcing(28, nd)
+    n = region.ncell
+    m = Model(region, max_days=nd, stations=np.arange(n))
+    m.monthly_outputs(3, doy_day0=1)
+    m.upload_forcing(0, P, T, S)
+    stor = np.zeros((nd, n))
+    for d in range(nd):                                # per-day API: state after every day
+        m.step_vertical(d + 1, d)
+        m.step_routing(d + 1, d)
+        st = m.get_state()
+        stor[d] = st["gw"] + st["river"] + st["loclake"] + st["locwetl"] + st["glolake"] + st["glowetl"] + st["res"]
+    q = m.discharge(0, nd)
+    bounds = [(0, 31), (31, 59), (59, nd)]
+    avail, sto = m.monthly("river_avail"), m.monthly("storage")
+    lo, hi = m.monthly("min_avail"), m.monthly("max_avail")
+    for k, (a, b) in enumerate(bounds):
+        acc_q, acc_s = np.zeros(n), np.zeros(n)
+        for d in range(a, b):                          # day order, as the kernel adds
+            acc_q += q[d]
+            acc_s += stor[d]
+        assert np.array_equal(avail[k], acc_q)
+        assert np.allclose(sto[k], acc_s, rtol=1e-12, atol=0)
+        assert np.array_equal(lo[k], q[a:b].min(axis=0))
+        assert np.array_equal(hi[k], q[a:b].max(axis=0))

@@ -31,6 +31,7 @@ using namespace wg;
 namespace {
 
 const double kPi = 3.141592653589793;   // daily.cpp:73
+const short kFirstDayInMonth[12] = {1, 32, 60, 91, 121, 152, 182, 213, 244, 274, 305, 335};
 
 // dailyWaterBalanceClass::calc_ext_rad (daily.cpp:2398-2449) for a latitude in degrees.
 double calc_ext_rad(short day, double lat_deg) {
@@ -994,10 +995,10 @@ wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday) {
   cudaError_t e = ctx->precision == 0
                       ? launch_pipeline(false, ctx->cd, ctx->sd, ctx->vd, ctx->forcing, ctx->mem, ctx->balance,
                                         ctx->rd, ctx->sync, ctx->outq, ctx->qst, doy, 0, oday, 1, 0, ctx->topo.nlevel,
-                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->stream)
+                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, ctx->stream)
                       : launch_pipeline(false, ctx->cf, ctx->sf, ctx->vf, ctx->forcing, ctx->mem, ctx->balance,
                                         ctx->rf, ctx->sync, ctx->outq, ctx->qst, doy, 0, oday, 1, 0, ctx->topo.nlevel,
-                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->stream);
+                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, ctx->stream);
   return cuda_fail(ctx, e, "step_routing");
 }
 
@@ -1020,7 +1021,7 @@ static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevSta
     if (ev) cudaEventRecord(ev[1], ctx->stream);
     if (e == cudaSuccess)
       e = launch_pipeline(true, c, s, v, ctx->forcing, ctx->mem, ctx->balance, ring, ctx->sync, ctx->outq, ctx->qst,
-                          doy0, fday0, fday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->layout,
+                          doy0, fday0, fday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->layout, ctx->mon,
                           ctx->stream);
     ctx->launches++;
     if (ev) cudaEventRecord(ev[2], ctx->stream);
@@ -1155,6 +1156,56 @@ wg_status wg_set_member_factors(wg_ctx *ctx, const float *prec_factor, const flo
   if (e == cudaSuccess)
     e = cudaMemcpy((float *)ctx->mem.prec_factor, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice);
   return cuda_fail(ctx, e, "set_member_factors");
+}
+
+wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
+  if (!ctx || nmonths < 0 || doy_day0 < 1 || doy_day0 > 365) return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "monthly_outputs");
+  if (ctx->mon_buf) {
+    cudaFree(ctx->mon_buf);
+    ctx->mon_buf = nullptr;
+  }
+  ctx->mon = DevMonthly{};
+  if (nmonths == 0) return WG_OK;
+  const size_t per = (size_t)nmonths * ctx->nstate();
+  e = cudaMalloc((void **)&ctx->mon_buf, 4 * per * sizeof(double));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "monthly_outputs");
+  DevMonthly &m = ctx->mon;
+  m.river_avail = ctx->mon_buf;
+  m.storage = ctx->mon_buf + per;
+  m.min_avail = ctx->mon_buf + 2 * per;
+  m.max_avail = ctx->mon_buf + 3 * per;
+  m.nmonths = nmonths;
+  m.doy_day0 = doy_day0;
+  int mo = 0;
+  for (int k = 1; k < 12; ++k) mo += (doy_day0 >= kFirstDayInMonth[k]) ? 1 : 0;
+  m.month0 = mo;
+  m.enabled = 1;
+  e = cudaMemsetAsync(ctx->mon_buf, 0, 2 * per * sizeof(double), ctx->stream);
+  if (e == cudaSuccess) e = launch_fill(m.min_avail, per, INFINITY, ctx->stream);
+  if (e == cudaSuccess) e = launch_fill(m.max_avail, per, -INFINITY, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  return cuda_fail(ctx, e, "monthly_outputs");
+}
+
+wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out) {
+  if (!ctx || !out || which < 0 || which > 3 || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths) return WG_ERR_INVALID;
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  const size_t N = ctx->nstate(), per = (size_t)ctx->mon.nmonths * N;
+  const int M = ctx->members;
+  std::vector<double> buf((size_t)nm * N);
+  cudaError_t e = cudaMemcpy(buf.data(), ctx->mon_buf + which * per + (size_t)m0 * N, buf.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "get_monthly");
+  const auto &c2s = ctx->topo.cell_of_slot;
+  for (int k = 0; k < nm; ++k)
+    for (int sl = 0; sl < ctx->n; ++sl)
+      for (int mm = 0; mm < M; ++mm)
+        out[((size_t)k * ctx->n + c2s[sl]) * M + mm] = buf[(size_t)k * N + (size_t)sl * M + mm];
+  return WG_OK;
 }
 
 wg_status wg_set_active_cells(wg_ctx *ctx, const uint8_t *active) {

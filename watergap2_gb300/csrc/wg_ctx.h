@@ -16,6 +16,7 @@ using wg::DevBalance;
 using wg::DevCellsT;
 using wg::DevForcing;
 using wg::DevMembers;
+using wg::DevMonthly;
 using wg::DevRingT;
 using wg::DevStateT;
 using wg::DevSync;
@@ -65,6 +66,8 @@ struct wg_ctx {
   DevBalance balance{};
   DevMembers mem{};
   DevSync sync{};
+  DevMonthly mon{};                        // wg_monthly_outputs
+  double *mon_buf = nullptr;
   double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
   float *staging = nullptr;
   float *staging_async = nullptr;          // staging of wg_upload_forcing_async
@@ -98,6 +101,7 @@ struct wg_ctx {
 
   ~wg_ctx() {
     release_tools();
+    if (mon_buf) cudaFree(mon_buf);
     for (void *p : allocs) cudaFree(p);
     if (own_stream && stream) cudaStreamDestroy(stream);
     if (copy_stream) cudaStreamDestroy(copy_stream);

@@ -102,6 +102,17 @@ struct DevBalance {
   int32_t enabled;
 };
 
+// Monthly aggregates of the routing outputs (routing.cpp:3964-4238: G_monthlyRiverAvail,
+// G_monthlyMin/MaxRiverAvail, monthly storage), [nmonths][n*members] each; month m
+// of the output calendar = year * 12 + month - month0 of output day od, the
+// calendar starting at day-of-year doy_day0 for output day 0.
+struct DevMonthly {
+  double *river_avail;   // sum of the day's transported volume [km3/month]
+  double *storage;       // sum of the day-end surface-water + groundwater storage [km3 x days]
+  double *min_avail, *max_avail;
+  int32_t nmonths, doy_day0, month0, enabled;
+};
+
 struct DevForcing {
   const float *prec, *temp, *swrad;   // [max_days][n] slot order
   int32_t max_days;

@@ -204,7 +204,8 @@ template <class R, bool FUSED, bool ENS>
 __global__ void __launch_bounds__(kMaxBlockThreads) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
                                                   double *outq, double *qst, int doy0, int fday0, int oday0,
-                                                  int ndays, int t_b, int t_e, int cell_warps, int idle_warp) {
+                                                  int ndays, int t_b, int t_e, int cell_warps, int idle_warp,
+                                                  DevMonthly mon) {
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const size_t N = (size_t)n * M;
@@ -282,6 +283,21 @@ __global__ void __launch_bounds__(kMaxBlockThreads) k_pipeline(DevCellsT<R> c, D
         st.laf_started[si] = 1;
         const int stn = c.station[s];
         if (stn >= 0) qst[((size_t)(oday0 + d) * c.nstation + stn) * M + mm] = (double)tv;
+        if (mon.enabled) {
+          // monthly epilogue: this thread owns the cell, so no atomics
+          const int od = oday0 + d;
+          const int yd = mon.doy_day0 - 1 + od;
+          const int mi = (yd / 365) * 12 + month_of(yd % 365 + 1) - mon.month0;
+          if (mi >= 0 && mi < mon.nmonths) {
+            const size_t k = (size_t)mi * N + si;
+            const double q = (double)tv;
+            mon.river_avail[k] += q;
+            mon.min_avail[k] = fmin(mon.min_avail[k], q);
+            mon.max_avail[k] = fmax(mon.max_avail[k], q);
+            mon.storage[k] += (double)rs.gw + (double)rs.river + (double)rs.loclake + (double)rs.locwetl +
+                              (double)rs.glolake + (double)rs.glowetl + (double)rs.res;
+          }
+        }
       }
     }
     if (t + 1 < t_e) {
@@ -388,6 +404,15 @@ cudaError_t launch_unf_forcing(const uint32_t *raw, float *dst, const int32_t *c
   return cudaGetLastError();
 }
 
+__global__ void k_fill(double *p, size_t n, double v) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+cudaError_t launch_fill(double *p, size_t n, double v, cudaStream_t st) {
+  k_fill<<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(p, n, v);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- launchers
 cudaError_t upload_fastmath_tables(const double exp2_tab[64], const double logF_tab[129], const double invF_tab[129]) {
   cudaError_t e = cudaMemcpyToSymbol(fm::g_exp2_tab, exp2_tab, 64 * sizeof(double));
@@ -443,7 +468,8 @@ template <class R>
 cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
                             const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
                             const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
-                            int t_b, int t_e, int blocks, int threads, const WarpLayout &lay, cudaStream_t st) {
+                            int t_b, int t_e, int blocks, int threads, const WarpLayout &lay, const DevMonthly &mon,
+                            cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(sync.counter, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
   int cell_warps = lay.cell_warps, idle_warp = mem.members > 1 ? -1 : lay.idle_warp;
@@ -452,7 +478,7 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
   void *args[] = {(void *)&c,    (void *)&s,    (void *)&v,     (void *)&f,     (void *)&mem,   (void *)&b,
                   (void *)&ring, (void *)&sync, (void *)&outq,  (void *)&qst,   (void *)&doy0,  (void *)&fday0,
                   (void *)&oday0, (void *)&ndays, (void *)&t_b, (void *)&t_e, (void *)&cell_warps,
-                  (void *)&idle_warp};
+                  (void *)&idle_warp, (void *)&mon};
   const bool ens = mem.members > 1;
   // cooperative (all blocks resident, or the launch fails) through the launch
   // attribute, which stream capture records into a graph kernel node
@@ -494,7 +520,8 @@ cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int
   template cudaError_t launch_pipeline<R>(bool, const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,  \
                                           const DevForcing &, const DevMembers &, const DevBalance &,             \
                                           const DevRingT<R> &, const DevSync &, double *, double *, int, int,     \
-                                          int, int, int, int, int, int, const WarpLayout &, cudaStream_t);        \
+                                          int, int, int, int, int, int, const WarpLayout &, const DevMonthly &,    \
+                                          cudaStream_t);                                                          \
   template cudaError_t launch_vertical_ahead<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevForcing &,   \
                                                 const DevMembers &, const DevBalance &, const DevRingT<R> &, int,  \
                                                 int, int, int, int, int, int, cudaStream_t);                       \

@@ -32,7 +32,7 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
            "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells",
-           "wg_upload_forcing_unf", "wg_read_unf")
+           "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly")
 
 
 class WgError(RuntimeError):
@@ -112,6 +112,8 @@ def load_library(path: str = LIB_PATH):
     lib.wg_set_member_factors.argtypes = [vp, vp, vp]
     lib.wg_set_active_cells.argtypes = [vp, vp]
     lib.wg_upload_forcing_unf.argtypes = [vp, i32, i32, i32, i32, vp, vp, vp, i32]
+    lib.wg_monthly_outputs.argtypes = [vp, i32, i32]
+    lib.wg_get_monthly.argtypes = [vp, i32, i32, i32, vp]
     lib.wg_read_unf.argtypes = [ctypes.c_char_p, vp, i64]
     lib.wg_read_unf.restype = i64
     lib.wg_save_snapshot.argtypes = [vp]
@@ -130,7 +132,7 @@ def load_library(path: str = LIB_PATH):
                  "wg_get_launch_shape", "wg_set_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
                  "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
                  "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async",
-                 "wg_set_active_cells", "wg_upload_forcing_unf"):
+                 "wg_set_active_cells", "wg_upload_forcing_unf", "wg_monthly_outputs", "wg_get_monthly"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -350,6 +352,20 @@ class Model:
         self._check(self.lib.wg_get_kernel_times(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)),
                     "get_kernel_times")
         return {"vertical_ahead_ms": a.value, "wavefront_ms": b.value, "launch_pairs": n.value}
+
+    MONTHLY = {"river_avail": 0, "storage": 1, "min_avail": 2, "max_avail": 3}
+
+    def monthly_outputs(self, nmonths: int, doy_day0: int = 1):
+        """wg_monthly_outputs: accumulate monthly aggregates for nmonths months."""
+        self._check(self.lib.wg_monthly_outputs(self.h, int(nmonths), int(doy_day0)), "monthly_outputs")
+        self.nmonths = int(nmonths)
+
+    def monthly(self, name: str, m0: int = 0, nm: int | None = None) -> np.ndarray:
+        """[nm, ncell] (or [nm, ncell, members]) monthly aggregate, cell order."""
+        nm = self.nmonths - m0 if nm is None else nm
+        out = np.zeros((nm, self.region.ncell) if self.members == 1 else (nm, self.region.ncell, self.members))
+        self._check(self.lib.wg_get_monthly(self.h, self.MONTHLY[name], int(m0), int(nm), _ptr(out)), "get_monthly")
+        return out
 
     def set_active_cells(self, active=None):
         """wg_set_active_cells: run only the cells where active is true (None: all)."""
