@@ -40,10 +40,19 @@ __device__ __forceinline__ double exp(double x) {
   const double inv_l = 92.33248261689366;           // 64 / ln 2
   const double l1 = 0.01083042469326756;            // ln2/64 to 32 bits: n*l1 is exact
   const double l2 = 2.9815858269852933e-12;         // ln2/64 - l1
-  if (x < -745.2) return 0.0;
-  if (x > 709.78) return __longlong_as_double(0x7ff0000000000000ll);
-  const double nd = rint(x * inv_l);
-  const int n = (int)nd;
+  // range test on the bit pattern (integer pipe): |x| >= 708 is never on the hot
+  // path, so the exact thresholds are only compared there
+  if ((__double_as_longlong(x) & 0x7fffffffffffffffll) >= 0x4086200000000000ll) {   // |x| >= 708
+    if (x < -745.2) return 0.0;
+    if (x > 709.78) return __longlong_as_double(0x7ff0000000000000ll);
+  }
+  // n = round(x * 64/ln2) with the 1.5 * 2^52 shifter: the low word of t is n and
+  // t - shifter is n as a double (one FMA and one add instead of a round and two
+  // conversions on the FP64 pipe)
+  const double shifter = 6755399441055744.0;
+  const double t = fma(x, inv_l, shifter);
+  const int n = __double2loint(t);
+  const double nd = t - shifter;
   double r = fma(-nd, l1, x);
   r = fma(-nd, l2, r);
   double q = fma(r, 1.0 / 120.0, 1.0 / 24.0);
@@ -61,10 +70,12 @@ __device__ __forceinline__ double log(double x) {
   int hi = __double2hiint(x);
   const int lo = __double2loint(x);
   int m = (hi >> 20) - 1023;
-  hi = (hi & 0x000fffff) | 0x3ff00000;              // y in [1, 2)
-  const double y = __hiloint2double(hi, lo);
-  const int j = __double2int_rn((y - 1.0) * 128.0);   // F = 1 + j/128 nearest to y
-  const double F = fma((double)j, 0.0078125, 1.0);
+  const int hm = hi & 0x000fffff;
+  const double y = __hiloint2double(hm | 0x3ff00000, lo);   // y in [1, 2)
+  // F = 1 + j/128 nearest to y, from the mantissa bits (integer pipe): j rounds
+  // the top 7 mantissa bits, half up; F is built from j's bits
+  const int j = (hm + 0x1000) >> 13;
+  const double F = __hiloint2double(0x3ff00000 + (j << 13), 0);
   const double f = y - F;                             // exact
   const double u = f * g_invF_tab[j];
   // log1p(u) = u - u^2/2 + u^3/3 - ... to degree 7
@@ -82,8 +93,9 @@ __device__ __forceinline__ double log(double x) {
 // x^y for x >= 0, y > 0 (the hot path's exponents are positive constants or
 // calibration parameters)
 __device__ __forceinline__ double pow(double x, double y) {
-  if (!(x > 0.0)) return 0.0;
-  if (x == 1.0) return 1.0;
+  const long long b = __double_as_longlong(x);
+  if (b <= 0) return 0.0;                              // x <= 0 (and -0)
+  if (b == 0x3ff0000000000000ll) return 1.0;           // x == 1
   return fm::exp(y * fm::log(x));
 }
 

@@ -61,7 +61,12 @@ template <> struct C<double> {
   }
   static __device__ __forceinline__ bool gt(double a, double b) { return key(a) > key(b); }
   static __device__ __forceinline__ bool le(double a, double b) { return key(a) <= key(b); }
+  static __device__ __forceinline__ bool lt(double a, double b) { return key(a) < key(b); }
   static __device__ __forceinline__ bool lt0(double a) { return key(a) < 0; }
+  static __device__ __forceinline__ bool gt0(double a) { return __double_as_longlong(a) > 0; }
+  static __device__ __forceinline__ bool le0(double a) { return __double_as_longlong(a) <= 0; }
+  // a < c and a <= c for a constant c > 0
+  static __device__ __forceinline__ bool lt_c(double a, double c) { return __double_as_longlong(a) < __double_as_longlong(c); }
   // a > c and |a| <= c for a constant c > 0
   static __device__ __forceinline__ bool gt_c(double a, double c) { return __double_as_longlong(a) > __double_as_longlong(c); }
   static __device__ __forceinline__ bool abs_le_c(double a, double c) {
@@ -71,7 +76,11 @@ template <> struct C<double> {
 template <> struct C<float> {
   static __device__ __forceinline__ bool gt(float a, float b) { return a > b; }
   static __device__ __forceinline__ bool le(float a, float b) { return a <= b; }
+  static __device__ __forceinline__ bool lt(float a, float b) { return a < b; }
   static __device__ __forceinline__ bool lt0(float a) { return a < 0.f; }
+  static __device__ __forceinline__ bool gt0(float a) { return a > 0.f; }
+  static __device__ __forceinline__ bool le0(float a) { return a <= 0.f; }
+  static __device__ __forceinline__ bool lt_c(float a, float c) { return a < c; }
   static __device__ __forceinline__ bool gt_c(float a, float c) { return a > c; }
   static __device__ __forceinline__ bool abs_le_c(float a, float c) { return fabsf(a) <= c; }
 };
@@ -91,7 +100,7 @@ __device__ __forceinline__ R lai_growing(int &days, int init, int &status, bool 
     if (days >= init) {
       days++;
       psum += prec;
-      if (psum > R(40.)) {
+      if (C<R>::gt_c(psum, R(40.))) {
         if (days >= init + 30) { days = init + 30; status = 1; }
         return lmin + (lmax - lmin) * R(days - init) * inv30;
       }
@@ -108,7 +117,7 @@ __device__ __forceinline__ R lai_growing(int &days, int init, int &status, bool 
     if (days <= 0) { days = 0; status = 0; psum = R(0); }
     return lmax - (lmax - lmin) * R(30 - days) * inv30;
   }
-  if (arid && (prec < R(0.5))) days--;
+  if (arid && C<R>::lt_c(prec, R(0.5))) days--;
   else days = 30 + init;
   return lmax;
 }
@@ -121,7 +130,7 @@ __device__ __forceinline__ R lai_nogrowing(int &days, int init, int &status, R l
     if (days > init) {
       days++;
       psum += prec;
-      if (psum > R(40.)) {
+      if (C<R>::gt_c(psum, R(40.))) {
         if (days >= init + 30) { days = init + 30; status = 1; }
         return lmin + (lmax - lmin) * R(days - init) * inv30;
       }
@@ -174,12 +183,13 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   else
     dailyLai = lai_nogrowing<R>(days, c.init_days[s], status, c.lai_min[s], c.lai_max[s], psum, dailyPrec);
 
-  const R albedo = (gsnow > R(3.)) ? c.albedo_snow[s] : c.albedo[s];                 // daily.cpp:366-379
+  typedef C<R> cmp;
+  const R albedo = cmp::gt_c(gsnow, R(3.)) ? c.albedo_snow[s] : c.albedo[s];                 // daily.cpp:366-379
   const R lat_heat = (Tf > 0.f) ? R(2.501) - R(0.002361) * T : R(2.835);      // daily.cpp:382-387
   const R rlh = m::rcp(lat_heat);
   const R solar_rad = R(0.0864) * rlh * R(SWf);
   R solar_fraction = (ext_rad == R(0)) ? R(0) : solar_rad * inv_s0;          // daily.cpp:430-448
-  if (solar_fraction > R(1.)) solar_fraction = R(1.);
+  if (cmp::gt_c(solar_fraction, R(1.))) solar_fraction = R(1.);
   const R ff = a_c * solar_fraction + b_c;
   const R net_emissivity = R(-0.02) + R(0.261) * m::exp(R(-0.000777) * T * T);
   const R tK = T + R(273.2);
@@ -190,8 +200,8 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   const R inc_svp = R(4098.) * e_s * (inv_t2 * inv_t2);                     // daily.cpp:484-532
   const R gamma = R(0.0016286 * 101.3) * rlh;
   const R apet = alpha * inc_svp * m::rcp(inc_svp + gamma);
-  const R dailyPET = (net_rad <= R(0)) ? R(0) : apet * net_rad;
-  const R owPET = (ow_net_rad <= R(0)) ? R(0) : apet * ow_net_rad;
+  const R dailyPET = cmp::le0(net_rad) ? R(0) : apet * net_rad;
+  const R owPET = cmp::le0(ow_net_rad) ? R(0) : apet * ow_net_rad;
   o.owp = dailyPrec;
   o.owpet = owPET;
 
@@ -199,7 +209,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   R canopyEvapo = R(0), prec_to_soil = R(0), soilPET = R(0), snowEvapo = R(0), effPrec = R(0);
   R immediate = R(0), dailyAET = R(0), runoff = R(0), total = R(0), gwr = R(0), pot = R(0);
   R overflow = R(0), neg_land_aet = R(0), cellAET = R(0), gwr_route = R(0), leak = R(0);
-  const bool land = landAreaFrac > R(0.);
+  const bool land = cmp::gt0(landAreaFrac);
   // prevLAF / landAreaFrac; exactly 1 while the land fraction does not change
   const R ratio = !land ? R(0) : (prevLAF == landAreaFrac ? R(1) : prevLAF / landAreaFrac);
 
@@ -209,12 +219,12 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
     canopy = R(0);
   } else {
     canopy *= ratio;
-    if (m::fabs_(canopy) <= R(WG_MIN_STOR_VOL)) canopy = R(0);
+    if (cmp::abs_le_c(canopy, R(WG_MIN_STOR_VOL))) canopy = R(0);
     initialStorage = canopy;
-    if (dailyLai > R(0.00001)) {
+    if (cmp::gt_c(dailyLai, R(0.00001))) {
       const R maxcs = c.mcwh[s] * dailyLai;
       const R deficiency = maxcs - canopy;
-      if (dailyPrec < deficiency) {
+      if (cmp::lt(dailyPrec, deficiency)) {
         canopy += dailyPrec;
         prec_to_soil = R(0);
       } else {
@@ -223,7 +233,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
       }
       const R cwc = canopy;
       canopyEvapo = dailyPET * m::pow(cwc / maxcs, R(0.66666666));
-      if (canopyEvapo > cwc) {
+      if (cmp::gt(canopyEvapo, cwc)) {
         canopyEvapo = cwc;
         soilPET = dailyPET - cwc;
         canopy = R(0);
@@ -237,7 +247,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
     }
     lsc += canopy - initialStorage;
   }
-  if (soilPET < R(0)) soilPET = R(0);
+  if (cmp::lt0(soilPET)) soilPET = R(0);
 
   // snow in elevation bands (daily.cpp:897-1062)
   R tempElevMax = R(0), snowChange = R(0), gs = R(0);
@@ -251,7 +261,6 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
       sb = R(0);
       gs = R(0);
     } else {
-      typedef C<R> cmp;
       R effBefore, melt = R(0);
       sb *= ratio;
       if (cmp::abs_le_c(sb, R(WG_MIN_STOR_VOL))) sb = R(0);
@@ -299,7 +308,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   gsnow = gs;
 
   // immediate runoff from built-up area (daily.cpp:1068-1071)
-  if (c.built_up[s] > R(0)) {
+  if (cmp::gt0(c.built_up[s])) {
     immediate = R(0.5) * effPrec * c.built_up[s];
     effPrec -= immediate;
   }
@@ -313,36 +322,36 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
     const R Smax = c.smax[s];
     soil *= ratio;
     initialStorage = soil;
-    if (soil > Smax) {
+    if (cmp::gt(soil, Smax)) {
       overflow = soil - Smax;
       soil = Smax;
     }
-    if (tempElevMax > t_snowfz) {
-      if (Smax > R(0)) {
+    if (cmp::gt(tempElevMax, t_snowfz)) {
+      if (cmp::gt0(Smax)) {
         const R sat = soil * c.inv_smax[s];
         runoff = effPrec * m::pow(sat, gamma_soil);
         const R lim = (maxDailyPET - canopyEvapo) * sat;
-        dailyAET = (soilPET > lim) ? lim : soilPET;
+        dailyAET = cmp::gt(soilPET, lim) ? lim : soilPET;
         soil += effPrec - dailyAET - runoff;
-        if (m::fabs_(soil) <= R(WG_MIN_STOR_VOL)) soil = R(0);
+        if (cmp::abs_le_c(soil, R(WG_MIN_STOR_VOL))) soil = R(0);
         effPrec = R(0);
-        if (soil < R(0)) {
+        if (cmp::lt0(soil)) {
           dailyAET += soil;
           soil = R(0);
         }
         runoff *= cfa;
         immediate *= cfa;
         const R fgr = c.fg[s] * runoff;
-        gwr = (c.rgmax[s] < fgr) ? c.rgmax[s] : fgr;
+        gwr = cmp::lt(c.rgmax[s], fgr) ? c.rgmax[s] : fgr;
         // the reference's inland-sink test here reads a grid nothing fills (globals.cpp:8),
         // so the arid rule applies by aridity and texture alone
-        if ((flags & F_ARID_GW) && (dailyPrec <= c.pcritgwa[s])) {
+        if ((flags & F_ARID_GW) && cmp::le(dailyPrec, c.pcritgwa[s])) {
           pot = gwr;
           gwr = R(0);
         }
         runoff -= pot;
         soil += pot * c.inv_cfa[s];
-        if (soil > Smax) {
+        if (cmp::gt(soil, Smax)) {
           overflow += soil - Smax;
           soil = Smax;
         }
@@ -359,18 +368,18 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
     gwr_route = gwr;   // G_dailyGwRecharge (daily.cpp:1232)
     lsc += soil - initialStorage;
     cellAET = (lsc - dailyPrec) * (cfa - R(1.0)) + (dailyAET + canopyEvapo + snowEvapo) * cfa;
-    if (cellAET < R(0)) {
+    if (cmp::lt0(cellAET)) {
       neg_land_aet = cellAET;
       cellAET = R(0);
     }
   }
   // surface runoff (daily.cpp:1244-1257)
-  if (neg_land_aet < R(0)) total = total + neg_land_aet;
-  if (total < R(0)) {
+  if (cmp::lt0(neg_land_aet)) total = total + neg_land_aet;
+  if (cmp::lt0(total)) {
     leak -= total;
     total = R(0);
   }
-  if ((total - gwr) < R(0)) {
+  if (cmp::lt0(total - gwr)) {
     soil += total - gwr;
     gwr = total;
   }
@@ -425,17 +434,18 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   const R cfa = c.cfa[s];
   rt.p_ow = R(0); rt.e_ow = R(0); rt.leak = R(0);
   const R f_land = c.area_f[s] * laf;
-  R dlsr = (laf <= R(0)) ? v.transfer * c.area_f[s] * laf_prev : v.rs * f_land;
+  typedef C<R> cmp;
+  R dlsr = cmp::le0(laf) ? v.transfer * c.area_f[s] * laf_prev : v.rs * f_land;
   // groundwater (routing.cpp:2061-2200)
   const R gw0 = st.gw;
   const R netGWin = v.gwr * f_land;
   R gw = gw0 * c.gw_e[s] + c.gw_ik[s] * netGWin * c.gw_ome[s];
-  if (m::fabs_(gw) <= R(WG_MIN_STOR_VOL)) gw = R(0);
+  if (cmp::abs_le_c(gw, R(WG_MIN_STOR_VOL))) gw = R(0);
   R gw_runoff = gw0 - gw + netGWin;
-  if (gw_runoff <= R(0)) {
+  if (cmp::le0(gw_runoff)) {
     gw_runoff = R(0);
     gw = gw0 + netGWin;
-    if (m::fabs_(gw) <= R(WG_MIN_STOR_VOL)) gw = R(0);
+    if (cmp::abs_le_c(gw, R(WG_MIN_STOR_VOL))) gw = R(0);
   }
   st.gw = gw;
   R inflow = dlsr + gw_runoff;
@@ -622,16 +632,16 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   const R eK = m::exp(-K);
   const R omeK = R(1.) - eK;
   R S, transported;
-  if (inflow * omeK + K * S0 * eK < R(0)) {   // sign of RivEvapoRemUseMax (routing.cpp:3444-3449)
+  if (cmp::lt0(inflow * omeK + K * S0 * eK)) {   // sign of RivEvapoRemUseMax (routing.cpp:3444-3449)
     const R maxUse = inflow + K * S0 * eK / omeK;
     S = R(0);
     transported = inflow + S0 - maxUse;
   } else {
     S = S0 * eK + inflow * omeK / K;
-    if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
+    if (cmp::abs_le_c(S, R(WG_MIN_STOR_VOL))) S = R(0);
     transported = inflow + S0 - S;
   }
-  if (transported < R(0)) {
+  if (cmp::lt0(transported)) {
     rt.leak -= transported;
     transported = R(0);
   }
