@@ -192,3 +192,24 @@ def test_monthly_aggregates_match_daily_outputs():
         assert np.allclose(sto[k], acc_s, rtol=1e-12, atol=0)
         assert np.array_equal(lo[k], q[a:b].min(axis=0))
         assert np.array_equal(hi[k], q[a:b].max(axis=0))
+
+
+def test_step_flags_equal_grid_barrier():
+    """Per-warp step flags and one grid barrier per step give the same bits
+    (global grid: many warps, deep drainage)."""
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_global()
+    nd = 40
+    P, T, S = sy.forcing(region, nd, doy0=200)
+    out = []
+    for flags in (0, 1):
+        m = Model(region, max_days=nd, record_balance=True)
+        m.step_sync(flags)
+        m.chunk_steps(16)                      # several launches: flags reset per launch
+        q = m.run(200, P, T, S)
+        out.append((q, m.balance(), m.get_state()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    for k in out[0][2]:
+        assert np.array_equal(out[0][2][k], out[1][2][k]), k

@@ -347,6 +347,40 @@ const T *upload_raw(wg_ctx *ctx, const std::vector<S> &v, wg_status &st) {
   return d;
 }
 
+// Step flags of the single-member layout: for every warp of cells (slots
+// 32w..32w+31) the warps holding its cells' upstream and downstream cells.
+wg_status setup_step_flags(wg_ctx *ctx) {
+  const int n = ctx->n, W = (n + 31) / 32;
+  std::vector<std::vector<int32_t>> deps(W);
+  for (int sl = 0; sl < n; ++sl) {
+    const int w = sl / 32;
+    for (int k = ctx->topo.up_ptr[sl]; k < ctx->topo.up_ptr[sl + 1]; ++k) {
+      const int u = ctx->topo.up_idx[k] / 32;
+      if (u != w) {
+        deps[w].push_back(u);
+        deps[u].push_back(w);   // w is downstream of u
+      }
+    }
+  }
+  std::vector<int32_t> ptr(W + 1, 0), idx;
+  for (int w = 0; w < W; ++w) {
+    auto &d = deps[w];
+    std::sort(d.begin(), d.end());
+    d.erase(std::unique(d.begin(), d.end()), d.end());
+    ptr[w + 1] = ptr[w] + (int32_t)d.size();
+    idx.insert(idx.end(), d.begin(), d.end());
+  }
+  wg_status st = WG_OK;
+  ctx->sync.dep_ptr = upload_raw<int32_t>(ctx, ptr, st);
+  ctx->sync.dep_idx = upload_raw<int32_t>(ctx, idx, st);
+  ctx->sync.wstep = ctx->alloc<int>(W);
+  if (st != WG_OK) return st;
+  if (!ctx->sync.wstep) return WG_ERR_NOMEM;
+  ctx->sync.nwarps = W;
+  ctx->sync.flow = 1;
+  return WG_OK;
+}
+
 // band-major slot layout of a cell-major [ncell][nb] array
 template <class T, class S>
 std::vector<T> bands_to_slots(const wg_ctx *ctx, const S *cellmajor, int nb) {
@@ -854,6 +888,10 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     ctx->err = "cooperative launch not possible";
     return WG_ERR_DEVICE;
   }
+  if (ctx->layout.idle_warp >= 0) {
+    st = setup_step_flags(ctx.get());
+    if (st != WG_OK) return st;
+  }
   st = wg_reset_balance(ctx.get());
   if (st != WG_OK) return st;
   *out = ctx.release();
@@ -1156,6 +1194,13 @@ wg_status wg_set_member_factors(wg_ctx *ctx, const float *prec_factor, const flo
   if (e == cudaSuccess)
     e = cudaMemcpy((float *)ctx->mem.prec_factor, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice);
   return cuda_fail(ctx, e, "set_member_factors");
+}
+
+wg_status wg_set_step_sync(wg_ctx *ctx, int32_t flags) {
+  if (!ctx || (flags != 0 && flags != 1)) return WG_ERR_INVALID;
+  if (flags == 1 && !ctx->sync.wstep) return WG_ERR_UNSUPPORTED;
+  ctx->sync.flow = flags;
+  return WG_OK;
 }
 
 wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {

@@ -136,6 +136,13 @@ struct DevRingT {
 struct DevSync {
   unsigned int *counter;   // monotonic arrival counter of the grid barrier
   int *error;              // 0 ok, nonzero: a barrier wait exceeded its limit (WG_ERR_TIMEOUT)
+  // step flags of the single-member layout (flow != 0): instead of a grid barrier
+  // per step, each warp of cells publishes the last step it completed (relative
+  // to the launch's first step, -1 before it) and waits only for the warps that
+  // hold its cells' upstream and downstream cells (CSR dep_ptr/dep_idx by warp)
+  int *wstep;
+  const int32_t *dep_ptr, *dep_idx;
+  int32_t nwarps, flow;
 };
 
 }  // namespace wg

@@ -65,6 +65,38 @@ __device__ __forceinline__ bool grid_barrier(const DevSync &sync, unsigned round
   return s_ok != 0;
 }
 
+__device__ __forceinline__ int ld_acquire_int(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_int(int *p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Step flags: wait until every warp this warp depends on has completed step
+// `need` (relative).  The lanes share the dependency list; bounded like the grid
+// barrier (a wait that runs out sets the error word; the caller then stops).
+__device__ __forceinline__ bool wait_deps(const DevSync &sync, int w, int need) {
+  bool ok = true;
+  const int k0 = sync.dep_ptr[w], k1 = sync.dep_ptr[w + 1];
+  for (int k = k0 + (int)(threadIdx.x & 31); k < k1; k += 32) {
+    const int *flag = sync.wstep + sync.dep_idx[k];
+    unsigned it = 0;
+    while (ld_acquire_int(flag) < need) {
+      if (*(volatile int *)sync.error || ++it > WG_BARRIER_SPIN_LIMIT) {
+        atomicExch(sync.error, 1);
+        ok = false;
+        break;
+      }
+      __nanosleep(32);
+    }
+    if (!ok) break;
+  }
+  return __all_sync(0xffffffffu, ok);
+}
+
 __device__ __forceinline__ void neumaier_add(double *acc, size_t k_sum, size_t k_comp, double x) {
   const double s = acc[k_sum];
   const double t = s + x;
@@ -213,13 +245,22 @@ __global__ void __launch_bounds__(kMaxBlockThreads) k_pipeline(DevCellsT<R> c, D
   // single-member layout with one idle warp per block (cell_warps warps of cells)
   long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long gstride = (long long)gridDim.x * blockDim.x;
+  int wpos = -1;   // this warp's position (flow mode): slots 32*wpos .. 32*wpos+31
   if (!ENS && idle_warp >= 0) {
     const int warp = threadIdx.x >> 5;
     const int weff = warp - (warp > idle_warp ? 1 : 0);
     gtid = warp == idle_warp ? (long long)N : ((long long)blockIdx.x * cell_warps + weff) * 32 + (threadIdx.x & 31);
     gstride = (long long)gridDim.x * cell_warps * 32;
+    if (warp != idle_warp) wpos = blockIdx.x * cell_warps + weff;
   }
+  // flow mode: every cell warp owns exactly its 32 slots (one cell per thread)
+  const bool flow = !ENS && sync.flow && idle_warp >= 0 && gstride >= (long long)N;
+  if (flow && (wpos < 0 || wpos >= sync.nwarps)) return;   // no cells: nothing to wait for or publish
   for (int t = t_b; t < t_e; ++t) {
+    if (flow && t > t_b) {
+      if (!wait_deps(sync, wpos, t - t_b - 1)) return;
+      __syncwarp();   // the lanes that acquired the flags order the others' loads
+    }
     if (t - c.nlevel + 1 < ndays) {   // some cell still has a day to compute
       double *q_now = outq + (size_t)(t & 1) * N;
       const double *q_prev = outq + (size_t)((t + 1) & 1) * N;
@@ -300,7 +341,13 @@ __global__ void __launch_bounds__(kMaxBlockThreads) k_pipeline(DevCellsT<R> c, D
         }
       }
     }
-    if (t + 1 < t_e) {
+    if (flow) {
+      // publish step t: every lane's writes of this step (fence, one instruction for
+      // the warp), then the flag (release)
+      __threadfence();
+      __syncwarp();
+      if ((threadIdx.x & 31) == 0) st_release_int(sync.wstep + wpos, t - t_b);
+    } else if (t + 1 < t_e) {
       if (!grid_barrier(sync, (unsigned)(t - t_b))) return;
     }
   }
@@ -471,6 +518,8 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
                             int t_b, int t_e, int blocks, int threads, const WarpLayout &lay, const DevMonthly &mon,
                             cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(sync.counter, 0, sizeof(unsigned), st);
+  if (e == cudaSuccess && sync.flow && sync.wstep)
+    e = cudaMemsetAsync(sync.wstep, 0xff, (size_t)sync.nwarps * sizeof(int), st);   // -1: no step done yet
   if (e != cudaSuccess) return e;
   int cell_warps = lay.cell_warps, idle_warp = mem.members > 1 ? -1 : lay.idle_warp;
   if (idle_warp >= 0 && (threads != lay.threads || (long long)blocks * cell_warps * 32 < (long long)c.n))

@@ -32,7 +32,7 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
            "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells",
-           "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly")
+           "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync")
 
 
 class WgError(RuntimeError):
@@ -113,6 +113,7 @@ def load_library(path: str = LIB_PATH):
     lib.wg_set_active_cells.argtypes = [vp, vp]
     lib.wg_upload_forcing_unf.argtypes = [vp, i32, i32, i32, i32, vp, vp, vp, i32]
     lib.wg_monthly_outputs.argtypes = [vp, i32, i32]
+    lib.wg_set_step_sync.argtypes = [vp, i32]
     lib.wg_get_monthly.argtypes = [vp, i32, i32, i32, vp]
     lib.wg_read_unf.argtypes = [ctypes.c_char_p, vp, i64]
     lib.wg_read_unf.restype = i64
@@ -132,7 +133,8 @@ def load_library(path: str = LIB_PATH):
                  "wg_get_launch_shape", "wg_set_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
                  "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
                  "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async",
-                 "wg_set_active_cells", "wg_upload_forcing_unf", "wg_monthly_outputs", "wg_get_monthly"):
+                 "wg_set_active_cells", "wg_upload_forcing_unf", "wg_monthly_outputs", "wg_get_monthly",
+                 "wg_set_step_sync"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -352,6 +354,10 @@ class Model:
         self._check(self.lib.wg_get_kernel_times(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)),
                     "get_kernel_times")
         return {"vertical_ahead_ms": a.value, "wavefront_ms": b.value, "launch_pairs": n.value}
+
+    def step_sync(self, flags: int):
+        """wg_set_step_sync: 0 grid barrier per step, 1 per-warp step flags."""
+        self._check(self.lib.wg_set_step_sync(self.h, int(flags)), "set_step_sync")
 
     MONTHLY = {"river_avail": 0, "storage": 1, "min_avail": 2, "max_avail": 3}
 
