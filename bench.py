@@ -570,9 +570,35 @@ def run_calibration():
     print(json.dumps(line), flush=True)
 
 
+def run_profile_ensemble(members: int = 256, days: int = 32, warm_days: int = 200):
+    """A short case for ncu of the ensemble kernels: 256 members of the global grid,
+    64 threads per block and 32-step chunks (the autotuner's choice on GB300), a
+    warm-up call that fills the wavefront, then one call of `days` steps (one
+    k_vertical_ahead<float,1> and one k_pipeline<float,1,1> launch):
+      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 2 -c 2 python bench.py --profile-ensemble"""
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_global()
+    nd = warm_days + days
+    P, T, S = sy.forcing(region, nd, seed=2, doy0=1)
+    pf = np.array([np.exp(np.random.default_rng((7, m)).normal(0.0, 0.3)) for m in range(members)], np.float32)
+    m = Model(region, max_days=nd, precision="fp32", members=members, prec_factor=pf, block_threads=64)
+    m.chunk_steps(32)
+    m.upload_forcing(0, P, T, S)
+    m.run_steps(1, 0, nd, 0, warm_days)
+    m.synchronize()
+    t0 = time.perf_counter()
+    m.run_steps(1, 0, nd, warm_days, warm_days + days)
+    m.synchronize()
+    dt = time.perf_counter() - t0
+    print(json.dumps({"profile_case": "ensemble, steady-state wavefront", "members": members, "ncell": region.ncell,
+                      "steps": days, "seconds": dt, "member_cell_days_per_s": members * region.ncell * days / dt}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile", action="store_true", help="run the short ncu case and exit")
+    ap.add_argument("--profile-ensemble", action="store_true", help="run the short ensemble ncu case and exit")
     ap.add_argument("--fine", action="store_true",
                     help="the 5-arc-minute mixed-precision run: FP32 vs FP64 errors at every outlet")
     ap.add_argument("--calibration", action="store_true",
@@ -589,6 +615,9 @@ def main():
         return
     if args.calibration:
         run_calibration()
+        return
+    if args.profile_ensemble:
+        run_profile_ensemble()
         return
     if args.fine:
         run_fine()

@@ -226,11 +226,12 @@ wg_status wg_get_launch_shape(const wg_ctx *ctx, int32_t *threads, int32_t *bloc
  * integrateWGHM.cpp:414-417). */
 wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values);
 
-/* How the wavefront's steps synchronise: 0 = one grid barrier per step; 1 =
- * per-warp step flags, each warp of cells waiting only for the warps that hold
- * its cells' upstream and downstream cells (the default where the
- * single-member layout is in use; WG_ERR_UNSUPPORTED elsewhere).  Results are
- * the same either way. */
+/* How the wavefront's steps synchronise: 0 = one grid barrier per step (the
+ * default); 1 = per-warp step flags, each warp of cells waiting only for the
+ * warps that hold its cells' upstream and downstream cells (single-member
+ * layout only, WG_ERR_UNSUPPORTED elsewhere).  Results are the same either way;
+ * on the global grid the flags measured 3.6 % slower (each warp polls 30-60
+ * neighbours scattered by the slot order). */
 wg_status wg_set_step_sync(wg_ctx *ctx, int32_t flags);
 
 /* Monthly aggregates of the routing outputs, accumulated by the wavefront
