@@ -570,11 +570,13 @@ def run_calibration():
     print(json.dumps(line), flush=True)
 
 
-def run_profile_ensemble(members: int = 256, days: int = 32, warm_days: int = 200):
-    """A short case for ncu of the ensemble kernels: 256 members of the global grid,
-    64 threads per block and 32-step chunks (the autotuner's choice on GB300), a
-    warm-up call that fills the wavefront, then one call of `days` steps (one
-    k_vertical_ahead<float,1> and one k_pipeline<float,1,1> launch):
+def run_profile_ensemble(members: int = 64, days: int = 32, warm_days: int = 200):
+    """A short case for ncu of the ensemble kernels: 64 members of the global grid
+    (a warp is 32 members of one cell, as with 256), 64 threads per block and
+    32-step chunks (the autotuner's choice on GB300), a 32-day ring so that the
+    case holds ~2.5 GB on the device; a warm-up call that fills the wavefront,
+    then one call of `days` steps (one k_vertical_ahead<float,1> and one
+    k_pipeline<float,1,1> launch):
       ncu -k regex:"k_pipeline|k_vertical_ahead" -s 2 -c 2 python bench.py --profile-ensemble"""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
@@ -582,7 +584,7 @@ def run_profile_ensemble(members: int = 256, days: int = 32, warm_days: int = 20
     nd = warm_days + days
     P, T, S = sy.forcing(region, nd, seed=2, doy0=1)
     pf = np.array([np.exp(np.random.default_rng((7, m)).normal(0.0, 0.3)) for m in range(members)], np.float32)
-    m = Model(region, max_days=nd, precision="fp32", members=members, prec_factor=pf, block_threads=64)
+    m = Model(region, max_days=nd, precision="fp32", members=members, prec_factor=pf, block_threads=64, ring_days=32)
     m.chunk_steps(32)
     m.upload_forcing(0, P, T, S)
     m.run_steps(1, 0, nd, 0, warm_days)
