@@ -287,7 +287,10 @@ void join_uploads(wg_ctx *ctx) {
   }
 }
 
-bool valid_block_threads(int threads) { return threads >= 32 && threads <= kMaxBlockThreads && threads % 32 == 0; }
+bool valid_block_threads(int threads, int precision) {
+  const int mx = precision == 0 ? Bounds<double>::threads : Bounds<float>::threads;
+  return threads >= 32 && threads <= mx && threads % 32 == 0;
+}
 
 // Single-member contexts: one block per SM with an equal share of the cells in
 // whole warps plus one idle warp (see place_warps), so that every SM and every
@@ -302,7 +305,7 @@ WarpLayout default_layout(wg_ctx *ctx) {
   const long long W = ((long long)ctx->nstate() + 31) / 32;
   const int cw = (int)std::max<long long>(2, (W + nsm - 1) / nsm);
   const int wpb = cw + 1;
-  if (wpb * 32 > kMaxBlockThreads) return lay;
+  if (ctx->precision != 0 || wpb * 32 > Bounds<double>::threads) return lay;   // FP64 only
   const int blocks = (int)((W + cw - 1) / cw);
   const int fits = ctx->precision == 0 ? pipeline_max_blocks<double>(true, false, wpb * 32)
                                        : pipeline_max_blocks<float>(true, false, wpb * 32);
@@ -605,7 +608,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->precision < 0 || opt->precision > 1) return WG_ERR_UNSUPPORTED;
   if (opt->members < 1 || (opt->members > 1 && opt->precision != 1)) return WG_ERR_UNSUPPORTED;
   if (opt->nstation < 0 || (opt->nstation > 0 && !opt->stations)) return WG_ERR_INVALID;
-  if (opt->block_threads != 0 && !valid_block_threads(opt->block_threads))
+  if (opt->block_threads != 0 && !valid_block_threads(opt->block_threads, opt->precision))
     return WG_ERR_INVALID;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
@@ -1283,7 +1286,7 @@ wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values) {
 }
 
 wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks) {
-  if (!ctx || !valid_block_threads(threads) || blocks < 0) return WG_ERR_INVALID;
+  if (!ctx || !valid_block_threads(threads, ctx->precision) || blocks < 0) return WG_ERR_INVALID;
   const bool ens = ctx->members > 1;
   const int maxb = ctx->precision == 0 ? pipeline_max_blocks<double>(true, ens, threads)
                                        : pipeline_max_blocks<float>(true, ens, threads);

@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) k_vertical(DevCellsT<R> c, DevStateT<R> s
 // ring buffer.  Results equal the in-wavefront computation: the vertical balance of
 // such a cell reads nothing routing writes.
 template <class R, bool ENS>
-__global__ void __launch_bounds__(kMaxBlockThreads) k_vertical_ahead(DevCellsT<R> c, DevStateT<R> st, DevForcing f,
+__global__ void __launch_bounds__(VaBounds<R, ENS>::threads, VaBounds<R, ENS>::min_blocks) k_vertical_ahead(DevCellsT<R> c, DevStateT<R> st, DevForcing f,
                                                         DevMembers mem, DevBalance b, DevRingT<R> ring, int doy0,
                                                         int fday0, int ndays, int t_b, int t_e) {
   const int n = c.n;
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads) k_vertical_ahead(DevCellsT<R
 }
 
 template <class R, bool FUSED, bool ENS>
-__global__ void __launch_bounds__(kMaxBlockThreads) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
+__global__ void __launch_bounds__(Bounds<R>::threads, Bounds<R>::min_blocks) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
                                                   double *outq, double *qst, int doy0, int fday0, int oday0,
                                                   int ndays, int t_b, int t_e, int cell_warps, int idle_warp,

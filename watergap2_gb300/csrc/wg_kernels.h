@@ -8,6 +8,18 @@ namespace wg {
 // Largest block of the day-pipelined kernels (k_pipeline, k_vertical_ahead).
 constexpr int kMaxBlockThreads = 512;
 
+// Launch bounds of the day-pipelined kernels per arithmetic type: FP64 runs one
+// block of up to 512 threads per SM (the single-member layout); FP32 blocks of at
+// most 256 threads, three per SM, so that its registers leave room for the
+// warps that hide its memory latency.
+template <class R> struct Bounds;
+template <> struct Bounds<double> { static constexpr int threads = 512, min_blocks = 1; };
+template <> struct Bounds<float> { static constexpr int threads = 256, min_blocks = 3; };
+// the ensemble's vertical-ahead kernel keeps a member's whole vertical state in
+// registers: two blocks per SM, no spills
+template <class R, bool ENS> struct VaBounds : Bounds<R> {};
+template <> struct VaBounds<float, true> { static constexpr int threads = 256, min_blocks = 2; };
+
 // Thread-to-slot layout of the single-member wavefront: each block runs
 // cell_warps warps of 32 consecutive slots plus one idle warp at warp index
 // idle_warp (idle_warp < 0: plain mapping, slot i on thread i mod the grid).
