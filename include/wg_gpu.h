@@ -105,9 +105,10 @@ typedef struct wg_options {
                               (source/enKF2wghmState.cpp:17-121)                       */
   const float *member_prec_factor;   /* [members] precipitation multiplier, or NULL   */
   const float *member_gamma_factor;  /* [members] multiplier on P_GAMRUN_C, or NULL   */
-  int32_t block_threads;   /* threads per block, a multiple of 32 up to 512; 0 = one   */
-                           /* block per SM for one member (256 if that does not fit),  */
-                           /* 256 for ensembles                                        */
+  int32_t block_threads;   /* threads per block, a multiple of 32: up to 512 (FP64),   */
+                           /* 256 (FP32), 128 (ensembles); 0 = one block per SM for    */
+                           /* one FP64 member, 256 for one FP32 member, 64 for         */
+                           /* ensembles                                                */
   int32_t ring_days;       /* days of vertical outputs buffered between the vertical
                               balance run ahead and routing; 0 = as many as fit in 2 GB */
 } wg_options;

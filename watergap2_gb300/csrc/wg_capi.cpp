@@ -287,8 +287,9 @@ void join_uploads(wg_ctx *ctx) {
   }
 }
 
-bool valid_block_threads(int threads, int precision) {
-  const int mx = precision == 0 ? Bounds<double>::threads : Bounds<float>::threads;
+bool valid_block_threads(int threads, int precision, int members) {
+  const int mx = members > 1 ? PipeBounds<float, true>::threads
+                             : (precision == 0 ? Bounds<double>::threads : Bounds<float>::threads);
   return threads >= 32 && threads <= mx && threads % 32 == 0;
 }
 
@@ -608,7 +609,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->precision < 0 || opt->precision > 1) return WG_ERR_UNSUPPORTED;
   if (opt->members < 1 || (opt->members > 1 && opt->precision != 1)) return WG_ERR_UNSUPPORTED;
   if (opt->nstation < 0 || (opt->nstation > 0 && !opt->stations)) return WG_ERR_INVALID;
-  if (opt->block_threads != 0 && !valid_block_threads(opt->block_threads, opt->precision))
+  if (opt->block_threads != 0 && !valid_block_threads(opt->block_threads, opt->precision, opt->members))
     return WG_ERR_INVALID;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
@@ -629,7 +630,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   ctx->nstation = opt->nstation;
   ctx->members = opt->members;
   ctx->precision = opt->precision;
-  ctx->threads = opt->block_threads ? opt->block_threads : 256;
+  ctx->threads = opt->block_threads ? opt->block_threads : (opt->members > 1 ? 64 : 256);
   if (cudaSetDevice(opt->device) != cudaSuccess) return WG_ERR_DEVICE;
   if (opt->stream) {
     ctx->stream = (cudaStream_t)opt->stream;
@@ -1286,7 +1287,7 @@ wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values) {
 }
 
 wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks) {
-  if (!ctx || !valid_block_threads(threads, ctx->precision) || blocks < 0) return WG_ERR_INVALID;
+  if (!ctx || !valid_block_threads(threads, ctx->precision, ctx->members) || blocks < 0) return WG_ERR_INVALID;
   const bool ens = ctx->members > 1;
   const int maxb = ctx->precision == 0 ? pipeline_max_blocks<double>(true, ens, threads)
                                        : pipeline_max_blocks<float>(true, ens, threads);

@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(VaBounds<R, ENS>::threads, VaBounds<R, ENS>::m
 }
 
 template <class R, bool FUSED, bool ENS>
-__global__ void __launch_bounds__(Bounds<R>::threads, Bounds<R>::min_blocks) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
+__global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS>::min_blocks) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
                                                   double *outq, double *qst, int doy0, int fday0, int oday0,
                                                   int ndays, int t_b, int t_e, int cell_warps, int idle_warp,

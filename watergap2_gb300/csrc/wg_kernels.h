@@ -19,6 +19,10 @@ template <> struct Bounds<float> { static constexpr int threads = 256, min_block
 // registers: two blocks per SM, no spills
 template <class R, bool ENS> struct VaBounds : Bounds<R> {};
 template <> struct VaBounds<float, true> { static constexpr int threads = 256, min_blocks = 2; };
+// the ensemble's wavefront kernel is bound by load latency: at most 128 threads
+// per block and 64 registers, so that an SM holds 32 warps of it (no spills)
+template <class R, bool ENS> struct PipeBounds : Bounds<R> {};
+template <> struct PipeBounds<float, true> { static constexpr int threads = 128, min_blocks = 8; };
 
 // Thread-to-slot layout of the single-member wavefront: each block runs
 // cell_warps warps of 32 consecutive slots plus one idle warp at warp index
