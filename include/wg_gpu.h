@@ -244,7 +244,10 @@ wg_status wg_set_step_sync(wg_ctx *ctx, int32_t flags);
 wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0);
 /* which: 0 river availability [km3/month] (sum of the daily transported volume),
  * 1 sum of the day-end surface-water + groundwater storage [km3 x days],
- * 2 smallest and 3 largest daily transported volume [km3/day];
+ * 2 smallest and 3 largest daily transported volume [km3/day],
+ * 4 cell runoff: transported volume minus upstream inflow (routing.cpp:3933-3939;
+ * in inland sinks minus the inflow) [km3/month],
+ * 5 sum of the daily river velocity [m/s x days];
  * out [nm][ncell][members], cell order. */
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out);
 

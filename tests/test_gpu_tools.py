@@ -183,15 +183,25 @@ def test_monthly_aggregates_match_daily_outputs():
     bounds = [(0, 31), (31, 59), (59, nd)]
     avail, sto = m.monthly("river_avail"), m.monthly("storage")
     lo, hi = m.monthly("min_avail"), m.monthly("max_avail")
+    cro, vel = m.monthly("cell_runoff"), m.monthly("velocity")
+    down = region.downstream
+    up = np.zeros((nd, n))                             # upstream inflow of every cell and day
+    for c in range(n):
+        if down[c] >= 0:
+            up[:, down[c]] += q[:, c]
+    sink = region.ldd < 0
     for k, (a, b) in enumerate(bounds):
-        acc_q, acc_s = np.zeros(n), np.zeros(n)
+        acc_q, acc_s, acc_r = np.zeros(n), np.zeros(n), np.zeros(n)
         for d in range(a, b):                          # day order, as the kernel adds
             acc_q += q[d]
             acc_s += stor[d]
+            acc_r += np.where(sink, 0.0, q[d]) - up[d]
         assert np.array_equal(avail[k], acc_q)
         assert np.allclose(sto[k], acc_s, rtol=1e-12, atol=0)
         assert np.array_equal(lo[k], q[a:b].min(axis=0))
         assert np.array_equal(hi[k], q[a:b].max(axis=0))
+        assert np.allclose(cro[k], acc_r, rtol=1e-9, atol=1e-12 * np.abs(acc_q).max())
+        assert np.all(np.isfinite(vel[k])) and np.all(vel[k] > 0)
 
 
 def test_step_flags_equal_grid_barrier():

@@ -1219,20 +1219,22 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
   ctx->mon = DevMonthly{};
   if (nmonths == 0) return WG_OK;
   const size_t per = (size_t)nmonths * ctx->nstate();
-  e = cudaMalloc((void **)&ctx->mon_buf, 4 * per * sizeof(double));
+  e = cudaMalloc((void **)&ctx->mon_buf, 6 * per * sizeof(double));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "monthly_outputs");
   DevMonthly &m = ctx->mon;
   m.river_avail = ctx->mon_buf;
   m.storage = ctx->mon_buf + per;
   m.min_avail = ctx->mon_buf + 2 * per;
   m.max_avail = ctx->mon_buf + 3 * per;
+  m.cell_runoff = ctx->mon_buf + 4 * per;
+  m.velocity = ctx->mon_buf + 5 * per;
   m.nmonths = nmonths;
   m.doy_day0 = doy_day0;
   int mo = 0;
   for (int k = 1; k < 12; ++k) mo += (doy_day0 >= kFirstDayInMonth[k]) ? 1 : 0;
   m.month0 = mo;
   m.enabled = 1;
-  e = cudaMemsetAsync(ctx->mon_buf, 0, 2 * per * sizeof(double), ctx->stream);
+  e = cudaMemsetAsync(ctx->mon_buf, 0, 6 * per * sizeof(double), ctx->stream);
   if (e == cudaSuccess) e = launch_fill(m.min_avail, per, INFINITY, ctx->stream);
   if (e == cudaSuccess) e = launch_fill(m.max_avail, per, -INFINITY, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -1240,7 +1242,7 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
 }
 
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out) {
-  if (!ctx || !out || which < 0 || which > 3 || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths) return WG_ERR_INVALID;
+  if (!ctx || !out || which < 0 || which > 5 || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths) return WG_ERR_INVALID;
   wg_status st = wg_synchronize(ctx);
   if (st != WG_OK) return st;
   const size_t N = ctx->nstate(), per = (size_t)ctx->mon.nmonths * N;

@@ -107,9 +107,11 @@ struct DevBalance {
 // of the output calendar = year * 12 + month - month0 of output day od, the
 // calendar starting at day-of-year doy_day0 for output day 0.
 struct DevMonthly {
-  double *river_avail;   // sum of the day's transported volume [km3/month]
+  double *river_avail;   // sum of the day's transported volume [km3/month]   (G_monthlyRiverAvail)
   double *storage;       // sum of the day-end surface-water + groundwater storage [km3 x days]
-  double *min_avail, *max_avail;
+  double *min_avail, *max_avail;   // (G_monthlyMin/MaxRiverAvail)
+  double *cell_runoff;   // sum of transported minus upstream inflow [km3/month] (G_monthlyCellRunoff)
+  double *velocity;      // sum of the river velocity [m/s x days]                (G_monthlyVelocity)
   int32_t nmonths, doy_day0, month0, enabled;
 };
 

@@ -337,6 +337,10 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
             mon.max_avail[k] = fmax(mon.max_avail[k], q);
             mon.storage[k] += (double)rs.gw + (double)rs.river + (double)rs.loclake + (double)rs.locwetl +
                               (double)rs.glolake + (double)rs.glowetl + (double)rs.res;
+            // CellRunoff (routing.cpp:3933-3939): in inland sinks the transported
+            // volume leaves the cell as evaporation
+            mon.cell_runoff[k] += ((fl & F_SINK) ? 0. : q) - up;
+            mon.velocity[k] += (double)rt.velocity / 86.4;   // km/d -> m/s
           }
         }
       }

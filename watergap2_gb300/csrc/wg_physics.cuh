@@ -394,6 +394,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
 template <class R>
 struct RTerms {
   R p_ow, e_ow, leak;
+  R velocity;   // river flow velocity of the day [km/d]
 };
 
 // Routing state of one cell (surface water and groundwater storages).
@@ -628,6 +629,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   // river (routing.cpp:3385-3514)
   const R S0 = st.river;
   const R velocity = (c.velo_opt == 0) ? c.default_velocity : river_velocity<R>(c, s, inflow, S0);
+  rt.velocity = velocity;
   const R K = velocity * c.inv_len[s];
   const R eK = m::exp(-K);
   const R omeK = R(1.) - eK;

@@ -359,7 +359,7 @@ class Model:
         """wg_set_step_sync: 0 grid barrier per step, 1 per-warp step flags."""
         self._check(self.lib.wg_set_step_sync(self.h, int(flags)), "set_step_sync")
 
-    MONTHLY = {"river_avail": 0, "storage": 1, "min_avail": 2, "max_avail": 3}
+    MONTHLY = {"river_avail": 0, "storage": 1, "min_avail": 2, "max_avail": 3, "cell_runoff": 4, "velocity": 5}
 
     def monthly_outputs(self, nmonths: int, doy_day0: int = 1):
         """wg_monthly_outputs: accumulate monthly aggregates for nmonths months."""
