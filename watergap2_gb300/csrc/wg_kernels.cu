@@ -150,14 +150,12 @@ __device__ __forceinline__ void store_rstate(const DevStateT<R> &s, size_t i, co
 // One cell-day of the vertical balance on state index si (slot s).
 template <class R>
 __device__ __forceinline__ void vertical_at(const DevCellsT<R> &c, const DevStateT<R> &st, size_t N, int s,
-                                            size_t si, int doy, R Pin, R gamma_soil, float Tf, float SWf,
-                                            VOut<R> &o) {
+                                            size_t si, int doy, R Pin, R gamma_soil, float Tf, float SWf, R laf,
+                                            R prev, VOut<R> &o) {
   const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
   const R ext = c.ext_rad[ti], inv_s0 = c.inv_s0[ti];
   R canopy = st.canopy[si], soil = st.soil[si], gsnow = st.snow[si], psum = st.lai_precsum[si];
   int days = st.lai_days[si], status = st.lai_status[si];
-  const R laf = st.laf[si];
-  const R prev = (st.laf_started[si] == 1) ? st.laf_prev[si] : laf;   // daily.cpp:159-169
   vertical_cell<R>(c, s, gamma_soil, canopy, soil, gsnow, st.snow_band + si, N, days, status, psum, laf, prev, Pin,
                    Tf, SWf, ext, inv_s0, o);
   st.canopy[si] = canopy; st.soil[si] = soil; st.snow[si] = gsnow; st.lai_precsum[si] = psum;
@@ -171,7 +169,10 @@ __global__ void __launch_bounds__(256) k_vertical(DevCellsT<R> c, DevStateT<R> s
   if (s >= c.n || (c.active && !c.active[s])) return;
   const size_t fo = (size_t)fday * c.n + s;
   VOut<R> o;
-  vertical_at<R>(c, st, (size_t)c.n, s, (size_t)s, doy, R(f.prec[fo]), c.gamma[s], f.temp[fo], f.swrad[fo], o);
+  const R laf = st.laf[s];
+  const R prev = (st.laf_started[s] == 1) ? st.laf_prev[s] : laf;   // daily.cpp:159-169
+  vertical_at<R>(c, st, (size_t)c.n, s, (size_t)s, doy, R(f.prec[fo]), c.gamma[s], f.temp[fo], f.swrad[fo], laf, prev,
+                 o);
   v.rs[s] = o.rs; v.gwr[s] = o.gwr; v.transfer[s] = o.transfer; v.owp[s] = o.owp; v.owpet[s] = o.owpet;
   v.land_in[s] = o.land_in; v.land_evap[s] = o.land_evap; v.land_leak[s] = o.land_leak;
 }
@@ -256,6 +257,21 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
   // flow mode: every cell warp owns exactly its 32 slots (one cell per thread)
   const bool flow = !ENS && sync.flow && idle_warp >= 0 && gstride >= (long long)N;
   if (flow && (wpos < 0 || wpos >= sync.nwarps)) return;   // no cells: nothing to wait for or publish
+  // one state per thread for the whole launch: its routing state and land
+  // fractions stay in registers from the first step to the last
+  const bool resident = FUSED && !ENS && gstride >= (long long)N;
+  RState<R> rs_keep{};
+  R laf_keep = R(0), lafp_keep = R(0), fswb_keep = R(0);
+  int started_keep = 0;
+  uint32_t fl_keep = 0;
+  if (resident && gtid < (long long)N) {
+    fl_keep = c.flags[gtid];
+    rs_keep = load_rstate(st, (size_t)gtid, fl_keep);
+    laf_keep = st.laf[gtid];
+    lafp_keep = st.laf_prev[gtid];
+    started_keep = st.laf_started[gtid];
+    if (fl_keep & (F_LOCLAKE | F_LOCWETL | F_GLOWETL)) fswb_keep = st.fswb_next[gtid];
+  }
   for (int t = t_b; t < t_e; ++t) {
     if (flow && t > t_b) {
       if (!wait_deps(sync, wpos, t - t_b - 1)) return;
@@ -277,6 +293,8 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
         const int month = month_of(doy);
         const uint32_t fl = c.flags[s];
         VOut<R> o;
+        const R laf = resident ? laf_keep : st.laf[si];
+        const R laf_prev = resident ? lafp_keep : st.laf_prev[si];
         if (FUSED && !(fl & F_VINLINE)) {
           const size_t ri = (size_t)(d % ring.ring_days) * N + si;
           o.rs = ring.rs[ri];
@@ -291,7 +309,9 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
             Pin *= R(mem.prec_factor[mm]);
             gam *= R(mem.gamma_factor[mm]);
           }
-          vertical_at<R>(c, st, N, s, si, doy, Pin, gam, f.temp[fo], f.swrad[fo], o);
+          const int started = resident ? started_keep : st.laf_started[si];
+          vertical_at<R>(c, st, N, s, si, doy, Pin, gam, f.temp[fo], f.swrad[fo], laf,
+                         started == 1 ? laf_prev : laf, o);   // daily.cpp:159-169
         } else {
           o.rs = v.rs[s]; o.gwr = v.gwr[s]; o.transfer = v.transfer[s]; o.owp = v.owp[s]; o.owpet = v.owpet[s];
           o.land_in = v.land_in[s]; o.land_evap = v.land_evap[s]; o.land_leak = v.land_leak[s];
@@ -300,11 +320,11 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
         double up = 0.;
         const int u0 = c.up_ptr[s], u1 = c.up_ptr[s + 1];
         for (int k = u0; k < u1; ++k) up += __ldcg(q_prev + (size_t)c.up_idx[k] * M + mm);
-        const R laf = st.laf[si], laf_prev = st.laf_prev[si];
-        RState<R> rs = load_rstate(st, si, fl);
+        RState<R> rs = resident ? rs_keep : load_rstate(st, si, fl);
         RTerms<R> rt;
         const R tv = routing_cell<R>(c, s, rs, doy, month, laf, laf_prev, o, up, rt);
-        store_rstate(st, si, rs, fl);
+        if (resident) rs_keep = rs;
+        else store_rstate(st, si, rs, fl);
         q_now[si] = (double)tv;
         if (b.enabled) {
           const double land_f = (double)c.area_f[s] * (double)laf;
@@ -315,13 +335,23 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
         // land-area fraction for the next day (routing.cpp:5034-5188, 5343-5352)
         R next = laf;
         if (fl & (F_LOCLAKE | F_LOCWETL | F_GLOWETL)) {
-          R fswb = st.fswb_next[si];
+          R fswb = resident ? fswb_keep : st.fswb_next[si];
           next = fraction_next<R>(fl, rs, c.ll100[s], c.lw100[s], c.gw100[s], laf, fswb);
-          st.fswb_next[si] = fswb;
-          st.laf[si] = next;
+          if (resident) {
+            fswb_keep = fswb;
+            laf_keep = next;
+          } else {
+            st.fswb_next[si] = fswb;
+            st.laf[si] = next;
+          }
         }
-        st.laf_prev[si] = laf;
-        st.laf_started[si] = 1;
+        if (resident) {
+          lafp_keep = laf;
+          started_keep = 1;
+        } else {
+          st.laf_prev[si] = laf;
+          st.laf_started[si] = 1;
+        }
         const int stn = c.station[s];
         if (stn >= 0) qst[((size_t)(oday0 + d) * c.nstation + stn) * M + mm] = (double)tv;
         if (mon.enabled) {
@@ -354,6 +384,13 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
     } else if (t + 1 < t_e) {
       if (!grid_barrier(sync, (unsigned)(t - t_b))) return;
     }
+  }
+  if (resident && gtid < (long long)N) {
+    store_rstate(st, (size_t)gtid, rs_keep, fl_keep);
+    st.laf[gtid] = laf_keep;
+    st.laf_prev[gtid] = lafp_keep;
+    st.laf_started[gtid] = started_keep;
+    if (fl_keep & (F_LOCLAKE | F_LOCWETL | F_GLOWETL)) st.fswb_next[gtid] = fswb_keep;
   }
 }
 
