@@ -386,6 +386,28 @@ def run_gpu(args, rank, world):
     num_levels = e2e_model.num_levels
 
     del e2e_model
+    # the reference's granularity through the C ABI: one whole-grid calcNewDay launch
+    # and one routing launch (a wavefront over the levels of one day) per day
+    per_day = None
+    if rank == 0:
+        pd_days = 30
+        pd = Model(region, max_days=pd_days, device=local, stream=stream.cuda_stream)
+        pd.upload_forcing(0, P[:pd_days], T[:pd_days], S[:pd_days])
+        for d in range(3):
+            pd.step_vertical(d + 1, d)
+            pd.step_routing(d + 1, d)
+        pd.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for d in range(3, pd_days):
+            pd.step_vertical(d + 1, d)
+            pd.step_routing(d + 1, d)
+        e1.record(stream)
+        pd.synchronize()
+        pd_ms = e0.elapsed_time(e1) / (pd_days - 3)
+        per_day = {"value": region.ncell / (pd_ms / 1000.0), "unit": "cell-days/s", "ms_per_day": pd_ms,
+                   "api": "wg_step_vertical + wg_step_routing per day (the reference's call granularity)"}
+        del pd
     ensemble = None
     if rank == 0 and not os.environ.get("WG_BENCH_NO_ENSEMBLE"):
         ensemble = run_ensemble(args, region, P, T, S, stream, local, value)
@@ -442,6 +464,7 @@ def run_gpu(args, rank, world):
                      "limiter": "FP64 pipe (see fp64), not HBM",
                      "vertical_ahead_launch_ms": va_ms},
         "fp64": fp64,
+        "per_day_api": per_day,
         "ensemble": ensemble,
         "cpu_baseline": {"value": cpu_val, "unit": "cell-days/s", "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_days} days of the same grid ({region.ncell * cpu_days} cell-days, "
