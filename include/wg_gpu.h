@@ -110,7 +110,8 @@ typedef struct wg_options {
                            /* one FP64 member, 256 for one FP32 member, 64 for         */
                            /* ensembles                                                */
   int32_t ring_days;       /* days of vertical outputs buffered between the vertical
-                              balance run ahead and routing; 0 = as many as fit in 2 GB */
+                              balance run ahead and routing; 0 = as many as fit in 8 GB
+                              or an eighth of the free device memory, the smaller */
 } wg_options;
 
 typedef struct wg_ctx wg_ctx;
@@ -287,7 +288,8 @@ wg_status wg_set_chunk_steps(wg_ctx *ctx, int32_t steps);
 int32_t wg_get_chunk_steps(const wg_ctx *ctx);
 
 /* Autotuner: times wg_run_steps(doy0, fday0, ndays, t_begin, t_begin + trial_steps)
- * for each launch shape -- threads per block 64/128/256/512 (for an ensemble,
+ * for each launch shape -- threads per block 64 to 512 as the kernels allow
+ * (FP64 up to 512, FP32 up to 256, ensembles 64 and 128; for an ensemble,
  * the members of one cell that share a block) and chunk steps 8, 16, ... up to
  * the ring capacity -- restoring the model state from a device snapshot before
  * each trial and after the last, and keeps the fastest shape.  The state, the

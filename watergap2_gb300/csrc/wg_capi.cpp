@@ -172,9 +172,6 @@ wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, 
   t.nlevel = dmax + 1;
   t.offset.resize(n);
   for (int i = 0; i < n; ++i) t.offset[i] = dmax - depth[i];
-  t.level_start.assign(t.nlevel + 1, 0);
-  for (int i = 0; i < n; ++i) t.level_start[t.offset[i] + 1]++;
-  for (int l = 0; l < t.nlevel; ++l) t.level_start[l + 1] += t.level_start[l];
   std::vector<int32_t> seq(order);
   std::stable_sort(seq.begin(), seq.end(), [&](int a, int b) {
     const uint32_t ca = cls ? cls[a] : 0u, cb = cls ? cls[b] : 0u;
@@ -423,7 +420,6 @@ wg_status upload_cells(wg_ctx *ctx, const HostConsts &h, DevCellsT<R> &c, double
   std::vector<int32_t> off_slot(ctx->n);
   for (int s = 0; s < ctx->n; ++s) off_slot[s] = ctx->topo.offset[ctx->topo.cell_of_slot[s]];
   c.offset = upload_raw<int32_t>(ctx, off_slot, st);
-  c.level_start = upload_raw<int32_t>(ctx, ctx->topo.level_start, st);
   c.up_ptr = upload_raw<int32_t>(ctx, ctx->topo.up_ptr, st);
   c.up_idx = upload_raw<int32_t>(ctx, ctx->topo.up_idx, st);
   return st;

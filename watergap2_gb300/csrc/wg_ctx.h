@@ -29,7 +29,6 @@ struct Topology {
   std::vector<int32_t> offset;        // per cell: pipeline step offset
   std::vector<int32_t> cell_of_slot;  // slot -> cell
   std::vector<int32_t> slot_of_cell;  // cell -> slot
-  std::vector<int32_t> level_start;   // [nlevel+1]
   std::vector<int32_t> up_ptr, up_idx;// slot space
   int32_t nlevel = 0;
 };

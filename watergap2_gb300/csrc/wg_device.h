@@ -70,7 +70,6 @@ struct DevCellsT {
   // topology in slot space
   const int32_t *up_ptr, *up_idx;               // upstream CSR, each list in reference routing order
   const int32_t *offset;                        // pipeline step offset of the slot
-  const int32_t *level_start;                   // [nlevel+1] first slot of each offset
   const uint8_t *active;                        // per slot: 0 = skipped by the day step (null: all run)
   int32_t nlevel;
   int32_t nstation;

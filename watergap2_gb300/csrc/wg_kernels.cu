@@ -9,9 +9,16 @@
 //                  distance of n to its outlet.  Every upstream cell of n then
 //                  has offset(n) - 1 and delivers day d's outflow exactly one step
 //                  earlier through a two-slot buffer, so one grid barrier per step
-//                  is the only synchronisation and every step keeps all cells busy.
-//                  With ENS the cells carry `members` independent states
-//                  (ensemble members), innermost in memory.
+//                  (or, optionally, per-warp step flags) is the only
+//                  synchronisation and every step keeps all cells busy.  Cells
+//                  without a water body take their vertical balance from the ring
+//                  that k_vertical_ahead filled; the monthly output aggregates are
+//                  accumulated in its epilogue.  With ENS the cells carry
+//                  `members` independent states (ensemble members), innermost in
+//                  memory.
+//  k_vertical_ahead  the vertical balance of the cells without a water body for
+//                  a chunk of days, state in registers, into the ring.
+//  k_unf_forcing / k_gather_forcing  forcing uploads into the slot layout.
 //  k_volume / k_balance_sum   compensated (Neumaier) FP64 water-balance sums.
 //
 // Precision: R = double is the plain FP64 path; R = float keeps state and
