@@ -112,6 +112,10 @@ typedef struct wg_options {
   int32_t ring_days;       /* days of vertical outputs buffered between the vertical
                               balance run ahead and routing; 0 = as many as fit in 8 GB
                               or an eighth of the free device memory, the smaller */
+  int32_t days_per_step;   /* days every cell advances per step of the day-pipelined
+                              wavefront (1..31; 0 = 1): a run of D days takes
+                              ceil(D / days_per_step) + levels - 1 steps.  Results
+                              do not depend on it                                    */
 } wg_options;
 
 typedef struct wg_ctx wg_ctx;

@@ -223,3 +223,46 @@ def test_step_flags_equal_grid_barrier():
     assert np.array_equal(out[0][1], out[1][1])
     for k in out[0][2]:
         assert np.array_equal(out[0][2][k], out[1][2][k]), k
+
+
+@pytest.mark.parametrize("kd", [2, 5])
+def test_days_per_step_equal_one_day_steps(kd):
+    """Several days per wavefront step (each cell routes kd consecutive days in
+    one step) give the same bits as one day per step: discharge, state and water
+    balance, with the run split across calls at arbitrary steps."""
+    from watergap2_gb300.gpu import Model
+    nd = 73                                          # not a multiple of kd
+    region, (P, T, S) = _region_and_forcing(29, nd, doy0=300)
+    ref = Model(region, max_days=nd, record_balance=True)
+    q_ref = ref.run(300, P, T, S)
+    m = Model(region, max_days=nd, record_balance=True, days_per_step=kd)
+    m.upload_forcing(0, P, T, S)
+    total = m.num_steps(nd)
+    assert total == -(-nd // kd) + ref.num_steps(nd) - nd
+    cuts = [0, 3, 11, total // 2, total]
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        m.run_steps(300, 0, nd, a, b)
+    assert np.array_equal(m.discharge(0, nd), q_ref)
+    assert np.array_equal(m.balance(), ref.balance())
+    s_ref, s = ref.get_state(), m.get_state()
+    for k in s_ref:
+        assert np.array_equal(s[k], s_ref[k]), k
+
+
+def test_days_per_step_global_and_ensemble():
+    """Global grid (deep drainage, water bodies) in FP64 with 4 days per step, and
+    an FP32 ensemble with 3 days per step, against one day per step."""
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_global()
+    nd = 30
+    P, T, S = sy.forcing(region, nd, doy0=120)
+    q1 = Model(region, max_days=nd).run(120, P, T, S)
+    m4 = Model(region, max_days=nd, days_per_step=4)
+    m4.chunk_steps(3)                                # several launch pairs
+    assert np.array_equal(m4.run(120, P, T, S), q1)
+    small, (Ps, Ts, Ss) = _region_and_forcing(30, nd, doy0=120)
+    pf = np.exp(np.random.default_rng(7).normal(0.0, 0.3, 40)).astype(np.float32)
+    e1 = Model(small, max_days=nd, precision="fp32", members=40, prec_factor=pf).run(120, Ps, Ts, Ss)
+    e3 = Model(small, max_days=nd, precision="fp32", members=40, prec_factor=pf, days_per_step=3)
+    assert np.array_equal(e3.run(120, Ps, Ts, Ss), e1)

@@ -607,6 +607,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->nstation < 0 || (opt->nstation > 0 && !opt->stations)) return WG_ERR_INVALID;
   if (opt->block_threads != 0 && !valid_block_threads(opt->block_threads, opt->precision, opt->members))
     return WG_ERR_INVALID;
+  if (opt->days_per_step < 0 || opt->days_per_step > 31) return WG_ERR_INVALID;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
     if (r->lct[i] < 1 || r->lct[i] > WG_NLCT) return WG_ERR_INVALID;
@@ -627,6 +628,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   ctx->members = opt->members;
   ctx->precision = opt->precision;
   ctx->threads = opt->block_threads ? opt->block_threads : (opt->members > 1 ? 64 : 256);
+  ctx->days_per_step = opt->days_per_step ? opt->days_per_step : 1;
   if (cudaSetDevice(opt->device) != cudaSuccess) return WG_ERR_DEVICE;
   if (opt->stream) {
     ctx->stream = (cudaStream_t)opt->stream;
@@ -793,7 +795,8 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = (size_t)16 << 30;
     const size_t ring_bytes = std::min<size_t>((size_t)8 << 30, free_b / 8);
     const size_t budget = opt->ring_days > 0 ? (size_t)opt->ring_days : ring_bytes / (2 * elem * N);
-    const int ring = (int)std::max<size_t>(8, std::min<size_t>(budget, (size_t)ctx->max_days));
+    const int ring = (int)std::max<size_t>(std::max(8, ctx->days_per_step), std::min<size_t>(budget, (size_t)ctx->max_days));
+    ctx->rd.days_per_step = ctx->rf.days_per_step = ctx->days_per_step;
     if (ctx->precision == 0) {
       ctx->rd.ring_days = ring;
       ctx->rd.rs = ctx->alloc<double>((size_t)ring * N);
@@ -813,7 +816,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   ctx->forcing.max_days = ctx->max_days;
   ctx->staging_days = std::min(ctx->max_days, 32);
   ctx->staging = ctx->alloc<float>((size_t)ctx->staging_days * n);
-  ctx->outq = ctx->alloc<double>((size_t)2 * N);
+  ctx->outq = ctx->alloc<double>((size_t)2 * ctx->days_per_step * N);   // two steps of days
   ctx->qst = ctx->alloc<double>((size_t)ctx->max_days * std::max(1, ctx->nstation) * ctx->members);
   ctx->balance.enabled = opt->record_balance ? 1 : 0;
   ctx->balance.acc = ctx->alloc<double>(ctx->balance.enabled ? (size_t)10 * N : 1);
@@ -837,7 +840,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     ctx->mem.gamma_factor = mf + ctx->members;
   }
   cudaMemset(ctx->sync.error, 0, sizeof(int));
-  cudaMemset(ctx->outq, 0, (size_t)2 * N * sizeof(double));
+  cudaMemset(ctx->outq, 0, (size_t)2 * ctx->days_per_step * N * sizeof(double));
   cudaMemset(ctx->qst, 0, (size_t)ctx->max_days * std::max(1, ctx->nstation) * ctx->members * sizeof(double));
 
   // ----- start-of-run state, cell order (the reference's set-up sequence; see file header)
@@ -1048,7 +1051,7 @@ wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday) {
 template <class R>
 static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
                                 const DevRingT<R> &ring, int doy0, int fday0, int ndays, int t_b, int t_e) {
-  const int chunk = (ctx->chunk_steps > 0 && ctx->chunk_steps <= ring.ring_days) ? ctx->chunk_steps : ring.ring_days;
+  const int chunk = (ctx->chunk_steps > 0 && ctx->chunk_steps <= ctx->max_chunk()) ? ctx->chunk_steps : ctx->max_chunk();
   for (int a = t_b; a < t_e; a += chunk) {
     const int b = std::min(t_e, a + chunk);
     cudaEvent_t *ev = ctx->timing ? ctx->timing_events() : nullptr;
@@ -1072,7 +1075,7 @@ extern "C" {
 
 wg_status wg_run_steps(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin, int32_t t_end) {
   if (!ctx || doy0 < 1 || doy0 > 365 || fday0 < 0 || ndays <= 0 || fday0 + ndays > ctx->max_days) return WG_ERR_INVALID;
-  const int total = ndays + ctx->topo.nlevel - 1;
+  const int total = ctx->total_steps(ndays);
   if (t_begin < 0 || t_end > total || t_begin > t_end) return WG_ERR_INVALID;
   if (t_begin == t_end) return WG_OK;
   cudaSetDevice(ctx->device);
@@ -1081,11 +1084,11 @@ wg_status wg_run_steps(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, 
                              : run_steps_impl(ctx, ctx->cf, ctx->sf, ctx->vf, ctx->rf, doy0, fday0, ndays, t_begin, t_end);
 }
 
-int32_t wg_run_num_steps(const wg_ctx *ctx, int32_t ndays) { return ctx ? ndays + ctx->topo.nlevel - 1 : 0; }
+int32_t wg_run_num_steps(const wg_ctx *ctx, int32_t ndays) { return ctx ? ctx->total_steps(ndays) : 0; }
 
 wg_status wg_run_days(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays) {
   if (!ctx) return WG_ERR_INVALID;
-  return wg_run_steps(ctx, doy0, fday0, ndays, 0, ndays + ctx->topo.nlevel - 1);
+  return wg_run_steps(ctx, doy0, fday0, ndays, 0, ctx->total_steps(ndays));
 }
 
 wg_status wg_synchronize(wg_ctx *ctx) {

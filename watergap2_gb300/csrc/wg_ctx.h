@@ -79,6 +79,7 @@ struct wg_ctx {
   std::vector<void *> allocs;
   std::string err;
   int chunk_steps = 0;                     // steps per (vertical-ahead, wavefront) launch pair
+  int days_per_step = 1;                   // days every cell advances per wavefront step
   Snapshot *snap = nullptr;                // device copy of the mutable state (autotuner)
   cudaGraph_t graph = nullptr;             // wg_graph_capture
   cudaGraphExec_t graph_exec = nullptr;
@@ -115,5 +116,9 @@ struct wg_ctx {
   }
   size_t nstate() const { return (size_t)n * members; }
   int ring_days() const { return precision == 0 ? rd.ring_days : rf.ring_days; }
+  // longest chunk of wavefront steps one launch pair may run: its days fit the ring
+  int max_chunk() const { return ring_days() / days_per_step; }
+  // wavefront steps of a run of ndays days
+  int total_steps(int ndays) const { return (ndays + days_per_step - 1) / days_per_step + topo.nlevel - 1; }
   void release_tools();   // snapshot and graph (wg_tune.cpp)
 };

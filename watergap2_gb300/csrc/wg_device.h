@@ -132,6 +132,7 @@ template <class R>
 struct DevRingT {
   R *rs, *gwr;
   int32_t ring_days;
+  int32_t days_per_step;   // days every cell advances per wavefront step (K >= 1)
 };
 
 struct DevSync {

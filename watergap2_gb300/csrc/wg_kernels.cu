@@ -202,7 +202,8 @@ __global__ void __launch_bounds__(VaBounds<R, ENS>::threads, VaBounds<R, ENS>::m
     const int mm = ENS ? (int)(i - (size_t)s * M) : 0;
     if ((c.flags[s] & F_VINLINE) || (c.active && !c.active[s])) continue;
     const int off = c.offset[s];
-    const int d0 = max(0, t_b - off), d1 = min(ndays, t_e - off);
+    const int kd = ring.days_per_step;   // step t routes days kd*(t-off) .. kd*(t-off)+kd-1
+    const int d0 = max(0, kd * (t_b - off)), d1 = min(ndays, kd * (t_e - off));
     if (d0 >= d1) continue;
     R canopy = st.canopy[i], soil = st.soil[i], gsnow = st.snow[i], psum = st.lai_precsum[i];
     int days = st.lai_days[i], status = st.lai_status[i];
@@ -249,6 +250,7 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const size_t N = (size_t)n * M;
+  const int kd = FUSED ? ring.days_per_step : 1;   // days per step (the per-day routing call: one)
   // thread -> first state index and stride: plain (i mod the grid), or the
   // single-member layout with one idle warp per block (cell_warps warps of cells)
   long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -284,18 +286,24 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
       if (!wait_deps(sync, wpos, t - t_b - 1)) return;
       __syncwarp();   // the lanes that acquired the flags order the others' loads
     }
-    if (t - c.nlevel + 1 < ndays) {   // some cell still has a day to compute
-      double *q_now = outq + (size_t)(t & 1) * N;
-      const double *q_prev = outq + (size_t)((t + 1) & 1) * N;
+    if (kd * (t - c.nlevel + 1) < ndays) {   // some cell still has a day to compute
+      double *q_now0 = outq + (size_t)(t & 1) * kd * N;
+      const double *q_prev0 = outq + (size_t)((t + 1) & 1) * kd * N;
       // state index i always belongs to thread i mod gstride, so a cell's state is read
       // and written by one thread; only upstream outflows cross threads (read via L2)
       for (long long i = gtid; i < (long long)N; i += gstride) {
         const int s = ENS ? (int)(i / M) : (int)i;
         const int mm = ENS ? (int)(i - (long long)s * M) : 0;
         const size_t si = (size_t)i;
-        const int d = t - c.offset[s];
-        if (d < 0 || d >= ndays) continue;   // this cell's wavefront has not reached it yet / is done
+        const int dbase = kd * (t - c.offset[s]);
+        if (dbase < 0 || dbase >= ndays) continue;   // this cell's wavefront has not reached it yet / is done
         if (c.active && !c.active[s]) continue;
+        // the step's kd days of this cell, in order; the upstream cells routed the
+        // same days one step earlier (their offset is one less)
+        for (int kk = 0; kk < kd && dbase + kk < ndays; ++kk) {
+        const int d = dbase + kk;
+        double *q_now = q_now0 + (size_t)kk * N;
+        const double *q_prev = q_prev0 + (size_t)kk * N;
         const int doy = (doy0 - 1 + d) % 365 + 1;
         const int month = month_of(doy);
         const uint32_t fl = c.flags[s];
@@ -380,6 +388,7 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
             mon.velocity[k] += (double)rt.velocity / 86.4;   // km/d -> m/s
           }
         }
+        }   // days of the step
       }
     }
     if (flow) {

@@ -45,7 +45,7 @@ void list_fields(wg_ctx *ctx, const DevStateT<R> &s, Snapshot &sn) {
   WG_STATE_I(X)
 #undef X
   sn.fields.push_back({(void *)s.snow_band, N * ctx->nband * sizeof(R)});
-  sn.fields.push_back({(void *)ctx->outq, 2 * N * sizeof(double)});
+  sn.fields.push_back({(void *)ctx->outq, 2 * (size_t)ctx->days_per_step * N * sizeof(double)});
   if (ctx->balance.enabled) sn.fields.push_back({(void *)ctx->balance.acc, 10 * N * sizeof(double)});
 }
 
@@ -143,20 +143,20 @@ wg_status wg_get_kernel_times(wg_ctx *ctx, double *vertical_ahead_ms, double *wa
 }
 
 wg_status wg_set_chunk_steps(wg_ctx *ctx, int32_t steps) {
-  if (!ctx || steps < 0 || steps > ctx->ring_days()) return WG_ERR_INVALID;
+  if (!ctx || steps < 0 || steps > ctx->max_chunk()) return WG_ERR_INVALID;
   ctx->chunk_steps = steps;
   return WG_OK;
 }
 
 int32_t wg_get_chunk_steps(const wg_ctx *ctx) {
   if (!ctx) return 0;
-  return (ctx->chunk_steps > 0 && ctx->chunk_steps <= ctx->ring_days()) ? ctx->chunk_steps : ctx->ring_days();
+  return (ctx->chunk_steps > 0 && ctx->chunk_steps <= ctx->max_chunk()) ? ctx->chunk_steps : ctx->max_chunk();
 }
 
 wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin,
                       int32_t trial_steps, wg_tune_result *out) {
   if (!ctx || !out || trial_steps <= 0) return WG_ERR_INVALID;
-  const int total = ndays + ctx->topo.nlevel - 1;
+  const int total = ctx->total_steps(ndays);
   if (t_begin < 0 || t_begin + trial_steps > total) return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
   const int th0 = ctx->threads, ch0 = ctx->chunk_steps;
@@ -169,8 +169,8 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
   // or whole cells per block when a cell has fewer members), chunk lengths 8..ring
   std::vector<int> ths = {64, 128, 256, 512};
   std::vector<int> chs;
-  for (int c = 8; c <= ctx->ring_days(); c *= 2) chs.push_back(c);
-  if (chs.empty() || chs.back() != ctx->ring_days()) chs.push_back(ctx->ring_days());
+  for (int c = 8; c <= ctx->max_chunk(); c *= 2) chs.push_back(c);
+  if (chs.empty() || chs.back() != ctx->max_chunk()) chs.push_back(ctx->max_chunk());
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -234,7 +234,7 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
 
 wg_status wg_graph_capture(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin, int32_t t_end) {
   if (!ctx) return WG_ERR_INVALID;
-  const int total = ndays + ctx->topo.nlevel - 1;
+  const int total = ctx->total_steps(ndays);
   if (doy0 < 1 || doy0 > 365 || fday0 < 0 || ndays <= 0 || fday0 + ndays > ctx->max_days || t_begin < 0 ||
       t_end > total || t_begin >= t_end)
     return WG_ERR_INVALID;

@@ -59,7 +59,7 @@ class _Options(ctypes.Structure):
                 ("record_balance", ctypes.c_int32), ("stations", ctypes.c_void_p), ("stream", ctypes.c_uint64),
                 ("precision", ctypes.c_int32), ("members", ctypes.c_int32), ("member_prec_factor", ctypes.c_void_p),
                 ("member_gamma_factor", ctypes.c_void_p), ("block_threads", ctypes.c_int32),
-                ("ring_days", ctypes.c_int32)]
+                ("ring_days", ctypes.c_int32), ("days_per_step", ctypes.c_int32)]
 
 
 _lib = None
@@ -170,7 +170,8 @@ class Model:
 
     def __init__(self, region: Region, max_days: int = 366, stations=None, record_balance: bool = False,
                  device: int = 0, stream: int = 0, precision: str = "fp64", members: int = 1,
-                 prec_factor=None, gamma_factor=None, block_threads: int = 0, ring_days: int = 0):
+                 prec_factor=None, gamma_factor=None, block_threads: int = 0, ring_days: int = 0,
+                 days_per_step: int = 0):
         self.lib = load_library()
         self.region = region
         self._keep = []
@@ -199,6 +200,7 @@ class Model:
         o.member_gamma_factor = self._gf.ctypes.data if self._gf is not None else None
         o.block_threads = int(block_threads)
         o.ring_days = int(ring_days)
+        o.days_per_step = int(days_per_step)
         self.max_days = int(max_days)
         h = ctypes.c_void_p()
         self._check(self.lib.wg_create(ctypes.byref(r), ctypes.byref(o), ctypes.byref(h)), "wg_create", None)
