@@ -284,15 +284,28 @@ wg_status wg_restore_snapshot(wg_ctx *ctx);
 wg_status wg_kernel_timing(wg_ctx *ctx, int32_t enable);
 wg_status wg_get_kernel_times(wg_ctx *ctx, double *vertical_ahead_ms, double *wavefront_ms, int32_t *launch_pairs);
 
-/* Wavefront steps per launch pair of wg_run_steps (one vertical-ahead launch,
- * then one cooperative wavefront launch): 1 .. the ring capacity
- * (wg_options.ring_days); 0 = the ring capacity.  No counterpart in the
- * reference (it has no day pipelining). */
+/* Wavefront steps per launch of wg_run_steps: 1 .. the ring capacity in steps
+ * (wg_options.ring_days / days_per_step; half of it with the vertical overlap
+ * below); 0 = the default: the ring capacity, or 16 steps with the overlap.
+ * No counterpart in the reference (it has no day pipelining). */
 wg_status wg_set_chunk_steps(wg_ctx *ctx, int32_t steps);
 int32_t wg_get_chunk_steps(const wg_ctx *ctx);
 
+/* Vertical overlap (one FP64 member with the default launch shape): each
+ * wavefront launch of wg_run_steps carries extra warps that run the vertical
+ * balance of the cells without water bodies for the next launch's steps, so the
+ * FP64 pipe has that work while the routing warps wait; the first chunk of each
+ * call runs its vertical balance in a launch of its own.  On by default where
+ * the shape allows it.  enable = 0 switches it off (one vertical-ahead launch
+ * before each wavefront launch); WG_ERR_UNSUPPORTED where the shape has no room
+ * for the extra warps.  wg_get_vertical_overlap returns the extra warps per
+ * block (0: off).  Results are the same bits either way. */
+wg_status wg_set_vertical_overlap(wg_ctx *ctx, int32_t enable);
+int32_t wg_get_vertical_overlap(const wg_ctx *ctx);
+
 /* Autotuner: times wg_run_steps(doy0, fday0, ndays, t_begin, t_begin + trial_steps)
- * for each launch shape -- threads per block 64 to 512 as the kernels allow
+ * for each launch shape -- the context's own (with and without the vertical
+ * overlap), threads per block 64 to 512 as the kernels allow
  * (FP64 up to 512, FP32 up to 256, ensembles 64 and 128; for an ensemble,
  * the members of one cell that share a block) and chunk steps 8, 16, ... up to
  * the ring capacity -- restoring the model state from a device snapshot before

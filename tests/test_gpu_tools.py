@@ -41,7 +41,7 @@ def test_autotune_leaves_state_and_results_unchanged():
     m.run_steps(1, 0, nd, 0, 40)
     st_before = m.get_state()
     res = m.autotune(1, 0, nd, 40, 32)
-    assert res["trials"] >= 4 and res["threads"] in (64, 128, 256, 512) and res["chunk_steps"] >= 1
+    assert res["trials"] >= 4 and res["threads"] % 32 == 0 and res["chunk_steps"] >= 1
     st_after = m.get_state()
     for k in st_before:
         assert np.array_equal(st_before[k], st_after[k]), k
@@ -72,7 +72,9 @@ def test_graph_replay_equals_direct_calls():
     assert np.array_equal(g.discharge(0, nd), q1)
     g.graph_launch()
     assert np.array_equal(g.discharge(0, nd), q2)
-    assert g.launch_count - n0 == 2 * 2 * -(-total // 16)
+    k = -(-total // 16)                             # wavefront launches per pass
+    per_pass = 1 + k if g.vertical_overlap() else 2 * k   # + the vertical-ahead launches
+    assert g.launch_count - n0 == 2 * per_pass
 
 
 def test_ensemble_autotune_and_graph():
@@ -266,3 +268,44 @@ def test_days_per_step_global_and_ensemble():
     e1 = Model(small, max_days=nd, precision="fp32", members=40, prec_factor=pf).run(120, Ps, Ts, Ss)
     e3 = Model(small, max_days=nd, precision="fp32", members=40, prec_factor=pf, days_per_step=3)
     assert np.array_equal(e3.run(120, Ps, Ts, Ss), e1)
+
+
+def test_vertical_overlap_equals_separate_launches():
+    """Vertical balance computed by extra warps of the previous wavefront launch
+    gives the same bits as its own launch before each chunk: discharge, state and
+    water balance, with short chunks and the run split across calls."""
+    from watergap2_gb300.gpu import Model
+    nd = 80
+    region, (P, T, S) = _region_and_forcing(31, nd, doy0=40)
+    out = []
+    for on in (False, True):
+        m = Model(region, max_days=nd, record_balance=True)
+        assert m.vertical_overlap() > 0                  # on by default for one FP64 member
+        m.vertical_overlap(on)
+        assert (m.vertical_overlap() > 0) == on
+        m.chunk_steps(7)
+        m.upload_forcing(0, P, T, S)
+        total = m.num_steps(nd)
+        for a, b in ((0, 5), (5, 30), (30, total)):
+            m.run_steps(40, 0, nd, a, b)
+        out.append((m.discharge(0, nd), m.balance(), m.get_state()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    for k in out[0][2]:
+        assert np.array_equal(out[0][2][k], out[1][2][k]), k
+
+
+def test_vertical_overlap_global_grid():
+    """Global grid (one block per SM, 14 warps of cells): overlap on and off agree."""
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_global()
+    nd = 60
+    P, T, S = sy.forcing(region, nd, doy0=250)
+    q = []
+    for on in (False, True):
+        m = Model(region, max_days=nd, record_balance=True)
+        m.vertical_overlap(on)
+        q.append((m.run(250, P, T, S), m.balance()))
+    assert np.array_equal(q[0][0], q[1][0])
+    assert np.array_equal(q[0][1], q[1][1])

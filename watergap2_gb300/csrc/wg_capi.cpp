@@ -310,12 +310,17 @@ WarpLayout default_layout(wg_ctx *ctx) {
   const int fits_r = ctx->precision == 0 ? pipeline_max_blocks<double>(false, false, wpb * 32)
                                          : pipeline_max_blocks<float>(false, false, wpb * 32);
   if (fits < blocks || fits_r < blocks) return lay;
+  // vertical-balance warps: fill the block to 20 warps (five per sub-partition at
+  // the 96 registers that kernel is built for), if at least two fit
+  const int va = 20 - wpb;
+  if (va >= 2 && pipeline_max_blocks<double>(true, false, (wpb + va) * 32, true) >= blocks) lay.va_warps = va;
   // the idle warp: the last warp of the sub-partition that has the fewest warps
+  // (of those that have any: a block of fewer than four warps leaves some empty)
   int cnt[4] = {0, 0, 0, 0};
   for (int w = 0; w < wpb; ++w) cnt[w & 3]++;
   int sp = 0;
   for (int k = 1; k < 4; ++k)
-    if (cnt[k] < cnt[sp]) sp = k;
+    if (cnt[k] > 0 && cnt[k] < cnt[sp]) sp = k;
   int idle = -1;
   for (int w = 0; w < wpb; ++w)
     if ((w & 3) == sp) idle = w;
@@ -642,6 +647,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   std::vector<uint32_t> cls(n);
   for (int i = 0; i < n; ++i) cls[i] = work_class(r, i);
   if (!opt->block_threads && ctx->members == 1) ctx->layout = default_layout(ctx.get());
+  ctx->va_warps_default = ctx->layout.va_warps;
   wg_status st = build_topology(n, r->downstream, r->rout_order, cls.data(), &ctx->layout, ctx->topo);
   if (st != WG_OK) return st;
   {
@@ -795,7 +801,8 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = (size_t)16 << 30;
     const size_t ring_bytes = std::min<size_t>((size_t)8 << 30, free_b / 8);
     const size_t budget = opt->ring_days > 0 ? (size_t)opt->ring_days : ring_bytes / (2 * elem * N);
-    const int ring = (int)std::max<size_t>(std::max(8, ctx->days_per_step), std::min<size_t>(budget, (size_t)ctx->max_days));
+    const int ring = (int)std::max<size_t>(std::max(8, 2 * ctx->days_per_step),
+                                           std::min<size_t>(budget, (size_t)ctx->max_days));
     ctx->rd.days_per_step = ctx->rf.days_per_step = ctx->days_per_step;
     if (ctx->precision == 0) {
       ctx->rd.ring_days = ring;
@@ -819,14 +826,15 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   ctx->outq = ctx->alloc<double>((size_t)2 * ctx->days_per_step * N);   // two steps of days
   ctx->qst = ctx->alloc<double>((size_t)ctx->max_days * std::max(1, ctx->nstation) * ctx->members);
   ctx->balance.enabled = opt->record_balance ? 1 : 0;
-  ctx->balance.acc = ctx->alloc<double>(ctx->balance.enabled ? (size_t)10 * N : 1);
+  ctx->balance.acc = ctx->alloc<double>(ctx->balance.enabled ? (size_t)WG_BALANCE_ARRAYS * N : 1);
   ctx->vol0 = ctx->alloc<double>(N);
   ctx->partial = ctx->alloc<double>((size_t)8 * ((N + 255) / 256));
   ctx->sync.counter = ctx->alloc<unsigned int>(1);
   ctx->sync.error = ctx->alloc<int>(1);
+  ctx->va_next = ctx->alloc<unsigned int>(1);
   float *mf = ctx->alloc<float>((size_t)2 * ctx->members);
   if (!fb || !ctx->staging || !ctx->outq || !ctx->qst || !ctx->balance.acc || !ctx->vol0 || !ctx->partial ||
-      !ctx->sync.counter || !ctx->sync.error || !mf)
+      !ctx->sync.counter || !ctx->sync.error || !ctx->va_next || !mf)
     return WG_ERR_NOMEM;
   {
     std::vector<float> fac(2 * ctx->members, 1.0f);
@@ -1036,34 +1044,48 @@ wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday) {
   cudaError_t e = ctx->precision == 0
                       ? launch_pipeline(false, ctx->cd, ctx->sd, ctx->vd, ctx->forcing, ctx->mem, ctx->balance,
                                         ctx->rd, ctx->sync, ctx->outq, ctx->qst, doy, 0, oday, 1, 0, ctx->topo.nlevel,
-                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, ctx->stream)
+                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, DevVaWork{}, ctx->stream)
                       : launch_pipeline(false, ctx->cf, ctx->sf, ctx->vf, ctx->forcing, ctx->mem, ctx->balance,
                                         ctx->rf, ctx->sync, ctx->outq, ctx->qst, doy, 0, oday, 1, 0, ctx->topo.nlevel,
-                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, ctx->stream);
+                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, DevVaWork{}, ctx->stream);
   return cuda_fail(ctx, e, "step_routing");
 }
 
 }  // extern "C"
 
-// Steps [t_b, t_e) of the day-pipelined wavefront of a run of ndays days: for each
-// chunk of at most ring_days steps, the vertical balance of the cells without water
-// bodies runs ahead (one launch), then the routing wavefront (one cooperative launch).
+// Steps [t_b, t_e) of the day-pipelined wavefront of a run of ndays days, in
+// chunks: the vertical balance of the cells without water bodies runs ahead of
+// each chunk's routing wavefront (one cooperative launch).  Without the overlap it
+// is one launch before each chunk; with it, the first chunk's runs alone and every
+// wavefront launch carries warps that compute the next chunk's, so the FP64 pipe
+// has their work while the routing warps wait on loads and step barriers.  Every
+// call ends with the vertical state exactly at step t_e either way.
 template <class R>
 static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
                                 const DevRingT<R> &ring, int doy0, int fday0, int ndays, int t_b, int t_e) {
-  const int chunk = (ctx->chunk_steps > 0 && ctx->chunk_steps <= ctx->max_chunk()) ? ctx->chunk_steps : ctx->max_chunk();
+  const bool ov = ctx->overlap();
+  const int chunk = ctx->eff_chunk();
+  DevVaWork vw{};
+  vw.next = ctx->va_next;
+  vw.nitems = (int)((ctx->nstate() + 31) / 32);
   for (int a = t_b; a < t_e; a += chunk) {
     const int b = std::min(t_e, a + chunk);
     cudaEvent_t *ev = ctx->timing ? ctx->timing_events() : nullptr;
     if (ev) cudaEventRecord(ev[0], ctx->stream);
-    cudaError_t e = launch_vertical_ahead(c, s, ctx->forcing, ctx->mem, ctx->balance, ring, doy0, fday0, ndays, a, b,
-                                          ctx->blocks_fused, ctx->threads, ctx->stream);
-    ctx->launches++;
+    cudaError_t e = cudaSuccess;
+    if (!ov || a == t_b) {
+      e = launch_vertical_ahead(c, s, ctx->forcing, ctx->mem, ctx->balance, ring, doy0, fday0, ndays, a, b,
+                                ctx->blocks_fused, ctx->threads, ctx->stream);
+      ctx->launches++;
+    }
     if (ev) cudaEventRecord(ev[1], ctx->stream);
+    vw.t_b = b;
+    vw.t_e = std::min(t_e, b + chunk);
+    vw.warps = (ov && vw.t_e > vw.t_b) ? ctx->layout.va_warps : 0;
     if (e == cudaSuccess)
       e = launch_pipeline(true, c, s, v, ctx->forcing, ctx->mem, ctx->balance, ring, ctx->sync, ctx->outq, ctx->qst,
                           doy0, fday0, fday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->layout, ctx->mon,
-                          ctx->stream);
+                          vw, ctx->stream);
     ctx->launches++;
     if (ev) cudaEventRecord(ev[2], ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "run_steps");
@@ -1124,7 +1146,7 @@ wg_status wg_reset_balance(wg_ctx *ctx) {
   cudaSetDevice(ctx->device);
   cudaError_t e = cudaSuccess;
   if (ctx->balance.enabled)
-    e = cudaMemsetAsync(ctx->balance.acc, 0, (size_t)10 * ctx->nstate() * sizeof(double), ctx->stream);
+    e = cudaMemsetAsync(ctx->balance.acc, 0, (size_t)WG_BALANCE_ARRAYS * ctx->nstate() * sizeof(double), ctx->stream);
   if (e == cudaSuccess)
     e = ctx->precision == 0 ? launch_volume(ctx->cd, ctx->sd, ctx->members, ctx->vol0, ctx->stream)
                             : launch_volume(ctx->cf, ctx->sf, ctx->members, ctx->vol0, ctx->stream);

@@ -80,6 +80,8 @@ struct wg_ctx {
   std::string err;
   int chunk_steps = 0;                     // steps per (vertical-ahead, wavefront) launch pair
   int days_per_step = 1;                   // days every cell advances per wavefront step
+  int va_warps_default = 0;                // vertical-balance warps the layout was sized for
+  unsigned int *va_next = nullptr;         // their work counter
   Snapshot *snap = nullptr;                // device copy of the mutable state (autotuner)
   cudaGraph_t graph = nullptr;             // wg_graph_capture
   cudaGraphExec_t graph_exec = nullptr;
@@ -118,6 +120,16 @@ struct wg_ctx {
   int ring_days() const { return precision == 0 ? rd.ring_days : rf.ring_days; }
   // longest chunk of wavefront steps one launch pair may run: its days fit the ring
   int max_chunk() const { return ring_days() / days_per_step; }
+  // the wavefront launches carry vertical-balance warps for the next chunk
+  bool overlap() const { return layout.va_warps > 0 && layout.idle_warp >= 0 && threads == layout.threads; }
+  // longest chunk: with the overlap the ring holds this chunk's and the next one's days
+  int chunk_cap() const { return overlap() ? max_chunk() / 2 : max_chunk(); }
+  // steps per launch: the set chunk length if it fits, else 16 with the overlap
+  // (the first chunk of each call runs its vertical balance alone) or the ring
+  int eff_chunk() const {
+    if (chunk_steps > 0 && chunk_steps <= chunk_cap()) return chunk_steps;
+    return overlap() ? std::min(16, chunk_cap()) : chunk_cap();
+  }
   // wavefront steps of a run of ndays days
   int total_steps(int ndays) const { return (ndays + days_per_step - 1) / days_per_step + topo.nlevel - 1; }
   void release_tools();   // snapshot and graph (wg_tune.cpp)

@@ -96,10 +96,16 @@ struct DevVertT {
 };
 
 // Per-(cell, member) water-balance accumulators, FP64, Neumaier-compensated.
+// Arrays 0-4: in, evap, out, up, leak; 5-9 their compensations; 10/11 the land leak
+// of the cells whose vertical balance runs ahead of routing and its compensation
+// (kept apart from 4, which the wavefront adds the river's leak of those cells to,
+// so that both can run at the same time).  The wavefront adds no in/evap for such
+// cells: their routing adds exactly zero open-water terms.
 struct DevBalance {
-  double *acc;      // [10][n*members]: in, evap, out, up, leak and their compensations
+  double *acc;      // [12][n*members]
   int32_t enabled;
 };
+constexpr int WG_BALANCE_ARRAYS = 12;
 
 // Monthly aggregates of the routing outputs (routing.cpp:3964-4238: G_monthlyRiverAvail,
 // G_monthlyMin/MaxRiverAvail, monthly storage), [nmonths][n*members] each; month m
@@ -133,6 +139,15 @@ struct DevRingT {
   R *rs, *gwr;
   int32_t ring_days;
   int32_t days_per_step;   // days every cell advances per wavefront step (K >= 1)
+};
+
+// Vertical balance of the cells without water bodies run by extra warps of the
+// wavefront launch (warps >= the block's routing warps) for the NEXT launch's
+// steps [t_b, t_e): the warps take 32 consecutive slots at a time from the
+// counter `next` until nitems groups are taken; warps = 0: no such warps.
+struct DevVaWork {
+  unsigned int *next;
+  int32_t warps, t_b, t_e, nitems;
 };
 
 struct DevSync {

@@ -29,6 +29,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "wg_device.h"
 #include "wg_kernels.h"
@@ -47,8 +48,16 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 
 // Grid-wide barrier for a cooperative launch (all blocks co-resident).  The
 // counter only grows; round r completes when it reaches (r+1)*gridDim.x.
-__device__ __forceinline__ bool grid_barrier(const DevSync &sync, unsigned round) {
-  __syncthreads();
+// Block-level part of the grid barrier: all threads of the block, or (nthr <
+// blockDim.x) the first nthr threads only, on hardware barrier 1, while the
+// block's other warps do independent work.
+__device__ __forceinline__ void block_sync(int nthr) {
+  if (nthr == (int)blockDim.x) __syncthreads();
+  else asm volatile("bar.sync 1, %0;" ::"r"(nthr) : "memory");
+}
+
+__device__ __forceinline__ bool grid_barrier(const DevSync &sync, unsigned round, int nthr) {
+  block_sync(nthr);
   __shared__ int s_ok;
   if (threadIdx.x == 0) {
     const unsigned target = (round + 1u) * gridDim.x;
@@ -68,7 +77,7 @@ __device__ __forceinline__ bool grid_barrier(const DevSync &sync, unsigned round
     __threadfence();
     s_ok = ok;
   }
-  __syncthreads();
+  block_sync(nthr);
   return s_ok != 0;
 }
 
@@ -112,6 +121,13 @@ __device__ __forceinline__ void neumaier_add(double *acc, size_t k_sum, size_t k
   else c += (x - t) + s;
   acc[k_sum] = t;
   acc[k_comp] = c;
+}
+
+__device__ __forceinline__ void record_routing_balance(const DevBalance &b, size_t N, size_t i, double up,
+                                                       double out, double leak) {
+  neumaier_add(b.acc, 2 * N + i, 7 * N + i, out);
+  neumaier_add(b.acc, 3 * N + i, 8 * N + i, up);
+  neumaier_add(b.acc, 4 * N + i, 9 * N + i, leak);
 }
 
 __device__ __forceinline__ void record_balance(const DevBalance &b, size_t N, size_t i, double in, double evap,
@@ -190,66 +206,97 @@ __global__ void __launch_bounds__(256) k_vertical(DevCellsT<R> c, DevStateT<R> s
 // the vertical state in registers, and leaves surface runoff and recharge in the
 // ring buffer.  Results equal the in-wavefront computation: the vertical balance of
 // such a cell reads nothing routing writes.
+// One (cell, member) state index i of the vertical balance run ahead: the days
+// the wavefront steps [t_b, t_e) will route, vertical state in registers, surface
+// runoff and recharge into the ring; balance terms into arrays 0, 1 and 10.
+template <class R, bool ENS>
+__device__ __forceinline__ void va_cell(const DevCellsT<R> &c, const DevStateT<R> &st, const DevForcing &f,
+                                        const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
+                                        int doy0, int fday0, int ndays, int t_b, int t_e, size_t i, size_t N) {
+  const int n = c.n;
+  const int M = ENS ? mem.members : 1;
+  const int s = ENS ? (int)(i / M) : (int)i;
+  const int mm = ENS ? (int)(i - (size_t)s * M) : 0;
+  if ((c.flags[s] & F_VINLINE) || (c.active && !c.active[s])) return;
+  const int off = c.offset[s];
+  const int kd = ring.days_per_step;   // step t routes days kd*(t-off) .. kd*(t-off)+kd-1
+  const int d0 = max(0, kd * (t_b - off)), d1 = min(ndays, kd * (t_e - off));
+  if (d0 >= d1) return;
+  R canopy = st.canopy[i], soil = st.soil[i], gsnow = st.snow[i], psum = st.lai_precsum[i];
+  int days = st.lai_days[i], status = st.lai_status[i];
+  const R laf = st.laf[i];   // constant for these cells (no water body)
+  R pf = R(1), gam = c.gamma[s];
+  if (ENS) {
+    pf = R(mem.prec_factor[mm]);
+    gam *= R(mem.gamma_factor[mm]);
+  }
+  double acc_in = 0., acc_ev = 0., acc_lk = 0.;
+  const double land_f = (double)c.area_f[s] * (double)laf;
+  for (int d = d0; d < d1; ++d) {
+    const int doy = (doy0 - 1 + d) % 365 + 1;
+    const size_t fo = (size_t)(fday0 + d) * n + s;
+    const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
+    VOut<R> o;
+    vertical_cell<R>(c, s, gam, canopy, soil, gsnow, st.snow_band + i, N, days, status, psum, laf, laf,
+                     R(f.prec[fo]) * pf, f.temp[fo], f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o);
+    const size_t ri = (size_t)(d % ring.ring_days) * N + i;
+    ring.rs[ri] = o.rs;
+    ring.gwr[ri] = o.gwr;
+    if (b.enabled) {
+      acc_in += (double)o.land_in * land_f;
+      acc_ev += (double)o.land_evap * land_f;
+      acc_lk += (double)o.land_leak * land_f;
+    }
+  }
+  st.canopy[i] = canopy; st.soil[i] = soil; st.snow[i] = gsnow; st.lai_precsum[i] = psum;
+  st.lai_days[i] = days; st.lai_status[i] = status;
+  if (b.enabled) {
+    neumaier_add(b.acc, 0 * N + i, 5 * N + i, acc_in);
+    neumaier_add(b.acc, 1 * N + i, 6 * N + i, acc_ev);
+    neumaier_add(b.acc, 10 * N + i, 11 * N + i, acc_lk);
+  }
+}
+
+// Vertical balance ahead of routing for the cells whose land fraction and open-water
+// fluxes do not depend on routing (no water body): each thread takes one
+// (cell, member) through the days the pipeline steps [t_b, t_e) will route, with
+// the vertical state in registers, and leaves surface runoff and recharge in the
+// ring buffer.  Results equal the in-wavefront computation: the vertical balance of
+// such a cell reads nothing routing writes.
 template <class R, bool ENS>
 __global__ void __launch_bounds__(VaBounds<R, ENS>::threads, VaBounds<R, ENS>::min_blocks) k_vertical_ahead(DevCellsT<R> c, DevStateT<R> st, DevForcing f,
                                                         DevMembers mem, DevBalance b, DevRingT<R> ring, int doy0,
                                                         int fday0, int ndays, int t_b, int t_e) {
-  const int n = c.n;
-  const int M = ENS ? mem.members : 1;
-  const size_t N = (size_t)n * M;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-    const int s = ENS ? (int)(i / M) : (int)i;
-    const int mm = ENS ? (int)(i - (size_t)s * M) : 0;
-    if ((c.flags[s] & F_VINLINE) || (c.active && !c.active[s])) continue;
-    const int off = c.offset[s];
-    const int kd = ring.days_per_step;   // step t routes days kd*(t-off) .. kd*(t-off)+kd-1
-    const int d0 = max(0, kd * (t_b - off)), d1 = min(ndays, kd * (t_e - off));
-    if (d0 >= d1) continue;
-    R canopy = st.canopy[i], soil = st.soil[i], gsnow = st.snow[i], psum = st.lai_precsum[i];
-    int days = st.lai_days[i], status = st.lai_status[i];
-    const R laf = st.laf[i];   // constant for these cells (no water body)
-    R pf = R(1), gam = c.gamma[s];
-    if (ENS) {
-      pf = R(mem.prec_factor[mm]);
-      gam *= R(mem.gamma_factor[mm]);
-    }
-    double acc_in = 0., acc_ev = 0., acc_lk = 0.;
-    const double land_f = (double)c.area_f[s] * (double)laf;
-    for (int d = d0; d < d1; ++d) {
-      const int doy = (doy0 - 1 + d) % 365 + 1;
-      const size_t fo = (size_t)(fday0 + d) * n + s;
-      const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
-      VOut<R> o;
-      vertical_cell<R>(c, s, gam, canopy, soil, gsnow, st.snow_band + i, N, days, status, psum, laf, laf,
-                       R(f.prec[fo]) * pf, f.temp[fo], f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o);
-      const size_t ri = (size_t)(d % ring.ring_days) * N + i;
-      ring.rs[ri] = o.rs;
-      ring.gwr[ri] = o.gwr;
-      if (b.enabled) {
-        acc_in += (double)o.land_in * land_f;
-        acc_ev += (double)o.land_evap * land_f;
-        acc_lk += (double)o.land_leak * land_f;
-      }
-    }
-    st.canopy[i] = canopy; st.soil[i] = soil; st.snow[i] = gsnow; st.lai_precsum[i] = psum;
-    st.lai_days[i] = days; st.lai_status[i] = status;
-    if (b.enabled) {
-      neumaier_add(b.acc, 0 * N + i, 5 * N + i, acc_in);
-      neumaier_add(b.acc, 1 * N + i, 6 * N + i, acc_ev);
-      neumaier_add(b.acc, 4 * N + i, 9 * N + i, acc_lk);
-    }
-  }
+  const size_t N = (size_t)c.n * (ENS ? mem.members : 1);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+    va_cell<R, ENS>(c, st, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e, i, N);
 }
 
-template <class R, bool FUSED, bool ENS>
-__global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS>::min_blocks) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
+template <class R, bool FUSED, bool ENS, bool VAW>
+__global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R, ENS, VAW>::min_blocks) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
                                                   double *outq, double *qst, int doy0, int fday0, int oday0,
                                                   int ndays, int t_b, int t_e, int cell_warps, int idle_warp,
-                                                  DevMonthly mon) {
+                                                  DevMonthly mon, DevVaWork vw) {
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const size_t N = (size_t)n * M;
+  if (VAW && (int)(threadIdx.x >> 5) >= (int)(blockDim.x >> 5) - vw.warps) {
+    // the block's last vw.warps warps: vertical balance ahead for the next launch's
+    // steps, 32 slots at a time from a shared counter, filling the FP64 pipe while
+    // the routing warps wait on loads and step barriers
+    const unsigned lane = threadIdx.x & 31;
+    for (;;) {
+      unsigned g = 0;
+      if (lane == 0) g = atomicAdd(vw.next, 1u);
+      g = __shfl_sync(0xffffffffu, g, 0);
+      if (g >= (unsigned)vw.nitems) break;
+      const size_t i = (size_t)g * 32 + lane;
+      if (i < N) va_cell<R, ENS>(c, st, f, mem, b, ring, doy0, fday0, ndays, vw.t_b, vw.t_e, i, N);
+    }
+    return;
+  }
+  const int route_threads = VAW ? (int)blockDim.x - 32 * vw.warps : (int)blockDim.x;
   const int kd = FUSED ? ring.days_per_step : 1;   // days per step (the per-day routing call: one)
   // thread -> first state index and stride: plain (i mod the grid), or the
   // single-member layout with one idle warp per block (cell_warps warps of cells)
@@ -264,7 +311,7 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
     if (warp != idle_warp) wpos = blockIdx.x * cell_warps + weff;
   }
   // flow mode: every cell warp owns exactly its 32 slots (one cell per thread)
-  const bool flow = !ENS && sync.flow && idle_warp >= 0 && gstride >= (long long)N;
+  const bool flow = !ENS && !VAW && sync.flow && idle_warp >= 0 && gstride >= (long long)N;
   if (flow && (wpos < 0 || wpos >= sync.nwarps)) return;   // no cells: nothing to wait for or publish
   // one state per thread for the whole launch: its routing state and land
   // fractions stay in registers from the first step to the last
@@ -343,9 +390,12 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
         q_now[si] = (double)tv;
         if (b.enabled) {
           const double land_f = (double)c.area_f[s] * (double)laf;
-          record_balance(b, N, si, (double)o.land_in * land_f + (double)rt.p_ow,
-                         (double)o.land_evap * land_f + (double)rt.e_ow, up, (double)tv,
-                         (double)o.land_leak * land_f + (double)rt.leak);
+          if (!FUSED || (fl & F_VINLINE))
+            record_balance(b, N, si, (double)o.land_in * land_f + (double)rt.p_ow,
+                           (double)o.land_evap * land_f + (double)rt.e_ow, up, (double)tv,
+                           (double)o.land_leak * land_f + (double)rt.leak);
+          else   // vertical ran ahead: its land terms are in arrays 0, 1 and 10
+            record_routing_balance(b, N, si, up, (double)tv, (double)rt.leak);
         }
         // land-area fraction for the next day (routing.cpp:5034-5188, 5343-5352)
         R next = laf;
@@ -398,7 +448,7 @@ __global__ void __launch_bounds__(PipeBounds<R, ENS>::threads, PipeBounds<R, ENS
       __syncwarp();
       if ((threadIdx.x & 31) == 0) st_release_int(sync.wstep + wpos, t - t_b);
     } else if (t + 1 < t_e) {
-      if (!grid_barrier(sync, (unsigned)(t - t_b))) return;
+      if (!grid_barrier(sync, (unsigned)(t - t_b), route_threads)) return;
     }
   }
   if (resident && gtid < (long long)N) {
@@ -435,7 +485,7 @@ __global__ void __launch_bounds__(256) k_balance_sum(DevCellsT<R> c, DevStateT<R
     const double ev = b.acc[1 * N + i] + b.acc[6 * N + i];
     const double out = b.acc[2 * N + i] + b.acc[7 * N + i];
     const double up = b.acc[3 * N + i] + b.acc[8 * N + i];
-    const double lk = b.acc[4 * N + i] + b.acc[9 * N + i];
+    const double lk = (b.acc[4 * N + i] + b.acc[9 * N + i]) + (b.acc[10 * N + i] + b.acc[11 * N + i]);
     val[0] = vnow;
     val[1] = in;
     val[2] = ev;
@@ -554,17 +604,23 @@ cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, 
 }
 
 template <class R>
-static const void *pipeline_fn(bool fused, bool ens) {
-  if (ens) return (const void *)k_pipeline<R, true, true>;
-  return fused ? (const void *)k_pipeline<R, true, false> : (const void *)k_pipeline<R, false, false>;
+static const void *pipeline_fn(bool fused, bool ens, bool vaw) {
+  if (ens) return (const void *)k_pipeline<R, true, true, false>;
+  if (vaw) {   // FP64 single member only
+    if constexpr (std::is_same<R, double>::value) return (const void *)k_pipeline<R, true, false, true>;
+    return nullptr;
+  }
+  return fused ? (const void *)k_pipeline<R, true, false, false> : (const void *)k_pipeline<R, false, false, false>;
 }
 
 template <class R>
-int pipeline_max_blocks(bool fused, bool ens, int threads) {
+int pipeline_max_blocks(bool fused, bool ens, int threads, bool vaw) {
   int dev = 0, nsm = 0, per = 0;
+  const void *fn = pipeline_fn<R>(fused, ens, vaw);
+  if (!fn) return 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pipeline_fn<R>(fused, ens), threads, 0);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0) != cudaSuccess) return 0;
   return per * nsm;
 }
 
@@ -573,19 +629,28 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
                             const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
                             const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
                             int t_b, int t_e, int blocks, int threads, const WarpLayout &lay, const DevMonthly &mon,
-                            cudaStream_t st) {
+                            const DevVaWork &vw, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(sync.counter, 0, sizeof(unsigned), st);
   if (e == cudaSuccess && sync.flow && sync.wstep)
     e = cudaMemsetAsync(sync.wstep, 0xff, (size_t)sync.nwarps * sizeof(int), st);   // -1: no step done yet
+  const bool vaw = fused && vw.warps > 0;
+  if (e == cudaSuccess && vaw) e = cudaMemsetAsync(vw.next, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
   int cell_warps = lay.cell_warps, idle_warp = mem.members > 1 ? -1 : lay.idle_warp;
   if (idle_warp >= 0 && (threads != lay.threads || (long long)blocks * cell_warps * 32 < (long long)c.n))
     idle_warp = -1;   // the layout does not describe this launch: plain mapping
+  // vertical-balance warps only on the single-member layout they were sized for
+  if (vaw && (idle_warp < 0 || mem.members > 1 || vw.warps != lay.va_warps)) return cudaErrorInvalidConfiguration;
+  DevVaWork vwk = vw;
+  if (!vaw) vwk.warps = 0;
   void *args[] = {(void *)&c,    (void *)&s,    (void *)&v,     (void *)&f,     (void *)&mem,   (void *)&b,
                   (void *)&ring, (void *)&sync, (void *)&outq,  (void *)&qst,   (void *)&doy0,  (void *)&fday0,
                   (void *)&oday0, (void *)&ndays, (void *)&t_b, (void *)&t_e, (void *)&cell_warps,
-                  (void *)&idle_warp, (void *)&mon};
+                  (void *)&idle_warp, (void *)&mon, (void *)&vwk};
   const bool ens = mem.members > 1;
+  const void *fn = pipeline_fn<R>(fused, ens, vaw);
+  if (!fn) return cudaErrorInvalidConfiguration;
+  if (vaw) threads += 32 * vw.warps;
   // cooperative (all blocks resident, or the launch fails) through the launch
   // attribute, which stream capture records into a graph kernel node
   cudaLaunchConfig_t cfg = {};
@@ -598,7 +663,7 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelExC(&cfg, pipeline_fn<R>(fused, ens), args);
+  return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 template <class R>
@@ -622,12 +687,12 @@ cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int
 #define WG_INSTANTIATE(R)                                                                                          \
   template cudaError_t launch_vertical<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,        \
                                           const DevForcing &, int, int, cudaStream_t);                             \
-  template int pipeline_max_blocks<R>(bool, bool, int);                                                           \
+  template int pipeline_max_blocks<R>(bool, bool, int, bool);                                                           \
   template cudaError_t launch_pipeline<R>(bool, const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,  \
                                           const DevForcing &, const DevMembers &, const DevBalance &,             \
                                           const DevRingT<R> &, const DevSync &, double *, double *, int, int,     \
                                           int, int, int, int, int, int, const WarpLayout &, const DevMonthly &,    \
-                                          cudaStream_t);                                                          \
+                                          const DevVaWork &, cudaStream_t);                                       \
   template cudaError_t launch_vertical_ahead<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevForcing &,   \
                                                 const DevMembers &, const DevBalance &, const DevRingT<R> &, int,  \
                                                 int, int, int, int, int, int, cudaStream_t);                       \

@@ -23,6 +23,10 @@ template <> struct VaBounds<float, true> { static constexpr int threads = 256, m
 // per block and 64 registers, so that an SM holds 32 warps of it (no spills)
 template <class R, bool ENS> struct PipeBounds : Bounds<R> {};
 template <> struct PipeBounds<float, true> { static constexpr int threads = 128, min_blocks = 8; };
+// the single-member FP64 wavefront with vertical-balance warps in the same block:
+// up to 20 warps (5 per SM sub-partition, 96 registers each)
+template <class R, bool ENS, bool VAW> struct WaveBounds : PipeBounds<R, ENS> {};
+template <class R> struct WaveBounds<R, false, true> { static constexpr int threads = 640, min_blocks = 1; };
 
 // Thread-to-slot layout of the single-member wavefront: each block runs
 // cell_warps warps of 32 consecutive slots plus one idle warp at warp index
@@ -30,6 +34,7 @@ template <> struct PipeBounds<float, true> { static constexpr int threads = 128,
 struct WarpLayout {
   int cell_warps = 0;
   int idle_warp = -1;
+  int va_warps = 0;    // vertical-balance warps appended to each wavefront block (0: none)
   int blocks = 0;
   int threads = 0;
 };
@@ -42,13 +47,13 @@ template <class R>
 cudaError_t launch_vertical(const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v, const DevForcing &f,
                             int doy, int fday, cudaStream_t st);
 template <class R>
-int pipeline_max_blocks(bool fused, bool ens, int threads);
+int pipeline_max_blocks(bool fused, bool ens, int threads, bool vaw = false);
 template <class R>
 cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
                             const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
                             const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
                             int t_b, int t_e, int blocks, int threads, const WarpLayout &lay, const DevMonthly &mon,
-                            cudaStream_t st);
+                            const DevVaWork &vw, cudaStream_t st);
 cudaError_t launch_fill(double *p, size_t n, double v, cudaStream_t st);
 template <class R>
 cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, const DevForcing &f,

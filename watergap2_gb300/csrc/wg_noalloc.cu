@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(kNoallocThreads) k_balance_partials_static(Dev
     const double ev = b.acc[1 * N + i] + b.acc[6 * N + i];
     const double out = b.acc[2 * N + i] + b.acc[7 * N + i];
     const double up = b.acc[3 * N + i] + b.acc[8 * N + i];
-    const double lk = b.acc[4 * N + i] + b.acc[9 * N + i];
+    const double lk = (b.acc[4 * N + i] + b.acc[9 * N + i]) + (b.acc[10 * N + i] + b.acc[11 * N + i]);
     val[0] = vnow;
     val[1] = in;
     val[2] = ev;

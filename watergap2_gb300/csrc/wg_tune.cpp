@@ -46,7 +46,7 @@ void list_fields(wg_ctx *ctx, const DevStateT<R> &s, Snapshot &sn) {
 #undef X
   sn.fields.push_back({(void *)s.snow_band, N * ctx->nband * sizeof(R)});
   sn.fields.push_back({(void *)ctx->outq, 2 * (size_t)ctx->days_per_step * N * sizeof(double)});
-  if (ctx->balance.enabled) sn.fields.push_back({(void *)ctx->balance.acc, 10 * N * sizeof(double)});
+  if (ctx->balance.enabled) sn.fields.push_back({(void *)ctx->balance.acc, WG_BALANCE_ARRAYS * N * sizeof(double)});
 }
 
 wg_status snapshot_save(wg_ctx *ctx) {
@@ -143,14 +143,28 @@ wg_status wg_get_kernel_times(wg_ctx *ctx, double *vertical_ahead_ms, double *wa
 }
 
 wg_status wg_set_chunk_steps(wg_ctx *ctx, int32_t steps) {
-  if (!ctx || steps < 0 || steps > ctx->max_chunk()) return WG_ERR_INVALID;
+  if (!ctx || steps < 0 || steps > ctx->chunk_cap()) return WG_ERR_INVALID;
   ctx->chunk_steps = steps;
   return WG_OK;
 }
 
+wg_status wg_set_vertical_overlap(wg_ctx *ctx, int32_t enable) {
+  if (!ctx) return WG_ERR_INVALID;
+  if (!enable) {
+    ctx->layout.va_warps = 0;
+    return WG_OK;
+  }
+  if (ctx->va_warps_default <= 0 || ctx->layout.idle_warp < 0 || ctx->threads != ctx->layout.threads)
+    return WG_ERR_UNSUPPORTED;
+  ctx->layout.va_warps = ctx->va_warps_default;
+  return WG_OK;
+}
+
+int32_t wg_get_vertical_overlap(const wg_ctx *ctx) { return ctx && ctx->overlap() ? ctx->layout.va_warps : 0; }
+
 int32_t wg_get_chunk_steps(const wg_ctx *ctx) {
   if (!ctx) return 0;
-  return (ctx->chunk_steps > 0 && ctx->chunk_steps <= ctx->max_chunk()) ? ctx->chunk_steps : ctx->max_chunk();
+  return ctx->eff_chunk();
 }
 
 wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin,
@@ -168,9 +182,6 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
   // candidates: block sizes 64..512 (for ensembles: members of one cell per block,
   // or whole cells per block when a cell has fewer members), chunk lengths 8..ring
   std::vector<int> ths = {64, 128, 256, 512};
-  std::vector<int> chs;
-  for (int c = 8; c <= ctx->max_chunk(); c *= 2) chs.push_back(c);
-  if (chs.empty() || chs.back() != ctx->max_chunk()) chs.push_back(ctx->max_chunk());
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -182,10 +193,21 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
     ctx->blocks_route = br0;
     ctx->layout = lay0;
   };
+  // first the context's own shape and layout; with vertical-balance warps, also
+  // the same layout without them
   ths.insert(ths.begin(), -1);
+  if (lay0.va_warps > 0) ths.insert(ths.begin() + 1, -2);
+  int best_va = lay0.va_warps;
   for (int th : ths) {
-    if (th < 0) restore_shape0();                          // first the context's own shape and layout
-    else if (wg_launch_shape(ctx, th, 0) != WG_OK) continue;   // does not fit the device
+    if (th < 0) {
+      restore_shape0();
+      if (th == -2) ctx->layout.va_warps = 0;
+    } else if (wg_launch_shape(ctx, th, 0) != WG_OK) {
+      continue;   // does not fit the device
+    }
+    std::vector<int> chs;   // chunk lengths 8 .. the longest this shape allows
+    for (int c = 8; c <= ctx->chunk_cap(); c *= 2) chs.push_back(c);
+    if (chs.empty() || chs.back() != ctx->chunk_cap()) chs.push_back(ctx->chunk_cap());
     for (int ch : chs) {
       if (ch > trial_steps && ch != chs.front()) continue;   // a chunk longer than the trial says nothing
       ctx->chunk_steps = ch;
@@ -204,6 +226,7 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
         best = ms;
         best_th = th;
         best_ch = ch;
+        best_va = ctx->layout.va_warps;
       }
     }
     if (st != WG_OK) break;
@@ -218,10 +241,12 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
     ctx->chunk_steps = ch0;
     return st != WG_OK ? st : WG_ERR_UNSUPPORTED;
   }
-  if (best_th < 0)
+  if (best_th < 0) {
     restore_shape0();
-  else
+    ctx->layout.va_warps = best_va;
+  } else {
     wg_launch_shape(ctx, best_th, 0);
+  }
   ctx->chunk_steps = best_ch;
   out->threads = ctx->threads;
   int32_t mb = 0;

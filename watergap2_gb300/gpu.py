@@ -29,7 +29,7 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_get_discharge", "wg_get_balance", "wg_reset_balance", "wg_synchronize", "wg_launch_shape",
            "wg_get_launch_shape", "wg_num_levels", "wg_launch_count", "wg_last_error", "wg_status_string",
            "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc",
-           "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
+           "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_set_vertical_overlap", "wg_get_vertical_overlap", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
            "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells",
            "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync")
@@ -122,6 +122,9 @@ def load_library(path: str = LIB_PATH):
     lib.wg_set_chunk_steps.argtypes = [vp, i32]
     lib.wg_get_chunk_steps.argtypes = [vp]
     lib.wg_get_chunk_steps.restype = i32
+    lib.wg_set_vertical_overlap.argtypes = [vp, i32]
+    lib.wg_get_vertical_overlap.argtypes = [vp]
+    lib.wg_get_vertical_overlap.restype = i32
     lib.wg_autotune.argtypes = [vp, i32, i32, i32, i32, i32, ctypes.POINTER(_TuneResult)]
     lib.wg_graph_capture.argtypes = [vp, i32, i32, i32, i32, i32]
     lib.wg_graph_launch.argtypes = [vp]
@@ -134,7 +137,7 @@ def load_library(path: str = LIB_PATH):
                  "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
                  "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async",
                  "wg_set_active_cells", "wg_upload_forcing_unf", "wg_monthly_outputs", "wg_get_monthly",
-                 "wg_set_step_sync"):
+                 "wg_set_step_sync", "wg_set_vertical_overlap"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -395,10 +398,16 @@ class Model:
         self._check(self.lib.wg_restore_snapshot(self.h), "restore_snapshot")
 
     def chunk_steps(self, steps: int | None = None) -> int:
-        """Set the wavefront steps per launch pair if given (0 = ring capacity); return the value in use."""
+        """Set the wavefront steps per launch if given (0 = the default); return the value in use."""
         if steps is not None:
             self._check(self.lib.wg_set_chunk_steps(self.h, int(steps)), "set_chunk_steps")
         return int(self.lib.wg_get_chunk_steps(self.h))
+
+    def vertical_overlap(self, enable: bool | None = None) -> int:
+        """Switch the vertical overlap on or off if given; return the extra warps per block (0: off)."""
+        if enable is not None:
+            self._check(self.lib.wg_set_vertical_overlap(self.h, int(bool(enable))), "set_vertical_overlap")
+        return int(self.lib.wg_get_vertical_overlap(self.h))
 
     def autotune(self, doy0: int, fday0: int, ndays: int, t_begin: int, trial_steps: int) -> dict:
         """wg_autotune: pick threads per block and chunk steps on a trial window; state unchanged."""
