@@ -334,6 +334,12 @@ wg_status wg_synchronize(wg_ctx *ctx);
  * loop of independent DFMA chains (the FP64 ceiling of the plain FP64 path). */
 wg_status wg_measure_fp64_peak(int32_t device, double *tflops);
 
+/* Diagnostic (numerics tests): the FP64 path's own math functions on n host
+ * values: fn 0 exp(x), 1 log(x), 2 pow(x, y), 3 the refined reciprocal 1/x,
+ * 4 the hardware's approximate reciprocal alone (the refinement's start).  y is
+ * read for fn 2 only. */
+wg_status wg_math_eval(int32_t device, int32_t fn, const double *x, const double *y, int64_t n, double *out);
+
 /* Information: number of drainage levels (longest flow path + 1), kernel
  * launches issued so far, and the last CUDA error string. */
 int32_t wg_num_levels(const wg_ctx *ctx);

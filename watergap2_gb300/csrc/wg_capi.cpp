@@ -999,6 +999,25 @@ wg_status wg_upload_forcing_unf(wg_ctx *ctx, int32_t day0, int32_t nd_file, int3
   return WG_OK;
 }
 
+wg_status wg_math_eval(int32_t device, int32_t fn, const double *x, const double *y, int64_t n, double *out) {
+  if (!x || !out || n < 0 || fn < 0 || fn > 4 || (fn == 2 && !y)) return WG_ERR_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return WG_ERR_DEVICE;
+  if (cudaSetDevice(device) != cudaSuccess) return WG_ERR_DEVICE;
+  double e2[64], lf[129], inv[129];
+  fill_fastmath_tables(e2, lf, inv);
+  cudaError_t e = upload_fastmath_tables(e2, lf, inv);
+  const size_t bytes = (size_t)std::max<int64_t>(n, 1) * sizeof(double);
+  double *d = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d, 3 * bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(d, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && fn == 2) e = cudaMemcpy(d + n, y, (size_t)n * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = launch_math_eval(fn, d, d + n, d + 2 * n, (size_t)n, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (d) cudaFree(d);
+  return e == cudaSuccess ? WG_OK : WG_ERR_CUDA;
+}
+
 int64_t wg_read_unf(const char *path, void *dst, int64_t bytes) {
   if (!path || !dst || bytes < 0) return -1;
   FILE *f = std::fopen(path, "rb");

@@ -12,7 +12,10 @@
 //        F = 1 + j/128, log x = m ln2 + log F + log1p(f/F), |f/F| <= 1/256,
 //        series of log1p to degree 7.
 // The tables (2^(j/64), log F, 1/F) are filled on the host from the C library by
-// fill_fastmath_tables() in wg_capi.cpp.  Accuracy: about 1 ulp for exp and log; pow(x, y) =
+// fill_fastmath_tables() in wg_capi.cpp.  Accuracy: about 1 ulp for exp and the
+// reciprocal rcp_pos; log to a few ulp of max(|log x|, 1) (just below x = 1 the
+// sum m ln2 + log F cancels, leaving an absolute error, which is what pow passes
+// on); pow(x, y) =
 // exp(y log x) has relative error ~ |y log x| * 2^-52, far inside the 1e-10
 // parity bound of the FP64 path.  Only finite positive arguments occur on the
 // hot path; x <= 0 in pow returns 0 (the hot path's pow arguments are >= 0 and
@@ -88,6 +91,22 @@ __device__ __forceinline__ double log(double x) {
   const double l1p = fma(-q, u2, u);
   const double md = (double)m;
   return fma(md, ln2_hi, g_logF_tab[j] + fma(md, ln2_lo, l1p));
+}
+
+// 1/x for finite normal nonzero x: the hardware's approximate reciprocal
+// (rcp.approx.ftz.f64, relative error checked against 2^-20 by the tests) refined
+// by one third-order Newton-Raphson step r' = r (1 + e + e^2), e = 1 - x r
+// (P. Markstein, "IA-64 and Elementary Functions", 2000, ch. 8), which cubes the
+// relative error: three FMAs on the FP64 pipe instead of a correctly rounded
+// division's longer sequence.  Result within about 1 ulp of 1/x (not always
+// correctly rounded).  The hot path calls it only with divisors bounded away from
+// zero (temperature + 237.3, latent heat, the canopy capacity, the wetted perimeter,
+// the river's outflow constant).
+__device__ __forceinline__ double rcp_pos(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  const double e = fma(-x, r, 1.0);
+  return fma(r, fma(e, e, e), r);
 }
 
 // x^y for x >= 0, y > 0 (the hot path's exponents are positive constants or

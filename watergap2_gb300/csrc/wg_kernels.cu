@@ -568,6 +568,29 @@ cudaError_t launch_fill(double *p, size_t n, double v, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------- launchers
+// The day step's FP64 math functions on arrays (numerics tests): 0 exp, 1 log,
+// 2 pow, 3 the refined reciprocal, 4 the hardware's approximate reciprocal alone.
+__global__ void k_math_eval(int fn, const double *x, const double *y, double *out, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = x[i];
+  double r = 0.;
+  switch (fn) {
+    case 0: r = fm::exp(a); break;
+    case 1: r = fm::log(a); break;
+    case 2: r = fm::pow(a, y[i]); break;
+    case 3: r = fm::rcp_pos(a); break;
+    default: asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(a)); break;
+  }
+  out[i] = r;
+}
+
+cudaError_t launch_math_eval(int fn, const double *x, const double *y, double *out, size_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_math_eval<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(fn, x, y, out, n);
+  return cudaGetLastError();
+}
+
 cudaError_t upload_fastmath_tables(const double exp2_tab[64], const double logF_tab[129], const double invF_tab[129]) {
   cudaError_t e = cudaMemcpyToSymbol(fm::g_exp2_tab, exp2_tab, 64 * sizeof(double));
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(fm::g_logF_tab, logF_tab, 129 * sizeof(double));

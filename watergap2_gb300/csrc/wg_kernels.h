@@ -39,6 +39,7 @@ struct WarpLayout {
   int threads = 0;
 };
 cudaError_t upload_fastmath_tables(const double exp2_tab[64], const double logF_tab[129], const double invF_tab[129]);
+cudaError_t launch_math_eval(int fn, const double *x, const double *y, double *out, size_t n, cudaStream_t st);
 cudaError_t launch_gather_forcing(const float *src, float *dst, const int32_t *cell_of_slot, int n, int ndays,
                                   cudaStream_t st);
 cudaError_t launch_unf_forcing(const uint32_t *raw, float *dst, const int32_t *cell_of_slot, int n, int nd_file,

@@ -36,7 +36,7 @@ template <class R> struct M;
 template <> struct M<double> {
   static __device__ __forceinline__ double exp(double x) { return fm::exp(x); }
   static __device__ __forceinline__ double pow(double x, double y) { return fm::pow(x, y); }
-  static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+  static __device__ __forceinline__ double rcp(double x) { return fm::rcp_pos(x); }   // x normal, nonzero
   static __device__ __forceinline__ double fabs_(double x) { return fabs(x); }
 };
 template <> struct M<float> {
@@ -232,7 +232,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
         prec_to_soil = dailyPrec - deficiency;
       }
       const R cwc = canopy;
-      canopyEvapo = dailyPET * m::pow(cwc / maxcs, R(0.66666666));
+      canopyEvapo = dailyPET * m::pow(cwc * m::rcp(maxcs), R(0.66666666));   // maxcs > 1e-5 mcwh
       if (cmp::gt(canopyEvapo, cwc)) {
         canopyEvapo = cwc;
         soilPET = dailyPET - cwc;
@@ -419,7 +419,7 @@ __device__ __forceinline__ R river_velocity(const DevCellsT<R> &c, int s, R rive
     depth = -bw * R(0.25) + sqrt(bw * bw * R(1.0 / 16.0) + R(0.5) * csa);
   }
   const R wp = bw + R(2.0 * 2.23606797749979) * depth;   // 2 sqrt(5)
-  const R hr = csa / wp;
+  const R hr = csa * m::rcp(wp);
   const R v = c.inv_mr[s] * m::pow(hr, R(2. / 3.)) * c.sqrt_slope[s] * R(86.4);
   return (v < R(0.00001)) ? R(0.00001) : v;
 }
@@ -635,11 +635,11 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   const R omeK = R(1.) - eK;
   R S, transported;
   if (cmp::lt0(inflow * omeK + K * S0 * eK)) {   // sign of RivEvapoRemUseMax (routing.cpp:3444-3449)
-    const R maxUse = inflow + K * S0 * eK / omeK;
+    const R maxUse = inflow + K * S0 * eK * m::rcp(omeK);   // K >= 1e-5 / length: omeK > 0
     S = R(0);
     transported = inflow + S0 - maxUse;
   } else {
-    S = S0 * eK + inflow * omeK / K;
+    S = S0 * eK + inflow * omeK * m::rcp(K);
     if (cmp::abs_le_c(S, R(WG_MIN_STOR_VOL))) S = R(0);
     transported = inflow + S0 - S;
   }

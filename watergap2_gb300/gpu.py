@@ -29,7 +29,8 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_get_discharge", "wg_get_balance", "wg_reset_balance", "wg_synchronize", "wg_launch_shape",
            "wg_get_launch_shape", "wg_num_levels", "wg_launch_count", "wg_last_error", "wg_status_string",
            "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc",
-           "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_set_vertical_overlap", "wg_get_vertical_overlap", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
+           "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_set_vertical_overlap", "wg_get_vertical_overlap",
+           "wg_math_eval", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
            "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells",
            "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync")
@@ -122,6 +123,7 @@ def load_library(path: str = LIB_PATH):
     lib.wg_set_chunk_steps.argtypes = [vp, i32]
     lib.wg_get_chunk_steps.argtypes = [vp]
     lib.wg_get_chunk_steps.restype = i32
+    lib.wg_math_eval.argtypes = [i32, i32, vp, vp, ctypes.c_int64, vp]
     lib.wg_set_vertical_overlap.argtypes = [vp, i32]
     lib.wg_get_vertical_overlap.argtypes = [vp]
     lib.wg_get_vertical_overlap.restype = i32
@@ -152,6 +154,22 @@ def read_unf(path: str, nbytes: int, out: np.ndarray | None = None) -> np.ndarra
     if got != nbytes:
         raise WgError(f"wg_read_unf {path}: read {got} of {nbytes} bytes")
     return buf
+
+
+MATH_FN = {"exp": 0, "log": 1, "pow": 2, "rcp": 3, "rcp_approx": 4}
+
+
+def math_eval(fn: str, x, y=None, device: int = 0) -> np.ndarray:
+    """wg_math_eval: the FP64 path's own exp / log / pow / reciprocal on the device."""
+    lib = load_library()
+    x = np.ascontiguousarray(x, np.float64)
+    yy = None if y is None else np.ascontiguousarray(np.broadcast_to(y, x.shape), np.float64)
+    out = np.empty_like(x)
+    rc = lib.wg_math_eval(int(device), MATH_FN[fn], x.ctypes.data, None if yy is None else yy.ctypes.data,
+                          int(x.size), out.ctypes.data)
+    if rc != WG_OK:
+        raise WgError(f"wg_math_eval: {STATUS.get(rc, rc)}")
+    return out
 
 
 def measure_fp64_peak(device: int = 0) -> float:
