@@ -1,10 +1,12 @@
 """Build recipe of the in-tree CUDA library ``_build/libwg_gpu.so`` (sm_103a only).
 
 Compiled with nvcc directly (no cmake): every translation unit in parallel,
-then one shared library.  ``--fmad=false`` keeps the arithmetic of the FP64
-path in the reference's expression order (no contraction into FMA), and the
-host code is compiled with ``-ffp-contract=off`` so that x86 and Arm hosts
-produce the same constants.
+then one shared library.  Device code lets the compiler contract a multiply
+and a dependent add into one FMA (nvcc's default): the FP64 day step is bound by
+the FP64 pipe, and an FMA is one instruction where the pair is two; the results
+stay within the FP64 path's parity bound of the reference's separately rounded
+arithmetic.  Host code is compiled with ``-ffp-contract=off`` so that x86 and
+Arm hosts produce the same constants.
 """
 from __future__ import annotations
 
@@ -28,7 +30,7 @@ def nvcc() -> str:
 
 
 def flags(extra=()):
-    return [*ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
+    return [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
             "-I", os.path.join(HERE, "..", "include"), *extra]
 
 
