@@ -72,6 +72,8 @@ template <> struct C<double> {
   static __device__ __forceinline__ bool abs_le_c(double a, double c) {
     return (__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFll) <= __double_as_longlong(c);
   }
+  static __device__ __forceinline__ bool is_zero(double a) { return (__double_as_longlong(a) << 1) == 0; }
+  static __device__ __forceinline__ bool is_one(double a) { return __double_as_longlong(a) == 0x3FF0000000000000ll; }
 };
 template <> struct C<float> {
   static __device__ __forceinline__ bool gt(float a, float b) { return a > b; }
@@ -83,6 +85,8 @@ template <> struct C<float> {
   static __device__ __forceinline__ bool lt_c(float a, float c) { return a < c; }
   static __device__ __forceinline__ bool gt_c(float a, float c) { return a > c; }
   static __device__ __forceinline__ bool abs_le_c(float a, float c) { return fabsf(a) <= c; }
+  static __device__ __forceinline__ bool is_zero(float a) { return a == 0.f; }
+  static __device__ __forceinline__ bool is_one(float a) { return a == 1.f; }
 };
 
 template <class R>
@@ -210,15 +214,17 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   R immediate = R(0), dailyAET = R(0), runoff = R(0), total = R(0), gwr = R(0), pot = R(0);
   R overflow = R(0), neg_land_aet = R(0), cellAET = R(0), gwr_route = R(0), leak = R(0);
   const bool land = cmp::gt0(landAreaFrac);
-  // prevLAF / landAreaFrac; exactly 1 while the land fraction does not change
+  // prevLAF / landAreaFrac; exactly 1 while the land fraction does not change, and
+  // then the storages are not rescaled (x * 1 = x)
   const R ratio = !land ? R(0) : (prevLAF == landAreaFrac ? R(1) : prevLAF / landAreaFrac);
+  const bool rescale = !cmp::is_one(ratio);
 
   // interception (daily.cpp:825-895)
   if (!land) {
     transfer = canopy;
     canopy = R(0);
   } else {
-    canopy *= ratio;
+    if (rescale) canopy *= ratio;
     if (cmp::abs_le_c(canopy, R(WG_MIN_STOR_VOL))) canopy = R(0);
     initialStorage = canopy;
     if (cmp::gt_c(dailyLai, R(0.00001))) {
@@ -256,13 +262,21 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   for (int e = 0; e < B; ++e) {
     R sb = band[e * bstride];
     R temp_elev = T - c.band_dt[(size_t)e * c.n + s];
+    if (land && cmp::is_zero(sb) && cmp::gt(temp_elev, t_snowfz)) {
+      // no snow and no snowfall in this band: the steps below would keep it at
+      // zero, melt nothing and pass the precipitation on -- the same bits, without
+      // the band's arithmetic and store
+      if (e == 0) tempElevMax = temp_elev;
+      effPrec += prec_to_soil;
+      continue;
+    }
     if (!land) {
       transfer += sb * invB;
       sb = R(0);
       gs = R(0);
     } else {
       R effBefore, melt = R(0);
-      sb *= ratio;
+      if (rescale) sb *= ratio;
       if (cmp::abs_le_c(sb, R(WG_MIN_STOR_VOL))) sb = R(0);
       initialStorage = sb;
       if (cmp::gt_c(sb, R(1000.))) {
@@ -320,7 +334,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
     soil = R(0);
   } else {
     const R Smax = c.smax[s];
-    soil *= ratio;
+    if (rescale) soil *= ratio;
     initialStorage = soil;
     if (cmp::gt(soil, Smax)) {
       overflow = soil - Smax;
