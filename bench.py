@@ -38,9 +38,13 @@ DAYS_PER_STEP = 365
 # algorithmic HBM bytes per cell-day of a day-by-day FP64 implementation with the
 # water bodies of this workload: vertical 224 + routing 96 + water bodies ~4
 BYTES_PER_CELL_DAY = 324.0
-# of which the wavefront kernel k_pipeline moves: routing 96 + water bodies 4 +
-# the vertical balance of the cells with water bodies (7.2 % of the cells x 224)
+# of which the routing part of the wavefront kernel k_pipeline moves: routing 96 +
+# water bodies 4 + the vertical balance of the cells with water bodies (7.2 % of
+# the cells x 224)
 WAVEFRONT_BYTES_PER_CELL_DAY = 116.2
+# the vertical balance of one cell-day without water bodies (run ahead of routing:
+# by k_vertical_ahead, or by the extra warps of the wavefront launches)
+VERTICAL_BYTES_PER_CELL_DAY = 224.0
 
 
 def profile_figures(path=os.path.join(ROOT, "profiles", "fp64_global_wavefront_kernels.md")):
@@ -312,6 +316,7 @@ def run_gpu(args, rank, world):
     kernel_ms = model.kernel_times()
     model.kernel_timing(False)
     vinline_frac = model.vinline_fraction()
+    chunk_steps, overlap_warps = model.chunk_steps(), model.vertical_overlap()
     elapsed_ms = ev0.elapsed_time(ev1)
     launch_ms = [a.elapsed_time(b) for a, b in per_step]
     model.run_steps(1, 0, ndays, nyears * DAYS_PER_STEP, total_steps)   # drain (untimed)
@@ -416,27 +421,39 @@ def run_gpu(args, rank, world):
             dist.destroy_process_group()
         return
     peaks, peak_kind = measured_peaks()
-    # dominant kernel: the wavefront kernel k_pipeline (one launch per timed step),
-    # its device time from the CUDA events the library records around it
-    pipe_ms = kernel_ms["wavefront_ms"] / kernel_ms["launch_pairs"]
-    va_ms = kernel_ms["vertical_ahead_ms"] / kernel_ms["launch_pairs"]
-    launch_cell_days = region.ncell * DAYS_PER_STEP
-    achieved = WAVEFRONT_BYTES_PER_CELL_DAY * launch_cell_days / (pipe_ms / 1000.0) / 1e9
+    # dominant kernel: the wavefront kernel k_pipeline, its device time from the CUDA
+    # events the library records around each launch.  Each timed step (one call of
+    # 365 wavefront steps) is one k_vertical_ahead launch for the first chunk and
+    # ceil(365 / chunk) wavefront launches, all but the last carrying the vertical
+    # balance of the next chunk's cells without water bodies (with the overlap on;
+    # without it, one k_vertical_ahead launch before every wavefront launch).
+    n_wave = kernel_ms["launch_pairs"]
+    pipe_ms_total, va_ms_total = kernel_ms["wavefront_ms"], kernel_ms["vertical_ahead_ms"]
+    pipe_ms = pipe_ms_total / n_wave
+    nplain = region.ncell * (1.0 - vinline_frac)
+    route_cd = region.ncell * DAYS_PER_STEP * args.steps                 # routing cell-days
+    va_days = chunk_steps if overlap_warps else DAYS_PER_STEP
+    va_alone_cd = nplain * va_days * args.steps                         # k_vertical_ahead
+    va_wave_cd = nplain * (DAYS_PER_STEP - va_days) * args.steps        # extra warps of k_pipeline
+    wave_bytes = WAVEFRONT_BYTES_PER_CELL_DAY * route_cd + VERTICAL_BYTES_PER_CELL_DAY * va_wave_cd
+    achieved = wave_bytes / (pipe_ms_total / 1000.0) / 1e9
     figs = profile_figures()
     traffic = None
-    if "traffic_bytes_per_cell_day k_pipeline" in figs:
-        traffic = figs["traffic_bytes_per_cell_day k_pipeline"] * launch_cell_days
+    if overlap_warps and chunk_steps == figs.get("chunk_steps"):
+        traffic = figs.get("traffic_bytes_per_launch k_pipeline")       # a launch of the same shape
     fp64 = None
     try:
         peak64 = fp64_peak_tflops()
         fp64 = {"peak": peak64, "unit": "TFLOP/s", "peak_kind": "measured (DFMA loop)"}
-        for kname, ms, cd in (("k_pipeline", pipe_ms, launch_cell_days),
-                              ("k_vertical_ahead", va_ms, launch_cell_days * (1.0 - vinline_frac))):
-            fl = figs.get(f"fp64_flops_per_cell_day {kname}")
-            if fl is not None:
-                ach = fl * cd / (ms / 1000.0) / 1e12
-                fp64[kname] = {"achieved": ach, "frac": ach / peak64, "flops_per_cell_day": fl,
-                               "launch_ms": ms, "pipe_busy_ncu": figs.get(f"fp64_pipe_busy {kname}")}
+        fl_route = figs.get("fp64_flops_per_cell_day routing")
+        fl_va = figs.get("fp64_flops_per_cell_day k_vertical_ahead")
+        if fl_route is not None and fl_va is not None:
+            for kname, ms, flops in (("k_pipeline", pipe_ms_total, fl_route * route_cd + fl_va * va_wave_cd),
+                                     ("k_vertical_ahead", va_ms_total, fl_va * va_alone_cd)):
+                ach = flops / (ms / 1000.0) / 1e12
+                fp64[kname] = {"achieved": ach, "frac": ach / peak64, "ms_per_timed_step": ms / args.steps,
+                               "pipe_busy_ncu": figs.get(f"fp64_pipe_busy {kname}")}
+            fp64["flops_per_cell_day"] = {"routing": fl_route, "vertical": fl_va}
     except Exception as exc:   # diagnostics only
         fp64 = {"error": str(exc)}
     cpu_threads = os.cpu_count() or 1
@@ -459,10 +476,14 @@ def run_gpu(args, rank, world):
                 "upload": "next year's forcing on the copy stream, overlapped with this year's run"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                      "frac": achieved / peaks.get("hbm_gbs"), "traffic": traffic,
-                     "peak_kind": peak_kind, "kernel": "k_pipeline (wavefront, 365 steps per launch)",
-                     "algorithmic_bytes_per_cell_day": WAVEFRONT_BYTES_PER_CELL_DAY, "launch_ms": pipe_ms,
+                     "peak_kind": peak_kind,
+                     "kernel": f"k_pipeline (wavefront, {chunk_steps} steps per launch, "
+                               f"{overlap_warps} vertical-balance warps per block)",
+                     "algorithmic_bytes_per_cell_day": {"routing": WAVEFRONT_BYTES_PER_CELL_DAY,
+                                                        "vertical": VERTICAL_BYTES_PER_CELL_DAY},
+                     "launch_ms": pipe_ms, "launches_per_timed_step": n_wave / args.steps,
                      "limiter": "FP64 pipe (see fp64), not HBM",
-                     "vertical_ahead_launch_ms": va_ms},
+                     "vertical_ahead_ms_per_timed_step": va_ms_total / args.steps},
         "fp64": fp64,
         "per_day_api": per_day,
         "ensemble": ensemble,
@@ -479,9 +500,12 @@ def run_gpu(args, rank, world):
 def run_profile_case(days: int = 120, warm_days: int = 200):
     """A short, self-contained case for ncu: the global grid, a warm-up call that
     fills the day-pipelined wavefront (warm_days steps), then one call of `days`
-    steady-state steps (one k_vertical_ahead and one k_pipeline launch; forcing and
-    state exceed L2).  Capture the second call's kernels:
-      ncu -k regex:k_pipeline -s 1 -c 1 python bench.py --profile"""
+    steady-state steps (forcing and state exceed L2).  With the default 16-step
+    chunks and the vertical overlap, the warm-up call is launches 0-13 of
+    k_vertical_ahead|k_pipeline (one vertical-ahead launch, 13 wavefront
+    launches) and the second call starts with its vertical-ahead launch (14) and
+    wavefront launches that carry the next chunk's vertical balance (15, 16, ...):
+      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 14 -c 3 python bench.py --profile"""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global()
@@ -498,7 +522,8 @@ def run_profile_case(days: int = 120, warm_days: int = 200):
     m.run_steps(1, 0, nd, warm_days + days, m.num_steps(nd))
     m.synchronize()
     print(json.dumps({"profile_case": "global grid, steady-state wavefront", "ncell": region.ncell, "steps": days,
-                      "seconds": dt, "cell_days_per_s": region.ncell * days / dt}))
+                      "seconds": dt, "cell_days_per_s": region.ncell * days / dt, "chunk_steps": m.chunk_steps(),
+                      "vertical_overlap_warps": m.vertical_overlap(), "vinline_fraction": m.vinline_fraction()}))
 
 
 def run_fine():
