@@ -67,11 +67,24 @@ def lib():
                                  ctypes.c_void_p, ctypes.c_int]
         _lib.wgo_bottom_width.argtypes = [ctypes.c_double]
         _lib.wgo_bottom_width.restype = ctypes.c_double
+        _lib.wgo_wtemp_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     return _lib
 
 
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+WT_NIN = 73   # doubles per water-temperature record (wgo_wt_in)
+
+
+def wtemp(records: np.ndarray) -> np.ndarray:
+    """wgo_wtemp on each row of records [n, 73]; returns [n, 12] (temperatures, ice)."""
+    rec = np.ascontiguousarray(records, np.float64)
+    assert rec.ndim == 2 and rec.shape[1] == WT_NIN
+    out = np.empty((rec.shape[0], 12))
+    lib().wgo_wtemp_batch(_ptr(rec), int(rec.shape[0]), _ptr(out))
+    return out
 
 
 class Oracle:

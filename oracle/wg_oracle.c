@@ -522,8 +522,131 @@ static double state_volume(const wgo_static *s, const wgo_state *st, int n) {
   return storage_km3(s, st, n, st->laf_started[n] ? st->laf_prev[n] : st->laf[n]);
 }
 
+/* one day's inputs of the water temperature that routing produces for a cell
+ * (routing.cpp:4287-4356): the water bodies' storages before the day, their
+ * evaporation [mm] after any reduction, the area reduction factors the day
+ * started with, and the outflows of each water body */
+typedef struct {
+  double loclake_prev, loclake_max, loclake_evapo, loclake_rf, loclake_out;
+  double locwetl_prev, locwetl_evapo, locwetl_rf, locwetl_out;
+  double glolake_prev, glolake_max, glolake_evapo, glolake_out;
+  double res_prev, res_evapo, res_out;
+  double glowetl_prev, glowetl_evapo, glowetl_rf, glowetl_out;
+} wt_route;
+
+static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
+                    const float *temp, const float *swrad, double *discharge, double *balance, int nthreads,
+                    wgo_wt_io *wt);
+
 int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
             const float *temp, const float *swrad, double *discharge, double *balance, int nthreads) {
+  return run_impl(s, st, doy0, ndays, prec, temp, swrad, discharge, balance, nthreads, NULL);
+}
+
+int wgo_run_wt(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
+               const float *temp, const float *swrad, double *discharge, double *balance, int nthreads,
+               wgo_wt_io *wt) {
+  if (!wt || !wt->longwave || !wt->gw_temp || !wt->inflow_cells || !wt->river_length_check || !wt->temp ||
+      !wt->ice || !wt->river_avail)
+    return -1;
+  return run_impl(s, st, doy0, ndays, prec, temp, swrad, discharge, balance, nthreads, wt);
+}
+
+void wgo_wt_init(int ncell, wgo_wt_io *wt) {
+  for (int k = 0; k < 6 * ncell; k++) {
+    wt->temp[k] = 15.;
+    wt->ice[k] = 0.;
+  }
+  for (int n = 0; n < ncell; n++) wt->river_avail[n] = 0.;
+}
+
+/* the water temperature of cell n after its routing (routing.cpp:4241-4513) */
+static void cell_water_temp(const wgo_static *s, const wgo_state *st, int n, int d, double cellArea, double cfa,
+                            const vout *vo, double localRunoff, double gw_runoff, const wt_route *r,
+                            double transportedVolume, double bw, float Tair, float SWin, wgo_wt_io *wt) {
+  const int N = s->ncell;
+  wgo_wt_in t;
+  t.calc_temp_pp = 0.; t.pp_withdrawal = 0.; t.pp_consumption = 0.;
+  for (int i = 0; i < 9; i++) {
+    const int m = wt->inflow_cells[(size_t)n * 9 + i];
+    if (m >= 0) {
+      t.inflow[i] = wt->river_avail[m];
+      t.inflow_temp[i] = wt->temp[m];
+    } else if (i == 4) {
+      t.inflow[i] = 0.;
+      t.inflow_temp[i] = wt->temp[n];
+    } else {
+      t.inflow[i] = 0.;
+      t.inflow_temp[i] = 15.;
+    }
+  }
+  for (int k = 0; k < 6; k++) t.ice[k] = wt->ice[(size_t)k * N + n];
+  t.short_rad = (double)SWin;
+  t.long_rad = (double)wt->longwave[(size_t)d * N + n];
+  t.air_temp = (double)Tair;
+  t.gw_temp = wt->gw_temp[n] < 0.f ? 0. : (double)wt->gw_temp[n];
+  t.cfa = cfa;
+  t.ow_pet = vo->owpet;
+  t.ow_prec = vo->owp;
+  t.cell_area = cellArea;
+  t.loclake_area = s->loc_lake[n];
+  t.loclake_stor_prev = r->loclake_prev + r->loclake_max;
+  t.loclake_temp_prev = wt->temp[(size_t)1 * N + n];
+  t.loclake_evapo = r->loclake_evapo;
+  t.loclake_rf = r->loclake_rf;
+  t.local_runoff = localRunoff;
+  t.local_gw_runoff = gw_runoff;
+  t.locwetl_area = s->loc_wetl[n];
+  t.locwetl_stor_prev = r->locwetl_prev;
+  t.locwetl_temp_prev = wt->temp[(size_t)2 * N + n];
+  t.locwetl_evapo = r->locwetl_evapo;
+  t.locwetl_rf = r->locwetl_rf;
+  t.locwetl_inflow = r->loclake_out;
+  t.locwetl_outflow = r->locwetl_out;
+  t.glolake_area = s->lake_area[n];
+  t.glolake_stor_prev = r->glolake_prev + r->glolake_max;
+  t.glolake_temp_prev = wt->temp[(size_t)3 * N + n];
+  t.glolake_evapo = r->glolake_evapo;
+  t.glolake_inflow = 0.;
+  for (int i = 0; i < 9; i++) t.glolake_inflow += t.inflow[i];
+  if (s->loc_wetl[n] > 0.) t.glolake_inflow += r->locwetl_out;
+  else if (s->loc_lake[n] > 0.) t.glolake_inflow += r->loclake_out;
+  t.res_inflow = s->lake_area[n] > 0. ? r->glolake_out : t.glolake_inflow;
+  t.res_area = s->res_area[n];
+  t.res_stor_prev = r->res_prev;
+  t.res_temp_prev = wt->temp[(size_t)4 * N + n];
+  t.res_evapo = r->res_evapo;
+  if (s->res_area[n] > 0.) t.glowetl_inflow = r->res_out;
+  else if (s->lake_area[n] > 0.) t.glowetl_inflow = r->glolake_out;
+  else t.glowetl_inflow = t.glolake_inflow;
+  t.glowetl_area = s->glo_wetl[n];
+  t.glowetl_stor_prev = r->glowetl_prev;
+  t.glowetl_temp_prev = wt->temp[(size_t)5 * N + n];
+  t.glowetl_evapo = r->glowetl_evapo;
+  t.glowetl_rf = r->glowetl_rf;
+  if (s->glo_wetl[n] > 0.) t.river_inflow = r->glowetl_out;
+  else if (s->res_area[n] > 0.) t.river_inflow = r->res_out;
+  else if (s->lake_area[n] > 0.) t.river_inflow = r->glolake_out;
+  else t.river_inflow = t.glolake_inflow;
+  t.river_stor = st->river[n];
+  t.gw_runoff_into_river = 0.;   /* fractional routing is off: nothing bypasses the water bodies */
+  t.runoff_into_river = 0.;
+  t.river_bottom_width = bw;
+  t.river_length = s->river_length[n];
+  t.river_length_check = wt->river_length_check[n];
+  t.has_outflow = s->downstream[n] >= 0 ? 1. : 0.;
+  double out[12];
+  wgo_wtemp(&t, out);
+  for (int k = 0; k < 6; k++) wt->ice[(size_t)k * N + n] = out[6 + k];
+  if (wt->daily_temp) wt->daily_temp[(size_t)d * N + n] = out[0];
+  for (int k = 0; k < 6; k++)
+    wt->temp[(size_t)k * N + n] = out[k] == -9999. ? (t.air_temp < 0. ? 0. : t.air_temp) : out[k];
+  wt->river_avail[n] = transportedVolume;
+}
+
+static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
+                    const float *temp, const float *swrad, double *discharge, double *balance, int nthreads,
+                    wgo_wt_io *wt) {
   const int N = s->ncell;
   if (s->nband <= 0 || N <= 0) return -1;
   vout *vo = (vout *)malloc(sizeof(vout) * (size_t)N);
@@ -592,6 +715,8 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
       const double wetlDepth = PAR(s, WGO_P_WET_D, n) * 0.001;
       const double owp = vo[n].owp, owpet = vo[n].owpet;
       double inflow = localRunoff, outflow = 0., maxStorage, totalInflow, PETgwr, PETgwrMax;
+      wt_route wr;
+      memset(&wr, 0, sizeof wr);
 
       /* local lake, routing.cpp:2318-2490 */
       if (s->loc_lake[n] > 0.) {
@@ -606,9 +731,11 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
         PETgwrMax = S0 + maxStorage + totalInflow;
         const double avail = PETgwrMax;
         if (PETgwrMax < 0.) PETgwrMax = 0.;
+        wr.loclake_prev = S0; wr.loclake_max = maxStorage; wr.loclake_rf = rf;
         if (PETgwr > PETgwrMax) {
           st->loclake[n] = (-1.) * maxStorage;
           e_ow += avail;
+          evapo *= PETgwrMax / PETgwr;
         } else {
           st->loclake[n] = S0 + totalInflow - PETgwr;
           e_ow += PETgwr;
@@ -626,6 +753,7 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
           st->loclake[n] = maxStorage;
         }
         inflow = outflow;
+        wr.loclake_evapo = evapo; wr.loclake_out = outflow;
         st->rf_loclake[n] = 1. - pow(fabs(st->loclake[n] - maxStorage) / (2. * maxStorage), (evaredex * EVAPO_RED_EXP));
         if (st->rf_loclake[n] < 0.) st->rf_loclake[n] = 0.;
         if (st->rf_loclake[n] > 1.) st->rf_loclake[n] = 1.;
@@ -641,9 +769,11 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
         totalInflow = inflow + pin;
         PETgwr = evapo * (cellArea / 1000000.) * (s->loc_wetl[n] / 100.);
         PETgwrMax = S0 + totalInflow;
+        wr.locwetl_prev = S0; wr.locwetl_rf = rf;
         if (PETgwr > PETgwrMax) {
           st->locwetl[n] = 0.;
           e_ow += PETgwrMax;
+          evapo *= PETgwrMax / PETgwr;
         } else {
           st->locwetl[n] = S0 + totalInflow - PETgwr;
           e_ow += PETgwr;
@@ -660,6 +790,7 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
           st->locwetl[n] = maxStorage;
         }
         inflow = outflow;
+        wr.locwetl_evapo = evapo; wr.locwetl_out = outflow;
         st->rf_locwetl[n] = 1. - pow(fabs(st->locwetl[n] - maxStorage) / (maxStorage), (evaredex * EVAPO_RED_EXP));
         if (st->rf_locwetl[n] < 0.) st->rf_locwetl[n] = 0.;
         if (st->rf_locwetl[n] > 1.) st->rf_locwetl[n] = 1.;
@@ -680,10 +811,12 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
         double PETgwrRemUse = evapo * (s->lake_area[n] / 1000000.);
         double PETgwrRemUseMax = totalInflow + maxStorage + S0;
         p_ow += pin;
+        wr.glolake_prev = S0; wr.glolake_max = maxStorage;
         if (PETgwrRemUse > PETgwrRemUseMax) {
           st->glolake[n] = (-1.) * maxStorage;
           outflow = 0.;
           e_ow += PETgwrRemUseMax;
+          evapo *= PETgwrRemUseMax / PETgwrRemUse;
         } else {
           st->glolake[n] = S0 * exp(-1. * swoutf) + (1. / swoutf) * (totalInflow - PETgwrRemUse) * (1. - exp(-1. * swoutf));
           outflow = totalInflow + S0 - st->glolake[n] - PETgwrRemUse;
@@ -699,6 +832,7 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
         }
         if (fabs(st->glolake[n]) <= MIN_STOR_VOL) st->glolake[n] = 0.;
         inflow = outflow;
+        wr.glolake_evapo = evapo; wr.glolake_out = outflow;
         st->rf_glolake[n] = 1. - pow(fabs(st->glolake[n] - maxStorage) / (2. * maxStorage), (evaredex * EVAPO_RED_EXP));
         if (st->rf_glolake[n] < 0.) st->rf_glolake[n] = 0.;
         if (st->rf_glolake[n] > 1.) st->rf_glolake[n] = 1.;
@@ -716,9 +850,11 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
         PETgwr = evapo * (s->res_area[n] / 1000000.);
         PETgwrMax = S0 + totalInflow;
         p_ow += pin;
+        wr.res_prev = S0;
         if (PETgwr > PETgwrMax) {
           st->res[n] = S0 + totalInflow - PETgwrMax;
           e_ow += PETgwrMax;
+          evapo *= PETgwrMax / PETgwr;
         } else {
           st->res[n] = S0 + totalInflow - PETgwr;
           e_ow += PETgwr;
@@ -759,6 +895,7 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
           st->res[n] = 0.;
         }
         inflow = outflow;
+        wr.res_evapo = evapo; wr.res_out = outflow;
         st->rf_res[n] = 1. - pow(fabs(st->res[n] - maxStorage) / maxStorage, EVAPO_RED_EXP_RES);
         if (st->rf_res[n] < 0.) st->rf_res[n] = 0.;
         if (st->rf_res[n] > 1.) st->rf_res[n] = 1.;
@@ -775,10 +912,12 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
         PETgwr = evapo * (cellArea / 1000000.) * ((s->glo_wetl[n]) / 100.);
         PETgwrMax = totalInflow + S0;
         p_ow += pin;
+        wr.glowetl_prev = S0; wr.glowetl_rf = rf;
         if (PETgwr > PETgwrMax) {
           st->glowetl[n] = 0.;
           outflow = 0.;
           e_ow += PETgwrMax;
+          evapo *= PETgwrMax / PETgwr;
         } else {
           st->glowetl[n] = S0 * exp(-1. * swoutf) + (1. / swoutf) * (totalInflow - PETgwr) * (1. - exp(-1. * swoutf));
           outflow = totalInflow + S0 - st->glowetl[n] - PETgwr;
@@ -790,6 +929,7 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
         }
         if (fabs(st->glowetl[n]) <= MIN_STOR_VOL) st->glowetl[n] = 0.;
         inflow = outflow;
+        wr.glowetl_evapo = evapo; wr.glowetl_out = outflow;
         st->rf_glowetl[n] = 1. - pow(fabs(st->glowetl[n] - maxStorage) / maxStorage, (evaredex * EVAPO_RED_EXP));
         if (st->rf_glowetl[n] < 0.) st->rf_glowetl[n] = 0.;
         if (st->rf_glowetl[n] > 1.) st->rf_glowetl[n] = 1.;
@@ -820,6 +960,9 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float
       const int down = s->downstream[n];
       if (down >= 0) inflow_up[down] += transportedVolume;
       if (discharge) discharge[(size_t)d * N + n] = transportedVolume;
+      if (wt)
+        cell_water_temp(s, st, n, d, cellArea, cfa, &vo[n], localRunoff, gw_runoff, &wr, transportedVolume, bw[n],
+                        T[n], SW[n], wt);
 
       if (balance) {
         const double fl = cellArea * (laf / 100.) / 1000000.;

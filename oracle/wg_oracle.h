@@ -13,7 +13,9 @@
  * for the option set of the hot path (time_series=1, cloud=2, petOpt=0,
  * intercept=1, use_kc=0, calc_albedo=0, clclOpt=0, subtract_use=0,
  * fractionalRoutingOpt=0, aridareaOpt=0, riverEvapoOpt=0, statcorrOpt=0,
- * use_alloc=0, glacierOpt=0, calc_wtemp=0, riverveloOpt 0/1/2).
+ * use_alloc=0, glacierOpt=0, calc_wtemp 0/1, riverveloOpt 0/1/2), and
+ *   calcWaterTempClass::calcWTemp         (source/calcWaterTemp.cpp:48-1324)
+ * with its call in routing (source/routing.cpp:4241-4513).
  *
  * Parity pin: in the build container this restatement is compared with the
  * reference's own daily.cpp/routing.cpp object code, linked into a harness
@@ -110,6 +112,59 @@ int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays,
 
 /* Derived river bottom width [m] (routing.cpp:490-495), exposed for tests. */
 double wgo_bottom_width(double bankfull);
+
+/* ---- water temperature (options.calc_wtemp = 1) ----------------------------
+ * Input record of one cell and day, the fields of the reference's
+ * calcWaterTempClass::transfer (source/calcWaterTemp.h:23-95) in that order,
+ * all as double (the two flags 0/1).  Indices of the swb arrays: [0] river,
+ * [1] local lake, [2] local wetland, [3] global lake, [4] reservoir,
+ * [5] global wetland. */
+typedef struct {
+  double calc_temp_pp, pp_withdrawal, pp_consumption;
+  double short_rad, long_rad, air_temp, cfa, ow_pet, ow_prec, cell_area, gw_temp;
+  double inflow[9], inflow_temp[9];     /* by inflow direction, [4] = the cell itself */
+  double ice[6];
+  double river_stor, gw_runoff_into_river, runoff_into_river, river_bottom_width, river_length,
+         river_length_check, river_inflow, has_outflow;
+  double loclake_area, loclake_stor_prev, loclake_temp_prev, loclake_evapo, loclake_rf, local_runoff,
+         local_gw_runoff;
+  double locwetl_area, locwetl_stor_prev, locwetl_temp_prev, locwetl_evapo, locwetl_rf, locwetl_inflow,
+         locwetl_outflow;
+  double glolake_area, glolake_stor_prev, glolake_temp_prev, glolake_evapo, glolake_inflow;
+  double res_inflow, res_area, res_stor_prev, res_temp_prev, res_evapo;
+  double glowetl_inflow, glowetl_area, glowetl_stor_prev, glowetl_temp_prev, glowetl_evapo, glowetl_rf;
+} wgo_wt_in;
+
+#define WGO_WT_NIN 73   /* doubles in wgo_wt_in */
+
+/* calcWaterTempClass::calcWTemp (source/calcWaterTemp.cpp:48-240): out[0..5]
+ * temperatures [degC] of river/outflow, local lake, local wetland, global lake,
+ * reservoir, global wetland (-9999 where none), out[6..11] their ice
+ * thickness [km]. */
+void wgo_wtemp(const wgo_wt_in *t, double out[12]);
+/* wgo_wtemp over n records of WGO_WT_NIN doubles each; out [n*12] */
+void wgo_wtemp_batch(const double *records, int n, double *out);
+
+/* Water temperature inputs and state of wgo_run_wt (caller-owned). */
+typedef struct {
+  const float *longwave;        /* [ndays*ncell] downward longwave [W/m2]              */
+  const float *gw_temp;         /* [ncell] climate.G_GW_Temperature_y [degC]           */
+  const int32_t *inflow_cells;  /* [ncell*9] G_inflow_cells, 0-based, -1 = none        */
+  const double *river_length_check;  /* [ncell] G_riverLengthCheck (as read, 55 = none) */
+  double *temp;                 /* [6*ncell] swb-major: previous day's temperatures    */
+  double *ice;                  /* [6*ncell] swb-major: ice thickness [km]             */
+  double *river_avail;          /* [ncell] G_RiverAvailPreStep                         */
+  double *daily_temp;           /* optional [ndays*ncell]: out[0] of each cell and day */
+} wgo_wt_io;
+
+/* The reference's start values (routing.cpp:172-198): 15 degC, no ice, no flow. */
+void wgo_wt_init(int ncell, wgo_wt_io *wt);
+
+/* wgo_run with the water temperature of every cell after its routing
+ * (routing.cpp:4241-4513). */
+int wgo_run_wt(const wgo_static *s, wgo_state *st, int doy0, int ndays,
+               const float *prec, const float *temp, const float *swrad,
+               double *discharge, double *balance, int nthreads, wgo_wt_io *wt);
 
 #ifdef __cplusplus
 }
