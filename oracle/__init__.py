@@ -50,6 +50,11 @@ class _State(ctypes.Structure):
     _fields_ = [(f, ctypes.c_void_p) for f in _STATE_ORDER]
 
 
+class _WtIO(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_void_p) for f in ("longwave", "gw_temp", "inflow_cells", "river_length_check",
+                                               "temp", "ice", "river_avail", "daily_temp")]
+
+
 def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -68,6 +73,10 @@ def lib():
         _lib.wgo_bottom_width.argtypes = [ctypes.c_double]
         _lib.wgo_bottom_width.restype = ctypes.c_double
         _lib.wgo_wtemp_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        _lib.wgo_wt_init.argtypes = [ctypes.c_int, ctypes.POINTER(_WtIO)]
+        _lib.wgo_run_wt.argtypes = [ctypes.POINTER(_Static), ctypes.POINTER(_State), ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_WtIO)]
     return _lib
 
 
@@ -109,6 +118,47 @@ class Oracle:
         rc = lib().wgo_init_state(ctypes.byref(self._static), ctypes.byref(self._cstate))
         if rc:
             raise RuntimeError(f"wgo_init_state failed: {rc}")
+
+    def init_water_temp(self, gw_temp, river_length_check=None):
+        """Switch on the water temperature: the reference's start values (15 degC,
+        no ice); gw_temp [ncell] the yearly groundwater temperature; the river
+        length check defaults to the region's river length as read."""
+        from watergap2_gb300.region import inflow_cells
+        n = self.region.ncell
+        self.wt = {"temp": np.zeros((6, n)), "ice": np.zeros((6, n)), "river_avail": np.zeros(n)}
+        self._wt_static = {
+            "gw_temp": np.ascontiguousarray(gw_temp, np.float32),
+            "inflow_cells": np.ascontiguousarray(inflow_cells(self.region), np.int32),
+            "river_length_check": np.ascontiguousarray(
+                self.region.extras["river_length_file"] if river_length_check is None else river_length_check,
+                np.float64),
+        }
+        io = self._wt_io(None, None)
+        lib().wgo_wt_init(n, ctypes.byref(io))
+
+    def _wt_io(self, lw, daily):
+        io = _WtIO()
+        io.longwave = _ptr(lw) if lw is not None else None
+        for k, v in self._wt_static.items():
+            setattr(io, k, _ptr(v))
+        for k, v in self.wt.items():
+            setattr(io, k, _ptr(v))
+        io.daily_temp = _ptr(daily) if daily is not None else None
+        return io
+
+    def run_wt(self, doy0, P, T, S, LW, discharge=False, daily_temp=False, nthreads=1):
+        """run() with the water temperature; returns (discharge, daily out[0] of every cell)."""
+        P, T, S, LW = (np.ascontiguousarray(x, np.float32) for x in (P, T, S, LW))
+        nd = P.shape[0]
+        q = np.zeros((nd, self.region.ncell)) if discharge else None
+        dt = np.zeros((nd, self.region.ncell)) if daily_temp else None
+        io = self._wt_io(LW, dt)
+        rc = lib().wgo_run_wt(ctypes.byref(self._static), ctypes.byref(self._cstate), int(doy0), nd,
+                              _ptr(P), _ptr(T), _ptr(S), _ptr(q) if q is not None else None, None,
+                              int(nthreads), ctypes.byref(io))
+        if rc:
+            raise RuntimeError(f"wgo_run_wt failed: {rc}")
+        return q, dt
 
     def run(self, doy0, P, T, S, discharge=False, balance=False, nthreads=1):
         P, T, S = (np.ascontiguousarray(x, np.float32) for x in (P, T, S))

@@ -50,7 +50,11 @@ def _full(values, dtype, fill=0):
     return out
 
 
-def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000):
+WT_FIELDS = ["wt_river", "wt_loclake", "wt_locwetl", "wt_glolake", "wt_res", "wt_glowetl",
+             "ice_river", "ice_loclake", "ice_locwetl", "ice_glolake", "ice_res", "ice_glowetl", "river_avail"]
+
+
+def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000, wtemp=None):
     n = region.ncell
     if n > NG:
         raise ValueError("region larger than the reference grid")
@@ -137,13 +141,22 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
     np.ascontiguousarray(P, np.float32).tofile(f"{d}/f_prec.bin")
     np.ascontiguousarray(T, np.float32).tofile(f"{d}/f_temp.bin")
     np.ascontiguousarray(S, np.float32).tofile(f"{d}/f_swrad.bin")
+    if wtemp is not None:   # (longwave [ndays, ncell], groundwater temperature [ncell])
+        from watergap2_gb300.region import inflow_cells
+        lw, gwt = wtemp
+        np.ascontiguousarray(lw, np.float32).tofile(f"{d}/f_lwrad.bin")
+        np.ascontiguousarray(gwt, np.float32).tofile(f"{d}/c_gwtemp.bin")
+        ic = np.zeros((NG, 9), np.int32)
+        ic[:n] = inflow_cells(region) + 1           # 1-based, 0 = none
+        _unf(f"{d}/G_INFLC.9.UNF4", ic.ravel(), np.int32)
     with open(f"{d}/meta.txt", "w") as f:
-        f.write(f"{n} {P.shape[0]} {doy0} {year0} {resopt} {region.river_velo_opt} {len(stations)} {len(snapshots)}\n")
+        f.write(f"{n} {P.shape[0]} {doy0} {year0} {resopt} {region.river_velo_opt} {len(stations)} {len(snapshots)} "
+                f"{0 if wtemp is None else 1}\n")
     with open(f"{d}/snapshots.txt", "w") as f:
         f.write(" ".join(str(int(s)) for s in snapshots) + "\n")
 
 
-def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None):
+def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wtemp=None):
     """Run the reference harness; returns dict(lai_a, lai_b, bottom_width, snapshots=[{field: array}],
     discharge=[ndays, nstation], stations=...)."""
     if not available():
@@ -156,7 +169,7 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None):
     stations = np.asarray(stations, np.int32)
     snapshots = list(snapshots or [ndays])
     tmp = workdir or tempfile.mkdtemp(prefix="wg_ref_")
-    write_case(region, tmp, P, T, S, doy0, stations, snapshots)
+    write_case(region, tmp, P, T, S, doy0, stations, snapshots, wtemp=wtemp)
     out = os.path.join(tmp, "out.bin")
     subprocess.run([HARNESS, tmp, out], check=True, stdout=subprocess.DEVNULL)
     raw = np.fromfile(out, np.float64)
@@ -172,8 +185,16 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None):
             snap[f] = raw[o:o + n].copy(); o += n
         bands = raw[o:o + REF_BANDS * n].reshape(REF_BANDS, n).T.copy(); o += REF_BANDS * n
         snap["snow_band"] = bands
+        if wtemp is not None:
+            for f in WT_FIELDS:
+                snap[f] = raw[o:o + n].copy(); o += n
         snaps.append(snap)
     res["snapshots"] = snaps
     res["discharge"] = raw[o:o + ndays * len(stations)].reshape(ndays, len(stations)).copy()
+    o += ndays * len(stations)
+    if wtemp is not None:
+        res["river_temp"] = raw[o:o + ndays * len(stations)].reshape(ndays, len(stations)).copy()
+        o += ndays * len(stations)
+    assert o == raw.size, (o, raw.size)
     res["stations"] = stations
     return res

@@ -56,11 +56,12 @@ static void write_raw(FILE *f, const double *p, size_t n) { fwrite(p, sizeof(dou
 int main(int argc, char **argv) {
   if (argc < 3) { fprintf(stderr, "usage: %s <case dir> <out file>\n", argv[0]); return 1; }
   std::string dir = argv[1];
-  int ncase, ndays, doy0, year0, resopt, velo, nstation, nsnap;
+  int ncase, ndays, doy0, year0, resopt, velo, nstation, nsnap, wtemp = 0;
   {
     std::ifstream m(dir + "/meta.txt");
     m >> ncase >> ndays >> doy0 >> year0 >> resopt >> velo >> nstation >> nsnap;
     if (!m) { fprintf(stderr, "harness: bad meta.txt\n"); return 2; }
+    if (!(m >> wtemp)) wtemp = 0;   // optional: water temperature (options.calc_wtemp)
   }
   std::vector<int> snap_days(nsnap);
   {
@@ -80,7 +81,9 @@ int main(int argc, char **argv) {
   options.aggrNUsGloLakResOpt = 0; options.climate_spatial_resolution = 0; options.resYearOpt = 0;
   options.resYearReference = 2000; options.resYearFirstToUse = 1900; options.resYearLastToUse = 2010;
   options.antNatOpt = 0; options.resNUsMeanYearFirst = 1971; options.resNUsMeanYearLast = 2000;
-  options.glacierOpt = 0; options.calc_wtemp = 0; options.start_year = year0; options.end_year = year0;
+  // calc_wtemp set directly: the option file parser would also switch on
+  // fractionalRoutingOpt (option.cpp:591-593), which this harness keeps off
+  options.glacierOpt = 0; options.calc_wtemp = wtemp; options.start_year = year0; options.end_year = year0;
   options.init_years = 0; options.time_step = 1; options.outLAImax = 0;
 
   ConfigFile cfg(dir + "/config.txt", year0, 1, "OL");
@@ -162,7 +165,16 @@ int main(int argc, char **argv) {
   auto P = read_raw<float>(dir + "/f_prec.bin", (size_t)ndays * ncase);
   auto T = read_raw<float>(dir + "/f_temp.bin", (size_t)ndays * ncase);
   auto S = read_raw<float>(dir + "/f_swrad.bin", (size_t)ndays * ncase);
+  std::vector<float> LW;
   std::vector<double> q((size_t)ndays * nstation, 0.0);
+  std::vector<double> wt_daily;   // water temperature state of the stations' cells after each day
+  if (wtemp) {
+    climate.init();   // allocates the month's daily grids (climate.cpp:44-56)
+    LW = read_raw<float>(dir + "/f_lwrad.bin", (size_t)ndays * ncase);
+    auto gwt = read_raw<float>(dir + "/c_gwtemp.bin", ncase);
+    for (int n = 0; n < ng; n++) climate.G_GW_Temperature_y[n] = n < ncase ? (double)gwt[n] : 10.;
+    wt_daily.assign((size_t)ndays * nstation, 0.0);
+  }
 
   int year = year0;
   int doy = doy0;
@@ -182,6 +194,12 @@ int main(int argc, char **argv) {
       climateYear.G_temperature_d365(n, doy - 1) = T[(size_t)d * ncase + n];
       climateYear.G_shortwave_d365(n, doy - 1) = S[(size_t)d * ncase + n];
     }
+    if (wtemp)   // the water temperature reads the month's daily grids (routing.cpp:4275-4277)
+      for (int n = 0; n < ncase; n++) {
+        climate.G_shortwave_d(n, day_in_month - 1) = S[(size_t)d * ncase + n];
+        climate.G_longwave_d(n, day_in_month - 1) = LW[(size_t)d * ncase + n];
+        climate.G_temperature_d(n, day_in_month - 1) = T[(size_t)d * ncase + n];
+      }
     for (int n = 0; n < ng; ++n)
       if (geo.G_contcell[n])
         dailyWaterBalance.calcNewDay((short)doy, (short)month, day_in_month, last_day_in_month[month], (short)year, n,
@@ -190,6 +208,8 @@ int main(int argc, char **argv) {
                     additionalOutIn, 0, calibParam);
     routing.updateLandAreaFrac(additionalOutIn);
     for (int b = 0; b < nstation; b++) q[(size_t)d * nstation + b] = routing.dailyRiverDischarge(b, doy - 1);
+    if (wtemp)
+      for (int b = 0; b < nstation; b++) wt_daily[(size_t)d * nstation + b] = routing.G_RiverWTempPreStep[stations[b]];
     if (snap_i < nsnap && snap_days[snap_i] == d + 1) {
       // state snapshot after day d+1, fixed field order (read by oracle/ref_case.py)
       std::vector<double> g(ncase);
@@ -218,6 +238,21 @@ int main(int argc, char **argv) {
       DUMP(dailyWaterBalance.G_dailyLocalSurfaceRunoff[n]);
       DUMP(dailyWaterBalance.G_dailyGwRecharge[n]);
       for (int e = 1; e <= 100; e++) DUMP(dailyWaterBalance.G_SnowInElevation(n, e));
+      if (wtemp) {   // water temperature state, the oracle's swb order
+        DUMP(routing.G_RiverWTempPreStep[n]);
+        DUMP(routing.G_locLakeTempPrevStep[n]);
+        DUMP(routing.G_locWetlTempPrevStep[n]);
+        DUMP(routing.G_gloLakeTempPrevStep[n]);
+        DUMP(routing.G_reservoirTempPrevStep[n]);
+        DUMP(routing.G_gloWetlandTempPrevStep[n]);
+        DUMP(routing.G_iceThicknessRiver[n]);
+        DUMP(routing.G_iceThicknesslocLake[n]);
+        DUMP(routing.G_iceThicknesslocWetland[n]);
+        DUMP(routing.G_iceThicknessGloLake[n]);
+        DUMP(routing.G_iceThicknessReservoir[n]);
+        DUMP(routing.G_iceThicknessGloWetland[n]);
+        DUMP(routing.G_RiverAvailPreStep[n]);
+      }
 #undef DUMP
       snap_i++;
     }
@@ -225,6 +260,7 @@ int main(int argc, char **argv) {
     if (doy == 1) year++;
   }
   write_raw(out, q.data(), q.size());
+  if (wtemp) write_raw(out, wt_daily.data(), wt_daily.size());
   fclose(out);
   return 0;
 }

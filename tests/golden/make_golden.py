@@ -6,7 +6,10 @@ runs each case below through the reference's calcNewDay/routing, and stores
 the inputs together with the reference's outputs, so that the tests can check
 the C restatement -- and through it the GPU library -- on any machine.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
+
+The water-temperature case (WT_CASES) adds longwave radiation, groundwater
+temperature and the reference's inflow-direction table to the inputs.
 """
 import os
 import sys
@@ -59,5 +62,51 @@ def main(names=None):
         print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+def wtemp_region(seed=21):
+    """A 24 x 48 block of the 0.5-degree grid with every water-body type; a third
+    of its inland sinks carry the reference's no-river marker (river length 55 in
+    the input file), so that the water temperature routes their local runoff into
+    the cell's water bodies."""
+    region = sy.region_small_swb(seed=seed, block_at=(100, 300))
+    raw = region.extras["river_length_file"].copy()
+    sinks = np.nonzero(region.downstream < 0)[0]
+    raw[sinks[::3]] = 55.0
+    region.extras["river_length_file"] = raw
+    region.arrays["river_length"] = raw * (region.contfreq / 100.)      # routing.cpp:480-482
+    return region
+
+
+# water temperature: name -> (region factory, days, first day of year, snapshot days)
+WT_CASES = {
+    "swb_wtemp_90d": (wtemp_region, 90, 240, [45, 90]),
+}
+
+
+def main_wtemp(names=None):
+    if not ref_case.available():
+        if not ref_case.build():
+            raise SystemExit("reference sources not found; cannot regenerate fixtures")
+    for name, (make, nd, doy0, snaps) in WT_CASES.items():
+        if names and name not in names:
+            continue
+        region = make()
+        P, T, S = sy.forcing(region, nd, doy0=doy0)
+        T = (T - 9.0).astype(np.float32)     # a cold autumn: ice forms, grows and breaks up
+        LW, GWT = sy.water_temp_inputs(region, nd, T)
+        outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+        stations = outl[:24]
+        res = ref_case.run(region, P, T, S, doy0=doy0, stations=stations, snapshots=snaps, wtemp=(LW, GWT))
+        extra = dict(P=P, T=T, S=S, LW=LW, GWT=GWT, doy0=np.array(doy0), stations=res["stations"],
+                     snap_days=np.array(snaps), discharge=res["discharge"], river_temp=res["river_temp"])
+        for i, snap in enumerate(res["snapshots"]):
+            snap.pop("snow_band")
+            for k in ref_case.WT_FIELDS + ["river", "soil", "gw"]:
+                extra[f"s{i}_{k}"] = snap[k]
+        path = os.path.join(HERE, f"{name}.npz")
+        save_npz(region, path, **extra)
+        print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 if __name__ == "__main__":
     main(sys.argv[1:])
+    main_wtemp(sys.argv[1:])

@@ -31,3 +31,43 @@ def test_wtemp_golden_records_cover_the_branches():
     assert (t == 0.).any(axis=0).all()                 # frozen or clamped to 0 degC
     assert (ice > 0).any(axis=0).all()                 # ice on every kind of water body
     assert (rec[:, 0] == 1).any()                      # power-plant cooling
+
+
+def _close(got, ref, floor):
+    """|got - ref| <= 1e-12 max(|ref|, floor): the reference ran 100 snow bands
+    (each synthetic band 20 times), the restatement 5, so sums differ in the last
+    place and carry into the temperatures."""
+    got, ref = np.asarray(got, np.float64), np.asarray(ref, np.float64)
+    return np.abs(got - ref) <= 1e-12 * np.maximum(np.abs(ref), floor)
+
+
+def test_oracle_water_temperature_in_routing_matches_reference():
+    """The restatement's routing with water temperature against the reference's
+    routing.cpp:4241-4513 (harness with calc_wtemp = 1) over a winter with ice:
+    river temperature at the stations every day, and every water body's
+    temperature, ice thickness and the river's last outflow at the snapshots."""
+    from oracle import Oracle, ref_case
+    from watergap2_gb300.region import load_npz
+    region, ex = load_npz(os.path.join(HERE, "golden", "swb_wtemp_90d.npz"))
+    P, T, S, LW = ex["P"], ex["T"], ex["S"], ex["LW"]
+    o = Oracle(region)
+    o.init_water_temp(ex["GWT"])
+    day, doy = 0, int(ex["doy0"])
+    temps = []
+    for i, sd in enumerate(int(x) for x in ex["snap_days"]):
+        _, dt = o.run_wt(doy, P[day:sd], T[day:sd], S[day:sd], LW[day:sd], daily_temp=True)
+        # the state the reference keeps after each day: -9999 becomes the air temperature (>= 0)
+        air = np.maximum(T[day:sd].astype(np.float64), 0.0)
+        temps.append(np.where(dt == -9999., air, dt))
+        doy = (doy - 1 + (sd - day)) % 365 + 1
+        day = sd
+        for k, f in enumerate(ref_case.WT_FIELDS[:6]):
+            assert _close(o.wt["temp"][k], ex[f"s{i}_{f}"], 1.0).all(), f
+        for k, f in enumerate(ref_case.WT_FIELDS[6:12]):
+            assert _close(o.wt["ice"][k], ex[f"s{i}_{f}"], 1e-9).all(), f
+        assert _close(o.wt["river_avail"], ex[f"s{i}_river_avail"], 1e-12).all()
+    got = np.concatenate(temps)[:, ex["stations"]]
+    assert _close(got, ex["river_temp"], 1.0).all()
+    # the case covers ice on every kind of water body and open rivers
+    assert all((ex[f"s1_{f}"] > 0).any() for f in ref_case.WT_FIELDS[6:12])
+    assert (ex["river_temp"] > 0).any() and (ex["river_temp"] == 0).any()

@@ -202,3 +202,29 @@ def load_npz(path: str):
     reg.extras = {k[2:]: z[k] for k in z.files if k.startswith("x_")}
     extra = {k[2:]: z[k] for k in z.files if k.startswith("e_")}
     return reg, extra
+
+
+def inflow_cells(region) -> np.ndarray:
+    """The cells flowing into each cell by direction, [ncell, 9] int32 (0-based,
+    -1 none), the table the reference's water temperature reads
+    (G_inflow_cells, built by rout_prepare.cpp:358-420): direction
+    3 * (1 - drow) + (1 + dcol) of the upstream cell's offset, [4] the cell
+    itself (never an inflow).  An upstream cell that is not a grid neighbour
+    takes the first free direction."""
+    n = region.ncell
+    out = np.full((n, 9), -1, np.int32)
+    down = region.downstream
+    for m in np.nonzero(down >= 0)[0]:
+        c = int(down[m])
+        k = -1
+        if region.row is not None:
+            drow, dcol = int(region.row[m]) - int(region.row[c]), int(region.col[m]) - int(region.col[c])
+            if abs(drow) <= 1 and abs(dcol) <= 1 and (drow, dcol) != (0, 0):
+                k = 3 * (1 - drow) + (1 + dcol)
+        if k < 0 or out[c, k] >= 0:
+            free = [j for j in range(9) if j != 4 and out[c, j] < 0]
+            if not free:
+                raise ValueError(f"cell {c} has more than 8 upstream cells")
+            k = free[0]
+        out[c, k] = m
+    return out

@@ -392,9 +392,12 @@ def region_64x64(seed: int = 1, nband: int = 5, row0: int = 60, col0: int = 300,
 
 def region_global(seed: int = 11, nband: int = 5, nland: int = 67420, n_outlets: int = 6000,
                   n_sinks: int = 60, swb=(2023, 1348, 300, 1200), river_velo_opt: int = 1,
-                  shape=(360, 720), name: str = "region_global") -> Region:
+                  shape=(360, 720), name: str = "region_global", block_at=None) -> Region:
     """Global 0.5-degree grid with a seeded land mask (default 67,420 land cells).
-    With another shape the grid spacing is 180/ny degrees."""
+    With another shape the grid spacing is 180/ny degrees, unless block_at =
+    (row0, col0) places the shape as a block of the 0.5-degree grid at that
+    0-based offset (no wrap in longitude): the geometry the reference's own
+    code reads."""
     rng = np.random.default_rng(seed)
     ny, nx = shape
     mask_f = fractal_field((ny, nx), 3.2, rng)
@@ -431,14 +434,16 @@ def region_global(seed: int = 11, nband: int = 5, nland: int = 67420, n_outlets:
     sel = rng.choice(ir.size, size=min(n_sinks, ir.size), replace=False)
     sinks = np.zeros_like(land)
     sinks[ir[sel], ic[sel]] = True
-    ldd, _ = flood_and_d8(dem, land, seeds | sinks, wrap=True)
+    wrap = block_at is None
+    ldd, _ = flood_and_d8(dem, land, seeds | sinks, wrap=wrap)
     ldd[sinks] = -1
     rr, cc = np.nonzero(land)
     index = -np.ones((ny, nx), np.int64)
     index[rr, cc] = np.arange(rr.size)
-    reg = _build_region(name, (rr + 1).astype(np.int64), (cc + 1).astype(np.int64), rr, cc, ldd, index,
+    r0, c0 = block_at if block_at is not None else (0, 0)
+    reg = _build_region(name, (rr + 1 + r0).astype(np.int64), (cc + 1 + c0).astype(np.int64), rr, cc, ldd, index,
                         dem[rr, cc], coastal[rr, cc], np.random.default_rng(seed + 2), nband, swb,
-                        river_velo_opt, wrap=True, res=180.0 / ny)
+                        river_velo_opt, wrap=wrap, res=0.5 if block_at is not None else 180.0 / ny)
     return reg
 
 
@@ -453,12 +458,13 @@ def region_5min(seed: int = 41, nband: int = 5, nland: int = 2_200_000, shape=(2
 
 
 def region_small_swb(seed: int = 21, nband: int = 5, ny: int = 24, nx: int = 48,
-                     river_velo_opt: int = 1) -> Region:
-    """Small grid with every water-body type, inland sinks and coastal cells (parity tests)."""
+                     river_velo_opt: int = 1, block_at=None) -> Region:
+    """Small grid with every water-body type, inland sinks and coastal cells (parity
+    tests); block_at = (row0, col0) puts it on the 0.5-degree grid (see region_global)."""
     nland = int(ny * nx * 0.55)
     return region_global(seed=seed, nband=nband, nland=nland, n_outlets=max(8, nland // 12), n_sinks=4,
                          swb=(max(4, nland // 20), max(4, nland // 20), max(3, nland // 60), max(4, nland // 40)),
-                         river_velo_opt=river_velo_opt, shape=(ny, nx))
+                         river_velo_opt=river_velo_opt, shape=(ny, nx), block_at=block_at)
 
 
 def forcing(region: Region, ndays: int, seed: int = 2, doy0: int = 1, day_offset: int = 0):
@@ -554,3 +560,18 @@ def forcing_year_parallel(region: Region, year: int, seed: int = 2, procs: int |
         shm.close()
         shm.unlink()
     return out
+
+
+def water_temp_inputs(region: Region, ndays: int, T: np.ndarray, seed: int = 9):
+    """Inputs the water temperature adds to the daily forcing: downward longwave
+    radiation [ndays, ncell] float32 (W/m2, from the air temperature through the
+    Stefan-Boltzmann law with a seeded effective emissivity), and the yearly
+    groundwater temperature [ncell] float32 (the annual mean air temperature of
+    the cell plus noise; negative values occur, as in the reference's input)."""
+    rng = np.random.default_rng(seed)
+    n = region.ncell
+    eps = rng.uniform(0.70, 0.95, (ndays, n))
+    tk = T.astype(np.float64) + 273.15
+    lw = (eps * 5.670374419e-8 * tk ** 4).astype(np.float32)
+    gw = (T.astype(np.float64).mean(axis=0) + rng.normal(0.0, 1.5, n)).astype(np.float32)
+    return lw, gw
