@@ -116,6 +116,11 @@ typedef struct wg_options {
                               wavefront (1..31; 0 = 1): a run of D days takes
                               ceil(D / days_per_step) + levels - 1 steps.  Results
                               do not depend on it                                    */
+  int32_t water_temp;      /* 1: water temperature of the river and every surface water
+                              body after each cell's routing (options.calc_wtemp = 1,
+                              routing.cpp:4241-4513; fractional routing stays off);
+                              FP64, one member.  Needs wg_upload_longwave and
+                              wg_set_water_temp_inputs                               */
 } wg_options;
 
 typedef struct wg_ctx wg_ctx;
@@ -169,6 +174,30 @@ wg_status wg_upload_forcing_unf(wg_ctx *ctx, int32_t day0, int32_t nd_file, int3
  * wg_upload_forcing_unf); returns the bytes read, -1 if the file cannot be
  * opened. */
 int64_t wg_read_unf(const char *path, void *dst, int64_t bytes);
+
+/* Water temperature (wg_options.water_temp = 1).  Downward longwave radiation
+ * [W/m2], day-major [ndays][ncell] cell order, into forcing slots day0.. (the
+ * reference's climate.G_longwave_d, climate.cpp:117-124). */
+wg_status wg_upload_longwave(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *longwave);
+
+/* The yearly groundwater temperature [degC] (climate.G_GW_Temperature_y,
+ * climate.cpp:109-111; negative values count as 0) and the river length as read
+ * from the input file (G_riverLengthCheck, routing.cpp:477; 55 marks a cell
+ * without a river), cell order; either may be NULL to keep the current values
+ * (start: 10 degC, the region's river length). */
+wg_status wg_set_water_temp_inputs(wg_ctx *ctx, const float *gw_temp, const double *river_length_check);
+
+/* Water temperature state, swb-major [6][ncell] cell order, swb 0 river,
+ * 1 local lake, 2 local wetland, 3 global lake, 4 reservoir, 5 global wetland:
+ * the previous day's temperature [degC] (G_RiverWTempPreStep and the
+ * *TempPrevStep grids; start 15) and ice thickness [km] (the G_iceThickness*
+ * grids; -9999 where the reference records none). */
+wg_status wg_get_water_temp(wg_ctx *ctx, double *temp, double *ice);
+wg_status wg_set_water_temp(wg_ctx *ctx, const double *temp, const double *ice);
+
+/* River temperature of the stations' cells after each output day [degC],
+ * [ndays][nstation] (the river entry of the state above, day by day). */
+wg_status wg_get_river_temp(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out);
 
 /* One day, the reference's call granularity: the vertical balance of every cell
  * (the OpenMP calcNewDay loop, source/integrateWGHM.cpp:767-783) for day of year

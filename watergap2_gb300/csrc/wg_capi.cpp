@@ -582,6 +582,14 @@ wg_status set_calib_param(wg_ctx *ctx, const DevCellsT<R> &c, int32_t k, const d
 }
 }  // namespace
 
+// cell-order host array -> slot-order device array (n values)
+template <class T>
+static wg_status to_slots(wg_ctx *ctx, const T *host, T *dev) {
+  std::vector<T> v(ctx->n);
+  for (int s = 0; s < ctx->n; ++s) v[s] = host[ctx->topo.cell_of_slot[s]];
+  return cuda_fail(ctx, cudaMemcpy(dev, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "water temperature");
+}
+
 extern "C" {
 
 const char *wg_status_string(wg_status s) {
@@ -602,6 +610,42 @@ const char *wg_last_error(const wg_ctx *ctx) { return ctx ? ctx->err.c_str() : "
 int32_t wg_num_levels(const wg_ctx *ctx) { return ctx ? ctx->topo.nlevel : 0; }
 int64_t wg_launch_count(const wg_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+// Water temperature buffers: state at the reference's start values (15 degC, no
+// ice: routing.cpp:172-197), the per-cell inputs in slot order.
+static wg_status setup_water_temp(wg_ctx *ctx, const wg_region *r) {
+  const int n = ctx->n;
+  const size_t N = ctx->nstate();
+  DevWaterTemp &w = ctx->wt;
+  w.temp = ctx->alloc<double>(6 * N);
+  w.ice = ctx->alloc<double>(6 * N);
+  w.outt = ctx->alloc<double>((size_t)2 * ctx->days_per_step * N);
+  w.lw = ctx->alloc<float>((size_t)ctx->max_days * n);
+  w.qst_t = ctx->alloc<double>((size_t)ctx->max_days * std::max(1, ctx->nstation));
+  if (!w.temp || !w.ice || !w.outt || !w.lw || !w.qst_t) return WG_ERR_NOMEM;
+  wg_status st = WG_OK;
+  std::vector<float> gwt(n, 10.f);
+  std::vector<double> lake(r->lake_area, r->lake_area + n), res(r->res_area, r->res_area + n);
+  std::vector<double> ll(r->loc_lake, r->loc_lake + n), lw(r->loc_wetl, r->loc_wetl + n);
+  std::vector<double> gw(r->glo_wetl, r->glo_wetl + n), len(r->river_length, r->river_length + n);
+  w.gwt = upload_slots<float>(ctx, gwt, st);
+  w.len_check = upload_slots<double>(ctx, len, st);
+  w.lake_km2 = upload_slots<double>(ctx, lake, st);
+  w.res_km2 = upload_slots<double>(ctx, res, st);
+  w.ll_pct = upload_slots<double>(ctx, ll, st);
+  w.lw_pct = upload_slots<double>(ctx, lw, st);
+  w.gw_pct = upload_slots<double>(ctx, gw, st);
+  if (st != WG_OK) return st;
+  std::vector<double> t15(6 * N, 15.), zero(6 * N, 0.);
+  cudaError_t e = cudaMemcpy(w.temp, t15.data(), 6 * N * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(w.ice, zero.data(), 6 * N * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(w.outt, 0, (size_t)2 * ctx->days_per_step * N * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset((void *)w.lw, 0, (size_t)ctx->max_days * n * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(w.qst_t, 0, (size_t)ctx->max_days * std::max(1, ctx->nstation) * sizeof(double));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "water temperature");
+  w.enabled = 1;
+  return WG_OK;
+}
+
 wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (!r || !opt || !out) return WG_ERR_INVALID;
   *out = nullptr;
@@ -613,6 +657,8 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->block_threads != 0 && !valid_block_threads(opt->block_threads, opt->precision, opt->members))
     return WG_ERR_INVALID;
   if (opt->days_per_step < 0 || opt->days_per_step > 31) return WG_ERR_INVALID;
+  if (opt->water_temp < 0 || opt->water_temp > 1) return WG_ERR_INVALID;
+  if (opt->water_temp && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
     if (r->lct[i] < 1 || r->lct[i] > WG_NLCT) return WG_ERR_INVALID;
@@ -647,6 +693,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   std::vector<uint32_t> cls(n);
   for (int i = 0; i < n; ++i) cls[i] = work_class(r, i);
   if (!opt->block_threads && ctx->members == 1) ctx->layout = default_layout(ctx.get());
+  if (opt->water_temp) ctx->layout.va_warps = 0;   // its wavefront kernel carries no vertical-balance warps
   ctx->va_warps_default = ctx->layout.va_warps;
   wg_status st = build_topology(n, r->downstream, r->rout_order, cls.data(), &ctx->layout, ctx->topo);
   if (st != WG_OK) return st;
@@ -809,6 +856,11 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
       ctx->rd.rs = ctx->alloc<double>((size_t)ring * N);
       ctx->rd.gwr = ctx->alloc<double>((size_t)ring * N);
       if (!ctx->rd.gwr) return WG_ERR_NOMEM;
+      if (opt->water_temp) {   // the river's open-water terms of the cells run ahead
+        ctx->rd.owp = ctx->alloc<double>((size_t)ring * N);
+        ctx->rd.owpet = ctx->alloc<double>((size_t)ring * N);
+        if (!ctx->rd.owpet) return WG_ERR_NOMEM;
+      }
     } else {
       ctx->rf.ring_days = ring;
       ctx->rf.rs = ctx->alloc<float>((size_t)ring * N);
@@ -883,6 +935,10 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   init.laf = laf.data(); init.laf_prev = zeros.data(); init.fswb_next = fswb.data(); init.laf_started = izero.data();
   st = ctx->precision == 0 ? broadcast_state(ctx.get(), ctx->sd, &init) : broadcast_state(ctx.get(), ctx->sf, &init);
   if (st != WG_OK) return st;
+  if (opt->water_temp) {
+    st = setup_water_temp(ctx.get(), r);
+    if (st != WG_OK) return st;
+  }
   const bool ens = ctx->members > 1;
   if (ctx->layout.idle_warp >= 0) ctx->threads = ctx->layout.threads;
   const int th = ctx->threads;
@@ -1018,6 +1074,86 @@ wg_status wg_math_eval(int32_t device, int32_t fn, const double *x, const double
   return e == cudaSuccess ? WG_OK : WG_ERR_CUDA;
 }
 
+wg_status wg_upload_longwave(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *longwave) {
+  if (!ctx || !longwave || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days) return WG_ERR_INVALID;
+  if (!ctx->wt.enabled) return WG_ERR_UNSUPPORTED;
+  cudaSetDevice(ctx->device);
+  join_uploads(ctx);
+  const int n = ctx->n;
+  for (int d = 0; d < ndays; d += ctx->staging_days) {
+    const int nd = std::min(ctx->staging_days, ndays - d);
+    cudaError_t e = cudaMemcpyAsync(ctx->staging, longwave + (size_t)d * n, (size_t)nd * n * sizeof(float),
+                                    cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+      e = launch_gather_forcing(ctx->staging, (float *)ctx->wt.lw + (size_t)(day0 + d) * n, ctx->d_cell_of_slot, n, nd,
+                                ctx->stream);
+    ctx->launches++;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "upload_longwave");
+  }
+  return WG_OK;
+}
+
+wg_status wg_set_water_temp_inputs(wg_ctx *ctx, const float *gw_temp, const double *river_length_check) {
+  if (!ctx) return WG_ERR_INVALID;
+  if (!ctx->wt.enabled) return WG_ERR_UNSUPPORTED;
+  cudaSetDevice(ctx->device);
+  wg_status st = wg_synchronize(ctx);
+  if (st == WG_OK && gw_temp) st = to_slots(ctx, gw_temp, (float *)ctx->wt.gwt);
+  if (st == WG_OK && river_length_check) st = to_slots(ctx, river_length_check, (double *)ctx->wt.len_check);
+  return st;
+}
+
+// [6][ncell] cell order <-> [6][N] slot order
+static wg_status water_temp_io(wg_ctx *ctx, double *temp, double *ice, const double *temp_in, const double *ice_in) {
+  if (!ctx) return WG_ERR_INVALID;
+  if (!ctx->wt.enabled) return WG_ERR_UNSUPPORTED;
+  cudaSetDevice(ctx->device);
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  const int n = ctx->n;
+  std::vector<double> buf((size_t)6 * n);
+  double *dev[2] = {ctx->wt.temp, ctx->wt.ice};
+  double *out[2] = {temp, ice};
+  const double *in[2] = {temp_in, ice_in};
+  for (int k = 0; k < 2; ++k) {
+    cudaError_t e = cudaSuccess;
+    if (in[k]) {
+      for (int j = 0; j < 6; ++j)
+        for (int s = 0; s < n; ++s) buf[(size_t)j * n + s] = in[k][(size_t)j * n + ctx->topo.cell_of_slot[s]];
+      e = cudaMemcpy(dev[k], buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice);
+    } else if (out[k]) {
+      e = cudaMemcpy(buf.data(), dev[k], buf.size() * sizeof(double), cudaMemcpyDeviceToHost);
+      for (int j = 0; j < 6 && e == cudaSuccess; ++j)
+        for (int s = 0; s < n; ++s) out[k][(size_t)j * n + ctx->topo.cell_of_slot[s]] = buf[(size_t)j * n + s];
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "water temperature");
+  }
+  return WG_OK;
+}
+
+wg_status wg_get_water_temp(wg_ctx *ctx, double *temp, double *ice) {
+  if (!temp && !ice) return WG_ERR_INVALID;
+  return water_temp_io(ctx, temp, ice, nullptr, nullptr);
+}
+
+wg_status wg_set_water_temp(wg_ctx *ctx, const double *temp, const double *ice) {
+  if (!temp && !ice) return WG_ERR_INVALID;
+  return water_temp_io(ctx, nullptr, nullptr, temp, ice);
+}
+
+wg_status wg_get_river_temp(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out) {
+  if (!ctx || !out || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days) return WG_ERR_INVALID;
+  if (!ctx->wt.enabled) return WG_ERR_UNSUPPORTED;
+  cudaSetDevice(ctx->device);
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  const size_t k = (size_t)std::max(1, ctx->nstation);
+  return cuda_fail(ctx,
+                   cudaMemcpy(out, ctx->wt.qst_t + (size_t)day0 * k, (size_t)ndays * ctx->nstation * sizeof(double),
+                              cudaMemcpyDeviceToHost),
+                   "get_river_temp");
+}
+
 int64_t wg_read_unf(const char *path, void *dst, int64_t bytes) {
   if (!path || !dst || bytes < 0) return -1;
   FILE *f = std::fopen(path, "rb");
@@ -1048,6 +1184,7 @@ wg_status wg_step_vertical(wg_ctx *ctx, int32_t doy, int32_t fday) {
   cudaSetDevice(ctx->device);
   join_uploads(ctx);
   ctx->launches++;
+  ctx->last_vertical_fday = fday;   // the day's forcing slot, for the water temperature of wg_step_routing
   cudaError_t e = ctx->precision == 0
                       ? launch_vertical(ctx->cd, ctx->sd, ctx->vd, ctx->forcing, doy, fday, ctx->stream)
                       : launch_vertical(ctx->cf, ctx->sf, ctx->vf, ctx->forcing, doy, fday, ctx->stream);
@@ -1062,11 +1199,15 @@ wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday) {
   ctx->launches++;
   cudaError_t e = ctx->precision == 0
                       ? launch_pipeline(false, ctx->cd, ctx->sd, ctx->vd, ctx->forcing, ctx->mem, ctx->balance,
-                                        ctx->rd, ctx->sync, ctx->outq, ctx->qst, doy, 0, oday, 1, 0, ctx->topo.nlevel,
-                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, DevVaWork{}, ctx->stream)
+                                        ctx->rd, ctx->sync, ctx->outq, ctx->qst, doy, ctx->last_vertical_fday, oday, 1,
+                                        0, ctx->topo.nlevel,
+                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, DevVaWork{}, ctx->wt,
+                                        ctx->stream)
                       : launch_pipeline(false, ctx->cf, ctx->sf, ctx->vf, ctx->forcing, ctx->mem, ctx->balance,
-                                        ctx->rf, ctx->sync, ctx->outq, ctx->qst, doy, 0, oday, 1, 0, ctx->topo.nlevel,
-                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, DevVaWork{}, ctx->stream);
+                                        ctx->rf, ctx->sync, ctx->outq, ctx->qst, doy, ctx->last_vertical_fday, oday, 1,
+                                        0, ctx->topo.nlevel,
+                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, DevVaWork{}, ctx->wt,
+                                        ctx->stream);
   return cuda_fail(ctx, e, "step_routing");
 }
 
@@ -1104,7 +1245,7 @@ static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevSta
     if (e == cudaSuccess)
       e = launch_pipeline(true, c, s, v, ctx->forcing, ctx->mem, ctx->balance, ring, ctx->sync, ctx->outq, ctx->qst,
                           doy0, fday0, fday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->layout, ctx->mon,
-                          vw, ctx->stream);
+                          vw, ctx->wt, ctx->stream);
     ctx->launches++;
     if (ev) cudaEventRecord(ev[2], ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "run_steps");

@@ -17,6 +17,7 @@ using wg::DevCellsT;
 using wg::DevForcing;
 using wg::DevMembers;
 using wg::DevMonthly;
+using wg::DevWaterTemp;
 using wg::DevRingT;
 using wg::DevStateT;
 using wg::DevSync;
@@ -80,6 +81,8 @@ struct wg_ctx {
   std::string err;
   int chunk_steps = 0;                     // steps per (vertical-ahead, wavefront) launch pair
   int days_per_step = 1;                   // days every cell advances per wavefront step
+  DevWaterTemp wt{};                       // water temperature (wt.enabled = 0: off)
+  int last_vertical_fday = 0;              // forcing slot of the last wg_step_vertical
   int va_warps_default = 0;                // vertical-balance warps the layout was sized for
   unsigned int *va_next = nullptr;         // their work counter
   Snapshot *snap = nullptr;                // device copy of the mutable state (autotuner)

@@ -137,8 +137,25 @@ struct DevMembers {
 template <class R>
 struct DevRingT {
   R *rs, *gwr;
+  R *owp, *owpet;          // open-water precipitation and PET (only with the water temperature, else null)
   int32_t ring_days;
   int32_t days_per_step;   // days every cell advances per wavefront step (K >= 1)
+};
+
+// Water temperature (routing.cpp:4241-4513): state and inputs, slot order.
+// swb index [0] river, [1] local lake, [2] local wetland, [3] global lake,
+// [4] reservoir, [5] global wetland.
+struct DevWaterTemp {
+  double *temp;              // [6][N] the previous day's temperatures [degC]
+  double *ice;               // [6][N] ice thickness [km] (-9999 where a water body has none)
+  double *outt;              // [2][days_per_step][N] river temperature of the step, read downstream
+  const float *lw;           // [max_days][n] downward longwave radiation [W/m2]
+  const float *gwt;          // [n] yearly groundwater temperature [degC]
+  const double *len_check;   // [n] river length as read (55: no river in the cell)
+  const double *lake_km2, *res_km2;   // [n] global lake and reservoir area [km2]
+  const double *ll_pct, *lw_pct, *gw_pct;   // [n] local lake, local and global wetland [% of the cell]
+  double *qst_t;             // [max_days][nstation] river temperature at the stations
+  int32_t enabled;
 };
 
 // Vertical balance of the cells without water bodies run by extra warps of the

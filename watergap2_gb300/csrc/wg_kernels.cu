@@ -35,6 +35,7 @@
 #include "wg_kernels.h"
 #include "wg_physics.cuh"
 #include "wg_volume.cuh"
+#include "wg_wtemp.cuh"
 
 namespace wg {
 
@@ -242,6 +243,10 @@ __device__ __forceinline__ void va_cell(const DevCellsT<R> &c, const DevStateT<R
     const size_t ri = (size_t)(d % ring.ring_days) * N + i;
     ring.rs[ri] = o.rs;
     ring.gwr[ri] = o.gwr;
+    if (ring.owp) {   // the water temperature's open-water terms of the river
+      ring.owp[ri] = o.owp;
+      ring.owpet[ri] = o.owpet;
+    }
     if (b.enabled) {
       acc_in += (double)o.land_in * land_f;
       acc_ev += (double)o.land_evap * land_f;
@@ -272,12 +277,91 @@ __global__ void __launch_bounds__(VaBounds<R, ENS>::threads, VaBounds<R, ENS>::m
     va_cell<R, ENS>(c, st, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e, i, N);
 }
 
-template <class R, bool FUSED, bool ENS, bool VAW>
+// Water temperature of cell s after its routing (routing.cpp:4241-4513): the
+// inputs of calcWTemp from the cell's routing terms, the upstream river outflow
+// of the day and the energy it carries; updates the cell's temperatures and ice
+// (a water body without a temperature keeps the air temperature, at least 0)
+// and returns the river temperature the downstream cell reads.
+template <class R>
+__device__ __forceinline__ double cell_water_temp(const DevCellsT<R> &c, const DevWaterTemp &w, const DevForcing &f,
+                                                  int s, size_t si, size_t N, size_t fo, uint32_t fl, const VOut<R> &o,
+                                                  const WTerms<R> &x, R river_stor, double tot_in, double e_in) {
+  wt::WtIn t;
+  t.calc_temp_pp = 0.; t.pp_withdrawal = 0.; t.pp_consumption = 0.;
+  t.short_rad = (double)f.swrad[fo];
+  t.long_rad = (double)w.lw[fo];
+  t.air_temp = (double)f.temp[fo];
+  const float g = w.gwt[s];
+  t.gw_temp = g < 0.f ? 0. : (double)g;
+  t.cfa = (double)c.cfa[s];
+  t.ow_pet = (double)o.owpet;
+  t.ow_prec = (double)o.owp;
+  t.cell_area = (double)c.area[s];
+  t.inflow_sum = tot_in;
+  t.inflow_energy = e_in;
+  t.own_temp_prev = w.temp[si];
+  for (int k = 0; k < 6; ++k) t.ice[k] = w.ice[(size_t)k * N + si];
+  t.loclake_area = w.ll_pct[s];
+  t.loclake_stor_prev = (double)x.loclake_prev + (double)x.loclake_max;
+  t.loclake_temp_prev = w.temp[1 * N + si];
+  t.loclake_evapo = (double)x.loclake_evapo;
+  t.loclake_rf = (double)x.loclake_rf;
+  t.local_runoff = (double)x.local_runoff;
+  t.local_gw_runoff = (double)x.gw_runoff;
+  t.locwetl_area = w.lw_pct[s];
+  t.locwetl_stor_prev = (double)x.locwetl_prev;
+  t.locwetl_temp_prev = w.temp[2 * N + si];
+  t.locwetl_evapo = (double)x.locwetl_evapo;
+  t.locwetl_rf = (double)x.locwetl_rf;
+  t.locwetl_inflow = (double)x.loclake_out;
+  t.locwetl_outflow = (double)x.locwetl_out;
+  t.glolake_area = w.lake_km2[s];
+  t.glolake_stor_prev = (double)x.glolake_prev + (double)x.glolake_max;
+  t.glolake_temp_prev = w.temp[3 * N + si];
+  t.glolake_evapo = (double)x.glolake_evapo;
+  t.glolake_inflow = tot_in;
+  if (t.locwetl_area > 0.) t.glolake_inflow += t.locwetl_outflow;
+  else if (t.loclake_area > 0.) t.glolake_inflow += t.locwetl_inflow;
+  t.res_area = w.res_km2[s];
+  t.res_inflow = t.glolake_area > 0. ? (double)x.glolake_out : t.glolake_inflow;
+  t.res_stor_prev = (double)x.res_prev;
+  t.res_temp_prev = w.temp[4 * N + si];
+  t.res_evapo = (double)x.res_evapo;
+  t.glowetl_area = w.gw_pct[s];
+  if (t.res_area > 0.) t.glowetl_inflow = (double)x.res_out;
+  else if (t.glolake_area > 0.) t.glowetl_inflow = (double)x.glolake_out;
+  else t.glowetl_inflow = t.glolake_inflow;
+  t.glowetl_stor_prev = (double)x.glowetl_prev;
+  t.glowetl_temp_prev = w.temp[5 * N + si];
+  t.glowetl_evapo = (double)x.glowetl_evapo;
+  t.glowetl_rf = (double)x.glowetl_rf;
+  if (t.glowetl_area > 0.) t.river_inflow = (double)x.glowetl_out;
+  else if (t.res_area > 0.) t.river_inflow = (double)x.res_out;
+  else if (t.glolake_area > 0.) t.river_inflow = (double)x.glolake_out;
+  else t.river_inflow = t.glolake_inflow;
+  t.river_stor = (double)river_stor;
+  t.gw_runoff_into_river = 0.;   // fractional routing is off: all runoff passes the water bodies
+  t.runoff_into_river = 0.;
+  t.river_bottom_width = (double)c.bw[s];
+  t.river_length = (double)c.rlen[s];
+  t.river_length_check = w.len_check[s];
+  t.has_outflow = (fl & F_OUTLET) ? 0. : 1.;
+  double out[12];
+  wt::water_temp_cell(t, out);
+  const double keep = t.air_temp < 0. ? 0. : t.air_temp;
+  for (int k = 0; k < 6; ++k) {
+    w.ice[(size_t)k * N + si] = out[6 + k];
+    w.temp[(size_t)k * N + si] = out[k] == -9999. ? keep : out[k];
+  }
+  return out[0] == -9999. ? keep : out[0];
+}
+
+template <class R, bool FUSED, bool ENS, bool VAW, bool WT>
 __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R, ENS, VAW>::min_blocks) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
                                                   double *outq, double *qst, int doy0, int fday0, int oday0,
                                                   int ndays, int t_b, int t_e, int cell_warps, int idle_warp,
-                                                  DevMonthly mon, DevVaWork vw) {
+                                                  DevMonthly mon, DevVaWork vw, DevWaterTemp wtp) {
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const size_t N = (size_t)n * M;
@@ -336,6 +420,8 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
     if (kd * (t - c.nlevel + 1) < ndays) {   // some cell still has a day to compute
       double *q_now0 = outq + (size_t)(t & 1) * kd * N;
       const double *q_prev0 = outq + (size_t)((t + 1) & 1) * kd * N;
+      double *t_now0 = WT ? wtp.outt + (size_t)(t & 1) * kd * N : nullptr;   // river temperature, same slots
+      const double *t_prev0 = WT ? wtp.outt + (size_t)((t + 1) & 1) * kd * N : nullptr;
       // state index i always belongs to thread i mod gstride, so a cell's state is read
       // and written by one thread; only upstream outflows cross threads (read via L2)
       for (long long i = gtid; i < (long long)N; i += gstride) {
@@ -363,6 +449,10 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
           o.gwr = ring.gwr[ri];
           o.transfer = R(0); o.owp = R(0); o.owpet = R(0);
           o.land_in = R(0); o.land_evap = R(0); o.land_leak = R(0);   // accounted ahead
+          if constexpr (WT) {
+            o.owp = ring.owp[ri];
+            o.owpet = ring.owpet[ri];
+          }
         } else if (FUSED) {
           const size_t fo = (size_t)(fday0 + d) * n + s;
           R Pin = R(f.prec[fo]);
@@ -379,15 +469,29 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
           o.land_in = v.land_in[s]; o.land_evap = v.land_evap[s]; o.land_leak = v.land_leak[s];
         }
         // upstream inflow, summed in FP64 in the reference's push order (routing.cpp:3955-3958)
-        double up = 0.;
+        double up = 0., e_up = 0.;
         const int u0 = c.up_ptr[s], u1 = c.up_ptr[s + 1];
-        for (int k = u0; k < u1; ++k) up += __ldcg(q_prev + (size_t)c.up_idx[k] * M + mm);
+        for (int k = u0; k < u1; ++k) {
+          const size_t ui = (size_t)c.up_idx[k] * M + mm;
+          const double qu = __ldcg(q_prev + ui);
+          up += qu;
+          if constexpr (WT)   // the energy the inflow carries (calcWaterTemp.cpp:76-83)
+            e_up += qu * WT_RHO_W * WT_HEAT_CAP_W * (__ldcg(t_prev0 + (size_t)kk * N + ui) + WT_CONV_K);
+        }
         RState<R> rs = resident ? rs_keep : load_rstate(st, si, fl);
         RTerms<R> rt;
-        const R tv = routing_cell<R>(c, s, rs, doy, month, laf, laf_prev, o, up, rt);
+        WTerms<R> wtm;
+        const R tv = routing_cell<R, WT>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtm);
         if (resident) rs_keep = rs;
         else store_rstate(st, si, rs, fl);
         q_now[si] = (double)tv;
+        if constexpr (WT) {
+          const size_t fo = (size_t)(fday0 + d) * n + s;
+          const double tr = cell_water_temp<R>(c, wtp, f, s, si, N, fo, fl, o, wtm, rs.river, up, e_up);
+          t_now0[(size_t)kk * N + si] = tr;
+          const int stw = c.station[s];
+          if (stw >= 0) wtp.qst_t[(size_t)(oday0 + d) * c.nstation + stw] = tr;
+        }
         if (b.enabled) {
           const double land_f = (double)c.area_f[s] * (double)laf;
           if (!FUSED || (fl & F_VINLINE))
@@ -627,19 +731,24 @@ cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, 
 }
 
 template <class R>
-static const void *pipeline_fn(bool fused, bool ens, bool vaw) {
-  if (ens) return (const void *)k_pipeline<R, true, true, false>;
-  if (vaw) {   // FP64 single member only
-    if constexpr (std::is_same<R, double>::value) return (const void *)k_pipeline<R, true, false, true>;
-    return nullptr;
+static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false) {
+  if (ens) return wt ? nullptr : (const void *)k_pipeline<R, true, true, false, false>;
+  if constexpr (std::is_same<R, double>::value) {   // FP64 single member only
+    if (wt) return vaw ? nullptr
+                       : (fused ? (const void *)k_pipeline<R, true, false, false, true>
+                                : (const void *)k_pipeline<R, false, false, false, true>);
+    if (vaw) return (const void *)k_pipeline<R, true, false, true, false>;
+  } else {
+    if (vaw || wt) return nullptr;
   }
-  return fused ? (const void *)k_pipeline<R, true, false, false> : (const void *)k_pipeline<R, false, false, false>;
+  return fused ? (const void *)k_pipeline<R, true, false, false, false>
+               : (const void *)k_pipeline<R, false, false, false, false>;
 }
 
 template <class R>
-int pipeline_max_blocks(bool fused, bool ens, int threads, bool vaw) {
+int pipeline_max_blocks(bool fused, bool ens, int threads, bool vaw, bool wt) {
   int dev = 0, nsm = 0, per = 0;
-  const void *fn = pipeline_fn<R>(fused, ens, vaw);
+  const void *fn = pipeline_fn<R>(fused, ens, vaw, wt);
   if (!fn) return 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -652,7 +761,7 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
                             const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
                             const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
                             int t_b, int t_e, int blocks, int threads, const WarpLayout &lay, const DevMonthly &mon,
-                            const DevVaWork &vw, cudaStream_t st) {
+                            const DevVaWork &vw, const DevWaterTemp &wtp, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(sync.counter, 0, sizeof(unsigned), st);
   if (e == cudaSuccess && sync.flow && sync.wstep)
     e = cudaMemsetAsync(sync.wstep, 0xff, (size_t)sync.nwarps * sizeof(int), st);   // -1: no step done yet
@@ -669,9 +778,9 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
   void *args[] = {(void *)&c,    (void *)&s,    (void *)&v,     (void *)&f,     (void *)&mem,   (void *)&b,
                   (void *)&ring, (void *)&sync, (void *)&outq,  (void *)&qst,   (void *)&doy0,  (void *)&fday0,
                   (void *)&oday0, (void *)&ndays, (void *)&t_b, (void *)&t_e, (void *)&cell_warps,
-                  (void *)&idle_warp, (void *)&mon, (void *)&vwk};
+                  (void *)&idle_warp, (void *)&mon, (void *)&vwk, (void *)&wtp};
   const bool ens = mem.members > 1;
-  const void *fn = pipeline_fn<R>(fused, ens, vaw);
+  const void *fn = pipeline_fn<R>(fused, ens, vaw, wtp.enabled != 0);
   if (!fn) return cudaErrorInvalidConfiguration;
   if (vaw) threads += 32 * vw.warps;
   // cooperative (all blocks resident, or the launch fails) through the launch
@@ -710,12 +819,12 @@ cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int
 #define WG_INSTANTIATE(R)                                                                                          \
   template cudaError_t launch_vertical<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,        \
                                           const DevForcing &, int, int, cudaStream_t);                             \
-  template int pipeline_max_blocks<R>(bool, bool, int, bool);                                                           \
+  template int pipeline_max_blocks<R>(bool, bool, int, bool, bool);                                                           \
   template cudaError_t launch_pipeline<R>(bool, const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,  \
                                           const DevForcing &, const DevMembers &, const DevBalance &,             \
                                           const DevRingT<R> &, const DevSync &, double *, double *, int, int,     \
                                           int, int, int, int, int, int, const WarpLayout &, const DevMonthly &,    \
-                                          const DevVaWork &, cudaStream_t);                                       \
+                                          const DevVaWork &, const DevWaterTemp &, cudaStream_t);                 \
   template cudaError_t launch_vertical_ahead<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevForcing &,   \
                                                 const DevMembers &, const DevBalance &, const DevRingT<R> &, int,  \
                                                 int, int, int, int, int, int, cudaStream_t);                       \

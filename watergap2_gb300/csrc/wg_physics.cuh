@@ -411,6 +411,20 @@ struct RTerms {
   R velocity;   // river flow velocity of the day [km/d]
 };
 
+// What the water temperature reads from a cell's routing (routing.cpp:4287-4356):
+// each water body's storage before the day and its capacity where the
+// reference adds it, its evaporation [mm] after any reduction, the area
+// reduction factor the day started with, its outflow, and the local runoff.
+template <class R>
+struct WTerms {
+  R loclake_prev, loclake_max, loclake_evapo, loclake_rf, loclake_out;
+  R locwetl_prev, locwetl_evapo, locwetl_rf, locwetl_out;
+  R glolake_prev, glolake_max, glolake_evapo, glolake_out;
+  R res_prev, res_evapo, res_out;
+  R glowetl_prev, glowetl_evapo, glowetl_rf, glowetl_out;
+  R local_runoff, gw_runoff;
+};
+
 // Routing state of one cell (surface water and groundwater storages).
 template <class R>
 struct RState {
@@ -441,9 +455,10 @@ __device__ __forceinline__ R river_velocity(const DevCellsT<R> &c, int s, R rive
 // One cell of routingClass::routing (routing.cpp:1835-4520) given the vertical
 // outputs and the summed upstream inflow (FP64 for every precision); returns the
 // transported volume.
-template <class R>
+template <class R, bool WT = false>
 __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R> &st, int doy, int month, R laf,
-                                          R laf_prev, const VOut<R> &v, double inflow_up, RTerms<R> &rt) {
+                                          R laf_prev, const VOut<R> &v, double inflow_up, RTerms<R> &rt,
+                                          WTerms<R> *wtm = nullptr) {
   typedef M<R> m;
   const uint32_t fl = c.flags[s];
   const R cfa = c.cfa[s];
@@ -464,6 +479,11 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   }
   st.gw = gw;
   R inflow = dlsr + gw_runoff;
+  if constexpr (WT) {
+    *wtm = WTerms<R>{};
+    wtm->local_runoff = inflow;
+    wtm->gw_runoff = gw_runoff;
+  }
   const R owp = v.owp, owpet = v.owpet;
   R outflow = R(0);
   const R a6 = c.a6[s];
@@ -482,9 +502,13 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (PETgwr > PETgwrMax) {
       S = -maxS;
       rt.e_ow += avail;
+      if constexpr (WT) evapo *= PETgwrMax / PETgwr;
     } else {
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
+    }
+    if constexpr (WT) {
+      wtm->loclake_prev = S0; wtm->loclake_max = maxS; wtm->loclake_rf = rf; wtm->loclake_evapo = evapo;
     }
     rt.p_ow += pin;
     if (S0 > R(0)) {
@@ -499,6 +523,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = maxS;
     }
     inflow = outflow;
+    if constexpr (WT) wtm->loclake_out = outflow;
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * (R(0.5) * c.inv_maxs_ll[s]), c.evx[s]);
     st.loclake = S;
     st.rf_loclake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -515,9 +540,13 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (PETgwr > PETgwrMax) {
       S = R(0);
       rt.e_ow += PETgwrMax;
+      if constexpr (WT) evapo *= PETgwrMax / PETgwr;
     } else {
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
+    }
+    if constexpr (WT) {
+      wtm->locwetl_prev = S0; wtm->locwetl_rf = rf; wtm->locwetl_evapo = evapo;
     }
     rt.p_ow += pin;
     if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
@@ -531,6 +560,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = maxS;
     }
     inflow = outflow;
+    if constexpr (WT) wtm->locwetl_out = outflow;
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_maxs_lw[s], c.evx[s]);
     st.locwetl = S;
     st.rf_locwetl = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -550,6 +580,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = -maxS;
       outflow = R(0);
       rt.e_ow += PUmax;
+      if constexpr (WT) evapo *= PUmax / PU;
     } else {
       S = S0 * c.sw_e[s] + c.sw_ik[s] * (TI - PU) * c.sw_ome[s];
       outflow = TI + S0 - S - PU;
@@ -565,6 +596,9 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     }
     if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     inflow = outflow;
+    if constexpr (WT) {
+      wtm->glolake_prev = S0; wtm->glolake_max = maxS; wtm->glolake_evapo = evapo; wtm->glolake_out = outflow;
+    }
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * (R(0.5) * c.inv_maxs_gl[s]), c.evx[s]);
     st.glolake = S;
     st.rf_glolake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -582,6 +616,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (PETgwr > PETgwrMax) {
       S = S0 + TI - PETgwrMax;
       rt.e_ow += PETgwrMax;
+      if constexpr (WT) evapo *= PETgwrMax / PETgwr;
     } else {
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
@@ -607,6 +642,9 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = R(0);
     }
     inflow = outflow;
+    if constexpr (WT) {
+      wtm->res_prev = S0; wtm->res_evapo = evapo; wtm->res_out = outflow;
+    }
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_rcap[s], R(2.81383));
     st.res = S;
     st.rf_res = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -625,6 +663,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = R(0);
       outflow = R(0);
       rt.e_ow += PETgwrMax;
+      if constexpr (WT) evapo *= PETgwrMax / PETgwr;
     } else {
       S = S0 * c.sw_e[s] + c.sw_ik[s] * (TI - PETgwr) * c.sw_ome[s];
       outflow = TI + S0 - S - PETgwr;
@@ -636,6 +675,9 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     }
     if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     inflow = outflow;
+    if constexpr (WT) {
+      wtm->glowetl_prev = S0; wtm->glowetl_rf = rf; wtm->glowetl_evapo = evapo; wtm->glowetl_out = outflow;
+    }
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_maxs_gw[s], c.evx[s]);
     st.glowetl = S;
     st.rf_glowetl = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);

@@ -30,7 +30,8 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_get_launch_shape", "wg_num_levels", "wg_launch_count", "wg_last_error", "wg_status_string",
            "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc",
            "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_set_vertical_overlap", "wg_get_vertical_overlap",
-           "wg_math_eval", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
+           "wg_math_eval", "wg_upload_longwave", "wg_set_water_temp_inputs", "wg_get_water_temp",
+           "wg_set_water_temp", "wg_get_river_temp", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
            "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells",
            "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync")
@@ -60,7 +61,7 @@ class _Options(ctypes.Structure):
                 ("record_balance", ctypes.c_int32), ("stations", ctypes.c_void_p), ("stream", ctypes.c_uint64),
                 ("precision", ctypes.c_int32), ("members", ctypes.c_int32), ("member_prec_factor", ctypes.c_void_p),
                 ("member_gamma_factor", ctypes.c_void_p), ("block_threads", ctypes.c_int32),
-                ("ring_days", ctypes.c_int32), ("days_per_step", ctypes.c_int32)]
+                ("ring_days", ctypes.c_int32), ("days_per_step", ctypes.c_int32), ("water_temp", ctypes.c_int32)]
 
 
 _lib = None
@@ -124,6 +125,11 @@ def load_library(path: str = LIB_PATH):
     lib.wg_get_chunk_steps.argtypes = [vp]
     lib.wg_get_chunk_steps.restype = i32
     lib.wg_math_eval.argtypes = [i32, i32, vp, vp, ctypes.c_int64, vp]
+    lib.wg_upload_longwave.argtypes = [vp, i32, i32, vp]
+    lib.wg_set_water_temp_inputs.argtypes = [vp, vp, vp]
+    lib.wg_get_water_temp.argtypes = [vp, vp, vp]
+    lib.wg_set_water_temp.argtypes = [vp, vp, vp]
+    lib.wg_get_river_temp.argtypes = [vp, i32, i32, vp]
     lib.wg_set_vertical_overlap.argtypes = [vp, i32]
     lib.wg_get_vertical_overlap.argtypes = [vp]
     lib.wg_get_vertical_overlap.restype = i32
@@ -139,7 +145,8 @@ def load_library(path: str = LIB_PATH):
                  "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
                  "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async",
                  "wg_set_active_cells", "wg_upload_forcing_unf", "wg_monthly_outputs", "wg_get_monthly",
-                 "wg_set_step_sync", "wg_set_vertical_overlap"):
+                 "wg_set_step_sync", "wg_set_vertical_overlap", "wg_upload_longwave", "wg_set_water_temp_inputs",
+                 "wg_get_water_temp", "wg_set_water_temp", "wg_get_river_temp"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -192,7 +199,7 @@ class Model:
     def __init__(self, region: Region, max_days: int = 366, stations=None, record_balance: bool = False,
                  device: int = 0, stream: int = 0, precision: str = "fp64", members: int = 1,
                  prec_factor=None, gamma_factor=None, block_threads: int = 0, ring_days: int = 0,
-                 days_per_step: int = 0):
+                 days_per_step: int = 0, water_temp: bool = False):
         self.lib = load_library()
         self.region = region
         self._keep = []
@@ -222,6 +229,7 @@ class Model:
         o.block_threads = int(block_threads)
         o.ring_days = int(ring_days)
         o.days_per_step = int(days_per_step)
+        o.water_temp = int(bool(water_temp))
         self.max_days = int(max_days)
         h = ctypes.c_void_p()
         self._check(self.lib.wg_create(ctypes.byref(r), ctypes.byref(o), ctypes.byref(h)), "wg_create", None)
@@ -420,6 +428,41 @@ class Model:
         if steps is not None:
             self._check(self.lib.wg_set_chunk_steps(self.h, int(steps)), "set_chunk_steps")
         return int(self.lib.wg_get_chunk_steps(self.h))
+
+    # ---- water temperature (water_temp=True)
+    def upload_longwave(self, day0: int, lw):
+        """wg_upload_longwave: downward longwave [ndays, ncell] W/m2 into forcing slots day0.."""
+        a = np.ascontiguousarray(lw, np.float32)
+        assert a.ndim == 2 and a.shape[1] == self.region.ncell
+        self._check(self.lib.wg_upload_longwave(self.h, int(day0), int(a.shape[0]), a.ctypes.data), "upload_longwave")
+
+    def set_water_temp_inputs(self, gw_temp=None, river_length_check=None):
+        """wg_set_water_temp_inputs: yearly groundwater temperature [ncell] and the river
+        length as read (55 = no river), either may be None."""
+        g = None if gw_temp is None else np.ascontiguousarray(gw_temp, np.float32)
+        r = None if river_length_check is None else np.ascontiguousarray(river_length_check, np.float64)
+        self._check(self.lib.wg_set_water_temp_inputs(self.h, None if g is None else g.ctypes.data,
+                                                      None if r is None else r.ctypes.data), "set_water_temp_inputs")
+
+    def water_temp(self):
+        """(temperature [6, ncell], ice thickness [6, ncell]); rows: river, local lake,
+        local wetland, global lake, reservoir, global wetland."""
+        n = self.region.ncell
+        t, i = np.empty((6, n)), np.empty((6, n))
+        self._check(self.lib.wg_get_water_temp(self.h, t.ctypes.data, i.ctypes.data), "get_water_temp")
+        return t, i
+
+    def set_water_temp(self, temp=None, ice=None):
+        t = None if temp is None else np.ascontiguousarray(temp, np.float64)
+        i = None if ice is None else np.ascontiguousarray(ice, np.float64)
+        self._check(self.lib.wg_set_water_temp(self.h, None if t is None else t.ctypes.data,
+                                               None if i is None else i.ctypes.data), "set_water_temp")
+
+    def river_temp(self, day0: int, ndays: int) -> np.ndarray:
+        """River temperature of the stations' cells after each output day [ndays, nstation]."""
+        out = np.empty((ndays, self.stations.size))
+        self._check(self.lib.wg_get_river_temp(self.h, int(day0), int(ndays), out.ctypes.data), "get_river_temp")
+        return out
 
     def vertical_overlap(self, enable: bool | None = None) -> int:
         """Switch the vertical overlap on or off if given; return the extra warps per block (0: off)."""
