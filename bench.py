@@ -197,6 +197,44 @@ def outlet_errors(q_test, q_ref):
             "daily_err_q99": float(np.quantile(daily, 0.99)), "daily_err_max": float(daily.max())}
 
 
+def run_water_temp(region, P, T, S, stream, local):
+    """The global grid with the water temperature (wg_options.water_temp: the
+    reference's calcWTemp for the river and every water body after each cell's
+    routing) against the same run without it: two years in one wavefront, the
+    second year timed with CUDA events (the first fills the wavefront)."""
+    import torch
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    nd = 2 * DAYS_PER_STEP
+    LW, GWT = sy.water_temp_inputs(region, nd, T[:nd])
+    out = {}
+    for name, kw in (("water_temp", dict(water_temp=True)), ("without", dict()),
+                     ("without_overlap_off", dict())):
+        m = Model(region, max_days=nd, device=local, stream=stream.cuda_stream, **kw)
+        if name == "without_overlap_off":
+            m.vertical_overlap(False)
+        m.upload_forcing(0, P[:nd], T[:nd], S[:nd])
+        if kw:
+            m.set_water_temp_inputs(GWT)
+            m.upload_longwave(0, LW)
+        m.run_steps(1, 0, nd, 0, DAYS_PER_STEP)
+        m.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        m.run_steps(1, 0, nd, DAYS_PER_STEP, 2 * DAYS_PER_STEP)
+        e1.record(stream)
+        m.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[name] = {"cell_days_per_s": region.ncell * DAYS_PER_STEP / (ms / 1000.0), "ms_per_year": ms}
+        if kw:
+            t, ice = m.water_temp()
+            out[name]["river_temp_mean"] = float(np.mean(t[0]))
+            out[name]["cells_with_river_ice"] = int(np.sum(ice[0] > 0))
+        del m
+    out["cost_vs_same_shape"] = out["without_overlap_off"]["cell_days_per_s"] / out["water_temp"]["cell_days_per_s"]
+    return out
+
+
 def run_ensemble(args, region, P, T, S, stream, local, plain_value):
     """Batched ensemble: ENS_MEMBERS members of the global grid over ENS_DAYS days in
     one day-pipelined wavefront (FP32 state, FP64 confluence and balance sums),
@@ -416,6 +454,9 @@ def run_gpu(args, rank, world):
     ensemble = None
     if rank == 0 and not os.environ.get("WG_BENCH_NO_ENSEMBLE"):
         ensemble = run_ensemble(args, region, P, T, S, stream, local, value)
+    water_temp = None
+    if rank == 0 and not os.environ.get("WG_BENCH_NO_WTEMP"):
+        water_temp = run_water_temp(region, P, T, S, stream, local)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -487,6 +528,7 @@ def run_gpu(args, rank, world):
         "fp64": fp64,
         "per_day_api": per_day,
         "ensemble": ensemble,
+        "water_temp": water_temp,
         "cpu_baseline": {"value": cpu_val, "unit": "cell-days/s", "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_days} days of the same grid ({region.ncell * cpu_days} cell-days, "
                                    f"{cpu_s:.1f} s), vertical pass on {cpu_threads} OpenMP threads, routing serial"},

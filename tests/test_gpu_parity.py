@@ -20,7 +20,8 @@ from helpers import STATE_KEYS, STORAGES, max_rel_err, state_errors
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-10
-FIXTURES = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+FIXTURES = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
+                  if "wtemp" not in os.path.basename(p))   # the water-temperature cases: test_gpu_wtemp.py
 
 
 @pytest.fixture(scope="module", autouse=True)
