@@ -200,17 +200,21 @@ def outlet_errors(q_test, q_ref):
 def run_water_temp(region, P, T, S, stream, local):
     """The global grid with the water temperature (wg_options.water_temp: the
     reference's calcWTemp for the river and every water body after each cell's
-    routing) against the same run without it: two years in one wavefront, the
-    second year timed with CUDA events (the first fills the wavefront)."""
+    routing, with fractional routing) against the plain run: two years in one
+    wavefront, the second year timed with CUDA events (the first fills the
+    wavefront)."""
     import torch
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     nd = 2 * DAYS_PER_STEP
     LW, GWT = sy.water_temp_inputs(region, nd, T[:nd])
     out = {}
+    # as the reference's option parser does, the water temperature runs with
+    # fractional routing (option.cpp:591-593)
+    region_wt = region.with_options(frac_routing=1)
     for name, kw in (("water_temp", dict(water_temp=True)), ("without", dict()),
                      ("without_overlap_off", dict())):
-        m = Model(region, max_days=nd, device=local, stream=stream.cuda_stream, **kw)
+        m = Model(region_wt if kw else region, max_days=nd, device=local, stream=stream.cuda_stream, **kw)
         if name == "without_overlap_off":
             m.vertical_overlap(False)
         m.upload_forcing(0, P[:nd], T[:nd], S[:nd])

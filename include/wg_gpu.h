@@ -56,7 +56,9 @@ typedef struct wg_region {
   int32_t ncell;
   int32_t nband;            /* snow elevation bands (the reference fixes 100)        */
   int32_t river_velo_opt;   /* options.riverveloOpt                                   */
-  int32_t pad0;
+  int32_t frac_routing;     /* options.fractionalRoutingOpt (0/1): runoff from outside
+                               the water bodies' catchment goes directly to the river
+                               (routing.cpp:1895-2046, 3408-3412); aridareaOpt = 0   */
   double default_velocity;  /* routingClass::defaultRiverVelocity [km/d]              */
   const double *lct_albedo, *lct_albedo_snow, *lct_ddf;        /* [18] LCT_22.DAT    */
   const float *lct_lai_a, *lct_lai_b;                           /* [18] laiClass      */

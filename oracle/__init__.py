@@ -19,7 +19,7 @@ _lib = None
 
 _STATIC_FIELDS = [
     ("ncell", ctypes.c_int32), ("nband", ctypes.c_int32), ("river_velo_opt", ctypes.c_int32),
-    ("pad0", ctypes.c_int32), ("default_velocity", ctypes.c_double),
+    ("frac_routing", ctypes.c_int32), ("default_velocity", ctypes.c_double),
     ("lct_albedo", ctypes.c_void_p), ("lct_albedo_snow", ctypes.c_void_p), ("lct_ddf", ctypes.c_void_p),
     ("lct_lai_a", ctypes.c_void_p), ("lct_lai_b", ctypes.c_void_p), ("lct_initial_days", ctypes.c_void_p),
     ("area_km2", ctypes.c_void_p), ("lat_deg", ctypes.c_void_p), ("contfreq", ctypes.c_void_p),
@@ -106,6 +106,7 @@ class Oracle:
         st = _Static()
         st.ncell, st.nband = region.ncell, region.nband
         st.river_velo_opt, st.default_velocity = region.river_velo_opt, region.default_velocity
+        st.frac_routing = int(getattr(region, "frac_routing", 0))
         for name, ctype in _STATIC_FIELDS[5:]:
             a = region.arrays[name]
             self._keep.append(a)

@@ -151,7 +151,7 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
         _unf(f"{d}/G_INFLC.9.UNF4", ic.ravel(), np.int32)
     with open(f"{d}/meta.txt", "w") as f:
         f.write(f"{n} {P.shape[0]} {doy0} {year0} {resopt} {region.river_velo_opt} {len(stations)} {len(snapshots)} "
-                f"{0 if wtemp is None else 1}\n")
+                f"{0 if wtemp is None else 1} {int(getattr(region, 'frac_routing', 0))}\n")
     with open(f"{d}/snapshots.txt", "w") as f:
         f.write(" ".join(str(int(s)) for s in snapshots) + "\n")
 

@@ -56,12 +56,13 @@ static void write_raw(FILE *f, const double *p, size_t n) { fwrite(p, sizeof(dou
 int main(int argc, char **argv) {
   if (argc < 3) { fprintf(stderr, "usage: %s <case dir> <out file>\n", argv[0]); return 1; }
   std::string dir = argv[1];
-  int ncase, ndays, doy0, year0, resopt, velo, nstation, nsnap, wtemp = 0;
+  int ncase, ndays, doy0, year0, resopt, velo, nstation, nsnap, wtemp = 0, frac = 0;
   {
     std::ifstream m(dir + "/meta.txt");
     m >> ncase >> ndays >> doy0 >> year0 >> resopt >> velo >> nstation >> nsnap;
     if (!m) { fprintf(stderr, "harness: bad meta.txt\n"); return 2; }
     if (!(m >> wtemp)) wtemp = 0;   // optional: water temperature (options.calc_wtemp)
+    if (!(m >> frac)) frac = 0;     // optional: options.fractionalRoutingOpt
   }
   std::vector<int> snap_days(nsnap);
   {
@@ -77,12 +78,12 @@ int main(int argc, char **argv) {
   options.rout_prepare = 0; options.timeStepCheckFlag = 0; options.riverveloOpt = velo; options.time_series = 1;
   options.subtract_use = 0; options.use_alloc = 0; options.delayedUseSatisfaction = 0; options.petOpt = 0;
   options.clclOpt = 0; options.permaOpt = 0; options.resOpt = resopt; options.landCoverOpt = 0; options.use_kc = 0;
-  options.statcorrOpt = 0; options.aridareaOpt = 0; options.fractionalRoutingOpt = 0; options.riverEvapoOpt = 0;
+  options.statcorrOpt = 0; options.aridareaOpt = 0; options.fractionalRoutingOpt = frac; options.riverEvapoOpt = 0;
   options.aggrNUsGloLakResOpt = 0; options.climate_spatial_resolution = 0; options.resYearOpt = 0;
   options.resYearReference = 2000; options.resYearFirstToUse = 1900; options.resYearLastToUse = 2010;
   options.antNatOpt = 0; options.resNUsMeanYearFirst = 1971; options.resNUsMeanYearLast = 2000;
-  // calc_wtemp set directly: the option file parser would also switch on
-  // fractionalRoutingOpt (option.cpp:591-593), which this harness keeps off
+  // calc_wtemp and fractionalRoutingOpt set directly (the option file parser
+  // switches fractional routing on with calc_wtemp, option.cpp:591-593)
   options.glacierOpt = 0; options.calc_wtemp = wtemp; options.start_year = year0; options.end_year = year0;
   options.init_years = 0; options.time_step = 1; options.outLAImax = 0;
 

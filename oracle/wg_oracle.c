@@ -562,8 +562,9 @@ void wgo_wt_init(int ncell, wgo_wt_io *wt) {
 
 /* the water temperature of cell n after its routing (routing.cpp:4241-4513) */
 static void cell_water_temp(const wgo_static *s, const wgo_state *st, int n, int d, double cellArea, double cfa,
-                            const vout *vo, double localRunoff, double gw_runoff, const wt_route *r,
-                            double transportedVolume, double bw, float Tair, float SWin, wgo_wt_io *wt) {
+                            const vout *vo, double localRunoff, double gw_runoff, double into_river,
+                            double gw_into_river, const wt_route *r, double transportedVolume, double bw, float Tair,
+                            float SWin, wgo_wt_io *wt) {
   const int N = s->ncell;
   wgo_wt_in t;
   t.calc_temp_pp = 0.; t.pp_withdrawal = 0.; t.pp_consumption = 0.;
@@ -629,8 +630,8 @@ static void cell_water_temp(const wgo_static *s, const wgo_state *st, int n, int
   else if (s->lake_area[n] > 0.) t.river_inflow = r->glolake_out;
   else t.river_inflow = t.glolake_inflow;
   t.river_stor = st->river[n];
-  t.gw_runoff_into_river = 0.;   /* fractional routing is off: nothing bypasses the water bodies */
-  t.runoff_into_river = 0.;
+  t.gw_runoff_into_river = gw_into_river;   /* zero without fractional routing */
+  t.runoff_into_river = into_river;
   t.river_bottom_width = bw;
   t.river_length = s->river_length[n];
   t.river_length_check = wt->river_length_check[n];
@@ -699,7 +700,25 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         if (fabs(st->gw[n]) <= MIN_STOR_VOL) st->gw[n] = 0.;
       }
       double localRunoff;
-      if (s->ldd[n] >= 0) {
+      double into_river = 0., gw_into_river = 0., local_gw = gw_runoff;
+      if (s->frac_routing && s->ldd[n] >= 0) {
+        /* fractional routing, routing.cpp:1897-1907, 1911-1915 (arid), 2024-2033 (humid):
+         * the part of the runoff from outside the water bodies' catchment (20 times
+         * their initial area) flows directly into the river; arid cells send all
+         * their groundwater runoff there */
+        double fc = (s->loc_lake[n] / 100. + s->loc_wetl[n] / 100. + s->glo_wetl[n] / 100.) * 20.;
+        if (fc > 1.) fc = 1.;
+        into_river = (1. - fc) * dailyLocalSurfaceRunoff;
+        if (s->aindex[n] == 1) {
+          local_gw = 0.;
+          localRunoff = fc * dailyLocalSurfaceRunoff;
+          gw_into_river = gw_runoff;
+        } else {
+          gw_into_river = (1. - fc) * gw_runoff;
+          local_gw = fc * gw_runoff;
+          localRunoff = (fc * dailyLocalSurfaceRunoff) + local_gw;
+        }
+      } else if (s->ldd[n] >= 0) {
         localRunoff = dailyLocalSurfaceRunoff;
         localRunoff += gw_runoff;
       } else {
@@ -936,6 +955,10 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
       }
       /* river, routing.cpp:3385-3514 */
       double riverInflow = inflow;
+      if (s->frac_routing && s->ldd[n] >= 0) {   /* routing.cpp:3408-3412 */
+        riverInflow += into_river;
+        riverInflow += gw_into_river;
+      }
       double riverVelocity;
       if (s->river_velo_opt == 0) riverVelocity = s->default_velocity;
       else riverVelocity = river_velocity(s, st, n, riverInflow, bw[n]);
@@ -961,8 +984,8 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
       if (down >= 0) inflow_up[down] += transportedVolume;
       if (discharge) discharge[(size_t)d * N + n] = transportedVolume;
       if (wt)
-        cell_water_temp(s, st, n, d, cellArea, cfa, &vo[n], localRunoff, gw_runoff, &wr, transportedVolume, bw[n],
-                        T[n], SW[n], wt);
+        cell_water_temp(s, st, n, d, cellArea, cfa, &vo[n], localRunoff, local_gw, into_river, gw_into_river, &wr,
+                        transportedVolume, bw[n], T[n], SW[n], wt);
 
       if (balance) {
         const double fl = cellArea * (laf / 100.) / 1000000.;

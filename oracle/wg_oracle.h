@@ -12,7 +12,7 @@
  *   routingClass::getRiverVelocity / getNewRiverVelocity (source/routing.cpp:7274-7341)
  * for the option set of the hot path (time_series=1, cloud=2, petOpt=0,
  * intercept=1, use_kc=0, calc_albedo=0, clclOpt=0, subtract_use=0,
- * fractionalRoutingOpt=0, aridareaOpt=0, riverEvapoOpt=0, statcorrOpt=0,
+ * fractionalRoutingOpt 0/1, aridareaOpt=0, riverEvapoOpt=0, statcorrOpt=0,
  * use_alloc=0, glacierOpt=0, calc_wtemp 0/1, riverveloOpt 0/1/2), and
  *   calcWaterTempClass::calcWTemp         (source/calcWaterTemp.cpp:48-1324)
  * with its call in routing (source/routing.cpp:4241-4513).
@@ -46,7 +46,7 @@ typedef struct {
   int32_t ncell;
   int32_t nband;            /* snow elevation bands (reference: 100)            */
   int32_t river_velo_opt;   /* options.riverveloOpt: 0 constant, 1 inflow-, 2 storage-based */
-  int32_t pad0;
+  int32_t frac_routing;     /* options.fractionalRoutingOpt (aridareaOpt stays 0)     */
   double  default_velocity; /* routingClass::defaultRiverVelocity [km/d]       */
   /* land-cover tables, 18 entries (LCT_22.DAT, LAI_22.DAT)                    */
   const double  *lct_albedo, *lct_albedo_snow, *lct_ddf;

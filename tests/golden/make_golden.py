@@ -31,6 +31,9 @@ CASES = {
     "region64_30d": (lambda: sy.region_64x64(seed=1), 30, 1, [30]),
     "swb_velo1_200d": (lambda: sy.region_small_swb(seed=21), 200, 20, [100, 200]),
     "swb_velo2_120d": (lambda: sy.region_small_swb(seed=5, ny=16, nx=32, river_velo_opt=2), 120, 300, [120]),
+    # fractional routing (options.fractionalRoutingOpt = 1) on a block of the 0.5-degree grid
+    "swb_frac_150d": (lambda: sy.region_small_swb(seed=33, block_at=(150, 420)).with_options(frac_routing=1),
+                      150, 60, [75, 150]),
 }
 
 
@@ -73,7 +76,9 @@ def wtemp_region(seed=21):
     raw[sinks[::3]] = 55.0
     region.extras["river_length_file"] = raw
     region.arrays["river_length"] = raw * (region.contfreq / 100.)      # routing.cpp:480-482
-    return region
+    # the reference's option parser switches fractional routing on with calc_wtemp
+    # (option.cpp:591-593)
+    return region.with_options(frac_routing=1)
 
 
 # water temperature: name -> (region factory, days, first day of year, snapshot days)

@@ -254,7 +254,7 @@ struct HostConsts {
   X(t_gradnt) X(elev0) X(area) X(area_f) X(gw_e) X(gw_ik) X(gw_ome) X(sw_k) X(sw_e) X(sw_ik) X(sw_ome) X(evx)    \
   X(a6) X(ll100) X(maxs_ll) X(inv_maxs_ll) X(lw100) X(maxs_lw) X(inv_maxs_lw) X(la6) X(maxs_gl) X(inv_maxs_gl)  \
   X(ra6) X(rcap) X(inv_rcap) X(rcap01) X(inv_rcap085) X(c_ratio) X(c4) X(one_m_c4) X(prov_rel) X(gw100)         \
-  X(maxs_gw) X(inv_maxs_gw) X(bw) X(inv_mr) X(sqrt_slope) X(inv_len) X(rlen)
+  X(maxs_gw) X(inv_maxs_gw) X(bw) X(inv_mr) X(sqrt_slope) X(inv_len) X(rlen) X(fcatch)
 #define X(f) std::vector<double> f;
   WG_RFIELDS(X)
 #undef X
@@ -405,6 +405,7 @@ wg_status upload_cells(wg_ctx *ctx, const HostConsts &h, DevCellsT<R> &c, double
   c.n = ctx->n;
   c.nband = ctx->nband;
   c.velo_opt = velo_opt;
+  c.frac_routing = ctx->frac_routing;
   c.nrow = h.nrow;
   c.default_velocity = (R)default_velocity;
   c.invB = (R)(1.0 / ctx->nband);
@@ -651,6 +652,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   *out = nullptr;
   if (r->ncell <= 0 || r->nband <= 0 || r->nband > 256 || opt->max_days <= 0) return WG_ERR_INVALID;
   if (r->river_velo_opt < 0 || r->river_velo_opt > 2) return WG_ERR_UNSUPPORTED;
+  if (r->frac_routing < 0 || r->frac_routing > 1) return WG_ERR_INVALID;
   if (opt->precision < 0 || opt->precision > 1) return WG_ERR_UNSUPPORTED;
   if (opt->members < 1 || (opt->members > 1 && opt->precision != 1)) return WG_ERR_UNSUPPORTED;
   if (opt->nstation < 0 || (opt->nstation > 0 && !opt->stations)) return WG_ERR_INVALID;
@@ -680,6 +682,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   ctx->precision = opt->precision;
   ctx->threads = opt->block_threads ? opt->block_threads : (opt->members > 1 ? 64 : 256);
   ctx->days_per_step = opt->days_per_step ? opt->days_per_step : 1;
+  ctx->frac_routing = r->frac_routing;
   if (cudaSetDevice(opt->device) != cudaSuccess) return WG_ERR_DEVICE;
   if (opt->stream) {
     ctx->stream = (cudaStream_t)opt->stream;
@@ -812,6 +815,10 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     h.inv_mr[i] = 1. / (P(RIVRGH, i) * r->roughness[i]);
     h.sqrt_slope[i] = pow(r->river_slope[i], 0.5);
     h.rlen[i] = r->river_length[i];
+    {   // fractional routing: catchment of the water bodies, 20 x their initial area (routing.cpp:759, 1899-1903)
+      double fc = (r->loc_lake[i] / 100. + r->loc_wetl[i] / 100. + r->glo_wetl[i] / 100.) * 20.;
+      h.fcatch[i] = fc > 1. ? 1. : fc;
+    }
     h.inv_len[i] = 1. / r->river_length[i];
     auto it = std::find(lats.begin(), lats.end(), r->lat_deg[i]);
     if (it == lats.end()) { lats.push_back(r->lat_deg[i]); h.ext_row[i] = (int32_t)lats.size() - 1; }

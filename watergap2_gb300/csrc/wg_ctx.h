@@ -81,6 +81,7 @@ struct wg_ctx {
   std::string err;
   int chunk_steps = 0;                     // steps per (vertical-ahead, wavefront) launch pair
   int days_per_step = 1;                   // days every cell advances per wavefront step
+  int frac_routing = 0;                    // options.fractionalRoutingOpt
   DevWaterTemp wt{};                       // water temperature (wt.enabled = 0: off)
   int last_vertical_fday = 0;              // forcing slot of the last wg_step_vertical
   int va_warps_default = 0;                // vertical-balance warps the layout was sized for

@@ -41,6 +41,7 @@ struct DevCellsT {
   int32_t n;        // cells
   int32_t nband;    // snow bands
   int32_t velo_opt; // riverveloOpt
+  int32_t frac_routing;   // fractionalRoutingOpt
   int32_t nrow;     // rows of the extraterrestrial-radiation table
   R default_velocity;
   R invB;           // 1 / nband
@@ -67,6 +68,7 @@ struct DevCellsT {
   const R *ra6, *rcap, *inv_rcap, *rcap01, *inv_rcap085, *c_ratio, *c4, *one_m_c4, *prov_rel;  // reservoir
   const R *gw100, *maxs_gw, *inv_maxs_gw;         // global wetland
   const R *bw, *inv_mr, *sqrt_slope, *inv_len, *rlen;   // river
+  const R *fcatch;                                // fractional routing: share of the runoff through the water bodies
   // topology in slot space
   const int32_t *up_ptr, *up_idx;               // upstream CSR, each list in reference routing order
   const int32_t *offset;                        // pipeline step offset of the slot

@@ -340,8 +340,8 @@ __device__ __forceinline__ double cell_water_temp(const DevCellsT<R> &c, const D
   else if (t.glolake_area > 0.) t.river_inflow = (double)x.glolake_out;
   else t.river_inflow = t.glolake_inflow;
   t.river_stor = (double)river_stor;
-  t.gw_runoff_into_river = 0.;   // fractional routing is off: all runoff passes the water bodies
-  t.runoff_into_river = 0.;
+  t.gw_runoff_into_river = (double)x.gw_into_river;   // zero without fractional routing
+  t.runoff_into_river = (double)x.runoff_into_river;
   t.river_bottom_width = (double)c.bw[s];
   t.river_length = (double)c.rlen[s];
   t.river_length_check = w.len_check[s];

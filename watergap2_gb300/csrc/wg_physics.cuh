@@ -422,7 +422,8 @@ struct WTerms {
   R glolake_prev, glolake_max, glolake_evapo, glolake_out;
   R res_prev, res_evapo, res_out;
   R glowetl_prev, glowetl_evapo, glowetl_rf, glowetl_out;
-  R local_runoff, gw_runoff;
+  R local_runoff, gw_runoff;          // into the water bodies
+  R runoff_into_river, gw_into_river;   // past them (fractional routing)
 };
 
 // Routing state of one cell (surface water and groundwater storages).
@@ -479,10 +480,29 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   }
   st.gw = gw;
   R inflow = dlsr + gw_runoff;
+  R into_river = R(0), gw_into_river = R(0), local_gw = gw_runoff;
+  if (c.frac_routing && !(fl & F_SINK)) {
+    // fractional routing (routing.cpp:1897-1907, 1911-1915, 2024-2033): the runoff
+    // from outside the water bodies' catchment flows directly into the river; arid
+    // cells send all their groundwater runoff there
+    const R fc = c.fcatch[s];
+    into_river = (R(1.) - fc) * dlsr;
+    if (fl & F_ARID) {
+      local_gw = R(0);
+      inflow = fc * dlsr;
+      gw_into_river = gw_runoff;
+    } else {
+      gw_into_river = (R(1.) - fc) * gw_runoff;
+      local_gw = fc * gw_runoff;
+      inflow = (fc * dlsr) + local_gw;
+    }
+  }
   if constexpr (WT) {
     *wtm = WTerms<R>{};
     wtm->local_runoff = inflow;
-    wtm->gw_runoff = gw_runoff;
+    wtm->gw_runoff = local_gw;
+    wtm->runoff_into_river = into_river;
+    wtm->gw_into_river = gw_into_river;
   }
   const R owp = v.owp, owpet = v.owpet;
   R outflow = R(0);
@@ -683,6 +703,10 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     st.rf_glowetl = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
   }
   // river (routing.cpp:3385-3514)
+  if (c.frac_routing && !(fl & F_SINK)) {   // routing.cpp:3408-3412
+    inflow += into_river;
+    inflow += gw_into_river;
+  }
   const R S0 = st.river;
   const R velocity = (c.velo_opt == 0) ? c.default_velocity : river_velocity<R>(c, s, inflow, S0);
   rt.velocity = velocity;

@@ -43,7 +43,7 @@ class WgError(RuntimeError):
 
 class _Region(ctypes.Structure):
     _fields_ = [("ncell", ctypes.c_int32), ("nband", ctypes.c_int32), ("river_velo_opt", ctypes.c_int32),
-                ("pad0", ctypes.c_int32), ("default_velocity", ctypes.c_double)] + \
+                ("frac_routing", ctypes.c_int32), ("default_velocity", ctypes.c_double)] + \
                [(name, ctypes.c_void_p) for name, _, _ in FIELDS]
 
 
@@ -207,6 +207,7 @@ class Model:
         r = _Region()
         r.ncell, r.nband, r.river_velo_opt = region.ncell, region.nband, region.river_velo_opt
         r.default_velocity = region.default_velocity
+        r.frac_routing = int(getattr(region, "frac_routing", 0))
         for name, _, _ in FIELDS:
             a = region.arrays[name]
             self._keep.append(a)

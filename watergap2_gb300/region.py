@@ -91,6 +91,9 @@ class Region:
     arrays: Dict[str, np.ndarray]
     river_velo_opt: int = 1
     default_velocity: float = 86.4   # routingClass::routingClass, routing.cpp:119-122
+    # options.fractionalRoutingOpt: part of the local runoff bypasses the cell's
+    # water bodies and flows directly into its river (routing.cpp:1895-2046, 3408-3412)
+    frac_routing: int = 0
     # grid placement, used by the fixture writers (0.5-degree rows/cols, 1-based)
     row: np.ndarray | None = None
     col: np.ndarray | None = None
@@ -112,6 +115,14 @@ class Region:
 
     def param(self, name: str) -> np.ndarray:
         return self.arrays["param"].reshape(NPARAM, self.ncell)[PARAM[name]]
+
+    def with_options(self, **kw) -> "Region":
+        """The same region with dataclass fields replaced (e.g. frac_routing=1)."""
+        out = dataclasses.replace(self, **kw)
+        for k in ("lct_tables", "extras"):
+            if k in self.__dict__:
+                out.__dict__[k] = self.__dict__[k]
+        return out
 
     def with_param(self, name: str, values) -> "Region":
         """The same region with calibration parameter ``name`` replaced (per cell)."""
@@ -177,7 +188,7 @@ def empty_state(ncell: int, nband: int) -> Dict[str, np.ndarray]:
 def save_npz(region: Region, path: str, **extra) -> None:
     """Store a region (and optional extra arrays) in one compressed .npz file."""
     payload = {f"a_{k}": v for k, v in region.arrays.items()}
-    meta = np.array([region.ncell, region.nband, region.river_velo_opt], np.int64)
+    meta = np.array([region.ncell, region.nband, region.river_velo_opt, region.frac_routing], np.int64)
     payload.update(meta=meta, default_velocity=np.array(region.default_velocity), name=np.array(region.name))
     if region.row is not None:
         payload.update(row=region.row, col=region.col)
@@ -194,8 +205,10 @@ def load_npz(path: str):
     """Inverse of save_npz: returns (region, extra_dict)."""
     z = np.load(path, allow_pickle=False)
     arrays = {k[2:]: z[k] for k in z.files if k.startswith("a_")}
-    ncell, nband, velo = (int(x) for x in z["meta"])
-    reg = Region(ncell=ncell, nband=nband, arrays=arrays, river_velo_opt=velo,
+    meta = [int(x) for x in z["meta"]]
+    ncell, nband, velo = meta[:3]
+    frac = meta[3] if len(meta) > 3 else 0
+    reg = Region(ncell=ncell, nband=nband, arrays=arrays, river_velo_opt=velo, frac_routing=frac,
                  default_velocity=float(z["default_velocity"]), name=str(z["name"]),
                  row=z["row"] if "row" in z.files else None, col=z["col"] if "col" in z.files else None)
     reg.lct_tables = {k[2:]: z[k] for k in z.files if k.startswith("t_")}
