@@ -63,6 +63,43 @@ class Context {
     check(wg_get_discharge(ctx_, day0, ndays, out), "wg_get_discharge");
   }
 
+  // day-pipelined run in pieces: steps [t_begin, t_end) of a run of ndays days
+  int num_steps(int ndays) const { return wg_run_num_steps(ctx_, ndays); }
+  void run_steps(int doy0, int fday0, int ndays, int t_begin, int t_end) {
+    check(wg_run_steps(ctx_, doy0, fday0, ndays, t_begin, t_end), "wg_run_steps");
+  }
+  // next year's forcing on the copy stream while the current one runs
+  void upload_forcing_async(int day0, int ndays, const float *prec, const float *temp, const float *swrad) {
+    check(wg_upload_forcing_async(ctx_, day0, ndays, prec, temp, swrad), "wg_upload_forcing_async");
+  }
+  // the reference's yearly UNF climate files as read (big-endian, cell-major)
+  void upload_forcing_unf(int day0, int nd_file, int d_first, int ndays, const void *prec, const void *temp,
+                          const void *swrad, bool overlap) {
+    check(wg_upload_forcing_unf(ctx_, day0, nd_file, d_first, ndays, prec, temp, swrad, overlap ? 1 : 0),
+          "wg_upload_forcing_unf");
+  }
+  // monthly aggregates of the routing outputs (river availability, min/max, storage, ...)
+  void monthly_outputs(int nmonths, int doy_day0) {
+    check(wg_monthly_outputs(ctx_, nmonths, doy_day0), "wg_monthly_outputs");
+  }
+  void monthly(int which, int m0, int nm, double *out) {
+    check(wg_get_monthly(ctx_, which, m0, nm, out), "wg_get_monthly");
+  }
+  // water temperature (wg_options.water_temp = 1)
+  void upload_longwave(int day0, int ndays, const float *longwave) {
+    check(wg_upload_longwave(ctx_, day0, ndays, longwave), "wg_upload_longwave");
+  }
+  void set_water_temp_inputs(const float *gw_temp, const double *river_length_check) {
+    check(wg_set_water_temp_inputs(ctx_, gw_temp, river_length_check), "wg_set_water_temp_inputs");
+  }
+  void water_temp(double *temp, double *ice) { check(wg_get_water_temp(ctx_, temp, ice), "wg_get_water_temp"); }
+  void set_water_temp(const double *temp, const double *ice) {
+    check(wg_set_water_temp(ctx_, temp, ice), "wg_set_water_temp");
+  }
+  void river_temp(int day0, int ndays, double *out) {
+    check(wg_get_river_temp(ctx_, day0, ndays, out), "wg_get_river_temp");
+  }
+
   void check(wg_status s, const char *what) const {
     if (s != WG_OK)
       throw Error(s, std::string(what) + ": " + wg_status_string(s) + (ctx_ ? std::string(" ") + wg_last_error(ctx_) : ""));

@@ -20,6 +20,11 @@ int main() {
   } catch (const wg::Error &e) {
     if (e.status != WG_ERR_INVALID) return 4;
   }
+  // the entry points without a context refuse before touching a device
+  if (wg_run_steps(nullptr, 1, 0, 1, 0, 1) != WG_ERR_INVALID) return 5;
+  if (wg_upload_longwave(nullptr, 0, 1, nullptr) != WG_ERR_INVALID) return 6;
+  if (wg_get_water_temp(nullptr, nullptr, nullptr) != WG_ERR_INVALID) return 7;
+  if (wg_get_river_temp(nullptr, 0, 1, nullptr) != WG_ERR_INVALID) return 8;
   std::printf("ok\n");
   return 0;
 }
