@@ -691,10 +691,38 @@ def run_profile_ensemble(members: int = 64, days: int = 32, warm_days: int = 200
                       "steps": days, "seconds": dt, "member_cell_days_per_s": members * region.ncell * days / dt}))
 
 
+def run_profile_wtemp(days: int = 32, warm_days: int = 200):
+    """A short case for ncu of the water-temperature wavefront: the global grid
+    with fractional routing and the water temperature, FP64, a warm-up call that
+    fills the wavefront, then one call of `days` steps in one chunk (one
+    k_vertical_ahead<double,0> and one k_pipeline<double,1,0,0,1> launch):
+      ncu -k regex:k_pipeline -s 1 -c 1 python bench.py --profile-wtemp"""
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_global().with_options(frac_routing=1)
+    nd = warm_days + days
+    P, T, S = sy.forcing(region, nd, seed=2, doy0=1)
+    LW, GWT = sy.water_temp_inputs(region, nd, T)
+    m = Model(region, max_days=nd, water_temp=True)
+    m.chunk_steps(warm_days)
+    m.upload_forcing(0, P, T, S)
+    m.upload_longwave(0, LW)
+    m.set_water_temp_inputs(GWT)
+    m.run_steps(1, 0, nd, 0, warm_days)
+    m.synchronize()
+    t0 = time.perf_counter()
+    m.run_steps(1, 0, nd, warm_days, warm_days + days)
+    m.synchronize()
+    dt = time.perf_counter() - t0
+    print(json.dumps({"profile_case": "water temperature, steady-state wavefront", "ncell": region.ncell,
+                      "steps": days, "seconds": dt, "cell_days_per_s": region.ncell * days / dt}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile", action="store_true", help="run the short ncu case and exit")
     ap.add_argument("--profile-ensemble", action="store_true", help="run the short ensemble ncu case and exit")
+    ap.add_argument("--profile-wtemp", action="store_true", help="run the short water-temperature ncu case and exit")
     ap.add_argument("--fine", action="store_true",
                     help="the 5-arc-minute mixed-precision run: FP32 vs FP64 errors at every outlet")
     ap.add_argument("--calibration", action="store_true",
@@ -711,6 +739,9 @@ def main():
         return
     if args.calibration:
         run_calibration()
+        return
+    if args.profile_wtemp:
+        run_profile_wtemp()
         return
     if args.profile_ensemble:
         run_profile_ensemble()
