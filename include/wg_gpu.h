@@ -358,8 +358,19 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
 wg_status wg_graph_capture(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin, int32_t t_end);
 wg_status wg_graph_launch(wg_ctx *ctx);
 
-/* Wait for the context's stream. */
+/* Wait for the context's stream.  WG_ERR_TIMEOUT: a device-side wait (the grid
+ * barrier of the wavefront, or a step flag) ran out of its iteration limit; the
+ * kernel returned without trapping, the CUDA context stays usable, and the
+ * library refuses further results until wg_clear_error (after restoring a
+ * state: the run stopped part way). */
 wg_status wg_synchronize(wg_ctx *ctx);
+wg_status wg_clear_error(wg_ctx *ctx);
+
+/* Failure-detection test hook: with extra_arrivals > 0 every grid-barrier wait
+ * of the following wavefront launches waits for that many arrivals that never
+ * come, runs out after its iteration limit (about a second) and reports
+ * WG_ERR_TIMEOUT through wg_synchronize.  0 (the default) for normal runs. */
+wg_status wg_set_barrier_test(wg_ctx *ctx, int32_t extra_arrivals);
 
 /* Diagnostic: FP64 fused-multiply-add throughput of a device in TFLOP/s, from a
  * loop of independent DFMA chains (the FP64 ceiling of the plain FP64 path). */

@@ -1296,6 +1296,22 @@ wg_status wg_synchronize(wg_ctx *ctx) {
   return WG_OK;
 }
 
+wg_status wg_clear_error(wg_ctx *ctx) {
+  if (!ctx) return WG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaMemset(ctx->sync.error, 0, sizeof(int));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "clear_error");
+  ctx->err.clear();
+  return WG_OK;
+}
+
+wg_status wg_set_barrier_test(wg_ctx *ctx, int32_t extra_arrivals) {
+  if (!ctx || extra_arrivals < 0) return WG_ERR_INVALID;
+  ctx->sync.extra_arrivals = (uint32_t)extra_arrivals;
+  return WG_OK;
+}
+
 wg_status wg_get_discharge(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out) {
   if (!ctx || !out || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days) return WG_ERR_INVALID;
   if (ctx->nstation == 0 || ndays == 0) return WG_OK;

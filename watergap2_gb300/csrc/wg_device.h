@@ -179,6 +179,9 @@ struct DevSync {
   int *wstep;
   const int32_t *dep_ptr, *dep_idx;
   int32_t nwarps, flow;
+  // failure-detection test: arrivals the grid barrier waits for beyond the grid's
+  // blocks (0 in every run; 1 makes each wait run out, see wg_set_barrier_test)
+  uint32_t extra_arrivals;
 };
 
 }  // namespace wg

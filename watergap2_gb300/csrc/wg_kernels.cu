@@ -61,7 +61,7 @@ __device__ __forceinline__ bool grid_barrier(const DevSync &sync, unsigned round
   block_sync(nthr);
   __shared__ int s_ok;
   if (threadIdx.x == 0) {
-    const unsigned target = (round + 1u) * gridDim.x;
+    const unsigned target = (round + 1u) * gridDim.x + sync.extra_arrivals;
     __threadfence();
     atomicAdd(sync.counter, 1u);
     unsigned it = 0;

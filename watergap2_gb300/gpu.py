@@ -31,7 +31,7 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_measure_fp64_peak", "wg_run_steps", "wg_run_num_steps", "wg_get_balance_noalloc",
            "wg_set_chunk_steps", "wg_get_chunk_steps", "wg_set_vertical_overlap", "wg_get_vertical_overlap",
            "wg_math_eval", "wg_upload_longwave", "wg_set_water_temp_inputs", "wg_get_water_temp",
-           "wg_set_water_temp", "wg_get_river_temp", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
+           "wg_set_water_temp", "wg_get_river_temp", "wg_clear_error", "wg_set_barrier_test", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
            "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells",
            "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync")
@@ -130,6 +130,8 @@ def load_library(path: str = LIB_PATH):
     lib.wg_get_water_temp.argtypes = [vp, vp, vp]
     lib.wg_set_water_temp.argtypes = [vp, vp, vp]
     lib.wg_get_river_temp.argtypes = [vp, i32, i32, vp]
+    lib.wg_clear_error.argtypes = [vp]
+    lib.wg_set_barrier_test.argtypes = [vp, i32]
     lib.wg_set_vertical_overlap.argtypes = [vp, i32]
     lib.wg_get_vertical_overlap.argtypes = [vp]
     lib.wg_get_vertical_overlap.restype = i32
@@ -146,7 +148,8 @@ def load_library(path: str = LIB_PATH):
                  "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async",
                  "wg_set_active_cells", "wg_upload_forcing_unf", "wg_monthly_outputs", "wg_get_monthly",
                  "wg_set_step_sync", "wg_set_vertical_overlap", "wg_upload_longwave", "wg_set_water_temp_inputs",
-                 "wg_get_water_temp", "wg_set_water_temp", "wg_get_river_temp"):
+                 "wg_get_water_temp", "wg_set_water_temp", "wg_get_river_temp", "wg_clear_error",
+                 "wg_set_barrier_test"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -429,6 +432,14 @@ class Model:
         if steps is not None:
             self._check(self.lib.wg_set_chunk_steps(self.h, int(steps)), "set_chunk_steps")
         return int(self.lib.wg_get_chunk_steps(self.h))
+
+    def clear_error(self):
+        """wg_clear_error: accept results again after a device-side wait ran out."""
+        self._check(self.lib.wg_clear_error(self.h), "clear_error")
+
+    def barrier_test(self, extra_arrivals: int):
+        """wg_set_barrier_test: make the grid-barrier waits run out (failure-detection tests)."""
+        self._check(self.lib.wg_set_barrier_test(self.h, int(extra_arrivals)), "set_barrier_test")
 
     # ---- water temperature (water_temp=True)
     def upload_longwave(self, day0: int, lw):
