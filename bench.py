@@ -236,6 +236,17 @@ def run_water_temp(region, P, T, S, stream, local):
             out[name]["cells_with_river_ice"] = int(np.sum(ice[0] > 0))
         del m
     out["cost_vs_same_shape"] = out["without_overlap_off"]["cell_days_per_s"] / out["water_temp"]["cell_days_per_s"]
+    # the oracle port with the water temperature on the host cores (a bounded sample)
+    from oracle import Oracle
+    cpu_days = int(os.environ.get("WG_CPU_WT_SAMPLE_DAYS", "200"))
+    threads = os.cpu_count() or 1
+    o = Oracle(region_wt)
+    o.init_water_temp(GWT)
+    t0 = time.perf_counter()
+    o.run_wt(1, P[:cpu_days], T[:cpu_days], S[:cpu_days], LW[:cpu_days], nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": region.ncell * cpu_days / cpu_s, "unit": "cell-days/s", "cores": threads,
+                           "kind": "port", "sample": f"{cpu_days} days of the same grid ({cpu_s:.1f} s)"}
     return out
 
 

@@ -82,3 +82,19 @@ def test_water_temperature_per_day_api_and_streaming():
     tr, ir = ref.water_temp()
     assert np.array_equal(ta, tr) and np.array_equal(ia, ir)          # chunking changes no bit
     assert np.array_equal(a.river_temp(0, nd), ref.river_temp(0, nd))
+
+
+def test_water_temperature_days_per_step():
+    """Several days per wavefront step carry the river temperature through the
+    same slots as the discharge: the same bits as one day per step."""
+    region, ex = _case()
+    nd, doy0 = ex["P"].shape[0], int(ex["doy0"])
+    a = _model(region, ex)
+    a.run_days(doy0, 0, nd)
+    b = _model(region, ex, days_per_step=3)
+    b.run_days(doy0, 0, nd)
+    ta, ia = a.water_temp()
+    tb, ib = b.water_temp()
+    assert np.array_equal(ta, tb) and np.array_equal(ia, ib)
+    assert np.array_equal(a.river_temp(0, nd), b.river_temp(0, nd))
+    assert np.array_equal(a.discharge(0, nd), b.discharge(0, nd))
