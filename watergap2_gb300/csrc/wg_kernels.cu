@@ -15,9 +15,14 @@
 //                  that k_vertical_ahead filled; the monthly output aggregates are
 //                  accumulated in its epilogue.  With ENS the cells carry
 //                  `members` independent states (ensemble members), innermost in
-//                  memory.
+//                  memory.  With VAW (one FP64 member) each block has five more
+//                  warps that run k_vertical_ahead's work for the next chunk
+//                  while the routing warps wait; with WT every cell also gets
+//                  its water temperature (calcWTemp), the river temperature
+//                  travelling downstream beside the outflow.
 //  k_vertical_ahead  the vertical balance of the cells without a water body for
 //                  a chunk of days, state in registers, into the ring.
+//  k_math_eval     the FP64 path's exp/log/pow/reciprocal on arrays (tests).
 //  k_unf_forcing / k_gather_forcing  forcing uploads into the slot layout.
 //  k_volume / k_balance_sum   compensated (Neumaier) FP64 water-balance sums.
 //
