@@ -439,114 +439,114 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
         // the step's kd days of this cell, in order; the upstream cells routed the
         // same days one step earlier (their offset is one less)
         for (int kk = 0; kk < kd && dbase + kk < ndays; ++kk) {
-        const int d = dbase + kk;
-        double *q_now = q_now0 + (size_t)kk * N;
-        const double *q_prev = q_prev0 + (size_t)kk * N;
-        const int doy = (doy0 - 1 + d) % 365 + 1;
-        const int month = month_of(doy);
-        const uint32_t fl = c.flags[s];
-        VOut<R> o;
-        const R laf = resident ? laf_keep : st.laf[si];
-        const R laf_prev = resident ? lafp_keep : st.laf_prev[si];
-        if (FUSED && !(fl & F_VINLINE)) {
-          const size_t ri = (size_t)(d % ring.ring_days) * N + si;
-          o.rs = ring.rs[ri];
-          o.gwr = ring.gwr[ri];
-          o.transfer = R(0); o.owp = R(0); o.owpet = R(0);
-          o.land_in = R(0); o.land_evap = R(0); o.land_leak = R(0);   // accounted ahead
-          if constexpr (WT) {
-            o.owp = ring.owp[ri];
-            o.owpet = ring.owpet[ri];
-          }
-        } else if (FUSED) {
-          const size_t fo = (size_t)(fday0 + d) * n + s;
-          R Pin = R(f.prec[fo]);
-          R gam = c.gamma[s];
-          if (ENS) {
-            Pin *= R(mem.prec_factor[mm]);
-            gam *= R(mem.gamma_factor[mm]);
-          }
-          const int started = resident ? started_keep : st.laf_started[si];
-          vertical_at<R>(c, st, N, s, si, doy, Pin, gam, f.temp[fo], f.swrad[fo], laf,
-                         started == 1 ? laf_prev : laf, o);   // daily.cpp:159-169
-        } else {
-          o.rs = v.rs[s]; o.gwr = v.gwr[s]; o.transfer = v.transfer[s]; o.owp = v.owp[s]; o.owpet = v.owpet[s];
-          o.land_in = v.land_in[s]; o.land_evap = v.land_evap[s]; o.land_leak = v.land_leak[s];
-        }
-        // upstream inflow, summed in FP64 in the reference's push order (routing.cpp:3955-3958)
-        double up = 0., e_up = 0.;
-        const int u0 = c.up_ptr[s], u1 = c.up_ptr[s + 1];
-        for (int k = u0; k < u1; ++k) {
-          const size_t ui = (size_t)c.up_idx[k] * M + mm;
-          const double qu = __ldcg(q_prev + ui);
-          up += qu;
-          if constexpr (WT)   // the energy the inflow carries (calcWaterTemp.cpp:76-83)
-            e_up += qu * WT_RHO_W * WT_HEAT_CAP_W * (__ldcg(t_prev0 + (size_t)kk * N + ui) + WT_CONV_K);
-        }
-        RState<R> rs = resident ? rs_keep : load_rstate(st, si, fl);
-        RTerms<R> rt;
-        WTerms<R> wtm;
-        const R tv = routing_cell<R, WT>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtm);
-        if (resident) rs_keep = rs;
-        else store_rstate(st, si, rs, fl);
-        q_now[si] = (double)tv;
-        if constexpr (WT) {
-          const size_t fo = (size_t)(fday0 + d) * n + s;
-          const double tr = cell_water_temp<R>(c, wtp, f, s, si, N, fo, fl, o, wtm, rs.river, up, e_up);
-          t_now0[(size_t)kk * N + si] = tr;
-          const int stw = c.station[s];
-          if (stw >= 0) wtp.qst_t[(size_t)(oday0 + d) * c.nstation + stw] = tr;
-        }
-        if (b.enabled) {
-          const double land_f = (double)c.area_f[s] * (double)laf;
-          if (!FUSED || (fl & F_VINLINE))
-            record_balance(b, N, si, (double)o.land_in * land_f + (double)rt.p_ow,
-                           (double)o.land_evap * land_f + (double)rt.e_ow, up, (double)tv,
-                           (double)o.land_leak * land_f + (double)rt.leak);
-          else   // vertical ran ahead: its land terms are in arrays 0, 1 and 10
-            record_routing_balance(b, N, si, up, (double)tv, (double)rt.leak);
-        }
-        // land-area fraction for the next day (routing.cpp:5034-5188, 5343-5352)
-        R next = laf;
-        if (fl & (F_LOCLAKE | F_LOCWETL | F_GLOWETL)) {
-          R fswb = resident ? fswb_keep : st.fswb_next[si];
-          next = fraction_next<R>(fl, rs, c.ll100[s], c.lw100[s], c.gw100[s], laf, fswb);
-          if (resident) {
-            fswb_keep = fswb;
-            laf_keep = next;
+          const int d = dbase + kk;
+          double *q_now = q_now0 + (size_t)kk * N;
+          const double *q_prev = q_prev0 + (size_t)kk * N;
+          const int doy = (doy0 - 1 + d) % 365 + 1;
+          const int month = month_of(doy);
+          const uint32_t fl = c.flags[s];
+          VOut<R> o;
+          const R laf = resident ? laf_keep : st.laf[si];
+          const R laf_prev = resident ? lafp_keep : st.laf_prev[si];
+          if (FUSED && !(fl & F_VINLINE)) {
+            const size_t ri = (size_t)(d % ring.ring_days) * N + si;
+            o.rs = ring.rs[ri];
+            o.gwr = ring.gwr[ri];
+            o.transfer = R(0); o.owp = R(0); o.owpet = R(0);
+            o.land_in = R(0); o.land_evap = R(0); o.land_leak = R(0);   // accounted ahead
+            if constexpr (WT) {
+              o.owp = ring.owp[ri];
+              o.owpet = ring.owpet[ri];
+            }
+          } else if (FUSED) {
+            const size_t fo = (size_t)(fday0 + d) * n + s;
+            R Pin = R(f.prec[fo]);
+            R gam = c.gamma[s];
+            if (ENS) {
+              Pin *= R(mem.prec_factor[mm]);
+              gam *= R(mem.gamma_factor[mm]);
+            }
+            const int started = resident ? started_keep : st.laf_started[si];
+            vertical_at<R>(c, st, N, s, si, doy, Pin, gam, f.temp[fo], f.swrad[fo], laf,
+                           started == 1 ? laf_prev : laf, o);   // daily.cpp:159-169
           } else {
-            st.fswb_next[si] = fswb;
-            st.laf[si] = next;
+            o.rs = v.rs[s]; o.gwr = v.gwr[s]; o.transfer = v.transfer[s]; o.owp = v.owp[s]; o.owpet = v.owpet[s];
+            o.land_in = v.land_in[s]; o.land_evap = v.land_evap[s]; o.land_leak = v.land_leak[s];
           }
-        }
-        if (resident) {
-          lafp_keep = laf;
-          started_keep = 1;
-        } else {
-          st.laf_prev[si] = laf;
-          st.laf_started[si] = 1;
-        }
-        const int stn = c.station[s];
-        if (stn >= 0) qst[((size_t)(oday0 + d) * c.nstation + stn) * M + mm] = (double)tv;
-        if (mon.enabled) {
-          // monthly epilogue: this thread owns the cell, so no atomics
-          const int od = oday0 + d;
-          const int yd = mon.doy_day0 - 1 + od;
-          const int mi = (yd / 365) * 12 + month_of(yd % 365 + 1) - mon.month0;
-          if (mi >= 0 && mi < mon.nmonths) {
-            const size_t k = (size_t)mi * N + si;
-            const double q = (double)tv;
-            mon.river_avail[k] += q;
-            mon.min_avail[k] = fmin(mon.min_avail[k], q);
-            mon.max_avail[k] = fmax(mon.max_avail[k], q);
-            mon.storage[k] += (double)rs.gw + (double)rs.river + (double)rs.loclake + (double)rs.locwetl +
-                              (double)rs.glolake + (double)rs.glowetl + (double)rs.res;
-            // CellRunoff (routing.cpp:3933-3939): in inland sinks the transported
-            // volume leaves the cell as evaporation
-            mon.cell_runoff[k] += ((fl & F_SINK) ? 0. : q) - up;
-            mon.velocity[k] += (double)rt.velocity / 86.4;   // km/d -> m/s
+          // upstream inflow, summed in FP64 in the reference's push order (routing.cpp:3955-3958)
+          double up = 0., e_up = 0.;
+          const int u0 = c.up_ptr[s], u1 = c.up_ptr[s + 1];
+          for (int k = u0; k < u1; ++k) {
+            const size_t ui = (size_t)c.up_idx[k] * M + mm;
+            const double qu = __ldcg(q_prev + ui);
+            up += qu;
+            if constexpr (WT)   // the energy the inflow carries (calcWaterTemp.cpp:76-83)
+              e_up += qu * WT_RHO_W * WT_HEAT_CAP_W * (__ldcg(t_prev0 + (size_t)kk * N + ui) + WT_CONV_K);
           }
-        }
+          RState<R> rs = resident ? rs_keep : load_rstate(st, si, fl);
+          RTerms<R> rt;
+          WTerms<R> wtm;
+          const R tv = routing_cell<R, WT>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtm);
+          if (resident) rs_keep = rs;
+          else store_rstate(st, si, rs, fl);
+          q_now[si] = (double)tv;
+          if constexpr (WT) {
+            const size_t fo = (size_t)(fday0 + d) * n + s;
+            const double tr = cell_water_temp<R>(c, wtp, f, s, si, N, fo, fl, o, wtm, rs.river, up, e_up);
+            t_now0[(size_t)kk * N + si] = tr;
+            const int stw = c.station[s];
+            if (stw >= 0) wtp.qst_t[(size_t)(oday0 + d) * c.nstation + stw] = tr;
+          }
+          if (b.enabled) {
+            const double land_f = (double)c.area_f[s] * (double)laf;
+            if (!FUSED || (fl & F_VINLINE))
+              record_balance(b, N, si, (double)o.land_in * land_f + (double)rt.p_ow,
+                             (double)o.land_evap * land_f + (double)rt.e_ow, up, (double)tv,
+                             (double)o.land_leak * land_f + (double)rt.leak);
+            else   // vertical ran ahead: its land terms are in arrays 0, 1 and 10
+              record_routing_balance(b, N, si, up, (double)tv, (double)rt.leak);
+          }
+          // land-area fraction for the next day (routing.cpp:5034-5188, 5343-5352)
+          R next = laf;
+          if (fl & (F_LOCLAKE | F_LOCWETL | F_GLOWETL)) {
+            R fswb = resident ? fswb_keep : st.fswb_next[si];
+            next = fraction_next<R>(fl, rs, c.ll100[s], c.lw100[s], c.gw100[s], laf, fswb);
+            if (resident) {
+              fswb_keep = fswb;
+              laf_keep = next;
+            } else {
+              st.fswb_next[si] = fswb;
+              st.laf[si] = next;
+            }
+          }
+          if (resident) {
+            lafp_keep = laf;
+            started_keep = 1;
+          } else {
+            st.laf_prev[si] = laf;
+            st.laf_started[si] = 1;
+          }
+          const int stn = c.station[s];
+          if (stn >= 0) qst[((size_t)(oday0 + d) * c.nstation + stn) * M + mm] = (double)tv;
+          if (mon.enabled) {
+            // monthly epilogue: this thread owns the cell, so no atomics
+            const int od = oday0 + d;
+            const int yd = mon.doy_day0 - 1 + od;
+            const int mi = (yd / 365) * 12 + month_of(yd % 365 + 1) - mon.month0;
+            if (mi >= 0 && mi < mon.nmonths) {
+              const size_t k = (size_t)mi * N + si;
+              const double q = (double)tv;
+              mon.river_avail[k] += q;
+              mon.min_avail[k] = fmin(mon.min_avail[k], q);
+              mon.max_avail[k] = fmax(mon.max_avail[k], q);
+              mon.storage[k] += (double)rs.gw + (double)rs.river + (double)rs.loclake + (double)rs.locwetl +
+                                (double)rs.glolake + (double)rs.glowetl + (double)rs.res;
+              // CellRunoff (routing.cpp:3933-3939): in inland sinks the transported
+              // volume leaves the cell as evaporation
+              mon.cell_runoff[k] += ((fl & F_SINK) ? 0. : q) - up;
+              mon.velocity[k] += (double)rt.velocity / 86.4;   // km/d -> m/s
+            }
+          }
         }   // days of the step
       }
     }
