@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
             const double qu = __ldcg(q_prev + ui);
             up += qu;
             if constexpr (WT)   // the energy the inflow carries (calcWaterTemp.cpp:76-83)
-              e_up += qu * WT_RHO_W * WT_HEAT_CAP_W * (__ldcg(t_prev0 + (size_t)kk * N + ui) + WT_CONV_K);
+              e_up += qu * WT_RC * (__ldcg(t_prev0 + (size_t)kk * N + ui) + WT_CONV_K);
           }
           RState<R> rs = resident ? rs_keep : load_rstate(st, si, fl);
           RTerms<R> rt;

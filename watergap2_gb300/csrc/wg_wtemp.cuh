@@ -2,10 +2,14 @@
 // reference's calcWaterTempClass::calcWTemp (source/calcWaterTemp.cpp:48-1324),
 // the energy balance of Beek et al. (2012) with the thermocline depth of
 // Wanders et al. (2019), for the river and the five kinds of surface water
-// body, with ice cover.  FP64, in the reference's expression order (pow(T, 4)
-// as two squarings and the thermocline's pow from fm::pow are the only changes
-// of rounding); the caller assembles the inputs from routing_cell's terms
-// (routing.cpp:4241-4356) and keeps the state (temperatures, ice thickness).
+// body, with ice cover.  FP64, branch for branch as the reference; the
+// arithmetic folds the constant factors (rho c, the ice growth per W/m2),
+// multiplies by 1e-6 and by one refined reciprocal of the volume's heat
+// capacity instead of dividing, takes pow(T, 4) as two squarings and the
+// thermocline's pow from fm::pow -- a few ulp of rounding against the oracle,
+// which keeps the reference's expression order.  The caller assembles the
+// inputs from routing_cell's terms (routing.cpp:4241-4356) and keeps the state
+// (temperatures, ice thickness).
 #pragma once
 #include "wg_fastmath.cuh"
 
@@ -49,6 +53,10 @@ __device__ __forceinline__ double pow4(double x) { const double x2 = x * x; retu
 #define WT_ALBEDO_W 0.08
 #define WT_ALBEDO_I 0.6
 #define WT_NO_TEMP (-9999.)
+// folded constants of the device version (the oracle keeps the reference's
+// separate factors): rho c [J/(km3 K)], and the day's ice growth per W/m2
+#define WT_RC (WT_RHO_W * WT_HEAT_CAP_W)
+#define WT_ICE_PER_FLUX (86400. / 1000. / (WT_LAMBDA_F * WT_RHO_W / 1.e9))
 
 
 /* temperature of precipitation and surface runoff [K] */
@@ -57,7 +65,7 @@ __device__ __forceinline__ double rain_k(const WtIn &t) { return wt_max(t.air_te
 /* growth of the ice cover over one day [km] (same expression in every water body;
  * the river passes its storage where the others pass their temperature) */
 __device__ __forceinline__ double ice_growth(double prev, const WtIn &t, double net_rad_ice) {
-  return ((-(WT_K_H_ICE * prev) + (WT_K_H * (-t.air_temp)) - net_rad_ice) / (WT_LAMBDA_F * WT_RHO_W / 1.e9) * 86400.) / 1000.;
+  return (-(WT_K_H_ICE * prev) + (WT_K_H * (-t.air_temp)) - net_rad_ice) * WT_ICE_PER_FLUX;
 }
 
 /* the clamps every water body ends with (calcWaterTemp.cpp:400-411 and the others) */
@@ -72,13 +80,14 @@ __device__ __forceinline__ void finish(const WtIn &t, double *temp, double *ice,
  * bring the temperature to the air temperature (calcWaterTemp.cpp:376-395) */
 __device__ __forceinline__ double open_water_temp(const WtIn &t, double energy, double sens, double vol) {
   if (!(vol > 0.)) return WT_NO_TEMP;
-  double temp = (energy / (vol * WT_RHO_W * WT_HEAT_CAP_W)) - WT_CONV_K;
+  const double inv = fm::rcp_pos(vol * WT_RC);   // vol > 0
+  double temp = energy * inv - WT_CONV_K;
   energy -= sens;
   if (temp >= t.air_temp) {
-    temp = (energy / (vol * WT_RHO_W * WT_HEAT_CAP_W)) - WT_CONV_K;
+    temp = energy * inv - WT_CONV_K;
     if (temp < t.air_temp) temp = t.air_temp;
   } else {
-    temp = (energy / (vol * WT_RHO_W * WT_HEAT_CAP_W)) - WT_CONV_K;
+    temp = energy * inv - WT_CONV_K;
     if (temp > t.air_temp) temp = t.air_temp;
   }
   return temp;
@@ -88,7 +97,7 @@ __device__ __forceinline__ double open_water_temp(const WtIn &t, double energy, 
  * with the day's inflows of temperature in_k [K] and volume in_vol */
 __device__ __forceinline__ double under_ice_temp(double energy_stor, double sens, double vol, double ice, double area, double in_vol,
                              int has_inflow, double in_k) {
-  double temp = (energy_stor - sens) / (vol * WT_RHO_W * WT_HEAT_CAP_W) - WT_CONV_K;
+  double temp = (energy_stor - sens) / (vol * WT_RC) - WT_CONV_K;
   if (temp < 0.) temp = 0.;
   if (has_inflow) {
     if ((vol - ice * area) > 0.)
@@ -107,13 +116,13 @@ __device__ __forceinline__ void loclake_temp(const WtIn &t, double nr_ice, doubl
   double temp = 0.;
   int ice_max = 0;
   const double area = t.cell_area * (t.loclake_area / 100.) * t.loclake_rf;
-  const double precip = t.ow_prec / 1000000. * area;
+  const double precip = t.ow_prec * 1.e-6 * area;
   double surf = t.local_runoff - t.local_gw_runoff;
   if (!(t.has_outflow != 0.) && t.river_length_check == 55.) {
     surf += t.runoff_into_river - t.gw_runoff_into_river;
     gw += t.gw_runoff_into_river;
   }
-  const double e_stor = t.loclake_stor_prev * WT_RHO_W * WT_HEAT_CAP_W * (t.loclake_temp_prev + WT_CONV_K);
+  const double e_stor = t.loclake_stor_prev * WT_RC * (t.loclake_temp_prev + WT_CONV_K);
   if (t.air_temp <= 0. || ice > 0.) {
     ice += ice_growth(t.loclake_temp_prev, t, nr_ice);
     if (ice * area >= t.loclake_stor_prev) {
@@ -132,14 +141,14 @@ __device__ __forceinline__ void loclake_temp(const WtIn &t, double nr_ice, doubl
       temp = under_ice_temp(e_stor, sens, t.loclake_stor_prev, ice, area, precip + surf + t.local_gw_runoff,
                             in_vol > 0., in_k);
     } else {
-      const double e_surf = surf * WT_RHO_W * WT_HEAT_CAP_W * rain_k(t);
-      const double e_prec = precip * WT_RHO_W * WT_HEAT_CAP_W * rain_k(t);
-      const double e_gw = gw * WT_RHO_W * WT_HEAT_CAP_W * (t.gw_temp + WT_CONV_K);
+      const double e_surf = surf * WT_RC * rain_k(t);
+      const double e_prec = precip * WT_RC * rain_k(t);
+      const double e_gw = gw * WT_RC * (t.gw_temp + WT_CONV_K);
       const double e_rad = nr_water * 1.e6 * 86400. * area;
       const double sens = WT_K_H * (t.loclake_temp_prev - t.air_temp) * 1.e6 * 86400. * area;
-      const double lat = lat_heat * WT_RHO_W * (t.loclake_evapo / 1000000. * area);
+      const double lat = lat_heat * WT_RHO_W * (t.loclake_evapo * 1.e-6 * area);
       const double energy = e_stor + e_rad - lat + e_prec + e_surf + e_gw;
-      const double vol = t.loclake_stor_prev + precip + surf + t.local_gw_runoff - (t.loclake_evapo / 1000000. * area);
+      const double vol = t.loclake_stor_prev + precip + surf + t.local_gw_runoff - (t.loclake_evapo * 1.e-6 * area);
       temp = open_water_temp(t, energy, sens, vol);
     }
   } else {
@@ -159,9 +168,9 @@ __device__ __forceinline__ void take_runoff(const WtIn &t, double *surf, double 
     *gw += t.gw_runoff_into_river;
   }
   *surf += t.local_runoff - t.local_gw_runoff;
-  *e_surf = *surf * WT_RHO_W * WT_HEAT_CAP_W * rain_k(t);
+  *e_surf = *surf * WT_RC * rain_k(t);
   *gw += t.local_gw_runoff;
-  *e_gw = *gw * WT_RHO_W * WT_HEAT_CAP_W * (t.gw_temp + WT_CONV_K);
+  *e_gw = *gw * WT_RC * (t.gw_temp + WT_CONV_K);
 }
 
 /* local wetland, calcWaterTemp.cpp:420-568 */
@@ -172,8 +181,8 @@ __device__ __forceinline__ void locwetl_temp(const WtIn &t, double nr_ice, doubl
   double temp = 0.;
   int ice_max = 0;
   const double area = t.cell_area * (t.locwetl_area / 100.) * t.locwetl_rf;
-  const double precip = t.ow_prec / 1000000. * area;
-  const double e_stor = t.locwetl_stor_prev * WT_RHO_W * WT_HEAT_CAP_W * (t.locwetl_temp_prev + WT_CONV_K);
+  const double precip = t.ow_prec * 1.e-6 * area;
+  const double e_stor = t.locwetl_stor_prev * WT_RC * (t.locwetl_temp_prev + WT_CONV_K);
   if (!gw_used) {
     take_runoff(t, &surf, &gw, &e_surf, &e_gw);
     sum_runoff = gw + surf;
@@ -197,14 +206,14 @@ __device__ __forceinline__ void locwetl_temp(const WtIn &t, double nr_ice, doubl
       temp = under_ice_temp(e_stor, sens, t.locwetl_stor_prev, ice, area, precip + sum_runoff + t.locwetl_inflow,
                             in_vol > 0., in_k);
     } else {
-      const double e_prec = precip * WT_RHO_W * WT_HEAT_CAP_W * rain_k(t);
+      const double e_prec = precip * WT_RC * rain_k(t);
       const double e_rad = nr_water * 1.e6 * 86400. * area;
       const double sens = WT_K_H * ((t.locwetl_temp_prev + WT_CONV_K) - (t.air_temp + WT_CONV_K)) * 1.e6 * 86400. * area;
-      const double lat = lat_heat * WT_RHO_W * (t.locwetl_evapo / 1000000. * area);
+      const double lat = lat_heat * WT_RHO_W * (t.locwetl_evapo * 1.e-6 * area);
       double e_in = 0.;
-      if (t.loclake_area > 0.) e_in = t.locwetl_inflow * WT_RHO_W * WT_HEAT_CAP_W * (loclake_temp + WT_CONV_K);
+      if (t.loclake_area > 0.) e_in = t.locwetl_inflow * WT_RC * (loclake_temp + WT_CONV_K);
       const double energy = e_stor + e_rad - lat + e_prec + e_in + e_surf + e_gw;
-      double vol = t.locwetl_stor_prev + precip - (t.locwetl_evapo / 1000000. * area) + t.locwetl_inflow;
+      double vol = t.locwetl_stor_prev + precip - (t.locwetl_evapo * 1.e-6 * area) + t.locwetl_inflow;
       if (!gw_used) vol += surf + gw;
       temp = open_water_temp(t, energy, sens, vol);
     }
@@ -246,8 +255,8 @@ __device__ __forceinline__ void lake_temp(const WtIn &t, int type, double nr_ice
   double ice = t.ice[type];
   double temp = 0.;
   int ice_max = 0;
-  const double precip = t.ow_prec / 1000000. * area;
-  const double e_stor = stor_prev * WT_RHO_W * WT_HEAT_CAP_W * (temp_prev + WT_CONV_K);
+  const double precip = t.ow_prec * 1.e-6 * area;
+  const double e_stor = stor_prev * WT_RC * (temp_prev + WT_CONV_K);
   if (!gw_used) {
     take_runoff(t, &surf, &gw, &e_surf, &e_gw);
     sum_runoff = surf + gw;
@@ -273,14 +282,14 @@ __device__ __forceinline__ void lake_temp(const WtIn &t, int type, double nr_ice
       }
       temp = under_ice_temp(e_stor, sens, stor_prev, ice, area, precip + sum_runoff + inflow, in_vol > 0., in_k);
     } else {
-      const double e_prec = precip * WT_RHO_W * WT_HEAT_CAP_W * rain_k(t);
+      const double e_prec = precip * WT_RC * rain_k(t);
       const double e_rad = nr_water * 1.e6 * 86400. * area;
       const double sens = WT_K_H * ((temp_prev + WT_CONV_K) - (t.air_temp + WT_CONV_K)) * 1.e6 * 86400. * area;
-      const double lat = lat_heat * WT_RHO_W * (evapo / 1000000. * area);
+      const double lat = lat_heat * WT_RHO_W * (evapo * 1.e-6 * area);
       double e_in = 0.;
-      if (mix_temp >= 0.) e_in = ((mix_temp + WT_CONV_K) * inflow * WT_RHO_W * WT_HEAT_CAP_W);
+      if (mix_temp >= 0.) e_in = ((mix_temp + WT_CONV_K) * inflow * WT_RC);
       const double energy = e_stor + e_rad - lat + e_prec + e_in + e_surf + e_gw;
-      double vol = stor_prev + precip - (evapo / 1000000. * area) + inflow;
+      double vol = stor_prev + precip - (evapo * 1.e-6 * area) + inflow;
       if (!gw_used) vol += surf + gw;
       temp = open_water_temp(t, energy, sens, vol);
     }
@@ -306,8 +315,8 @@ __device__ __forceinline__ void river_temp(const WtIn &t, double nr_ice, double 
             sqrt(t.river_bottom_width / 1000. * t.river_bottom_width / (16. * 1000.) + 0.5 * csa);
     area = t.river_stor / depth;
   }
-  const double e_stor = t.river_stor * WT_RHO_W * WT_HEAT_CAP_W * (t.own_temp_prev + WT_CONV_K);
-  const double precip = t.ow_prec * area / 1000000.;
+  const double e_stor = t.river_stor * WT_RC * (t.own_temp_prev + WT_CONV_K);
+  const double precip = t.ow_prec * area * 1.e-6;
   double surf = t.runoff_into_river - t.gw_runoff_into_river;
   if (!gw_used) {
     surf += (t.local_runoff - t.local_gw_runoff);
@@ -340,20 +349,20 @@ __device__ __forceinline__ void river_temp(const WtIn &t, double nr_ice, double 
       }
       temp = under_ice_temp(e_stor, sens, vol, ice, area, precip + surf + gw + t.river_inflow, in_vol > 0., in_k);
     } else {
-      const double e_surf = surf * WT_RHO_W * WT_HEAT_CAP_W * rain_k(t);
-      const double e_gw = gw * WT_RHO_W * WT_HEAT_CAP_W * (t.gw_temp + WT_CONV_K);
-      const double evapo = ((1.0 - t.cfa) * t.ow_prec + (t.cfa * t.ow_pet)) * area / 1000000.;
+      const double e_surf = surf * WT_RC * rain_k(t);
+      const double e_gw = gw * WT_RC * (t.gw_temp + WT_CONV_K);
+      const double evapo = ((1.0 - t.cfa) * t.ow_prec + (t.cfa * t.ow_pet)) * area * 1.e-6;
       if (evapo >= t.river_stor + t.river_inflow + precip + surf + gw) {
         *temp_out = WT_NO_TEMP;   /* everything evaporates; the ice record is reset */
         *ice_out = 0.;
         return;
       }
-      const double e_prec = precip * WT_RHO_W * WT_HEAT_CAP_W * rain_k(t);
+      const double e_prec = precip * WT_RC * rain_k(t);
       const double e_rad = nr_water * 1.e6 * 86400. * area;
       const double sens = WT_K_H * ((t.own_temp_prev + WT_CONV_K) - (t.air_temp + WT_CONV_K)) * 1.e6 * 86400. * area;
       const double lat = lat_heat * WT_RHO_W * evapo;
       double e_in = 0.;
-      if (mix_temp >= 0.) e_in = t.river_inflow * WT_RHO_W * WT_HEAT_CAP_W * (mix_temp + WT_CONV_K);
+      if (mix_temp >= 0.) e_in = t.river_inflow * WT_RC * (mix_temp + WT_CONV_K);
       const double energy = e_stor + e_rad - lat + e_in + e_prec + e_surf + e_gw;
       vol = t.river_stor + t.river_inflow + precip + surf + gw - evapo;
       temp = open_water_temp(t, energy, sens, vol);
@@ -405,7 +414,7 @@ __device__ __forceinline__ void water_temp_cell(const WtIn &t, double out[12]) {
   double tmp, ice;
   tot_in = t.inflow_sum;
   e_in = t.inflow_energy;
-  if (tot_in > 0.) in_temp = e_in / (tot_in * WT_RHO_W * WT_HEAT_CAP_W) - WT_CONV_K;
+  if (tot_in > 0.) in_temp = e_in / (tot_in * WT_RC) - WT_CONV_K;
   const double lat_heat = t.air_temp > 0. ? (2.501 - 0.002361 * t.air_temp) * 1.e6 : 0.;
   const double net_long = t.long_rad - 1. * 0.00000005670374419 * pow4(t.air_temp + WT_CONV_K);
   const double nr_water = (t.short_rad * (1. - WT_ALBEDO_W) + net_long);
