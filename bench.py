@@ -213,7 +213,7 @@ def run_water_temp(region, P, T, S, stream, local):
     # fractional routing (option.cpp:591-593)
     region_wt = region.with_options(frac_routing=1)
     for name, kw in (("water_temp", dict(water_temp=True)), ("without", dict()),
-                     ("without_overlap_off", dict())):
+                     ("without_overlap_off", dict())):   # the vertical overlap is on in the first two
         m = Model(region_wt if kw else region, max_days=nd, device=local, stream=stream.cuda_stream, **kw)
         if name == "without_overlap_off":
             m.vertical_overlap(False)

@@ -696,7 +696,6 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   std::vector<uint32_t> cls(n);
   for (int i = 0; i < n; ++i) cls[i] = work_class(r, i);
   if (!opt->block_threads && ctx->members == 1) ctx->layout = default_layout(ctx.get());
-  if (opt->water_temp) ctx->layout.va_warps = 0;   // its wavefront kernel carries no vertical-balance warps
   ctx->va_warps_default = ctx->layout.va_warps;
   wg_status st = build_topology(n, r->downstream, r->rout_order, cls.data(), &ctx->layout, ctx->topo);
   if (st != WG_OK) return st;

@@ -739,7 +739,7 @@ template <class R>
 static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false) {
   if (ens) return wt ? nullptr : (const void *)k_pipeline<R, true, true, false, false>;
   if constexpr (std::is_same<R, double>::value) {   // FP64 single member only
-    if (wt) return vaw ? nullptr
+    if (wt) return vaw ? (fused ? (const void *)k_pipeline<R, true, false, true, true> : nullptr)
                        : (fused ? (const void *)k_pipeline<R, true, false, false, true>
                                 : (const void *)k_pipeline<R, false, false, false, true>);
     if (vaw) return (const void *)k_pipeline<R, true, false, true, false>;
