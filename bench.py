@@ -235,7 +235,7 @@ def run_water_temp(region, P, T, S, stream, local):
             out[name]["river_temp_mean"] = float(np.mean(t[0]))
             out[name]["cells_with_river_ice"] = int(np.sum(ice[0] > 0))
         del m
-    out["cost_vs_same_shape"] = out["without_overlap_off"]["cell_days_per_s"] / out["water_temp"]["cell_days_per_s"]
+    out["cost_vs_plain"] = out["without"]["cell_days_per_s"] / out["water_temp"]["cell_days_per_s"]
     # the oracle port with the water temperature on the host cores (a bounded sample)
     from oracle import Oracle
     cpu_days = int(os.environ.get("WG_CPU_WT_SAMPLE_DAYS", "200"))
