@@ -317,6 +317,7 @@ def fp64_peak_tflops():
 
 def run_gpu(args, rank, world):
     import torch
+    from watergap2_gb300 import replicas
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
 
@@ -374,12 +375,9 @@ def run_gpu(args, rank, world):
     launch_ms = [a.elapsed_time(b) for a, b in per_step]
     model.run_steps(1, 0, ndays, nyears * DAYS_PER_STEP, total_steps)   # drain (untimed)
     model.synchronize()
-    if dist:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = replicas.job_seconds(elapsed_ms / 1000.0, dist, device="cuda") * 1000.0   # max over ranks
     cell_days = region.ncell * DAYS_PER_STEP * args.steps
-    value = cell_days * world / (elapsed_ms / 1000.0)
+    value = replicas.whole_job_value(cell_days, world, elapsed_ms / 1000.0)
     lag = model.num_levels - 1
     q_dev = model.discharge(0, ndays)
 
@@ -434,11 +432,8 @@ def run_gpu(args, rank, world):
     e2e_s = time.perf_counter() - t0
     e2e_model.run_steps(1, 0, ndays, nyears * DAYS_PER_STEP, total_steps)
     same = bool(np.array_equal(e2e_model.discharge(0, ndays), q_dev))
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = cell_days * world / e2e_s
+    e2e_s = replicas.job_seconds(e2e_s, dist, device="cuda")
+    e2e_value = replicas.whole_job_value(cell_days, world, e2e_s)
     h2d = 3 * DAYS_PER_STEP * region.ncell * 4
     d2h = DAYS_PER_STEP * nst * 8
     num_levels = e2e_model.num_levels
