@@ -35,6 +35,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-days/s on 1 GB300 (plain FP64 vs batched FP32 ensemble) at stated error"
 DAYS_PER_STEP = 365
+# days every cell advances per wavefront step (wg_options.days_per_step): the
+# step barrier and the start-of-step load latency are paid once per 5 days; a
+# timed step (one year) is 73 wavefront steps.  Results are the same bits.
+WAVEFRONT_DAYS = 5
+WSTEPS_PER_YEAR = DAYS_PER_STEP // WAVEFRONT_DAYS
 # algorithmic HBM bytes per cell-day of a day-by-day FP64 implementation with the
 # water bodies of this workload: vertical 224 + routing 96 + water bodies ~4
 BYTES_PER_CELL_DAY = 324.0
@@ -173,7 +178,7 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": "global 0.5-degree grid, 67,420 cells, lakes/wetlands/reservoirs, FP64",
-                   "days_per_step": DAYS_PER_STEP, "ncell": region.ncell},
+                   "days_per_timed_step": DAYS_PER_STEP, "ncell": region.ncell},
         "cpu_baseline": {"value": value, "unit": "cell-days/s", "cores": threads, "kind": "port",
                          "sample": f"{sample_days} days x {region.ncell} cells per step, vertical pass on "
                                    f"{threads} OpenMP threads, routing serial as in the reference"},
@@ -200,13 +205,13 @@ def outlet_errors(q_test, q_ref):
 def run_water_temp(region, P, T, S, stream, local):
     """The global grid with the water temperature (wg_options.water_temp: the
     reference's calcWTemp for the river and every water body after each cell's
-    routing, with fractional routing) against the plain run: two years in one
-    wavefront, the second year timed with CUDA events (the first fills the
-    wavefront)."""
+    routing, with fractional routing) against the plain run: four years in one
+    wavefront, the fourth timed with CUDA events (the first three fill the
+    wavefront: 219 steps of 5 days for its 198 levels)."""
     import torch
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
-    nd = 2 * DAYS_PER_STEP
+    nd = 4 * DAYS_PER_STEP
     LW, GWT = sy.water_temp_inputs(region, nd, T[:nd])
     out = {}
     # as the reference's option parser does, the water temperature runs with
@@ -214,18 +219,20 @@ def run_water_temp(region, P, T, S, stream, local):
     region_wt = region.with_options(frac_routing=1)
     for name, kw in (("water_temp", dict(water_temp=True)), ("without", dict()),
                      ("without_overlap_off", dict())):   # the vertical overlap is on in the first two
-        m = Model(region_wt if kw else region, max_days=nd, device=local, stream=stream.cuda_stream, **kw)
+        m = Model(region_wt if kw else region, max_days=nd, device=local, stream=stream.cuda_stream,
+                  days_per_step=WAVEFRONT_DAYS, **kw)
         if name == "without_overlap_off":
             m.vertical_overlap(False)
         m.upload_forcing(0, P[:nd], T[:nd], S[:nd])
         if kw:
             m.set_water_temp_inputs(GWT)
             m.upload_longwave(0, LW)
-        m.run_steps(1, 0, nd, 0, DAYS_PER_STEP)
+        assert 3 * WSTEPS_PER_YEAR >= m.num_levels - 1
+        m.run_steps(1, 0, nd, 0, 3 * WSTEPS_PER_YEAR)
         m.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        m.run_steps(1, 0, nd, DAYS_PER_STEP, 2 * DAYS_PER_STEP)
+        m.run_steps(1, 0, nd, 3 * WSTEPS_PER_YEAR, 4 * WSTEPS_PER_YEAR)
         e1.record(stream)
         m.synchronize()
         ms = e0.elapsed_time(e1)
@@ -266,7 +273,7 @@ def run_ensemble(args, region, P, T, S, stream, local, plain_value):
     gf = np.array([np.random.default_rng((8, m)).uniform(0.7, 1.3) for m in range(M)], np.float32)
     pf[0] = gf[0] = 1.0
     ens = Model(region, max_days=nd, device=local, stream=stream.cuda_stream, precision="fp32", members=M,
-                prec_factor=pf, gamma_factor=gf)
+                prec_factor=pf, gamma_factor=gf, days_per_step=WAVEFRONT_DAYS)
     ens.upload_forcing(0, P, T, S)
     total = ens.num_steps(nd)
     lag = ens.num_levels - 1
@@ -332,7 +339,8 @@ def run_gpu(args, rank, world):
     nyears = args.warmup + args.steps
     P, T, S = args.forcing
     stream = torch.cuda.Stream(device=local)
-    model = Model(region, max_days=nyears * DAYS_PER_STEP, device=local, stream=stream.cuda_stream)
+    model = Model(region, max_days=nyears * DAYS_PER_STEP, device=local, stream=stream.cuda_stream,
+                  days_per_step=WAVEFRONT_DAYS)
     nst = model.stations.size
 
     # ---- value: device-resident forcing.  The whole nyears-year run is one
@@ -342,8 +350,8 @@ def run_gpu(args, rank, world):
     model.upload_forcing(0, P, T, S)
     model.synchronize()
     total_steps = model.num_steps(ndays)
-    assert args.warmup * DAYS_PER_STEP >= model.num_levels - 1, "warm-up must fill the wavefront"
-    model.run_steps(1, 0, ndays, 0, args.warmup * DAYS_PER_STEP)
+    assert args.warmup * WSTEPS_PER_YEAR >= model.num_levels - 1, "warm-up must fill the wavefront"
+    model.run_steps(1, 0, ndays, 0, args.warmup * WSTEPS_PER_YEAR)
     model.synchronize()
     launches0 = model.launch_count
     model.kernel_timing(True)
@@ -355,10 +363,10 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
         ev0.record(stream)
         for k in range(args.steps):
-            t0 = (args.warmup + k) * DAYS_PER_STEP
+            t0 = (args.warmup + k) * WSTEPS_PER_YEAR
             e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e_a.record(stream)
-            model.run_steps(1, 0, ndays, t0, t0 + DAYS_PER_STEP)
+            model.run_steps(1, 0, ndays, t0, t0 + WSTEPS_PER_YEAR)
             e_b.record(stream)
             per_step.append((e_a, e_b))
         ev1.record(stream)
@@ -373,19 +381,20 @@ def run_gpu(args, rank, world):
     chunk_steps, overlap_warps = model.chunk_steps(), model.vertical_overlap()
     elapsed_ms = ev0.elapsed_time(ev1)
     launch_ms = [a.elapsed_time(b) for a, b in per_step]
-    model.run_steps(1, 0, ndays, nyears * DAYS_PER_STEP, total_steps)   # drain (untimed)
+    model.run_steps(1, 0, ndays, nyears * WSTEPS_PER_YEAR, total_steps)   # drain (untimed)
     model.synchronize()
     elapsed_ms = replicas.job_seconds(elapsed_ms / 1000.0, dist, device="cuda") * 1000.0   # max over ranks
     cell_days = region.ncell * DAYS_PER_STEP * args.steps
     value = replicas.whole_job_value(cell_days, world, elapsed_ms / 1000.0)
-    lag = model.num_levels - 1
+    lag = (model.num_levels - 1) * WAVEFRONT_DAYS   # days a cell trails the first cells
     q_dev = model.discharge(0, ndays)
 
     # ---- e2e: the same run through the C ABI with host buffers: every step copies
     # that year's forcing from pinned host memory and reads back the outlet
     # discharge of the 365 days the step completed
     del model
-    e2e_model = Model(region, max_days=ndays + DAYS_PER_STEP, device=local, stream=stream.cuda_stream)
+    e2e_model = Model(region, max_days=ndays + DAYS_PER_STEP, device=local, stream=stream.cuda_stream,
+                      days_per_step=WAVEFRONT_DAYS)
     pin = [torch.empty((ndays, region.ncell), dtype=torch.float32, pin_memory=True) for _ in range(3)]
     for t_, a in zip(pin, (P, T, S)):
         t_.numpy()[:] = a
@@ -409,7 +418,7 @@ def run_gpu(args, rank, world):
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)] if record else None
         if record:
             ev[0].record(stream)
-        e2e_model.run_steps(1, 0, ndays, k * DAYS_PER_STEP, (k + 1) * DAYS_PER_STEP)
+        e2e_model.run_steps(1, 0, ndays, k * WSTEPS_PER_YEAR, (k + 1) * WSTEPS_PER_YEAR)
         if record:
             ev[1].record(stream)
         upload(k + 1, overlap=True)
@@ -430,7 +439,7 @@ def run_gpu(args, rank, world):
         e2e_step(args.warmup + k, record=True)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    e2e_model.run_steps(1, 0, ndays, nyears * DAYS_PER_STEP, total_steps)
+    e2e_model.run_steps(1, 0, ndays, nyears * WSTEPS_PER_YEAR, total_steps)
     same = bool(np.array_equal(e2e_model.discharge(0, ndays), q_dev))
     e2e_s = replicas.job_seconds(e2e_s, dist, device="cuda")
     e2e_value = replicas.whole_job_value(cell_days, world, e2e_s)
@@ -483,14 +492,14 @@ def run_gpu(args, rank, world):
     pipe_ms = pipe_ms_total / n_wave
     nplain = region.ncell * (1.0 - vinline_frac)
     route_cd = region.ncell * DAYS_PER_STEP * args.steps                 # routing cell-days
-    va_days = chunk_steps if overlap_warps else DAYS_PER_STEP
+    va_days = chunk_steps * WAVEFRONT_DAYS if overlap_warps else DAYS_PER_STEP
     va_alone_cd = nplain * va_days * args.steps                         # k_vertical_ahead
     va_wave_cd = nplain * (DAYS_PER_STEP - va_days) * args.steps        # extra warps of k_pipeline
     wave_bytes = WAVEFRONT_BYTES_PER_CELL_DAY * route_cd + VERTICAL_BYTES_PER_CELL_DAY * va_wave_cd
     achieved = wave_bytes / (pipe_ms_total / 1000.0) / 1e9
     figs = profile_figures()
     traffic = None
-    if overlap_warps and chunk_steps == figs.get("chunk_steps"):
+    if overlap_warps and chunk_steps == figs.get("chunk_steps") and WAVEFRONT_DAYS == figs.get("days_per_step"):
         traffic = figs.get("traffic_bytes_per_launch k_pipeline")       # a launch of the same shape
     fp64 = None
     try:
@@ -516,7 +525,8 @@ def run_gpu(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators)",
         "config": {"workload": "global 0.5-degree grid, 67,420 cells, lakes/wetlands/reservoirs, FP64, "
                                "1 step = 365 days of every cell (10 steps = the 10-year run)",
-                   "ncell": region.ncell, "days_per_step": DAYS_PER_STEP, "levels": num_levels,
+                   "ncell": region.ncell, "days_per_timed_step": DAYS_PER_STEP,
+                   "days_per_wavefront_step": WAVEFRONT_DAYS, "levels": num_levels,
                    "stations": int(nst), "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (295 MB of forcing read per step)"},
         "gpu_launches": int(gpu_launches),
@@ -549,32 +559,34 @@ def run_gpu(args, rank, world):
         dist.destroy_process_group()
 
 
-def run_profile_case(days: int = 120, warm_days: int = 200):
-    """A short, self-contained case for ncu: the global grid, a warm-up call that
-    fills the day-pipelined wavefront (warm_days steps), then one call of `days`
-    steady-state steps (forcing and state exceed L2).  With the default 16-step
-    chunks and the vertical overlap, the warm-up call is launches 0-13 of
-    k_vertical_ahead|k_pipeline (one vertical-ahead launch, 13 wavefront
-    launches) and the second call starts with its vertical-ahead launch (14) and
-    wavefront launches that carry the next chunk's vertical balance (15, 16, ...):
-      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 14 -c 3 python bench.py --profile"""
+def run_profile_case(steps: int = 24, warm_steps: int = 200):
+    """A short, self-contained case for ncu: the global grid as the bench runs it
+    (WAVEFRONT_DAYS days per wavefront step, default chunks of 4 steps, vertical
+    overlap), a warm-up call of warm_steps steps that fills the day-pipelined
+    wavefront, then one call of `steps` steady-state steps (forcing and state
+    exceed L2).  The warm-up call is launches 0-50 of k_vertical_ahead|k_pipeline
+    (one vertical-ahead launch, 50 wavefront launches); the second call starts
+    with its vertical-ahead launch (51) and wavefront launches that carry the
+    next chunk's vertical balance (52, 53, ...):
+      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 51 -c 3 python bench.py --profile"""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global()
-    nd = warm_days + days
+    nd = (warm_steps + steps) * WAVEFRONT_DAYS
     P, T, S = sy.forcing(region, nd, seed=2, doy0=1)
-    m = Model(region, max_days=nd)
+    m = Model(region, max_days=nd, days_per_step=WAVEFRONT_DAYS)
     m.upload_forcing(0, P, T, S)
-    m.run_steps(1, 0, nd, 0, warm_days)
+    m.run_steps(1, 0, nd, 0, warm_steps)
     m.synchronize()
     t0 = time.perf_counter()
-    m.run_steps(1, 0, nd, warm_days, warm_days + days)
+    m.run_steps(1, 0, nd, warm_steps, warm_steps + steps)
     m.synchronize()
     dt = time.perf_counter() - t0
-    m.run_steps(1, 0, nd, warm_days + days, m.num_steps(nd))
+    m.run_steps(1, 0, nd, warm_steps + steps, m.num_steps(nd))
     m.synchronize()
-    print(json.dumps({"profile_case": "global grid, steady-state wavefront", "ncell": region.ncell, "steps": days,
-                      "seconds": dt, "cell_days_per_s": region.ncell * days / dt, "chunk_steps": m.chunk_steps(),
+    print(json.dumps({"profile_case": "global grid, steady-state wavefront", "ncell": region.ncell, "steps": steps,
+                      "days_per_step": WAVEFRONT_DAYS, "seconds": dt,
+                      "cell_days_per_s": region.ncell * steps * WAVEFRONT_DAYS / dt, "chunk_steps": m.chunk_steps(),
                       "vertical_overlap_warps": m.vertical_overlap(), "vinline_fraction": m.vinline_fraction()}))
 
 

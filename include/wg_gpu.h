@@ -317,7 +317,8 @@ wg_status wg_get_kernel_times(wg_ctx *ctx, double *vertical_ahead_ms, double *wa
 
 /* Wavefront steps per launch of wg_run_steps: 1 .. the ring capacity in steps
  * (wg_options.ring_days / days_per_step; half of it with the vertical overlap
- * below); 0 = the default: the ring capacity, or 16 steps with the overlap.
+ * below); 0 = the default: the ring capacity, or ceil(16 / days_per_step)
+ * steps with the overlap.
  * No counterpart in the reference (it has no day pipelining). */
 wg_status wg_set_chunk_steps(wg_ctx *ctx, int32_t steps);
 int32_t wg_get_chunk_steps(const wg_ctx *ctx);

@@ -128,11 +128,12 @@ struct wg_ctx {
   bool overlap() const { return layout.va_warps > 0 && layout.idle_warp >= 0 && threads == layout.threads; }
   // longest chunk: with the overlap the ring holds this chunk's and the next one's days
   int chunk_cap() const { return overlap() ? max_chunk() / 2 : max_chunk(); }
-  // steps per launch: the set chunk length if it fits, else 16 with the overlap
-  // (the first chunk of each call runs its vertical balance alone) or the ring
+  // steps per launch: the set chunk length if it fits, else about 16 days with
+  // the overlap (the first chunk of each call runs its vertical balance alone)
+  // or the ring
   int eff_chunk() const {
     if (chunk_steps > 0 && chunk_steps <= chunk_cap()) return chunk_steps;
-    return overlap() ? std::min(16, chunk_cap()) : chunk_cap();
+    return overlap() ? std::min((16 + days_per_step - 1) / days_per_step, chunk_cap()) : chunk_cap();
   }
   // wavefront steps of a run of ndays days
   int total_steps(int ndays) const { return (ndays + days_per_step - 1) / days_per_step + topo.nlevel - 1; }
