@@ -682,31 +682,34 @@ def run_calibration():
     print(json.dumps(line), flush=True)
 
 
-def run_profile_ensemble(members: int = 64, days: int = 32, warm_days: int = 200):
+def run_profile_ensemble(members: int = 64, steps: int = 12, warm_steps: int = 200):
     """A short case for ncu of the ensemble kernels: 64 members of the global grid
-    (a warp is 32 members of one cell, as with 256), 64 threads per block and
-    32-step chunks (the autotuner's choice on GB300), a 32-day ring so that the
-    case holds ~2.5 GB on the device; a warm-up call that fills the wavefront,
-    then one call of `days` steps (one k_vertical_ahead<float,1> and one
-    k_pipeline<float,1,1> launch):
-      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 2 -c 2 python bench.py --profile-ensemble"""
+    (a warp is 32 members of one cell, as with 256), as the bench runs them:
+    five days per wavefront step, 128 threads per block and 12-step chunks (the
+    autotuner's choice on GB300), a 60-day ring so that the case holds ~2.5 GB
+    on the device; a warm-up call of warm_steps steps (17 launch pairs) that
+    fills the wavefront, then one call of `steps` steps (one
+    k_vertical_ahead<float,1> and one k_pipeline<float,1,1> launch):
+      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 34 -c 2 python bench.py --profile-ensemble"""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global()
-    nd = warm_days + days
+    nd = (warm_steps + steps) * WAVEFRONT_DAYS
     P, T, S = sy.forcing(region, nd, seed=2, doy0=1)
     pf = np.array([np.exp(np.random.default_rng((7, m)).normal(0.0, 0.3)) for m in range(members)], np.float32)
-    m = Model(region, max_days=nd, precision="fp32", members=members, prec_factor=pf, block_threads=64, ring_days=32)
-    m.chunk_steps(32)
+    m = Model(region, max_days=nd, precision="fp32", members=members, prec_factor=pf, block_threads=128,
+              ring_days=60, days_per_step=WAVEFRONT_DAYS)
+    m.chunk_steps(steps)
     m.upload_forcing(0, P, T, S)
-    m.run_steps(1, 0, nd, 0, warm_days)
+    m.run_steps(1, 0, nd, 0, warm_steps)
     m.synchronize()
     t0 = time.perf_counter()
-    m.run_steps(1, 0, nd, warm_days, warm_days + days)
+    m.run_steps(1, 0, nd, warm_steps, warm_steps + steps)
     m.synchronize()
     dt = time.perf_counter() - t0
     print(json.dumps({"profile_case": "ensemble, steady-state wavefront", "members": members, "ncell": region.ncell,
-                      "steps": days, "seconds": dt, "member_cell_days_per_s": members * region.ncell * days / dt}))
+                      "steps": steps, "days_per_step": WAVEFRONT_DAYS, "seconds": dt,
+                      "member_cell_days_per_s": members * region.ncell * steps * WAVEFRONT_DAYS / dt}))
 
 
 def run_profile_wtemp(days: int = 32, warm_days: int = 200):
