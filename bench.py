@@ -712,31 +712,35 @@ def run_profile_ensemble(members: int = 64, steps: int = 12, warm_steps: int = 2
                       "member_cell_days_per_s": members * region.ncell * steps * WAVEFRONT_DAYS / dt}))
 
 
-def run_profile_wtemp(days: int = 32, warm_days: int = 200):
-    """A short case for ncu of the water-temperature wavefront: the global grid
-    with fractional routing and the water temperature, FP64, a warm-up call that
-    fills the wavefront, then one call of `days` steps in one chunk (one
-    k_vertical_ahead<double,0> and one k_pipeline<double,1,0,0,1> launch):
-      ncu -k regex:k_pipeline -s 1 -c 1 python bench.py --profile-wtemp"""
+def run_profile_wtemp(steps: int = 24, warm_steps: int = 200):
+    """A short case for ncu of the water-temperature wavefront, as the bench
+    runs it: the global grid with fractional routing and the water temperature,
+    FP64, WAVEFRONT_DAYS days per wavefront step, default chunks of 4 steps,
+    vertical overlap.  A warm-up call of warm_steps steps fills the wavefront
+    (launches 0-50 of k_vertical_ahead|k_pipeline); the second call starts with
+    its vertical-ahead launch (51) and wavefront launches that carry the next
+    chunk's vertical balance (52, 53, ...):
+      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 51 -c 3 python bench.py --profile-wtemp"""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global().with_options(frac_routing=1)
-    nd = warm_days + days
+    nd = (warm_steps + steps) * WAVEFRONT_DAYS
     P, T, S = sy.forcing(region, nd, seed=2, doy0=1)
     LW, GWT = sy.water_temp_inputs(region, nd, T)
-    m = Model(region, max_days=nd, water_temp=True)
-    m.chunk_steps(warm_days)
+    m = Model(region, max_days=nd, water_temp=True, days_per_step=WAVEFRONT_DAYS)
     m.upload_forcing(0, P, T, S)
     m.upload_longwave(0, LW)
     m.set_water_temp_inputs(GWT)
-    m.run_steps(1, 0, nd, 0, warm_days)
+    m.run_steps(1, 0, nd, 0, warm_steps)
     m.synchronize()
     t0 = time.perf_counter()
-    m.run_steps(1, 0, nd, warm_days, warm_days + days)
+    m.run_steps(1, 0, nd, warm_steps, warm_steps + steps)
     m.synchronize()
     dt = time.perf_counter() - t0
     print(json.dumps({"profile_case": "water temperature, steady-state wavefront", "ncell": region.ncell,
-                      "steps": days, "seconds": dt, "cell_days_per_s": region.ncell * days / dt}))
+                      "steps": steps, "days_per_step": WAVEFRONT_DAYS, "seconds": dt,
+                      "cell_days_per_s": region.ncell * steps * WAVEFRONT_DAYS / dt, "chunk_steps": m.chunk_steps(),
+                      "vertical_overlap_warps": m.vertical_overlap()}))
 
 
 def main():
