@@ -55,6 +55,22 @@ class _WtIO(ctypes.Structure):
                                                "temp", "ice", "river_avail", "daily_temp")]
 
 
+class _WuIO(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_void_p) for f in ("nus", "nug", "wdr", "cons", "row_of_day", "frgi", "state",
+                                               "daily_actual")]
+
+
+WU_NSTATE = 12
+_DAYS_IN_MONTH = np.array([31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31], np.float64)
+
+
+def daily_use(m3_per_month) -> np.ndarray:
+    """dailyNUInit's conversion (routing.cpp:966-975): m3 per month [..., 12, ncell]
+    -> km3 per day, the multipliers M_NETABSSW/M_NETABSGW being 1."""
+    v = np.asarray(m3_per_month, np.float64)
+    return v / (1000000000. * _DAYS_IN_MONTH[:, None])
+
+
 def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -77,6 +93,9 @@ def lib():
         _lib.wgo_run_wt.argtypes = [ctypes.POINTER(_Static), ctypes.POINTER(_State), ctypes.c_int, ctypes.c_int,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_WtIO)]
+        _lib.wgo_run_wu.argtypes = [ctypes.POINTER(_Static), ctypes.POINTER(_State), ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_WuIO)]
     return _lib
 
 
@@ -160,6 +179,39 @@ class Oracle:
         if rc:
             raise RuntimeError(f"wgo_run_wt failed: {rc}")
         return q, dt
+
+    def init_water_use(self, frac_return_gw_irrig):
+        """Switch on water use: its state starts at zero (routing.cpp:790-848);
+        frac_return_gw_irrig [ncell] is G_fractreturngw_irrig."""
+        self.wu = np.zeros((WU_NSTATE, self.region.ncell))
+        self._wu_frgi = np.ascontiguousarray(frac_return_gw_irrig, np.float64)
+
+    def run_wu(self, doy0, P, T, S, use, discharge=False, balance=False, daily_actual=False, nthreads=1):
+        """run() with water use.  use = (nus, nug, irrigation withdrawal, irrigation
+        consumptive use), each [years, 12, ncell] m3 per month; the first day is in
+        year 0 and every day of year 1 of the day-of-year count starts the next
+        year, as the reference's driver reads the yearly files.  Returns
+        (discharge, balance, daily actual use [ndays, ncell] km3)."""
+        from watergap2_gb300.region import use_rows
+        P, T, S = (np.ascontiguousarray(x, np.float32) for x in (P, T, S))
+        nd, n = P.shape[0], self.region.ncell
+        tabs = [np.ascontiguousarray(daily_use(u).reshape(-1, n)) for u in use]
+        rows = np.ascontiguousarray(use_rows(doy0, nd), np.int32)
+        if rows.max() >= tabs[0].shape[0]:
+            raise ValueError("water use covers fewer years than the run")
+        q = np.zeros((nd, n)) if discharge else None
+        b = np.zeros((nd, 6)) if balance else None
+        da = np.zeros((nd, n)) if daily_actual else None
+        io = _WuIO()
+        io.nus, io.nug, io.wdr, io.cons = (_ptr(t) for t in tabs)
+        io.row_of_day, io.frgi, io.state = _ptr(rows), _ptr(self._wu_frgi), _ptr(self.wu)
+        io.daily_actual = _ptr(da) if da is not None else None
+        rc = lib().wgo_run_wu(ctypes.byref(self._static), ctypes.byref(self._cstate), int(doy0), nd,
+                              _ptr(P), _ptr(T), _ptr(S), _ptr(q) if q is not None else None,
+                              _ptr(b) if b is not None else None, int(nthreads), ctypes.byref(io))
+        if rc:
+            raise RuntimeError(f"wgo_run_wu failed: {rc}")
+        return q, b, da
 
     def run(self, doy0, P, T, S, discharge=False, balance=False, nthreads=1):
         P, T, S = (np.ascontiguousarray(x, np.float32) for x in (P, T, S))

@@ -50,11 +50,14 @@ def _full(values, dtype, fill=0):
     return out
 
 
+WU_FIELDS = ["wu_remaining", "wu_unsat_irrig", "wu_unsat_other", "wu_reduced_return", "wu_irrig_withdrawal",
+             "wu_irrig_consumptive", "wu_total_unsat", "wu_unsat_prev", "wu_unsat_irrig_prev", "wu_unsat_other_prev",
+             "wu_reduced_return_prev", "wu_actual"]
 WT_FIELDS = ["wt_river", "wt_loclake", "wt_locwetl", "wt_glolake", "wt_res", "wt_glowetl",
              "ice_river", "ice_loclake", "ice_locwetl", "ice_glolake", "ice_res", "ice_glowetl", "river_avail"]
 
 
-def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000, wtemp=None):
+def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000, wtemp=None, wuse=None):
     n = region.ncell
     if n > NG:
         raise ValueError("region larger than the reference grid")
@@ -123,6 +126,10 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
         full = np.ones(NG)
         full[:n] = par[k]
         obj[key] = [float(x) for x in full]
+    # multipliers of the net abstractions (routing.cpp:910-916), which getValue
+    # reads as 0 when absent
+    obj["net_abstraction_surfacewater_mult"] = [1.0] * NG
+    obj["net_abstraction_groundwater_mult"] = [1.0] * NG
     with open(f"{d}/params.json", "w") as f:
         json.dump(obj, f)
     with open(f"{d}/config.txt", "w") as f:
@@ -149,14 +156,27 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
         ic = np.zeros((NG, 9), np.int32)
         ic[:n] = inflow_cells(region) + 1           # 1-based, 0 = none
         _unf(f"{d}/G_INFLC.9.UNF4", ic.ravel(), np.int32)
+    if wuse is not None:
+        # (nus, nug, irrigation withdrawal, irrigation consumptive use: [years, 12, ncell] m3 per month,
+        #  fraction of irrigation return flow into groundwater [ncell]); the yearly files dailyNUInit
+        #  reads (routing.cpp:892-907), cell-major [cell][month]
+        nus, nug, wdr, cons, frgi = wuse
+        _unf(f"{d}/G_FRACTRETURNGW_IRRIG.UNF0", _full(np.asarray(frgi), np.float32), np.float32)
+        _unf(f"{d}/GLWDunits.UNF4", np.zeros(NG, np.int32), np.int32)
+        for k in range(np.asarray(nus).shape[0]):
+            for name, arr in (("G_NETUSE_SW_m3", nus), ("G_NETUSE_GW_m3", nug),
+                              ("G_IRRIG_WITHDRAWAL_USE_SW_m3", wdr), ("G_IRRIG_CONS_USE_SW_m3", cons)):
+                full = np.zeros((NG, 12), np.float32)
+                full[:n] = np.asarray(arr[k], np.float32).T
+                _unf(f"{d}/{name}_{year0 + k}.12.UNF0", full.ravel(), np.float32)
     with open(f"{d}/meta.txt", "w") as f:
         f.write(f"{n} {P.shape[0]} {doy0} {year0} {resopt} {region.river_velo_opt} {len(stations)} {len(snapshots)} "
-                f"{0 if wtemp is None else 1} {int(getattr(region, 'frac_routing', 0))}\n")
+                f"{0 if wtemp is None else 1} {int(getattr(region, 'frac_routing', 0))} {0 if wuse is None else 1}\n")
     with open(f"{d}/snapshots.txt", "w") as f:
         f.write(" ".join(str(int(s)) for s in snapshots) + "\n")
 
 
-def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wtemp=None):
+def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wtemp=None, wuse=None):
     """Run the reference harness; returns dict(lai_a, lai_b, bottom_width, snapshots=[{field: array}],
     discharge=[ndays, nstation], stations=...)."""
     if not available():
@@ -169,7 +189,7 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
     stations = np.asarray(stations, np.int32)
     snapshots = list(snapshots or [ndays])
     tmp = workdir or tempfile.mkdtemp(prefix="wg_ref_")
-    write_case(region, tmp, P, T, S, doy0, stations, snapshots, wtemp=wtemp)
+    write_case(region, tmp, P, T, S, doy0, stations, snapshots, wtemp=wtemp, wuse=wuse)
     out = os.path.join(tmp, "out.bin")
     subprocess.run([HARNESS, tmp, out], check=True, stdout=subprocess.DEVNULL)
     raw = np.fromfile(out, np.float64)
@@ -187,6 +207,9 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
         snap["snow_band"] = bands
         if wtemp is not None:
             for f in WT_FIELDS:
+                snap[f] = raw[o:o + n].copy(); o += n
+        if wuse is not None:
+            for f in WU_FIELDS:
                 snap[f] = raw[o:o + n].copy(); o += n
         snaps.append(snap)
     res["snapshots"] = snaps

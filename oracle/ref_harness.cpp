@@ -56,13 +56,14 @@ static void write_raw(FILE *f, const double *p, size_t n) { fwrite(p, sizeof(dou
 int main(int argc, char **argv) {
   if (argc < 3) { fprintf(stderr, "usage: %s <case dir> <out file>\n", argv[0]); return 1; }
   std::string dir = argv[1];
-  int ncase, ndays, doy0, year0, resopt, velo, nstation, nsnap, wtemp = 0, frac = 0;
+  int ncase, ndays, doy0, year0, resopt, velo, nstation, nsnap, wtemp = 0, frac = 0, wuse = 0;
   {
     std::ifstream m(dir + "/meta.txt");
     m >> ncase >> ndays >> doy0 >> year0 >> resopt >> velo >> nstation >> nsnap;
     if (!m) { fprintf(stderr, "harness: bad meta.txt\n"); return 2; }
     if (!(m >> wtemp)) wtemp = 0;   // optional: water temperature (options.calc_wtemp)
     if (!(m >> frac)) frac = 0;     // optional: options.fractionalRoutingOpt
+    if (!(m >> wuse)) wuse = 0;     // optional: water use (options.subtract_use = 2)
   }
   std::vector<int> snap_days(nsnap);
   {
@@ -84,6 +85,9 @@ int main(int argc, char **argv) {
   options.antNatOpt = 0; options.resNUsMeanYearFirst = 1971; options.resNUsMeanYearLast = 2000;
   // calc_wtemp and fractionalRoutingOpt set directly (the option file parser
   // switches fractional routing on with calc_wtemp, option.cpp:591-593)
+  // water use: net abstractions from the yearly G_NETUSE_*_m3 files, satisfied in
+  // the cell itself (use_alloc, delayedUseSatisfaction and aggrNUsGloLakResOpt off)
+  if (wuse) options.subtract_use = 2;
   options.glacierOpt = 0; options.calc_wtemp = wtemp; options.start_year = year0; options.end_year = year0;
   options.init_years = 0; options.time_step = 1; options.outLAImax = 0;
 
@@ -185,6 +189,8 @@ int main(int argc, char **argv) {
     if (!year_started || doy == 1) {
       dailyWaterBalance.annualInit();
       routing.annualInit(year, 1, additionalOutIn);
+      // the year's net uses, read as integrate_wghm_ does (integrateWGHM.cpp:645-646)
+      if (wuse) routing.dailyNUInit(dir, (short)year, calibParam);
       year_started = true;
     }
     int month = 0;
@@ -205,9 +211,12 @@ int main(int argc, char **argv) {
       if (geo.G_contcell[n])
         dailyWaterBalance.calcNewDay((short)doy, (short)month, day_in_month, last_day_in_month[month], (short)year, n,
                                      wghmState, additionalOutIn, snowIO, 0, calibParam);
+    if (wuse) routing.calcNextDay_M(month);   // integrateWGHM.cpp:794-796
     routing.routing((short)year, (short)doy, (short)month, day_in_month, last_day_in_month[month], wghmState,
                     additionalOutIn, 0, calibParam);
     routing.updateLandAreaFrac(additionalOutIn);
+    // end of the year (integrateWGHM.cpp:940-944), before the day's snapshot
+    if (wuse && doy == 365) routing.annualWaterUsePostProcessing((short)year, additionalOutIn);
     for (int b = 0; b < nstation; b++) q[(size_t)d * nstation + b] = routing.dailyRiverDischarge(b, doy - 1);
     if (wtemp)
       for (int b = 0; b < nstation; b++) wt_daily[(size_t)d * nstation + b] = routing.G_RiverWTempPreStep[stations[b]];
@@ -253,6 +262,20 @@ int main(int argc, char **argv) {
         DUMP(routing.G_iceThicknessReservoir[n]);
         DUMP(routing.G_iceThicknessGloWetland[n]);
         DUMP(routing.G_RiverAvailPreStep[n]);
+      }
+      if (wuse) {   // water-use state, the oracle's order
+        DUMP(routing.G_dailyRemainingUse[n]);
+        DUMP(routing.G_unsatisfiedNAsFromIrrig[n]);
+        DUMP(routing.G_unsatisfiedNAsFromOtherSectors[n]);
+        DUMP(routing.G_reducedReturnFlow[n]);
+        DUMP(routing.G_withdrawalIrrigFromSwb[n]);
+        DUMP(routing.G_consumptiveUseIrrigFromSwb[n]);
+        DUMP(routing.G_totalUnsatisfiedUse[n]);
+        DUMP(routing.G_UnsatisfiedUsePrevYear[n]);
+        DUMP(routing.G_unsatisfiedNAsFromIrrigPrevYear[n]);
+        DUMP(routing.G_unsatisfiedNAsFromOtherSectorsPrevYear[n]);
+        DUMP(routing.G_reducedReturnFlowPrevYear[n]);
+        DUMP(routing.G_actualUse[n]);
       }
 #undef DUMP
       snap_i++;

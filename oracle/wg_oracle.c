@@ -536,11 +536,71 @@ typedef struct {
 
 static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
                     const float *temp, const float *swrad, double *discharge, double *balance, int nthreads,
-                    wgo_wt_io *wt);
+                    wgo_wt_io *wt, wgo_wu_io *wu);
 
 int wgo_run(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
             const float *temp, const float *swrad, double *discharge, double *balance, int nthreads) {
-  return run_impl(s, st, doy0, ndays, prec, temp, swrad, discharge, balance, nthreads, NULL);
+  return run_impl(s, st, doy0, ndays, prec, temp, swrad, discharge, balance, nthreads, NULL, NULL);
+}
+
+int wgo_run_wu(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
+               const float *temp, const float *swrad, double *discharge, double *balance, int nthreads,
+               wgo_wu_io *wu) {
+  if (!wu || !wu->nus || !wu->nug || !wu->wdr || !wu->cons || !wu->row_of_day || !wu->frgi || !wu->state)
+    return -1;
+  return run_impl(s, st, doy0, ndays, prec, temp, swrad, discharge, balance, nthreads, NULL, wu);
+}
+
+/* routingClass::updateNetAbstractionGW (routing.cpp:5503-5572): the day's NAg
+ * after the previous day's unsatisfied surface-water demand (w: the water-use
+ * state rows of the cell, stride N) */
+static double update_nag(double *w, size_t N, double nug, double frgi) {
+  double *rem = &w[0], *ui = &w[1 * N], *uo = &w[2 * N], *rrf = &w[3 * N];
+  const double wdr = w[4 * N], cons = w[5 * N];
+  if (*rem > 1.e-12) {
+    if (wdr > 0.) {
+      double eff = cons / wdr;
+      double factor = 1 - (1 - frgi) * (1 - eff);
+      double WUsiNew = 1 / factor * (wdr * factor - *rem);
+      if (WUsiNew < 0.) {
+        WUsiNew = 0.;
+        *ui += wdr * factor;
+        *uo += *rem - (wdr * factor);
+      } else {
+        *ui += *rem;
+      }
+      double returnflowChange = (frgi * (1 - eff) * (WUsiNew - wdr));
+      *rrf += returnflowChange;
+      *rem = 0.;
+      return nug - returnflowChange;
+    }
+    *uo += *rem;
+    return nug;
+  } else if (*rem < -1.e-12) {
+    double fromIrrig = *rem + *uo;
+    if (fromIrrig < 0.) {
+      *uo = 0.;
+    } else {
+      *uo += *rem;
+      *rem = 0.;
+      return nug;
+    }
+    if (*ui == 0.) {
+      *rem = 0.;
+      return nug;
+    }
+    double ratio = (fromIrrig / *ui);
+    if (ratio < -1.) {
+      ratio = -1.;
+      fromIrrig = *ui * -1.;
+    }
+    double returnflowChange = (ratio * *rrf);
+    *ui += fromIrrig;
+    *rrf += returnflowChange;
+    *rem = 0.;
+    return nug - returnflowChange;
+  }
+  return nug;
 }
 
 int wgo_run_wt(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
@@ -549,7 +609,7 @@ int wgo_run_wt(const wgo_static *s, wgo_state *st, int doy0, int ndays, const fl
   if (!wt || !wt->longwave || !wt->gw_temp || !wt->inflow_cells || !wt->river_length_check || !wt->temp ||
       !wt->ice || !wt->river_avail)
     return -1;
-  return run_impl(s, st, doy0, ndays, prec, temp, swrad, discharge, balance, nthreads, wt);
+  return run_impl(s, st, doy0, ndays, prec, temp, swrad, discharge, balance, nthreads, wt, NULL);
 }
 
 void wgo_wt_init(int ncell, wgo_wt_io *wt) {
@@ -645,9 +705,11 @@ static void cell_water_temp(const wgo_static *s, const wgo_state *st, int n, int
   wt->river_avail[n] = transportedVolume;
 }
 
+static const int days_in_month[12] = {31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31};   /* routing.cpp:107 */
+
 static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
                     const float *temp, const float *swrad, double *discharge, double *balance, int nthreads,
-                    wgo_wt_io *wt) {
+                    wgo_wt_io *wt, wgo_wu_io *wu) {
   const int N = s->ncell;
   if (s->nband <= 0 || N <= 0) return -1;
   vout *vo = (vout *)malloc(sizeof(vout) * (size_t)N);
@@ -674,6 +736,14 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
     for (int n = 0; n < N; n++) vertical_cell(s, st, n, day, (double)P[n], (double)T[n], (double)SW[n], &vo[n]);
 
     double b_in = 0., b_evap = 0., b_out = 0., b_leak = 0.;
+    double *W = wu ? wu->state : NULL;
+    const size_t wo = wu ? (size_t)wu->row_of_day[d] * (size_t)N : 0;
+#define WU(k) W[(size_t)(k) * (size_t)N + (size_t)n]
+    if (wu && day == 1)   /* annualInit (routing.cpp:994-1010) */
+      for (int n = 0; n < N; n++) {
+        WU(7) = WU(6); WU(8) = WU(1); WU(9) = WU(2); WU(10) = WU(3);
+        WU(11) = 0.;
+      }
     /* routing sweep in routing order (routing.cpp:1830-4520) */
     for (int n = 0; n < N; n++) inflow_up[n] = 0.;
     for (int rc = 0; rc < N; rc++) {
@@ -691,6 +761,14 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
       const double kg = PAR(s, WGO_P_GWOUTF_C, n);
       double gwPrev = st->gw[n];
       double netGWin = vo[n].gwr * cellArea * (laf / 100.) / 1000000.;
+      double remainingUse = 0., dailyActualUse = 0., nug = 0.;
+      if (wu) {   /* routing.cpp:1926-1933 and the other groundwater variants */
+        nug = wu->nug[wo + n];
+        if (WU(0) != 0.) nug = update_nag(&WU(0), (size_t)N, nug, wu->frgi[n]);
+        netGWin -= nug;
+        e_ow += nug;
+        remainingUse = wu->nus[wo + n];   /* routing.cpp:2225-2290 */
+      }
       st->gw[n] = gwPrev * exp(-1. * kg) + (1. / kg) * netGWin * (1. - exp(-1. * kg));
       if (fabs(st->gw[n]) <= MIN_STOR_VOL) st->gw[n] = 0.;
       double gw_runoff = gwPrev - st->gw[n] + netGWin;
@@ -818,6 +896,7 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
       inflow += inflow_up[n];
       const double inflowUpstream = inflow_up[n];
       (void)inflowUpstream;   /* CellRunoff output only (routing.cpp:3941-3946) */
+      double remUseGloLake = 0., remUseRes = 0.;
       /* global lake, routing.cpp:2630-2804 */
       if (s->lake_area[n] > 0.) {
         double S0 = st->glolake[n];
@@ -828,6 +907,12 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         double pin = (owp * (s->lake_area[n] / 1000000.));
         totalInflow = inflow + pin;
         double PETgwrRemUse = evapo * (s->lake_area[n] / 1000000.);
+        double remUseStart = 0.;
+        if (wu) {   /* routing.cpp:2676-2692 */
+          remUseGloLake = (s->res_area[n] > 0.) ? 0.5 * remainingUse : remainingUse;
+          remUseStart = remUseGloLake;
+          PETgwrRemUse += remUseGloLake;
+        }
         double PETgwrRemUseMax = totalInflow + maxStorage + S0;
         p_ow += pin;
         wr.glolake_prev = S0; wr.glolake_max = maxStorage;
@@ -836,7 +921,10 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
           outflow = 0.;
           e_ow += PETgwrRemUseMax;
           evapo *= PETgwrRemUseMax / PETgwrRemUse;
+          if (remUseGloLake > 0.) remUseGloLake -= remUseGloLake * PETgwrRemUseMax / PETgwrRemUse;
+          else remUseGloLake = 0.;
         } else {
+          remUseGloLake = 0.;
           st->glolake[n] = S0 * exp(-1. * swoutf) + (1. / swoutf) * (totalInflow - PETgwrRemUse) * (1. - exp(-1. * swoutf));
           outflow = totalInflow + S0 - st->glolake[n] - PETgwrRemUse;
           if (st->glolake[n] > maxStorage) {
@@ -851,6 +939,7 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         }
         if (fabs(st->glolake[n]) <= MIN_STOR_VOL) st->glolake[n] = 0.;
         inflow = outflow;
+        dailyActualUse = remUseStart - remUseGloLake;   /* routing.cpp:2788 */
         wr.glolake_evapo = evapo; wr.glolake_out = outflow;
         st->rf_glolake[n] = 1. - pow(fabs(st->glolake[n] - maxStorage) / (2. * maxStorage), (evaredex * EVAPO_RED_EXP));
         if (st->rf_glolake[n] < 0.) st->rf_glolake[n] = 0.;
@@ -870,6 +959,12 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         PETgwrMax = S0 + totalInflow;
         p_ow += pin;
         wr.res_prev = S0;
+        double remUseResStart = 0.;
+        if (wu) {   /* routing.cpp:2869-2877 */
+          if (s->lake_area[n] > 0.) remUseRes = 0.5 * remainingUse + remUseGloLake;
+          else remUseRes = remainingUse;
+          remUseResStart = remUseRes;
+        }
         if (PETgwr > PETgwrMax) {
           st->res[n] = S0 + totalInflow - PETgwrMax;
           e_ow += PETgwrMax;
@@ -877,6 +972,24 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         } else {
           st->res[n] = S0 + totalInflow - PETgwr;
           e_ow += PETgwr;
+        }
+        if (wu) {   /* routing.cpp:2922-2946 */
+          if (remUseRes < 0.) {
+            st->res[n] -= remUseRes;
+            e_ow += remUseRes;
+            remUseRes = 0.;
+          } else if (st->res[n] > (s->stor_cap[n] * 0.1)) {
+            if (remUseRes < (st->res[n] - (s->stor_cap[n] * 0.1))) {
+              st->res[n] -= remUseRes;
+              e_ow += remUseRes;
+              remUseRes = 0.;
+            } else {
+              const double used = (st->res[n] - (s->stor_cap[n] * 0.1));
+              remUseRes -= used;
+              st->res[n] = s->stor_cap[n] * 0.1;
+              e_ow += used;
+            }
+          }
         }
         if (fabs(st->res[n]) <= MIN_STOR_VOL) st->res[n] = 0.;
         if (month == s->start_month[n] - 1) {
@@ -887,8 +1000,10 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         }
         double prov_rel;
         if (s->res_type[n] == 1) {
-          /* net use is out of scope: monthly demand of the downstream area is 0 */
-          double monthlyUse = 0.0;
+          /* routing.cpp:2974-2988; the downstream allocation coefficients are zero */
+          double dailyUse = wu ? wu->nus[wo + n] : 0.0;
+          double monthlyUse = dailyUse * days_in_month[month];
+          monthlyUse = monthlyUse * 1000000000. / (days_in_month[month] * 86400.);
           if (s->mean_demand[n] >= 0.5 * s->mean_outflow[n])
             prov_rel = s->mean_outflow[n] / 2. * (1. + monthlyUse / s->mean_demand[n]);
           else
@@ -914,11 +1029,14 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
           st->res[n] = 0.;
         }
         inflow = outflow;
+        dailyActualUse += remUseResStart - remUseRes;   /* routing.cpp:3068 */
         wr.res_evapo = evapo; wr.res_out = outflow;
         st->rf_res[n] = 1. - pow(fabs(st->res[n] - maxStorage) / maxStorage, EVAPO_RED_EXP_RES);
         if (st->rf_res[n] < 0.) st->rf_res[n] = 0.;
         if (st->rf_res[n] > 1.) st->rf_res[n] = 1.;
       }
+      if (wu && (s->res_area[n] > 0. || s->lake_area[n] > 0.))   /* routing.cpp:3099-3105 */
+        remainingUse = (s->res_area[n] > 0.) ? remUseRes : remUseGloLake;
       /* global wetland, routing.cpp:3178-3297 */
       if (s->glo_wetl[n] > 0) {
         double S0 = st->glowetl[n];
@@ -965,7 +1083,8 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
       double K = riverVelocity / s->river_length[n];
       double S0 = st->river[n];
       riverInflow += 0.;   /* G_dailyRiverPrecip = 0 without river evaporation */
-      double RiverEvapoRemUse = 0. + 0.;
+      double RiverEvapoRemUse = remainingUse + 0.;   /* routing.cpp:3466-3468 */
+      const double remUseRiverStart = remainingUse;
       double RivEvapoRemUseMax = riverInflow + (K * S0 * exp(-1. * K)) / (1. - exp(-1. * K));
       double transportedVolume;
       double leak = 0.;
@@ -973,11 +1092,47 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         st->river[n] = 0.;
         transportedVolume = riverInflow + S0 - RivEvapoRemUseMax;
         if (transportedVolume < 0.) { leak -= transportedVolume; transportedVolume = 0.; }
+        if (wu) {
+          e_ow += RivEvapoRemUseMax;
+          if (remainingUse > 0.) remainingUse -= remainingUse * RivEvapoRemUseMax / RiverEvapoRemUse;
+          else remainingUse = 0.;
+        }
       } else {
         st->river[n] = S0 * exp(-1. * K) + (1. / K) * (riverInflow - RiverEvapoRemUse) * (1. - exp(-1. * K));
         if (fabs(st->river[n]) <= MIN_STOR_VOL) st->river[n] = 0.;
         transportedVolume = riverInflow + S0 - st->river[n] - RiverEvapoRemUse;
         if (transportedVolume < 0.) { leak -= transportedVolume; transportedVolume = 0.; }
+        if (wu) e_ow += RiverEvapoRemUse;
+        remainingUse = 0.;
+      }
+      if (wu) {
+        /* what is left comes from the local lake, down to -maxStorage (routing.cpp:3590-3625) */
+        if ((s->loc_lake[n] > 0.) && (remainingUse > 0.)) {
+          const double maxLL = ((s->loc_lake[n]) / 100.) * cellArea * lakeDepth;
+          if (st->loclake[n] > (-1.) * maxLL) {
+            if (remainingUse < (maxLL + st->loclake[n])) {
+              st->loclake[n] -= remainingUse;
+              e_ow += remainingUse;
+              remainingUse = 0.;
+            } else {
+              const double used = (maxLL + st->loclake[n]);
+              remainingUse -= used;
+              st->loclake[n] = (-1.) * maxLL;
+              e_ow += used;
+            }
+          }
+          st->rf_loclake[n] = 1. - pow(fabs(st->loclake[n] - maxLL) / (2. * maxLL), (evaredex * EVAPO_RED_EXP));
+          if (st->rf_loclake[n] < 0.) st->rf_loclake[n] = 0.;
+          if (st->rf_loclake[n] > 1.) st->rf_loclake[n] = 1.;
+        }
+        dailyActualUse += remUseRiverStart - remainingUse;
+        /* bookkeeping of the cell's day (routing.cpp:3736, 3906-3919) */
+        WU(11) += dailyActualUse;
+        WU(6) += remainingUse;
+        WU(0) = remainingUse;
+        WU(4) = wu->wdr[wo + n];
+        WU(5) = wu->cons[wo + n];
+        if (wu->daily_actual) wu->daily_actual[(size_t)d * N + n] = dailyActualUse + nug;
       }
       /* push downstream, routing.cpp:3955-3958 */
       const int down = s->downstream[n];
@@ -1013,6 +1168,24 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
       st->laf_prev[n] = st->laf[n];
       st->laf[n] = lafNext;
     }
+    if (wu && day == 365)   /* annualWaterUsePostProcessing (routing.cpp:5246-5296) */
+      for (int n = 0; n < N; n++) {
+        if (WU(6) < WU(7)) {
+          WU(7) = WU(6); WU(8) = WU(1); WU(9) = WU(2); WU(10) = WU(3);
+          WU(1) = 0.; WU(2) = 0.; WU(3) = 0.; WU(6) = 0.;
+        } else {
+          WU(6) -= WU(7); WU(1) -= WU(8); WU(2) -= WU(9); WU(3) -= WU(10);
+          if ((WU(1) + WU(2)) < 0) {
+            WU(1) = 0; WU(2) = 0; WU(3) = 0;
+          } else if (WU(2) < 0) {
+            WU(1) += WU(2); WU(2) = 0;
+          } else if (WU(1) < 0) {
+            WU(2) += WU(1); WU(1) = 0; WU(3) = 0;
+          }
+          if (WU(3) > 0) { WU(3) = 0; WU(1) = 0; }
+        }
+      }
+#undef WU
     if (balance) {
       double stot = 0.;
       for (int n = 0; n < N; n++) stot += state_volume(s, st, n);

@@ -11,7 +11,7 @@
  *   routingClass::updateLandAreaFrac      (source/routing.cpp:5343-5352)
  *   routingClass::getRiverVelocity / getNewRiverVelocity (source/routing.cpp:7274-7341)
  * for the option set of the hot path (time_series=1, cloud=2, petOpt=0,
- * intercept=1, use_kc=0, calc_albedo=0, clclOpt=0, subtract_use=0,
+ * intercept=1, use_kc=0, calc_albedo=0, clclOpt=0, subtract_use 0/2,
  * fractionalRoutingOpt 0/1, aridareaOpt=0, riverEvapoOpt=0, statcorrOpt=0,
  * use_alloc=0, glacierOpt=0, calc_wtemp 0/1, riverveloOpt 0/1/2), and
  *   calcWaterTempClass::calcWTemp         (source/calcWaterTemp.cpp:48-1324)
@@ -165,6 +165,37 @@ void wgo_wt_init(int ncell, wgo_wt_io *wt);
 int wgo_run_wt(const wgo_static *s, wgo_state *st, int doy0, int ndays,
                const float *prec, const float *temp, const float *swrad,
                double *discharge, double *balance, int nthreads, wgo_wt_io *wt);
+
+/* ---- water use (options.subtract_use = 2, use_alloc = 0,
+ * delayedUseSatisfaction = 0, aggrNUsGloLakResOpt = 0) ------------------------
+ * Net abstractions satisfied in the cell itself: NUg from groundwater (adapted
+ * by updateNetAbstractionGW, routing.cpp:5503-5572, when the previous day left
+ * demand unsatisfied), NUs from the global lake and reservoir (routing.cpp:
+ * 2676-2789, 2866-2946, 3066-3105), the river (routing.cpp:3465-3514) and the
+ * local lake (routing.cpp:3590-3630), the bookkeeping of the end of the cell
+ * (routing.cpp:3736, 3906-3919), the year start (annualInit, routing.cpp:
+ * 994-1010) and end (annualWaterUsePostProcessing, routing.cpp:5246-5296).
+ * Irrigation reservoirs' release reads the cell's own NUs (the downstream
+ * allocation coefficients of routing.cpp:3001-3007 are zero). */
+#define WGO_WU_NSTATE 12
+/* state rows: 0 G_dailyRemainingUse, 1 G_unsatisfiedNAsFromIrrig,
+ * 2 G_unsatisfiedNAsFromOtherSectors, 3 G_reducedReturnFlow,
+ * 4 G_withdrawalIrrigFromSwb, 5 G_consumptiveUseIrrigFromSwb,
+ * 6 G_totalUnsatisfiedUse, 7 G_UnsatisfiedUsePrevYear,
+ * 8 G_unsatisfiedNAsFromIrrigPrevYear, 9 G_unsatisfiedNAsFromOtherSectorsPrevYear,
+ * 10 G_reducedReturnFlowPrevYear, 11 G_actualUse */
+typedef struct {
+  const double *nus, *nug, *wdr, *cons;  /* [nrow*ncell] daily values [km3/d] (dailyNUInit) */
+  const int32_t *row_of_day;             /* [ndays] table row of each simulated day         */
+  const double *frgi;                    /* [ncell] G_fractreturngw_irrig                   */
+  double *state;                         /* [WGO_WU_NSTATE*ncell]                           */
+  double *daily_actual;                  /* optional [ndays*ncell]: actual NUs + NUg        */
+} wgo_wu_io;
+
+/* wgo_run with water use. */
+int wgo_run_wu(const wgo_static *s, wgo_state *st, int doy0, int ndays,
+               const float *prec, const float *temp, const float *swrad,
+               double *discharge, double *balance, int nthreads, wgo_wu_io *wu);
 
 #ifdef __cplusplus
 }

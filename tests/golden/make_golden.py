@@ -9,7 +9,8 @@ the C restatement -- and through it the GPU library -- on any machine.
     python tests/golden/make_golden.py [case ...]
 
 The water-temperature case (WT_CASES) adds longwave radiation, groundwater
-temperature and the reference's inflow-direction table to the inputs.
+temperature and the reference's inflow-direction table to the inputs; the
+water-use case (WU_CASES) adds three years of monthly net abstractions.
 """
 import os
 import sys
@@ -112,6 +113,49 @@ def main_wtemp(names=None):
         print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+# water use (options.subtract_use = 2, satisfied in the cell itself):
+# name -> (region factory, days, first day of year, snapshot days, water-use seed)
+WU_CASES = {
+    # two year ends (days 36 and 401): annualWaterUsePostProcessing and annualInit
+    "swb_wuse_420d": (lambda: sy.region_small_swb(seed=21, ny=16, nx=32, block_at=(100, 300)), 420, 330,
+                      [36, 200, 401, 420], 13),
+}
+
+
+def main_wuse(names=None):
+    if not ref_case.available():
+        if not ref_case.build():
+            raise SystemExit("reference sources not found; cannot regenerate fixtures")
+    for name, (make, nd, doy0, snaps, seed) in WU_CASES.items():
+        if names and name not in names:
+            continue
+        region = make()
+        P, T, S = sy.forcing(region, nd, doy0=doy0)
+        nus, nug, wdr, cons, frgi = sy.water_use_inputs(region, 3, seed=seed)
+        # most water-body cells abstract more than their lakes and reservoirs hold over a
+        # year: local lakes go below zero, reservoirs down to their 10 % floor
+        a = region.arrays
+        heavy = np.nonzero((a["loc_lake"] > 0) | (a["res_area"] > 0) | (a["lake_area"] > 0))[0][::3]
+        keep = np.ones(region.ncell, bool)
+        keep[heavy] = False
+        nus = np.where(keep[None, None, :], nus, np.abs(nus) * 20.0 + np.float32(3.0e8)).astype(np.float32)
+        outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+        stations = outl[:24]
+        res = ref_case.run(region, P, T, S, doy0=doy0, stations=stations, snapshots=snaps,
+                           wuse=(nus, nug, wdr, cons, frgi))
+        extra = dict(P=P, T=T, S=S, NUS=nus, NUG=nug, WDR=wdr, CONS=cons, FRGI=frgi, doy0=np.array(doy0),
+                     stations=res["stations"], snap_days=np.array(snaps), discharge=res["discharge"])
+        for i, snap in enumerate(res["snapshots"]):
+            snap.pop("snow_band")
+            for k in ref_case.WU_FIELDS + ["gw", "river", "loclake", "locwetl", "glolake", "glowetl", "res",
+                                           "rf_loclake", "rf_glolake", "rf_res", "k_release", "laf", "soil"]:
+                extra[f"s{i}_{k}"] = snap[k]
+        path = os.path.join(HERE, f"{name}.npz")
+        save_npz(region, path, **extra)
+        print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 if __name__ == "__main__":
     main(sys.argv[1:])
     main_wtemp(sys.argv[1:])
+    main_wuse(sys.argv[1:])

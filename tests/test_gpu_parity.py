@@ -21,7 +21,7 @@ from helpers import STATE_KEYS, STORAGES, max_rel_err, state_errors
 pytestmark = pytest.mark.gpu
 RTOL = 1e-10
 FIXTURES = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                  if "wtemp" not in os.path.basename(p))   # the water-temperature cases: test_gpu_wtemp.py
+                  if not ({"wtemp", "wuse"} & set(os.path.basename(p)[:-4].split("_"))))   # test_gpu_wtemp.py, test_gpu_wuse.py
 
 
 @pytest.fixture(scope="module", autouse=True)

@@ -18,7 +18,7 @@ from oracle import Oracle
 from watergap2_gb300.region import load_npz
 
 FIXTURES = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                  if "wtemp" not in os.path.basename(p))   # the water-temperature cases: test_wtemp_oracle.py
+                  if not ({"wtemp", "wuse"} & set(os.path.basename(p)[:-4].split("_"))))   # test_wtemp_oracle.py, test_wuse_oracle.py
 STATE_KEYS = ["canopy", "soil", "snow", "lai_days", "lai_status", "lai_precsum", "gw", "river", "loclake",
               "locwetl", "glolake", "glowetl", "res", "rf_loclake", "rf_locwetl", "rf_glolake", "rf_glowetl",
               "rf_res", "k_release", "laf", "laf_prev"]

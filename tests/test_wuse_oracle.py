@@ -1,0 +1,78 @@
+"""The oracle's water use (subtract_use = 2, demand satisfied in the cell itself)
+against the reference's own daily.cpp/routing.cpp run with the same monthly net
+abstractions (tests/golden/swb_wuse_420d.npz, made by tests/golden/make_golden.py):
+every storage, the water-use state of routingClass (remaining and unsatisfied
+use, reduced return flows, the previous year's values after two year ends) and
+the stations' discharge."""
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURE = os.path.join(HERE, "golden", "swb_wuse_420d.npz")
+STORES = ["gw", "river", "loclake", "locwetl", "glolake", "glowetl", "res", "rf_loclake", "rf_glolake", "rf_res",
+          "k_release", "laf", "soil"]
+
+
+def _load():
+    from watergap2_gb300.region import load_npz
+    return load_npz(FIXTURE)
+
+
+def _close(got, ref, floor, tol=1e-10):
+    got, ref = np.asarray(got, np.float64), np.asarray(ref, np.float64)
+    err = np.abs(got - ref) / np.maximum(np.abs(ref), floor)
+    return float(err.max()) if err.size else 0.0
+
+
+def _use(ex):
+    return ex["NUS"], ex["NUG"], ex["WDR"], ex["CONS"]
+
+
+def test_fixture_exercises_water_use():
+    region, ex = _load()
+    from oracle.ref_case import WU_FIELDS
+    last = len(ex["snap_days"]) - 1
+    # unmet demand, adapted groundwater abstraction and both year-end branches occur
+    assert any(np.any(ex[f"s{i}_wu_remaining"] > 0) for i in range(last + 1))
+    assert np.any(ex[f"s{last}_wu_reduced_return"] != 0)
+    assert np.any(ex[f"s{last}_wu_unsat_prev"] > 0)
+    assert np.any(ex["NUS"] < 0) and np.any(ex["NUG"] < 0)
+    assert (ex[f"s{last}_loclake"] < 0).any()          # local lakes drawn below zero by abstraction
+    assert (ex[f"s{last}_glolake"] < 0).any()          # and global lakes
+    for f in WU_FIELDS:
+        assert f"s0_{f}" in ex
+
+
+@pytest.mark.parametrize("nthreads", [1, 4])
+def test_oracle_water_use_matches_reference(nthreads):
+    import oracle
+    from oracle.ref_case import WU_FIELDS
+    region, ex = _load()
+    doy0 = int(ex["doy0"])
+    P, T, S = ex["P"], ex["T"], ex["S"]
+    worst = {}
+    prev = 0
+    o = oracle.Oracle(region)
+    o.init_water_use(ex["FRGI"])
+    qs = []
+    for i, sd in enumerate(ex["snap_days"]):
+        sd = int(sd)
+        # continue the same run: the call's year index restarts, so pass the tables from its own year on
+        d0doy = (doy0 - 1 + prev) % 365 + 1
+        years_done = int(np.sum(((doy0 - 1 + np.arange(1, prev + 1)) % 365 + 1) == 1)) if prev else 0
+        use = tuple(u[years_done:] for u in _use(ex))
+        q, b, _ = o.run_wu(d0doy, P[prev:sd], T[prev:sd], S[prev:sd], use, discharge=True, balance=True,
+                           nthreads=nthreads)
+        qs.append(q)
+        assert np.abs(b[:, 5]).max() < 1e-9 * max(1.0, np.abs(b[:, 0]).max())
+        for f in STORES:
+            worst[f] = max(worst.get(f, 0.0), _close(o.state[f], ex[f"s{i}_{f}"], 1e-9))
+        for k, f in enumerate(WU_FIELDS):
+            worst[f] = max(worst.get(f, 0.0), _close(o.wu[k], ex[f"s{i}_{f}"], 1e-9))
+        prev = sd
+    q = np.concatenate(qs)[:, ex["stations"]]
+    worst["discharge"] = _close(q, ex["discharge"], 1e-9)
+    bad = {k: v for k, v in worst.items() if not v <= 1e-10}
+    assert not bad, bad

@@ -241,3 +241,29 @@ def inflow_cells(region) -> np.ndarray:
             k = free[0]
         out[c, k] = m
     return out
+
+
+_FIRST_DAY_OF_MONTH = np.array([1, 32, 60, 91, 121, 152, 182, 213, 244, 274, 305, 335])
+
+
+def use_rows(doy0: int, ndays: int) -> np.ndarray:
+    """Row of the water-use tables for each day of a run that starts on day of
+    year doy0: 12 x (years since the first day) + month, a new year starting at
+    every day 1 after the first day (the reference reads one year's net uses at
+    each year start, integrateWGHM.cpp:645-646)."""
+    doy = (doy0 - 1 + np.arange(ndays)) % 365 + 1
+    year = np.cumsum(np.r_[0, (doy[1:] == 1).astype(np.int64)])
+    month = np.searchsorted(_FIRST_DAY_OF_MONTH, doy, side="right") - 1
+    return (12 * year + month).astype(np.int64)
+
+
+def year_spans(doy0: int, ndays: int) -> list:
+    """The run's days split at year starts: [(first day index, days, day of year
+    of the first day, year index)]."""
+    out, d, doy, k = [], 0, int(doy0), 0
+    while d < ndays:
+        m = min(ndays - d, 365 - doy + 1)
+        out.append((d, m, doy, k))
+        d += m
+        doy, k = 1, k + 1
+    return out

@@ -575,3 +575,41 @@ def water_temp_inputs(region: Region, ndays: int, T: np.ndarray, seed: int = 9):
     lw = (eps * 5.670374419e-8 * tk ** 4).astype(np.float32)
     gw = (T.astype(np.float64).mean(axis=0) + rng.normal(0.0, 1.5, n)).astype(np.float32)
     return lw, gw
+
+
+def water_use_inputs(region: Region, nyears: int, seed: int = 13, scale: float = 1.0):
+    """Monthly net abstractions as the reference's yearly water-use files hold
+    them (m3 per month, float32, [nyears, 12, ncell]): net abstraction from
+    surface water (NUs) and from groundwater (NUg), and the withdrawal and
+    consumptive use of irrigation from surface water; plus the fraction of
+    irrigation return flow that reaches groundwater [ncell] float32.
+
+    About 60 % of the cells use water (lognormal, a few cells far beyond what
+    their storages hold, so that demand stays unsatisfied), one in ten of those
+    returns water (negative NUs, as return flows make it in the reference's
+    input); NUg is negative where irrigation returns more to groundwater than
+    is pumped.  Irrigation withdrawal exceeds its consumptive use by the
+    efficiency U(0.3, 0.9)."""
+    rng = np.random.default_rng(seed)
+    n = region.ncell
+    area = cell_area_km2(region.row) if region.row is not None else np.full(n, 2500.0)
+    users = rng.random(n) < 0.6
+    base = rng.lognormal(np.log(2.0e5), 1.6, n) * (area / 2500.0) * scale   # m3 per month
+    base[rng.random(n) < 0.03] *= 200.0                                     # unmet demand
+    season = 1.0 + 0.6 * np.sin(2.0 * np.pi * (np.arange(12) - 3.0) / 12.0)
+    out = []
+    for k in range(4):
+        noise = rng.lognormal(0.0, 0.3, (nyears, 12, n))
+        out.append(base[None, None, :] * season[None, :, None] * noise)
+    nus, nug, wdr, _ = out
+    sign_s = np.where(rng.random(n) < 0.1, -0.3, 1.0)
+    sign_g = np.where(rng.random(n) < 0.25, -0.5, 0.4)
+    nus = nus * (users * sign_s)[None, None, :]
+    nug = nug * (users * sign_g)[None, None, :]
+    irr = users & (rng.random(n) < 0.7)
+    wdr = wdr * 1.5 * irr[None, None, :]
+    eff = rng.uniform(0.3, 0.9, n)
+    cons = wdr * eff[None, None, :]
+    frgi = rng.uniform(0.1, 0.9, n).astype(np.float32)
+    f32 = lambda a: np.ascontiguousarray(a, np.float32)
+    return f32(nus), f32(nug), f32(wdr), f32(cons), frgi
