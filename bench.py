@@ -257,6 +257,56 @@ def run_water_temp(region, P, T, S, stream, local):
     return out
 
 
+def run_water_use(region, P, T, S, stream, local):
+    """The global grid with water use (wg_options.water_use: the reference's
+    subtract_use = 2, every cell meeting its monthly net abstractions from its own
+    global lake, reservoir, river, local lake and groundwater) against the plain
+    run: four years in one wavefront with each year's tables, the fourth timed
+    with CUDA events (the first three fill the wavefront).  Synthetic monthly net
+    abstractions (synthetic.water_use_inputs, seeded)."""
+    import torch
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    nd = 4 * DAYS_PER_STEP
+    nus, nug, wdr, cons, frgi = sy.water_use_inputs(region, 4)
+    use = (nus, nug, wdr, cons)
+    out = {}
+    for name, kw in (("water_use", dict(water_use=True)), ("without", dict())):
+        m = Model(region, max_days=nd, device=local, stream=stream.cuda_stream, days_per_step=WAVEFRONT_DAYS, **kw)
+        m.upload_forcing(0, P[:nd], T[:nd], S[:nd])
+        if kw:
+            m.set_water_use_inputs(frgi)
+            m.upload_water_use_run(0, 1, nd, use)
+        assert 3 * WSTEPS_PER_YEAR >= m.num_levels - 1
+        m.run_steps(1, 0, nd, 0, 3 * WSTEPS_PER_YEAR)
+        m.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        m.run_steps(1, 0, nd, 3 * WSTEPS_PER_YEAR, 4 * WSTEPS_PER_YEAR)
+        e1.record(stream)
+        m.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[name] = {"cell_days_per_s": region.ncell * DAYS_PER_STEP / (ms / 1000.0), "ms_per_year": ms}
+        if kw:
+            w = m.water_use()
+            out[name]["actual_use_km3_last_year"] = float(np.sum(w[11]))
+            out[name]["unsatisfied_km3_last_year"] = float(np.sum(w[6]))
+        del m
+    out["cost_vs_plain"] = out["without"]["cell_days_per_s"] / out["water_use"]["cell_days_per_s"]
+    # the oracle port with water use on the host cores (a bounded sample)
+    from oracle import Oracle
+    cpu_days = int(os.environ.get("WG_CPU_WU_SAMPLE_DAYS", "200"))
+    threads = os.cpu_count() or 1
+    o = Oracle(region)
+    o.init_water_use(frgi)
+    t0 = time.perf_counter()
+    o.run_wu(1, P[:cpu_days], T[:cpu_days], S[:cpu_days], use, nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": region.ncell * cpu_days / cpu_s, "unit": "cell-days/s", "cores": threads,
+                           "kind": "port", "sample": f"{cpu_days} days of the same grid ({cpu_s:.1f} s)"}
+    return out
+
+
 def run_ensemble(args, region, P, T, S, stream, local, plain_value):
     """Batched ensemble: ENS_MEMBERS members of the global grid over ENS_DAYS days in
     one day-pipelined wavefront (FP32 state, FP64 confluence and balance sums),
@@ -476,6 +526,9 @@ def run_gpu(args, rank, world):
     water_temp = None
     if rank == 0 and not os.environ.get("WG_BENCH_NO_WTEMP"):
         water_temp = run_water_temp(region, P, T, S, stream, local)
+    water_use = None
+    if rank == 0 and not os.environ.get("WG_BENCH_NO_WUSE"):
+        water_use = run_water_use(region, P, T, S, stream, local)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -549,6 +602,7 @@ def run_gpu(args, rank, world):
         "per_day_api": per_day,
         "ensemble": ensemble,
         "water_temp": water_temp,
+        "water_use": water_use,
         "cpu_baseline": {"value": cpu_val, "unit": "cell-days/s", "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_days} days of the same grid ({region.ncell * cpu_days} cell-days, "
                                    f"{cpu_s:.1f} s), vertical pass on {cpu_threads} OpenMP threads, routing serial"},

@@ -123,6 +123,13 @@ typedef struct wg_options {
                               routing.cpp:4241-4513; fractional routing stays off);
                               FP64, one member.  Needs wg_upload_longwave and
                               wg_set_water_temp_inputs                               */
+  int32_t water_use;       /* 1: net water abstractions (options.subtract_use = 2,
+                              with use_alloc, delayedUseSatisfaction and
+                              aggrNUsGloLakResOpt 0): every cell meets its demand
+                              from its own global lake, reservoir, river and local
+                              lake and from groundwater.  FP64, one member, not
+                              together with water_temp.  Tables by
+                              wg_upload_water_use (days without one: no use)      */
 } wg_options;
 
 typedef struct wg_ctx wg_ctx;
@@ -201,6 +208,39 @@ wg_status wg_set_water_temp(wg_ctx *ctx, const double *temp, const double *ice);
  * [ndays][nstation] (the river entry of the state above, day by day). */
 wg_status wg_get_river_temp(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out);
 
+/* Water use (wg_options.water_use = 1).  One year's monthly net abstractions
+ * [12][ncell] cell order, m3 per month, as the reference's yearly input files
+ * hold them (G_NETUSE_SW_m3 / G_NETUSE_GW_m3 already multiplied by the
+ * M_NETABSSW / M_NETABSGW calibration factors; G_IRRIG_WITHDRAWAL_USE_SW_m3,
+ * G_IRRIG_CONS_USE_SW_m3; dailyNUInit, routing.cpp:884-976), for forcing slots
+ * fday0 .. fday0+ndays-1, whose first day is day of year doy0; the days must
+ * lie in one year (doy0 + ndays - 1 <= 365).  Converted to km3 per day as the
+ * reference does; the tables of the last ceil(max_days / 365) + 1 calls are
+ * kept (a call reuses the oldest).  Irrigation reservoirs' provisional release
+ * follows the month's use of their cell (routing.cpp:2970-2994; the downstream
+ * allocation coefficients are zero). */
+wg_status wg_upload_water_use(wg_ctx *ctx, int32_t fday0, int32_t ndays, int32_t doy0, const double *nus_m3,
+                              const double *nug_m3, const double *irrig_withdrawal_sw_m3,
+                              const double *irrig_consumptive_sw_m3);
+
+/* Fraction of irrigation return flow that reaches groundwater [ncell]
+ * (G_fractreturngw_irrig, read by routingClass::init, routing.cpp:540-543);
+ * start: 0. */
+wg_status wg_set_water_use_inputs(wg_ctx *ctx, const double *frac_return_gw_irrig);
+
+/* Water-use state of routingClass, [WG_WU_NSTATE][ncell] cell order, km3:
+ * 0 G_dailyRemainingUse, 1 G_unsatisfiedNAsFromIrrig,
+ * 2 G_unsatisfiedNAsFromOtherSectors, 3 G_reducedReturnFlow,
+ * 4 G_withdrawalIrrigFromSwb, 5 G_consumptiveUseIrrigFromSwb (per day),
+ * 6 G_totalUnsatisfiedUse, 7 G_UnsatisfiedUsePrevYear,
+ * 8 G_unsatisfiedNAsFromIrrigPrevYear, 9 G_unsatisfiedNAsFromOtherSectorsPrevYear,
+ * 10 G_reducedReturnFlowPrevYear, 11 G_actualUse (this year); start: 0.
+ * The balance of wg_get_balance counts the net abstractions with the
+ * evaporation (out[2]). */
+#define WG_WU_NSTATE 12
+wg_status wg_get_water_use(wg_ctx *ctx, double *out);
+wg_status wg_set_water_use(wg_ctx *ctx, const double *in);
+
 /* One day, the reference's call granularity: the vertical balance of every cell
  * (the OpenMP calcNewDay loop, source/integrateWGHM.cpp:767-783) for day of year
  * doy (1..365) from forcing slot fday ... */
@@ -230,7 +270,8 @@ wg_status wg_get_discharge(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out
 
 /* Water balance: out[0] total storage [km3] (land storages over the land fraction
  * plus all surface-water and groundwater storages), out[1..4] accumulated
- * inflow (precipitation), evaporation, outflow at outlets and sinks, and clamp
+ * inflow (precipitation), evaporation (with water use: and net abstractions),
+ * outflow at outlets and sinks, and clamp
  * corrections since the last wg_reset_balance, out[5] the largest per-cell
  * closure residual relative to the cell's throughput.  Sums are compensated FP64. */
 wg_status wg_get_balance(wg_ctx *ctx, double out[6]);

@@ -1,0 +1,133 @@
+"""Water use on the GPU (wg_options.water_use: subtract_use = 2, demand met in
+the cell itself) against the reference's own code run with the same monthly net
+abstractions (tests/golden/swb_wuse_420d.npz; the oracle's restatement is pinned
+to it in tests/test_wuse_oracle.py): storages, the water-use state after two
+year ends and the stations' discharge, through the wavefront at one and five
+days per step, split runs and the per-day entry points; the water balance with
+the abstractions closes."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+TOL = 1e-10   # |GPU - reference| <= TOL * max(|reference|, floor)
+STORES = ["gw", "river", "loclake", "locwetl", "glolake", "glowetl", "res", "rf_loclake", "rf_glolake", "rf_res",
+          "k_release", "laf", "soil"]
+
+
+def _case():
+    from watergap2_gb300.region import load_npz
+    return load_npz(os.path.join(HERE, "golden", "swb_wuse_420d.npz"))
+
+
+def _use(ex):
+    return ex["NUS"], ex["NUG"], ex["WDR"], ex["CONS"]
+
+
+def _model(region, ex, **kw):
+    from watergap2_gb300.gpu import Model
+    nd, doy0 = ex["P"].shape[0], int(ex["doy0"])
+    m = Model(region, max_days=nd, stations=ex["stations"], water_use=True, **kw)
+    m.set_water_use_inputs(ex["FRGI"])
+    m.upload_forcing(0, ex["P"], ex["T"], ex["S"])
+    m.upload_water_use_run(0, doy0, nd, _use(ex))
+    return m
+
+
+def _worst(got, ref, floor):
+    got, ref = np.asarray(got, np.float64), np.asarray(ref, np.float64)
+    return float((np.abs(got - ref) / np.maximum(np.abs(ref), floor)).max())
+
+
+def _check_snapshot(m, ex, i):
+    from oracle.ref_case import WU_FIELDS
+    st = m.get_state()
+    wu = m.water_use()
+    bad = {}
+    for f in STORES:
+        e = _worst(st[f], ex[f"s{i}_{f}"], 1e-9)
+        if not e <= TOL:
+            bad[f] = e
+    for k, f in enumerate(WU_FIELDS):
+        e = _worst(wu[k], ex[f"s{i}_{f}"], 1e-9)
+        if not e <= TOL:
+            bad[f] = e
+    assert not bad, (i, bad)
+
+
+@pytest.mark.parametrize("kd", [1, 5])
+def test_water_use_matches_reference(kd):
+    region, ex = _case()
+    doy0 = int(ex["doy0"])
+    m = _model(region, ex, days_per_step=kd)
+    prev = 0
+    for i, sd in enumerate(ex["snap_days"]):
+        sd = int(sd)
+        m.run_days((doy0 - 1 + prev) % 365 + 1, prev, sd - prev)
+        _check_snapshot(m, ex, i)
+        prev = sd
+    q = m.discharge(0, prev)
+    assert _worst(q, ex["discharge"], 1e-9) <= TOL
+
+
+def test_water_use_per_day_api_and_split_runs():
+    """The per-day entry points and a wavefront run split across calls (chunks of
+    seven steps) give the same state as one call."""
+    region, ex = _case()
+    nd, doy0 = ex["P"].shape[0], int(ex["doy0"])
+    a = _model(region, ex, days_per_step=5)
+    a.chunk_steps(7)
+    total = a.num_steps(nd)
+    for lo, hi in ((0, 13), (13, 50), (50, total)):
+        a.run_steps(doy0, 0, nd, lo, hi)
+    b = _model(region, ex)
+    for d in range(nd):
+        doy = (doy0 - 1 + d) % 365 + 1
+        b.step_vertical(doy, d)
+        b.step_routing(doy, d)
+    last = len(ex["snap_days"]) - 1
+    for m in (a, b):
+        _check_snapshot(m, ex, last)
+
+
+def test_water_use_balance_closes_and_state_round_trips():
+    region, ex = _case()
+    nd, doy0 = ex["P"].shape[0], int(ex["doy0"])
+    m = _model(region, ex, days_per_step=5, record_balance=True)
+    s0 = m.balance()[0]
+    m.run_days(doy0, 0, nd)
+    bal = m.balance()
+    total, pin, evap, out, leak, worst = bal
+    resid = (total - s0) - (pin - evap - out + leak)
+    assert abs(resid) <= 1e-12 * max(abs(total), pin), (resid, total, pin)
+    assert worst <= 1e-12, worst
+    # net abstractions leave through the evaporation term: more than the run without use
+    from watergap2_gb300.gpu import Model
+    p = Model(region, max_days=nd, stations=ex["stations"], record_balance=True, days_per_step=5)
+    p.upload_forcing(0, ex["P"], ex["T"], ex["S"])
+    p.run_days(doy0, 0, nd)
+    assert bal[2] > p.balance()[2]
+    # checkpoint / restart of the water-use state
+    w = m.water_use()
+    m.set_water_use(w * 0.5)
+    assert np.array_equal(m.water_use(), w * 0.5)
+
+
+def test_days_without_tables_use_no_water():
+    """Forcing days with no uploaded table run without water use: the results equal
+    a context without water use."""
+    from watergap2_gb300.gpu import Model
+    region, ex = _case()
+    nd, doy0 = 120, int(ex["doy0"])
+    a = Model(region, max_days=nd, stations=ex["stations"], water_use=True, days_per_step=5)
+    a.upload_forcing(0, ex["P"][:nd], ex["T"][:nd], ex["S"][:nd])
+    a.run_days(doy0, 0, nd)
+    b = Model(region, max_days=nd, stations=ex["stations"], days_per_step=5)
+    b.upload_forcing(0, ex["P"][:nd], ex["T"][:nd], ex["S"][:nd])
+    b.run_days(doy0, 0, nd)
+    sa, sb = a.get_state(), b.get_state()
+    for f in STORES:
+        assert np.array_equal(sa[f], sb[f]), f
+    assert np.array_equal(a.discharge(0, nd), b.discharge(0, nd))

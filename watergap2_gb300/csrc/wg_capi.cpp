@@ -611,6 +611,50 @@ const char *wg_last_error(const wg_ctx *ctx) { return ctx ? ctx->err.c_str() : "
 int32_t wg_num_levels(const wg_ctx *ctx) { return ctx ? ctx->topo.nlevel : 0; }
 int64_t wg_launch_count(const wg_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+// Provisional release of a reservoir [m3/s] for the month's use of the cell
+// [m3/s] (routing.cpp:2970-2994): irrigation reservoirs (type 1) follow the
+// demand, others release their mean outflow.
+static double provisional_release(int type, double mean_outflow, double mean_demand, double monthlyUse) {
+  if (type != 1) return mean_outflow;
+  if (mean_demand >= 0.5 * mean_outflow) return mean_outflow / 2. * (1. + monthlyUse / mean_demand);
+  return mean_outflow + monthlyUse - mean_demand;
+}
+
+// Water-use tables and state: blocks of 12 monthly rows, block 0 without use
+// (the provisional release of every reservoir as without water use), one block
+// per year uploaded, enough for a run of max_days; state at zero.
+static wg_status setup_water_use(wg_ctx *ctx, const wg_region *r) {
+  const int n = ctx->n;
+  const size_t N = ctx->nstate();
+  DevWaterUse &w = ctx->wu;
+  ctx->wu_blocks = 1 + ((ctx->max_days + 364) / 365 + 1);
+  const size_t block = (size_t)12 * wg::WU_FIELDS * N;
+  w.tab = ctx->alloc<double>((size_t)ctx->wu_blocks * block);
+  w.row_of_fday = ctx->alloc<int32_t>((size_t)ctx->max_days);
+  w.frgi = ctx->alloc<double>(N);
+  w.st = ctx->alloc<double>((size_t)wg::WU_NSTATE * N);
+  if (!w.tab || !w.row_of_fday || !w.frgi || !w.st) return WG_ERR_NOMEM;
+  ctx->wu_prov0.assign(N, 0.);
+  ctx->wu_res.clear();
+  for (int s = 0; s < n; ++s) {
+    const int i = ctx->topo.cell_of_slot[s];
+    if (r->res_area[i] > 0.) {
+      ctx->wu_prov0[s] = provisional_release(r->res_type[i], r->mean_outflow[i], r->mean_demand[i], 0.0);
+      ctx->wu_res.push_back({s, i, (int)r->res_type[i], r->mean_outflow[i], r->mean_demand[i]});
+    }
+  }
+  std::vector<double> zero(block, 0.);
+  for (int m = 0; m < 12; ++m)
+    std::copy(ctx->wu_prov0.begin(), ctx->wu_prov0.end(), zero.begin() + ((size_t)m * wg::WU_FIELDS + 4) * N);
+  cudaError_t e = cudaMemcpy((void *)w.tab, zero.data(), block * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset((void *)w.row_of_fday, 0, (size_t)ctx->max_days * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMemset((void *)w.frgi, 0, N * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset(w.st, 0, (size_t)wg::WU_NSTATE * N * sizeof(double));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "water use");
+  w.enabled = 1;
+  return WG_OK;
+}
+
 // Water temperature buffers: state at the reference's start values (15 degC, no
 // ice: routing.cpp:172-197), the per-cell inputs in slot order.
 static wg_status setup_water_temp(wg_ctx *ctx, const wg_region *r) {
@@ -661,6 +705,8 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->days_per_step < 0 || opt->days_per_step > 31) return WG_ERR_INVALID;
   if (opt->water_temp < 0 || opt->water_temp > 1) return WG_ERR_INVALID;
   if (opt->water_temp && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
+  if (opt->water_use < 0 || opt->water_use > 1) return WG_ERR_INVALID;
+  if (opt->water_use && (opt->precision != 0 || opt->members != 1 || opt->water_temp)) return WG_ERR_UNSUPPORTED;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
     if (r->lct[i] < 1 || r->lct[i] > WG_NLCT) return WG_ERR_INVALID;
@@ -793,16 +839,8 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
       h.c_ratio[i] = r->stor_cap[i] / (r->mean_outflow[i] * 31536000. / 1000000000.);
       h.c4[i] = (4. * h.c_ratio[i] * h.c_ratio[i]);
       h.one_m_c4[i] = (1.0 - ((4. * h.c_ratio[i] * h.c_ratio[i])));
-      if (r->res_type[i] == 1) {
-        // net use is out of scope: the downstream monthly demand is 0 (routing.cpp:2961-2983)
-        const double monthlyUse = 0.0;
-        if (r->mean_demand[i] >= 0.5 * r->mean_outflow[i])
-          h.prov_rel[i] = r->mean_outflow[i] / 2. * (1. + monthlyUse / r->mean_demand[i]);
-        else
-          h.prov_rel[i] = r->mean_outflow[i] + monthlyUse - r->mean_demand[i];
-      } else {
-        h.prov_rel[i] = r->mean_outflow[i];
-      }
+      // without water use the month's demand is 0 (routing.cpp:2970-2994)
+      h.prov_rel[i] = provisional_release(r->res_type[i], r->mean_outflow[i], r->mean_demand[i], 0.0);
     }
     h.start_month[i] = r->start_month[i];
     h.gw100[i] = r->glo_wetl[i] / 100.;
@@ -943,6 +981,10 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (st != WG_OK) return st;
   if (opt->water_temp) {
     st = setup_water_temp(ctx.get(), r);
+    if (st != WG_OK) return st;
+  }
+  if (opt->water_use) {
+    st = setup_water_use(ctx.get(), r);
     if (st != WG_OK) return st;
   }
   const bool ens = ctx->members > 1;
@@ -1160,6 +1202,89 @@ wg_status wg_get_river_temp(wg_ctx *ctx, int32_t day0, int32_t ndays, double *ou
                    "get_river_temp");
 }
 
+wg_status wg_upload_water_use(wg_ctx *ctx, int32_t fday0, int32_t ndays, int32_t doy0, const double *nus_m3,
+                              const double *nug_m3, const double *irrig_withdrawal_sw_m3,
+                              const double *irrig_consumptive_sw_m3) {
+  if (!ctx || !nus_m3 || !nug_m3 || !irrig_withdrawal_sw_m3 || !irrig_consumptive_sw_m3) return WG_ERR_INVALID;
+  if (fday0 < 0 || ndays < 1 || fday0 + ndays > ctx->max_days || doy0 < 1 || doy0 + ndays - 1 > 365)
+    return WG_ERR_INVALID;
+  if (!ctx->wu.enabled) return WG_ERR_UNSUPPORTED;
+  cudaSetDevice(ctx->device);
+  wg_status st = wg_synchronize(ctx);   // no launch may still read the block this call fills
+  if (st != WG_OK) return st;
+  static const int days_in_month[12] = {31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31};   // routing.cpp:107
+  const int n = ctx->n;
+  const size_t N = ctx->nstate();
+  const int F = wg::WU_FIELDS;
+  const int b = 1 + (ctx->wu_next++ % (ctx->wu_blocks - 1));
+  const size_t block = (size_t)12 * F * N;
+  std::vector<double> buf(block, 0.);
+  const double *src[4] = {nus_m3, nug_m3, irrig_withdrawal_sw_m3, irrig_consumptive_sw_m3};
+  for (int m = 0; m < 12; ++m) {
+    const double per_day = 1000000000. * (double)days_in_month[m];   // dailyNUInit, routing.cpp:966-975
+    for (int k = 0; k < 4; ++k) {
+      double *row = buf.data() + ((size_t)m * F + k) * N;
+      const double *in = src[k] + (size_t)m * n;
+      for (int s = 0; s < n; ++s) row[s] = in[ctx->topo.cell_of_slot[s]] / per_day;
+    }
+    double *prov = buf.data() + ((size_t)m * F + 4) * N;
+    std::copy(ctx->wu_prov0.begin(), ctx->wu_prov0.end(), prov);
+    for (const auto &res : ctx->wu_res) {   // routing.cpp:2970-2994
+      const double dailyUse = buf[((size_t)m * F + 0) * N + res.slot];
+      double monthlyUse = dailyUse * days_in_month[m];
+      monthlyUse = monthlyUse * 1000000000. / (days_in_month[m] * 86400.);
+      prov[res.slot] = provisional_release(res.type, res.mean_outflow, res.mean_demand, monthlyUse);
+    }
+  }
+  std::vector<int32_t> rows(ndays);
+  for (int d = 0; d < ndays; ++d) {
+    const int doy = doy0 + d;
+    int mo = 0;
+    for (int k = 1; k < 12; ++k) mo += (doy >= kFirstDayInMonth[k]) ? 1 : 0;
+    rows[d] = 12 * b + mo;
+  }
+  cudaError_t e = cudaMemcpy((void *)(ctx->wu.tab + (size_t)b * block), buf.data(), block * sizeof(double),
+                             cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy((void *)(ctx->wu.row_of_fday + fday0), rows.data(), (size_t)ndays * sizeof(int32_t),
+                   cudaMemcpyHostToDevice);
+  return cuda_fail(ctx, e, "upload_water_use");
+}
+
+wg_status wg_set_water_use_inputs(wg_ctx *ctx, const double *frac_return_gw_irrig) {
+  if (!ctx || !frac_return_gw_irrig) return WG_ERR_INVALID;
+  if (!ctx->wu.enabled) return WG_ERR_UNSUPPORTED;
+  cudaSetDevice(ctx->device);
+  wg_status st = wg_synchronize(ctx);
+  if (st == WG_OK) st = to_slots(ctx, frac_return_gw_irrig, (double *)ctx->wu.frgi);
+  return st;
+}
+
+// [WG_WU_NSTATE][ncell] cell order <-> [WG_WU_NSTATE][N] slot order
+static wg_status water_use_io(wg_ctx *ctx, double *out, const double *in) {
+  if (!ctx || (!out && !in)) return WG_ERR_INVALID;
+  if (!ctx->wu.enabled) return WG_ERR_UNSUPPORTED;
+  cudaSetDevice(ctx->device);
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  const int n = ctx->n, K = wg::WU_NSTATE;
+  std::vector<double> buf((size_t)K * n);
+  cudaError_t e;
+  if (in) {
+    for (int j = 0; j < K; ++j)
+      for (int s = 0; s < n; ++s) buf[(size_t)j * n + s] = in[(size_t)j * n + ctx->topo.cell_of_slot[s]];
+    e = cudaMemcpy(ctx->wu.st, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice);
+  } else {
+    e = cudaMemcpy(buf.data(), ctx->wu.st, buf.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    for (int j = 0; j < K && e == cudaSuccess; ++j)
+      for (int s = 0; s < n; ++s) out[(size_t)j * n + ctx->topo.cell_of_slot[s]] = buf[(size_t)j * n + s];
+  }
+  return cuda_fail(ctx, e, "water use");
+}
+
+wg_status wg_get_water_use(wg_ctx *ctx, double *out) { return out ? water_use_io(ctx, out, nullptr) : WG_ERR_INVALID; }
+wg_status wg_set_water_use(wg_ctx *ctx, const double *in) { return in ? water_use_io(ctx, nullptr, in) : WG_ERR_INVALID; }
+
 int64_t wg_read_unf(const char *path, void *dst, int64_t bytes) {
   if (!path || !dst || bytes < 0) return -1;
   FILE *f = std::fopen(path, "rb");
@@ -1208,12 +1333,12 @@ wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday) {
                                         ctx->rd, ctx->sync, ctx->outq, ctx->qst, doy, ctx->last_vertical_fday, oday, 1,
                                         0, ctx->topo.nlevel,
                                         ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, DevVaWork{}, ctx->wt,
-                                        ctx->stream)
+                                        ctx->wu, ctx->stream)
                       : launch_pipeline(false, ctx->cf, ctx->sf, ctx->vf, ctx->forcing, ctx->mem, ctx->balance,
                                         ctx->rf, ctx->sync, ctx->outq, ctx->qst, doy, ctx->last_vertical_fday, oday, 1,
                                         0, ctx->topo.nlevel,
                                         ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, DevVaWork{}, ctx->wt,
-                                        ctx->stream);
+                                        ctx->wu, ctx->stream);
   return cuda_fail(ctx, e, "step_routing");
 }
 
@@ -1251,7 +1376,7 @@ static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevSta
     if (e == cudaSuccess)
       e = launch_pipeline(true, c, s, v, ctx->forcing, ctx->mem, ctx->balance, ring, ctx->sync, ctx->outq, ctx->qst,
                           doy0, fday0, fday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->layout, ctx->mon,
-                          vw, ctx->wt, ctx->stream);
+                          vw, ctx->wt, ctx->wu, ctx->stream);
     ctx->launches++;
     if (ev) cudaEventRecord(ev[2], ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "run_steps");

@@ -18,6 +18,7 @@ using wg::DevForcing;
 using wg::DevMembers;
 using wg::DevMonthly;
 using wg::DevWaterTemp;
+using wg::DevWaterUse;
 using wg::DevRingT;
 using wg::DevStateT;
 using wg::DevSync;
@@ -83,6 +84,11 @@ struct wg_ctx {
   int days_per_step = 1;                   // days every cell advances per wavefront step
   int frac_routing = 0;                    // options.fractionalRoutingOpt
   DevWaterTemp wt{};                       // water temperature (wt.enabled = 0: off)
+  DevWaterUse wu{};                        // water use (wu.enabled = 0: off)
+  int wu_blocks = 0, wu_next = 0;          // 12-row table blocks (block 0: no use), next to fill
+  std::vector<double> wu_prov0;            // [n] slot order: provisional release without use
+  struct WuRes { int slot, cell, type; double mean_outflow, mean_demand; };
+  std::vector<WuRes> wu_res;               // the reservoirs, for the monthly provisional release
   int last_vertical_fday = 0;              // forcing slot of the last wg_step_vertical
   int va_warps_default = 0;                // vertical-balance warps the layout was sized for
   unsigned int *va_next = nullptr;         // their work counter

@@ -101,13 +101,14 @@ struct DevVertT {
 // Arrays 0-4: in, evap, out, up, leak; 5-9 their compensations; 10/11 the land leak
 // of the cells whose vertical balance runs ahead of routing and its compensation
 // (kept apart from 4, which the wavefront adds the river's leak of those cells to,
-// so that both can run at the same time).  The wavefront adds no in/evap for such
-// cells: their routing adds exactly zero open-water terms.
+// so that both can run at the same time); 12/13 the net abstractions (water use)
+// routing takes from such cells, apart from 1 for the same reason.  The wavefront
+// adds no in/evap for such cells: their routing adds exactly zero open-water terms.
 struct DevBalance {
-  double *acc;      // [12][n*members]
+  double *acc;      // [14][n*members]
   int32_t enabled;
 };
-constexpr int WG_BALANCE_ARRAYS = 12;
+constexpr int WG_BALANCE_ARRAYS = 14;
 
 // Monthly aggregates of the routing outputs (routing.cpp:3964-4238: G_monthlyRiverAvail,
 // G_monthlyMin/MaxRiverAvail, monthly storage), [nmonths][n*members] each; month m
@@ -157,6 +158,25 @@ struct DevWaterTemp {
   const double *lake_km2, *res_km2;   // [n] global lake and reservoir area [km2]
   const double *ll_pct, *lw_pct, *gw_pct;   // [n] local lake, local and global wetland [% of the cell]
   double *qst_t;             // [max_days][nstation] river temperature at the stations
+  int32_t enabled;
+};
+
+// Water use (subtract_use = 2, demand satisfied in the cell itself), slot order.
+// Table row r of forcing day f is row_of_fday[f]; row r holds, for every slot,
+// the day's net abstraction from surface water (NUs) and from groundwater (NUg),
+// irrigation withdrawal and consumptive use from surface water [km3/d], and the
+// provisional release of a reservoir [m3/s] (routing.cpp:2974-2994); rows 0-11
+// are zero use.  State rows (k * N): 0 remaining use, 1/2 unsatisfied NAs from
+// irrigation / other sectors, 3 reduced return flow, 4/5 irrigation withdrawal /
+// consumptive use of the last day, 6 total unsatisfied use, 7-10 the previous
+// year's 6, 1, 2, 3, 11 actual use of the year.
+constexpr int WU_FIELDS = 5;
+constexpr int WU_NSTATE = 12;
+struct DevWaterUse {
+  const double *tab;          // [rows][WU_FIELDS][N]
+  const int32_t *row_of_fday; // [max_days]
+  const double *frgi;         // [N] fraction of irrigation return flow into groundwater
+  double *st;                 // [WU_NSTATE][N]
   int32_t enabled;
 };
 

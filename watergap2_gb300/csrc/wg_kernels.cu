@@ -361,12 +361,16 @@ __device__ __forceinline__ double cell_water_temp(const DevCellsT<R> &c, const D
   return out[0] == -9999. ? keep : out[0];
 }
 
-template <class R, bool FUSED, bool ENS, bool VAW, bool WT>
+// X: what each cell computes after its routing, bit 0 the water temperature,
+// bit 1 the water use.
+template <class R, bool FUSED, bool ENS, bool VAW, int X>
 __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R, ENS, VAW>::min_blocks) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
                                                   double *outq, double *qst, int doy0, int fday0, int oday0,
                                                   int ndays, int t_b, int t_e, int cell_warps, int idle_warp,
-                                                  DevMonthly mon, DevVaWork vw, DevWaterTemp wtp) {
+                                                  DevMonthly mon, DevVaWork vw, DevWaterTemp wtp, DevWaterUse wu) {
+  constexpr bool WT = (X & 1) != 0;
+  constexpr bool WU = (X & 2) != 0;
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const size_t N = (size_t)n * M;
@@ -486,7 +490,8 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
           RState<R> rs = resident ? rs_keep : load_rstate(st, si, fl);
           RTerms<R> rt;
           WTerms<R> wtm;
-          const R tv = routing_cell<R, WT>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtm);
+          const size_t wrow = WU ? (size_t)wu.row_of_fday[fday0 + d] * WU_FIELDS * N : 0;
+          const R tv = routing_cell<R, WT, WU>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtm, &wu, wrow, si, N);
           if (resident) rs_keep = rs;
           else store_rstate(st, si, rs, fl);
           q_now[si] = (double)tv;
@@ -503,8 +508,10 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
               record_balance(b, N, si, (double)o.land_in * land_f + (double)rt.p_ow,
                              (double)o.land_evap * land_f + (double)rt.e_ow, up, (double)tv,
                              (double)o.land_leak * land_f + (double)rt.leak);
-            else   // vertical ran ahead: its land terms are in arrays 0, 1 and 10
+            else {   // vertical ran ahead: its land terms are in arrays 0, 1 and 10
               record_routing_balance(b, N, si, up, (double)tv, (double)rt.leak);
+              if constexpr (WU) neumaier_add(b.acc, 12 * N + si, 13 * N + si, (double)rt.e_ow);
+            }
           }
           // land-area fraction for the next day (routing.cpp:5034-5188, 5343-5352)
           R next = laf;
@@ -591,7 +598,7 @@ __global__ void __launch_bounds__(256) k_balance_sum(DevCellsT<R> c, DevStateT<R
     const int s = (int)(i / M);
     const double vnow = cell_volume<R>(c, st, N, s, i);
     const double in = b.acc[0 * N + i] + b.acc[5 * N + i];
-    const double ev = b.acc[1 * N + i] + b.acc[6 * N + i];
+    const double ev = (b.acc[1 * N + i] + b.acc[6 * N + i]) + (b.acc[12 * N + i] + b.acc[13 * N + i]);
     const double out = b.acc[2 * N + i] + b.acc[7 * N + i];
     const double up = b.acc[3 * N + i] + b.acc[8 * N + i];
     const double lk = (b.acc[4 * N + i] + b.acc[9 * N + i]) + (b.acc[10 * N + i] + b.acc[11 * N + i]);
@@ -735,25 +742,32 @@ cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, 
   return cudaGetLastError();
 }
 
-template <class R>
-static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false) {
-  if (ens) return wt ? nullptr : (const void *)k_pipeline<R, true, true, false, false>;
-  if constexpr (std::is_same<R, double>::value) {   // FP64 single member only
-    if (wt) return vaw ? (fused ? (const void *)k_pipeline<R, true, false, true, true> : nullptr)
-                       : (fused ? (const void *)k_pipeline<R, true, false, false, true>
-                                : (const void *)k_pipeline<R, false, false, false, true>);
-    if (vaw) return (const void *)k_pipeline<R, true, false, true, false>;
-  } else {
-    if (vaw || wt) return nullptr;
-  }
-  return fused ? (const void *)k_pipeline<R, true, false, false, false>
-               : (const void *)k_pipeline<R, false, false, false, false>;
+template <class R, int X>
+static const void *pipeline_fn_x(bool fused, bool vaw) {
+  return vaw ? (fused ? (const void *)k_pipeline<R, true, false, true, X> : nullptr)
+             : (fused ? (const void *)k_pipeline<R, true, false, false, X>
+                      : (const void *)k_pipeline<R, false, false, false, X>);
 }
 
 template <class R>
-int pipeline_max_blocks(bool fused, bool ens, int threads, bool vaw, bool wt) {
+static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false) {
+  if (ens) return (wt || wu) ? nullptr : (const void *)k_pipeline<R, true, true, false, 0>;
+  if constexpr (std::is_same<R, double>::value) {   // FP64 single member only
+    if (wt && wu) return nullptr;
+    if (wt) return pipeline_fn_x<R, 1>(fused, vaw);
+    if (wu) return pipeline_fn_x<R, 2>(fused, vaw);
+    if (vaw) return (const void *)k_pipeline<R, true, false, true, 0>;
+  } else {
+    if (vaw || wt || wu) return nullptr;
+  }
+  return fused ? (const void *)k_pipeline<R, true, false, false, 0>
+               : (const void *)k_pipeline<R, false, false, false, 0>;
+}
+
+template <class R>
+int pipeline_max_blocks(bool fused, bool ens, int threads, bool vaw, bool wt, bool wu) {
   int dev = 0, nsm = 0, per = 0;
-  const void *fn = pipeline_fn<R>(fused, ens, vaw, wt);
+  const void *fn = pipeline_fn<R>(fused, ens, vaw, wt, wu);
   if (!fn) return 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -766,7 +780,7 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
                             const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
                             const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
                             int t_b, int t_e, int blocks, int threads, const WarpLayout &lay, const DevMonthly &mon,
-                            const DevVaWork &vw, const DevWaterTemp &wtp, cudaStream_t st) {
+                            const DevVaWork &vw, const DevWaterTemp &wtp, const DevWaterUse &wu, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(sync.counter, 0, sizeof(unsigned), st);
   if (e == cudaSuccess && sync.flow && sync.wstep)
     e = cudaMemsetAsync(sync.wstep, 0xff, (size_t)sync.nwarps * sizeof(int), st);   // -1: no step done yet
@@ -783,9 +797,9 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
   void *args[] = {(void *)&c,    (void *)&s,    (void *)&v,     (void *)&f,     (void *)&mem,   (void *)&b,
                   (void *)&ring, (void *)&sync, (void *)&outq,  (void *)&qst,   (void *)&doy0,  (void *)&fday0,
                   (void *)&oday0, (void *)&ndays, (void *)&t_b, (void *)&t_e, (void *)&cell_warps,
-                  (void *)&idle_warp, (void *)&mon, (void *)&vwk, (void *)&wtp};
+                  (void *)&idle_warp, (void *)&mon, (void *)&vwk, (void *)&wtp, (void *)&wu};
   const bool ens = mem.members > 1;
-  const void *fn = pipeline_fn<R>(fused, ens, vaw, wtp.enabled != 0);
+  const void *fn = pipeline_fn<R>(fused, ens, vaw, wtp.enabled != 0, wu.enabled != 0);
   if (!fn) return cudaErrorInvalidConfiguration;
   if (vaw) threads += 32 * vw.warps;
   // cooperative (all blocks resident, or the launch fails) through the launch
@@ -824,12 +838,13 @@ cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int
 #define WG_INSTANTIATE(R)                                                                                          \
   template cudaError_t launch_vertical<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,        \
                                           const DevForcing &, int, int, cudaStream_t);                             \
-  template int pipeline_max_blocks<R>(bool, bool, int, bool, bool);                                                           \
+  template int pipeline_max_blocks<R>(bool, bool, int, bool, bool, bool);                                        \
   template cudaError_t launch_pipeline<R>(bool, const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,  \
                                           const DevForcing &, const DevMembers &, const DevBalance &,             \
                                           const DevRingT<R> &, const DevSync &, double *, double *, int, int,     \
                                           int, int, int, int, int, int, const WarpLayout &, const DevMonthly &,    \
-                                          const DevVaWork &, const DevWaterTemp &, cudaStream_t);                 \
+                                          const DevVaWork &, const DevWaterTemp &, const DevWaterUse &,           \
+                                          cudaStream_t);                                                          \
   template cudaError_t launch_vertical_ahead<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevForcing &,   \
                                                 const DevMembers &, const DevBalance &, const DevRingT<R> &, int,  \
                                                 int, int, int, int, int, int, cudaStream_t);                       \

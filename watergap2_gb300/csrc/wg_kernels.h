@@ -48,13 +48,13 @@ template <class R>
 cudaError_t launch_vertical(const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v, const DevForcing &f,
                             int doy, int fday, cudaStream_t st);
 template <class R>
-int pipeline_max_blocks(bool fused, bool ens, int threads, bool vaw = false, bool wt = false);
+int pipeline_max_blocks(bool fused, bool ens, int threads, bool vaw = false, bool wt = false, bool wu = false);
 template <class R>
 cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
                             const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
                             const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
                             int t_b, int t_e, int blocks, int threads, const WarpLayout &lay, const DevMonthly &mon,
-                            const DevVaWork &vw, const DevWaterTemp &wtp, cudaStream_t st);
+                            const DevVaWork &vw, const DevWaterTemp &wtp, const DevWaterUse &wu, cudaStream_t st);
 cudaError_t launch_fill(double *p, size_t n, double v, cudaStream_t st);
 template <class R>
 cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, const DevForcing &f,

@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kNoallocThreads) k_balance_partials_static(Dev
     const int s = (int)(i / M);
     const double vnow = cell_volume<R>(c, st, N, s, i);
     const double in = b.acc[0 * N + i] + b.acc[5 * N + i];
-    const double ev = b.acc[1 * N + i] + b.acc[6 * N + i];
+    const double ev = (b.acc[1 * N + i] + b.acc[6 * N + i]) + (b.acc[12 * N + i] + b.acc[13 * N + i]);
     const double out = b.acc[2 * N + i] + b.acc[7 * N + i];
     const double up = b.acc[3 * N + i] + b.acc[8 * N + i];
     const double lk = (b.acc[4 * N + i] + b.acc[9 * N + i]) + (b.acc[10 * N + i] + b.acc[11 * N + i]);

@@ -453,23 +453,118 @@ __device__ __forceinline__ R river_velocity(const DevCellsT<R> &c, int s, R rive
   return (v < R(0.00001)) ? R(0.00001) : v;
 }
 
+// routingClass::updateNetAbstractionGW (routing.cpp:5503-5572): the day's net
+// abstraction from groundwater after the previous day's unsatisfied surface-water
+// demand w[0] -- return flows of irrigation from surface water are reduced (or
+// given back) in the proportion that reaches groundwater.  w: the cell's
+// water-use state, row stride N.
+__device__ __forceinline__ double wu_update_nag(double *w, size_t N, double nug, double frgi) {
+  const double rem = w[0];
+  double ui = w[1 * N], uo = w[2 * N], rrf = w[3 * N];
+  const double wdr = w[4 * N], cons = w[5 * N];
+  double out = nug;
+  if (rem > 1.e-12) {
+    if (wdr > 0.) {
+      const double eff = cons / wdr;
+      const double factor = 1. - (1. - frgi) * (1. - eff);
+      double wnew = 1. / factor * (wdr * factor - rem);
+      if (wnew < 0.) {
+        wnew = 0.;
+        ui += wdr * factor;
+        uo += rem - (wdr * factor);
+      } else {
+        ui += rem;
+      }
+      const double change = frgi * (1. - eff) * (wnew - wdr);
+      rrf += change;
+      w[0] = 0.;
+      out = nug - change;
+    } else {
+      uo += rem;
+    }
+  } else if (rem < -1.e-12) {
+    double from_irrig = rem + uo;
+    if (from_irrig >= 0.) {
+      uo += rem;
+      w[0] = 0.;
+    } else {
+      uo = 0.;
+      w[0] = 0.;
+      if (ui != 0.) {
+        double ratio = from_irrig / ui;
+        if (ratio < -1.) {
+          ratio = -1.;
+          from_irrig = ui * -1.;
+        }
+        const double change = ratio * rrf;
+        ui += from_irrig;
+        rrf += change;
+        out = nug - change;
+      }
+    }
+  }
+  w[1 * N] = ui; w[2 * N] = uo; w[3 * N] = rrf;
+  return out;
+}
+
+// End of a year for the cell's water-use state (annualWaterUsePostProcessing,
+// routing.cpp:5256-5296).
+__device__ __forceinline__ void wu_year_end(double *w, size_t N) {
+  double tot = w[6 * N], ui = w[1 * N], uo = w[2 * N], rrf = w[3 * N];
+  const double prev = w[7 * N];
+  if (tot < prev) {
+    w[7 * N] = tot; w[8 * N] = ui; w[9 * N] = uo; w[10 * N] = rrf;
+    ui = 0.; uo = 0.; rrf = 0.; tot = 0.;
+  } else {
+    tot -= prev; ui -= w[8 * N]; uo -= w[9 * N]; rrf -= w[10 * N];
+    if ((ui + uo) < 0.) {
+      ui = 0.; uo = 0.; rrf = 0.;
+    } else if (uo < 0.) {
+      ui += uo; uo = 0.;
+    } else if (ui < 0.) {
+      uo += ui; ui = 0.; rrf = 0.;
+    }
+    if (rrf > 0.) { rrf = 0.; ui = 0.; }
+  }
+  w[6 * N] = tot; w[1 * N] = ui; w[2 * N] = uo; w[3 * N] = rrf;
+}
+
 // One cell of routingClass::routing (routing.cpp:1835-4520) given the vertical
 // outputs and the summed upstream inflow (FP64 for every precision); returns the
-// transported volume.
-template <class R, bool WT = false>
+// transported volume.  WU: water use (subtract_use = 2, satisfied in the cell):
+// wu points at the tables and state, wrow is the offset of the day's table row,
+// si/NN the state index and the state count.
+template <class R, bool WT = false, bool WU = false>
 __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R> &st, int doy, int month, R laf,
                                           R laf_prev, const VOut<R> &v, double inflow_up, RTerms<R> &rt,
-                                          WTerms<R> *wtm = nullptr) {
+                                          WTerms<R> *wtm = nullptr, const DevWaterUse *wu = nullptr, size_t wrow = 0,
+                                          size_t si = 0, size_t NN = 0) {
   typedef M<R> m;
   const uint32_t fl = c.flags[s];
   const R cfa = c.cfa[s];
   rt.p_ow = R(0); rt.e_ow = R(0); rt.leak = R(0);
+  R remainingUse = R(0), dailyActualUse = R(0), remUseGL = R(0), remUseRes = R(0);
+  double *W = nullptr;
+  if constexpr (WU) {
+    W = wu->st + si;
+    if (doy == 1) {   // annualInit (routing.cpp:994-1010)
+      W[7 * NN] = W[6 * NN]; W[8 * NN] = W[1 * NN]; W[9 * NN] = W[2 * NN]; W[10 * NN] = W[3 * NN];
+      W[11 * NN] = 0.;
+    }
+  }
   const R f_land = c.area_f[s] * laf;
   typedef C<R> cmp;
   R dlsr = cmp::le0(laf) ? v.transfer * c.area_f[s] * laf_prev : v.rs * f_land;
   // groundwater (routing.cpp:2061-2200)
   const R gw0 = st.gw;
-  const R netGWin = v.gwr * f_land;
+  R netGWin = v.gwr * f_land;
+  if constexpr (WU) {   // routing.cpp:1926-1933 (and the other groundwater variants)
+    double nug = wu->tab[wrow + NN + si];
+    if (W[0] != 0.) nug = wu_update_nag(W, NN, nug, wu->frgi[si]);
+    netGWin -= R(nug);
+    rt.e_ow += R(nug);
+    remainingUse = R(wu->tab[wrow + si]);   // routing.cpp:2225-2290
+  }
   R gw = gw0 * c.gw_e[s] + c.gw_ik[s] * netGWin * c.gw_ome[s];
   if (cmp::abs_le_c(gw, R(WG_MIN_STOR_VOL))) gw = R(0);
   R gw_runoff = gw0 - gw + netGWin;
@@ -592,7 +687,13 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (evapo < R(0)) evapo = R(0);
     const R pin = owp * c.la6[s];
     const R TI = inflow + pin;
-    const R PU = evapo * c.la6[s];
+    R PU = evapo * c.la6[s];
+    R remGL0 = R(0);
+    if constexpr (WU) {   // routing.cpp:2676-2692
+      remUseGL = (fl & F_RES) ? R(0.5) * remainingUse : remainingUse;
+      remGL0 = remUseGL;
+      PU += remUseGL;
+    }
     const R PUmax = TI + maxS + S0;
     rt.p_ow += pin;
     R S;
@@ -601,7 +702,9 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       outflow = R(0);
       rt.e_ow += PUmax;
       if constexpr (WT) evapo *= PUmax / PU;
+      if constexpr (WU) remUseGL = (remUseGL > R(0)) ? remUseGL - remUseGL * PUmax / PU : R(0);
     } else {
+      if constexpr (WU) remUseGL = R(0);
       S = S0 * c.sw_e[s] + c.sw_ik[s] * (TI - PU) * c.sw_ome[s];
       outflow = TI + S0 - S - PU;
       if (S > maxS) {
@@ -616,6 +719,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     }
     if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     inflow = outflow;
+    if constexpr (WU) dailyActualUse = remGL0 - remUseGL;   // routing.cpp:2788
     if constexpr (WT) {
       wtm->glolake_prev = S0; wtm->glolake_max = maxS; wtm->glolake_evapo = evapo; wtm->glolake_out = outflow;
     }
@@ -632,6 +736,11 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     const R PETgwr = evapo * c.ra6[s];
     const R PETgwrMax = S0 + TI;
     rt.p_ow += pin;
+    R remRes0 = R(0);
+    if constexpr (WU) {   // routing.cpp:2869-2877
+      remUseRes = (fl & F_GLOLAKE) ? R(0.5) * remainingUse + remUseGL : remainingUse;
+      remRes0 = remUseRes;
+    }
     R S;
     if (PETgwr > PETgwrMax) {
       S = S0 + TI - PETgwrMax;
@@ -641,15 +750,36 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
     }
+    if constexpr (WU) {   // net abstraction down to 10 % of the capacity (routing.cpp:2922-2946)
+      const R floor10 = c.rcap01[s];
+      if (remUseRes < R(0)) {
+        S -= remUseRes;
+        rt.e_ow += remUseRes;
+        remUseRes = R(0);
+      } else if (S > floor10) {
+        if (remUseRes < S - floor10) {
+          S -= remUseRes;
+          rt.e_ow += remUseRes;
+          remUseRes = R(0);
+        } else {
+          const R used = S - floor10;
+          remUseRes -= used;
+          S = floor10;
+          rt.e_ow += used;
+        }
+      }
+    }
     if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     R K = st.k_release;
     if (month == c.start_month[s] - 1 && doy == c_first_day_in_month[month]) {
       K = (S < c.rcap01[s]) ? R(0.1) : S * c.inv_rcap085[s];
       st.k_release = K;
     }
+    // the provisional release of an irrigation reservoir follows the month's demand
+    const R prov = WU ? R(wu->tab[wrow + 4 * NN + si]) : c.prov_rel[s];
     R release;
-    if (c.c_ratio[s] >= R(0.5)) release = K * c.prov_rel[s];
-    else release = c.c4[s] * K * c.prov_rel[s] + c.one_m_c4[s] * inflow * R(1.0e9 / 86400.);
+    if (c.c_ratio[s] >= R(0.5)) release = K * prov;
+    else release = c.c4[s] * K * prov + c.one_m_c4[s] * inflow * R(1.0e9 / 86400.);
     outflow = ((S >= c.rcap01[s]) ? release : R(0.1) * release) * R(86400. / 1.0e9);
     if (outflow < R(0)) outflow = R(0);
     S -= outflow;
@@ -662,12 +792,16 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = R(0);
     }
     inflow = outflow;
+    if constexpr (WU) dailyActualUse += remRes0 - remUseRes;   // routing.cpp:3068
     if constexpr (WT) {
       wtm->res_prev = S0; wtm->res_evapo = evapo; wtm->res_out = outflow;
     }
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_rcap[s], R(2.81383));
     st.res = S;
     st.rf_res = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
+  }
+  if constexpr (WU) {   // routing.cpp:3099-3105
+    if (fl & (F_RES | F_GLOLAKE)) remainingUse = (fl & F_RES) ? remUseRes : remUseGL;
   }
   if (fl & F_GLOWETL) {  // global wetland (routing.cpp:3178-3297)
     const R S0 = st.glowetl, maxS = c.maxs_gw[s], rf = st.rf_glowetl;
@@ -714,7 +848,22 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   const R eK = m::exp(-K);
   const R omeK = R(1.) - eK;
   R S, transported;
-  if (cmp::lt0(inflow * omeK + K * S0 * eK)) {   // sign of RivEvapoRemUseMax (routing.cpp:3444-3449)
+  const R remRiver0 = remainingUse;
+  if constexpr (WU) {   // the use the river can meet (routing.cpp:3465-3514)
+    const R maxUse = inflow + K * S0 * eK * m::rcp(omeK);
+    if (remRiver0 > maxUse) {
+      S = R(0);
+      transported = inflow + S0 - maxUse;
+      rt.e_ow += maxUse;
+      remainingUse = (remRiver0 > R(0)) ? remRiver0 - remRiver0 * maxUse / remRiver0 : R(0);
+    } else {
+      S = S0 * eK + (inflow - remRiver0) * omeK * m::rcp(K);
+      if (cmp::abs_le_c(S, R(WG_MIN_STOR_VOL))) S = R(0);
+      transported = inflow + S0 - S - remRiver0;
+      rt.e_ow += remRiver0;
+      remainingUse = R(0);
+    }
+  } else if (cmp::lt0(inflow * omeK + K * S0 * eK)) {   // sign of RivEvapoRemUseMax (routing.cpp:3444-3449)
     const R maxUse = inflow + K * S0 * eK * m::rcp(omeK);   // K >= 1e-5 / length: omeK > 0
     S = R(0);
     transported = inflow + S0 - maxUse;
@@ -728,6 +877,36 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     transported = R(0);
   }
   st.river = S;
+  if constexpr (WU) {
+    // what is left comes from the local lake, down to -maxStorage (routing.cpp:3590-3625)
+    if ((fl & F_LOCLAKE) && remainingUse > R(0)) {
+      const R maxS = c.maxs_ll[s];
+      R L = st.loclake;
+      if (L > -maxS) {
+        if (remainingUse < maxS + L) {
+          L -= remainingUse;
+          rt.e_ow += remainingUse;
+          remainingUse = R(0);
+        } else {
+          const R used = maxS + L;
+          remainingUse -= used;
+          L = -maxS;
+          rt.e_ow += used;
+        }
+      }
+      st.loclake = L;
+      R r = R(1.) - m::pow(m::fabs_(L - maxS) * (R(0.5) * c.inv_maxs_ll[s]), c.evx[s]);
+      st.rf_loclake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
+    }
+    dailyActualUse += remRiver0 - remainingUse;
+    // the cell's bookkeeping (routing.cpp:3736, 3906-3919)
+    W[11 * NN] += (double)dailyActualUse;
+    W[6 * NN] += (double)remainingUse;
+    W[0] = (double)remainingUse;
+    W[4 * NN] = wu->tab[wrow + 2 * NN + si];
+    W[5 * NN] = wu->tab[wrow + 3 * NN + si];
+    if (doy == 365) wu_year_end(W, NN);
+  }
   return transported;
 }
 

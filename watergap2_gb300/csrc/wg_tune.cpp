@@ -47,6 +47,7 @@ void list_fields(wg_ctx *ctx, const DevStateT<R> &s, Snapshot &sn) {
   sn.fields.push_back({(void *)s.snow_band, N * ctx->nband * sizeof(R)});
   sn.fields.push_back({(void *)ctx->outq, 2 * (size_t)ctx->days_per_step * N * sizeof(double)});
   if (ctx->balance.enabled) sn.fields.push_back({(void *)ctx->balance.acc, WG_BALANCE_ARRAYS * N * sizeof(double)});
+  if (ctx->wu.enabled) sn.fields.push_back({(void *)ctx->wu.st, (size_t)wg::WU_NSTATE * N * sizeof(double)});
   if (ctx->wt.enabled) {
     sn.fields.push_back({(void *)ctx->wt.temp, 6 * N * sizeof(double)});
     sn.fields.push_back({(void *)ctx->wt.ice, 6 * N * sizeof(double)});

@@ -34,7 +34,8 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_set_water_temp", "wg_get_river_temp", "wg_clear_error", "wg_set_barrier_test", "wg_autotune", "wg_graph_capture", "wg_graph_launch",
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
            "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells",
-           "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync")
+           "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync",
+           "wg_upload_water_use", "wg_set_water_use_inputs", "wg_get_water_use", "wg_set_water_use")
 
 
 class WgError(RuntimeError):
@@ -61,7 +62,8 @@ class _Options(ctypes.Structure):
                 ("record_balance", ctypes.c_int32), ("stations", ctypes.c_void_p), ("stream", ctypes.c_uint64),
                 ("precision", ctypes.c_int32), ("members", ctypes.c_int32), ("member_prec_factor", ctypes.c_void_p),
                 ("member_gamma_factor", ctypes.c_void_p), ("block_threads", ctypes.c_int32),
-                ("ring_days", ctypes.c_int32), ("days_per_step", ctypes.c_int32), ("water_temp", ctypes.c_int32)]
+                ("ring_days", ctypes.c_int32), ("days_per_step", ctypes.c_int32), ("water_temp", ctypes.c_int32),
+                ("water_use", ctypes.c_int32)]
 
 
 _lib = None
@@ -126,6 +128,10 @@ def load_library(path: str = LIB_PATH):
     lib.wg_get_chunk_steps.restype = i32
     lib.wg_math_eval.argtypes = [i32, i32, vp, vp, ctypes.c_int64, vp]
     lib.wg_upload_longwave.argtypes = [vp, i32, i32, vp]
+    lib.wg_upload_water_use.argtypes = [vp, i32, i32, i32, vp, vp, vp, vp]
+    lib.wg_set_water_use_inputs.argtypes = [vp, vp]
+    lib.wg_get_water_use.argtypes = [vp, vp]
+    lib.wg_set_water_use.argtypes = [vp, vp]
     lib.wg_set_water_temp_inputs.argtypes = [vp, vp, vp]
     lib.wg_get_water_temp.argtypes = [vp, vp, vp]
     lib.wg_set_water_temp.argtypes = [vp, vp, vp]
@@ -149,7 +155,8 @@ def load_library(path: str = LIB_PATH):
                  "wg_set_active_cells", "wg_upload_forcing_unf", "wg_monthly_outputs", "wg_get_monthly",
                  "wg_set_step_sync", "wg_set_vertical_overlap", "wg_upload_longwave", "wg_set_water_temp_inputs",
                  "wg_get_water_temp", "wg_set_water_temp", "wg_get_river_temp", "wg_clear_error",
-                 "wg_set_barrier_test"):
+                 "wg_set_barrier_test", "wg_upload_water_use", "wg_set_water_use_inputs", "wg_get_water_use",
+                 "wg_set_water_use"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -202,7 +209,7 @@ class Model:
     def __init__(self, region: Region, max_days: int = 366, stations=None, record_balance: bool = False,
                  device: int = 0, stream: int = 0, precision: str = "fp64", members: int = 1,
                  prec_factor=None, gamma_factor=None, block_threads: int = 0, ring_days: int = 0,
-                 days_per_step: int = 0, water_temp: bool = False):
+                 days_per_step: int = 0, water_temp: bool = False, water_use: bool = False):
         self.lib = load_library()
         self.region = region
         self._keep = []
@@ -234,6 +241,7 @@ class Model:
         o.ring_days = int(ring_days)
         o.days_per_step = int(days_per_step)
         o.water_temp = int(bool(water_temp))
+        o.water_use = int(bool(water_use))
         self.max_days = int(max_days)
         h = ctypes.c_void_p()
         self._check(self.lib.wg_create(ctypes.byref(r), ctypes.byref(o), ctypes.byref(h)), "wg_create", None)
@@ -475,6 +483,42 @@ class Model:
         out = np.empty((ndays, self.stations.size))
         self._check(self.lib.wg_get_river_temp(self.h, int(day0), int(ndays), out.ctypes.data), "get_river_temp")
         return out
+
+    # ---- water use (water_use=True)
+    def upload_water_use(self, fday0: int, ndays: int, doy0: int, nus, nug, irrig_withdrawal, irrig_consumptive):
+        """wg_upload_water_use: one year's monthly net abstractions [12, ncell] (m3 per month)
+        for forcing slots fday0 .. fday0+ndays-1, the first on day of year doy0."""
+        arrs = [np.ascontiguousarray(a, np.float64) for a in (nus, nug, irrig_withdrawal, irrig_consumptive)]
+        for a in arrs:
+            if a.shape != (12, self.region.ncell):
+                raise ValueError("water-use tables are [12, ncell]")
+        self._check(self.lib.wg_upload_water_use(self.h, int(fday0), int(ndays), int(doy0),
+                                                 *[a.ctypes.data for a in arrs]), "upload_water_use")
+
+    def upload_water_use_run(self, fday0: int, doy0: int, ndays: int, use):
+        """The tables of a whole run: use = (nus, nug, irrigation withdrawal, irrigation
+        consumptive use), each [years, 12, ncell]; year k of the run (a new year at every
+        day 1 after the first day) takes table k."""
+        from .region import year_spans
+        for d, m, doy, k in year_spans(doy0, ndays):
+            self.upload_water_use(fday0 + d, m, doy, *(u[k] for u in use))
+
+    def set_water_use_inputs(self, frac_return_gw_irrig):
+        """wg_set_water_use_inputs: fraction of irrigation return flow into groundwater [ncell]."""
+        a = np.ascontiguousarray(frac_return_gw_irrig, np.float64)
+        self._check(self.lib.wg_set_water_use_inputs(self.h, a.ctypes.data), "set_water_use_inputs")
+
+    def water_use(self) -> np.ndarray:
+        """wg_get_water_use: the water-use state [12, ncell] (remaining, unsatisfied and actual use)."""
+        out = np.empty((12, self.region.ncell))
+        self._check(self.lib.wg_get_water_use(self.h, out.ctypes.data), "get_water_use")
+        return out
+
+    def set_water_use(self, state):
+        a = np.ascontiguousarray(state, np.float64)
+        if a.shape != (12, self.region.ncell):
+            raise ValueError("water-use state is [12, ncell]")
+        self._check(self.lib.wg_set_water_use(self.h, a.ctypes.data), "set_water_use")
 
     def vertical_overlap(self, enable: bool | None = None) -> int:
         """Switch the vertical overlap on or off if given; return the extra warps per block (0: off)."""
