@@ -99,6 +99,18 @@ class Context {
   void river_temp(int day0, int ndays, double *out) {
     check(wg_get_river_temp(ctx_, day0, ndays, out), "wg_get_river_temp");
   }
+  // water use (wg_options.water_use = 1)
+  void upload_water_use(int fday0, int ndays, int doy0, const double *nus_m3, const double *nug_m3,
+                        const double *irrig_withdrawal_sw_m3, const double *irrig_consumptive_sw_m3) {
+    check(wg_upload_water_use(ctx_, fday0, ndays, doy0, nus_m3, nug_m3, irrig_withdrawal_sw_m3,
+                              irrig_consumptive_sw_m3),
+          "wg_upload_water_use");
+  }
+  void set_water_use_inputs(const double *frac_return_gw_irrig) {
+    check(wg_set_water_use_inputs(ctx_, frac_return_gw_irrig), "wg_set_water_use_inputs");
+  }
+  void water_use(double *out) { check(wg_get_water_use(ctx_, out), "wg_get_water_use"); }
+  void set_water_use(const double *in) { check(wg_set_water_use(ctx_, in), "wg_set_water_use"); }
 
   void check(wg_status s, const char *what) const {
     if (s != WG_OK)

@@ -25,6 +25,9 @@ int main() {
   if (wg_upload_longwave(nullptr, 0, 1, nullptr) != WG_ERR_INVALID) return 6;
   if (wg_get_water_temp(nullptr, nullptr, nullptr) != WG_ERR_INVALID) return 7;
   if (wg_get_river_temp(nullptr, 0, 1, nullptr) != WG_ERR_INVALID) return 8;
+  if (wg_upload_water_use(nullptr, 0, 1, 1, nullptr, nullptr, nullptr, nullptr) != WG_ERR_INVALID) return 9;
+  if (wg_get_water_use(nullptr, nullptr) != WG_ERR_INVALID) return 10;
+  if (wg_set_water_use_inputs(nullptr, nullptr) != WG_ERR_INVALID) return 11;
   std::printf("ok\n");
   return 0;
 }
