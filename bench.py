@@ -644,6 +644,34 @@ def run_profile_case(steps: int = 24, warm_steps: int = 200):
                       "vertical_overlap_warps": m.vertical_overlap(), "vinline_fraction": m.vinline_fraction()}))
 
 
+def run_profile_wuse(steps: int = 24, warm_steps: int = 200):
+    """The ncu case of the water-use wavefront, as the bench runs it: the global
+    grid with water use (three years of synthetic tables), FP64,
+    WAVEFRONT_DAYS days per wavefront step, default chunks of 4 steps, vertical
+    overlap; launches as in run_profile_case:
+      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 51 -c 3 python bench.py --profile-wuse"""
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_global()
+    nd = (warm_steps + steps) * WAVEFRONT_DAYS
+    P, T, S = sy.forcing(region, nd, seed=2, doy0=1)
+    nus, nug, wdr, cons, frgi = sy.water_use_inputs(region, (nd + 364) // 365)
+    m = Model(region, max_days=nd, water_use=True, days_per_step=WAVEFRONT_DAYS)
+    m.upload_forcing(0, P, T, S)
+    m.set_water_use_inputs(frgi)
+    m.upload_water_use_run(0, 1, nd, (nus, nug, wdr, cons))
+    m.run_steps(1, 0, nd, 0, warm_steps)
+    m.synchronize()
+    t0 = time.perf_counter()
+    m.run_steps(1, 0, nd, warm_steps, warm_steps + steps)
+    m.synchronize()
+    dt = time.perf_counter() - t0
+    print(json.dumps({"profile_case": "water use, steady-state wavefront", "ncell": region.ncell,
+                      "steps": steps, "days_per_step": WAVEFRONT_DAYS, "seconds": dt,
+                      "cell_days_per_s": region.ncell * steps * WAVEFRONT_DAYS / dt, "chunk_steps": m.chunk_steps(),
+                      "vertical_overlap_warps": m.vertical_overlap()}))
+
+
 def run_fine():
     """Mixed precision at fine resolution: the 5-arc-minute grid (~2.2 M cells),
     FP32 state and fluxes with FP64 confluence and balance sums against the FP64
@@ -802,6 +830,7 @@ def main():
     ap.add_argument("--profile", action="store_true", help="run the short ncu case and exit")
     ap.add_argument("--profile-ensemble", action="store_true", help="run the short ensemble ncu case and exit")
     ap.add_argument("--profile-wtemp", action="store_true", help="run the short water-temperature ncu case and exit")
+    ap.add_argument("--profile-wuse", action="store_true", help="run the short water-use ncu case and exit")
     ap.add_argument("--fine", action="store_true",
                     help="the 5-arc-minute mixed-precision run: FP32 vs FP64 errors at every outlet")
     ap.add_argument("--calibration", action="store_true",
@@ -821,6 +850,9 @@ def main():
         return
     if args.profile_wtemp:
         run_profile_wtemp()
+        return
+    if args.profile_wuse:
+        run_profile_wuse()
         return
     if args.profile_ensemble:
         run_profile_ensemble()
