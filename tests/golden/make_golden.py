@@ -119,6 +119,9 @@ WU_CASES = {
     # two year ends (days 36 and 401): annualWaterUsePostProcessing and annualInit
     "swb_wuse_420d": (lambda: sy.region_small_swb(seed=21, ny=16, nx=32, block_at=(100, 300)), 420, 330,
                       [36, 200, 401, 420], 13),
+    # with fractional routing (the groundwater variants of routing.cpp:1986-2146 take NUg too)
+    "swb_wuse_frac_200d": (lambda: sy.region_small_swb(seed=34, ny=16, nx=32, block_at=(150, 420))
+                           .with_options(frac_routing=1), 200, 200, [166, 200], 17),
 }
 
 

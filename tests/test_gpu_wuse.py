@@ -17,9 +17,9 @@ STORES = ["gw", "river", "loclake", "locwetl", "glolake", "glowetl", "res", "rf_
           "k_release", "laf", "soil"]
 
 
-def _case():
+def _case(name="swb_wuse_420d"):
     from watergap2_gb300.region import load_npz
-    return load_npz(os.path.join(HERE, "golden", "swb_wuse_420d.npz"))
+    return load_npz(os.path.join(HERE, "golden", f"{name}.npz"))
 
 
 def _use(ex):
@@ -57,9 +57,10 @@ def _check_snapshot(m, ex, i):
     assert not bad, (i, bad)
 
 
+@pytest.mark.parametrize("name", ["swb_wuse_420d", "swb_wuse_frac_200d"])   # the second with fractional routing
 @pytest.mark.parametrize("kd", [1, 5])
-def test_water_use_matches_reference(kd):
-    region, ex = _case()
+def test_water_use_matches_reference(name, kd):
+    region, ex = _case(name)
     doy0 = int(ex["doy0"])
     m = _model(region, ex, days_per_step=kd)
     prev = 0
@@ -68,8 +69,8 @@ def test_water_use_matches_reference(kd):
         m.run_days((doy0 - 1 + prev) % 365 + 1, prev, sd - prev)
         _check_snapshot(m, ex, i)
         prev = sd
-    q = m.discharge(0, prev)
-    assert _worst(q, ex["discharge"], 1e-9) <= TOL
+    from test_wuse_oracle import discharge_err
+    assert discharge_err(m.discharge(0, prev), ex["discharge"]) <= TOL
 
 
 def test_water_use_per_day_api_and_split_runs():
