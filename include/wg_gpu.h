@@ -127,8 +127,8 @@ typedef struct wg_options {
                               with use_alloc, delayedUseSatisfaction and
                               aggrNUsGloLakResOpt 0): every cell meets its demand
                               from its own global lake, reservoir, river and local
-                              lake and from groundwater.  FP64, one member, not
-                              together with water_temp.  Tables by
+                              lake and from groundwater.  FP64, one member (with
+                              or without water_temp).  Tables by
                               wg_upload_water_use (days without one: no use)      */
 } wg_options;
 

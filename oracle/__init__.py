@@ -96,6 +96,9 @@ def lib():
         _lib.wgo_run_wu.argtypes = [ctypes.POINTER(_Static), ctypes.POINTER(_State), ctypes.c_int, ctypes.c_int,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_WuIO)]
+        _lib.wgo_run_wt_wu.argtypes = [ctypes.POINTER(_Static), ctypes.POINTER(_State), ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_WtIO), ctypes.POINTER(_WuIO)]
     return _lib
 
 
@@ -185,6 +188,30 @@ class Oracle:
         frac_return_gw_irrig [ncell] is G_fractreturngw_irrig."""
         self.wu = np.zeros((WU_NSTATE, self.region.ncell))
         self._wu_frgi = np.ascontiguousarray(frac_return_gw_irrig, np.float64)
+
+    def run_wt_wu(self, doy0, P, T, S, LW, use, discharge=False, daily_temp=False, nthreads=1):
+        """run() with the water temperature (init_water_temp) and water use
+        (init_water_use); returns (discharge, daily out[0] of every cell)."""
+        from watergap2_gb300.region import use_rows
+        P, T, S, LW = (np.ascontiguousarray(x, np.float32) for x in (P, T, S, LW))
+        nd, n = P.shape[0], self.region.ncell
+        tabs = [np.ascontiguousarray(daily_use(u).reshape(-1, n)) for u in use]
+        rows = np.ascontiguousarray(use_rows(doy0, nd), np.int32)
+        if rows.max() >= tabs[0].shape[0]:
+            raise ValueError("water use covers fewer years than the run")
+        q = np.zeros((nd, n)) if discharge else None
+        dt = np.zeros((nd, n)) if daily_temp else None
+        wt = self._wt_io(LW, dt)
+        io = _WuIO()
+        io.nus, io.nug, io.wdr, io.cons = (_ptr(t) for t in tabs)
+        io.row_of_day, io.frgi, io.state = _ptr(rows), _ptr(self._wu_frgi), _ptr(self.wu)
+        io.daily_actual = None
+        rc = lib().wgo_run_wt_wu(ctypes.byref(self._static), ctypes.byref(self._cstate), int(doy0), nd,
+                                 _ptr(P), _ptr(T), _ptr(S), _ptr(q) if q is not None else None, None,
+                                 int(nthreads), ctypes.byref(wt), ctypes.byref(io))
+        if rc:
+            raise RuntimeError(f"wgo_run_wt_wu failed: {rc}")
+        return q, dt
 
     def run_wu(self, doy0, P, T, S, use, discharge=False, balance=False, daily_actual=False, nthreads=1):
         """run() with water use.  use = (nus, nug, irrigation withdrawal, irrigation

@@ -551,6 +551,17 @@ int wgo_run_wu(const wgo_static *s, wgo_state *st, int doy0, int ndays, const fl
   return run_impl(s, st, doy0, ndays, prec, temp, swrad, discharge, balance, nthreads, NULL, wu);
 }
 
+int wgo_run_wt_wu(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
+                  const float *temp, const float *swrad, double *discharge, double *balance, int nthreads,
+                  wgo_wt_io *wt, wgo_wu_io *wu) {
+  if (!wt || !wt->longwave || !wt->gw_temp || !wt->inflow_cells || !wt->river_length_check || !wt->temp ||
+      !wt->ice || !wt->river_avail)
+    return -1;
+  if (!wu || !wu->nus || !wu->nug || !wu->wdr || !wu->cons || !wu->row_of_day || !wu->frgi || !wu->state)
+    return -1;
+  return run_impl(s, st, doy0, ndays, prec, temp, swrad, discharge, balance, nthreads, wt, wu);
+}
+
 /* routingClass::updateNetAbstractionGW (routing.cpp:5503-5572): the day's NAg
  * after the previous day's unsatisfied surface-water demand (w: the water-use
  * state rows of the cell, stride N) */

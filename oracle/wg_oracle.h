@@ -196,6 +196,10 @@ typedef struct {
 int wgo_run_wu(const wgo_static *s, wgo_state *st, int doy0, int ndays,
                const float *prec, const float *temp, const float *swrad,
                double *discharge, double *balance, int nthreads, wgo_wu_io *wu);
+/* wgo_run with water use and the water temperature. */
+int wgo_run_wt_wu(const wgo_static *s, wgo_state *st, int doy0, int ndays,
+                  const float *prec, const float *temp, const float *swrad,
+                  double *discharge, double *balance, int nthreads, wgo_wt_io *wt, wgo_wu_io *wu);
 
 #ifdef __cplusplus
 }

@@ -158,7 +158,43 @@ def main_wuse(names=None):
         print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+def main_wtemp_wuse(names=None, name="swb_wtemp_wuse_120d"):
+    """Water use together with the water temperature (calc_wtemp = 1, subtract_use
+    = 2): the water-temperature region and a cold season across a year end."""
+    if names and name not in names:
+        return
+    if not ref_case.available():
+        if not ref_case.build():
+            raise SystemExit("reference sources not found; cannot regenerate fixtures")
+    region = wtemp_region(seed=21)
+    nd, doy0, snaps = 120, 300, [66, 120]
+    P, T, S = sy.forcing(region, nd, doy0=doy0)
+    T = (T - 9.0).astype(np.float32)
+    LW, GWT = sy.water_temp_inputs(region, nd, T)
+    nus, nug, wdr, cons, frgi = sy.water_use_inputs(region, 2, seed=19)
+    a = region.arrays
+    heavy = np.nonzero((a["loc_lake"] > 0) | (a["res_area"] > 0) | (a["lake_area"] > 0))[0][::3]
+    keep = np.ones(region.ncell, bool)
+    keep[heavy] = False
+    nus = np.where(keep[None, None, :], nus, np.abs(nus) * 20.0 + np.float32(3.0e8)).astype(np.float32)
+    outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+    stations = outl[:24]
+    res = ref_case.run(region, P, T, S, doy0=doy0, stations=stations, snapshots=snaps, wtemp=(LW, GWT),
+                       wuse=(nus, nug, wdr, cons, frgi))
+    extra = dict(P=P, T=T, S=S, LW=LW, GWT=GWT, NUS=nus, NUG=nug, WDR=wdr, CONS=cons, FRGI=frgi,
+                 doy0=np.array(doy0), stations=res["stations"], snap_days=np.array(snaps),
+                 discharge=res["discharge"], river_temp=res["river_temp"])
+    for i, snap in enumerate(res["snapshots"]):
+        snap.pop("snow_band")
+        for k in ref_case.WT_FIELDS + ref_case.WU_FIELDS + ["river", "soil", "gw", "loclake", "glolake", "res"]:
+            extra[f"s{i}_{k}"] = snap[k]
+    path = os.path.join(HERE, f"{name}.npz")
+    save_npz(region, path, **extra)
+    print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 if __name__ == "__main__":
     main(sys.argv[1:])
     main_wtemp(sys.argv[1:])
     main_wuse(sys.argv[1:])
+    main_wtemp_wuse(sys.argv[1:])

@@ -47,7 +47,8 @@ def _check_snapshot(m, ex, i):
     wu = m.water_use()
     bad = {}
     for f in STORES:
-        e = _worst(st[f], ex[f"s{i}_{f}"], 1e-9)
+        # reduction factors are fractions in [0, 1]: compared absolutely
+        e = _worst(st[f], ex[f"s{i}_{f}"], 1.0 if f.startswith("rf_") else 1e-9)
         if not e <= TOL:
             bad[f] = e
     for k, f in enumerate(WU_FIELDS):
@@ -132,3 +133,42 @@ def test_days_without_tables_use_no_water():
     for f in STORES:
         assert np.array_equal(sa[f], sb[f]), f
     assert np.array_equal(a.discharge(0, nd), b.discharge(0, nd))
+
+
+def test_water_use_with_temperature_matches_reference():
+    """Water use together with the water temperature (k_pipeline<double,...,3>)
+    against the reference run with both (tests/golden/swb_wtemp_wuse_120d.npz)."""
+    from oracle.ref_case import WT_FIELDS, WU_FIELDS
+    from test_wuse_oracle import discharge_err
+    from watergap2_gb300.gpu import Model
+    region, ex = _case("swb_wtemp_wuse_120d")
+    nd, doy0 = ex["P"].shape[0], int(ex["doy0"])
+    m = Model(region, max_days=nd, stations=ex["stations"], water_use=True, water_temp=True, days_per_step=5)
+    m.set_water_use_inputs(ex["FRGI"])
+    m.set_water_temp_inputs(ex["GWT"], region.extras["river_length_file"])
+    m.upload_forcing(0, ex["P"], ex["T"], ex["S"])
+    m.upload_longwave(0, ex["LW"])
+    m.upload_water_use_run(0, doy0, nd, _use(ex))
+    prev = 0
+    for i, sd in enumerate(ex["snap_days"]):
+        sd = int(sd)
+        m.run_days((doy0 - 1 + prev) % 365 + 1, prev, sd - prev)
+        temp, ice = m.water_temp()
+        wu = m.water_use()
+        st = m.get_state()
+        bad = {}
+        for k in range(6):
+            if not _worst(temp[k], ex[f"s{i}_{WT_FIELDS[k]}"], 1.0) <= TOL:
+                bad[WT_FIELDS[k]] = _worst(temp[k], ex[f"s{i}_{WT_FIELDS[k]}"], 1.0)
+            if not _worst(ice[k], ex[f"s{i}_{WT_FIELDS[6 + k]}"], 1e-9) <= TOL:
+                bad[WT_FIELDS[6 + k]] = _worst(ice[k], ex[f"s{i}_{WT_FIELDS[6 + k]}"], 1e-9)
+        for k, f in enumerate(WU_FIELDS):
+            if not _worst(wu[k], ex[f"s{i}_{f}"], 1e-9) <= TOL:
+                bad[f] = _worst(wu[k], ex[f"s{i}_{f}"], 1e-9)
+        for f in ("river", "soil", "gw", "loclake", "glolake", "res"):
+            if not _worst(st[f], ex[f"s{i}_{f}"], 1e-9) <= TOL:
+                bad[f] = _worst(st[f], ex[f"s{i}_{f}"], 1e-9)
+        assert not bad, (i, bad)
+        prev = sd
+    assert discharge_err(m.discharge(0, nd), ex["discharge"]) <= TOL
+    assert _worst(m.river_temp(0, nd), ex["river_temp"], 1.0) <= TOL

@@ -88,3 +88,35 @@ def test_oracle_water_use_matches_reference(path, nthreads):
     worst["discharge"] = discharge_err(q, ex["discharge"])
     bad = {k: v for k, v in worst.items() if not v <= 1e-10}
     assert not bad, bad
+
+
+def test_oracle_water_use_with_temperature_matches_reference():
+    """Water use and the water temperature together (tests/golden/swb_wtemp_wuse_120d.npz:
+    a cold season across a year end, ice on the water bodies, lakes drawn down)."""
+    import oracle
+    from oracle.ref_case import WT_FIELDS, WU_FIELDS
+    from watergap2_gb300.region import load_npz
+    region, ex = load_npz(os.path.join(HERE, "golden", "swb_wtemp_wuse_120d.npz"))
+    o = oracle.Oracle(region)
+    o.init_water_temp(ex["GWT"])
+    o.init_water_use(ex["FRGI"])
+    doy0, prev = int(ex["doy0"]), 0
+    worst = {}
+    for i, sd in enumerate(ex["snap_days"]):
+        sd = int(sd)
+        years_done = int(np.sum(((doy0 - 1 + np.arange(1, prev + 1)) % 365 + 1) == 1)) if prev else 0
+        use = tuple(u[years_done:] for u in _use(ex))
+        o.run_wt_wu((doy0 - 1 + prev) % 365 + 1, ex["P"][prev:sd], ex["T"][prev:sd], ex["S"][prev:sd],
+                    ex["LW"][prev:sd], use)
+        for k in range(6):
+            worst[WT_FIELDS[k]] = max(worst.get(WT_FIELDS[k], 0.0), _close(o.wt["temp"][k], ex[f"s{i}_{WT_FIELDS[k]}"], 1.0))
+            f = WT_FIELDS[6 + k]
+            worst[f] = max(worst.get(f, 0.0), _close(o.wt["ice"][k], ex[f"s{i}_{f}"], 1e-9))
+        for k, f in enumerate(WU_FIELDS):
+            worst[f] = max(worst.get(f, 0.0), _close(o.wu[k], ex[f"s{i}_{f}"], 1e-9))
+        for f in ("river", "soil", "gw", "loclake", "glolake", "res"):
+            worst[f] = max(worst.get(f, 0.0), _close(o.state[f], ex[f"s{i}_{f}"], 1e-9))
+        prev = sd
+    bad = {k: v for k, v in worst.items() if not v <= 1e-10}
+    assert not bad, bad
+    assert (ex["s1_ice_river"] > 0).any() and (ex["s1_wu_actual"] != 0).any()

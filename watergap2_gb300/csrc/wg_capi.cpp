@@ -706,7 +706,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->water_temp < 0 || opt->water_temp > 1) return WG_ERR_INVALID;
   if (opt->water_temp && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
   if (opt->water_use < 0 || opt->water_use > 1) return WG_ERR_INVALID;
-  if (opt->water_use && (opt->precision != 0 || opt->members != 1 || opt->water_temp)) return WG_ERR_UNSUPPORTED;
+  if (opt->water_use && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
     if (r->lct[i] < 1 || r->lct[i] > WG_NLCT) return WG_ERR_INVALID;

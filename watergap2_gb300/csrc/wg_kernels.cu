@@ -753,7 +753,7 @@ template <class R>
 static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false) {
   if (ens) return (wt || wu) ? nullptr : (const void *)k_pipeline<R, true, true, false, 0>;
   if constexpr (std::is_same<R, double>::value) {   // FP64 single member only
-    if (wt && wu) return nullptr;
+    if (wt && wu) return pipeline_fn_x<R, 3>(fused, vaw);
     if (wt) return pipeline_fn_x<R, 1>(fused, vaw);
     if (wu) return pipeline_fn_x<R, 2>(fused, vaw);
     if (vaw) return (const void *)k_pipeline<R, true, false, true, 0>;
