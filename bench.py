@@ -751,7 +751,7 @@ def run_fine():
 def run_calibration():
     """Calibration workload: 1,000 basins cut from the global drainage tree, gamma
     and CFA calibrated to targets from hidden true parameters, by the reference's
-    bisection and by the learned proposer (plain FP64 model as judge)."""
+    bisection and by the learned proposer (the plain FP64 model checking every step)."""
     import torch
     torch.cuda.set_device(0)
     from watergap2_gb300.calibration import run_workload

@@ -2,7 +2,7 @@
  *
  * No counterpart in the reference: its calibration (calibGammaClass::findNewGamma,
  * source/calibration.cpp:266-636) only bisects.  This network proposes a step of
- * (gamma, correction factor) from basin summaries; the plain model judges every
+ * (gamma, correction factor) from basin summaries; the plain model checks every
  * proposal.  It is a 4-layer MLP of width 128 -- inputs zero-padded to 128
  * features, ReLU hidden layers, 16 outputs of which the caller uses the first
  * out_dim -- with BF16 weights and activations and FP32 accumulation; forward

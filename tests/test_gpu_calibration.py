@@ -2,7 +2,7 @@
 basins cut from the global drainage tree, training runs of the plain model
 batched as FP32 ensemble members, the network trained by the tensor-core
 kernels, then both methods calibrate the same basins with the FP64 plain model
-as judge.  What the network gains: fewer plain-model calls per basin at the
+as the arbiter.  What the network gains: fewer plain-model calls per basin at the
 same 1 % discharge criterion."""
 import pytest
 

@@ -1,6 +1,6 @@
 """Basin calibration of the runoff coefficient gamma and the areal correction
 factor CFA against a target long-term mean discharge -- by the reference's
-bisection, and by the learned step proposer with the plain model as judge.
+bisection, and by the learned step proposer with the plain model as the arbiter.
 
 Reference: calibGammaClass::findNewGamma (source/calibration.cpp:266-636),
 driven by integrate_wghm_ (source/integrateWGHM.cpp:220, 414-442, 970, 1096-1109):
