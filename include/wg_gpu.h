@@ -127,8 +127,9 @@ typedef struct wg_options {
                               with use_alloc, delayedUseSatisfaction and
                               aggrNUsGloLakResOpt 0): every cell meets its demand
                               from its own global lake, reservoir, river and local
-                              lake and from groundwater.  FP64, one member (with
-                              or without water_temp).  Tables by
+                              lake and from groundwater.  Any precision and member
+                              count (with water_temp: FP64, one member); the
+                              members share the tables.  Tables by
                               wg_upload_water_use (days without one: no use)      */
 } wg_options;
 
@@ -228,7 +229,7 @@ wg_status wg_upload_water_use(wg_ctx *ctx, int32_t fday0, int32_t ndays, int32_t
  * start: 0. */
 wg_status wg_set_water_use_inputs(wg_ctx *ctx, const double *frac_return_gw_irrig);
 
-/* Water-use state of routingClass, [WG_WU_NSTATE][ncell] cell order, km3:
+/* Water-use state of routingClass, [WG_WU_NSTATE][ncell][members] cell order, km3:
  * 0 G_dailyRemainingUse, 1 G_unsatisfiedNAsFromIrrig,
  * 2 G_unsatisfiedNAsFromOtherSectors, 3 G_reducedReturnFlow,
  * 4 G_withdrawalIrrigFromSwb, 5 G_consumptiveUseIrrigFromSwb (per day),

@@ -625,16 +625,16 @@ static double provisional_release(int type, double mean_outflow, double mean_dem
 // per year uploaded, enough for a run of max_days; state at zero.
 static wg_status setup_water_use(wg_ctx *ctx, const wg_region *r) {
   const int n = ctx->n;
-  const size_t N = ctx->nstate();
+  const size_t N = ctx->nstate();   // state per member, tables per cell
   DevWaterUse &w = ctx->wu;
   ctx->wu_blocks = 1 + ((ctx->max_days + 364) / 365 + 1);
-  const size_t block = (size_t)12 * wg::WU_FIELDS * N;
+  const size_t block = (size_t)12 * wg::WU_FIELDS * n;
   w.tab = ctx->alloc<double>((size_t)ctx->wu_blocks * block);
   w.row_of_fday = ctx->alloc<int32_t>((size_t)ctx->max_days);
-  w.frgi = ctx->alloc<double>(N);
+  w.frgi = ctx->alloc<double>((size_t)n);
   w.st = ctx->alloc<double>((size_t)wg::WU_NSTATE * N);
   if (!w.tab || !w.row_of_fday || !w.frgi || !w.st) return WG_ERR_NOMEM;
-  ctx->wu_prov0.assign(N, 0.);
+  ctx->wu_prov0.assign(n, 0.);
   ctx->wu_res.clear();
   for (int s = 0; s < n; ++s) {
     const int i = ctx->topo.cell_of_slot[s];
@@ -645,10 +645,10 @@ static wg_status setup_water_use(wg_ctx *ctx, const wg_region *r) {
   }
   std::vector<double> zero(block, 0.);
   for (int m = 0; m < 12; ++m)
-    std::copy(ctx->wu_prov0.begin(), ctx->wu_prov0.end(), zero.begin() + ((size_t)m * wg::WU_FIELDS + 4) * N);
+    std::copy(ctx->wu_prov0.begin(), ctx->wu_prov0.end(), zero.begin() + ((size_t)m * wg::WU_FIELDS + 4) * n);
   cudaError_t e = cudaMemcpy((void *)w.tab, zero.data(), block * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset((void *)w.row_of_fday, 0, (size_t)ctx->max_days * sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMemset((void *)w.frgi, 0, N * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset((void *)w.frgi, 0, (size_t)n * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(w.st, 0, (size_t)wg::WU_NSTATE * N * sizeof(double));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "water use");
   w.enabled = 1;
@@ -706,7 +706,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->water_temp < 0 || opt->water_temp > 1) return WG_ERR_INVALID;
   if (opt->water_temp && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
   if (opt->water_use < 0 || opt->water_use > 1) return WG_ERR_INVALID;
-  if (opt->water_use && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
+  if (opt->water_use && opt->water_temp && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
     if (r->lct[i] < 1 || r->lct[i] > WG_NLCT) return WG_ERR_INVALID;
@@ -1214,7 +1214,7 @@ wg_status wg_upload_water_use(wg_ctx *ctx, int32_t fday0, int32_t ndays, int32_t
   if (st != WG_OK) return st;
   static const int days_in_month[12] = {31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31};   // routing.cpp:107
   const int n = ctx->n;
-  const size_t N = ctx->nstate();
+  const size_t N = (size_t)n;   // tables per cell
   const int F = wg::WU_FIELDS;
   const int b = 1 + (ctx->wu_next++ % (ctx->wu_blocks - 1));
   const size_t block = (size_t)12 * F * N;
@@ -1256,7 +1256,7 @@ wg_status wg_set_water_use_inputs(wg_ctx *ctx, const double *frac_return_gw_irri
   if (!ctx->wu.enabled) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
   wg_status st = wg_synchronize(ctx);
-  if (st == WG_OK) st = to_slots(ctx, frac_return_gw_irrig, (double *)ctx->wu.frgi);
+  if (st == WG_OK) st = to_slots(ctx, frac_return_gw_irrig, (double *)ctx->wu.frgi);   // per cell
   return st;
 }
 
@@ -1267,17 +1267,22 @@ static wg_status water_use_io(wg_ctx *ctx, double *out, const double *in) {
   cudaSetDevice(ctx->device);
   wg_status st = wg_synchronize(ctx);
   if (st != WG_OK) return st;
-  const int n = ctx->n, K = wg::WU_NSTATE;
-  std::vector<double> buf((size_t)K * n);
+  const int n = ctx->n, K = wg::WU_NSTATE, M = ctx->members;
+  const size_t N = ctx->nstate();
+  std::vector<double> buf((size_t)K * N);
   cudaError_t e;
   if (in) {
     for (int j = 0; j < K; ++j)
-      for (int s = 0; s < n; ++s) buf[(size_t)j * n + s] = in[(size_t)j * n + ctx->topo.cell_of_slot[s]];
+      for (int s = 0; s < n; ++s)
+        for (int mm = 0; mm < M; ++mm)
+          buf[(size_t)j * N + (size_t)s * M + mm] = in[(size_t)j * N + (size_t)ctx->topo.cell_of_slot[s] * M + mm];
     e = cudaMemcpy(ctx->wu.st, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice);
   } else {
     e = cudaMemcpy(buf.data(), ctx->wu.st, buf.size() * sizeof(double), cudaMemcpyDeviceToHost);
     for (int j = 0; j < K && e == cudaSuccess; ++j)
-      for (int s = 0; s < n; ++s) out[(size_t)j * n + ctx->topo.cell_of_slot[s]] = buf[(size_t)j * n + s];
+      for (int s = 0; s < n; ++s)
+        for (int mm = 0; mm < M; ++mm)
+          out[(size_t)j * N + (size_t)ctx->topo.cell_of_slot[s] * M + mm] = buf[(size_t)j * N + (size_t)s * M + mm];
   }
   return cuda_fail(ctx, e, "water use");
 }

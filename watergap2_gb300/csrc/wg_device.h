@@ -162,7 +162,7 @@ struct DevWaterTemp {
 };
 
 // Water use (subtract_use = 2, demand satisfied in the cell itself), slot order.
-// Table row r of forcing day f is row_of_fday[f]; row r holds, for every slot,
+// Table row r of forcing day f is row_of_fday[f]; row r holds, for every cell slot,
 // the day's net abstraction from surface water (NUs) and from groundwater (NUg),
 // irrigation withdrawal and consumptive use from surface water [km3/d], and the
 // provisional release of a reservoir [m3/s] (routing.cpp:2974-2994); rows 0-11
@@ -173,9 +173,9 @@ struct DevWaterTemp {
 constexpr int WU_FIELDS = 5;
 constexpr int WU_NSTATE = 12;
 struct DevWaterUse {
-  const double *tab;          // [rows][WU_FIELDS][N]
+  const double *tab;          // [rows][WU_FIELDS][n] (per cell, shared by the members)
   const int32_t *row_of_fday; // [max_days]
-  const double *frgi;         // [N] fraction of irrigation return flow into groundwater
+  const double *frgi;         // [n] fraction of irrigation return flow into groundwater
   double *st;                 // [WU_NSTATE][N]
   int32_t enabled;
 };

@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
           RState<R> rs = resident ? rs_keep : load_rstate(st, si, fl);
           RTerms<R> rt;
           WTerms<R> wtm;
-          const size_t wrow = WU ? (size_t)wu.row_of_fday[fday0 + d] * WU_FIELDS * N : 0;
+          const size_t wrow = WU ? (size_t)wu.row_of_fday[fday0 + d] * WU_FIELDS * (size_t)n : 0;
           const R tv = routing_cell<R, WT, WU>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtm, &wu, wrow, si, N);
           if (resident) rs_keep = rs;
           else store_rstate(st, si, rs, fl);
@@ -751,14 +751,16 @@ static const void *pipeline_fn_x(bool fused, bool vaw) {
 
 template <class R>
 static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false) {
-  if (ens) return (wt || wu) ? nullptr : (const void *)k_pipeline<R, true, true, false, 0>;
+  if (ens) return wt ? nullptr
+                     : (wu ? (const void *)k_pipeline<R, true, true, false, 2> : (const void *)k_pipeline<R, true, true, false, 0>);
   if constexpr (std::is_same<R, double>::value) {   // FP64 single member only
     if (wt && wu) return pipeline_fn_x<R, 3>(fused, vaw);
     if (wt) return pipeline_fn_x<R, 1>(fused, vaw);
     if (wu) return pipeline_fn_x<R, 2>(fused, vaw);
     if (vaw) return (const void *)k_pipeline<R, true, false, true, 0>;
-  } else {
-    if (vaw || wt || wu) return nullptr;
+  } else {   // FP32: no vertical-balance warps, no water temperature
+    if (vaw || wt) return nullptr;
+    if (wu) return fused ? (const void *)k_pipeline<R, true, false, false, 2> : (const void *)k_pipeline<R, false, false, false, 2>;
   }
   return fused ? (const void *)k_pipeline<R, true, false, false, 0>
                : (const void *)k_pipeline<R, false, false, false, 0>;

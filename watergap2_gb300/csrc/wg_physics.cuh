@@ -532,8 +532,8 @@ __device__ __forceinline__ void wu_year_end(double *w, size_t N) {
 // One cell of routingClass::routing (routing.cpp:1835-4520) given the vertical
 // outputs and the summed upstream inflow (FP64 for every precision); returns the
 // transported volume.  WU: water use (subtract_use = 2, satisfied in the cell):
-// wu points at the tables and state, wrow is the offset of the day's table row,
-// si/NN the state index and the state count.
+// wu points at the tables (per cell: slot s, stride c.n) and the state (per
+// member: state index si, stride NN), wrow is the offset of the day's table row.
 template <class R, bool WT = false, bool WU = false>
 __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R> &st, int doy, int month, R laf,
                                           R laf_prev, const VOut<R> &v, double inflow_up, RTerms<R> &rt,
@@ -559,11 +559,12 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   const R gw0 = st.gw;
   R netGWin = v.gwr * f_land;
   if constexpr (WU) {   // routing.cpp:1926-1933 (and the other groundwater variants)
-    double nug = wu->tab[wrow + NN + si];
-    if (W[0] != 0.) nug = wu_update_nag(W, NN, nug, wu->frgi[si]);
+    const size_t tn = (size_t)c.n;
+    double nug = wu->tab[wrow + tn + s];
+    if (W[0] != 0.) nug = wu_update_nag(W, NN, nug, wu->frgi[s]);
     netGWin -= R(nug);
     rt.e_ow += R(nug);
-    remainingUse = R(wu->tab[wrow + si]);   // routing.cpp:2225-2290
+    remainingUse = R(wu->tab[wrow + s]);   // routing.cpp:2225-2290
   }
   R gw = gw0 * c.gw_e[s] + c.gw_ik[s] * netGWin * c.gw_ome[s];
   if (cmp::abs_le_c(gw, R(WG_MIN_STOR_VOL))) gw = R(0);
@@ -776,7 +777,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       st.k_release = K;
     }
     // the provisional release of an irrigation reservoir follows the month's demand
-    const R prov = WU ? R(wu->tab[wrow + 4 * NN + si]) : c.prov_rel[s];
+    const R prov = WU ? R(wu->tab[wrow + 4 * (size_t)c.n + s]) : c.prov_rel[s];
     R release;
     if (c.c_ratio[s] >= R(0.5)) release = K * prov;
     else release = c.c4[s] * K * prov + c.one_m_c4[s] * inflow * R(1.0e9 / 86400.);
@@ -903,8 +904,8 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     W[11 * NN] += (double)dailyActualUse;
     W[6 * NN] += (double)remainingUse;
     W[0] = (double)remainingUse;
-    W[4 * NN] = wu->tab[wrow + 2 * NN + si];
-    W[5 * NN] = wu->tab[wrow + 3 * NN + si];
+    W[4 * NN] = wu->tab[wrow + 2 * (size_t)c.n + s];
+    W[5 * NN] = wu->tab[wrow + 3 * (size_t)c.n + s];
     if (doy == 365) wu_year_end(W, NN);
   }
   return transported;

@@ -508,16 +508,20 @@ class Model:
         a = np.ascontiguousarray(frac_return_gw_irrig, np.float64)
         self._check(self.lib.wg_set_water_use_inputs(self.h, a.ctypes.data), "set_water_use_inputs")
 
+    def _wu_shape(self):
+        return (12, self.region.ncell) if self.members == 1 else (12, self.region.ncell, self.members)
+
     def water_use(self) -> np.ndarray:
-        """wg_get_water_use: the water-use state [12, ncell] (remaining, unsatisfied and actual use)."""
-        out = np.empty((12, self.region.ncell))
+        """wg_get_water_use: the water-use state [12, ncell] (remaining, unsatisfied and
+        actual use); [12, ncell, members] for ensembles."""
+        out = np.empty(self._wu_shape())
         self._check(self.lib.wg_get_water_use(self.h, out.ctypes.data), "get_water_use")
         return out
 
     def set_water_use(self, state):
         a = np.ascontiguousarray(state, np.float64)
-        if a.shape != (12, self.region.ncell):
-            raise ValueError("water-use state is [12, ncell]")
+        if a.shape != self._wu_shape():
+            raise ValueError(f"water-use state is {self._wu_shape()}")
         self._check(self.lib.wg_set_water_use(self.h, a.ctypes.data), "set_water_use")
 
     def vertical_overlap(self, enable: bool | None = None) -> int:
