@@ -125,7 +125,9 @@ typedef struct wg_options {
                               wg_set_water_temp_inputs                               */
   int32_t water_use;       /* 1: net water abstractions (options.subtract_use = 2,
                               with use_alloc, delayedUseSatisfaction and
-                              aggrNUsGloLakResOpt 0): every cell meets its demand
+                              aggrNUsGloLakResOpt 0); 2: the same with
+                              delayedUseSatisfaction = 1 (a day's unmet demand adds
+                              to the next day's): every cell meets its demand
                               from its own global lake, reservoir, river and local
                               lake and from groundwater.  Any precision and member
                               count (with water_temp: FP64, one member); the

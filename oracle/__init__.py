@@ -57,7 +57,7 @@ class _WtIO(ctypes.Structure):
 
 class _WuIO(ctypes.Structure):
     _fields_ = [(f, ctypes.c_void_p) for f in ("nus", "nug", "wdr", "cons", "row_of_day", "frgi", "state",
-                                               "daily_actual")]
+                                               "daily_actual")] + [("delayed", ctypes.c_int32)]
 
 
 WU_NSTATE = 12
@@ -183,10 +183,12 @@ class Oracle:
             raise RuntimeError(f"wgo_run_wt failed: {rc}")
         return q, dt
 
-    def init_water_use(self, frac_return_gw_irrig):
+    def init_water_use(self, frac_return_gw_irrig, delayed=False):
         """Switch on water use: its state starts at zero (routing.cpp:790-848);
-        frac_return_gw_irrig [ncell] is G_fractreturngw_irrig."""
+        frac_return_gw_irrig [ncell] is G_fractreturngw_irrig; delayed: unmet
+        demand carried to the next day (options.delayedUseSatisfaction)."""
         self.wu = np.zeros((WU_NSTATE, self.region.ncell))
+        self._wu_delayed = int(bool(delayed))
         self._wu_frgi = np.ascontiguousarray(frac_return_gw_irrig, np.float64)
 
     def run_wt_wu(self, doy0, P, T, S, LW, use, discharge=False, daily_temp=False, nthreads=1):
@@ -206,6 +208,7 @@ class Oracle:
         io.nus, io.nug, io.wdr, io.cons = (_ptr(t) for t in tabs)
         io.row_of_day, io.frgi, io.state = _ptr(rows), _ptr(self._wu_frgi), _ptr(self.wu)
         io.daily_actual = None
+        io.delayed = self._wu_delayed
         rc = lib().wgo_run_wt_wu(ctypes.byref(self._static), ctypes.byref(self._cstate), int(doy0), nd,
                                  _ptr(P), _ptr(T), _ptr(S), _ptr(q) if q is not None else None, None,
                                  int(nthreads), ctypes.byref(wt), ctypes.byref(io))
@@ -233,6 +236,7 @@ class Oracle:
         io.nus, io.nug, io.wdr, io.cons = (_ptr(t) for t in tabs)
         io.row_of_day, io.frgi, io.state = _ptr(rows), _ptr(self._wu_frgi), _ptr(self.wu)
         io.daily_actual = _ptr(da) if da is not None else None
+        io.delayed = self._wu_delayed
         rc = lib().wgo_run_wu(ctypes.byref(self._static), ctypes.byref(self._cstate), int(doy0), nd,
                               _ptr(P), _ptr(T), _ptr(S), _ptr(q) if q is not None else None,
                               _ptr(b) if b is not None else None, int(nthreads), ctypes.byref(io))

@@ -57,7 +57,8 @@ WT_FIELDS = ["wt_river", "wt_loclake", "wt_locwetl", "wt_glolake", "wt_res", "wt
              "ice_river", "ice_loclake", "ice_locwetl", "ice_glolake", "ice_res", "ice_glowetl", "river_avail"]
 
 
-def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000, wtemp=None, wuse=None):
+def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000, wtemp=None, wuse=None,
+               delayed=False):
     n = region.ncell
     if n > NG:
         raise ValueError("region larger than the reference grid")
@@ -171,12 +172,13 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
                 _unf(f"{d}/{name}_{year0 + k}.12.UNF0", full.ravel(), np.float32)
     with open(f"{d}/meta.txt", "w") as f:
         f.write(f"{n} {P.shape[0]} {doy0} {year0} {resopt} {region.river_velo_opt} {len(stations)} {len(snapshots)} "
-                f"{0 if wtemp is None else 1} {int(getattr(region, 'frac_routing', 0))} {0 if wuse is None else 1}\n")
+                f"{0 if wtemp is None else 1} {int(getattr(region, 'frac_routing', 0))} "
+                f"{0 if wuse is None else (2 if delayed else 1)}\n")
     with open(f"{d}/snapshots.txt", "w") as f:
         f.write(" ".join(str(int(s)) for s in snapshots) + "\n")
 
 
-def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wtemp=None, wuse=None):
+def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wtemp=None, wuse=None, delayed=False):
     """Run the reference harness; returns dict(lai_a, lai_b, bottom_width, snapshots=[{field: array}],
     discharge=[ndays, nstation], stations=...)."""
     if not available():
@@ -189,7 +191,7 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
     stations = np.asarray(stations, np.int32)
     snapshots = list(snapshots or [ndays])
     tmp = workdir or tempfile.mkdtemp(prefix="wg_ref_")
-    write_case(region, tmp, P, T, S, doy0, stations, snapshots, wtemp=wtemp, wuse=wuse)
+    write_case(region, tmp, P, T, S, doy0, stations, snapshots, wtemp=wtemp, wuse=wuse, delayed=delayed)
     out = os.path.join(tmp, "out.bin")
     subprocess.run([HARNESS, tmp, out], check=True, stdout=subprocess.DEVNULL)
     raw = np.fromfile(out, np.float64)

@@ -88,6 +88,7 @@ int main(int argc, char **argv) {
   // water use: net abstractions from the yearly G_NETUSE_*_m3 files, satisfied in
   // the cell itself (use_alloc, delayedUseSatisfaction and aggrNUsGloLakResOpt off)
   if (wuse) options.subtract_use = 2;
+  if (wuse == 2) options.delayedUseSatisfaction = 1;   // unmet demand carried to the next day
   options.glacierOpt = 0; options.calc_wtemp = wtemp; options.start_year = year0; options.end_year = year0;
   options.init_years = 0; options.time_step = 1; options.outLAImax = 0;
 

@@ -772,13 +772,18 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
       const double kg = PAR(s, WGO_P_GWOUTF_C, n);
       double gwPrev = st->gw[n];
       double netGWin = vo[n].gwr * cellArea * (laf / 100.) / 1000000.;
-      double remainingUse = 0., dailyActualUse = 0., nug = 0.;
+      double remainingUse = 0., dailyActualUse = 0., nug = 0., prevTotalUnsat = 0.;
       if (wu) {   /* routing.cpp:1926-1933 and the other groundwater variants */
         nug = wu->nug[wo + n];
         if (WU(0) != 0.) nug = update_nag(&WU(0), (size_t)N, nug, wu->frgi[n]);
         netGWin -= nug;
         e_ow += nug;
         remainingUse = wu->nus[wo + n];   /* routing.cpp:2225-2290 */
+        if (wu->delayed) {                /* routing.cpp:2236-2244 */
+          remainingUse += WU(6);
+          prevTotalUnsat = WU(6);
+          WU(6) = 0.;
+        }
       }
       st->gw[n] = gwPrev * exp(-1. * kg) + (1. / kg) * netGWin * (1. - exp(-1. * kg));
       if (fabs(st->gw[n]) <= MIN_STOR_VOL) st->gw[n] = 0.;
@@ -1139,8 +1144,13 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         dailyActualUse += remUseRiverStart - remainingUse;
         /* bookkeeping of the cell's day (routing.cpp:3736, 3906-3919) */
         WU(11) += dailyActualUse;
-        WU(6) += remainingUse;
-        WU(0) = remainingUse;
+        if (wu->delayed) {   /* routing.cpp:3900-3905 */
+          WU(0) = remainingUse - prevTotalUnsat;
+          WU(6) = remainingUse;
+        } else {
+          WU(6) += remainingUse;
+          WU(0) = remainingUse;
+        }
         WU(4) = wu->wdr[wo + n];
         WU(5) = wu->cons[wo + n];
         if (wu->daily_actual) wu->daily_actual[(size_t)d * N + n] = dailyActualUse + nug;

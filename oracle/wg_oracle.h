@@ -190,6 +190,9 @@ typedef struct {
   const double *frgi;                    /* [ncell] G_fractreturngw_irrig                   */
   double *state;                         /* [WGO_WU_NSTATE*ncell]                           */
   double *daily_actual;                  /* optional [ndays*ncell]: actual NUs + NUg        */
+  int32_t delayed;                       /* 1: options.delayedUseSatisfaction (unmet demand
+                                            adds to the next day's, routing.cpp:2236-2244,
+                                            3900-3905)                                      */
 } wgo_wu_io;
 
 /* wgo_run with water use. */

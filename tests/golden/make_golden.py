@@ -114,7 +114,7 @@ def main_wtemp(names=None):
 
 
 # water use (options.subtract_use = 2, satisfied in the cell itself):
-# name -> (region factory, days, first day of year, snapshot days, water-use seed)
+# name -> (region factory, days, first day of year, snapshot days, water-use seed[, delayed])
 WU_CASES = {
     # two year ends (days 36 and 401): annualWaterUsePostProcessing and annualInit
     "swb_wuse_420d": (lambda: sy.region_small_swb(seed=21, ny=16, nx=32, block_at=(100, 300)), 420, 330,
@@ -122,6 +122,9 @@ WU_CASES = {
     # with fractional routing (the groundwater variants of routing.cpp:1986-2146 take NUg too)
     "swb_wuse_frac_200d": (lambda: sy.region_small_swb(seed=34, ny=16, nx=32, block_at=(150, 420))
                            .with_options(frac_routing=1), 200, 200, [166, 200], 17),
+    # delayed satisfaction (options.delayedUseSatisfaction = 1): unmet demand adds to the next day's
+    "swb_wuse_delayed_420d": (lambda: sy.region_small_swb(seed=21, ny=16, nx=32, block_at=(100, 300)), 420, 330,
+                              [36, 200, 401, 420], 13, True),
 }
 
 
@@ -129,7 +132,8 @@ def main_wuse(names=None):
     if not ref_case.available():
         if not ref_case.build():
             raise SystemExit("reference sources not found; cannot regenerate fixtures")
-    for name, (make, nd, doy0, snaps, seed) in WU_CASES.items():
+    for name, (make, nd, doy0, snaps, seed, *opt) in WU_CASES.items():
+        delayed = bool(opt and opt[0])
         if names and name not in names:
             continue
         region = make()
@@ -145,8 +149,9 @@ def main_wuse(names=None):
         outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
         stations = outl[:24]
         res = ref_case.run(region, P, T, S, doy0=doy0, stations=stations, snapshots=snaps,
-                           wuse=(nus, nug, wdr, cons, frgi))
+                           wuse=(nus, nug, wdr, cons, frgi), delayed=delayed)
         extra = dict(P=P, T=T, S=S, NUS=nus, NUG=nug, WDR=wdr, CONS=cons, FRGI=frgi, doy0=np.array(doy0),
+                     delayed=np.array(int(delayed)),
                      stations=res["stations"], snap_days=np.array(snaps), discharge=res["discharge"])
         for i, snap in enumerate(res["snapshots"]):
             snap.pop("snow_band")

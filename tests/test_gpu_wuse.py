@@ -29,7 +29,8 @@ def _use(ex):
 def _model(region, ex, **kw):
     from watergap2_gb300.gpu import Model
     nd, doy0 = ex["P"].shape[0], int(ex["doy0"])
-    m = Model(region, max_days=nd, stations=ex["stations"], water_use=True, **kw)
+    delayed = "delayed" in ex and bool(ex["delayed"])
+    m = Model(region, max_days=nd, stations=ex["stations"], water_use=2 if delayed else True, **kw)
     m.set_water_use_inputs(ex["FRGI"])
     m.upload_forcing(0, ex["P"], ex["T"], ex["S"])
     m.upload_water_use_run(0, doy0, nd, _use(ex))
@@ -51,14 +52,16 @@ def _check_snapshot(m, ex, i):
         e = _worst(st[f], ex[f"s{i}_{f}"], 1.0 if f.startswith("rf_") else 1e-9)
         if not e <= TOL:
             bad[f] = e
+    from test_wuse_oracle import WU_FLOOR
     for k, f in enumerate(WU_FIELDS):
-        e = _worst(wu[k], ex[f"s{i}_{f}"], 1e-9)
+        e = _worst(wu[k], ex[f"s{i}_{f}"], WU_FLOOR)
         if not e <= TOL:
             bad[f] = e
     assert not bad, (i, bad)
 
 
-@pytest.mark.parametrize("name", ["swb_wuse_420d", "swb_wuse_frac_200d"])   # the second with fractional routing
+@pytest.mark.parametrize("name", ["swb_wuse_420d", "swb_wuse_frac_200d",    # with fractional routing
+                                  "swb_wuse_delayed_420d"])                  # delayed satisfaction
 @pytest.mark.parametrize("kd", [1, 5])
 def test_water_use_matches_reference(name, kd):
     region, ex = _case(name)

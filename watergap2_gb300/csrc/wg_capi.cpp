@@ -705,7 +705,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->days_per_step < 0 || opt->days_per_step > 31) return WG_ERR_INVALID;
   if (opt->water_temp < 0 || opt->water_temp > 1) return WG_ERR_INVALID;
   if (opt->water_temp && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
-  if (opt->water_use < 0 || opt->water_use > 1) return WG_ERR_INVALID;
+  if (opt->water_use < 0 || opt->water_use > 2) return WG_ERR_INVALID;
   if (opt->water_use && opt->water_temp && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
@@ -986,6 +986,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->water_use) {
     st = setup_water_use(ctx.get(), r);
     if (st != WG_OK) return st;
+    ctx->wu.delayed = opt->water_use == 2;
   }
   const bool ens = ctx->members > 1;
   if (ctx->layout.idle_warp >= 0) ctx->threads = ctx->layout.threads;

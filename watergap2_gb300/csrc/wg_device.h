@@ -178,6 +178,7 @@ struct DevWaterUse {
   const double *frgi;         // [n] fraction of irrigation return flow into groundwater
   double *st;                 // [WU_NSTATE][N]
   int32_t enabled;
+  int32_t delayed;            // unmet demand adds to the next day's (delayedUseSatisfaction)
 };
 
 // Vertical balance of the cells without water bodies run by extra warps of the

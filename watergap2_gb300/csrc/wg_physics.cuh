@@ -544,6 +544,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   const R cfa = c.cfa[s];
   rt.p_ow = R(0); rt.e_ow = R(0); rt.leak = R(0);
   R remainingUse = R(0), dailyActualUse = R(0), remUseGL = R(0), remUseRes = R(0);
+  double prevTotalUnsat = 0.;
   double *W = nullptr;
   if constexpr (WU) {
     W = wu->st + si;
@@ -565,6 +566,11 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     netGWin -= R(nug);
     rt.e_ow += R(nug);
     remainingUse = R(wu->tab[wrow + s]);   // routing.cpp:2225-2290
+    if (wu->delayed) {   // routing.cpp:2236-2244
+      prevTotalUnsat = W[6 * NN];
+      remainingUse = R((double)remainingUse + prevTotalUnsat);
+      W[6 * NN] = 0.;
+    }
   }
   R gw = gw0 * c.gw_e[s] + c.gw_ik[s] * netGWin * c.gw_ome[s];
   if (cmp::abs_le_c(gw, R(WG_MIN_STOR_VOL))) gw = R(0);
@@ -902,8 +908,13 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     dailyActualUse += remRiver0 - remainingUse;
     // the cell's bookkeeping (routing.cpp:3736, 3906-3919)
     W[11 * NN] += (double)dailyActualUse;
-    W[6 * NN] += (double)remainingUse;
-    W[0] = (double)remainingUse;
+    if (wu->delayed) {   // routing.cpp:3900-3905
+      W[0] = (double)remainingUse - prevTotalUnsat;
+      W[6 * NN] = (double)remainingUse;
+    } else {
+      W[6 * NN] += (double)remainingUse;
+      W[0] = (double)remainingUse;
+    }
     W[4 * NN] = wu->tab[wrow + 2 * (size_t)c.n + s];
     W[5 * NN] = wu->tab[wrow + 3 * (size_t)c.n + s];
     if (doy == 365) wu_year_end(W, NN);

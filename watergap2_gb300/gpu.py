@@ -209,7 +209,7 @@ class Model:
     def __init__(self, region: Region, max_days: int = 366, stations=None, record_balance: bool = False,
                  device: int = 0, stream: int = 0, precision: str = "fp64", members: int = 1,
                  prec_factor=None, gamma_factor=None, block_threads: int = 0, ring_days: int = 0,
-                 days_per_step: int = 0, water_temp: bool = False, water_use: bool = False):
+                 days_per_step: int = 0, water_temp: bool = False, water_use: int | bool = False):
         self.lib = load_library()
         self.region = region
         self._keep = []
@@ -241,7 +241,7 @@ class Model:
         o.ring_days = int(ring_days)
         o.days_per_step = int(days_per_step)
         o.water_temp = int(bool(water_temp))
-        o.water_use = int(bool(water_use))
+        o.water_use = int(water_use)   # True/1; 2: delayed satisfaction
         self.max_days = int(max_days)
         h = ctypes.c_void_p()
         self._check(self.lib.wg_create(ctypes.byref(r), ctypes.byref(o), ctypes.byref(h)), "wg_create", None)
