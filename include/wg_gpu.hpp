@@ -159,6 +159,20 @@ class RoutingGpu {
   template <class AdditionalOutputInputFile>
   void updateLandAreaFrac(AdditionalOutputInputFile &) {}
 
+  // Water use (wg_options.water_use): in place of dailyNUInit (routing.cpp:884-976),
+  // the year's monthly net uses [12][ncell] in m3 as the yearly files hold them
+  // (M_NETABSSW / M_NETABSGW applied) for forcing slots fday0.. starting on day of
+  // year doy0; calcNextDay_M (routing.cpp:7405-7447) is the device's table row
+  // lookup, and annualWaterUsePostProcessing (routing.cpp:5246-5296) runs in the
+  // kernel on each cell's day 365, so both are no-ops here.
+  void dailyNUInit(int fday0, int ndays, int doy0, const double *nus_m3, const double *nug_m3,
+                   const double *irrig_withdrawal_sw_m3, const double *irrig_consumptive_sw_m3) {
+    ctx_.upload_water_use(fday0, ndays, doy0, nus_m3, nug_m3, irrig_withdrawal_sw_m3, irrig_consumptive_sw_m3);
+  }
+  void calcNextDay_M(const short /*month*/) {}
+  template <class AdditionalOutputInputFile>
+  void annualWaterUsePostProcessing(short /*year*/, AdditionalOutputInputFile &) {}
+
  private:
   Context &ctx_;
   int oday_ = 0;
