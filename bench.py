@@ -621,8 +621,9 @@ def run_profile_case(steps: int = 24, warm_steps: int = 200):
     exceed L2).  The warm-up call is launches 0-50 of k_vertical_ahead|k_pipeline
     (one vertical-ahead launch, 50 wavefront launches); the second call starts
     with its vertical-ahead launch (51) and wavefront launches that carry the
-    next chunk's vertical balance (52, 53, ...):
-      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 51 -c 3 python bench.py --profile"""
+    next chunk's vertical balance (52, 53, ...).  One kernel per capture:
+      ncu --set full --clock-control none -k regex:k_pipeline -s 50 -c 2 -o prof python bench.py --profile
+      ncu --set full --clock-control none -k regex:k_vertical_ahead -s 1 -c 1 -o prof python bench.py --profile"""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global()
@@ -649,7 +650,7 @@ def run_profile_wuse(steps: int = 24, warm_steps: int = 200):
     grid with water use (three years of synthetic tables), FP64,
     WAVEFRONT_DAYS days per wavefront step, default chunks of 4 steps, vertical
     overlap; launches as in run_profile_case:
-      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 51 -c 3 python bench.py --profile-wuse"""
+      ncu --set full --clock-control none -k regex:k_pipeline -s 50 -c 2 -o prof python bench.py --profile-wuse"""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global()
@@ -771,8 +772,9 @@ def run_profile_ensemble(members: int = 64, steps: int = 12, warm_steps: int = 2
     autotuner's choice on GB300), a 60-day ring so that the case holds ~2.5 GB
     on the device; a warm-up call of warm_steps steps (17 launch pairs) that
     fills the wavefront, then one call of `steps` steps (one
-    k_vertical_ahead<float,1> and one k_pipeline<float,1,1> launch):
-      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 34 -c 2 python bench.py --profile-ensemble"""
+    k_vertical_ahead<float,1> and one k_pipeline<float,1,1> launch), one kernel per capture:
+      ncu --set full --clock-control none -k regex:k_pipeline -s 17 -c 1 -o prof python bench.py --profile-ensemble
+      ncu --set full --clock-control none -k regex:k_vertical_ahead -s 17 -c 1 -o prof python bench.py --profile-ensemble"""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global()
@@ -802,7 +804,7 @@ def run_profile_wtemp(steps: int = 24, warm_steps: int = 200):
     (launches 0-50 of k_vertical_ahead|k_pipeline); the second call starts with
     its vertical-ahead launch (51) and wavefront launches that carry the next
     chunk's vertical balance (52, 53, ...):
-      ncu -k regex:"k_pipeline|k_vertical_ahead" -s 51 -c 3 python bench.py --profile-wtemp"""
+      ncu --set full --clock-control none -k regex:k_pipeline -s 50 -c 2 -o prof python bench.py --profile-wtemp"""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global().with_options(frac_routing=1)

@@ -281,15 +281,17 @@ wg_status wg_get_balance(wg_ctx *ctx, double out[6]);
 wg_status wg_reset_balance(wg_ctx *ctx);
 
 /* The same sums as wg_get_balance, for callers that cannot allocate device
- * memory after set-up -- for example a data-assimilation driver that runs its
- * cycles inside CUDA stream capture, or a process whose free device memory is
- * held by another framework's allocator.  No counterpart in the reference (it
- * has no balance check).  Allocates nothing: the per-block partial sums go to a
- * fixed 4 MiB device array inside the library, which limits the context to
+ * memory after set-up -- for example a process whose free device memory is held
+ * by another framework's caching allocator, or a driver that sizes every buffer
+ * at start and must not allocate afterwards.  No counterpart in the reference
+ * (it has no balance check).  Allocates nothing: the per-block partial sums go
+ * to a fixed 4 MiB device array inside the library, which limits the context to
  * 16,777,216 states (cells x members); larger contexts get WG_ERR_INVALID and a
- * message in wg_last_error.  The first call on a device looks up the array's
- * device address (make it before any stream capture).  All calls share the
- * array: calls that overlap on the GPU race.  Needs record_balance. */
+ * message in wg_last_error.  The call waits for the context's stream and copies
+ * the sums to `out`, so it is made outside CUDA stream capture.  The first call
+ * on a device looks up the array's device address (a failed lookup is retried
+ * by the next call).  All calls share the array: calls that overlap on the GPU
+ * race.  Needs record_balance. */
 wg_status wg_get_balance_noalloc(wg_ctx *ctx, double out[6]);
 
 /* Launch shape of the persistent kernels: threads per block (a multiple of 32

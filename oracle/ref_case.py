@@ -32,9 +32,11 @@ def available() -> bool:
     return os.path.exists(HARNESS)
 
 
-def build() -> bool:
-    src = os.environ.get("WG_REFERENCE_SOURCE", "/root/reference/source")
-    if not os.path.isdir(src):
+def build(src: str | None = None) -> bool:
+    """Compile the harness from the reference's sources in `src` (default: the
+    WG_REFERENCE_SOURCE environment variable); False where there are none."""
+    src = src or os.environ.get("WG_REFERENCE_SOURCE")
+    if not src or not os.path.isdir(src):
         return False
     subprocess.run(["make", "-s", "-C", _HERE, "-j8", "ref", f"REF={src}"], check=True)
     return True

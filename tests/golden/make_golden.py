@@ -25,6 +25,8 @@ from watergap2_gb300 import synthetic as sy  # noqa: E402
 from watergap2_gb300.region import save_npz  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference's sources (WG_REFERENCE_SOURCE, else the build container's mount)
+REF_SOURCE = os.environ.get("WG_REFERENCE_SOURCE") or "/root/reference/source"
 
 # name -> (region factory, days, first day of year, snapshot days)
 CASES = {
@@ -40,7 +42,7 @@ CASES = {
 
 def main(names=None):
     if not ref_case.available():
-        if not ref_case.build():
+        if not ref_case.build(REF_SOURCE):
             raise SystemExit("reference sources not found; cannot regenerate fixtures")
     for name, (make, nd, doy0, snaps) in CASES.items():
         if names and name not in names:
@@ -90,7 +92,7 @@ WT_CASES = {
 
 def main_wtemp(names=None):
     if not ref_case.available():
-        if not ref_case.build():
+        if not ref_case.build(REF_SOURCE):
             raise SystemExit("reference sources not found; cannot regenerate fixtures")
     for name, (make, nd, doy0, snaps) in WT_CASES.items():
         if names and name not in names:
@@ -130,7 +132,7 @@ WU_CASES = {
 
 def main_wuse(names=None):
     if not ref_case.available():
-        if not ref_case.build():
+        if not ref_case.build(REF_SOURCE):
             raise SystemExit("reference sources not found; cannot regenerate fixtures")
     for name, (make, nd, doy0, snaps, seed, *opt) in WU_CASES.items():
         delayed = bool(opt and opt[0])
@@ -169,7 +171,7 @@ def main_wtemp_wuse(names=None, name="swb_wtemp_wuse_120d"):
     if names and name not in names:
         return
     if not ref_case.available():
-        if not ref_case.build():
+        if not ref_case.build(REF_SOURCE):
             raise SystemExit("reference sources not found; cannot regenerate fixtures")
     region = wtemp_region(seed=21)
     nd, doy0, snaps = 120, 300, [66, 120]

@@ -23,6 +23,8 @@ sys.path.insert(0, ROOT)
 from oracle import ref_case  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference's sources (WG_REFERENCE_SOURCE, else the build container's mount)
+REF_SOURCE = os.environ.get("WG_REFERENCE_SOURCE") or "/root/reference/source"
 REF = os.path.join(ROOT, "oracle", "_ref", "wg_ref_wtemp")
 NIN = 73
 # field offsets of a record (calcWaterTempClass::transfer order)
@@ -126,7 +128,7 @@ def records(n, seed=7):
 
 def main(n=2000):
     if not os.path.exists(REF):
-        if not ref_case.build():
+        if not ref_case.build(REF_SOURCE):
             raise SystemExit("reference sources not found; cannot regenerate fixtures")
     rec = records(n)
     out = subprocess.run([REF], input=rec.astype("<f8").tobytes(), stdout=subprocess.PIPE, check=True).stdout

@@ -1,6 +1,7 @@
 """wg_get_balance_noalloc, the balance sums for callers that cannot allocate
-device memory (a driver running inside stream capture, or one whose device
-memory is held by another allocator), against wg_get_balance.
+device memory once set up (one whose free device memory is held by another
+framework's allocator, or one that sizes every buffer at start), against
+wg_get_balance.
 
 Collected last on purpose (file name), so that a failure here does not stop a
 -x run before the other tests.  Runs alone in a fresh process as well as after

@@ -2,12 +2,13 @@
 // wg_get_balance for callers that cannot allocate device memory.
 //
 // Who needs it: a caller whose device memory is owned by someone else once the
-// model is set up -- a data-assimilation driver that sizes every buffer at start
-// and runs its cycles inside CUDA stream capture, where cudaMalloc may not be
-// called, or a process whose free device memory is held by another framework's
-// caching allocator.  wg_get_balance itself reduces into a per-block scratch
-// buffer; this variant keeps that scratch in a fixed device array of this file,
-// so the call allocates nothing.
+// model is set up -- a host framework whose caching allocator holds the free
+// device memory, or a driver that sizes every buffer at start and must not
+// allocate afterwards.  wg_get_balance itself reduces into a per-block scratch
+// buffer it allocates; this variant keeps that scratch in a fixed device array of
+// this file, so the call allocates nothing.  The call still waits for the
+// context's stream and copies the six sums to the caller's host array, so it is
+// made outside CUDA stream capture.
 //
 // The array holds the partial sums of at most kNoallocMaxBlocks blocks of 256
 // states, i.e. contexts of at most 16,777,216 states (cells x members); larger
@@ -18,8 +19,9 @@
 // reads, so nothing needs clearing between calls.
 //
 // Host code must not use the array's name as a device address; the address is
-// taken with cudaGetSymbolAddress once per device, on the first call made on
-// that device (so make that first call before any stream capture).
+// taken with cudaGetSymbolAddress on the device, with that device current, on the
+// first call made on that device (a lookup that fails is not cached: the next
+// call tries again).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -37,8 +39,7 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoallocScratchDoubles
 
 constexpr int kMaxDevices = 64;
 static double *s_scratch[kMaxDevices];
-static cudaError_t s_scratch_err[kMaxDevices];
-static std::once_flag s_scratch_once[kMaxDevices];
+static std::mutex s_scratch_mutex;
 
 // Per-block partial sums, as k_balance_sum: 0 storage, 1 in, 2 evap, 3 outlet
 // outflow, 4 clamp corrections (each Neumaier-compensated), 5 largest relative
@@ -109,12 +110,19 @@ __global__ void __launch_bounds__(32) k_balance_final_static(double *scratch, in
 
 static cudaError_t noalloc_scratch(int device, double **out) {
   if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::call_once(s_scratch_once[device], [device]() {
-    // the caller has made `device` current
-    s_scratch_err[device] = cudaGetSymbolAddress((void **)&s_scratch[device], g_noalloc_scratch);
-  });
+  std::lock_guard<std::mutex> lock(s_scratch_mutex);
+  if (!s_scratch[device]) {
+    // the caller has made `device` current; only a successful lookup is kept
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      *out = nullptr;
+      return e;
+    }
+    s_scratch[device] = static_cast<double *>(p);
+  }
   *out = s_scratch[device];
-  return s_scratch_err[device];
+  return cudaSuccess;
 }
 
 int64_t noalloc_max_states() { return (int64_t)kNoallocMaxBlocks * kNoallocThreads; }
@@ -124,6 +132,10 @@ cudaError_t balance_noalloc(int device, const DevCellsT<R> &c, const DevStateT<R
                             const double *vol0, cudaStream_t st, double out[6]) {
   const size_t N = (size_t)c.n * M;
   if ((int64_t)N > noalloc_max_states()) return cudaErrorInvalidValue;
+  if (N == 0) {   // no states: every sum is zero (a launch of zero blocks is an error)
+    for (int k = 0; k < 6; ++k) out[k] = 0.;
+    return cudaSuccess;
+  }
   double *scratch = nullptr;
   cudaError_t e = noalloc_scratch(device, &scratch);
   if (e != cudaSuccess) return e;
