@@ -21,7 +21,6 @@ from __future__ import annotations
 
 import argparse
 import json
-import multiprocessing as mp
 import os
 import statistics
 import subprocess
@@ -67,24 +66,11 @@ def profile_figures(path=os.path.join(ROOT, "profiles", "fp64_global_wavefront_k
     return out
 
 
-def _forcing_block(args):
-    seed, y = args
-    from watergap2_gb300 import synthetic as sy
-    region = sy.region_global()
-    return sy.forcing(region, DAYS_PER_STEP, seed=seed, doy0=1, day_offset=y * DAYS_PER_STEP)
-
-
 def make_forcing(nyears, seed=2, procs=None):
-    """Forcing for nyears independent years, generated in parallel (spawned workers,
-    before any CUDA context exists)."""
-    procs = procs or min(nyears, os.cpu_count() or 1)
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(procs) as pool:
-        blocks = pool.map(_forcing_block, [(seed, y) for y in range(nyears)])
-    P = np.concatenate([b[0] for b in blocks])
-    T = np.concatenate([b[1] for b in blocks])
-    S = np.concatenate([b[2] for b in blocks])
-    return P, T, S
+    """Forcing for nyears years of the global grid, one year per spawned worker
+    (before any CUDA context exists)."""
+    from watergap2_gb300 import synthetic as sy
+    return sy.forcing_years("region_global", nyears, seed=seed, procs=procs)
 
 
 class ClockSampler:

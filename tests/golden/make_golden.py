@@ -20,6 +20,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 
+sys.path.insert(0, os.path.join(ROOT, "tests"))
 from oracle import ref_case  # noqa: E402
 from watergap2_gb300 import synthetic as sy  # noqa: E402
 from watergap2_gb300.region import save_npz  # noqa: E402
@@ -200,7 +201,92 @@ def main_wtemp_wuse(names=None, name="swb_wtemp_wuse_120d"):
     print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+# Workloads whose inputs are too large to store: the fixture keeps the seeds, a
+# digest of the regenerated inputs, and the reference's outputs -- the daily
+# discharge of a set of stations, every state field of a sample of cells, and
+# the exact sum over all cells of every state field at each snapshot.
+#   name -> (region factory, days, first day of year, forcing seed, snapshot days,
+#            cells sampled at the last snapshot: every k-th cell plus every cell
+#            with a water body (None: all cells), station choice)
+REGEN_CASES = {
+    # the 64 x 64 all-land region over a whole year (one outlet)
+    "config1_region64_365d": ("region_64x64", 365, 1, 2, [182, 365], None, "region64"),
+    # the global 0.5-degree grid, 67,420 cells, water bodies on, 120 days from 1 January
+    "config2_global_120d": ("region_global", 120, 1, 2, [60, 120], 16, "global"),
+}
+REGEN_KEYS = ["canopy", "soil", "snow", "lai_days", "lai_status", "lai_precsum", "gw", "river", "loclake",
+              "locwetl", "glolake", "glowetl", "res", "rf_loclake", "rf_locwetl", "rf_glolake", "rf_glowetl",
+              "rf_res", "laf", "laf_prev"]
+
+
+def regen_stations(region, kind, seed=5):
+    """Stations of a regenerated case: for the 64 x 64 region its outlet and every
+    64th cell of the routing order; on the global grid the 384 outlets with the
+    largest basins, 128 other outlets and 256 interior cells (seeded)."""
+    outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+    if kind == "region64":
+        return np.unique(np.concatenate([outl, region.rout_order[::64]])).astype(np.int32)
+    from watergap2_gb300.basins import dfs_order
+    order, tin, tout = dfs_order(region.downstream)
+    size = tout[outl] - tin[outl] + 1
+    big = outl[np.argsort(-size, kind="stable")[:384]]
+    rng = np.random.default_rng(seed)
+    rest = np.setdiff1d(outl, big)
+    other = rng.choice(rest, size=min(128, rest.size), replace=False)
+    interior = np.setdiff1d(np.arange(region.ncell), outl)
+    inner = rng.choice(interior, size=256, replace=False)
+    return np.unique(np.concatenate([big, other, inner])).astype(np.int32)
+
+
+def regen_sample(region, every):
+    if every is None:
+        return np.arange(region.ncell, dtype=np.int32)
+    a = region.arrays
+    wb = (a["loc_lake"] > 0) | (a["loc_wetl"] > 0) | (a["glo_wetl"] > 0) | (a["glo_lake"] > 0) | \
+         (a["glo_res"] > 0) | (a["lake_area"] > 0) | (a["res_area"] > 0)
+    keep = wb.copy()
+    keep[::every] = True
+    return np.nonzero(keep)[0].astype(np.int32)
+
+
+def regen_inputs(name):
+    """(region, P, T, S, doy0, snapshot days, sampled cells, stations) of a regenerated case."""
+    fac, nd, doy0, seed, snaps, every, kind = REGEN_CASES[name]
+    region = getattr(sy, fac)()
+    P, T, S = sy.forcing(region, nd, seed=seed, doy0=doy0)
+    return region, P, T, S, doy0, snaps, regen_sample(region, every), regen_stations(region, kind)
+
+
+def main_regen(names=None):
+    from helpers import field_sums, input_digest
+    if not ref_case.available():
+        if not ref_case.build(REF_SOURCE):
+            raise SystemExit("reference sources not found; cannot regenerate fixtures")
+    for name in REGEN_CASES:
+        if names and name not in names:
+            continue
+        region, P, T, S, doy0, snaps, sample, stations = regen_inputs(name)
+        res = ref_case.run(region, P, T, S, doy0=doy0, stations=stations, snapshots=snaps)
+        rep = ref_case.REF_BANDS // region.nband
+        out = dict(digest=np.array(input_digest(region, P, T, S)), stations=res["stations"],
+                   snap_days=np.array(snaps), discharge=res["discharge"], sample=sample,
+                   keys=np.array(REGEN_KEYS))
+        for i, snap in enumerate(res["snapshots"]):
+            bands = snap.pop("snow_band").reshape(region.ncell, region.nband, rep)
+            assert np.array_equal(bands, np.repeat(bands[:, :, :1], rep, axis=2))
+            snap["snow_band"] = bands[:, :, 0].copy()
+            out[f"s{i}_sums"] = field_sums(snap, REGEN_KEYS + ["snow_band"])
+            if i == len(snaps) - 1:
+                for k in REGEN_KEYS + ["snow_band", "k_release"]:
+                    out[f"s{i}_{k}"] = snap[k][sample]
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"{name}: {region.ncell} cells x {P.shape[0]} days, {sample.size} sampled cells, "
+              f"{len(stations)} stations -> {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 if __name__ == "__main__":
+    main_regen(sys.argv[1:])
     main(sys.argv[1:])
     main_wtemp(sys.argv[1:])
     main_wuse(sys.argv[1:])

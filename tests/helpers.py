@@ -29,3 +29,46 @@ def state_errors(got, ref, keys=STATE_KEYS, mask=None):
             g, r = g[mask], r[mask]
         out[k] = max_rel_err(g, r)
     return out
+
+
+def input_digest(region, *arrays) -> str:
+    """SHA-256 over a region's arrays (by name) and further input arrays: the
+    fixtures whose inputs are regenerated from their seeds record it, so that a
+    generator that draws differently on another host is reported as such."""
+    import hashlib
+    h = hashlib.sha256()
+    for k in sorted(region.arrays):
+        h.update(k.encode())
+        h.update(np.ascontiguousarray(region.arrays[k]).tobytes())
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def field_sums(state: dict, keys) -> np.ndarray:
+    """Exactly rounded sum over all cells of each state field (math.fsum)."""
+    import math
+    return np.array([math.fsum(np.asarray(state[k], np.float64).ravel().tolist()) for k in keys])
+
+
+REF_BANDS = 100   # the reference's snow elevation bands (daily.h:122)
+
+
+def ref_bound() -> float:
+    """Bound of the oracle against the reference's own outputs: bit for bit on
+    the x86-64 host that made the fixtures (the oracle run with the reference's
+    100 bands); elsewhere libm may round a transcendental differently in the
+    last place."""
+    import platform
+    return 0.0 if platform.machine() in ("x86_64", "AMD64") else 1e-12
+
+
+def rel_err(got, ref) -> float:
+    """Largest |got - ref| / |ref| (0/0 counts as 0; no floor)."""
+    got = np.asarray(got, np.float64).ravel()
+    ref = np.asarray(ref, np.float64).ravel()
+    if ref.size == 0:
+        return 0.0
+    d = np.abs(got - ref)
+    same = (d == 0) | (np.isnan(got) & np.isnan(ref))
+    return float(np.max(np.where(same, 0.0, d / np.maximum(np.abs(ref), 1e-300))))

@@ -1,12 +1,13 @@
 """The CPU oracle against the reference's own outputs (golden fixtures).
 
 The fixtures in tests/golden/ hold inputs and the results of the reference's
-calcNewDay/routing object code (made by tests/golden/make_golden.py).  The C
-restatement reproduces them bit for bit on the x86 host that made them; on
-other hosts libm may round differently in the last place, hence the 1e-12
-relative bound.  The fixtures were made with the reference's 100 bands (each of
-the 5 synthetic bands replicated 20 times); the restatement runs the 5 bands, so
-band sums differ from the reference's only in rounding.
+calcNewDay/routing object code (made by tests/golden/make_golden.py); the
+workloads too large to store keep their seeds, a digest of the regenerated
+inputs and the reference's outputs.  The reference runs 100 snow bands (each of
+the 5 synthetic bands replicated 20 times); the oracle, run with the same 100
+bands, reproduces every output bit for bit on the x86-64 host that made the
+fixtures (elsewhere libm may round a transcendental differently in the last
+place: 1e-12 relative).
 """
 import glob
 import os
@@ -18,17 +19,11 @@ from oracle import Oracle
 from watergap2_gb300.region import load_npz
 
 FIXTURES = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                  if not ({"wtemp", "wuse"} & set(os.path.basename(p)[:-4].split("_"))))   # test_wtemp_oracle.py, test_wuse_oracle.py
+                  if not ({"wtemp", "wuse"} & set(os.path.basename(p)[:-4].split("_")))
+                  and not os.path.basename(p).startswith("config"))   # regenerated workloads: own tests   # test_wtemp_oracle.py, test_wuse_oracle.py
 STATE_KEYS = ["canopy", "soil", "snow", "lai_days", "lai_status", "lai_precsum", "gw", "river", "loclake",
               "locwetl", "glolake", "glowetl", "res", "rf_loclake", "rf_locwetl", "rf_glolake", "rf_glowetl",
               "rf_res", "k_release", "laf", "laf_prev"]
-
-
-def rel_err(a, b, floor=1e-30):
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
-    scale = np.maximum(np.abs(b), floor)
-    return float(np.max(np.abs(a - b) / scale)) if a.size else 0.0
 
 
 def test_fixtures_present():
@@ -37,11 +32,14 @@ def test_fixtures_present():
 
 @pytest.mark.parametrize("path", FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
 def test_oracle_matches_reference(path):
+    from helpers import REF_BANDS, ref_bound, rel_err
     region, ex = load_npz(path)
     P, T, S = ex["P"], ex["T"], ex["S"]
     doy0 = int(ex["doy0"])
     snaps = [int(x) for x in ex["snap_days"]]
-    o = Oracle(region)
+    rep = REF_BANDS // region.nband
+    o = Oracle(region.with_bands(REF_BANDS))
+    bound = ref_bound()
     q_all = []
     day = 0
     doy = doy0
@@ -56,14 +54,11 @@ def test_oracle_matches_reference(path):
             if k == "k_release":   # only defined in reservoir cells (routing.cpp:443-446)
                 m = region.res_area > 0
                 ref, got = ref[m], got[m]
-            # tiny storages are compared absolutely (km3 / mm near the 1e-15 snapping limit)
-            err = np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-9)) if ref.size else 0.0
-            assert err <= 1e-12, (k, err)
-        got_b = o.state["snow_band"].reshape(region.ncell, region.nband)
-        assert np.max(np.abs(got_b - ex[f"s{i}_snow_band"]) / np.maximum(np.abs(ex[f"s{i}_snow_band"]), 1e-9)) <= 1e-12
+            assert rel_err(got, ref) <= bound, k
+        got_b = o.state["snow_band"].reshape(region.ncell, region.nband, rep)[:, :, 0]
+        assert rel_err(got_b, ex[f"s{i}_snow_band"]) <= bound
     q = np.concatenate(q_all)[:, ex["stations"]]
-    ref_q = ex["discharge"][: q.shape[0]]
-    assert np.max(np.abs(q - ref_q) / np.maximum(np.abs(ref_q), 1e-12)) <= 1e-12
+    assert rel_err(q, ex["discharge"][: q.shape[0]]) <= bound
 
 
 @pytest.mark.parametrize("path", FIXTURES[:2], ids=lambda p: os.path.basename(p)[:-4])
@@ -73,3 +68,52 @@ def test_oracle_mass_balance_closes(path):
     _, b = o.run(int(ex["doy0"]), ex["P"], ex["T"], ex["S"], balance=True)
     resid = np.abs(b[:, 5])
     assert np.max(resid / b[:, 0]) < 1e-12
+
+
+def _regen_module():
+    import importlib.util
+    path = os.path.join(os.path.dirname(__file__), "golden", "make_golden.py")
+    spec = importlib.util.spec_from_file_location("make_golden", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+REGEN = ["config1_region64_365d", "config2_global_120d"]
+
+
+@pytest.mark.parametrize("name", REGEN)
+def test_oracle_matches_reference_on_workload(name):
+    """The 64 x 64 region over a year and the 67,420-cell global grid with every
+    kind of water body over 120 days, inputs regenerated from their seeds: the
+    oracle, run with the reference's 100 snow bands (each of the 5 synthetic
+    bands 20 times), against the reference's stations, sampled cells and exact
+    sums over all cells -- bit for bit."""
+    from helpers import REF_BANDS, field_sums, input_digest, ref_bound, rel_err
+    mg = _regen_module()
+    ex = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{name}.npz"))
+    region, P, T, S, doy0, snaps, sample, stations = mg.regen_inputs(name)
+    if input_digest(region, P, T, S) != str(ex["digest"]):
+        pytest.fail(f"{name}: the seeded generators drew different inputs on this host (numpy {np.__version__})")
+    assert np.array_equal(stations, ex["stations"]) and np.array_equal(sample, ex["sample"])
+    keys = [str(k) for k in ex["keys"]]
+    rep = REF_BANDS // region.nband
+    o = Oracle(region.with_bands(REF_BANDS))
+    bound = ref_bound()
+    q_all, day, doy = [], 0, doy0
+    for i, sd in enumerate(snaps):
+        q, _ = o.run(doy, P[day:sd], T[day:sd], S[day:sd], discharge=True, nthreads=os.cpu_count() or 1)
+        q_all.append(q[:, stations])
+        doy = (doy - 1 + (sd - day)) % 365 + 1
+        day = sd
+        bands = o.state["snow_band"].reshape(region.ncell, region.nband, rep)
+        st = dict(o.state, snow_band=bands[:, :, 0])
+        assert rel_err(field_sums(st, keys + ["snow_band"]), ex[f"s{i}_sums"]) <= bound, i
+        if f"s{i}_soil" in ex:
+            for k in keys + ["snow_band", "k_release"]:
+                ref, got = ex[f"s{i}_{k}"], st[k][sample]
+                if k == "k_release":   # only defined in reservoir cells (routing.cpp:443-446)
+                    m = region.res_area[sample] > 0
+                    ref, got = ref[m], got[m]
+                assert rel_err(got, ref) <= bound, k
+    assert rel_err(np.concatenate(q_all), ex["discharge"]) <= bound

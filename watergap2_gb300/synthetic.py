@@ -503,6 +503,24 @@ def forcing(region: Region, ndays: int, seed: int = 2, doy0: int = 1, day_offset
     return P, T, S
 
 
+def _forcing_year(args):
+    factory, seed, y = args
+    region = globals()[factory]()
+    return forcing(region, 365, seed=seed, doy0=1, day_offset=y * 365)
+
+
+def forcing_years(factory: str, nyears: int, seed: int = 2, procs: int | None = None):
+    """forcing(region, 365 * nyears, seed, doy0=1) of the region that the
+    generator `factory` (e.g. "region_global") makes with its defaults, one year
+    per spawned worker (safe after a CUDA context exists in the caller); the same
+    numbers as one forcing() call."""
+    import multiprocessing as mp
+    procs = procs or max(1, min(nyears, os.cpu_count() or 1))
+    with mp.get_context("spawn").Pool(procs) as pool:
+        blocks = pool.map(_forcing_year, [(factory, seed, y) for y in range(nyears)])
+    return tuple(np.concatenate([b[k] for b in blocks]) for k in range(3))
+
+
 def _forcing_chunk(args):
     """Worker of forcing_parallel: cells [c0, c1) of year block blk into shared memory."""
     from multiprocessing import shared_memory
