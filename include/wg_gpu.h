@@ -17,12 +17,15 @@
  * the library's own kernels (an exceeded wait, an inconsistent topology) come
  * back as status codes, never as traps.
  *
- * Option set (the reference's optionClass, source/option.h): time_series=1,
- * cloud=2, petOpt=0, intercept=1, use_kc=0, calc_albedo=0, clclOpt=0,
- * subtract_use=0, use_alloc=0, fractionalRoutingOpt=0, aridareaOpt=0,
- * riverEvapoOpt=0, statcorrOpt=0, glacierOpt=0, calc_wtemp=0, antNatOpt=0,
- * resYearOpt=0, riverveloOpt 0/1/2.  Other option values are out of scope and
- * rejected with WG_ERR_UNSUPPORTED.
+ * Option set (the reference's optionClass, source/option.h:43-68), given by
+ * wg_model_options (wg_options.model) and the region: time_series=1, cloud=2,
+ * petOpt=0, intercept=1, use_kc=0, calc_albedo=0, clclOpt=0, permaOpt=0,
+ * glacierOpt=0, landCoverOpt=0, aridareaOpt=0, riverEvapoOpt=0, statcorrOpt 0/1,
+ * use_alloc=0, aggrNUsGloLakResOpt=0, antNatOpt=0, resYearOpt=0, resOpt 0/1,
+ * climate_spatial_resolution=0, riverveloOpt 0/1/2, fractionalRoutingOpt 0/1,
+ * subtract_use 0/2 with delayedUseSatisfaction 0/1 and calc_wtemp 0/1
+ * (wg_options.water_use, water_temp).  Other option values are out of scope
+ * and rejected with WG_ERR_UNSUPPORTED; wg_last_error(NULL) names the option.
  */
 #ifndef WG_GPU_H
 #define WG_GPU_H
@@ -92,6 +95,46 @@ typedef struct wg_state_view {
   int32_t *laf_started;
 } wg_state_view;
 
+/* The reference's model switches (optionClass members, source/option.h:43-68;
+ * the option file's values, option.cpp:125-165 and 400-600) as a caller that
+ * runs the reference has them.  wg_create refuses every value outside the built
+ * set with WG_ERR_UNSUPPORTED, so a configuration the library does not compute
+ * never runs silently as a different model.  wg_model_options_default fills
+ * the built defaults (the values in brackets). */
+typedef struct wg_model_options {
+  int32_t time_series;         /* [1] daily forcing from the yearly .365 grids (daily.cpp:194-248) */
+  int32_t cloud;               /* [2] net longwave from the extraterrestrial radiation, no
+                                  longwave or cloud forcing (daily.cpp:203, 241, 412-440) */
+  int32_t intercept;           /* [1] canopy interception (daily.cpp:825-895)             */
+  int32_t calc_albedo;         /* [0] land-cover albedo table (daily.cpp:369-380, 1679)   */
+  int32_t use_kc;              /* [0] no crop coefficient on PET (daily.cpp:373, 768)     */
+  int32_t pet_opt;             /* [0] Priestley-Taylor PET (daily.cpp:208, 272, 489-725)  */
+  int32_t clcl_opt;            /* [0] no climate-land-cover classification (daily.cpp:273, 303) */
+  int32_t perma_opt;           /* [0] no permafrost input (integrateWGHM.cpp:578-604)     */
+  int32_t glacier_opt;         /* [0] no glacier input (daily.cpp:2063, routing.cpp:617, 811) */
+  int32_t land_cover_opt;      /* [0] one land-cover map for the run (integrateWGHM.cpp:530-549) */
+  int32_t arid_area_opt;       /* [0] no arid-area groundwater routing (routing.cpp:1924-2059,
+                                  2392, 3305)                                               */
+  int32_t river_evapo_opt;     /* [0] no river evaporation (routing.cpp:3441, 3546, 4562)  */
+  int32_t statcorr_opt;        /* [0] or 1: each cell's outflow multiplied by its station
+                                  correction factor G_statCorrFact, the calibration
+                                  parameter P_CFS of wg_region.param (routing.cpp:3929-3931) */
+  int32_t use_alloc;           /* [0] no second-cell allocation of unmet water use
+                                  (routing.cpp:2249-2271)                                 */
+  int32_t aggr_nus_glo_lak_res_opt;  /* [0] no aggregation of water use over a global lake's
+                                        riparian cells (routing.cpp:926-971)               */
+  int32_t ant_nat_opt;         /* [0] anthropogenic run (routing.cpp:435-440)             */
+  int32_t res_year_opt;        /* [0] reservoirs by the reference year (routing.cpp:1054-1072,
+                                  5670)                                                   */
+  int32_t res_opt;             /* [1] reservoir algorithm; 0 only for a region without
+                                  reservoir cells (the reference then treats regulated
+                                  lakes as global lakes, routing.cpp:411-430)            */
+  int32_t climate_spatial_resolution;   /* [0] the standard land mask (geo.cpp:65,
+                                           integrateWGHM.cpp:474-478)                     */
+} wg_model_options;
+
+void wg_model_options_default(wg_model_options *opt);
+
 typedef struct wg_options {
   int32_t device;          /* CUDA device ordinal                                     */
   int32_t max_days;        /* capacity of the device forcing buffer, in days          */
@@ -133,6 +176,8 @@ typedef struct wg_options {
                               count (with water_temp: FP64, one member); the
                               members share the tables.  Tables by
                               wg_upload_water_use (days without one: no use)      */
+  const wg_model_options *model;   /* the reference's model switches; NULL = the defaults
+                              of wg_model_options_default                          */
 } wg_options;
 
 typedef struct wg_ctx wg_ctx;
@@ -433,6 +478,7 @@ wg_status wg_math_eval(int32_t device, int32_t fn, const double *x, const double
  * launches issued so far, and the last CUDA error string. */
 int32_t wg_num_levels(const wg_ctx *ctx);
 int64_t wg_launch_count(const wg_ctx *ctx);
+/* wg_last_error(NULL): why the calling thread's last wg_create failed. */
 const char *wg_last_error(const wg_ctx *ctx);
 const char *wg_status_string(wg_status s);
 

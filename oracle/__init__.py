@@ -34,6 +34,7 @@ _STATIC_FIELDS = [
     ("start_month", ctypes.c_void_p),
     ("river_length", ctypes.c_void_p), ("river_slope", ctypes.c_void_p), ("roughness", ctypes.c_void_p),
     ("bankfull", ctypes.c_void_p), ("downstream", ctypes.c_void_p), ("rout_order", ctypes.c_void_p),
+    ("statcorr_opt", ctypes.c_int32),
 ]
 
 _STATE_ORDER = ["canopy", "soil", "snow", "snow_band", "lai_days", "lai_status", "lai_precsum",
@@ -86,6 +87,7 @@ def lib():
         _lib.wgo_run.argtypes = [ctypes.POINTER(_Static), ctypes.POINTER(_State), ctypes.c_int, ctypes.c_int,
                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                  ctypes.c_void_p, ctypes.c_int]
+        _lib.wgo_last_timing.argtypes = [ctypes.c_void_p]
         _lib.wgo_bottom_width.argtypes = [ctypes.c_double]
         _lib.wgo_bottom_width.restype = ctypes.c_double
         _lib.wgo_wtemp_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
@@ -129,10 +131,11 @@ class Oracle:
         st.ncell, st.nband = region.ncell, region.nband
         st.river_velo_opt, st.default_velocity = region.river_velo_opt, region.default_velocity
         st.frac_routing = int(getattr(region, "frac_routing", 0))
-        for name, ctype in _STATIC_FIELDS[5:]:
+        for name, ctype in _STATIC_FIELDS[5:-1]:
             a = region.arrays[name]
             self._keep.append(a)
             setattr(st, name, a.ctypes.data)
+        st.statcorr_opt = int(getattr(region, "statcorr_opt", 0))
         self._static = st
         self.state = empty_state(region.ncell, region.nband)
         self._cstate = _State()
@@ -256,3 +259,10 @@ class Oracle:
         if rc:
             raise RuntimeError(f"wgo_run failed: {rc}")
         return q, b
+
+    @staticmethod
+    def last_timing() -> dict:
+        """Wall time of the vertical and the routing pass of the last run."""
+        out = np.zeros(2)
+        lib().wgo_last_timing(_ptr(out))
+        return {"vertical_s": float(out[0]), "routing_s": float(out[1])}

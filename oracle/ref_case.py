@@ -175,14 +175,16 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
     with open(f"{d}/meta.txt", "w") as f:
         f.write(f"{n} {P.shape[0]} {doy0} {year0} {resopt} {region.river_velo_opt} {len(stations)} {len(snapshots)} "
                 f"{0 if wtemp is None else 1} {int(getattr(region, 'frac_routing', 0))} "
-                f"{0 if wuse is None else (2 if delayed else 1)}\n")
+                f"{0 if wuse is None else (2 if delayed else 1)} {int(getattr(region, 'statcorr_opt', 0))}\n")
     with open(f"{d}/snapshots.txt", "w") as f:
         f.write(" ".join(str(int(s)) for s in snapshots) + "\n")
 
 
-def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wtemp=None, wuse=None, delayed=False):
+def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wtemp=None, wuse=None, delayed=False,
+        threads=1):
     """Run the reference harness; returns dict(lai_a, lai_b, bottom_width, snapshots=[{field: array}],
-    discharge=[ndays, nstation], stations=...)."""
+    discharge=[ndays, nstation], stations=..., timing=dict(threads, vertical_s, routing_s)): the vertical
+    pass on `threads` OpenMP threads, routing serial, as integrate_wghm_ runs them."""
     if not available():
         raise RuntimeError("reference harness not built (make -C oracle ref)")
     ndays = P.shape[0]
@@ -195,7 +197,8 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
     tmp = workdir or tempfile.mkdtemp(prefix="wg_ref_")
     write_case(region, tmp, P, T, S, doy0, stations, snapshots, wtemp=wtemp, wuse=wuse, delayed=delayed)
     out = os.path.join(tmp, "out.bin")
-    subprocess.run([HARNESS, tmp, out], check=True, stdout=subprocess.DEVNULL)
+    env = dict(os.environ, WG_REF_THREADS=str(int(threads)))
+    subprocess.run([HARNESS, tmp, out], check=True, stdout=subprocess.DEVNULL, env=env)
     raw = np.fromfile(out, np.float64)
     o = 0
     res = {"lai_a": raw[o:o + 18].copy(), "lai_b": raw[o + 18:o + 36].copy()}
@@ -224,4 +227,7 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
         o += ndays * len(stations)
     assert o == raw.size, (o, raw.size)
     res["stations"] = stations
+    with open(os.path.join(tmp, "timing.txt")) as f:
+        th, tv, tr = f.read().split()[:3]
+    res["timing"] = {"threads": int(th), "vertical_s": float(tv), "routing_s": float(tr)}
     return res

@@ -29,6 +29,8 @@
 #include <set>
 #include <list>
 #include <functional>
+#include <chrono>
+#include <omp.h>
 // The harness needs write access to a few members the reference keeps private
 // (laiClass::G_LAImax, calibParamClass::calibParamJson, LAI state for the dump).
 #define private public
@@ -56,7 +58,7 @@ static void write_raw(FILE *f, const double *p, size_t n) { fwrite(p, sizeof(dou
 int main(int argc, char **argv) {
   if (argc < 3) { fprintf(stderr, "usage: %s <case dir> <out file>\n", argv[0]); return 1; }
   std::string dir = argv[1];
-  int ncase, ndays, doy0, year0, resopt, velo, nstation, nsnap, wtemp = 0, frac = 0, wuse = 0;
+  int ncase, ndays, doy0, year0, resopt, velo, nstation, nsnap, wtemp = 0, frac = 0, wuse = 0, statcorr = 0;
   {
     std::ifstream m(dir + "/meta.txt");
     m >> ncase >> ndays >> doy0 >> year0 >> resopt >> velo >> nstation >> nsnap;
@@ -64,6 +66,7 @@ int main(int argc, char **argv) {
     if (!(m >> wtemp)) wtemp = 0;   // optional: water temperature (options.calc_wtemp)
     if (!(m >> frac)) frac = 0;     // optional: options.fractionalRoutingOpt
     if (!(m >> wuse)) wuse = 0;     // optional: water use (options.subtract_use = 2)
+    if (!(m >> statcorr)) statcorr = 0;   // optional: options.statcorrOpt
   }
   std::vector<int> snap_days(nsnap);
   {
@@ -79,7 +82,7 @@ int main(int argc, char **argv) {
   options.rout_prepare = 0; options.timeStepCheckFlag = 0; options.riverveloOpt = velo; options.time_series = 1;
   options.subtract_use = 0; options.use_alloc = 0; options.delayedUseSatisfaction = 0; options.petOpt = 0;
   options.clclOpt = 0; options.permaOpt = 0; options.resOpt = resopt; options.landCoverOpt = 0; options.use_kc = 0;
-  options.statcorrOpt = 0; options.aridareaOpt = 0; options.fractionalRoutingOpt = frac; options.riverEvapoOpt = 0;
+  options.statcorrOpt = statcorr; options.aridareaOpt = 0; options.fractionalRoutingOpt = frac; options.riverEvapoOpt = 0;
   options.aggrNUsGloLakResOpt = 0; options.climate_spatial_resolution = 0; options.resYearOpt = 0;
   options.resYearReference = 2000; options.resYearFirstToUse = 1900; options.resYearLastToUse = 2010;
   options.antNatOpt = 0; options.resNUsMeanYearFirst = 1971; options.resNUsMeanYearLast = 2000;
@@ -182,6 +185,15 @@ int main(int argc, char **argv) {
     wt_daily.assign((size_t)ndays * nstation, 0.0);
   }
 
+  // the vertical pass runs the reference's OpenMP cell loop (integrateWGHM.cpp:767-783)
+  // on WG_REF_THREADS threads (default 1); routing is serial as in the reference.
+  // Wall time of each pass goes to <case dir>/timing.txt (the CPU baseline).
+  int nthreads = 1;
+  if (const char *e = getenv("WG_REF_THREADS")) nthreads = std::max(1, atoi(e));
+  omp_set_num_threads(nthreads);
+  using clk = std::chrono::steady_clock;
+  double t_vert = 0., t_rout = 0.;
+
   int year = year0;
   int doy = doy0;
   int snap_i = 0;
@@ -208,14 +220,20 @@ int main(int argc, char **argv) {
         climate.G_longwave_d(n, day_in_month - 1) = LW[(size_t)d * ncase + n];
         climate.G_temperature_d(n, day_in_month - 1) = T[(size_t)d * ncase + n];
       }
+    const auto c0 = clk::now();
+#pragma omp parallel for if (nthreads > 1)
     for (int n = 0; n < ng; ++n)
       if (geo.G_contcell[n])
         dailyWaterBalance.calcNewDay((short)doy, (short)month, day_in_month, last_day_in_month[month], (short)year, n,
                                      wghmState, additionalOutIn, snowIO, 0, calibParam);
+    const auto c1 = clk::now();
     if (wuse) routing.calcNextDay_M(month);   // integrateWGHM.cpp:794-796
     routing.routing((short)year, (short)doy, (short)month, day_in_month, last_day_in_month[month], wghmState,
                     additionalOutIn, 0, calibParam);
     routing.updateLandAreaFrac(additionalOutIn);
+    const auto c2 = clk::now();
+    t_vert += std::chrono::duration<double>(c1 - c0).count();
+    t_rout += std::chrono::duration<double>(c2 - c1).count();
     // end of the year (integrateWGHM.cpp:940-944), before the day's snapshot
     if (wuse && doy == 365) routing.annualWaterUsePostProcessing((short)year, additionalOutIn);
     for (int b = 0; b < nstation; b++) q[(size_t)d * nstation + b] = routing.dailyRiverDischarge(b, doy - 1);
@@ -287,5 +305,9 @@ int main(int argc, char **argv) {
   write_raw(out, q.data(), q.size());
   if (wtemp) write_raw(out, wt_daily.data(), wt_daily.size());
   fclose(out);
+  if (FILE *tf = fopen((dir + "/timing.txt").c_str(), "w")) {
+    fprintf(tf, "%d %.9f %.9f %d %d\n", nthreads, t_vert, t_rout, ndays, ncase);
+    fclose(tf);
+  }
   return 0;
 }

@@ -534,6 +534,22 @@ typedef struct {
   double glowetl_prev, glowetl_evapo, glowetl_rf, glowetl_out;
 } wt_route;
 
+/* wall time of the passes of the last run (the CPU baseline's split) */
+static double g_time_vertical, g_time_routing;
+
+void wgo_last_timing(double out[2]) {
+  out[0] = g_time_vertical;
+  out[1] = g_time_routing;
+}
+
+static double wall_now(void) {
+#ifdef _OPENMP
+  return omp_get_wtime();
+#else
+  return 0.;
+#endif
+}
+
 static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
                     const float *temp, const float *swrad, double *discharge, double *balance, int nthreads,
                     wgo_wt_io *wt, wgo_wu_io *wu);
@@ -733,6 +749,7 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
 #else
   (void)nthreads;
 #endif
+  g_time_vertical = g_time_routing = 0.;
   double s_prev = 0.;
   if (balance)
     for (int n = 0; n < N; n++) s_prev += state_volume(s, st, n);
@@ -743,8 +760,11 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
     while (month < 11 && day >= first_day_in_month[month + 1]) month++;
     const float *P = prec + (size_t)d * N, *T = temp + (size_t)d * N, *SW = swrad + (size_t)d * N;
     /* vertical pass: the reference's OpenMP cell loop (integrateWGHM.cpp:767-783) */
+    const double w0 = wall_now();
 #pragma omp parallel for schedule(static) if (nthreads > 1)
     for (int n = 0; n < N; n++) vertical_cell(s, st, n, day, (double)P[n], (double)T[n], (double)SW[n], &vo[n]);
+    const double w1 = wall_now();
+    g_time_vertical += w1 - w0;
 
     double b_in = 0., b_evap = 0., b_out = 0., b_leak = 0.;
     double *W = wu ? wu->state : NULL;
@@ -1155,6 +1175,11 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         WU(5) = wu->cons[wo + n];
         if (wu->daily_actual) wu->daily_actual[(size_t)d * N + n] = dailyActualUse + nug;
       }
+      if (s->statcorr_opt == 1) {   /* station correction, routing.cpp:3929-3931 */
+        const double before = transportedVolume;
+        transportedVolume *= PAR(s, WGO_P_CFS, n);
+        leak += transportedVolume - before;   /* water the correction adds (removes) */
+      }
       /* push downstream, routing.cpp:3955-3958 */
       const int down = s->downstream[n];
       if (down >= 0) inflow_up[down] += transportedVolume;
@@ -1207,6 +1232,7 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         }
       }
 #undef WU
+    g_time_routing += wall_now() - w1;
     if (balance) {
       double stot = 0.;
       for (int n = 0; n < N; n++) stot += state_volume(s, st, n);

@@ -82,6 +82,9 @@ typedef struct {
   /* topology                                                                  */
   const int32_t *downstream;  /* 0-based, -1 outlet / sink                      */
   const int32_t *rout_order;  /* cells in processing order (G_routingCell-1)   */
+  int32_t statcorr_opt;       /* options.statcorrOpt: 1 multiplies each cell's
+                                 outflow by its G_statCorrFact = P_CFS
+                                 (routing.cpp:3929-3931)                       */
 } wgo_static;
 
 /* Dynamic state, caller-owned, updated in place. */
@@ -203,6 +206,10 @@ int wgo_run_wu(const wgo_static *s, wgo_state *st, int doy0, int ndays,
 int wgo_run_wt_wu(const wgo_static *s, wgo_state *st, int doy0, int ndays,
                   const float *prec, const float *temp, const float *swrad,
                   double *discharge, double *balance, int nthreads, wgo_wt_io *wt, wgo_wu_io *wu);
+
+/* Wall time [s] of the vertical pass and of the routing pass of the last run
+ * (out[0], out[1]): the CPU baseline's split. */
+void wgo_last_timing(double out[2]);
 
 #ifdef __cplusplus
 }

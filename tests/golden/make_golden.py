@@ -38,7 +38,20 @@ CASES = {
     # fractional routing (options.fractionalRoutingOpt = 1) on a block of the 0.5-degree grid
     "swb_frac_150d": (lambda: sy.region_small_swb(seed=33, block_at=(150, 420)).with_options(frac_routing=1),
                       150, 60, [75, 150]),
+    # station correction (options.statcorrOpt = 1): outflow x P_CFS (routing.cpp:3929-3931)
+    "swb_statcorr_120d": (lambda: statcorr_region(seed=22), 120, 150, [60, 120]),
 }
+
+
+def statcorr_region(seed=22):
+    """A region with every water-body type whose cells carry station correction
+    factors P_CFS: 1 in most cells (as the reference sets them outside its
+    calibration stations), U(0.6, 1.4) in every fifth cell."""
+    region = sy.region_small_swb(seed=seed, block_at=(120, 200))
+    rng = np.random.default_rng(seed + 100)
+    f = np.ones(region.ncell)
+    f[::5] = rng.uniform(0.6, 1.4, f[::5].size)
+    return region.with_param("P_CFS", f).with_options(statcorr_opt=1)
 
 
 def main(names=None):

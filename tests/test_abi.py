@@ -9,7 +9,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "wg_gpu.h")
 MLP_HEADER = os.path.join(ROOT, "include", "wg_mlp.h")
-PATTERN = r"^\s*(?:wg_status|int32_t|int64_t|const char \*)\s*(wg_\w+)\s*\("
+PATTERN = r"^\s*(?:wg_status|int32_t|int64_t|void|const char \*)\s*(wg_\w+)\s*\("
 
 
 def declared_symbols(header=HEADER):

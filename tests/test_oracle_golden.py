@@ -117,3 +117,13 @@ def test_oracle_matches_reference_on_workload(name):
                     ref, got = ref[m], got[m]
                 assert rel_err(got, ref) <= bound, k
     assert rel_err(np.concatenate(q_all), ex["discharge"]) <= bound
+
+
+def test_station_correction_fixture_changes_discharge():
+    """The statcorrOpt fixture exercises the correction: without it the oracle's
+    station discharge differs from the reference's."""
+    region, ex = load_npz(os.path.join(os.path.dirname(__file__), "golden", "swb_statcorr_120d.npz"))
+    assert region.statcorr_opt == 1 and np.any(region.param("P_CFS") != 1.0)
+    o = Oracle(region.with_options(statcorr_opt=0).with_bands(100))
+    q, _ = o.run(int(ex["doy0"]), ex["P"], ex["T"], ex["S"], discharge=True)
+    assert not np.allclose(q[:, ex["stations"]], ex["discharge"], rtol=1e-6)

@@ -260,6 +260,7 @@ struct HostConsts {
 #undef X
   std::vector<double> band_dt;   // [ncell][nband]
   std::vector<double> ext, inv_s0;
+  std::vector<double> statcorr;  // G_statCorrFact (P_CFS) with statcorrOpt = 1, else empty
   int nrow = 0;
 };
 
@@ -428,6 +429,7 @@ wg_status upload_cells(wg_ctx *ctx, const HostConsts &h, DevCellsT<R> &c, double
   c.offset = upload_raw<int32_t>(ctx, off_slot, st);
   c.up_ptr = upload_raw<int32_t>(ctx, ctx->topo.up_ptr, st);
   c.up_idx = upload_raw<int32_t>(ctx, ctx->topo.up_idx, st);
+  c.statcorr = h.statcorr.empty() ? nullptr : upload_slots<R>(ctx, h.statcorr, st);
   return st;
 }
 
@@ -607,7 +609,19 @@ const char *wg_status_string(wg_status s) {
   return "unknown";
 }
 
-const char *wg_last_error(const wg_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
+// why the calling thread's last wg_create failed (wg_last_error(NULL))
+thread_local std::string t_create_err;
+
+const char *wg_last_error(const wg_ctx *ctx) { return ctx ? ctx->err.c_str() : t_create_err.c_str(); }
+
+void wg_model_options_default(wg_model_options *o) {
+  if (!o) return;
+  *o = wg_model_options{};
+  o->time_series = 1;
+  o->cloud = 2;
+  o->intercept = 1;
+  o->res_opt = 1;
+}
 int32_t wg_num_levels(const wg_ctx *ctx) { return ctx ? ctx->topo.nlevel : 0; }
 int64_t wg_launch_count(const wg_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
@@ -691,9 +705,60 @@ static wg_status setup_water_temp(wg_ctx *ctx, const wg_region *r) {
   return WG_OK;
 }
 
+namespace {
+
+// The reference's options outside the built set: refused with their name.
+wg_status check_model_options(const wg_region *r, const wg_options *opt) {
+  wg_model_options m;
+  wg_model_options_default(&m);
+  if (opt->model) m = *opt->model;
+  struct {
+    const char *name;
+    int32_t value, want;
+  } fixed[] = {{"time_series", m.time_series, 1}, {"cloud", m.cloud, 2}, {"intercept", m.intercept, 1},
+               {"calc_albedo", m.calc_albedo, 0}, {"use_kc", m.use_kc, 0}, {"petOpt", m.pet_opt, 0},
+               {"clclOpt", m.clcl_opt, 0}, {"permaOpt", m.perma_opt, 0}, {"glacierOpt", m.glacier_opt, 0},
+               {"landCoverOpt", m.land_cover_opt, 0}, {"aridareaOpt", m.arid_area_opt, 0},
+               {"riverEvapoOpt", m.river_evapo_opt, 0}, {"use_alloc", m.use_alloc, 0},
+               {"aggrNUsGloLakResOpt", m.aggr_nus_glo_lak_res_opt, 0}, {"antNatOpt", m.ant_nat_opt, 0},
+               {"resYearOpt", m.res_year_opt, 0}, {"climate_spatial_resolution", m.climate_spatial_resolution, 0}};
+  for (const auto &f : fixed)
+    if (f.value != f.want) {
+      t_create_err = std::string("options.") + f.name + " = " + std::to_string(f.value) +
+                     " is not built (built: " + std::to_string(f.want) + ")";
+      return WG_ERR_UNSUPPORTED;
+    }
+  if (m.statcorr_opt != 0 && m.statcorr_opt != 1) {
+    t_create_err = "options.statcorrOpt = " + std::to_string(m.statcorr_opt) + " is not built (built: 0, 1)";
+    return WG_ERR_UNSUPPORTED;
+  }
+  if (m.statcorr_opt == 1 && opt->water_temp) {
+    t_create_err = "options.statcorrOpt = 1 together with calc_wtemp = 1 is not built";
+    return WG_ERR_UNSUPPORTED;
+  }
+  if (m.res_opt != 1) {
+    bool any_res = false;
+    for (int i = 0; i < r->ncell && !any_res; ++i) any_res = r->res_area[i] > 0.;
+    if (m.res_opt != 0 || any_res) {
+      t_create_err = "options.resOpt = " + std::to_string(m.res_opt) +
+                     " is not built (built: 1; 0 for a region without reservoirs)";
+      return WG_ERR_UNSUPPORTED;
+    }
+  }
+  if (r->river_velo_opt < 0 || r->river_velo_opt > 2) {
+    t_create_err = "options.riverveloOpt = " + std::to_string(r->river_velo_opt) + " is not built (built: 0, 1, 2)";
+    return WG_ERR_UNSUPPORTED;
+  }
+  return WG_OK;
+}
+
+}  // namespace
+
 wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
+  t_create_err.clear();
   if (!r || !opt || !out) return WG_ERR_INVALID;
   *out = nullptr;
+  if (wg_status ms = check_model_options(r, opt); ms != WG_OK) return ms;
   if (r->ncell <= 0 || r->nband <= 0 || r->nband > 256 || opt->max_days <= 0) return WG_ERR_INVALID;
   if (r->river_velo_opt < 0 || r->river_velo_opt > 2) return WG_ERR_UNSUPPORTED;
   if (r->frac_routing < 0 || r->frac_routing > 1) return WG_ERR_INVALID;
@@ -754,7 +819,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
 
   // ----- per-cell constants in cell order, with the reference's expressions
   auto P = [&](int k, int i) { return r->param[(size_t)k * n + i]; };
-  enum { GAMRUN = 0, CFA = 1, RIVRGH = 4, LAK_D = 5, WET_D = 6, SWOUTF = 7, EVAREDEX = 8, NETRAD = 9, PTC_HUM = 10,
+  enum { GAMRUN = 0, CFA = 1, CFS = 2, RIVRGH = 4, LAK_D = 5, WET_D = 6, SWOUTF = 7, EVAREDEX = 8, NETRAD = 9, PTC_HUM = 10,
          PTC_ARI = 11, PET_MXDY = 12, MCWH = 13, T_SNOWFZ = 15, T_SNOWMT = 16, DEGDAY = 17, T_GRADNT = 18,
          PCRITGWA = 21, GWOUTF = 22, PREC = 25 };
   HostConsts h;
@@ -865,6 +930,10 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     const int cidx = opt->stations[k];
     if (cidx < 0 || cidx >= n) return WG_ERR_INVALID;
     h.station[cidx] = k;
+  }
+  if (opt->model && opt->model->statcorr_opt == 1) {   // G_statCorrFact = P_CFS (integrateWGHM.cpp:364)
+    h.statcorr.resize(n);
+    for (int i = 0; i < n; ++i) h.statcorr[i] = P(CFS, i);
   }
   h.nrow = (int)lats.size();
   h.ext.resize((size_t)365 * h.nrow);

@@ -69,6 +69,7 @@ struct DevCellsT {
   const R *gw100, *maxs_gw, *inv_maxs_gw;         // global wetland
   const R *bw, *inv_mr, *sqrt_slope, *inv_len, *rlen;   // river
   const R *fcatch;                                // fractional routing: share of the runoff through the water bodies
+  const R *statcorr;                              // station correction factor P_CFS (statcorrOpt = 1), else null
   // topology in slot space
   const int32_t *up_ptr, *up_idx;               // upstream CSR, each list in reference routing order
   const int32_t *offset;                        // pipeline step offset of the slot

@@ -919,6 +919,11 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     W[5 * NN] = wu->tab[wrow + 3 * (size_t)c.n + s];
     if (doy == 365) wu_year_end(W, NN);
   }
+  if (c.statcorr) {   // station correction (statcorrOpt = 1, routing.cpp:3929-3931)
+    const R corrected = transported * c.statcorr[s];
+    rt.leak += corrected - transported;   // water the correction adds (removes)
+    transported = corrected;
+  }
   return transported;
 }
 

@@ -35,7 +35,8 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_set_calib_param", "wg_save_snapshot", "wg_restore_snapshot", "wg_kernel_timing",
            "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells",
            "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync",
-           "wg_upload_water_use", "wg_set_water_use_inputs", "wg_get_water_use", "wg_set_water_use")
+           "wg_upload_water_use", "wg_set_water_use_inputs", "wg_get_water_use", "wg_set_water_use",
+           "wg_model_options_default")
 
 
 class WgError(RuntimeError):
@@ -63,7 +64,18 @@ class _Options(ctypes.Structure):
                 ("precision", ctypes.c_int32), ("members", ctypes.c_int32), ("member_prec_factor", ctypes.c_void_p),
                 ("member_gamma_factor", ctypes.c_void_p), ("block_threads", ctypes.c_int32),
                 ("ring_days", ctypes.c_int32), ("days_per_step", ctypes.c_int32), ("water_temp", ctypes.c_int32),
-                ("water_use", ctypes.c_int32)]
+                ("water_use", ctypes.c_int32), ("model", ctypes.c_void_p)]
+
+
+# wg_model_options: the reference's model switches (optionClass, option.h:43-68)
+MODEL_OPTIONS = ("time_series", "cloud", "intercept", "calc_albedo", "use_kc", "pet_opt", "clcl_opt", "perma_opt",
+                 "glacier_opt", "land_cover_opt", "arid_area_opt", "river_evapo_opt", "statcorr_opt", "use_alloc",
+                 "aggr_nus_glo_lak_res_opt", "ant_nat_opt", "res_year_opt", "res_opt",
+                 "climate_spatial_resolution")
+
+
+class _ModelOptions(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_int32) for f in MODEL_OPTIONS]
 
 
 _lib = None
@@ -79,6 +91,8 @@ def load_library(path: str = LIB_PATH):
     lib = ctypes.CDLL(path)
     vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
     lib.wg_create.argtypes = [ctypes.POINTER(_Region), ctypes.POINTER(_Options), ctypes.POINTER(vp)]
+    lib.wg_model_options_default.argtypes = [ctypes.POINTER(_ModelOptions)]
+    lib.wg_model_options_default.restype = None
     lib.wg_destroy.argtypes = [vp]
     lib.wg_set_state.argtypes = [vp, ctypes.POINTER(_StateView)]
     lib.wg_get_state.argtypes = [vp, ctypes.POINTER(_StateView)]
@@ -209,7 +223,8 @@ class Model:
     def __init__(self, region: Region, max_days: int = 366, stations=None, record_balance: bool = False,
                  device: int = 0, stream: int = 0, precision: str = "fp64", members: int = 1,
                  prec_factor=None, gamma_factor=None, block_threads: int = 0, ring_days: int = 0,
-                 days_per_step: int = 0, water_temp: bool = False, water_use: int | bool = False):
+                 days_per_step: int = 0, water_temp: bool = False, water_use: int | bool = False,
+                 model_options: dict | None = None):
         self.lib = load_library()
         self.region = region
         self._keep = []
@@ -242,6 +257,16 @@ class Model:
         o.days_per_step = int(days_per_step)
         o.water_temp = int(bool(water_temp))
         o.water_use = int(water_use)   # True/1; 2: delayed satisfaction
+        # the reference's model switches: the built defaults, the region's station
+        # correction, then the caller's values (refused by wg_create if not built)
+        self._model = _ModelOptions()
+        self.lib.wg_model_options_default(ctypes.byref(self._model))
+        self._model.statcorr_opt = int(getattr(region, "statcorr_opt", 0))
+        for k, v in (model_options or {}).items():
+            if k not in MODEL_OPTIONS:
+                raise WgError(f"unknown model option {k}")
+            setattr(self._model, k, int(v))
+        o.model = ctypes.addressof(self._model)
         self.max_days = int(max_days)
         h = ctypes.c_void_p()
         self._check(self.lib.wg_create(ctypes.byref(r), ctypes.byref(o), ctypes.byref(h)), "wg_create", None)
@@ -252,6 +277,8 @@ class Model:
             msg = ""
             if h is not None and getattr(self, "h", None):
                 msg = self.lib.wg_last_error(self.h).decode()
+            elif h is None:   # wg_create: the calling thread's reason
+                msg = self.lib.wg_last_error(None).decode()
             raise WgError(f"{what}: {STATUS.get(rc, rc)} {msg}")
 
     def close(self):

@@ -94,6 +94,9 @@ class Region:
     # options.fractionalRoutingOpt: part of the local runoff bypasses the cell's
     # water bodies and flows directly into its river (routing.cpp:1895-2046, 3408-3412)
     frac_routing: int = 0
+    # options.statcorrOpt: each cell's outflow multiplied by its station correction
+    # factor, the calibration parameter P_CFS (routing.cpp:3929-3931)
+    statcorr_opt: int = 0
     # grid placement, used by the fixture writers (0.5-degree rows/cols, 1-based)
     row: np.ndarray | None = None
     col: np.ndarray | None = None
@@ -188,7 +191,8 @@ def empty_state(ncell: int, nband: int) -> Dict[str, np.ndarray]:
 def save_npz(region: Region, path: str, **extra) -> None:
     """Store a region (and optional extra arrays) in one compressed .npz file."""
     payload = {f"a_{k}": v for k, v in region.arrays.items()}
-    meta = np.array([region.ncell, region.nband, region.river_velo_opt, region.frac_routing], np.int64)
+    meta = np.array([region.ncell, region.nband, region.river_velo_opt, region.frac_routing, region.statcorr_opt],
+                    np.int64)
     payload.update(meta=meta, default_velocity=np.array(region.default_velocity), name=np.array(region.name))
     if region.row is not None:
         payload.update(row=region.row, col=region.col)
@@ -208,7 +212,8 @@ def load_npz(path: str):
     meta = [int(x) for x in z["meta"]]
     ncell, nband, velo = meta[:3]
     frac = meta[3] if len(meta) > 3 else 0
-    reg = Region(ncell=ncell, nband=nband, arrays=arrays, river_velo_opt=velo, frac_routing=frac,
+    statcorr = meta[4] if len(meta) > 4 else 0
+    reg = Region(ncell=ncell, nband=nband, arrays=arrays, river_velo_opt=velo, frac_routing=frac, statcorr_opt=statcorr,
                  default_velocity=float(z["default_velocity"]), name=str(z["name"]),
                  row=z["row"] if "row" in z.files else None, col=z["col"] if "col" in z.files else None)
     reg.lct_tables = {k[2:]: z[k] for k in z.files if k.startswith("t_")}
