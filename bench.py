@@ -305,14 +305,53 @@ def run_water_use(region, P, T, S, stream, local):
     return out
 
 
+# algorithmic HBM bytes per member-cell-day of the ensemble (FP32 state, the
+# forcing and static parameters shared by the members of one cell in a block):
+# per member state r+w 72, perturbed gamma 4, outputs 8; per block of members
+# forcing 12 + static parameters 40
+ENS_BYTES_PER_MEMBER = 84.0
+ENS_BYTES_PER_BLOCK = 52.0
+
+
+def ensemble_member_errors(region, P, T, S, pf, gf, ens, nd, stream, local):
+    """Discharge error of every member of the ensemble against an FP64 run of the
+    same member's inputs (precipitation x pf[m], gamma x gf[m]): per member the
+    outlet errors of outlet_errors; summarised over the members."""
+    from watergap2_gb300.gpu import Model
+    ref = Model(region, max_days=nd, device=local, stream=stream.cuda_stream, days_per_step=WAVEFRONT_DAYS,
+                stations=ens.stations)
+    ref.upload_forcing(0, P, T, S)
+    ref.save_snapshot()
+    g0 = region.param("P_GAMRUN_C").copy()
+    rows = []
+    for m in range(ens.members):
+        ref.restore_snapshot()
+        ref.set_calib_param("P_GAMRUN_C", g0 * float(gf[m]))
+        ref.upload_forcing(0, (P * pf[m]).astype(np.float32), None, None)
+        ref.run_days(1, 0, nd)
+        rows.append(outlet_errors(ens.member_discharge(m, 0, nd), ref.discharge(0, nd)))
+    del ref
+    keys = rows[0].keys()
+    arr = {k: np.array([r[k] for r in rows]) for k in keys}
+    return {"members": len(rows),
+            "daily_err_max": {"max": float(arr["daily_err_max"].max()),
+                              "median": float(np.median(arr["daily_err_max"])),
+                              "q99": float(np.quantile(arr["daily_err_max"], 0.99)),
+                              "members_above_1e-5": int((arr["daily_err_max"] > 1e-5).sum())},
+            "mean_err_max": {"max": float(arr["mean_err_max"].max()),
+                             "median": float(np.median(arr["mean_err_max"]))},
+            "daily_err_q99_max": float(arr["daily_err_q99"].max()),
+            "member0": rows[0], "worst_member": int(np.argmax(arr["daily_err_max"]))}
+
+
 def run_ensemble(args, region, P, T, S, stream, local, plain_value):
     """Batched ensemble: ENS_MEMBERS members of the global grid over ENS_DAYS days in
     one day-pipelined wavefront (FP32 state, FP64 confluence and balance sums),
     launch shape and chunk length from the autotuner, the whole run captured in one
     CUDA graph and replayed.  Members: precipitation x lognormal(0, 0.3), runoff
     coefficient gamma x U(0.7, 1.3), each from its own seed; member 0 unperturbed.
-    Discharge error: members 0 and 1 of the first replay against FP64 runs of the
-    same inputs."""
+    Discharge error: every member of the first replay against an FP64 run of its
+    own inputs."""
     import torch
     from watergap2_gb300.gpu import Model
     M, nd = ENS_MEMBERS, ENS_DAYS
@@ -330,19 +369,7 @@ def run_ensemble(args, region, P, T, S, stream, local, plain_value):
     # first replay: from the initial state, checked against FP64
     ens.graph_launch()
     ens.synchronize()
-    nst = ens.stations.size
-    q_m = np.empty((2, nd, nst))
-    for d0 in range(0, nd, 73):
-        q = ens.discharge(d0, min(73, nd - d0))            # [days, stations, members]
-        q_m[:, d0:d0 + q.shape[0]] = np.moveaxis(q[:, :, :2], 2, 0)
-        del q
-    errors = {}
-    for m in (0, 1):
-        reg = region if gf[m] == 1.0 else region.with_param("P_GAMRUN_C", region.param("P_GAMRUN_C") * float(gf[m]))
-        ref = Model(reg, max_days=nd, device=local, stream=stream.cuda_stream)
-        q64 = ref.run(1, (P * pf[m]).astype(np.float32), T, S)
-        del ref
-        errors[f"member{m}"] = dict(outlet_errors(q_m[m], q64), prec_factor=float(pf[m]), gamma_factor=float(gf[m]))
+    errors = ensemble_member_errors(region, P, T, S, pf, gf, ens, nd, stream, local)
     for _ in range(max(0, args.warmup - 1)):
         ens.graph_launch()
     ens.synchronize()
@@ -358,11 +385,49 @@ def run_ensemble(args, region, P, T, S, stream, local, plain_value):
     ens.synchronize()
     ms = e0.elapsed_time(e1) / reps
     value = M * region.ncell * nd / (ms / 1000.0)
+    # roofline of the whole run (both kernels of each launch pair move the
+    # algorithmic bytes counted per member-cell-day; the run is one CUDA graph)
+    peaks, peak_kind = measured_peaks()
+    per_mcd = ENS_BYTES_PER_MEMBER + ENS_BYTES_PER_BLOCK / tune["threads"]
+    achieved = value * per_mcd / 1e9
+    figs = profile_figures(os.path.join(ROOT, "profiles", "ensemble_global_kernels.md"))
+    traffic = figs.get("dram_bytes_per_member_cell_day")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                "frac": achieved / peaks.get("hbm_gbs"), "peak_kind": peak_kind,
+                "algorithmic_bytes_per_member_cell_day": per_mcd,
+                "traffic_bytes_per_member_cell_day": traffic,
+                "kernel": "k_vertical_ahead<float,1> + k_pipeline<float,1,1> (whole graph-captured run)"}
     return {"metric": "member-cell-days/s", "value": value, "members": M, "days": nd, "ncell": region.ncell,
             "ms_per_run": ms, "runs_timed": reps, "gpu_launches": int(ens.launch_count - l0),
             "dtype": "f32 state, f64 sums", "vs_plain_fp64": value / plain_value, "autotune": tune,
             "graph": "whole run (all launch pairs) captured once, replayed per run",
-            "discharge_error_vs_fp64": errors}
+            "roofline": roofline, "discharge_error_vs_fp64": errors}
+
+
+def run_closure(region, P, T, S, stream, local, ndays=365):
+    """The daily mass-balance closure of the global grid (FP64, compensated sums):
+    one year through the per-day entry points with the balance recorded; each
+    day the change of the total storage against that day's inflow - evaporation
+    - outflow + clamp corrections, relative to the day's throughput, and the
+    largest per-cell closure residual."""
+    from watergap2_gb300.gpu import Model
+    m = Model(region, max_days=ndays, device=local, stream=stream.cuda_stream, record_balance=True)
+    m.upload_forcing(0, P[:ndays], T[:ndays], S[:ndays])
+    prev = m.balance()
+    daily, cells = [], []
+    for d in range(ndays):
+        m.step_vertical(d + 1, d)
+        m.step_routing(d + 1, d)
+        b = m.balance()
+        flux = (b[1] - prev[1]) - (b[2] - prev[2]) - (b[3] - prev[3]) + (b[4] - prev[4])
+        daily.append(abs((b[0] - prev[0]) - flux) / max(b[1] - prev[1], b[2] - prev[2], b[3] - prev[3]))
+        cells.append(b[5])
+        prev = b
+    del m
+    return {"days": ndays, "max_daily_residual_rel": float(max(daily)),
+            "median_daily_residual_rel": float(statistics.median(daily)),
+            "max_cell_residual_rel": float(max(cells)), "bound": 1e-12,
+            "closed_every_day": bool(max(daily) <= 1e-12 and max(cells) <= 1e-12)}
 
 
 def fp64_peak_tflops():
@@ -496,28 +561,36 @@ def run_gpu(args, rank, world):
     num_levels = e2e_model.num_levels
 
     del e2e_model
-    # the reference's granularity through the C ABI: one whole-grid calcNewDay launch
-    # and one routing launch (a wavefront over the levels of one day) per day
+    # the reference's granularity through the C ABI: per day one whole-grid
+    # calcNewDay call and one routing call (integrate_wghm_'s loop, which the C++
+    # stand-ins of include/wg_gpu.hpp keep), the model read at every month end:
+    # with the calls deferred (wg_set_deferred, the stand-ins' mode) each month
+    # runs as one day-pipelined launch sequence; immediate: two launches a day
     per_day = None
     if rank == 0:
-        pd_days = 30
-        pd = Model(region, max_days=pd_days, device=local, stream=stream.cuda_stream)
-        pd.upload_forcing(0, P[:pd_days], T[:pd_days], S[:pd_days])
-        for d in range(3):
-            pd.step_vertical(d + 1, d)
-            pd.step_routing(d + 1, d)
-        pd.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for d in range(3, pd_days):
-            pd.step_vertical(d + 1, d)
-            pd.step_routing(d + 1, d)
-        e1.record(stream)
-        pd.synchronize()
-        pd_ms = e0.elapsed_time(e1) / (pd_days - 3)
-        per_day = {"value": region.ncell / (pd_ms / 1000.0), "unit": "cell-days/s", "ms_per_day": pd_ms,
-                   "api": "wg_step_vertical + wg_step_routing per day (the reference's call granularity)"}
-        del pd
+        per_day = {"api": "wg_step_vertical + wg_step_routing per day, state read at every month end "
+                          "(integrate_wghm_'s loop through the drop-in stand-ins)"}
+        month_end = set(np.cumsum([31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31]).tolist())
+        for name, deferred, nd in (("deferred", True, DAYS_PER_STEP), ("immediate", False, 60)):
+            pd = Model(region, max_days=nd, device=local, stream=stream.cuda_stream)
+            pd.upload_forcing(0, P[:nd], T[:nd], S[:nd])
+            pd.synchronize()
+            if deferred:
+                pd.set_deferred(True)
+            t0 = time.perf_counter()
+            for d in range(nd):
+                pd.step_vertical(d + 1, d)
+                pd.step_routing(d + 1, d)
+                if d + 1 in month_end:
+                    pd.get_state()
+            pd.synchronize()
+            sec = time.perf_counter() - t0
+            per_day[name] = {"value": region.ncell * nd / sec, "unit": "cell-days/s", "days": nd,
+                             "ms_per_day": 1000.0 * sec / nd}
+            del pd
+        per_day["value"] = per_day["deferred"]["value"]
+        per_day["unit"] = "cell-days/s"
+    closure = run_closure(region, P, T, S, stream, local) if rank == 0 else None
     ensemble = None
     if rank == 0 and not os.environ.get("WG_BENCH_NO_ENSEMBLE"):
         ensemble = run_ensemble(args, region, P, T, S, stream, local, value)
@@ -527,6 +600,14 @@ def run_gpu(args, rank, world):
     water_use = None
     if rank == 0 and not os.environ.get("WG_BENCH_NO_WUSE"):
         water_use = run_water_use(region, P, T, S, stream, local)
+    # the other configurations, bounded: one simulated year of the 5-arc-minute
+    # grid in both precisions, and the learned-calibration workload
+    fine = None
+    if rank == 0 and not os.environ.get("WG_BENCH_NO_FINE"):
+        fine = fine_workload(1, device=local)
+    calibration = None
+    if rank == 0 and not os.environ.get("WG_BENCH_NO_CALIB"):
+        calibration = calibration_workload(device=local)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -598,9 +679,12 @@ def run_gpu(args, rank, world):
                      "vertical_ahead_ms_per_timed_step": va_ms_total / args.steps},
         "fp64": fp64,
         "per_day_api": per_day,
+        "closure": closure,
         "ensemble": ensemble,
         "water_temp": water_temp,
         "water_use": water_use,
+        "fine_5min": fine,
+        "calibration": calibration,
         "cpu_baseline": {"value": cpu_val, "unit": "cell-days/s", "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_days} days of the same grid ({region.ncell * cpu_days} cell-days, "
                                    f"{cpu_s:.1f} s), vertical pass on {cpu_threads} OpenMP threads, routing serial"},
@@ -672,21 +756,27 @@ def run_profile_wuse(steps: int = 24, warm_steps: int = 200):
 
 
 def run_fine():
-    """Mixed precision at fine resolution: the 5-arc-minute grid (~2.2 M cells),
-    FP32 state and fluxes with FP64 confluence and balance sums against the FP64
-    run of the same inputs, WG_FINE_YEARS (default 5) simulated years; discharge
-    error at every outlet and storage error at the end, and the throughput of both
-    precisions (one wavefront over the whole run, forcing resident in HBM)."""
+    """--fine: fine_workload over WG_FINE_YEARS (default 5) simulated years."""
     import torch
     torch.cuda.set_device(0)
+    print(json.dumps(fine_workload(int(os.environ.get("WG_FINE_YEARS", "5")))), flush=True)
+
+
+def fine_workload(years, device=0):
+    """Mixed precision at fine resolution: the 5-arc-minute grid (~2.2 M cells),
+    FP32 state and fluxes with FP64 confluence and balance sums against the FP64
+    run of the same inputs over `years` simulated years; discharge error at every
+    outlet and storage error at the end, and the throughput of both precisions
+    (one wavefront over the whole run, forcing resident in HBM)."""
+    import torch
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
-    years = int(os.environ.get("WG_FINE_YEARS", "5"))
     t_all = time.perf_counter()
     region = sy.region_5min()
     t_gen = time.perf_counter() - t_all
     nd = 365 * years
-    models = {"fp64": Model(region, max_days=nd), "fp32": Model(region, max_days=nd, precision="fp32")}
+    models = {"fp64": Model(region, max_days=nd, device=device),
+              "fp32": Model(region, max_days=nd, precision="fp32", device=device)}
     for y in range(years):
         def up(f, y=y):
             for m in models.values():
@@ -744,23 +834,28 @@ def run_fine():
             "fp32_speedup": res["fp32"]["cell_days_per_s"] / res["fp64"]["cell_days_per_s"],
             "discharge_error": err_q, "storage_error_end": err_s, "grid_seconds": t_gen, "setup_seconds": t_setup,
             "data": "synthetic (seeded generators; forcing in parallel chunks, seed 43)"}
-    print(json.dumps(line), flush=True)
+    del models
+    return line
 
 
 def run_calibration():
+    """--calibration: calibration_workload printed."""
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps(calibration_workload()), flush=True)
+
+
+def calibration_workload(device=0):
     """Calibration workload: 1,000 basins cut from the global drainage tree, gamma
     and CFA calibrated to targets from hidden true parameters, by the reference's
     bisection and by the learned proposer (the plain FP64 model checking every step)."""
-    import torch
-    torch.cuda.set_device(0)
     from watergap2_gb300.calibration import run_workload
-    out = run_workload(nbasin=1000, lo=20, hi=20000, ndays=730, epochs=40,
+    out = run_workload(nbasin=1000, lo=20, hi=20000, ndays=730, epochs=40, device=device,
                        log=lambda *a: print(*a, file=sys.stderr, flush=True))
-    line = {"workload": "learned calibration: 1,000 basins (cells log-uniform 20..20,000, capped at the largest "
+    return {"workload": "learned calibration: 1,000 basins (cells log-uniform 20..20,000, capped at the largest "
                         "basin of the tree), gamma in [0.1, 5], CFA in [0.5, 1.5], 1 % discharge criterion, "
                         "2-year runs (1 spin-up, 1 evaluated)",
             "metric": "calibrations/hour and plain-model calls per basin", **out}
-    print(json.dumps(line), flush=True)
 
 
 def run_profile_ensemble(members: int = 64, steps: int = 12, warm_steps: int = 200):

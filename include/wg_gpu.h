@@ -202,7 +202,9 @@ wg_status wg_get_member_state(wg_ctx *ctx, int32_t member, wg_state_view *state)
 
 /* Copy ndays of day-major forcing [ndays*ncell] (precipitation mm, temperature C,
  * shortwave W/m2; the reference's climateYear.G_*_d365 floats, climateYear.h:12-15)
- * into forcing slots [day0, day0+ndays) of the device buffer. */
+ * into forcing slots [day0, day0+ndays) of the device buffer.  A NULL variable
+ * keeps the slots' current values (e.g. a precipitation scenario over the same
+ * temperature and radiation). */
 wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec,
                             const float *temp, const float *swrad);
 /* The same upload on the context's copy stream, overlapped with runs already
@@ -298,6 +300,20 @@ wg_status wg_step_vertical(wg_ctx *ctx, int32_t doy, int32_t fday);
  * output slot oday. */
 wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday);
 
+/* Deferred per-day calls (one member): with enable != 0 the two entry points
+ * above only queue their day; consecutive days (day of year, forcing slot and
+ * output slot each one more than the day before) run as one day-pipelined run
+ * -- the same results as their per-day launches -- when the caller next needs
+ * a result or changes an input: every other entry point of this header that
+ * takes the context runs the queue first (reads of state, discharge, balance,
+ * water use or temperature, uploads, parameter changes, wg_synchronize).  So a
+ * driver that keeps the reference's day loop (a calcNewDay pass and a routing
+ * call per day, integrateWGHM.cpp:767-798) and reads the model once a month
+ * gets the pipelined speed.  Errors of the queued days are reported by the
+ * call that runs them.  enable = 0 runs the queue and returns to immediate
+ * launches.  No counterpart in the reference. */
+wg_status wg_set_deferred(wg_ctx *ctx, int32_t enable);
+
 /* ndays consecutive days in one persistent launch (days pipelined along the
  * drainage depth); identical results to ndays calls of the two entry points
  * above.  Forcing slots fday0.., discharge output slots from fday0 too. */
@@ -315,6 +331,20 @@ int32_t wg_run_num_steps(const wg_ctx *ctx, int32_t ndays);
 /* Daily discharge (transported volume, km3/d) of the stations,
  * [ndays][nstation][members], for output slots [day0, day0+ndays). */
 wg_status wg_get_discharge(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out);
+/* The same for one member of an ensemble, [ndays][nstation] (a data-assimilation
+ * driver reads one member's simulated discharge, as each member process of the
+ * reference writes its own, enKF2wghmState.cpp:17-121). */
+wg_status wg_get_member_discharge(wg_ctx *ctx, int32_t member, int32_t day0, int32_t ndays, double *out);
+
+/* Daily routing storages (one member): with enable != 0 the day step records,
+ * for every cell and output day, the day-end storages the reference writes into
+ * its state file each day (routing.cpp:5001-5020; WghmStateFile cells,
+ * wghmStateFile.h:38-47): local lake, local wetland, global lake, global
+ * wetland, reservoir, river, groundwater [km3].  Allocates max_days x 7 x ncell
+ * doubles on the device at the first enable.  wg_get_daily_storages returns
+ * output days [day0, day0+ndays) as [ndays][7][ncell], cell order. */
+wg_status wg_record_daily_storages(wg_ctx *ctx, int32_t enable);
+wg_status wg_get_daily_storages(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out);
 
 /* Water balance: out[0] total storage [km3] (land storages over the land fraction
  * plus all surface-water and groundwater storages), out[1..4] accumulated

@@ -39,7 +39,20 @@ def build(src: str | None = None) -> bool:
     if not src or not os.path.isdir(src):
         return False
     subprocess.run(["make", "-s", "-C", _HERE, "-j8", "ref", f"REF={src}"], check=True)
+    with open(os.path.join(_HERE, "_ref", "source_dir.txt"), "w") as f:
+        f.write(os.path.abspath(src))
     return True
+
+
+def source_dir() -> str | None:
+    """The reference source directory the harness was last built from (None if
+    it was not built here or the sources are gone)."""
+    path = os.path.join(_HERE, "_ref", "source_dir.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        src = f.read().strip()
+    return src if os.path.isdir(src) else None
 
 
 def _unf(path, arr, dt):

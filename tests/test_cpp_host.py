@@ -22,3 +22,17 @@ def test_cpp_shim_compiles_links_and_runs(tmp_path):
     subprocess.run(cmd, check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True)
     assert out.stdout.strip() == "ok"
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_dropin_shims_compile_with_the_reference_classes():
+    """include/wg_gpu.hpp's stand-ins instantiated with the reference's own
+    WghmStateFile, AdditionalOutputInputFile, SnowInElevationFile and
+    calibParamClass (their headers, where the reference sources were built)."""
+    from oracle import ref_case
+    src = ref_case.source_dir()
+    if src is None:
+        pytest.skip("the reference's sources are not on this machine")
+    cmd = ["g++", "-std=c++17", "-fsyntax-only", "-w", "-I", os.path.join(ROOT, "include"), "-I", src,
+           os.path.join(ROOT, "tests", "cpp", "shim_reference_types.cpp")]
+    subprocess.run(cmd, check=True)

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -261,8 +262,23 @@ struct HostConsts {
   std::vector<double> band_dt;   // [ncell][nband]
   std::vector<double> ext, inv_s0;
   std::vector<double> statcorr;  // G_statCorrFact (P_CFS) with statcorrOpt = 1, else empty
+  std::vector<float> snow_thr;   // [ncell][nband] FP32 paths' snowfall thresholds (snowfall_threshold)
+  std::vector<double> t_gradnt64, t_snowfz64;
   int nrow = 0;
 };
+
+// The largest float temperature t at which a band gets snowfall as the FP64 path
+// decides it: ((double)t - band_dt) <= t_snowfz (daily.cpp:982), band_dt =
+// (elev_b - elev_0) * P_T_GRADNT in FP64.  The test is monotone in t, so the FP32
+// paths compare their float temperature with this value and take the same
+// decision for every input.
+float snowfall_threshold(double band_dt, double t_snowfz) {
+  auto snow = [&](float t) { return ((double)t - band_dt) <= t_snowfz; };
+  float t = (float)(t_snowfz + band_dt);
+  for (int k = 0; k < 64 && snow(t) && t < FLT_MAX; ++k) t = std::nextafter(t, FLT_MAX);
+  for (int k = 0; k < 64 && !snow(t); ++k) t = std::nextafter(t, -FLT_MAX);
+  return t;
+}
 
 inline double safe_inv(double x) { return x != 0. ? 1. / x : 0.; }
 
@@ -421,6 +437,18 @@ wg_status upload_cells(wg_ctx *ctx, const HostConsts &h, DevCellsT<R> &c, double
   WG_RFIELDS(X)
 #undef X
   c.band_dt = upload_raw<R>(ctx, bands_to_slots<double>(ctx, h.band_dt.data(), ctx->nband), st);
+  c.snow_thr = nullptr;
+  c.thr64 = nullptr;
+  if (sizeof(R) == 4) {   // the FP32 paths' snowfall decisions (vertical_cell)
+    c.snow_thr = upload_raw<float>(ctx, bands_to_slots<float>(ctx, h.snow_thr.data(), ctx->nband), st);
+    std::vector<double> t64(2 * (size_t)ctx->n);
+    for (int sl = 0; sl < ctx->n; ++sl) {
+      const int cell = ctx->topo.cell_of_slot[sl];
+      t64[sl] = h.t_gradnt64[cell];
+      t64[(size_t)ctx->n + sl] = h.t_snowfz64[cell];
+    }
+    c.thr64 = upload_raw<double>(ctx, t64, st);
+  }
   c.band_el = upload_raw<int16_t>(ctx, bands_to_slots<int16_t>(ctx, h.band_el.data(), ctx->nband), st);
   c.ext_rad = upload_raw<R>(ctx, h.ext, st);
   c.inv_s0 = upload_raw<R>(ctx, h.inv_s0, st);
@@ -592,6 +620,9 @@ static wg_status to_slots(wg_ctx *ctx, const T *host, T *dev) {
   for (int s = 0; s < ctx->n; ++s) v[s] = host[ctx->topo.cell_of_slot[s]];
   return cuda_fail(ctx, cudaMemcpy(dev, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "water temperature");
 }
+
+static wg_status vertical_now(wg_ctx *ctx, int doy, int fday);
+static wg_status routing_now(wg_ctx *ctx, int doy, int oday);
 
 extern "C" {
 
@@ -829,6 +860,9 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
 #undef X
   h.band_dt.resize((size_t)n * B);
   h.band_el.resize((size_t)n * B);
+  h.snow_thr.resize((size_t)n * B);
+  h.t_gradnt64.resize(n);
+  h.t_snowfz64.resize(n);
   std::vector<double> lats;
   for (int i = 0; i < n; ++i) {
     const int lct = r->lct[i];
@@ -874,7 +908,10 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     for (int b = 0; b < B; ++b) {
       h.band_dt[(size_t)i * B + b] = (el[b + 1] - el[0]) * P(T_GRADNT, i);
       h.band_el[(size_t)i * B + b] = el[b + 1];
+      h.snow_thr[(size_t)i * B + b] = snowfall_threshold(h.band_dt[(size_t)i * B + b], P(T_SNOWFZ, i));
     }
+    h.t_gradnt64[i] = P(T_GRADNT, i);
+    h.t_snowfz64[i] = P(T_SNOWFZ, i);
     const double kg = P(GWOUTF, i);
     h.gw_e[i] = exp(-1. * kg);
     h.gw_ik[i] = 1. / kg;
@@ -1093,27 +1130,31 @@ wg_status wg_destroy(wg_ctx *ctx) {
 
 wg_status wg_set_state(wg_ctx *ctx, const wg_state_view *v) {
   if (!ctx || !v) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   return state_io(ctx, v, 0, true);
 }
 
 wg_status wg_get_state(wg_ctx *ctx, wg_state_view *v) {
   if (!ctx || !v) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   return state_io(ctx, v, 0, false);
 }
 
 wg_status wg_set_member_state(wg_ctx *ctx, int32_t member, const wg_state_view *v) {
   if (!ctx || !v) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   return state_io(ctx, v, member, true);
 }
 
 wg_status wg_get_member_state(wg_ctx *ctx, int32_t member, wg_state_view *v) {
   if (!ctx || !v) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   return state_io(ctx, v, member, false);
 }
 
 static wg_status upload_forcing_on(wg_ctx *ctx, cudaStream_t st, float *staging, int32_t day0, int32_t ndays,
                                    const float *prec, const float *temp, const float *swrad) {
-  if (!ctx || !prec || !temp || !swrad || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days)
+  if (!ctx || (!prec && !temp && !swrad) || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days)
     return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
   const int n = ctx->n;
@@ -1122,6 +1163,7 @@ static wg_status upload_forcing_on(wg_ctx *ctx, cudaStream_t st, float *staging,
   for (int d = 0; d < ndays; d += ctx->staging_days) {
     const int nd = std::min(ctx->staging_days, ndays - d);
     for (int k = 0; k < 3; ++k) {
+      if (!src[k]) continue;   // the slots keep this variable's values
       cudaError_t e = cudaMemcpyAsync(staging, src[k] + (size_t)d * n, (size_t)nd * n * sizeof(float),
                                       cudaMemcpyHostToDevice, st);
       if (e == cudaSuccess)
@@ -1136,6 +1178,7 @@ static wg_status upload_forcing_on(wg_ctx *ctx, cudaStream_t st, float *staging,
 wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec, const float *temp,
                             const float *swrad) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   join_uploads(ctx);   // after the overlapped uploads, in the order of the calls
   return upload_forcing_on(ctx, ctx->stream, ctx->staging, day0, ndays, prec, temp, swrad);
 }
@@ -1145,6 +1188,7 @@ wg_status wg_upload_forcing_unf(wg_ctx *ctx, int32_t day0, int32_t nd_file, int3
   if (!ctx || !prec || !temp || !swrad || nd_file <= 0 || d_first < 0 || ndays < 0 || d_first + ndays > nd_file ||
       day0 < 0 || day0 + ndays > ctx->max_days)
     return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   cudaSetDevice(ctx->device);
   const int which = overlap ? 1 : 0;
   const size_t per = (size_t)ctx->n * nd_file;
@@ -1194,6 +1238,7 @@ wg_status wg_math_eval(int32_t device, int32_t fn, const double *x, const double
 
 wg_status wg_upload_longwave(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *longwave) {
   if (!ctx || !longwave || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (!ctx->wt.enabled) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
   join_uploads(ctx);
@@ -1213,6 +1258,7 @@ wg_status wg_upload_longwave(wg_ctx *ctx, int32_t day0, int32_t ndays, const flo
 
 wg_status wg_set_water_temp_inputs(wg_ctx *ctx, const float *gw_temp, const double *river_length_check) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (!ctx->wt.enabled) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
   wg_status st = wg_synchronize(ctx);
@@ -1250,17 +1296,22 @@ static wg_status water_temp_io(wg_ctx *ctx, double *temp, double *ice, const dou
 }
 
 wg_status wg_get_water_temp(wg_ctx *ctx, double *temp, double *ice) {
+  if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (!temp && !ice) return WG_ERR_INVALID;
   return water_temp_io(ctx, temp, ice, nullptr, nullptr);
 }
 
 wg_status wg_set_water_temp(wg_ctx *ctx, const double *temp, const double *ice) {
+  if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (!temp && !ice) return WG_ERR_INVALID;
   return water_temp_io(ctx, nullptr, nullptr, temp, ice);
 }
 
 wg_status wg_get_river_temp(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out) {
   if (!ctx || !out || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (!ctx->wt.enabled) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
   wg_status st = wg_synchronize(ctx);
@@ -1276,6 +1327,7 @@ wg_status wg_upload_water_use(wg_ctx *ctx, int32_t fday0, int32_t ndays, int32_t
                               const double *nug_m3, const double *irrig_withdrawal_sw_m3,
                               const double *irrig_consumptive_sw_m3) {
   if (!ctx || !nus_m3 || !nug_m3 || !irrig_withdrawal_sw_m3 || !irrig_consumptive_sw_m3) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (fday0 < 0 || ndays < 1 || fday0 + ndays > ctx->max_days || doy0 < 1 || doy0 + ndays - 1 > 365)
     return WG_ERR_INVALID;
   if (!ctx->wu.enabled) return WG_ERR_UNSUPPORTED;
@@ -1323,6 +1375,7 @@ wg_status wg_upload_water_use(wg_ctx *ctx, int32_t fday0, int32_t ndays, int32_t
 
 wg_status wg_set_water_use_inputs(wg_ctx *ctx, const double *frac_return_gw_irrig) {
   if (!ctx || !frac_return_gw_irrig) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (!ctx->wu.enabled) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
   wg_status st = wg_synchronize(ctx);
@@ -1333,6 +1386,7 @@ wg_status wg_set_water_use_inputs(wg_ctx *ctx, const double *frac_return_gw_irri
 // [WG_WU_NSTATE][ncell] cell order <-> [WG_WU_NSTATE][N] slot order
 static wg_status water_use_io(wg_ctx *ctx, double *out, const double *in) {
   if (!ctx || (!out && !in)) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (!ctx->wu.enabled) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
   wg_status st = wg_synchronize(ctx);
@@ -1372,6 +1426,7 @@ int64_t wg_read_unf(const char *path, void *dst, int64_t bytes) {
 wg_status wg_upload_forcing_async(wg_ctx *ctx, int32_t day0, int32_t ndays, const float *prec, const float *temp,
                                   const float *swrad) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   // its own staging buffer: the copy stream is not ordered after uploads on the
   // context's stream
   if (!ctx->staging_async) ctx->staging_async = ctx->alloc<float>((size_t)ctx->staging_days * ctx->n);
@@ -1387,34 +1442,39 @@ wg_status wg_upload_forcing_async(wg_ctx *ctx, int32_t day0, int32_t ndays, cons
 wg_status wg_step_vertical(wg_ctx *ctx, int32_t doy, int32_t fday) {
   if (!ctx || doy < 1 || doy > 365 || fday < 0 || fday >= ctx->max_days) return WG_ERR_INVALID;
   if (ctx->members != 1) return WG_ERR_UNSUPPORTED;
-  cudaSetDevice(ctx->device);
-  join_uploads(ctx);
-  ctx->launches++;
-  ctx->last_vertical_fday = fday;   // the day's forcing slot, for the water temperature of wg_step_routing
-  cudaError_t e = ctx->precision == 0
-                      ? launch_vertical(ctx->cd, ctx->sd, ctx->vd, ctx->forcing, doy, fday, ctx->stream)
-                      : launch_vertical(ctx->cf, ctx->sf, ctx->vf, ctx->forcing, doy, fday, ctx->stream);
-  return cuda_fail(ctx, e, "step_vertical");
+  auto &q = ctx->defer;
+  if (!q.on) return vertical_now(ctx, doy, fday);
+  if (q.vpending) WG_FLUSH(ctx);   // two vertical calls in a row: the first runs alone
+  q.vpending = true;
+  q.vdoy = doy;
+  q.vfday = fday;
+  return WG_OK;
 }
 
 wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday) {
   if (!ctx || doy < 1 || doy > 365 || oday < 0 || oday >= ctx->max_days) return WG_ERR_INVALID;
   if (ctx->members != 1) return WG_ERR_UNSUPPORTED;
-  cudaSetDevice(ctx->device);
-  join_uploads(ctx);
-  ctx->launches++;
-  cudaError_t e = ctx->precision == 0
-                      ? launch_pipeline(false, ctx->cd, ctx->sd, ctx->vd, ctx->forcing, ctx->mem, ctx->balance,
-                                        ctx->rd, ctx->sync, ctx->outq, ctx->qst, doy, ctx->last_vertical_fday, oday, 1,
-                                        0, ctx->topo.nlevel,
-                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, DevVaWork{}, ctx->wt,
-                                        ctx->wu, ctx->stream)
-                      : launch_pipeline(false, ctx->cf, ctx->sf, ctx->vf, ctx->forcing, ctx->mem, ctx->balance,
-                                        ctx->rf, ctx->sync, ctx->outq, ctx->qst, doy, ctx->last_vertical_fday, oday, 1,
-                                        0, ctx->topo.nlevel,
-                                        ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon, DevVaWork{}, ctx->wt,
-                                        ctx->wu, ctx->stream);
-  return cuda_fail(ctx, e, "step_routing");
+  auto &q = ctx->defer;
+  if (!q.on) return routing_now(ctx, doy, oday);
+  if (!q.vpending || q.vdoy != doy) {   // not the pair of a queued vertical call: in order, now
+    WG_FLUSH(ctx);
+    return routing_now(ctx, doy, oday);
+  }
+  q.vpending = false;   // this day's vertical call is consumed by the queue
+  const bool follows = q.ndays > 0 && doy == (q.doy0 - 1 + q.ndays) % 365 + 1 && q.vfday == q.fday0 + q.ndays &&
+                       oday == q.oday0 + q.ndays;
+  if (!follows) {
+    if (q.ndays > 0) {   // the queued run first, then this day starts a new one
+      wg_status st = flush_deferred(ctx);
+      if (st != WG_OK) return st;
+    }
+    q.doy0 = doy;
+    q.fday0 = q.vfday;
+    q.oday0 = oday;
+    q.ndays = 0;
+  }
+  q.ndays++;
+  return WG_OK;
 }
 
 }  // extern "C"
@@ -1428,7 +1488,8 @@ wg_status wg_step_routing(wg_ctx *ctx, int32_t doy, int32_t oday) {
 // call ends with the vertical state exactly at step t_e either way.
 template <class R>
 static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
-                                const DevRingT<R> &ring, int doy0, int fday0, int ndays, int t_b, int t_e) {
+                                const DevRingT<R> &ring, int doy0, int fday0, int oday0, int ndays, int t_b,
+                                int t_e) {
   const bool ov = ctx->overlap();
   const int chunk = ctx->eff_chunk();
   DevVaWork vw{};
@@ -1450,7 +1511,7 @@ static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevSta
     vw.warps = (ov && vw.t_e > vw.t_b) ? ctx->layout.va_warps : 0;
     if (e == cudaSuccess)
       e = launch_pipeline(true, c, s, v, ctx->forcing, ctx->mem, ctx->balance, ring, ctx->sync, ctx->outq, ctx->qst,
-                          doy0, fday0, fday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->layout, ctx->mon,
+                          doy0, fday0, oday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->layout, ctx->mon,
                           vw, ctx->wt, ctx->wu, ctx->stream);
     ctx->launches++;
     if (ev) cudaEventRecord(ev[2], ctx->stream);
@@ -1461,15 +1522,80 @@ static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevSta
 
 extern "C" {
 
+}  // extern "C"
+
+// steps [t_begin, t_end) of a run whose station and monthly outputs start at slot oday0
+static wg_status run_steps_at(wg_ctx *ctx, int doy0, int fday0, int oday0, int ndays, int t_begin, int t_end) {
+  cudaSetDevice(ctx->device);
+  join_uploads(ctx);
+  return ctx->precision == 0
+             ? run_steps_impl(ctx, ctx->cd, ctx->sd, ctx->vd, ctx->rd, doy0, fday0, oday0, ndays, t_begin, t_end)
+             : run_steps_impl(ctx, ctx->cf, ctx->sf, ctx->vf, ctx->rf, doy0, fday0, oday0, ndays, t_begin, t_end);
+}
+
+static wg_status vertical_now(wg_ctx *ctx, int doy, int fday) {
+  cudaSetDevice(ctx->device);
+  join_uploads(ctx);
+  ctx->launches++;
+  ctx->last_vertical_fday = fday;   // the day's forcing slot, for the water temperature of wg_step_routing
+  cudaError_t e = ctx->precision == 0
+                      ? launch_vertical(ctx->cd, ctx->sd, ctx->vd, ctx->forcing, doy, fday, ctx->stream)
+                      : launch_vertical(ctx->cf, ctx->sf, ctx->vf, ctx->forcing, doy, fday, ctx->stream);
+  return cuda_fail(ctx, e, "step_vertical");
+}
+
+static wg_status routing_now(wg_ctx *ctx, int doy, int oday) {
+  cudaSetDevice(ctx->device);
+  join_uploads(ctx);
+  ctx->launches++;
+  cudaError_t e = ctx->precision == 0
+                      ? launch_pipeline(false, ctx->cd, ctx->sd, ctx->vd, ctx->forcing, ctx->mem, ctx->balance,
+                                        ctx->rd, ctx->sync, ctx->outq, ctx->qst, doy, ctx->last_vertical_fday, oday, 1,
+                                        0, ctx->topo.nlevel, ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon,
+                                        DevVaWork{}, ctx->wt, ctx->wu, ctx->stream)
+                      : launch_pipeline(false, ctx->cf, ctx->sf, ctx->vf, ctx->forcing, ctx->mem, ctx->balance,
+                                        ctx->rf, ctx->sync, ctx->outq, ctx->qst, doy, ctx->last_vertical_fday, oday, 1,
+                                        0, ctx->topo.nlevel, ctx->blocks_route, ctx->threads, ctx->layout, ctx->mon,
+                                        DevVaWork{}, ctx->wt, ctx->wu, ctx->stream);
+  return cuda_fail(ctx, e, "step_routing");
+}
+
+// Run what the deferred per-day calls have queued: the consecutive days as one
+// day-pipelined run (the same results as their per-day launches), then a
+// vertical balance still waiting for its routing call.
+wg_status flush_deferred(wg_ctx *ctx) {
+  auto &q = ctx->defer;
+  wg_status st = WG_OK;
+  if (q.ndays > 0) {
+    const int nd = q.ndays;
+    q.ndays = 0;
+    st = run_steps_at(ctx, q.doy0, q.fday0, q.oday0, nd, 0, ctx->total_steps(nd));
+    if (st == WG_OK) ctx->last_vertical_fday = q.fday0 + nd - 1;
+  }
+  if (st == WG_OK && q.vpending) {
+    q.vpending = false;
+    st = vertical_now(ctx, q.vdoy, q.vfday);
+  }
+  return st;
+}
+
+extern "C" {
+
+wg_status wg_set_deferred(wg_ctx *ctx, int32_t enable) {
+  if (!ctx) return WG_ERR_INVALID;
+  if (ctx->members != 1) return WG_ERR_UNSUPPORTED;
+  wg_status st = flush_deferred(ctx);
+  ctx->defer.on = enable != 0;
+  return st;
+}
+
 wg_status wg_run_steps(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin, int32_t t_end) {
   if (!ctx || doy0 < 1 || doy0 > 365 || fday0 < 0 || ndays <= 0 || fday0 + ndays > ctx->max_days) return WG_ERR_INVALID;
   const int total = ctx->total_steps(ndays);
   if (t_begin < 0 || t_end > total || t_begin > t_end) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (t_begin == t_end) return WG_OK;
-  cudaSetDevice(ctx->device);
-  join_uploads(ctx);
-  return ctx->precision == 0 ? run_steps_impl(ctx, ctx->cd, ctx->sd, ctx->vd, ctx->rd, doy0, fday0, ndays, t_begin, t_end)
-                             : run_steps_impl(ctx, ctx->cf, ctx->sf, ctx->vf, ctx->rf, doy0, fday0, ndays, t_begin, t_end);
+  return run_steps_at(ctx, doy0, fday0, fday0, ndays, t_begin, t_end);
 }
 
 int32_t wg_run_num_steps(const wg_ctx *ctx, int32_t ndays) { return ctx ? ctx->total_steps(ndays) : 0; }
@@ -1481,6 +1607,7 @@ wg_status wg_run_days(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays) {
 
 wg_status wg_synchronize(wg_ctx *ctx) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   cudaSetDevice(ctx->device);
   cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -1507,12 +1634,14 @@ wg_status wg_clear_error(wg_ctx *ctx) {
 
 wg_status wg_set_barrier_test(wg_ctx *ctx, int32_t extra_arrivals) {
   if (!ctx || extra_arrivals < 0) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   ctx->sync.extra_arrivals = (uint32_t)extra_arrivals;
   return WG_OK;
 }
 
 wg_status wg_get_discharge(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out) {
   if (!ctx || !out || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (ctx->nstation == 0 || ndays == 0) return WG_OK;
   wg_status st = wg_synchronize(ctx);
   if (st != WG_OK) return st;
@@ -1523,8 +1652,56 @@ wg_status wg_get_discharge(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out
                    "get_discharge");
 }
 
+wg_status wg_get_member_discharge(wg_ctx *ctx, int32_t member, int32_t day0, int32_t ndays, double *out) {
+  if (!ctx || !out || member < 0 || member >= ctx->members || day0 < 0 || ndays < 0 ||
+      day0 + ndays > ctx->max_days)
+    return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
+  if (ctx->nstation == 0 || ndays == 0) return WG_OK;
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  const size_t M = ctx->members, rows = (size_t)ndays * ctx->nstation;
+  // [day][station][member]: one element of every (day, station) row
+  return cuda_fail(ctx,
+                   cudaMemcpy2D(out, sizeof(double), ctx->qst + (size_t)day0 * ctx->nstation * M + member,
+                                M * sizeof(double), sizeof(double), rows, cudaMemcpyDeviceToHost),
+                   "get_member_discharge");
+}
+
+wg_status wg_record_daily_storages(wg_ctx *ctx, int32_t enable) {
+  if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
+  if (ctx->members != 1) return WG_ERR_UNSUPPORTED;
+  cudaSetDevice(ctx->device);
+  if (enable && !ctx->daily_storage_buf) {
+    ctx->daily_storage_buf = ctx->alloc<double>((size_t)ctx->max_days * 7 * ctx->nstate());
+    if (!ctx->daily_storage_buf) return WG_ERR_NOMEM;
+  }
+  ctx->mon.daily_storage = enable ? ctx->daily_storage_buf : nullptr;
+  ctx->mon.daily_days = enable ? ctx->max_days : 0;
+  return WG_OK;
+}
+
+wg_status wg_get_daily_storages(wg_ctx *ctx, int32_t day0, int32_t ndays, double *out) {
+  if (!ctx || !out || day0 < 0 || ndays < 0 || day0 + ndays > ctx->max_days) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
+  if (!ctx->mon.daily_storage) return WG_ERR_INVALID;
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  const int n = ctx->n;
+  std::vector<double> slots((size_t)ndays * 7 * n);
+  cudaError_t e = cudaMemcpy(slots.data(), ctx->mon.daily_storage + (size_t)day0 * 7 * n,
+                             slots.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "get_daily_storages");
+  const auto &c2s = ctx->topo.cell_of_slot;
+  for (size_t r = 0; r < (size_t)ndays * 7; ++r)
+    for (int sl = 0; sl < n; ++sl) out[r * n + c2s[sl]] = slots[r * n + sl];
+  return WG_OK;
+}
+
 wg_status wg_reset_balance(wg_ctx *ctx) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   cudaSetDevice(ctx->device);
   cudaError_t e = cudaSuccess;
   if (ctx->balance.enabled)
@@ -1538,6 +1715,7 @@ wg_status wg_reset_balance(wg_ctx *ctx) {
 
 wg_status wg_get_balance(wg_ctx *ctx, double out[6]) {
   if (!ctx || !out) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (!ctx->balance.enabled) return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
   int nb = 0;
@@ -1568,6 +1746,7 @@ wg_status wg_get_balance(wg_ctx *ctx, double out[6]) {
 
 wg_status wg_get_balance_noalloc(wg_ctx *ctx, double out[6]) {
   if (!ctx || !out) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (!ctx->balance.enabled) return WG_ERR_INVALID;
   if ((int64_t)ctx->nstate() > noalloc_max_states()) {
     ctx->err = "wg_get_balance_noalloc: " + std::to_string(ctx->nstate()) + " states exceed its fixed scratch of " +
@@ -1589,6 +1768,7 @@ wg_status wg_get_balance_noalloc(wg_ctx *ctx, double out[6]) {
 
 wg_status wg_set_member_factors(wg_ctx *ctx, const float *prec_factor, const float *gamma_factor) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   cudaSetDevice(ctx->device);
   const int M = ctx->members;
   std::vector<float> fac(2 * (size_t)M, 1.0f);
@@ -1605,6 +1785,7 @@ wg_status wg_set_member_factors(wg_ctx *ctx, const float *prec_factor, const flo
 
 wg_status wg_set_step_sync(wg_ctx *ctx, int32_t flags) {
   if (!ctx || (flags != 0 && flags != 1)) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (flags == 1 && !ctx->sync.wstep) return WG_ERR_UNSUPPORTED;
   ctx->sync.flow = flags;
   return WG_OK;
@@ -1612,6 +1793,7 @@ wg_status wg_set_step_sync(wg_ctx *ctx, int32_t flags) {
 
 wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
   if (!ctx || nmonths < 0 || doy_day0 < 1 || doy_day0 > 365) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   cudaSetDevice(ctx->device);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "monthly_outputs");
@@ -1619,7 +1801,13 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
     cudaFree(ctx->mon_buf);
     ctx->mon_buf = nullptr;
   }
-  ctx->mon = DevMonthly{};
+  {   // the daily storage record is kept
+    double *ds = ctx->mon.daily_storage;
+    const int dd = ctx->mon.daily_days;
+    ctx->mon = DevMonthly{};
+    ctx->mon.daily_storage = ds;
+    ctx->mon.daily_days = dd;
+  }
   if (nmonths == 0) return WG_OK;
   const size_t per = (size_t)nmonths * ctx->nstate();
   e = cudaMalloc((void **)&ctx->mon_buf, 6 * per * sizeof(double));
@@ -1646,6 +1834,7 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
 
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out) {
   if (!ctx || !out || which < 0 || which > 5 || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   wg_status st = wg_synchronize(ctx);
   if (st != WG_OK) return st;
   const size_t N = ctx->nstate(), per = (size_t)ctx->mon.nmonths * N;
@@ -1664,6 +1853,7 @@ wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, dou
 
 wg_status wg_set_active_cells(wg_ctx *ctx, const uint8_t *active) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   cudaSetDevice(ctx->device);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "set_active_cells");
@@ -1684,6 +1874,7 @@ wg_status wg_set_active_cells(wg_ctx *ctx, const uint8_t *active) {
 
 wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values) {
   if (!ctx || !values) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (k != 0 && k != 1) return WG_ERR_UNSUPPORTED;
   for (int i = 0; i < ctx->n; ++i)
     if (!(values[i] > 0.) || !std::isfinite(values[i])) return WG_ERR_INVALID;
@@ -1693,6 +1884,7 @@ wg_status wg_set_calib_param(wg_ctx *ctx, int32_t k, const double *values) {
 
 wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks) {
   if (!ctx || !valid_block_threads(threads, ctx->precision, ctx->members) || blocks < 0) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   const bool ens = ctx->members > 1;
   const int maxb = ctx->precision == 0 ? pipeline_max_blocks<double>(true, ens, threads)
                                        : pipeline_max_blocks<float>(true, ens, threads);

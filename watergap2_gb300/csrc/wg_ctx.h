@@ -69,6 +69,7 @@ struct wg_ctx {
   DevSync sync{};
   DevMonthly mon{};                        // wg_monthly_outputs
   double *mon_buf = nullptr;
+  double *daily_storage_buf = nullptr;     // wg_record_daily_storages (context allocation)
   double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
   float *staging = nullptr;
   float *staging_async = nullptr;          // staging of wg_upload_forcing_async
@@ -90,6 +91,12 @@ struct wg_ctx {
   struct WuRes { int slot, cell, type; double mean_outflow, mean_demand; };
   std::vector<WuRes> wu_res;               // the reservoirs, for the monthly provisional release
   int last_vertical_fday = 0;              // forcing slot of the last wg_step_vertical
+  struct Deferred {                        // wg_set_deferred: the per-day calls queued
+    bool on = false;
+    int doy0 = 0, fday0 = 0, oday0 = 0, ndays = 0;   // consecutive days with both calls made
+    bool vpending = false;                 // a vertical call waiting for its routing call
+    int vdoy = 0, vfday = 0;
+  } defer;
   int va_warps_default = 0;                // vertical-balance warps the layout was sized for
   unsigned int *va_next = nullptr;         // their work counter
   Snapshot *snap = nullptr;                // device copy of the mutable state (autotuner)
@@ -145,3 +152,15 @@ struct wg_ctx {
   int total_steps(int ndays) const { return (ndays + days_per_step - 1) / days_per_step + topo.nlevel - 1; }
   void release_tools();   // snapshot and graph (wg_tune.cpp)
 };
+
+// Runs the per-day calls that wg_set_deferred has queued (wg_capi.cpp); every
+// entry point that reads or changes the model, its inputs or its run shape
+// calls it first.
+wg_status flush_deferred(wg_ctx *ctx);
+#define WG_FLUSH(ctx)                                    \
+  do {                                                   \
+    if ((ctx)->defer.on) {                               \
+      const wg_status wg_flush_st_ = flush_deferred(ctx); \
+      if (wg_flush_st_ != WG_OK) return wg_flush_st_;    \
+    }                                                    \
+  } while (0)

@@ -56,6 +56,9 @@ struct DevCellsT {
   const R *albedo, *albedo_snow, *ddf_m, *lai_min, *lai_max, *smax, *inv_smax, *fg, *rgmax, *built_up;
   const R *t_gradnt, *elev0;
   const R *band_dt;             // [nband][n] (elev_b - elev_0) * P_T_GRADNT
+  const float *snow_thr;        // FP32 paths: [nband][n] the largest float temperature at which the
+                                // band gets snowfall as the FP64 path decides it (null in FP64)
+  const double *thr64;          // FP32 paths: [2][n] P_T_GRADNT and P_T_SNOWFZ in FP64 (null in FP64)
   const int16_t *band_el;       // [nband][n] band elevation [m]
   // routing
   const R *area, *area_f;       // km2, km2 * 1e-8 (mm x % -> km3)
@@ -122,6 +125,12 @@ struct DevMonthly {
   double *cell_runoff;   // sum of transported minus upstream inflow [km3/month] (G_monthlyCellRunoff)
   double *velocity;      // sum of the river velocity [m/s x days]                (G_monthlyVelocity)
   int32_t nmonths, doy_day0, month0, enabled;
+  // the day-end routing storages of every cell and output day, [day][7][n*members]
+  // in the order the reference writes them into its state file (routing.cpp:5001-5020):
+  // local lake, local wetland, global lake, global wetland, reservoir, river,
+  // groundwater [km3]; null: not recorded
+  double *daily_storage;
+  int32_t daily_days;
 };
 
 struct DevForcing {

@@ -535,6 +535,16 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
           }
           const int stn = c.station[s];
           if (stn >= 0) qst[((size_t)(oday0 + d) * c.nstation + stn) * M + mm] = (double)tv;
+          if (mon.daily_storage && oday0 + d < mon.daily_days) {   // the state file's daily storages
+            double *ds = mon.daily_storage + (size_t)(oday0 + d) * 7 * N + si;
+            ds[0] = (double)rs.loclake;
+            ds[N] = (double)rs.locwetl;
+            ds[2 * N] = (double)rs.glolake;
+            ds[3 * N] = (double)rs.glowetl;
+            ds[4 * N] = (double)rs.res;
+            ds[5 * N] = (double)rs.river;
+            ds[6 * N] = (double)rs.gw;
+          }
           if (mon.enabled) {
             // monthly epilogue: this thread owns the cell, so no atomics
             const int od = oday0 + d;

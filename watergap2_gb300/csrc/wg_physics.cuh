@@ -255,18 +255,25 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   }
   if (cmp::lt0(soilPET)) soilPET = R(0);
 
-  // snow in elevation bands (daily.cpp:897-1062)
-  R tempElevMax = R(0), snowChange = R(0), gs = R(0);
+  // snow in elevation bands (daily.cpp:897-1062).  Whether a band gets snowfall
+  // (temp_elev <= P_T_SNOWFZ, daily.cpp:982) decides where the day's precipitation
+  // goes; the FP32 paths take that decision as the FP64 path does, from the float
+  // temperature and a per-band float threshold prepared on the host, so that FP32
+  // rounding of temp_elev never moves a band's precipitation between snow and rain.
+  constexpr bool fp32 = sizeof(R) == 4;
+  R snowChange = R(0), gs = R(0);
+  bool above0 = cmp::gt(R(0), c.t_snowfz[s]);   // band 0 above freezing: the soil runs (daily.cpp:1076)
   int thresh = 0;
   const R t_snowfz = c.t_snowfz[s], t_snowmt = c.t_snowmt[s], ddf_m = c.ddf_m[s];
   for (int e = 0; e < B; ++e) {
     R sb = band[e * bstride];
     R temp_elev = T - c.band_dt[(size_t)e * c.n + s];
-    if (land && cmp::is_zero(sb) && cmp::gt(temp_elev, t_snowfz)) {
+    bool snowfall = fp32 ? Tf <= c.snow_thr[(size_t)e * c.n + s] : cmp::le(temp_elev, t_snowfz);
+    if (land && cmp::is_zero(sb) && !snowfall) {
       // no snow and no snowfall in this band: the steps below would keep it at
       // zero, melt nothing and pass the precipitation on -- the same bits, without
       // the band's arithmetic and store
-      if (e == 0) tempElevMax = temp_elev;
+      if (e == 0) above0 = true;
       effPrec += prec_to_soil;
       continue;
     }
@@ -280,10 +287,22 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
       if (cmp::abs_le_c(sb, R(WG_MIN_STOR_VOL))) sb = R(0);
       initialStorage = sb;
       if (cmp::gt_c(sb, R(1000.))) {
-        if (thresh == 0) thresh = c.band_el[(size_t)e * c.n + s];
-        else if (thresh > 0) temp_elev = T - (R(thresh) - c.elev0[s]) * c.t_gradnt[s];
+        if (thresh == 0) {
+          thresh = c.band_el[(size_t)e * c.n + s];
+        } else if (thresh > 0) {
+          // the remembered threshold elevation's temperature, rounded as the reference
+          // rounds it (no contraction into an FMA); the FP32 paths decide in FP64
+          temp_elev = T - (R(thresh) - c.elev0[s]) * c.t_gradnt[s];
+          if constexpr (fp32) {
+            const double te = __dsub_rn((double)Tf, __dmul_rn((double)thresh - (double)c.elev0[s], c.thr64[s]));
+            snowfall = te <= c.thr64[(size_t)c.n + s];
+          } else {
+            temp_elev = __dsub_rn(T, __dmul_rn(R(thresh) - c.elev0[s], c.t_gradnt[s]));
+            snowfall = cmp::le(temp_elev, t_snowfz);
+          }
+        }
       }
-      if (cmp::le(temp_elev, t_snowfz)) {
+      if (snowfall) {
         effBefore = R(0);
         sb += prec_to_soil;
         if (cmp::gt(sb, soilPET)) {
@@ -306,7 +325,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
         }
       }
       snowChange += sb - initialStorage;
-      if (e == 0) tempElevMax = temp_elev;
+      if (e == 0) above0 = !snowfall;
       gs += sb;
       effPrec += effBefore + melt;
     }
@@ -340,7 +359,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
       overflow = soil - Smax;
       soil = Smax;
     }
-    if (cmp::gt(tempElevMax, t_snowfz)) {
+    if (above0) {
       if (cmp::gt0(Smax)) {
         const R sat = soil * c.inv_smax[s];
         runoff = effPrec * m::pow(sat, gamma_soil);

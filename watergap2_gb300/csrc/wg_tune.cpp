@@ -109,6 +109,7 @@ extern "C" {
 
 wg_status wg_save_snapshot(wg_ctx *ctx) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   cudaSetDevice(ctx->device);
   wg_status st = snapshot_save(ctx);
   return st != WG_OK ? st : wg_synchronize(ctx);
@@ -116,6 +117,7 @@ wg_status wg_save_snapshot(wg_ctx *ctx) {
 
 wg_status wg_restore_snapshot(wg_ctx *ctx) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   cudaSetDevice(ctx->device);
   wg_status st = snapshot_restore(ctx);
   return st != WG_OK ? st : wg_synchronize(ctx);
@@ -123,6 +125,7 @@ wg_status wg_restore_snapshot(wg_ctx *ctx) {
 
 wg_status wg_kernel_timing(wg_ctx *ctx, int32_t enable) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   ctx->timing = enable != 0;
   ctx->tev_used = 0;
   return WG_OK;
@@ -130,6 +133,7 @@ wg_status wg_kernel_timing(wg_ctx *ctx, int32_t enable) {
 
 wg_status wg_get_kernel_times(wg_ctx *ctx, double *vertical_ahead_ms, double *wavefront_ms, int32_t *launch_pairs) {
   if (!ctx || !vertical_ahead_ms || !wavefront_ms || !launch_pairs) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   wg_status st = wg_synchronize(ctx);
   if (st != WG_OK) return st;
   double va = 0., wf = 0.;
@@ -150,12 +154,14 @@ wg_status wg_get_kernel_times(wg_ctx *ctx, double *vertical_ahead_ms, double *wa
 
 wg_status wg_set_chunk_steps(wg_ctx *ctx, int32_t steps) {
   if (!ctx || steps < 0 || steps > ctx->chunk_cap()) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   ctx->chunk_steps = steps;
   return WG_OK;
 }
 
 wg_status wg_set_vertical_overlap(wg_ctx *ctx, int32_t enable) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   if (!enable) {
     ctx->layout.va_warps = 0;
     return WG_OK;
@@ -176,6 +182,7 @@ int32_t wg_get_chunk_steps(const wg_ctx *ctx) {
 wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin,
                       int32_t trial_steps, wg_tune_result *out) {
   if (!ctx || !out || trial_steps <= 0) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   const int total = ctx->total_steps(ndays);
   if (t_begin < 0 || t_begin + trial_steps > total) return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
@@ -265,6 +272,7 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
 
 wg_status wg_graph_capture(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, int32_t t_begin, int32_t t_end) {
   if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   const int total = ctx->total_steps(ndays);
   if (doy0 < 1 || doy0 > 365 || fday0 < 0 || ndays <= 0 || fday0 + ndays > ctx->max_days || t_begin < 0 ||
       t_end > total || t_begin >= t_end)
@@ -307,6 +315,7 @@ wg_status wg_graph_capture(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t nda
 
 wg_status wg_graph_launch(wg_ctx *ctx) {
   if (!ctx || !ctx->graph_exec) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
   cudaSetDevice(ctx->device);
   ctx->launches += ctx->graph_launches;
   return fail(ctx, cudaGraphLaunch(ctx->graph_exec, ctx->stream), "graph launch");

@@ -36,7 +36,8 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_get_kernel_times", "wg_set_member_factors", "wg_upload_forcing_async", "wg_set_active_cells",
            "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync",
            "wg_upload_water_use", "wg_set_water_use_inputs", "wg_get_water_use", "wg_set_water_use",
-           "wg_model_options_default")
+           "wg_model_options_default", "wg_get_member_discharge", "wg_set_deferred",
+           "wg_record_daily_storages", "wg_get_daily_storages")
 
 
 class WgError(RuntimeError):
@@ -110,6 +111,10 @@ def load_library(path: str = LIB_PATH):
     lib.wg_run_num_steps.argtypes = [vp, i32]
     lib.wg_run_num_steps.restype = i32
     lib.wg_get_discharge.argtypes = [vp, i32, i32, vp]
+    lib.wg_get_member_discharge.argtypes = [vp, i32, i32, i32, vp]
+    lib.wg_set_deferred.argtypes = [vp, i32]
+    lib.wg_record_daily_storages.argtypes = [vp, i32]
+    lib.wg_get_daily_storages.argtypes = [vp, i32, i32, vp]
     lib.wg_get_balance.argtypes = [vp, vp]
     lib.wg_reset_balance.argtypes = [vp]
     lib.wg_get_balance_noalloc.argtypes = [vp, vp]
@@ -304,9 +309,9 @@ class Model:
         """Forcing of len(P) days into day slots day0..; with overlap, on the copy
         stream alongside runs in flight (wg_upload_forcing_async: the days written
         must not be read by those runs; pinned sources stay unchanged until the
-        next synchronize)."""
-        P, T, S = (np.ascontiguousarray(x, np.float32) for x in (P, T, S))
-        nd = P.shape[0]
+        next synchronize).  A variable given as None keeps the slots' values."""
+        P, T, S = (None if x is None else np.ascontiguousarray(x, np.float32) for x in (P, T, S))
+        nd = next(x for x in (P, T, S) if x is not None).shape[0]
         fn = self.lib.wg_upload_forcing_async if overlap else self.lib.wg_upload_forcing
         if overlap:
             self._inflight.append((P, T, S))   # alive until the next synchronize
@@ -330,6 +335,22 @@ class Model:
     def step_vertical(self, doy: int, fday: int):
         self._check(self.lib.wg_step_vertical(self.h, int(doy), int(fday)), "step_vertical")
 
+    def set_deferred(self, enable: bool = True):
+        """wg_set_deferred: queue the per-day calls and run consecutive days as one
+        day-pipelined run when a result is next needed."""
+        self._check(self.lib.wg_set_deferred(self.h, int(bool(enable))), "set_deferred")
+
+    def record_daily_storages(self, enable: bool = True):
+        """wg_record_daily_storages: keep every cell's day-end routing storages."""
+        self._check(self.lib.wg_record_daily_storages(self.h, int(bool(enable))), "record_daily_storages")
+
+    def daily_storages(self, day0: int, ndays: int) -> np.ndarray:
+        """[ndays, 7, ncell]: local lake, local wetland, global lake, global wetland,
+        reservoir, river, groundwater [km3] after each output day."""
+        out = np.zeros((ndays, 7, self.region.ncell))
+        self._check(self.lib.wg_get_daily_storages(self.h, int(day0), int(ndays), _ptr(out)), "get_daily_storages")
+        return out
+
     def step_routing(self, doy: int, oday: int):
         self._check(self.lib.wg_step_routing(self.h, int(doy), int(oday)), "step_routing")
 
@@ -352,6 +373,13 @@ class Model:
         shape = (ndays, self.stations.size) if self.members == 1 else (ndays, self.stations.size, self.members)
         out = np.zeros(shape)
         self._check(self.lib.wg_get_discharge(self.h, int(day0), int(ndays), _ptr(out)), "get_discharge")
+        return out
+
+    def member_discharge(self, member: int, day0: int, ndays: int) -> np.ndarray:
+        """Discharge of one ensemble member [ndays, nstation]."""
+        out = np.zeros((ndays, self.stations.size))
+        self._check(self.lib.wg_get_member_discharge(self.h, int(member), int(day0), int(ndays), _ptr(out)),
+                    "get_member_discharge")
         return out
 
     def discharge_into(self, day0: int, ndays: int, out: np.ndarray) -> np.ndarray:
