@@ -115,8 +115,8 @@ class Context {
   void set_water_use(const double *in) { check(wg_set_water_use(ctx_, in), "wg_set_water_use"); }
 
   void check(wg_status s, const char *what) const {
-    if (s != WG_OK)
-      throw Error(s, std::string(what) + ": " + wg_status_string(s) + (ctx_ ? std::string(" ") + wg_last_error(ctx_) : ""));
+    if (s != WG_OK)   // without a context: why this thread's wg_create failed
+      throw Error(s, std::string(what) + ": " + wg_status_string(s) + " " + wg_last_error(ctx_));
   }
 
  private:

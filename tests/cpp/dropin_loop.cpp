@@ -14,6 +14,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <exception>
 #include <string>
 #include <vector>
 
@@ -66,7 +67,18 @@ static std::vector<T> slurp(FILE *f, size_t count) {
   return v;
 }
 
+static int run(int argc, char **argv);
+
 int main(int argc, char **argv) {
+  try {
+    return run(argc, argv);
+  } catch (const std::exception &e) {
+    fprintf(stderr, "dropin_loop: %s\n", e.what());
+    return 5;
+  }
+}
+
+static int run(int argc, char **argv) {
   if (argc < 3) return 1;
   const std::string dir = argv[1];
   const int years = atoi(argv[2]);
@@ -97,6 +109,7 @@ int main(int argc, char **argv) {
 
   wg_options o{};
   o.max_days = 365;
+  o.members = 1;
   std::vector<int32_t> stations(n);
   for (int i = 0; i < n; ++i) stations[i] = i;
   o.nstation = n;

@@ -58,7 +58,8 @@ def test_dropin_loop_matches_pipelined_run(tmp_path):
     tmp = str(tmp_path)
     _write_case(tmp, region, P, T, S)
     exe = _build(tmp)
-    run = subprocess.run([exe, tmp, str(YEARS)], check=True, capture_output=True, text=True)
+    run = subprocess.run([exe, tmp, str(YEARS)], capture_output=True, text=True)
+    assert run.returncode == 0, (run.returncode, run.stdout[-2000:], run.stderr[-2000:])
     secs = float(run.stdout.split()[0])
     raw = np.fromfile(os.path.join(tmp, "out.bin"), np.float64)
     o = 0

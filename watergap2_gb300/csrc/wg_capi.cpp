@@ -254,7 +254,7 @@ struct HostConsts {
   X(albedo) X(albedo_snow) X(ddf_m) X(lai_min) X(lai_max) X(smax) X(inv_smax) X(fg) X(rgmax) X(built_up)         \
   X(t_gradnt) X(elev0) X(area) X(area_f) X(gw_e) X(gw_ik) X(gw_ome) X(sw_k) X(sw_e) X(sw_ik) X(sw_ome) X(evx)    \
   X(a6) X(ll100) X(maxs_ll) X(inv_maxs_ll) X(lw100) X(maxs_lw) X(inv_maxs_lw) X(la6) X(maxs_gl) X(inv_maxs_gl)  \
-  X(ra6) X(rcap) X(inv_rcap) X(rcap01) X(inv_rcap085) X(c_ratio) X(c4) X(one_m_c4) X(prov_rel) X(gw100)         \
+  X(ra6) X(rcap) X(rcap01) X(c_ratio) X(c4) X(one_m_c4) X(prov_rel) X(gw100)                                   \
   X(maxs_gw) X(inv_maxs_gw) X(bw) X(inv_mr) X(sqrt_slope) X(inv_len) X(rlen) X(fcatch)
 #define X(f) std::vector<double> f;
   WG_RFIELDS(X)
@@ -934,9 +934,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     h.inv_maxs_gl[i] = safe_inv(h.maxs_gl[i]);
     h.ra6[i] = r->res_area[i] / 1000000.;
     h.rcap[i] = r->stor_cap[i];
-    h.inv_rcap[i] = safe_inv(r->stor_cap[i]);
     h.rcap01[i] = r->stor_cap[i] * 0.1;
-    h.inv_rcap085[i] = safe_inv(r->stor_cap[i] * 0.85);
     if (r->res_area[i] > 0.) {
       h.c_ratio[i] = r->stor_cap[i] / (r->mean_outflow[i] * 31536000. / 1000000000.);
       h.c4[i] = (4. * h.c_ratio[i] * h.c_ratio[i]);

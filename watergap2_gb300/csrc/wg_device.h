@@ -68,7 +68,7 @@ struct DevCellsT {
   const R *ll100, *maxs_ll, *inv_maxs_ll;         // local lake
   const R *lw100, *maxs_lw, *inv_maxs_lw;         // local wetland
   const R *la6, *maxs_gl, *inv_maxs_gl;           // global lake
-  const R *ra6, *rcap, *inv_rcap, *rcap01, *inv_rcap085, *c_ratio, *c4, *one_m_c4, *prov_rel;  // reservoir
+  const R *ra6, *rcap, *rcap01, *c_ratio, *c4, *one_m_c4, *prov_rel;   // reservoir
   const R *gw100, *maxs_gw, *inv_maxs_gw;         // global wetland
   const R *bw, *inv_mr, *sqrt_slope, *inv_len, *rlen;   // river
   const R *fcatch;                                // fractional routing: share of the runoff through the water bodies

@@ -46,6 +46,26 @@ template <> struct M<float> {
   static __device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
 };
 
+// Operations rounded once each and never contracted into an FMA (FP64), for the
+// few expressions whose rounding the reference's storages integrate without
+// feedback: a reservoir's release is not a function of its storage, so a
+// rounding that differs from the reference's in the same direction every day
+// (a folded constant like 1e9 / 86400, a product contracted with a sum) moves
+// its storage a little further each day.  FP32: the plain operations.
+template <class R> struct E;
+template <> struct E<double> {
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+};
+template <> struct E<float> {
+  static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+  static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+  static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+  static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+};
+
 // Comparisons of the day step's hot loops.  On GB300 a double compare issues on
 // the FP64 pipe (2 lanes per SM per clock) like an FMA; these give the same
 // answers for every non-NaN operand from integer instructions on the bit
@@ -753,14 +773,15 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     st.glolake = S;
     st.rf_glolake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
   }
-  if (fl & F_RES) {  // reservoir (routing.cpp:2807-3082)
+  if (fl & F_RES) {  // reservoir (routing.cpp:2807-3082), each expression rounded as the reference rounds it
+    typedef E<R> x;
     const R S0 = st.res, maxS = c.rcap[s], rf = st.rf_res;
-    R evapo = (R(1.0) - cfa) * owp + cfa * owpet * rf;
+    R evapo = x::add(x::mul(x::sub(R(1.0), cfa), owp), x::mul(cfa, x::mul(owpet, rf)));   // routing.cpp:2832-2836
     if (evapo < R(0)) evapo = R(0);
-    const R pin = owp * c.ra6[s];
-    const R TI = inflow + pin;
-    const R PETgwr = evapo * c.ra6[s];
-    const R PETgwrMax = S0 + TI;
+    const R pin = x::mul(owp, c.ra6[s]);
+    const R TI = x::add(inflow, pin);
+    const R PETgwr = x::mul(evapo, c.ra6[s]);
+    const R PETgwrMax = x::add(S0, TI);
     rt.p_ow += pin;
     R remRes0 = R(0);
     if constexpr (WU) {   // routing.cpp:2869-2877
@@ -798,15 +819,19 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     R K = st.k_release;
     if (month == c.start_month[s] - 1 && doy == c_first_day_in_month[month]) {
-      K = (S < c.rcap01[s]) ? R(0.1) : S * c.inv_rcap085[s];
+      K = (S < c.rcap01[s]) ? R(0.1) : x::div(S, x::mul(maxS, R(0.85)));   // routing.cpp:2959-2962
       st.k_release = K;
     }
     // the provisional release of an irrigation reservoir follows the month's demand
     const R prov = WU ? R(wu->tab[wrow + 4 * (size_t)c.n + s]) : c.prov_rel[s];
-    R release;
-    if (c.c_ratio[s] >= R(0.5)) release = K * prov;
-    else release = c.c4[s] * K * prov + c.one_m_c4[s] * inflow * R(1.0e9 / 86400.);
-    outflow = ((S >= c.rcap01[s]) ? release : R(0.1) * release) * R(86400. / 1.0e9);
+    R release;   // m3/s (routing.cpp:3003-3008)
+    if (c.c_ratio[s] >= R(0.5)) release = x::mul(K, prov);
+    else
+      release = x::add(x::mul(x::mul(c.c4[s], K), prov),
+                       x::div(x::mul(x::mul(c.one_m_c4[s], inflow), R(1.0e9)), R(86400.)));
+    // km3 per day; a tenth below 10 % of the capacity (routing.cpp:3012-3017)
+    outflow = (S >= c.rcap01[s]) ? x::div(x::mul(release, R(86400.)), R(1.0e9))
+                                 : x::div(x::mul(x::mul(R(0.1), release), R(86400.)), R(1.0e9));
     if (outflow < R(0)) outflow = R(0);
     S -= outflow;
     if (S > maxS) {
@@ -822,7 +847,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if constexpr (WT) {
       wtm->res_prev = S0; wtm->res_evapo = evapo; wtm->res_out = outflow;
     }
-    R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_rcap[s], R(2.81383));
+    R r = R(1.) - m::pow(x::div(m::fabs_(S - maxS), maxS), R(2.81383));   // routing.cpp:3071-3072
     st.res = S;
     st.rf_res = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
   }
