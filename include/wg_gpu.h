@@ -229,6 +229,12 @@ wg_status wg_upload_forcing_async(wg_ctx *ctx, int32_t day0, int32_t ndays, cons
 wg_status wg_upload_forcing_unf(wg_ctx *ctx, int32_t day0, int32_t nd_file, int32_t d_first, int32_t ndays,
                                 const void *prec, const void *temp, const void *swrad, int32_t overlap);
 
+/* The same from native float arrays, cell-major [ncell][nd_file] -- the layout of
+ * the reference's yearly grids in memory (climateYear.G_*_d365(n, day - 1),
+ * DailyGrid, grid.h:471-474), so a driver passes them without a transpose. */
+wg_status wg_upload_forcing_cells(wg_ctx *ctx, int32_t day0, int32_t nd_file, int32_t d_first, int32_t ndays,
+                                  const float *prec, const float *temp, const float *swrad, int32_t overlap);
+
 /* Read `bytes` bytes of a file into dst (e.g. a pinned buffer for
  * wg_upload_forcing_unf); returns the bytes read, -1 if the file cannot be
  * opened. */

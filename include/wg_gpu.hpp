@@ -74,6 +74,12 @@ class Context {
   void upload_forcing_async(int day0, int ndays, const float *prec, const float *temp, const float *swrad) {
     check(wg_upload_forcing_async(ctx_, day0, ndays, prec, temp, swrad), "wg_upload_forcing_async");
   }
+  // the reference's in-memory yearly grids, cell-major [ncell][nd_file] native floats
+  void upload_forcing_cells(int day0, int nd_file, int d_first, int ndays, const float *prec, const float *temp,
+                            const float *swrad, bool overlap = false) {
+    check(wg_upload_forcing_cells(ctx_, day0, nd_file, d_first, ndays, prec, temp, swrad, overlap ? 1 : 0),
+          "wg_upload_forcing_cells");
+  }
   // the reference's yearly UNF climate files as read (big-endian, cell-major)
   void upload_forcing_unf(int day0, int nd_file, int d_first, int ndays, const void *prec, const void *temp,
                           const void *swrad, bool overlap) {

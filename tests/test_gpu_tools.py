@@ -164,6 +164,29 @@ def test_forcing_from_unf_files_equals_day_major_upload(tmp_path):
     assert np.array_equal(m.discharge(0, nd), q_ref)
 
 
+def test_forcing_from_cell_major_arrays_equals_day_major_upload():
+    """The reference's in-memory yearly grids (cell-major native floats, as
+    climateYear.G_*_d365 holds them) transposed on the GPU give the same run as
+    the day-major upload, straight and overlapped, a year at a time and a part
+    of a year (d_first)."""
+    from watergap2_gb300.gpu import Model
+    nd = 2 * 365
+    region, (P, T, S) = _region_and_forcing(29, nd)
+    ref = Model(region, max_days=nd)
+    q_ref = ref.run(1, P, T, S)
+    m = Model(region, max_days=nd)
+    for y in range(2):
+        sl = slice(365 * y, 365 * (y + 1))
+        cm = [np.ascontiguousarray(x[sl].T) for x in (P, T, S)]      # [ncell][365]
+        if y == 0:
+            m.upload_forcing_cells(0, *cm, d_first=0, ndays=200)
+            m.upload_forcing_cells(200, *cm, d_first=200, ndays=165)
+        else:
+            m.upload_forcing_cells(365, *cm, overlap=True)
+    m.run_days(1, 0, nd)
+    assert np.array_equal(m.discharge(0, nd), q_ref)
+
+
 def test_monthly_aggregates_match_daily_outputs():
     """The wavefront's monthly epilogue against the daily outputs: sums of the
     daily discharge of every cell, their minimum and maximum, and the sum of the

@@ -1181,8 +1181,13 @@ wg_status wg_upload_forcing(wg_ctx *ctx, int32_t day0, int32_t ndays, const floa
   return upload_forcing_on(ctx, ctx->stream, ctx->staging, day0, ndays, prec, temp, swrad);
 }
 
-wg_status wg_upload_forcing_unf(wg_ctx *ctx, int32_t day0, int32_t nd_file, int32_t d_first, int32_t ndays,
-                                const void *prec, const void *temp, const void *swrad, int32_t overlap) {
+}  // extern "C"
+
+// cell-major forcing [ncell][nd_file] to the device as it is; transpose (and the
+// byte swap of big-endian file bytes) there
+static wg_status upload_cell_major(wg_ctx *ctx, int32_t day0, int32_t nd_file, int32_t d_first, int32_t ndays,
+                                   const void *prec, const void *temp, const void *swrad, int32_t overlap,
+                                   bool big_endian) {
   if (!ctx || !prec || !temp || !swrad || nd_file <= 0 || d_first < 0 || ndays < 0 || d_first + ndays > nd_file ||
       day0 < 0 || day0 + ndays > ctx->max_days)
     return WG_ERR_INVALID;
@@ -1203,7 +1208,7 @@ wg_status wg_upload_forcing_unf(wg_ctx *ctx, int32_t day0, int32_t nd_file, int3
     cudaError_t e = cudaMemcpyAsync(ctx->unf_raw[which], src[k], per * 4, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
       e = launch_unf_forcing(ctx->unf_raw[which], dst[k] + (size_t)day0 * ctx->n, ctx->d_cell_of_slot, ctx->n,
-                             nd_file, d_first, ndays, st);
+                             nd_file, d_first, ndays, st, big_endian);
     ctx->launches++;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "upload_forcing_unf");
   }
@@ -1213,6 +1218,18 @@ wg_status wg_upload_forcing_unf(wg_ctx *ctx, int32_t day0, int32_t nd_file, int3
     ctx->upload_pending = true;
   }
   return WG_OK;
+}
+
+extern "C" {
+
+wg_status wg_upload_forcing_unf(wg_ctx *ctx, int32_t day0, int32_t nd_file, int32_t d_first, int32_t ndays,
+                                const void *prec, const void *temp, const void *swrad, int32_t overlap) {
+  return upload_cell_major(ctx, day0, nd_file, d_first, ndays, prec, temp, swrad, overlap, true);
+}
+
+wg_status wg_upload_forcing_cells(wg_ctx *ctx, int32_t day0, int32_t nd_file, int32_t d_first, int32_t ndays,
+                                  const float *prec, const float *temp, const float *swrad, int32_t overlap) {
+  return upload_cell_major(ctx, day0, nd_file, d_first, ndays, prec, temp, swrad, overlap, false);
 }
 
 wg_status wg_math_eval(int32_t device, int32_t fn, const double *x, const double *y, int64_t n, double *out) {

@@ -659,7 +659,7 @@ __global__ void k_gather_forcing(const float *__restrict__ src, float *__restric
 // 32 slots of one day (contiguous); the byte swap is one byte permute.
 __global__ void __launch_bounds__(256) k_unf_forcing(const uint32_t *__restrict__ raw, float *__restrict__ dst,
                                                      const int32_t *__restrict__ cell_of_slot, int n, int nd_file,
-                                                     int d_first, int nd) {
+                                                     int d_first, int nd, unsigned swap) {
   __shared__ float tile[32][33];
   const int s0 = blockIdx.x * 32, d0 = blockIdx.y * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -667,7 +667,7 @@ __global__ void __launch_bounds__(256) k_unf_forcing(const uint32_t *__restrict_
     const int s = s0 + r, d = d0 + tx;
     if (s < n && d < nd) {
       const uint32_t v = raw[(size_t)cell_of_slot[s] * nd_file + d_first + d];
-      tile[r][tx] = __uint_as_float(__byte_perm(v, 0u, 0x0123));
+      tile[r][tx] = __uint_as_float(__byte_perm(v, 0u, swap));   // 0x0123: big-endian file bytes
     }
   }
   __syncthreads();
@@ -678,9 +678,10 @@ __global__ void __launch_bounds__(256) k_unf_forcing(const uint32_t *__restrict_
 }
 
 cudaError_t launch_unf_forcing(const uint32_t *raw, float *dst, const int32_t *cell_of_slot, int n, int nd_file,
-                               int d_first, int nd, cudaStream_t st) {
+                               int d_first, int nd, cudaStream_t st, bool big_endian) {
   const dim3 grid((unsigned)((n + 31) / 32), (unsigned)((nd + 31) / 32));
-  k_unf_forcing<<<grid, 256, 0, st>>>(raw, dst, cell_of_slot, n, nd_file, d_first, nd);
+  k_unf_forcing<<<grid, 256, 0, st>>>(raw, dst, cell_of_slot, n, nd_file, d_first, nd,
+                                      big_endian ? 0x0123u : 0x3210u);
   return cudaGetLastError();
 }
 

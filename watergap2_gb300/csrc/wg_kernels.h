@@ -43,7 +43,7 @@ cudaError_t launch_math_eval(int fn, const double *x, const double *y, double *o
 cudaError_t launch_gather_forcing(const float *src, float *dst, const int32_t *cell_of_slot, int n, int ndays,
                                   cudaStream_t st);
 cudaError_t launch_unf_forcing(const uint32_t *raw, float *dst, const int32_t *cell_of_slot, int n, int nd_file,
-                               int d_first, int nd, cudaStream_t st);
+                               int d_first, int nd, cudaStream_t st, bool big_endian = true);
 template <class R>
 cudaError_t launch_vertical(const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v, const DevForcing &f,
                             int doy, int fday, cudaStream_t st);

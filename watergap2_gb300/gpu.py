@@ -37,7 +37,7 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync",
            "wg_upload_water_use", "wg_set_water_use_inputs", "wg_get_water_use", "wg_set_water_use",
            "wg_model_options_default", "wg_get_member_discharge", "wg_set_deferred",
-           "wg_record_daily_storages", "wg_get_daily_storages")
+           "wg_record_daily_storages", "wg_get_daily_storages", "wg_upload_forcing_cells")
 
 
 class WgError(RuntimeError):
@@ -113,6 +113,7 @@ def load_library(path: str = LIB_PATH):
     lib.wg_get_discharge.argtypes = [vp, i32, i32, vp]
     lib.wg_get_member_discharge.argtypes = [vp, i32, i32, i32, vp]
     lib.wg_set_deferred.argtypes = [vp, i32]
+    lib.wg_upload_forcing_cells.argtypes = [vp, i32, i32, i32, i32, vp, vp, vp, i32]
     lib.wg_record_daily_storages.argtypes = [vp, i32]
     lib.wg_get_daily_storages.argtypes = [vp, i32, i32, vp]
     lib.wg_get_balance.argtypes = [vp, vp]
@@ -316,6 +317,18 @@ class Model:
         if overlap:
             self._inflight.append((P, T, S))   # alive until the next synchronize
         self._check(fn(self.h, int(day0), nd, _ptr(P), _ptr(T), _ptr(S)), "upload_forcing")
+
+    def upload_forcing_cells(self, day0: int, P, T, S, d_first: int = 0, ndays: int | None = None,
+                             overlap: bool = False):
+        """Cell-major float forcing [ncell, nd_file] (the reference's in-memory
+        yearly grids) into day slots day0..: wg_upload_forcing_cells."""
+        P, T, S = (np.ascontiguousarray(x, np.float32) for x in (P, T, S))
+        nd_file = P.shape[1]
+        ndays = nd_file - d_first if ndays is None else ndays
+        if overlap:
+            self._inflight.append((P, T, S))
+        self._check(self.lib.wg_upload_forcing_cells(self.h, int(day0), nd_file, int(d_first), int(ndays), _ptr(P),
+                                                     _ptr(T), _ptr(S), int(bool(overlap))), "upload_forcing_cells")
 
     def upload_forcing_unf(self, day0: int, prec_raw, temp_raw, swrad_raw, nd_file: int = 365, d_first: int = 0,
                            ndays: int | None = None, overlap: bool = False):
