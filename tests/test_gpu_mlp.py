@@ -20,6 +20,8 @@ def test_forward_matches_cpu_restatement():
     y = net.forward(x)
     y_ref, _ = mo.forward(net.params(), x)
     scale = np.abs(y_ref).max()
+    print(f"forward: max {np.abs(y - y_ref).max() / scale:.2e}, median {np.median(np.abs(y - y_ref)) / scale:.2e} "
+          "of the output scale")
     # FP32 accumulation order differs; a BF16 rounding of a hidden activation can
     # land one unit apart -- far below the output scale
     assert np.abs(y - y_ref).max() <= 2e-2 * scale, (np.abs(y - y_ref).max(), scale)
@@ -36,6 +38,7 @@ def test_gradient_matches_cpu_restatement():
     g_ref, loss_ref = mo.gradient(net.params(), x, t)
     assert abs(loss - loss_ref) <= 1e-3 * loss_ref
     rel = np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)
+    print(f"gradient: relative norm error {rel:.2e}, loss {abs(loss - loss_ref) / loss_ref:.2e}")
     assert rel <= 2e-2, rel
     # every layer's block agrees, biases included
     o = 0
