@@ -22,10 +22,11 @@ def test_forward_matches_cpu_restatement():
     scale = np.abs(y_ref).max()
     print(f"forward: max {np.abs(y - y_ref).max() / scale:.2e}, median {np.median(np.abs(y - y_ref)) / scale:.2e} "
           "of the output scale")
-    # FP32 accumulation order differs; a BF16 rounding of a hidden activation can
-    # land one unit apart -- far below the output scale
-    assert np.abs(y - y_ref).max() <= 2e-2 * scale, (np.abs(y - y_ref).max(), scale)
-    assert np.median(np.abs(y - y_ref)) <= 1e-3 * scale
+    # FP32 accumulation order differs, so a BF16 rounding of a hidden activation
+    # can land one unit apart (measured on GB300: max 3.5e-5, median 3e-9 of the
+    # output scale)
+    assert np.abs(y - y_ref).max() <= 1e-3 * scale, (np.abs(y - y_ref).max(), scale)
+    assert np.median(np.abs(y - y_ref)) <= 1e-6 * scale
 
 
 def test_gradient_matches_cpu_restatement():
@@ -36,16 +37,16 @@ def test_gradient_matches_cpu_restatement():
     t = rng.normal(size=(256, 2)).astype(np.float32)
     g, loss = net.gradient(x, t)
     g_ref, loss_ref = mo.gradient(net.params(), x, t)
-    assert abs(loss - loss_ref) <= 1e-3 * loss_ref
+    assert abs(loss - loss_ref) <= 1e-6 * loss_ref
     rel = np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)
     print(f"gradient: relative norm error {rel:.2e}, loss {abs(loss - loss_ref) / loss_ref:.2e}")
-    assert rel <= 2e-2, rel
+    assert rel <= 1e-4, rel   # measured on GB300: 3.4e-6
     # every layer's block agrees, biases included
     o = 0
     for n_out in (128, 128, 128, 16):
         for size in (n_out * 128, n_out):
             a, b = g[o:o + size], g_ref[o:o + size]
-            assert np.linalg.norm(a - b) <= 3e-2 * np.linalg.norm(b) + 1e-7, o
+            assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(b) + 1e-9, o
             o += size
 
 

@@ -38,12 +38,17 @@ template <> struct M<double> {
   static __device__ __forceinline__ double pow(double x, double y) { return fm::pow(x, y); }
   static __device__ __forceinline__ double rcp(double x) { return fm::rcp_pos(x); }   // x normal, nonzero
   static __device__ __forceinline__ double fabs_(double x) { return fabs(x); }
+  // 1 - exp(-k) as the reference writes it (its rounding is the parity target)
+  static __device__ __forceinline__ double one_m_exp_neg(double k, double e) { return 1. - e; }
 };
 template <> struct M<float> {
   static __device__ __forceinline__ float exp(float x) { return expf(x); }
   static __device__ __forceinline__ float pow(float x, float y) { return (x > 0.f) ? powf(x, y) : 0.f; }
   static __device__ __forceinline__ float rcp(float x) { return 1.0f / x; }
   static __device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
+  // 1 - exp(-k) without the cancellation of the subtraction: a slow river's
+  // small k leaves 1 - expf(-k) with a relative error of 1e-7 / k in FP32
+  static __device__ __forceinline__ float one_m_exp_neg(float k, float) { return -expm1f(-k); }
 };
 
 // Operations rounded once each and never contracted into an FMA (FP64), for the
@@ -897,7 +902,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   rt.velocity = velocity;
   const R K = velocity * c.inv_len[s];
   const R eK = m::exp(-K);
-  const R omeK = R(1.) - eK;
+  const R omeK = m::one_m_exp_neg(K, eK);
   R S, transported;
   const R remRiver0 = remainingUse;
   if constexpr (WU) {   // the use the river can meet (routing.cpp:3465-3514)
