@@ -441,6 +441,16 @@ wg_status upload_cells(wg_ctx *ctx, const HostConsts &h, DevCellsT<R> &c, double
   c.thr64 = nullptr;
   if (sizeof(R) == 4) {   // the FP32 paths' snowfall decisions (vertical_cell)
     c.snow_thr = upload_raw<float>(ctx, bands_to_slots<float>(ctx, h.snow_thr.data(), ctx->nband), st);
+    // the arid recharge rule dailyPrec <= P_PCRITGWA (daily.cpp:1172) on a float
+    // precipitation: against the largest float not above the FP64 threshold it
+    // takes the FP64 path's decision for every input
+    std::vector<float> pc(ctx->n);
+    for (int i = 0; i < ctx->n; ++i) {
+      float f = (float)h.pcritgwa[i];
+      if ((double)f > h.pcritgwa[i]) f = std::nextafter(f, -FLT_MAX);
+      pc[i] = f;
+    }
+    c.pcritgwa = (const R *)upload_slots<float>(ctx, pc, st);
     std::vector<double> t64(2 * (size_t)ctx->n);
     for (int sl = 0; sl < ctx->n; ++sl) {
       const int cell = ctx->topo.cell_of_slot[sl];
