@@ -581,8 +581,8 @@ def run_gpu(args, rank, world):
             for d in range(nd):
                 pd.step_vertical(d + 1, d)
                 pd.step_routing(d + 1, d)
-                if d + 1 in month_end:
-                    pd.get_state()
+                if d + 1 in month_end:   # what integrate_wghm_ reads at a month end (integrateWGHM.cpp:830-847)
+                    pd.get_state(fields=("canopy", "soil", "snow", "snow_band", "laf"))
             pd.synchronize()
             sec = time.perf_counter() - t0
             per_day[name] = {"value": region.ncell * nd / sec, "unit": "cell-days/s", "days": nd,

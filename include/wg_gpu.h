@@ -83,7 +83,8 @@ typedef struct wg_region {
 } wg_region;
 
 /* Host view of the dynamic state (caller-owned arrays, length ncell unless noted;
- * snow_band is [ncell*nband], cell-major). */
+ * snow_band is [ncell*nband], cell-major).  A NULL field is skipped: a get or set
+ * copies only the fields given. */
 typedef struct wg_state_view {
   double *canopy, *soil, *snow, *snow_band;
   int32_t *lai_days, *lai_status;

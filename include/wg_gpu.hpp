@@ -179,8 +179,6 @@ class DropInCore {
     ctx.check(wg_set_deferred(ctx.get(), 1), "wg_set_deferred");
     ctx.check(wg_record_daily_storages(ctx.get(), 1), "wg_record_daily_storages");
     canopy.resize(n); soil.resize(n); snow.resize(n); snow_band.resize((size_t)n * nband); laf.resize(n);
-    laf_prev.resize(n); fswb.resize(n); scratch.resize(n * 16);
-    lai_days.resize(n); lai_status.resize(n); laf_started.resize(n);
   }
   Context &ctx;
   const int n, nband;
@@ -191,21 +189,16 @@ class DropInCore {
   std::vector<int> month_days;               // day_in_month of the month's routed days
   std::vector<int> month_slots;              // their output slots
   // host copies, valid after sync()
-  std::vector<double> canopy, soil, snow, snow_band, laf, laf_prev, fswb, scratch;
-  std::vector<int32_t> lai_days, lai_status, laf_started;
+  std::vector<double> canopy, soil, snow, snow_band, laf;
   bool fresh = false;
 
-  // run what is queued and copy the state the month end reads
+  // run what is queued and copy the state the month end reads (the other
+  // fields of the view stay null: wg_get_state skips them)
   void sync() {
     if (fresh) return;
     wg_state_view v{};
-    double *sc = scratch.data();
     v.canopy = canopy.data(); v.soil = soil.data(); v.snow = snow.data(); v.snow_band = snow_band.data();
-    v.lai_days = lai_days.data(); v.lai_status = lai_status.data(); v.lai_precsum = sc;
-    v.gw = sc + n; v.river = sc + 2 * n; v.loclake = sc + 3 * n; v.locwetl = sc + 4 * n; v.glolake = sc + 5 * n;
-    v.glowetl = sc + 6 * n; v.res = sc + 7 * n; v.rf_loclake = sc + 8 * n; v.rf_locwetl = sc + 9 * n;
-    v.rf_glolake = sc + 10 * n; v.rf_glowetl = sc + 11 * n; v.rf_res = sc + 12 * n; v.k_release = sc + 13 * n;
-    v.laf = laf.data(); v.laf_prev = laf_prev.data(); v.fswb_next = fswb.data(); v.laf_started = laf_started.data();
+    v.laf = laf.data();
     ctx.state(v);
     fresh = true;
   }

@@ -415,8 +415,11 @@ class Model:
     def reset_balance(self):
         self._check(self.lib.wg_reset_balance(self.h), "reset_balance")
 
-    def get_state(self, member: int = 0) -> dict:
+    def get_state(self, member: int = 0, fields=None) -> dict:
+        """The state in cell order; `fields` limits the copy to those fields."""
         st = empty_state(self.region.ncell, self.region.nband)
+        if fields is not None:
+            st = {k: a for k, a in st.items() if k in fields}
         v = _StateView()
         for k, a in st.items():
             setattr(v, k, a.ctypes.data)
