@@ -98,3 +98,48 @@ def test_water_temperature_days_per_step():
     assert np.array_equal(ta, tb) and np.array_equal(ia, ib)
     assert np.array_equal(a.river_temp(0, nd), b.river_temp(0, nd))
     assert np.array_equal(a.discharge(0, nd), b.discharge(0, nd))
+
+
+def test_global_grid_as_benchmarked_vs_oracle():
+    """The global grid with fractional routing and the water temperature of
+    every water body, in the bench's launch set-up (five days per wavefront
+    step, chunks of four steps, the next chunk's vertical balance inside the
+    wavefront launches), over a northern winter: the temperature and ice of
+    every water body of every cell after 90 days, and the outlets' daily river
+    temperature (within 1e-11 of the temperature in K) and discharge, against
+    the oracle."""
+    from oracle import Oracle
+    from watergap2_gb300 import synthetic as sy
+    from watergap2_gb300.gpu import Model
+    region = sy.region_global().with_options(frac_routing=1)
+    nd = 90
+    P, T, S = sy.forcing(region, nd, seed=2, doy0=1)
+    LW, GWT = sy.water_temp_inputs(region, nd, T)
+    outlets = np.nonzero(region.downstream < 0)[0]
+    m = Model(region, max_days=nd, stations=outlets, water_temp=True, days_per_step=5)
+    assert m.vertical_overlap() > 0 and m.chunk_steps() == 4
+    m.set_water_temp_inputs(GWT)
+    m.upload_forcing(0, P, T, S)
+    m.upload_longwave(0, LW)
+    m.run_days(1, 0, nd)
+    temp, ice = m.water_temp()
+    tq, q = m.river_temp(0, nd), m.discharge(0, nd)
+    del m
+    o = Oracle(region)
+    o.init_water_temp(GWT)
+    q_ref, dt = o.run_wt(1, P, T, S, LW, discharge=True, daily_temp=True, nthreads=os.cpu_count() or 1)
+    t_ref = np.where(dt == -9999., np.maximum(T.astype(np.float64), 0.0), dt)
+    bad_t = ~_close(temp, o.wt["temp"], 1.0)
+    bad_i = ~_close(ice, o.wt["ice"], 1e-9)
+    print("global grid, 90 days: largest |temp diff|", np.abs(temp - o.wt["temp"]).max(),
+          "largest |ice diff|", np.abs(ice - o.wt["ice"]).max(), "cells with ice", int((ice > 0).sum()))
+    assert not bad_t.any(), np.argwhere(bad_t)[:5]
+    assert not bad_i.any(), np.argwhere(bad_i)[:5]
+    # a temperature is the energy over the heat capacity in K, less 273.15: its
+    # rounding scales with the absolute temperature, and a river near 0 degC that
+    # carries its upstream cells' rounding for weeks differs by ~1e-10 degC
+    bad = np.argwhere(np.abs(tq - t_ref[:, outlets]) > 1e-11 * (np.abs(t_ref[:, outlets]) + 273.15))
+    assert len(bad) == 0, (len(bad), [(int(d), int(outlets[j]), float(tq[d, j]), float(t_ref[d, outlets[j]]))
+                                      for d, j in bad[:8]])
+    assert np.all(np.abs(q - q_ref[:, outlets]) <= 1e-10 * np.maximum(np.abs(q_ref[:, outlets]), 1e-12))
+    assert (ice > 0).sum() > 1000 and (ice[3:5] > 0).any()   # rivers and global lakes/reservoirs under ice

@@ -282,85 +282,6 @@ __global__ void __launch_bounds__(VaBounds<R, ENS>::threads, VaBounds<R, ENS>::m
     va_cell<R, ENS>(c, st, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e, i, N);
 }
 
-// Water temperature of cell s after its routing (routing.cpp:4241-4513): the
-// inputs of calcWTemp from the cell's routing terms, the upstream river outflow
-// of the day and the energy it carries; updates the cell's temperatures and ice
-// (a water body without a temperature keeps the air temperature, at least 0)
-// and returns the river temperature the downstream cell reads.
-template <class R>
-__device__ __forceinline__ double cell_water_temp(const DevCellsT<R> &c, const DevWaterTemp &w, const DevForcing &f,
-                                                  int s, size_t si, size_t N, size_t fo, uint32_t fl, const VOut<R> &o,
-                                                  const WTerms<R> &x, R river_stor, double tot_in, double e_in) {
-  wt::WtIn t;
-  t.calc_temp_pp = 0.; t.pp_withdrawal = 0.; t.pp_consumption = 0.;
-  t.short_rad = (double)f.swrad[fo];
-  t.long_rad = (double)w.lw[fo];
-  t.air_temp = (double)f.temp[fo];
-  const float g = w.gwt[s];
-  t.gw_temp = g < 0.f ? 0. : (double)g;
-  t.cfa = (double)c.cfa[s];
-  t.ow_pet = (double)o.owpet;
-  t.ow_prec = (double)o.owp;
-  t.cell_area = (double)c.area[s];
-  t.inflow_sum = tot_in;
-  t.inflow_energy = e_in;
-  t.own_temp_prev = w.temp[si];
-  for (int k = 0; k < 6; ++k) t.ice[k] = w.ice[(size_t)k * N + si];
-  t.loclake_area = w.ll_pct[s];
-  t.loclake_stor_prev = (double)x.loclake_prev + (double)x.loclake_max;
-  t.loclake_temp_prev = w.temp[1 * N + si];
-  t.loclake_evapo = (double)x.loclake_evapo;
-  t.loclake_rf = (double)x.loclake_rf;
-  t.local_runoff = (double)x.local_runoff;
-  t.local_gw_runoff = (double)x.gw_runoff;
-  t.locwetl_area = w.lw_pct[s];
-  t.locwetl_stor_prev = (double)x.locwetl_prev;
-  t.locwetl_temp_prev = w.temp[2 * N + si];
-  t.locwetl_evapo = (double)x.locwetl_evapo;
-  t.locwetl_rf = (double)x.locwetl_rf;
-  t.locwetl_inflow = (double)x.loclake_out;
-  t.locwetl_outflow = (double)x.locwetl_out;
-  t.glolake_area = w.lake_km2[s];
-  t.glolake_stor_prev = (double)x.glolake_prev + (double)x.glolake_max;
-  t.glolake_temp_prev = w.temp[3 * N + si];
-  t.glolake_evapo = (double)x.glolake_evapo;
-  t.glolake_inflow = tot_in;
-  if (t.locwetl_area > 0.) t.glolake_inflow += t.locwetl_outflow;
-  else if (t.loclake_area > 0.) t.glolake_inflow += t.locwetl_inflow;
-  t.res_area = w.res_km2[s];
-  t.res_inflow = t.glolake_area > 0. ? (double)x.glolake_out : t.glolake_inflow;
-  t.res_stor_prev = (double)x.res_prev;
-  t.res_temp_prev = w.temp[4 * N + si];
-  t.res_evapo = (double)x.res_evapo;
-  t.glowetl_area = w.gw_pct[s];
-  if (t.res_area > 0.) t.glowetl_inflow = (double)x.res_out;
-  else if (t.glolake_area > 0.) t.glowetl_inflow = (double)x.glolake_out;
-  else t.glowetl_inflow = t.glolake_inflow;
-  t.glowetl_stor_prev = (double)x.glowetl_prev;
-  t.glowetl_temp_prev = w.temp[5 * N + si];
-  t.glowetl_evapo = (double)x.glowetl_evapo;
-  t.glowetl_rf = (double)x.glowetl_rf;
-  if (t.glowetl_area > 0.) t.river_inflow = (double)x.glowetl_out;
-  else if (t.res_area > 0.) t.river_inflow = (double)x.res_out;
-  else if (t.glolake_area > 0.) t.river_inflow = (double)x.glolake_out;
-  else t.river_inflow = t.glolake_inflow;
-  t.river_stor = (double)river_stor;
-  t.gw_runoff_into_river = (double)x.gw_into_river;   // zero without fractional routing
-  t.runoff_into_river = (double)x.runoff_into_river;
-  t.river_bottom_width = (double)c.bw[s];
-  t.river_length = (double)c.rlen[s];
-  t.river_length_check = w.len_check[s];
-  t.has_outflow = (fl & F_OUTLET) ? 0. : 1.;
-  double out[12];
-  wt::water_temp_cell(t, out);
-  const double keep = t.air_temp < 0. ? 0. : t.air_temp;
-  for (int k = 0; k < 6; ++k) {
-    w.ice[(size_t)k * N + si] = out[6 + k];
-    w.temp[(size_t)k * N + si] = out[k] == -9999. ? keep : out[k];
-  }
-  return out[0] == -9999. ? keep : out[0];
-}
-
 // X: what each cell computes after its routing, bit 0 the water temperature,
 // bit 1 the water use.
 template <class R, bool FUSED, bool ENS, bool VAW, int X>
@@ -390,6 +311,7 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
     return;
   }
   const int route_threads = VAW ? (int)blockDim.x - 32 * vw.warps : (int)blockDim.x;
+
   const int kd = FUSED ? ring.days_per_step : 1;   // days per step (the per-day routing call: one)
   // thread -> first state index and stride: plain (i mod the grid), or the
   // single-member layout with one idle warp per block (cell_warps warps of cells)
@@ -406,21 +328,11 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
   // flow mode: every cell warp owns exactly its 32 slots (one cell per thread)
   const bool flow = !ENS && !VAW && sync.flow && idle_warp >= 0 && gstride >= (long long)N;
   if (flow && (wpos < 0 || wpos >= sync.nwarps)) return;   // no cells: nothing to wait for or publish
-  // one state per thread for the whole launch: its routing state and land
-  // fractions stay in registers from the first step to the last
-  const bool resident = FUSED && !ENS && gstride >= (long long)N;
-  RState<R> rs_keep{};
-  R laf_keep = R(0), lafp_keep = R(0), fswb_keep = R(0);
-  int started_keep = 0;
-  uint32_t fl_keep = 0;
-  if (resident && gtid < (long long)N) {
-    fl_keep = c.flags[gtid];
-    rs_keep = load_rstate(st, (size_t)gtid, fl_keep);
-    laf_keep = st.laf[gtid];
-    lafp_keep = st.laf_prev[gtid];
-    started_keep = st.laf_started[gtid];
-    if (fl_keep & (F_LOCLAKE | F_LOCWETL | F_GLOWETL)) fswb_keep = st.fswb_next[gtid];
-  }
+  // A cell's routing state and land fractions are read and written each day
+  // (mostly L2 hits: the state of the grid is a few MB).  Holding them in
+  // registers for the whole launch instead took ~32 registers per thread, which
+  // the wavefront launch with vertical-balance warps (96 registers per thread)
+  // paid in spills, and measured ~1 % slower on the global grid.
   for (int t = t_b; t < t_e; ++t) {
     if (flow && t > t_b) {
       if (!wait_deps(sync, wpos, t - t_b - 1)) return;
@@ -450,8 +362,8 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
           const int month = month_of(doy);
           const uint32_t fl = c.flags[s];
           VOut<R> o;
-          const R laf = resident ? laf_keep : st.laf[si];
-          const R laf_prev = resident ? lafp_keep : st.laf_prev[si];
+          const R laf = st.laf[si];
+          const R laf_prev = st.laf_prev[si];
           if (FUSED && !(fl & F_VINLINE)) {
             const size_t ri = (size_t)(d % ring.ring_days) * N + si;
             o.rs = ring.rs[ri];
@@ -470,7 +382,7 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
               Pin *= R(mem.prec_factor[mm]);
               gam *= R(mem.gamma_factor[mm]);
             }
-            const int started = resident ? started_keep : st.laf_started[si];
+            const int started = st.laf_started[si];
             vertical_at<R>(c, st, N, s, si, doy, Pin, gam, f.temp[fo], f.swrad[fo], laf,
                            started == 1 ? laf_prev : laf, o);   // daily.cpp:159-169
           } else {
@@ -487,17 +399,24 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
             if constexpr (WT)   // the energy the inflow carries (calcWaterTemp.cpp:76-83)
               e_up += qu * WT_RC * (__ldcg(t_prev0 + (size_t)kk * N + ui) + WT_CONV_K);
           }
-          RState<R> rs = resident ? rs_keep : load_rstate(st, si, fl);
+          RState<R> rs = load_rstate(st, si, fl);
           RTerms<R> rt;
-          WTerms<R> wtm;
-          const size_t wrow = WU ? (size_t)wu.row_of_fday[fday0 + d] * WU_FIELDS * (size_t)n : 0;
-          const R tv = routing_cell<R, WT, WU>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtm, &wu, wrow, si, N);
-          if (resident) rs_keep = rs;
-          else store_rstate(st, si, rs, fl);
-          q_now[si] = (double)tv;
+          // the water temperature (routing.cpp:4241-4513) body by body inside
+          // routing_cell, the river after it
+          wt::WtDay wtd;
           if constexpr (WT) {
             const size_t fo = (size_t)(fday0 + d) * n + s;
-            const double tr = cell_water_temp<R>(c, wtp, f, s, si, N, fo, fl, o, wtm, rs.river, up, e_up);
+            const float g = wtp.gwt[s];
+            wtd.begin(&wtp, s, si, N, fl, (double)f.temp[fo], (double)f.swrad[fo], (double)wtp.lw[fo], (double)o.owp,
+                      (double)c.area[s], g < 0.f ? 0. : (double)g, up, e_up);
+          }
+          const size_t wrow = WU ? (size_t)wu.row_of_fday[fday0 + d] * WU_FIELDS * (size_t)n : 0;
+          const R tv = routing_cell<R, WT, WU>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtd, &wu, wrow, si, N);
+          store_rstate(st, si, rs, fl);
+          q_now[si] = (double)tv;
+          if constexpr (WT) {
+            const double tr = wtd.river((double)rs.river, (double)c.bw[s], (double)c.rlen[s], (double)c.cfa[s],
+                                        (double)o.owpet);
             t_now0[(size_t)kk * N + si] = tr;
             const int stw = c.station[s];
             if (stw >= 0) wtp.qst_t[(size_t)(oday0 + d) * c.nstation + stw] = tr;
@@ -514,25 +433,13 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
             }
           }
           // land-area fraction for the next day (routing.cpp:5034-5188, 5343-5352)
-          R next = laf;
           if (fl & (F_LOCLAKE | F_LOCWETL | F_GLOWETL)) {
-            R fswb = resident ? fswb_keep : st.fswb_next[si];
-            next = fraction_next<R>(fl, rs, c.ll100[s], c.lw100[s], c.gw100[s], laf, fswb);
-            if (resident) {
-              fswb_keep = fswb;
-              laf_keep = next;
-            } else {
-              st.fswb_next[si] = fswb;
-              st.laf[si] = next;
-            }
+            R fswb = st.fswb_next[si];
+            st.laf[si] = fraction_next<R>(fl, rs, c.ll100[s], c.lw100[s], c.gw100[s], laf, fswb);
+            st.fswb_next[si] = fswb;
           }
-          if (resident) {
-            lafp_keep = laf;
-            started_keep = 1;
-          } else {
-            st.laf_prev[si] = laf;
-            st.laf_started[si] = 1;
-          }
+          st.laf_prev[si] = laf;
+          st.laf_started[si] = 1;
           const int stn = c.station[s];
           if (stn >= 0) qst[((size_t)(oday0 + d) * c.nstation + stn) * M + mm] = (double)tv;
           if (mon.daily_storage && oday0 + d < mon.daily_days) {   // the state file's daily storages
@@ -576,13 +483,6 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
     } else if (t + 1 < t_e) {
       if (!grid_barrier(sync, (unsigned)(t - t_b), route_threads)) return;
     }
-  }
-  if (resident && gtid < (long long)N) {
-    store_rstate(st, (size_t)gtid, rs_keep, fl_keep);
-    st.laf[gtid] = laf_keep;
-    st.laf_prev[gtid] = lafp_keep;
-    st.laf_started[gtid] = started_keep;
-    if (fl_keep & (F_LOCLAKE | F_LOCWETL | F_GLOWETL)) st.fswb_next[gtid] = fswb_keep;
   }
 }
 

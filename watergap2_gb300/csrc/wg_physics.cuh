@@ -18,6 +18,7 @@
 #pragma once
 #include "wg_device.h"
 #include "wg_fastmath.cuh"
+#include "wg_wtemp.cuh"
 
 namespace wg {
 
@@ -455,21 +456,6 @@ struct RTerms {
   R velocity;   // river flow velocity of the day [km/d]
 };
 
-// What the water temperature reads from a cell's routing (routing.cpp:4287-4356):
-// each water body's storage before the day and its capacity where the
-// reference adds it, its evaporation [mm] after any reduction, the area
-// reduction factor the day started with, its outflow, and the local runoff.
-template <class R>
-struct WTerms {
-  R loclake_prev, loclake_max, loclake_evapo, loclake_rf, loclake_out;
-  R locwetl_prev, locwetl_evapo, locwetl_rf, locwetl_out;
-  R glolake_prev, glolake_max, glolake_evapo, glolake_out;
-  R res_prev, res_evapo, res_out;
-  R glowetl_prev, glowetl_evapo, glowetl_rf, glowetl_out;
-  R local_runoff, gw_runoff;          // into the water bodies
-  R runoff_into_river, gw_into_river;   // past them (fractional routing)
-};
-
 // Routing state of one cell (surface water and groundwater storages).
 template <class R>
 struct RState {
@@ -575,13 +561,17 @@ __device__ __forceinline__ void wu_year_end(double *w, size_t N) {
 
 // One cell of routingClass::routing (routing.cpp:1835-4520) given the vertical
 // outputs and the summed upstream inflow (FP64 for every precision); returns the
-// transported volume.  WU: water use (subtract_use = 2, satisfied in the cell):
+// transported volume.  WT (FP64): the water temperature of each water body runs
+// through wtd as soon as the body's routing is done (the reference reads the
+// same terms after the cell's routing, routing.cpp:4287-4356: each body's
+// storage before the day, its evaporation after any reduction, its reduction
+// factor and outflow, and the local runoff).  WU: water use (subtract_use = 2, satisfied in the cell):
 // wu points at the tables (per cell: slot s, stride c.n) and the state (per
 // member: state index si, stride NN), wrow is the offset of the day's table row.
 template <class R, bool WT = false, bool WU = false>
 __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R> &st, int doy, int month, R laf,
                                           R laf_prev, const VOut<R> &v, double inflow_up, RTerms<R> &rt,
-                                          WTerms<R> *wtm = nullptr, const DevWaterUse *wu = nullptr, size_t wrow = 0,
+                                          wt::WtDay *wtd = nullptr, const DevWaterUse *wu = nullptr, size_t wrow = 0,
                                           size_t si = 0, size_t NN = 0) {
   typedef M<R> m;
   const uint32_t fl = c.flags[s];
@@ -643,13 +633,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       inflow = (fc * dlsr) + local_gw;
     }
   }
-  if constexpr (WT) {
-    *wtm = WTerms<R>{};
-    wtm->local_runoff = inflow;
-    wtm->gw_runoff = local_gw;
-    wtm->runoff_into_river = into_river;
-    wtm->gw_into_river = gw_into_river;
-  }
+  if constexpr (WT) wtd->runoff(inflow, local_gw, into_river, gw_into_river);
   const R owp = v.owp, owpet = v.owpet;
   R outflow = R(0);
   const R a6 = c.a6[s];
@@ -673,9 +657,6 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
     }
-    if constexpr (WT) {
-      wtm->loclake_prev = S0; wtm->loclake_max = maxS; wtm->loclake_rf = rf; wtm->loclake_evapo = evapo;
-    }
     rt.p_ow += pin;
     if (S0 > R(0)) {
       outflow = c.sw_k[s] * S0 * m::pow(S0 * c.inv_maxs_ll[s], R(1.5));
@@ -689,7 +670,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = maxS;
     }
     inflow = outflow;
-    if constexpr (WT) wtm->loclake_out = outflow;
+    if constexpr (WT) wtd->loclake((double)S0 + (double)maxS, evapo, rf, outflow);
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * (R(0.5) * c.inv_maxs_ll[s]), c.evx[s]);
     st.loclake = S;
     st.rf_loclake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -711,9 +692,6 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
     }
-    if constexpr (WT) {
-      wtm->locwetl_prev = S0; wtm->locwetl_rf = rf; wtm->locwetl_evapo = evapo;
-    }
     rt.p_ow += pin;
     if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     if (S > R(0)) {
@@ -726,12 +704,13 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = maxS;
     }
     inflow = outflow;
-    if constexpr (WT) wtm->locwetl_out = outflow;
+    if constexpr (WT) wtd->locwetl(S0, evapo, rf, outflow);
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_maxs_lw[s], c.evx[s]);
     st.locwetl = S;
     st.rf_locwetl = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
   }
   inflow = R((double)inflow + inflow_up);   // routing.cpp:2623-2624
+  if constexpr (WT) wtd->locals_done();
   if (fl & F_GLOLAKE) {  // global lake (routing.cpp:2630-2804)
     const R S0 = st.glolake, maxS = c.maxs_gl[s], rf = st.rf_glolake;
     R evapo = (R(1.0) - cfa) * owp + cfa * owpet * rf;
@@ -771,9 +750,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     inflow = outflow;
     if constexpr (WU) dailyActualUse = remGL0 - remUseGL;   // routing.cpp:2788
-    if constexpr (WT) {
-      wtm->glolake_prev = S0; wtm->glolake_max = maxS; wtm->glolake_evapo = evapo; wtm->glolake_out = outflow;
-    }
+    if constexpr (WT) wtd->glolake((double)S0 + (double)maxS, evapo, outflow);
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * (R(0.5) * c.inv_maxs_gl[s]), c.evx[s]);
     st.glolake = S;
     st.rf_glolake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -849,9 +826,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     }
     inflow = outflow;
     if constexpr (WU) dailyActualUse += remRes0 - remUseRes;   // routing.cpp:3068
-    if constexpr (WT) {
-      wtm->res_prev = S0; wtm->res_evapo = evapo; wtm->res_out = outflow;
-    }
+    if constexpr (WT) wtd->res(S0, evapo, outflow);
     R r = R(1.) - m::pow(x::div(m::fabs_(S - maxS), maxS), R(2.81383));   // routing.cpp:3071-3072
     st.res = S;
     st.rf_res = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -885,9 +860,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     }
     if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     inflow = outflow;
-    if constexpr (WT) {
-      wtm->glowetl_prev = S0; wtm->glowetl_rf = rf; wtm->glowetl_evapo = evapo; wtm->glowetl_out = outflow;
-    }
+    if constexpr (WT) wtd->glowetl(S0, evapo, rf, outflow);
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_maxs_gw[s], c.evx[s]);
     st.glowetl = S;
     st.rf_glowetl = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
