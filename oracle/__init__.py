@@ -58,11 +58,31 @@ class _WtIO(ctypes.Structure):
 
 class _WuIO(ctypes.Structure):
     _fields_ = [(f, ctypes.c_void_p) for f in ("nus", "nug", "wdr", "cons", "row_of_day", "frgi", "state",
-                                               "daily_actual")] + [("delayed", ctypes.c_int32)]
+                                               "daily_actual")] + [("delayed", ctypes.c_int32)] + \
+               [("nus_agg", ctypes.c_void_p), ("glwd_unit", ctypes.c_void_p)]
 
 
-WU_NSTATE = 12
+WU_NSTATE = 13
 _DAYS_IN_MONTH = np.array([31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31], np.float64)
+
+
+def aggregate_nus(region, glwd_unit, nus_m3) -> np.ndarray:
+    """dailyNUInit's aggregation over GLWD units (routing.cpp:926-965) of NUs
+    [years, 12, ncell] m3 per month, month by month (wgo_aggregate_nus)."""
+    nus = np.asarray(nus_m3, np.float64)
+    unit = np.ascontiguousarray(glwd_unit, np.int32)
+    lake = np.ascontiguousarray(region.lake_area, np.float64)
+    res = np.ascontiguousarray(region.res_area, np.float64)
+    out = np.empty_like(nus)
+    flat_in, flat_out = nus.reshape(-1, nus.shape[-1]), out.reshape(-1, nus.shape[-1])
+    for k in range(flat_in.shape[0]):
+        src = np.ascontiguousarray(flat_in[k])
+        dst = np.empty_like(src)
+        if lib().wgo_aggregate_nus(region.ncell, _ptr(lake), _ptr(res), _ptr(unit), _ptr(src), _ptr(dst)):
+            raise ValueError("GLWD units: every global lake or reservoir outflow cell needs a unit > 0, "
+                             "one outflow cell per unit")
+        flat_out[k] = dst
+    return out
 
 
 def daily_use(m3_per_month) -> np.ndarray:
@@ -89,6 +109,8 @@ def lib():
                                  ctypes.c_void_p, ctypes.c_int]
         _lib.wgo_last_timing.argtypes = [ctypes.c_void_p]
         _lib.wgo_bottom_width.argtypes = [ctypes.c_double]
+        _lib.wgo_aggregate_nus.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 5
+        _lib.wgo_aggregate_nus.restype = ctypes.c_int
         _lib.wgo_bottom_width.restype = ctypes.c_double
         _lib.wgo_wtemp_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         _lib.wgo_wt_init.argtypes = [ctypes.c_int, ctypes.POINTER(_WtIO)]
@@ -186,32 +208,51 @@ class Oracle:
             raise RuntimeError(f"wgo_run_wt failed: {rc}")
         return q, dt
 
-    def init_water_use(self, frac_return_gw_irrig, delayed=False):
+    def init_water_use(self, frac_return_gw_irrig, delayed=False, glwd_unit=None):
         """Switch on water use: its state starts at zero (routing.cpp:790-848);
         frac_return_gw_irrig [ncell] is G_fractreturngw_irrig; delayed: unmet
-        demand carried to the next day (options.delayedUseSatisfaction)."""
+        demand carried to the next day (options.delayedUseSatisfaction);
+        glwd_unit [ncell] (G_glwdUnit, 0 none): aggrNUsGloLakResOpt = 1, the
+        riparian cells' NUs met by their global lake's or reservoir's outflow cell."""
         self.wu = np.zeros((WU_NSTATE, self.region.ncell))
         self._wu_delayed = int(bool(delayed))
         self._wu_frgi = np.ascontiguousarray(frac_return_gw_irrig, np.float64)
+        self._wu_unit = None if glwd_unit is None else np.ascontiguousarray(glwd_unit, np.int32)
 
-    def run_wt_wu(self, doy0, P, T, S, LW, use, discharge=False, daily_temp=False, nthreads=1):
-        """run() with the water temperature (init_water_temp) and water use
-        (init_water_use); returns (discharge, daily out[0] of every cell)."""
+    def _wu_tables(self, doy0, nd, use):
+        """The daily tables of run_wu (and the GLWD-aggregated NUs where
+        init_water_use had units): ([nus, nug, wdr, cons], rows, nus_agg or None)."""
         from watergap2_gb300.region import use_rows
-        P, T, S, LW = (np.ascontiguousarray(x, np.float32) for x in (P, T, S, LW))
-        nd, n = P.shape[0], self.region.ncell
+        n = self.region.ncell
         tabs = [np.ascontiguousarray(daily_use(u).reshape(-1, n)) for u in use]
         rows = np.ascontiguousarray(use_rows(doy0, nd), np.int32)
         if rows.max() >= tabs[0].shape[0]:
             raise ValueError("water use covers fewer years than the run")
-        q = np.zeros((nd, n)) if discharge else None
-        dt = np.zeros((nd, n)) if daily_temp else None
-        wt = self._wt_io(LW, dt)
+        agg = None
+        if self._wu_unit is not None:
+            agg = np.ascontiguousarray(daily_use(aggregate_nus(self.region, self._wu_unit, use[0])).reshape(-1, n))
+        return tabs, rows, agg
+
+    def _wu_io(self, tabs, rows, agg, da=None):
         io = _WuIO()
         io.nus, io.nug, io.wdr, io.cons = (_ptr(t) for t in tabs)
         io.row_of_day, io.frgi, io.state = _ptr(rows), _ptr(self._wu_frgi), _ptr(self.wu)
-        io.daily_actual = None
+        io.daily_actual = _ptr(da) if da is not None else None
         io.delayed = self._wu_delayed
+        io.nus_agg = _ptr(agg) if agg is not None else None
+        io.glwd_unit = _ptr(self._wu_unit) if agg is not None else None
+        return io
+
+    def run_wt_wu(self, doy0, P, T, S, LW, use, discharge=False, daily_temp=False, nthreads=1):
+        """run() with the water temperature (init_water_temp) and water use
+        (init_water_use); returns (discharge, daily out[0] of every cell)."""
+        P, T, S, LW = (np.ascontiguousarray(x, np.float32) for x in (P, T, S, LW))
+        nd, n = P.shape[0], self.region.ncell
+        tabs, rows, agg = self._wu_tables(doy0, nd, use)
+        q = np.zeros((nd, n)) if discharge else None
+        dt = np.zeros((nd, n)) if daily_temp else None
+        wt = self._wt_io(LW, dt)
+        io = self._wu_io(tabs, rows, agg)
         rc = lib().wgo_run_wt_wu(ctypes.byref(self._static), ctypes.byref(self._cstate), int(doy0), nd,
                                  _ptr(P), _ptr(T), _ptr(S), _ptr(q) if q is not None else None, None,
                                  int(nthreads), ctypes.byref(wt), ctypes.byref(io))
@@ -225,21 +266,13 @@ class Oracle:
         year 0 and every day of year 1 of the day-of-year count starts the next
         year, as the reference's driver reads the yearly files.  Returns
         (discharge, balance, daily actual use [ndays, ncell] km3)."""
-        from watergap2_gb300.region import use_rows
         P, T, S = (np.ascontiguousarray(x, np.float32) for x in (P, T, S))
         nd, n = P.shape[0], self.region.ncell
-        tabs = [np.ascontiguousarray(daily_use(u).reshape(-1, n)) for u in use]
-        rows = np.ascontiguousarray(use_rows(doy0, nd), np.int32)
-        if rows.max() >= tabs[0].shape[0]:
-            raise ValueError("water use covers fewer years than the run")
+        tabs, rows, agg = self._wu_tables(doy0, nd, use)
         q = np.zeros((nd, n)) if discharge else None
         b = np.zeros((nd, 6)) if balance else None
         da = np.zeros((nd, n)) if daily_actual else None
-        io = _WuIO()
-        io.nus, io.nug, io.wdr, io.cons = (_ptr(t) for t in tabs)
-        io.row_of_day, io.frgi, io.state = _ptr(rows), _ptr(self._wu_frgi), _ptr(self.wu)
-        io.daily_actual = _ptr(da) if da is not None else None
-        io.delayed = self._wu_delayed
+        io = self._wu_io(tabs, rows, agg, da)
         rc = lib().wgo_run_wu(ctypes.byref(self._static), ctypes.byref(self._cstate), int(doy0), nd,
                               _ptr(P), _ptr(T), _ptr(S), _ptr(q) if q is not None else None,
                               _ptr(b) if b is not None else None, int(nthreads), ctypes.byref(io))

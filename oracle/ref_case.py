@@ -73,7 +73,7 @@ WT_FIELDS = ["wt_river", "wt_loclake", "wt_locwetl", "wt_glolake", "wt_res", "wt
 
 
 def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000, wtemp=None, wuse=None,
-               delayed=False):
+               delayed=False, glwd_unit=None):
     n = region.ncell
     if n > NG:
         raise ValueError("region larger than the reference grid")
@@ -178,7 +178,8 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
         #  reads (routing.cpp:892-907), cell-major [cell][month]
         nus, nug, wdr, cons, frgi = wuse
         _unf(f"{d}/G_FRACTRETURNGW_IRRIG.UNF0", _full(np.asarray(frgi), np.float32), np.float32)
-        _unf(f"{d}/GLWDunits.UNF4", np.zeros(NG, np.int32), np.int32)
+        units = np.zeros(NG, np.int32) if glwd_unit is None else _full(np.asarray(glwd_unit), np.int32)
+        _unf(f"{d}/GLWDunits.UNF4", units, np.int32)
         for k in range(np.asarray(nus).shape[0]):
             for name, arr in (("G_NETUSE_SW_m3", nus), ("G_NETUSE_GW_m3", nug),
                               ("G_IRRIG_WITHDRAWAL_USE_SW_m3", wdr), ("G_IRRIG_CONS_USE_SW_m3", cons)):
@@ -188,13 +189,14 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
     with open(f"{d}/meta.txt", "w") as f:
         f.write(f"{n} {P.shape[0]} {doy0} {year0} {resopt} {region.river_velo_opt} {len(stations)} {len(snapshots)} "
                 f"{0 if wtemp is None else 1} {int(getattr(region, 'frac_routing', 0))} "
-                f"{0 if wuse is None else (2 if delayed else 1)} {int(getattr(region, 'statcorr_opt', 0))}\n")
+                f"{0 if wuse is None else (2 if delayed else 1) + (0 if glwd_unit is None else 2)} "
+                f"{int(getattr(region, 'statcorr_opt', 0))}\n")
     with open(f"{d}/snapshots.txt", "w") as f:
         f.write(" ".join(str(int(s)) for s in snapshots) + "\n")
 
 
 def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wtemp=None, wuse=None, delayed=False,
-        threads=1):
+        threads=1, glwd_unit=None):
     """Run the reference harness; returns dict(lai_a, lai_b, bottom_width, snapshots=[{field: array}],
     discharge=[ndays, nstation], stations=..., timing=dict(threads, vertical_s, routing_s)): the vertical
     pass on `threads` OpenMP threads, routing serial, as integrate_wghm_ runs them."""
@@ -208,7 +210,8 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
     stations = np.asarray(stations, np.int32)
     snapshots = list(snapshots or [ndays])
     tmp = workdir or tempfile.mkdtemp(prefix="wg_ref_")
-    write_case(region, tmp, P, T, S, doy0, stations, snapshots, wtemp=wtemp, wuse=wuse, delayed=delayed)
+    write_case(region, tmp, P, T, S, doy0, stations, snapshots, wtemp=wtemp, wuse=wuse, delayed=delayed,
+               glwd_unit=glwd_unit)
     out = os.path.join(tmp, "out.bin")
     env = dict(os.environ, WG_REF_THREADS=str(int(threads)))
     subprocess.run([HARNESS, tmp, out], check=True, stdout=subprocess.DEVNULL, env=env)
@@ -229,7 +232,7 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
             for f in WT_FIELDS:
                 snap[f] = raw[o:o + n].copy(); o += n
         if wuse is not None:
-            for f in WU_FIELDS:
+            for f in WU_FIELDS + (["wu_unsat_riparian"] if glwd_unit is not None else []):
                 snap[f] = raw[o:o + n].copy(); o += n
         snaps.append(snap)
     res["snapshots"] = snaps

@@ -65,7 +65,9 @@ int main(int argc, char **argv) {
     if (!m) { fprintf(stderr, "harness: bad meta.txt\n"); return 2; }
     if (!(m >> wtemp)) wtemp = 0;   // optional: water temperature (options.calc_wtemp)
     if (!(m >> frac)) frac = 0;     // optional: options.fractionalRoutingOpt
-    if (!(m >> wuse)) wuse = 0;     // optional: water use (options.subtract_use = 2)
+    if (!(m >> wuse)) wuse = 0;     // optional: water use (options.subtract_use = 2); 1/2 cell-local
+                                    // (2: delayed satisfaction), 3/4 the same with the NUs of global
+                                    // lakes' riparian cells aggregated (aggrNUsGloLakResOpt = 1)
     if (!(m >> statcorr)) statcorr = 0;   // optional: options.statcorrOpt
   }
   std::vector<int> snap_days(nsnap);
@@ -91,7 +93,8 @@ int main(int argc, char **argv) {
   // water use: net abstractions from the yearly G_NETUSE_*_m3 files, satisfied in
   // the cell itself (use_alloc, delayedUseSatisfaction and aggrNUsGloLakResOpt off)
   if (wuse) options.subtract_use = 2;
-  if (wuse == 2) options.delayedUseSatisfaction = 1;   // unmet demand carried to the next day
+  if (wuse == 2 || wuse == 4) options.delayedUseSatisfaction = 1;   // unmet demand carried to the next day
+  if (wuse >= 3) options.aggrNUsGloLakResOpt = 1;   // GLWD units from <case>/GLWDunits.UNF4
   options.glacierOpt = 0; options.calc_wtemp = wtemp; options.start_year = year0; options.end_year = year0;
   options.init_years = 0; options.time_step = 1; options.outLAImax = 0;
 
@@ -295,6 +298,7 @@ int main(int argc, char **argv) {
         DUMP(routing.G_unsatisfiedNAsFromOtherSectorsPrevYear[n]);
         DUMP(routing.G_reducedReturnFlowPrevYear[n]);
         DUMP(routing.G_actualUse[n]);
+        if (wuse >= 3) DUMP(routing.G_unsatUseRiparian[n]);
       }
 #undef DUMP
       snap_i++;

@@ -734,6 +734,82 @@ static void cell_water_temp(const wgo_static *s, const wgo_state *st, int n, int
 
 static const int days_in_month[12] = {31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31};   /* routing.cpp:107 */
 
+/* GLWD units (aggrNUsGloLakResOpt): the cells of every unit > 0 in cell order;
+ * per cell its unit's range [lo, hi) in cells.  Returns 0, or -1 where an
+ * outflow cell (lake_area or res_area > 0) has unit 0 or a unit has two outflow
+ * cells (the reference's loops would then aggregate over every cell without a
+ * unit, or twice). */
+typedef struct {
+  int *cells, *lo, *hi;
+} glwd_lists;
+
+static const int32_t *g_unit_key;
+static int cmp_unit_cell(const void *a, const void *b) {
+  const int i = *(const int *)a, j = *(const int *)b;
+  if (g_unit_key[i] != g_unit_key[j]) return g_unit_key[i] < g_unit_key[j] ? -1 : 1;
+  return i < j ? -1 : (i > j);
+}
+
+static int glwd_build(int N, const double *lake_area, const double *res_area, const int32_t *unit, glwd_lists *g) {
+  const size_t cap = (size_t)(N > 0 ? N : 1);
+  g->cells = (int *)malloc(sizeof(int) * cap);
+  g->lo = (int *)malloc(sizeof(int) * cap);
+  g->hi = (int *)malloc(sizeof(int) * cap);
+  if (!g->cells || !g->lo || !g->hi) return -2;
+  int m = 0;
+  for (int i = 0; i < N; i++) {
+    g->lo[i] = g->hi[i] = 0;
+    if (unit[i] > 0) g->cells[m++] = i;
+  }
+  g_unit_key = unit;
+  qsort(g->cells, (size_t)m, sizeof(int), cmp_unit_cell);
+  for (int k = 0; k < m;) {
+    int e = k, outflows = 0;
+    while (e < m && unit[g->cells[e]] == unit[g->cells[k]]) {
+      const int c = g->cells[e];
+      if (lake_area[c] > 0. || res_area[c] > 0.) outflows++;
+      e++;
+    }
+    if (outflows > 1) return -1;
+    for (int j = k; j < e; j++) {
+      g->lo[g->cells[j]] = k;
+      g->hi[g->cells[j]] = e;
+    }
+    k = e;
+  }
+  for (int i = 0; i < N; i++)
+    if ((lake_area[i] > 0. || res_area[i] > 0.) && unit[i] <= 0) return -1;
+  return 0;
+}
+
+static void glwd_free(glwd_lists *g) {
+  free(g->cells); free(g->lo); free(g->hi);
+  g->cells = g->lo = g->hi = NULL;
+}
+
+/* routing.cpp:926-965, one month */
+int wgo_aggregate_nus(int ncell, const double *lake_area, const double *res_area, const int32_t *glwd_unit,
+                      const double *nus, double *out) {
+  glwd_lists g = {NULL, NULL, NULL};
+  const int rc = glwd_build(ncell, lake_area, res_area, glwd_unit, &g);
+  if (rc == 0) {
+    for (int n = 0; n < ncell; n++) out[n] = nus[n];
+    for (int n = 0; n < ncell; n++) {
+      if (!(lake_area[n] > 0. || res_area[n] > 0.)) continue;   /* an outflow cell */
+      for (int k = g.lo[n]; k < g.hi[n]; k++) {
+        const int i = g.cells[k];
+        if (i == n) continue;
+        if (nus[i] > 0.) {
+          out[n] += out[i];
+          out[i] = 0.;
+        }
+      }
+    }
+  }
+  glwd_free(&g);
+  return rc;
+}
+
 static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, const float *prec,
                     const float *temp, const float *swrad, double *discharge, double *balance, int nthreads,
                     wgo_wt_io *wt, wgo_wu_io *wu) {
@@ -744,6 +820,15 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
   double *bw = (double *)malloc(sizeof(double) * (size_t)N);
   if (!vo || !inflow_up || !bw) return -2;
   for (int n = 0; n < N; n++) bw[n] = wgo_bottom_width(s->bankfull[n]);
+  glwd_lists glwd = {NULL, NULL, NULL};
+  if (wu && wu->nus_agg) {
+    const int rc = wu->glwd_unit ? glwd_build(N, s->lake_area, s->res_area, wu->glwd_unit, &glwd) : -1;
+    if (rc) {
+      glwd_free(&glwd);
+      free(vo); free(inflow_up); free(bw);
+      return -3;
+    }
+  }
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
@@ -792,18 +877,23 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
       const double kg = PAR(s, WGO_P_GWOUTF_C, n);
       double gwPrev = st->gw[n];
       double netGWin = vo[n].gwr * cellArea * (laf / 100.) / 1000000.;
-      double remainingUse = 0., dailyActualUse = 0., nug = 0., prevTotalUnsat = 0.;
+      double remainingUse = 0., dailyActualUse = 0., nug = 0., prevTotalUnsat = 0., totalDesiredUse = 0.;
       if (wu) {   /* routing.cpp:1926-1933 and the other groundwater variants */
         nug = wu->nug[wo + n];
         if (WU(0) != 0.) nug = update_nag(&WU(0), (size_t)N, nug, wu->frgi[n]);
         netGWin -= nug;
         e_ow += nug;
         remainingUse = wu->nus[wo + n];   /* routing.cpp:2225-2290 */
+        if (wu->nus_agg) {                /* routing.cpp:2199-2222 */
+          if (s->res_area[n] > 0. || s->lake_area[n] > 0.) remainingUse = wu->nus_agg[wo + n];
+          else if (wu->glwd_unit[n] > 0) remainingUse = wu->nus_agg[wo + n] + WU(12);
+        }
         if (wu->delayed) {                /* routing.cpp:2236-2244 */
           remainingUse += WU(6);
           prevTotalUnsat = WU(6);
           WU(6) = 0.;
         }
+        totalDesiredUse = remainingUse;
       }
       st->gw[n] = gwPrev * exp(-1. * kg) + (1. / kg) * netGWin * (1. - exp(-1. * kg));
       if (fabs(st->gw[n]) <= MIN_STOR_VOL) st->gw[n] = 0.;
@@ -1071,8 +1161,45 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
         if (st->rf_res[n] < 0.) st->rf_res[n] = 0.;
         if (st->rf_res[n] > 1.) st->rf_res[n] = 1.;
       }
-      if (wu && (s->res_area[n] > 0. || s->lake_area[n] > 0.))   /* routing.cpp:3099-3105 */
-        remainingUse = (s->res_area[n] > 0.) ? remUseRes : remUseGloLake;
+      if (wu && (s->res_area[n] > 0. || s->lake_area[n] > 0.)) {
+        const double remAfter = (s->res_area[n] > 0.) ? remUseRes : remUseGloLake;
+        if (!wu->nus_agg) {   /* routing.cpp:3166-3172 */
+          remainingUse = remAfter;
+        } else {   /* routing.cpp:3083-3165: what the lake or reservoir left of the unit's NUs */
+          const double agg = wu->nus_agg[wo + n], own = wu->nus[wo + n];
+          const double rUseAllocUnsat = totalDesiredUse - agg;
+          for (int k = glwd.lo[n]; k < glwd.hi[n]; k++) {
+            const int i = glwd.cells[k];
+            double *rip_i = &W[(size_t)12 * (size_t)N + (size_t)i];
+            if ((remAfter - rUseAllocUnsat) > 0.) {
+              if (own <= 0.) {
+                if (n == i) {
+                  remainingUse = (agg < 0) ? remAfter : rUseAllocUnsat;
+                  WU(12) = 0.;
+                } else if (wu->nus[wo + i] <= 0.) {
+                  *rip_i = 0.;
+                } else {
+                  *rip_i = (wu->nus[wo + i] / (agg - own)) * (remAfter - rUseAllocUnsat);
+                }
+              } else {
+                if (n == i) {
+                  remainingUse = (own / agg) * (remAfter - rUseAllocUnsat) + rUseAllocUnsat;
+                  WU(12) = 0.;
+                } else if (wu->nus[wo + i] < 0.) {
+                  *rip_i = 0.;
+                } else {
+                  *rip_i = wu->nus[wo + i] / agg * (remAfter - rUseAllocUnsat);
+                }
+              }
+            } else {
+              *rip_i = 0.;
+              WU(12) = 0.;
+              remainingUse = remAfter;
+            }
+          }
+        }
+      }
+
       /* global wetland, routing.cpp:3178-3297 */
       if (s->glo_wetl[n] > 0) {
         double S0 = st->glowetl[n];
@@ -1243,6 +1370,7 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
     }
     doy = (doy % 365) + 1;
   }
+  glwd_free(&glwd);
   free(vo); free(inflow_up); free(bw);
   return 0;
 }

@@ -170,7 +170,7 @@ int wgo_run_wt(const wgo_static *s, wgo_state *st, int doy0, int ndays,
                double *discharge, double *balance, int nthreads, wgo_wt_io *wt);
 
 /* ---- water use (options.subtract_use = 2, use_alloc = 0,
- * delayedUseSatisfaction = 0, aggrNUsGloLakResOpt = 0) ------------------------
+ * delayedUseSatisfaction 0 or 1, aggrNUsGloLakResOpt 0 or 1) -----------------
  * Net abstractions satisfied in the cell itself: NUg from groundwater (adapted
  * by updateNetAbstractionGW, routing.cpp:5503-5572, when the previous day left
  * demand unsatisfied), NUs from the global lake and reservoir (routing.cpp:
@@ -179,14 +179,20 @@ int wgo_run_wt(const wgo_static *s, wgo_state *st, int doy0, int ndays,
  * (routing.cpp:3736, 3906-3919), the year start (annualInit, routing.cpp:
  * 994-1010) and end (annualWaterUsePostProcessing, routing.cpp:5246-5296).
  * Irrigation reservoirs' release reads the cell's own NUs (the downstream
- * allocation coefficients of routing.cpp:3001-3007 are zero). */
-#define WGO_WU_NSTATE 12
+ * allocation coefficients of routing.cpp:3001-3007 are zero).
+ * With nus_agg (aggrNUsGloLakResOpt = 1): the outflow cell of a global lake or
+ * reservoir meets the positive NUs of its GLWD unit's riparian cells
+ * (aggregated by wgo_aggregate_nus, routing.cpp:926-965) and hands what it could
+ * not meet back to each of them, in proportion to their NUs, as demand of
+ * their next routing (routing.cpp:2199-2222, 3083-3165); every outflow cell
+ * has a unit > 0, one outflow cell per unit. */
+#define WGO_WU_NSTATE 13
 /* state rows: 0 G_dailyRemainingUse, 1 G_unsatisfiedNAsFromIrrig,
  * 2 G_unsatisfiedNAsFromOtherSectors, 3 G_reducedReturnFlow,
  * 4 G_withdrawalIrrigFromSwb, 5 G_consumptiveUseIrrigFromSwb,
  * 6 G_totalUnsatisfiedUse, 7 G_UnsatisfiedUsePrevYear,
  * 8 G_unsatisfiedNAsFromIrrigPrevYear, 9 G_unsatisfiedNAsFromOtherSectorsPrevYear,
- * 10 G_reducedReturnFlowPrevYear, 11 G_actualUse */
+ * 10 G_reducedReturnFlowPrevYear, 11 G_actualUse, 12 G_unsatUseRiparian */
 typedef struct {
   const double *nus, *nug, *wdr, *cons;  /* [nrow*ncell] daily values [km3/d] (dailyNUInit) */
   const int32_t *row_of_day;             /* [ndays] table row of each simulated day         */
@@ -196,7 +202,19 @@ typedef struct {
   int32_t delayed;                       /* 1: options.delayedUseSatisfaction (unmet demand
                                             adds to the next day's, routing.cpp:2236-2244,
                                             3900-3905)                                      */
+  const double *nus_agg;                 /* NULL, or [nrow*ncell] daily NUs aggregated over
+                                            the GLWD units (aggrNUsGloLakResOpt = 1)        */
+  const int32_t *glwd_unit;              /* [ncell] G_glwdUnit (0: none) with nus_agg       */
 } wgo_wu_io;
+
+/* dailyNUInit's aggregation of NUs over GLWD units (routing.cpp:926-965), on one
+ * month's values [ncell] in m3 (in place: out starts as a copy of nus): each
+ * outflow cell of a global lake or reservoir (lake_area or res_area > 0) takes,
+ * in cell order, the aggregated value of every other cell of its unit whose own
+ * NUs is positive, which drops to 0.  Returns 0, or -1 where an outflow cell has
+ * unit 0 or a unit has two outflow cells. */
+int wgo_aggregate_nus(int ncell, const double *lake_area, const double *res_area, const int32_t *glwd_unit,
+                      const double *nus, double *out);
 
 /* wgo_run with water use. */
 int wgo_run_wu(const wgo_static *s, wgo_state *st, int doy0, int ndays,

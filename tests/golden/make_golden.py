@@ -179,6 +179,53 @@ def main_wuse(names=None):
         print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+# water use with the NUs of global lakes' and reservoirs' riparian cells met by
+# their outflow cell (aggrNUsGloLakResOpt = 1; GLWD units from synthetic.glwd_units):
+# name -> (region factory, days, first day of year, snapshot days, water-use seed, delayed)
+GLWD_CASES = {
+    "swb_wuse_glwd_420d": (lambda: sy.region_small_swb(seed=21, ny=16, nx=32, block_at=(100, 300)), 420, 330,
+                           [36, 200, 401, 420], 13, False),
+    "swb_wuse_glwd_delayed_200d": (lambda: sy.region_small_swb(seed=34, ny=16, nx=32, block_at=(150, 420)), 200, 120,
+                                   [90, 200], 17, True),
+}
+
+
+def main_wuse_glwd(names=None):
+    if not ref_case.available():
+        if not ref_case.build(REF_SOURCE):
+            raise SystemExit("reference sources not found; cannot regenerate fixtures")
+    for name, (make, nd, doy0, snaps, seed, delayed) in GLWD_CASES.items():
+        if names and name not in names:
+            continue
+        region = make()
+        unit = sy.glwd_units(region)
+        P, T, S = sy.forcing(region, nd, doy0=doy0)
+        nus, nug, wdr, cons, frgi = sy.water_use_inputs(region, 3, seed=seed)
+        # riparian cells abstract more than their lakes and reservoirs can give
+        # (unmet aggregated use goes back to them); a few of them return water
+        rip = np.nonzero((unit > 0) & (region.lake_area <= 0) & (region.res_area <= 0))[0]
+        big = np.abs(nus[:, :, rip]) * 30.0 + np.float32(5.0e8)
+        big[:, :, ::5] *= -0.2
+        nus = nus.copy()
+        nus[:, :, rip] = big.astype(np.float32)
+        outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+        stations = outl[:24]
+        res = ref_case.run(region, P, T, S, doy0=doy0, stations=stations, snapshots=snaps,
+                           wuse=(nus, nug, wdr, cons, frgi), delayed=delayed, glwd_unit=unit)
+        extra = dict(P=P, T=T, S=S, NUS=nus, NUG=nug, WDR=wdr, CONS=cons, FRGI=frgi, GLWD=unit,
+                     doy0=np.array(doy0), delayed=np.array(int(delayed)),
+                     stations=res["stations"], snap_days=np.array(snaps), discharge=res["discharge"])
+        for i, snap in enumerate(res["snapshots"]):
+            snap.pop("snow_band")
+            for k in ref_case.WU_FIELDS + ["wu_unsat_riparian", "gw", "river", "loclake", "locwetl", "glolake",
+                                           "glowetl", "res", "rf_loclake", "rf_glolake", "rf_res", "k_release", "laf",
+                                           "soil"]:
+                extra[f"s{i}_{k}"] = snap[k]
+        path = os.path.join(HERE, f"{name}.npz")
+        save_npz(region, path, **extra)
+        print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 def main_wtemp_wuse(names=None, name="swb_wtemp_wuse_120d"):
     """Water use together with the water temperature (calc_wtemp = 1, subtract_use
     = 2): the water-temperature region and a cold season across a year end."""
@@ -303,4 +350,5 @@ if __name__ == "__main__":
     main(sys.argv[1:])
     main_wtemp(sys.argv[1:])
     main_wuse(sys.argv[1:])
+    main_wuse_glwd(sys.argv[1:])
     main_wtemp_wuse(sys.argv[1:])

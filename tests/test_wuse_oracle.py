@@ -12,7 +12,11 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURE = os.path.join(HERE, "golden", "swb_wuse_420d.npz")
 FIXTURES = [FIXTURE, os.path.join(HERE, "golden", "swb_wuse_frac_200d.npz"),   # with fractional routing
-            os.path.join(HERE, "golden", "swb_wuse_delayed_420d.npz")]         # delayed satisfaction
+            os.path.join(HERE, "golden", "swb_wuse_delayed_420d.npz"),         # delayed satisfaction
+            # the NUs of global lakes' and reservoirs' riparian cells met by their outflow cell
+            # (aggrNUsGloLakResOpt = 1), without and with delayed satisfaction
+            os.path.join(HERE, "golden", "swb_wuse_glwd_420d.npz"),
+            os.path.join(HERE, "golden", "swb_wuse_glwd_delayed_200d.npz")]
 STORES = ["gw", "river", "loclake", "locwetl", "glolake", "glowetl", "res", "rf_loclake", "rf_glolake", "rf_res",
           "k_release", "laf", "soil"]
 
@@ -68,8 +72,9 @@ def test_fixture_exercises_water_use():
 @pytest.mark.parametrize("nthreads", [1, 4])
 def test_oracle_water_use_matches_reference(path, nthreads):
     """Bit for bit (on the x86-64 host that made the fixtures), the oracle run
-    with the reference's 100 snow bands: storages, the 12 water-use state values
-    at every snapshot and the stations' daily discharge."""
+    with the reference's 100 snow bands: storages, the water-use state values
+    (with GLWD units also G_unsatUseRiparian) at every snapshot and the stations'
+    daily discharge."""
     import oracle
     from helpers import REF_BANDS, ref_bound, rel_err
     from oracle.ref_case import WU_FIELDS
@@ -79,7 +84,9 @@ def test_oracle_water_use_matches_reference(path, nthreads):
     worst = {}
     prev = 0
     o = oracle.Oracle(region.with_bands(REF_BANDS))
-    o.init_water_use(ex["FRGI"], delayed=bool(ex["delayed"]) if "delayed" in ex else False)
+    glwd = ex["GLWD"] if "GLWD" in ex else None
+    o.init_water_use(ex["FRGI"], delayed=bool(ex["delayed"]) if "delayed" in ex else False, glwd_unit=glwd)
+    fields = WU_FIELDS + (["wu_unsat_riparian"] if glwd is not None else [])
     qs = []
     for i, sd in enumerate(ex["snap_days"]):
         sd = int(sd)
@@ -93,7 +100,7 @@ def test_oracle_water_use_matches_reference(path, nthreads):
         assert np.abs(b[:, 5]).max() < 1e-9 * max(1.0, np.abs(b[:, 0]).max())
         for f in STORES:
             worst[f] = max(worst.get(f, 0.0), rel_err(o.state[f], ex[f"s{i}_{f}"]))
-        for k, f in enumerate(WU_FIELDS):
+        for k, f in enumerate(fields):
             worst[f] = max(worst.get(f, 0.0), rel_err(o.wu[k], ex[f"s{i}_{f}"]))
         prev = sd
     q = np.concatenate(qs)[:, ex["stations"]]
@@ -133,3 +140,46 @@ def test_oracle_water_use_with_temperature_matches_reference():
     bad = {k: v for k, v in worst.items() if not v <= ref_bound()}
     assert not bad, bad
     assert (ex["s1_ice_river"] > 0).any() and (ex["s1_wu_actual"] != 0).any()
+
+
+def test_glwd_fixtures_exercise_the_aggregation():
+    """The GLWD fixtures reach every branch that matters: aggregated use left
+    unmet and handed back to riparian cells (G_unsatUseRiparian > 0) at the
+    snapshots, riparian cells upstream and downstream of their outflow cell,
+    and riparian cells that return water (negative NUs)."""
+    for name in ("swb_wuse_glwd_420d", "swb_wuse_glwd_delayed_200d"):
+        region, ex = _load(os.path.join(HERE, "golden", f"{name}.npz"))
+        unit = ex["GLWD"]
+        outflow = (region.lake_area > 0) | (region.res_area > 0)
+        assert np.all(unit[outflow] > 0)
+        rip = (unit > 0) & ~outflow
+        down = region.downstream
+        assert any(down[i] >= 0 and outflow[down[i]] for i in np.nonzero(rip)[0])         # upstream riparian
+        assert any(down[c] >= 0 and rip[down[c]] for c in np.nonzero(outflow)[0])        # downstream riparian
+        assert (ex["NUS"][..., rip] < 0).any()
+        assert any((ex[f"s{i}_wu_unsat_riparian"] > 0).any() for i in range(len(ex["snap_days"])))
+
+
+def test_aggregate_nus_refuses_what_the_reference_would_mangle():
+    """An outflow cell without a unit would aggregate every cell without one, and
+    two outflow cells in one unit would aggregate it twice: both are refused."""
+    from oracle import aggregate_nus
+    from watergap2_gb300 import synthetic as sy
+    region, ex = _load(os.path.join(HERE, "golden", "swb_wuse_glwd_420d.npz"))
+    unit = ex["GLWD"].copy()
+    nus = ex["NUS"][:1].astype(np.float64)
+    agg = aggregate_nus(region, unit, nus)
+    outflow = np.nonzero((region.lake_area > 0) | (region.res_area > 0))[0]
+    # the unit's positive NUs end in the outflow cell; the totals stay
+    assert np.allclose(agg.sum(axis=-1), nus.sum(axis=-1), rtol=1e-12)
+    moved = (unit > 0) & (nus[0, 0] > 0) & ~np.isin(np.arange(region.ncell), outflow)
+    assert np.all(agg[0, 0, moved] == 0)
+    bad = unit.copy()
+    bad[outflow[0]] = 0
+    with pytest.raises(ValueError):
+        aggregate_nus(region, bad, nus)
+    bad = unit.copy()
+    bad[outflow[1]] = bad[outflow[0]]
+    with pytest.raises(ValueError):
+        aggregate_nus(region, bad, nus)
+    assert sy.glwd_units(region).tolist() == unit.tolist()

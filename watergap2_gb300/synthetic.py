@@ -595,6 +595,32 @@ def water_temp_inputs(region: Region, ndays: int, T: np.ndarray, seed: int = 9):
     return lw, gw
 
 
+def glwd_units(region: Region) -> np.ndarray:
+    """GLWD units (the reference's GLWDunits.UNF4, G_glwdUnit) [ncell] int32, 0 =
+    none: the outflow cell of each global lake or reservoir (lake_area or
+    res_area > 0), in cell order, gets unit k + 1 together with its riparian
+    cells -- the cells draining into it directly and the cell it drains into --
+    where those are neither outflow cells nor in an earlier unit.  The riparian
+    cells upstream come before the outflow cell in routing order, the one
+    downstream after it."""
+    n = region.ncell
+    unit = np.zeros(n, np.int32)
+    outflow = (region.lake_area > 0) | (region.res_area > 0)
+    down = region.downstream
+    ups = [[] for _ in range(n)]
+    for i in range(n):
+        if down[i] >= 0:
+            ups[down[i]].append(i)
+    k = 0
+    for c in np.nonzero(outflow)[0]:
+        k += 1
+        unit[c] = k
+        for r in ups[c] + ([int(down[c])] if down[c] >= 0 else []):
+            if not outflow[r] and unit[r] == 0:
+                unit[r] = k
+    return unit
+
+
 def water_use_inputs(region: Region, nyears: int, seed: int = 13, scale: float = 1.0):
     """Monthly net abstractions as the reference's yearly water-use files hold
     them (m3 per month, float32, [nyears, 12, ncell]): net abstraction from
