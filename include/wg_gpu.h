@@ -80,6 +80,11 @@ typedef struct wg_region {
   const double *river_length, *river_slope, *roughness, *bankfull;
   const int32_t *downstream;   /* 0-based downstream cell, -1 at outlets and sinks   */
   const int32_t *rout_order;   /* reference routing order (G_routingCell - 1)          */
+  const int32_t *glwd_unit;    /* G_glwdUnit (GLWDunits.UNF4, 0: none), or NULL; used with
+                                  wg_model_options.aggr_nus_glo_lak_res_opt = 1: every
+                                  global lake or reservoir outflow cell has a unit > 0,
+                                  one outflow cell per unit, and the cells of a unit do
+                                  not drain out of it and back in                     */
 } wg_region;
 
 /* Host view of the dynamic state (caller-owned arrays, length ncell unless noted;
@@ -123,7 +128,11 @@ typedef struct wg_model_options {
   int32_t use_alloc;           /* [0] no second-cell allocation of unmet water use
                                   (routing.cpp:2249-2271)                                 */
   int32_t aggr_nus_glo_lak_res_opt;  /* [0] no aggregation of water use over a global lake's
-                                        riparian cells (routing.cpp:926-971)               */
+                                        riparian cells (routing.cpp:926-971); 1 with water
+                                        use and wg_region.glwd_unit: a riparian cell's
+                                        positive NUs is met by its unit's outflow cell,
+                                        which hands what it cannot meet back
+                                        (routing.cpp:2199-2222, 3083-3165)               */
   int32_t ant_nat_opt;         /* [0] anthropogenic run (routing.cpp:435-440)             */
   int32_t res_year_opt;        /* [0] reservoirs by the reference year (routing.cpp:1054-1072,
                                   5670)                                                   */
@@ -171,7 +180,12 @@ typedef struct wg_options {
                               with use_alloc, delayedUseSatisfaction and
                               aggrNUsGloLakResOpt 0); 2: the same with
                               delayedUseSatisfaction = 1 (a day's unmet demand adds
-                              to the next day's): every cell meets its demand
+                              to the next day's); with
+                              model->aggr_nus_glo_lak_res_opt = 1 and
+                              wg_region.glwd_unit, the riparian cells' net
+                              abstractions are met by their global lake's or
+                              reservoir's outflow cell (FP64, one member, no
+                              water temperature).  Otherwise every cell meets its demand
                               from its own global lake, reservoir, river and local
                               lake and from groundwater.  Any precision and member
                               count (with water_temp: FP64, one member); the
@@ -291,10 +305,11 @@ wg_status wg_set_water_use_inputs(wg_ctx *ctx, const double *frac_return_gw_irri
  * 4 G_withdrawalIrrigFromSwb, 5 G_consumptiveUseIrrigFromSwb (per day),
  * 6 G_totalUnsatisfiedUse, 7 G_UnsatisfiedUsePrevYear,
  * 8 G_unsatisfiedNAsFromIrrigPrevYear, 9 G_unsatisfiedNAsFromOtherSectorsPrevYear,
- * 10 G_reducedReturnFlowPrevYear, 11 G_actualUse (this year); start: 0.
+ * 10 G_reducedReturnFlowPrevYear, 11 G_actualUse (this year),
+ * 12 G_unsatUseRiparian; start: 0.
  * The balance of wg_get_balance counts the net abstractions with the
  * evaporation (out[2]). */
-#define WG_WU_NSTATE 12
+#define WG_WU_NSTATE 13
 wg_status wg_get_water_use(wg_ctx *ctx, double *out);
 wg_status wg_set_water_use(wg_ctx *ctx, const double *in);
 

@@ -383,6 +383,9 @@ class RoutingGpu {
         additionalOutIn.additionalOutputInput((int)i, 50) = wu[10 * N + i];
         additionalOutIn.additionalOutputInput((int)i, 51) = wu[8 * N + i];
         additionalOutIn.additionalOutputInput((int)i, 52) = wu[9 * N + i];
+        // G_unsatUseRiparian, which the outflow cell's hand-back writes on the
+        // month's last day (routing.cpp:3121-3154); zero outside GLWD units
+        additionalOutIn.additionalOutputInput((int)i, 42) = wu[12 * N + i];
       }
     }
     if (dwb_.month_end) {

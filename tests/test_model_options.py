@@ -12,7 +12,7 @@ from watergap2_gb300 import synthetic as sy
 REFUSED = {
     "time_series": 0, "cloud": 0, "intercept": 0, "calc_albedo": 1, "use_kc": 1, "pet_opt": 1,
     "clcl_opt": 1, "perma_opt": 1, "glacier_opt": 1, "land_cover_opt": 1, "arid_area_opt": 1,
-    "river_evapo_opt": 1, "statcorr_opt": 2, "use_alloc": 1, "aggr_nus_glo_lak_res_opt": 1,
+    "river_evapo_opt": 1, "statcorr_opt": 2, "use_alloc": 1, "aggr_nus_glo_lak_res_opt": 2,
     "ant_nat_opt": 1, "res_year_opt": 1, "climate_spatial_resolution": 1,
 }
 NAMES = {"pet_opt": "petOpt", "clcl_opt": "clclOpt", "perma_opt": "permaOpt", "glacier_opt": "glacierOpt",
@@ -72,3 +72,33 @@ def test_station_correction_with_water_temperature_refused(region):
     from watergap2_gb300.gpu import Model, WgError
     with pytest.raises(WgError, match="statcorrOpt = 1 together with calc_wtemp"):
         Model(region.with_options(statcorr_opt=1), max_days=2, water_temp=True)
+
+
+def test_glwd_aggregation_conditions(region):
+    """aggrNUsGloLakResOpt = 1 (Model(glwd_unit=...)) needs water use and the
+    units, and is built for FP64, one member, without the water temperature;
+    units where an outflow cell has none, or a unit has two outflow cells, are
+    refused with the reason; a valid set gets past the checks (on a host without
+    a GPU wg_create then stops at the device check)."""
+    from watergap2_gb300.gpu import Model, WgError
+    unit = sy.glwd_units(region)
+    with pytest.raises(WgError, match="needs water use"):
+        Model(region, max_days=2, glwd_unit=unit)
+    with pytest.raises(WgError, match="unsupported.*FP64, one member"):
+        Model(region, max_days=2, water_use=True, glwd_unit=unit, precision="fp32")
+    with pytest.raises(WgError, match="unsupported.*FP64, one member"):
+        Model(region, max_days=2, water_use=True, glwd_unit=unit, water_temp=True)
+    outflow = np.nonzero((region.lake_area > 0) | (region.res_area > 0))[0]
+    bad = unit.copy()
+    bad[outflow[0]] = 0
+    with pytest.raises(WgError, match="has no unit"):
+        Model(region, max_days=2, water_use=True, glwd_unit=bad)
+    bad = unit.copy()
+    bad[outflow[1]] = bad[outflow[0]]
+    with pytest.raises(WgError, match="2 outflow cells"):
+        Model(region, max_days=2, water_use=True, glwd_unit=bad)
+    for wu in (1, 2):
+        try:
+            Model(region, max_days=2, water_use=wu, glwd_unit=unit)
+        except WgError as exc:
+            assert "invalid" not in str(exc) and "unsupported" not in str(exc), exc

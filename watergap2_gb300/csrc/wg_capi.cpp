@@ -144,7 +144,7 @@ void place_warps(const std::vector<int32_t> &seq, const uint32_t *cls, int n, co
 }
 
 wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, const uint32_t *cls,
-                         const WarpLayout *lay, Topology &t) {
+                         const WarpLayout *lay, Topology &t, const int32_t *node_of) {
   for (int i = 0; i < n; ++i)
     if (down[i] < -1 || down[i] >= n || down[i] == i) return WG_ERR_TOPOLOGY;
   std::vector<int32_t> order;
@@ -165,10 +165,47 @@ wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, 
   // distance to the outlet, downstream first
   std::vector<int32_t> depth(n, 0);
   int32_t dmax = 0;
-  for (int k = n - 1; k >= 0; --k) {
-    const int c = order[k];
-    depth[c] = down[c] < 0 ? 0 : depth[down[c]] + 1;
-    dmax = std::max(dmax, depth[c]);
+  if (!node_of) {
+    for (int k = n - 1; k >= 0; --k) {
+      const int c = order[k];
+      depth[c] = down[c] < 0 ? 0 : depth[down[c]] + 1;
+      dmax = std::max(dmax, depth[c]);
+    }
+  } else {
+    // cells that one thread routes together (node_of: the same node) share one
+    // offset: the longest path to an outlet over the graph of nodes, which must
+    // stay acyclic (a node's cells may not drain out of it and back in)
+    std::vector<std::vector<int32_t>> succ(n);
+    std::vector<int32_t> indeg(n, 0);
+    for (int c = 0; c < n; ++c) {
+      if (node_of[c] < 0 || node_of[c] >= n || node_of[node_of[c]] != node_of[c]) return WG_ERR_TOPOLOGY;
+      if (down[c] < 0) continue;
+      const int a = node_of[c], b = node_of[down[c]];
+      if (a != b) {
+        succ[a].push_back(b);
+        indeg[b]++;
+      }
+    }
+    std::vector<int32_t> topo_nodes, frontier;
+    for (int c = 0; c < n; ++c)
+      if (node_of[c] == c && indeg[c] == 0) frontier.push_back(c);
+    while (!frontier.empty()) {
+      const int a = frontier.back();
+      frontier.pop_back();
+      topo_nodes.push_back(a);
+      for (int b : succ[a])
+        if (--indeg[b] == 0) frontier.push_back(b);
+    }
+    int nodes = 0;
+    for (int c = 0; c < n; ++c) nodes += node_of[c] == c;
+    if ((int)topo_nodes.size() != nodes) return WG_ERR_TOPOLOGY;
+    std::vector<int32_t> ndepth(n, 0);
+    for (int k = (int)topo_nodes.size() - 1; k >= 0; --k) {
+      const int a = topo_nodes[k];
+      for (int b : succ[a]) ndepth[a] = std::max(ndepth[a], ndepth[b] + 1);
+      dmax = std::max(dmax, ndepth[a]);
+    }
+    for (int c = 0; c < n; ++c) depth[c] = ndepth[node_of[c]];
   }
   t.nlevel = dmax + 1;
   t.offset.resize(n);
@@ -706,8 +743,90 @@ static wg_status setup_water_use(wg_ctx *ctx, const wg_region *r) {
   if (e == cudaSuccess) e = cudaMemset((void *)w.frgi, 0, (size_t)n * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(w.st, 0, (size_t)wg::WU_NSTATE * N * sizeof(double));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "water use");
+  if (ctx->glwd.on) {   // the units in slot space: per unit its slots in routing order and in cell order
+    const auto &g = ctx->glwd;
+    const size_t nu = g.ptr.size() - 1;
+    std::vector<int32_t> unit_of(n), mem(g.cells.size()), idx(g.cells.size());
+    for (int s = 0; s < n; ++s) unit_of[s] = g.unit_of[ctx->topo.cell_of_slot[s]];
+    for (size_t u = 0; u < nu; ++u) {
+      std::vector<int32_t> by_rout(g.cells.begin() + g.ptr[u], g.cells.begin() + g.ptr[u + 1]);
+      std::sort(by_rout.begin(), by_rout.end(),
+                [&](int a, int b) { return ctx->topo.rout_pos[a] < ctx->topo.rout_pos[b]; });
+      for (int k = g.ptr[u]; k < g.ptr[u + 1]; ++k) {
+        mem[k] = ctx->topo.slot_of_cell[by_rout[k - g.ptr[u]]];
+        idx[k] = ctx->topo.slot_of_cell[g.cells[k]];
+      }
+    }
+    wg_status us = WG_OK;
+    w.unit_of = upload_raw<int32_t>(ctx, unit_of, us);
+    w.unit_ptr = upload_raw<int32_t>(ctx, g.ptr, us);
+    w.unit_mem = upload_raw<int32_t>(ctx, mem, us);
+    w.unit_idx = upload_raw<int32_t>(ctx, idx, us);
+    if (us != WG_OK) return us;
+    w.glwd = 1;
+  }
   w.enabled = 1;
   return WG_OK;
+}
+
+// GLWD units of a region (aggrNUsGloLakResOpt = 1): every outflow cell of a
+// global lake or reservoir needs a unit > 0 and a unit at most one outflow cell
+// (the reference's loops would otherwise aggregate over every cell without a
+// unit, or twice: routing.cpp:935-962, 3094-3095).
+static wg_status glwd_setup(const wg_region *r, wg_ctx::Glwd &g) {
+  const int n = r->ncell;
+  g.unit.assign(r->glwd_unit, r->glwd_unit + n);
+  g.outflow.assign(n, 0);
+  g.unit_of.assign(n, -1);
+  std::map<int32_t, std::vector<int32_t>> cells;   // unit -> cells in cell order
+  for (int i = 0; i < n; ++i) {
+    g.outflow[i] = (r->lake_area[i] > 0. || r->res_area[i] > 0.) ? 1 : 0;
+    if (g.outflow[i] && g.unit[i] <= 0) {
+      t_create_err = "GLWD units: outflow cell " + std::to_string(i) + " of a global lake or reservoir has no unit";
+      return WG_ERR_INVALID;
+    }
+    if (g.unit[i] > 0) cells[g.unit[i]].push_back(i);
+  }
+  g.ptr.assign(1, 0);
+  g.cells.clear();
+  for (const auto &kv : cells) {
+    int outflows = 0;
+    for (int c : kv.second) outflows += g.outflow[c];
+    if (outflows > 1) {
+      t_create_err = "GLWD units: unit " + std::to_string(kv.first) + " has " + std::to_string(outflows) +
+                     " outflow cells of global lakes or reservoirs";
+      return WG_ERR_INVALID;
+    }
+    const int u = outflows ? (int)g.ptr.size() - 1 : -2;
+    for (int c : kv.second) g.unit_of[c] = u;
+    if (outflows) {
+      g.cells.insert(g.cells.end(), kv.second.begin(), kv.second.end());
+      g.ptr.push_back((int32_t)g.cells.size());
+    }
+  }
+  g.on = true;
+  return WG_OK;
+}
+
+// dailyNUInit's aggregation of one month's NUs [m3, cell order] over the GLWD
+// units (routing.cpp:926-965): each outflow cell, in cell order, takes the
+// aggregated value of every other cell of its unit whose own NUs is positive,
+// which drops to zero.
+static void glwd_aggregate(const wg_ctx::Glwd &g, const double *nus, double *out, int n) {
+  std::copy(nus, nus + n, out);
+  for (size_t u = 0; u + 1 < g.ptr.size(); ++u) {
+    int o = -1;
+    for (int k = g.ptr[u]; k < g.ptr[u + 1]; ++k)
+      if (g.outflow[g.cells[k]]) o = g.cells[k];
+    for (int k = g.ptr[u]; k < g.ptr[u + 1]; ++k) {
+      const int i = g.cells[k];
+      if (i == o) continue;
+      if (nus[i] > 0.) {
+        out[o] += out[i];
+        out[i] = 0.;
+      }
+    }
+  }
 }
 
 // Water temperature buffers: state at the reference's start values (15 degC, no
@@ -761,7 +880,7 @@ wg_status check_model_options(const wg_region *r, const wg_options *opt) {
                {"clclOpt", m.clcl_opt, 0}, {"permaOpt", m.perma_opt, 0}, {"glacierOpt", m.glacier_opt, 0},
                {"landCoverOpt", m.land_cover_opt, 0}, {"aridareaOpt", m.arid_area_opt, 0},
                {"riverEvapoOpt", m.river_evapo_opt, 0}, {"use_alloc", m.use_alloc, 0},
-               {"aggrNUsGloLakResOpt", m.aggr_nus_glo_lak_res_opt, 0}, {"antNatOpt", m.ant_nat_opt, 0},
+               {"antNatOpt", m.ant_nat_opt, 0},
                {"resYearOpt", m.res_year_opt, 0}, {"climate_spatial_resolution", m.climate_spatial_resolution, 0}};
   for (const auto &f : fixed)
     if (f.value != f.want) {
@@ -769,6 +888,21 @@ wg_status check_model_options(const wg_region *r, const wg_options *opt) {
                      " is not built (built: " + std::to_string(f.want) + ")";
       return WG_ERR_UNSUPPORTED;
     }
+  if (m.aggr_nus_glo_lak_res_opt != 0 && m.aggr_nus_glo_lak_res_opt != 1) {
+    t_create_err = "options.aggrNUsGloLakResOpt = " + std::to_string(m.aggr_nus_glo_lak_res_opt) +
+                   " is not built (built: 0, 1)";
+    return WG_ERR_UNSUPPORTED;
+  }
+  if (m.aggr_nus_glo_lak_res_opt == 1) {
+    if (!opt->water_use || !r->glwd_unit) {
+      t_create_err = "options.aggrNUsGloLakResOpt = 1 needs water use and the GLWD units (wg_region.glwd_unit)";
+      return WG_ERR_INVALID;
+    }
+    if (opt->precision != 0 || opt->members != 1 || opt->water_temp) {
+      t_create_err = "options.aggrNUsGloLakResOpt = 1 is built for FP64, one member, without the water temperature";
+      return WG_ERR_UNSUPPORTED;
+    }
+  }
   if (m.statcorr_opt != 0 && m.statcorr_opt != 1) {
     t_create_err = "options.statcorrOpt = " + std::to_string(m.statcorr_opt) + " is not built (built: 0, 1)";
     return WG_ERR_UNSUPPORTED;
@@ -813,6 +947,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (opt->water_temp && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
   if (opt->water_use < 0 || opt->water_use > 2) return WG_ERR_INVALID;
   if (opt->water_use && opt->water_temp && (opt->precision != 0 || opt->members != 1)) return WG_ERR_UNSUPPORTED;
+  const bool aggr = opt->model && opt->model->aggr_nus_glo_lak_res_opt == 1;
   const int n = r->ncell, B = r->nband;
   for (int i = 0; i < n; ++i) {
     if (r->lct[i] < 1 || r->lct[i] > WG_NLCT) return WG_ERR_INVALID;
@@ -822,9 +957,15 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     }
     if (!(r->river_length[i] > 0.)) return WG_ERR_INVALID;
   }
+  wg_ctx::Glwd glwd;   // GLWD units, checked before any device is touched
+  if (aggr) {
+    wg_status gs = glwd_setup(r, glwd);
+    if (gs != WG_OK) return gs;
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= opt->device) return WG_ERR_DEVICE;
   std::unique_ptr<wg_ctx> ctx(new wg_ctx());
+  ctx->glwd = std::move(glwd);
   ctx->device = opt->device;
   ctx->n = n;
   ctx->nband = B;
@@ -849,8 +990,30 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   for (int i = 0; i < n; ++i) cls[i] = work_class(r, i);
   if (!opt->block_threads && ctx->members == 1) ctx->layout = default_layout(ctx.get());
   ctx->va_warps_default = ctx->layout.va_warps;
-  wg_status st = build_topology(n, r->downstream, r->rout_order, cls.data(), &ctx->layout, ctx->topo);
-  if (st != WG_OK) return st;
+  std::vector<int32_t> node_of;   // GLWD units: a unit's cells are one node of the wavefront
+  if (aggr) {
+    std::vector<int32_t> order;
+    if (r->rout_order) order.assign(r->rout_order, r->rout_order + n);
+    else if (reference_rout_order(n, r->downstream, order) != WG_OK) return WG_ERR_TOPOLOGY;
+    node_of.resize(n);
+    for (int i = 0; i < n; ++i) node_of[i] = i;
+    std::vector<int32_t> first(ctx->glwd.ptr.size(), -1);   // per unit its first cell in routing order
+    for (int k = 0; k < n; ++k) {
+      const int c = order[k];
+      if (c < 0 || c >= n) return WG_ERR_TOPOLOGY;
+      const int u = ctx->glwd.unit_of[c];
+      if (u >= 0 && first[u] < 0) first[u] = c;
+    }
+    for (int i = 0; i < n; ++i)
+      if (ctx->glwd.unit_of[i] >= 0) node_of[i] = first[ctx->glwd.unit_of[i]];
+  }
+  wg_status st = build_topology(n, r->downstream, r->rout_order, cls.data(), &ctx->layout, ctx->topo,
+                                aggr ? node_of.data() : nullptr);
+  if (st != WG_OK) {
+    if (aggr && st == WG_ERR_TOPOLOGY)
+      t_create_err = "GLWD units: the cells of a unit drain out of it and back in (no wavefront order)";
+    return st;
+  }
   {
     double e2[64], lf[129], inv[129];
     fill_fastmath_tables(e2, lf, inv);
@@ -1367,12 +1530,18 @@ wg_status wg_upload_water_use(wg_ctx *ctx, int32_t fday0, int32_t ndays, int32_t
   const size_t block = (size_t)12 * F * N;
   std::vector<double> buf(block, 0.);
   const double *src[4] = {nus_m3, nug_m3, irrig_withdrawal_sw_m3, irrig_consumptive_sw_m3};
+  std::vector<double> agg(ctx->glwd.on ? n : 0);
   for (int m = 0; m < 12; ++m) {
     const double per_day = 1000000000. * (double)days_in_month[m];   // dailyNUInit, routing.cpp:966-975
     for (int k = 0; k < 4; ++k) {
       double *row = buf.data() + ((size_t)m * F + k) * N;
       const double *in = src[k] + (size_t)m * n;
       for (int s = 0; s < n; ++s) row[s] = in[ctx->topo.cell_of_slot[s]] / per_day;
+    }
+    if (ctx->glwd.on) {   // NUs aggregated over the GLWD units, then per day (routing.cpp:926-975)
+      glwd_aggregate(ctx->glwd, nus_m3 + (size_t)m * n, agg.data(), n);
+      double *row = buf.data() + ((size_t)m * F + 5) * N;
+      for (int s = 0; s < n; ++s) row[s] = agg[ctx->topo.cell_of_slot[s]] / per_day;
     }
     double *prov = buf.data() + ((size_t)m * F + 4) * N;
     std::copy(ctx->wu_prov0.begin(), ctx->wu_prov0.end(), prov);

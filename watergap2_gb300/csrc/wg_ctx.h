@@ -90,6 +90,15 @@ struct wg_ctx {
   std::vector<double> wu_prov0;            // [n] slot order: provisional release without use
   struct WuRes { int slot, cell, type; double mean_outflow, mean_demand; };
   std::vector<WuRes> wu_res;               // the reservoirs, for the monthly provisional release
+  // GLWD units (aggrNUsGloLakResOpt = 1): per cell its unit (G_glwdUnit) and
+  // whether it is a global lake's or reservoir's outflow cell; per cell the index
+  // of its unit among the units with an outflow cell (-1 no unit, -2 a unit
+  // without one), and the cells of each such unit in cell order
+  struct Glwd {
+    bool on = false;
+    std::vector<int32_t> unit, unit_of, ptr, cells;
+    std::vector<uint8_t> outflow;
+  } glwd;
   int last_vertical_fday = 0;              // forcing slot of the last wg_step_vertical
   struct Deferred {                        // wg_set_deferred: the per-day calls queued
     bool on = false;

@@ -175,13 +175,15 @@ struct DevWaterTemp {
 // Table row r of forcing day f is row_of_fday[f]; row r holds, for every cell slot,
 // the day's net abstraction from surface water (NUs) and from groundwater (NUg),
 // irrigation withdrawal and consumptive use from surface water [km3/d], and the
-// provisional release of a reservoir [m3/s] (routing.cpp:2974-2994); rows 0-11
+// provisional release of a reservoir [m3/s] (routing.cpp:2974-2994), and NUs
+// aggregated over GLWD units (routing.cpp:926-965; NUs where none); rows 0-11
 // are zero use.  State rows (k * N): 0 remaining use, 1/2 unsatisfied NAs from
 // irrigation / other sectors, 3 reduced return flow, 4/5 irrigation withdrawal /
 // consumptive use of the last day, 6 total unsatisfied use, 7-10 the previous
-// year's 6, 1, 2, 3, 11 actual use of the year.
-constexpr int WU_FIELDS = 5;
-constexpr int WU_NSTATE = 12;
+// year's 6, 1, 2, 3, 11 actual use of the year, 12 a riparian cell's share of
+// its outflow cell's unmet use (G_unsatUseRiparian).
+constexpr int WU_FIELDS = 6;
+constexpr int WU_NSTATE = 13;
 struct DevWaterUse {
   const double *tab;          // [rows][WU_FIELDS][n] (per cell, shared by the members)
   const int32_t *row_of_fday; // [max_days]
@@ -189,6 +191,12 @@ struct DevWaterUse {
   double *st;                 // [WU_NSTATE][N]
   int32_t enabled;
   int32_t delayed;            // unmet demand adds to the next day's (delayedUseSatisfaction)
+  // GLWD units (aggrNUsGloLakResOpt = 1, one member): per slot its unit index
+  // (-1 no unit, -2 a unit without a global lake or reservoir outflow cell);
+  // the slots of unit u in routing order unit_mem[unit_ptr[u] .. unit_ptr[u+1])
+  // and in cell order unit_idx[...]
+  const int32_t *unit_of, *unit_ptr, *unit_mem, *unit_idx;
+  int32_t glwd;
 };
 
 // Vertical balance of the cells without water bodies run by extra warps of the

@@ -283,7 +283,8 @@ __global__ void __launch_bounds__(VaBounds<R, ENS>::threads, VaBounds<R, ENS>::m
 }
 
 // X: what each cell computes after its routing, bit 0 the water temperature,
-// bit 1 the water use.
+// bit 1 the water use, bit 2 (with bit 1) the water use of GLWD units' riparian
+// cells met by their outflow cell.
 template <class R, bool FUSED, bool ENS, bool VAW, int X>
 __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R, ENS, VAW>::min_blocks) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
@@ -292,6 +293,7 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
                                                   DevMonthly mon, DevVaWork vw, DevWaterTemp wtp, DevWaterUse wu) {
   constexpr bool WT = (X & 1) != 0;
   constexpr bool WU = (X & 2) != 0;
+  constexpr bool GL = (X & 4) != 0;   // water use with GLWD units (aggrNUsGloLakResOpt = 1)
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const size_t N = (size_t)n * M;
@@ -326,7 +328,7 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
     if (warp != idle_warp) wpos = blockIdx.x * cell_warps + weff;
   }
   // flow mode: every cell warp owns exactly its 32 slots (one cell per thread)
-  const bool flow = !ENS && !VAW && sync.flow && idle_warp >= 0 && gstride >= (long long)N;
+  const bool flow = !ENS && !VAW && !GL && sync.flow && idle_warp >= 0 && gstride >= (long long)N;
   if (flow && (wpos < 0 || wpos >= sync.nwarps)) return;   // no cells: nothing to wait for or publish
   // A cell's routing state and land fractions are read and written each day
   // (mostly L2 hits: the state of the grid is a few MB).  Holding them in
@@ -346,15 +348,33 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
       // state index i always belongs to thread i mod gstride, so a cell's state is read
       // and written by one thread; only upstream outflows cross threads (read via L2)
       for (long long i = gtid; i < (long long)N; i += gstride) {
-        const int s = ENS ? (int)(i / M) : (int)i;
-        const int mm = ENS ? (int)(i - (long long)s * M) : 0;
-        const size_t si = (size_t)i;
-        const int dbase = kd * (t - c.offset[s]);
+        const int s0 = ENS ? (int)(i / M) : (int)i;
+        const int mm = ENS ? (int)(i - (long long)s0 * M) : 0;
+        const int dbase = kd * (t - c.offset[s0]);
         if (dbase < 0 || dbase >= ndays) continue;   // this cell's wavefront has not reached it yet / is done
-        if (c.active && !c.active[s]) continue;
+        // a GLWD unit whose riparian cells' use its outflow cell meets (GL) is routed
+        // by the thread of its first cell in routing order, cell by cell in that
+        // order each day (its cells share one wavefront offset): a riparian cell
+        // after the outflow cell sees the unmet share of the same day, one before
+        // it that of the day before, as in the reference's sweep
+        int unit = -1, m_b = 0, m_e = 1;
+        if constexpr (GL) {
+          const int u = wu.unit_of[s0];
+          if (u >= 0) {
+            if (wu.unit_mem[wu.unit_ptr[u]] != s0) continue;   // routed by the unit's first cell
+            unit = u;
+            m_b = wu.unit_ptr[u];
+            m_e = wu.unit_ptr[u + 1];
+          }
+        }
+        if (unit < 0 && c.active && !c.active[s0]) continue;
         // the step's kd days of this cell, in order; the upstream cells routed the
         // same days one step earlier (their offset is one less)
         for (int kk = 0; kk < kd && dbase + kk < ndays; ++kk) {
+         for (int m = m_b; m < m_e; ++m) {
+          const int s = unit >= 0 ? wu.unit_mem[m] : s0;
+          const size_t si = unit >= 0 ? (size_t)s : (size_t)i;
+          if (unit >= 0 && c.active && !c.active[s]) continue;
           const int d = dbase + kk;
           double *q_now = q_now0 + (size_t)kk * N;
           const double *q_prev = q_prev0 + (size_t)kk * N;
@@ -394,7 +414,8 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
           const int u0 = c.up_ptr[s], u1 = c.up_ptr[s + 1];
           for (int k = u0; k < u1; ++k) {
             const size_t ui = (size_t)c.up_idx[k] * M + mm;
-            const double qu = __ldcg(q_prev + ui);
+            // an upstream cell of the same unit was routed this step, earlier in this loop
+            const double qu = (GL && unit >= 0 && wu.unit_of[c.up_idx[k]] == unit) ? q_now[ui] : __ldcg(q_prev + ui);
             up += qu;
             if constexpr (WT)   // the energy the inflow carries (calcWaterTemp.cpp:76-83)
               e_up += qu * WT_RC * (__ldcg(t_prev0 + (size_t)kk * N + ui) + WT_CONV_K);
@@ -411,7 +432,8 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
                       (double)c.area[s], g < 0.f ? 0. : (double)g, up, e_up);
           }
           const size_t wrow = WU ? (size_t)wu.row_of_fday[fday0 + d] * WU_FIELDS * (size_t)n : 0;
-          const R tv = routing_cell<R, WT, WU>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtd, &wu, wrow, si, N);
+          const R tv = routing_cell<R, WT, WU, GL>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtd, &wu, wrow, si,
+                                                   N);
           store_rstate(st, si, rs, fl);
           q_now[si] = (double)tv;
           if constexpr (WT) {
@@ -471,6 +493,7 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
               mon.velocity[k] += (double)rt.velocity / 86.4;   // km/d -> m/s
             }
           }
+         }   // cells of the unit
         }   // days of the step
       }
     }
@@ -661,10 +684,12 @@ static const void *pipeline_fn_x(bool fused, bool vaw) {
 }
 
 template <class R>
-static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false) {
+static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false, bool gl = false) {
+  if (gl && (ens || wt || !wu || !std::is_same<R, double>::value)) return nullptr;   // GLWD units: FP64, one member
   if (ens) return wt ? nullptr
                      : (wu ? (const void *)k_pipeline<R, true, true, false, 2> : (const void *)k_pipeline<R, true, true, false, 0>);
   if constexpr (std::is_same<R, double>::value) {   // FP64 single member only
+    if (gl) return pipeline_fn_x<R, 6>(fused, vaw);
     if (wt && wu) return pipeline_fn_x<R, 3>(fused, vaw);
     if (wt) return pipeline_fn_x<R, 1>(fused, vaw);
     if (wu) return pipeline_fn_x<R, 2>(fused, vaw);
@@ -712,7 +737,7 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
                   (void *)&oday0, (void *)&ndays, (void *)&t_b, (void *)&t_e, (void *)&cell_warps,
                   (void *)&idle_warp, (void *)&mon, (void *)&vwk, (void *)&wtp, (void *)&wu};
   const bool ens = mem.members > 1;
-  const void *fn = pipeline_fn<R>(fused, ens, vaw, wtp.enabled != 0, wu.enabled != 0);
+  const void *fn = pipeline_fn<R>(fused, ens, vaw, wtp.enabled != 0, wu.enabled != 0, wu.enabled && wu.glwd);
   if (!fn) return cudaErrorInvalidConfiguration;
   if (vaw) threads += 32 * vw.warps;
   // cooperative (all blocks resident, or the launch fails) through the launch

@@ -568,7 +568,7 @@ __device__ __forceinline__ void wu_year_end(double *w, size_t N) {
 // factor and outflow, and the local runoff).  WU: water use (subtract_use = 2, satisfied in the cell):
 // wu points at the tables (per cell: slot s, stride c.n) and the state (per
 // member: state index si, stride NN), wrow is the offset of the day's table row.
-template <class R, bool WT = false, bool WU = false>
+template <class R, bool WT = false, bool WU = false, bool GL = false>
 __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R> &st, int doy, int month, R laf,
                                           R laf_prev, const VOut<R> &v, double inflow_up, RTerms<R> &rt,
                                           wt::WtDay *wtd = nullptr, const DevWaterUse *wu = nullptr, size_t wrow = 0,
@@ -600,12 +600,18 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     netGWin -= R(nug);
     rt.e_ow += R(nug);
     remainingUse = R(wu->tab[wrow + s]);   // routing.cpp:2225-2290
+    if constexpr (GL) {   // routing.cpp:2199-2222: NUs aggregated over the GLWD unit
+      const double agg = wu->tab[wrow + 5 * tn + s];
+      if (fl & (F_GLOLAKE | F_RES)) remainingUse = R(agg);                  // the unit's outflow cell
+      else if (wu->unit_of[s] != -1) remainingUse = R(agg + W[12 * NN]);   // a riparian cell
+    }
     if (wu->delayed) {   // routing.cpp:2236-2244
       prevTotalUnsat = W[6 * NN];
       remainingUse = R((double)remainingUse + prevTotalUnsat);
       W[6 * NN] = 0.;
     }
   }
+  [[maybe_unused]] const R totalDesiredUse = remainingUse;
   R gw = gw0 * c.gw_e[s] + c.gw_ik[s] * netGWin * c.gw_ome[s];
   if (cmp::abs_le_c(gw, R(WG_MIN_STOR_VOL))) gw = R(0);
   R gw_runoff = gw0 - gw + netGWin;
@@ -831,8 +837,48 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     st.res = S;
     st.rf_res = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
   }
-  if constexpr (WU) {   // routing.cpp:3099-3105
-    if (fl & (F_RES | F_GLOLAKE)) remainingUse = (fl & F_RES) ? remUseRes : remUseGL;
+  if constexpr (WU) {   // routing.cpp:3083-3172
+    if (fl & (F_RES | F_GLOLAKE)) {
+      const R remAfter = (fl & F_RES) ? remUseRes : remUseGL;
+      if constexpr (GL) {
+        // what the lake or reservoir left of its unit's NUs goes back to the unit's
+        // riparian cells in proportion to their NUs, as demand of their next routing;
+        // the unit's cells in cell order, as the reference's loop over all cells
+        const size_t tn = (size_t)c.n;
+        const int u = wu->unit_of[s];
+        const double agg = wu->tab[wrow + 5 * tn + s], own = wu->tab[wrow + s];
+        const double rUseAllocUnsat = (double)totalDesiredUse - agg;
+        const double left = (double)remAfter - rUseAllocUnsat;
+        for (int k = wu->unit_ptr[u]; k < wu->unit_ptr[u + 1]; ++k) {
+          const int i = wu->unit_idx[k];
+          double *rip_i = wu->st + 12 * NN + (size_t)i;   // one member: state index = slot
+          const double nus_i = wu->tab[wrow + i];
+          if (left > 0.) {
+            if (own <= 0.) {
+              if (i == s) {
+                remainingUse = (agg < 0) ? remAfter : R(rUseAllocUnsat);
+                W[12 * NN] = 0.;
+              } else {
+                *rip_i = (nus_i <= 0.) ? 0. : (nus_i / (agg - own)) * left;
+              }
+            } else {
+              if (i == s) {
+                remainingUse = R((own / agg) * left + rUseAllocUnsat);
+                W[12 * NN] = 0.;
+              } else {
+                *rip_i = (nus_i < 0.) ? 0. : nus_i / agg * left;
+              }
+            }
+          } else {
+            *rip_i = 0.;
+            W[12 * NN] = 0.;
+            remainingUse = remAfter;
+          }
+        }
+      } else {
+        remainingUse = remAfter;
+      }
+    }
   }
   if (fl & F_GLOWETL) {  // global wetland (routing.cpp:3178-3297)
     const R S0 = st.glowetl, maxS = c.maxs_gw[s], rf = st.rf_glowetl;

@@ -20,6 +20,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libwg_gpu.so")
 
 WG_OK = 0
+WU_NSTATE = 13   # WG_WU_NSTATE: rows of the water-use state
 STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported option", 3: "CUDA error", 4: "out of device memory",
           5: "invalid drainage topology", 6: "device wait exceeded its limit", 7: "no usable device"}
 
@@ -47,7 +48,7 @@ class WgError(RuntimeError):
 class _Region(ctypes.Structure):
     _fields_ = [("ncell", ctypes.c_int32), ("nband", ctypes.c_int32), ("river_velo_opt", ctypes.c_int32),
                 ("frac_routing", ctypes.c_int32), ("default_velocity", ctypes.c_double)] + \
-               [(name, ctypes.c_void_p) for name, _, _ in FIELDS]
+               [(name, ctypes.c_void_p) for name, _, _ in FIELDS] + [("glwd_unit", ctypes.c_void_p)]
 
 
 class _StateView(ctypes.Structure):
@@ -230,7 +231,7 @@ class Model:
                  device: int = 0, stream: int = 0, precision: str = "fp64", members: int = 1,
                  prec_factor=None, gamma_factor=None, block_threads: int = 0, ring_days: int = 0,
                  days_per_step: int = 0, water_temp: bool = False, water_use: int | bool = False,
-                 model_options: dict | None = None):
+                 model_options: dict | None = None, glwd_unit=None):
         self.lib = load_library()
         self.region = region
         self._keep = []
@@ -243,6 +244,14 @@ class Model:
             a = region.arrays[name]
             self._keep.append(a)
             setattr(r, name, a.ctypes.data)
+        # GLWD units (G_glwdUnit): with water use, the riparian cells' net abstractions
+        # are met by their global lake's or reservoir's outflow cell (aggrNUsGloLakResOpt = 1)
+        if glwd_unit is not None:
+            u = np.ascontiguousarray(glwd_unit, np.int32)
+            if u.shape != (region.ncell,):
+                raise ValueError("glwd_unit is one unit per cell")
+            self._keep.append(u)
+            r.glwd_unit = u.ctypes.data
         self.stations = np.ascontiguousarray(
             np.nonzero(region.downstream < 0)[0] if stations is None else stations, np.int32)
         o = _Options()
@@ -268,6 +277,7 @@ class Model:
         self._model = _ModelOptions()
         self.lib.wg_model_options_default(ctypes.byref(self._model))
         self._model.statcorr_opt = int(getattr(region, "statcorr_opt", 0))
+        self._model.aggr_nus_glo_lak_res_opt = int(glwd_unit is not None)
         for k, v in (model_options or {}).items():
             if k not in MODEL_OPTIONS:
                 raise WgError(f"unknown model option {k}")
@@ -580,11 +590,13 @@ class Model:
         self._check(self.lib.wg_set_water_use_inputs(self.h, a.ctypes.data), "set_water_use_inputs")
 
     def _wu_shape(self):
-        return (12, self.region.ncell) if self.members == 1 else (12, self.region.ncell, self.members)
+        k = WU_NSTATE
+        return (k, self.region.ncell) if self.members == 1 else (k, self.region.ncell, self.members)
 
     def water_use(self) -> np.ndarray:
-        """wg_get_water_use: the water-use state [12, ncell] (remaining, unsatisfied and
-        actual use); [12, ncell, members] for ensembles."""
+        """wg_get_water_use: the water-use state [13, ncell] (remaining, unsatisfied and
+        actual use, a riparian cell's share of its outflow cell's unmet use);
+        [13, ncell, members] for ensembles."""
         out = np.empty(self._wu_shape())
         self._check(self.lib.wg_get_water_use(self.h, out.ctypes.data), "get_water_use")
         return out
