@@ -261,7 +261,10 @@ def run_water_use(region, P, T, S, stream, local):
     global lake, reservoir, river, local lake and groundwater) against the plain
     run: four years in one wavefront with each year's tables, the fourth timed
     with CUDA events (the first three fill the wavefront).  Synthetic monthly net
-    abstractions (synthetic.water_use_inputs, seeded)."""
+    abstractions (synthetic.water_use_inputs, seeded).  The "glwd" leg adds the
+    GLWD units of synthetic.glwd_units (aggrNUsGloLakResOpt = 1: the riparian
+    cells' use met by their global lake's or reservoir's outflow cell; each
+    unit's cells routed by one thread)."""
     import torch
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
@@ -269,7 +272,9 @@ def run_water_use(region, P, T, S, stream, local):
     nus, nug, wdr, cons, frgi = sy.water_use_inputs(region, 4)
     use = (nus, nug, wdr, cons)
     out = {}
-    for name, kw in (("water_use", dict(water_use=True)), ("without", dict())):
+    unit = sy.glwd_units(region)
+    for name, kw in (("water_use", dict(water_use=True)), ("glwd", dict(water_use=True, glwd_unit=unit)),
+                     ("without", dict())):
         m = Model(region, max_days=nd, device=local, stream=stream.cuda_stream, days_per_step=WAVEFRONT_DAYS, **kw)
         m.upload_forcing(0, P[:nd], T[:nd], S[:nd])
         if kw:
@@ -289,8 +294,13 @@ def run_water_use(region, P, T, S, stream, local):
             w = m.water_use()
             out[name]["actual_use_km3_last_year"] = float(np.sum(w[11]))
             out[name]["unsatisfied_km3_last_year"] = float(np.sum(w[6]))
+        if "glwd_unit" in kw:
+            out[name]["glwd_units"] = int(unit.max())
+            out[name]["cells_in_units"] = int((unit > 0).sum())
+            out[name]["levels"] = m.num_levels
         del m
     out["cost_vs_plain"] = out["without"]["cell_days_per_s"] / out["water_use"]["cell_days_per_s"]
+    out["glwd_cost_vs_water_use"] = out["water_use"]["cell_days_per_s"] / out["glwd"]["cell_days_per_s"]
     # the oracle port with water use on the host cores (a bounded sample)
     from oracle import Oracle
     cpu_days = int(os.environ.get("WG_CPU_WU_SAMPLE_DAYS", "200"))
