@@ -96,6 +96,41 @@ def test_ensemble_autotune_and_graph():
     assert np.array_equal(m.discharge(0, nd), q_ref)
 
 
+@pytest.mark.parametrize("kd", [1, 5])
+def test_ensemble_stream_overlap_same_bits(kd):
+    """Ensemble: the next chunk's vertical balance on the second stream, beside
+    the wavefront launch of this chunk (the wavefront on all, 3/4 or 1/2 of its
+    blocks), gives the same bits as the launches one after the other, with
+    short chunks (many launch pairs, the ring reused), across calls, and
+    replayed from a CUDA graph."""
+    from watergap2_gb300.gpu import Model
+    nd, M = 75, 64
+    region, (P, T, S) = _region_and_forcing(24, nd, doy0=150)
+    pf = np.exp(np.random.default_rng(5).normal(0.0, 0.3, M)).astype(np.float32)
+    kw = dict(max_days=nd, precision="fp32", members=M, prec_factor=pf, days_per_step=kd)
+    ref = Model(region, **kw)
+    assert ref.vertical_overlap() == 0
+    q_ref = ref.run(150, P, T, S)
+    for frac in (4, 3, 2):
+        m = Model(region, **kw)
+        assert m.vertical_overlap(True) == 1
+        th, blocks, _ = m.launch_shape()
+        m.launch_shape(th, max(1, blocks * frac // 4))
+        m.chunk_steps(2)
+        m.upload_forcing(0, P, T, S)
+        total = m.num_steps(nd)
+        for lo, hi in ((0, 7), (7, 20), (20, total)):
+            m.run_steps(150, 0, nd, lo, hi)
+        assert np.array_equal(m.discharge(0, nd), q_ref), frac
+    g = Model(region, **kw)
+    g.vertical_overlap(True)
+    g.chunk_steps(3)
+    g.upload_forcing(0, P, T, S)
+    g.graph_capture(150, 0, nd, 0, g.num_steps(nd))
+    g.graph_launch()
+    assert np.array_equal(g.discharge(0, nd), q_ref)
+
+
 def test_overlapped_uploads_give_the_same_run():
     """Year-by-year forcing on the copy stream, each year uploaded while the
     previous one runs, equals the run with all forcing uploaded first."""

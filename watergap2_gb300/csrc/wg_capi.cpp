@@ -1167,7 +1167,8 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     const size_t elem = ctx->precision == 0 ? sizeof(double) : sizeof(float);
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = (size_t)16 << 30;
-    const size_t ring_bytes = std::min<size_t>((size_t)8 << 30, free_b / 8);
+    // (ensembles: 24 GB, so that the ring holds two chunks of the stream overlap)
+    const size_t ring_bytes = std::min<size_t>((size_t)(ctx->members > 1 ? 24 : 8) << 30, free_b / 8);
     const size_t budget = opt->ring_days > 0 ? (size_t)opt->ring_days : ring_bytes / (2 * elem * N);
     const int ring = (int)std::max<size_t>(std::max(8, 2 * ctx->days_per_step),
                                            std::min<size_t>(budget, (size_t)ctx->max_days));
@@ -1280,6 +1281,12 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
   if (ctx->blocks_fused <= 0 || ctx->blocks_route <= 0) {
     ctx->err = "cooperative launch not possible";
     return WG_ERR_DEVICE;
+  }
+  if (ens) {   // the second stream of the ensemble's stream overlap (off until switched on or tuned)
+    if (cudaStreamCreateWithFlags(&ctx->va_stream, cudaStreamNonBlocking) != cudaSuccess) return WG_ERR_CUDA;
+    for (cudaEvent_t *e : {&ctx->ev_fork, &ctx->ev_va, &ctx->ev_pipe[0], &ctx->ev_pipe[1]})
+      if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return WG_ERR_CUDA;
+    ctx->blocks_va = std::min(vertical_ahead_max_blocks<float>(true, th), need);
   }
   if (ctx->layout.idle_warp >= 0) {
     st = setup_step_flags(ctx.get());
@@ -1686,6 +1693,41 @@ static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevSta
                                 int t_e) {
   const bool ov = ctx->overlap();
   const int chunk = ctx->eff_chunk();
+  if (ctx->ens_overlap && ctx->members > 1 && ctx->va_stream) {
+    // the next chunk's vertical balance on the second stream, beside this chunk's
+    // wavefront launch: the vertical balance of chunk k+1 writes ring slots that
+    // the wavefront launch of chunk k-1 read (the ring holds two chunks), and the
+    // wavefront launch of chunk k waits for chunk k's vertical balance; the call
+    // ends with both streams joined on the context's stream
+    auto va = [&](int a, int b) {
+      ctx->launches++;
+      return launch_vertical_ahead(c, s, ctx->forcing, ctx->mem, ctx->balance, ring, doy0, fday0, ndays, a, b,
+                                   ctx->blocks_va, ctx->threads, ctx->va_stream);
+    };
+    cudaError_t e = cudaEventRecord(ctx->ev_fork, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->va_stream, ctx->ev_fork, 0);
+    if (e == cudaSuccess) e = va(t_b, std::min(t_e, t_b + chunk));
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_va, ctx->va_stream);
+    int k = 0;
+    for (int a = t_b; a < t_e && e == cudaSuccess; a += chunk, ++k) {
+      const int b = std::min(t_e, a + chunk);
+      e = cudaStreamWaitEvent(ctx->stream, ctx->ev_va, 0);
+      if (e == cudaSuccess)
+        e = launch_pipeline(true, c, s, v, ctx->forcing, ctx->mem, ctx->balance, ring, ctx->sync, ctx->outq, ctx->qst,
+                            doy0, fday0, oday0, ndays, a, b, ctx->blocks_fused, ctx->threads, ctx->layout, ctx->mon,
+                            DevVaWork{}, ctx->wt, ctx->wu, ctx->stream);
+      ctx->launches++;
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_pipe[k & 1], ctx->stream);
+      if (e == cudaSuccess && b < t_e) {
+        if (k >= 1) e = cudaStreamWaitEvent(ctx->va_stream, ctx->ev_pipe[(k - 1) & 1], 0);
+        if (e == cudaSuccess) e = va(b, std::min(t_e, b + chunk));
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_va, ctx->va_stream);
+      }
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_va, ctx->va_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_va, 0);
+    return e == cudaSuccess ? WG_OK : cuda_fail(ctx, e, "run_steps");
+  }
   DevVaWork vw{};
   vw.next = ctx->va_next;
   vw.nitems = (int)((ctx->nstate() + 31) / 32);
@@ -2090,6 +2132,7 @@ wg_status wg_launch_shape(wg_ctx *ctx, int32_t threads, int32_t blocks) {
   ctx->threads = threads;
   ctx->blocks_fused = std::min(blocks > 0 ? std::min(blocks, maxb) : maxb, need);
   ctx->blocks_route = std::min(blocks > 0 ? std::min(blocks, maxr) : maxr, need);
+  if (ens && ctx->precision == 1) ctx->blocks_va = std::min(vertical_ahead_max_blocks<float>(true, threads), need);
   return WG_OK;
 }
 

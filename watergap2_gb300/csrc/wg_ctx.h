@@ -112,6 +112,15 @@ struct wg_ctx {
   cudaGraph_t graph = nullptr;             // wg_graph_capture
   cudaGraphExec_t graph_exec = nullptr;
   int graph_launches = 0;                  // kernels in the captured graph
+  // ensembles (FP32, members > 1): the next chunk's vertical balance runs on a
+  // second stream while this chunk's wavefront launch runs (ens_overlap), the
+  // wavefront launch leaving room on the SMs for its blocks; the ring then holds
+  // two chunks' days.  The fork event starts the second stream after the
+  // context's stream, the others order the launches (wg_capi.cpp run_steps_impl)
+  bool ens_overlap = false;
+  cudaStream_t va_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_va = nullptr, ev_pipe[2] = {nullptr, nullptr};
+  int blocks_va = 0;                       // grid of the vertical-ahead launches on va_stream
   bool timing = false;                     // CUDA events around each launch pair of wg_run_steps
   std::vector<cudaEvent_t> tev;            // 3 per recorded launch pair
   size_t tev_used = 0;
@@ -134,6 +143,9 @@ struct wg_ctx {
     if (own_stream && stream) cudaStreamDestroy(stream);
     if (copy_stream) cudaStreamDestroy(copy_stream);
     if (upload_done) cudaEventDestroy(upload_done);
+    if (va_stream) cudaStreamDestroy(va_stream);
+    for (cudaEvent_t e : {ev_fork, ev_va, ev_pipe[0], ev_pipe[1]})
+      if (e) cudaEventDestroy(e);
   }
   template <class T>
   T *alloc(size_t count) {
@@ -149,13 +161,15 @@ struct wg_ctx {
   // the wavefront launches carry vertical-balance warps for the next chunk
   bool overlap() const { return layout.va_warps > 0 && layout.idle_warp >= 0 && threads == layout.threads; }
   // longest chunk: with the overlap the ring holds this chunk's and the next one's days
-  int chunk_cap() const { return overlap() ? max_chunk() / 2 : max_chunk(); }
+  int chunk_cap() const { return (overlap() || ens_overlap) ? max_chunk() / 2 : max_chunk(); }
   // steps per launch: the set chunk length if it fits, else about 16 days with
   // the overlap (the first chunk of each call runs its vertical balance alone)
   // or the ring
   int eff_chunk() const {
     if (chunk_steps > 0 && chunk_steps <= chunk_cap()) return chunk_steps;
     return overlap() ? std::min((16 + days_per_step - 1) / days_per_step, chunk_cap()) : chunk_cap();
+    // (with ens_overlap the longest chunk that fits the ring: the launches of a
+    // chunk pair run side by side, so fewer, longer chunks lose less at their ends)
   }
   // wavefront steps of a run of ndays days
   int total_steps(int ndays) const { return (ndays + days_per_step - 1) / days_per_step + topo.nlevel - 1; }

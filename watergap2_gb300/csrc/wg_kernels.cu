@@ -714,6 +714,16 @@ int pipeline_max_blocks(bool fused, bool ens, int threads, bool vaw, bool wt, bo
 }
 
 template <class R>
+int vertical_ahead_max_blocks(bool ens, int threads) {
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const void *fn = ens ? (const void *)k_vertical_ahead<R, true> : (const void *)k_vertical_ahead<R, false>;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0) != cudaSuccess) return 0;
+  return per * nsm;
+}
+
+template <class R>
 cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
                             const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
                             const DevSync &sync, double *outq, double *qst, int doy0, int fday0, int oday0, int ndays,
@@ -777,6 +787,7 @@ cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int
   template cudaError_t launch_vertical<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,        \
                                           const DevForcing &, int, int, cudaStream_t);                             \
   template int pipeline_max_blocks<R>(bool, bool, int, bool, bool, bool);                                        \
+  template int vertical_ahead_max_blocks<R>(bool, int);                                                           \
   template cudaError_t launch_pipeline<R>(bool, const DevCellsT<R> &, const DevStateT<R> &, const DevVertT<R> &,  \
                                           const DevForcing &, const DevMembers &, const DevBalance &,             \
                                           const DevRingT<R> &, const DevSync &, double *, double *, int, int,     \

@@ -49,6 +49,9 @@ cudaError_t launch_vertical(const DevCellsT<R> &c, const DevStateT<R> &s, const 
                             int doy, int fday, cudaStream_t st);
 template <class R>
 int pipeline_max_blocks(bool fused, bool ens, int threads, bool vaw = false, bool wt = false, bool wu = false);
+// blocks of k_vertical_ahead resident on the whole device at once (its own occupancy)
+template <class R>
+int vertical_ahead_max_blocks(bool ens, int threads);
 template <class R>
 cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R> &s, const DevVertT<R> &v,
                             const DevForcing &f, const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,

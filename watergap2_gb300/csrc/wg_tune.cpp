@@ -162,6 +162,11 @@ wg_status wg_set_chunk_steps(wg_ctx *ctx, int32_t steps) {
 wg_status wg_set_vertical_overlap(wg_ctx *ctx, int32_t enable) {
   if (!ctx) return WG_ERR_INVALID;
   WG_FLUSH(ctx);
+  if (ctx->members > 1) {   // ensembles: the next chunk's vertical balance on the second stream
+    if (!ctx->va_stream) return WG_ERR_UNSUPPORTED;
+    ctx->ens_overlap = enable != 0;
+    return WG_OK;
+  }
   if (!enable) {
     ctx->layout.va_warps = 0;
     return WG_OK;
@@ -172,7 +177,10 @@ wg_status wg_set_vertical_overlap(wg_ctx *ctx, int32_t enable) {
   return WG_OK;
 }
 
-int32_t wg_get_vertical_overlap(const wg_ctx *ctx) { return ctx && ctx->overlap() ? ctx->layout.va_warps : 0; }
+int32_t wg_get_vertical_overlap(const wg_ctx *ctx) {
+  if (ctx && ctx->members > 1) return ctx->ens_overlap ? 1 : 0;
+  return ctx && ctx->overlap() ? ctx->layout.va_warps : 0;
+}
 
 int32_t wg_get_chunk_steps(const wg_ctx *ctx) {
   if (!ctx) return 0;
@@ -187,7 +195,8 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
   if (t_begin < 0 || t_begin + trial_steps > total) return WG_ERR_INVALID;
   cudaSetDevice(ctx->device);
   const int th0 = ctx->threads, ch0 = ctx->chunk_steps;
-  const int bf0 = ctx->blocks_fused, br0 = ctx->blocks_route;
+  const int bf0 = ctx->blocks_fused, br0 = ctx->blocks_route, bv0 = ctx->blocks_va;
+  const bool eo0 = ctx->ens_overlap;
   const WarpLayout lay0 = ctx->layout;
   int32_t tmp = 0;
   wg_status st = snapshot_save(ctx);
@@ -204,8 +213,17 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
     ctx->threads = th0;
     ctx->blocks_fused = bf0;
     ctx->blocks_route = br0;
+    ctx->blocks_va = bv0;
     ctx->layout = lay0;
   };
+  // ensembles: without and with the stream overlap, the wavefront launch on all
+  // its blocks or on 3/4 or 1/2 of them (leaving the SMs room for the vertical
+  // balance beside it)
+  struct Ov { bool on; int num; };
+  std::vector<Ov> ovs = {{false, 4}};
+  if (ctx->members > 1 && ctx->va_stream) ovs = {{false, 4}, {true, 4}, {true, 3}, {true, 2}};
+  bool best_eo = eo0;
+  int best_blocks = bf0;
   // first the context's own shape and layout; with vertical-balance warps, also
   // the same layout without them
   ths.insert(ths.begin(), -1);
@@ -218,30 +236,39 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
     } else if (wg_launch_shape(ctx, th, 0) != WG_OK) {
       continue;   // does not fit the device
     }
-    std::vector<int> chs;   // chunk lengths 8 .. the longest this shape allows
-    for (int c = 8; c <= ctx->chunk_cap(); c *= 2) chs.push_back(c);
-    if (chs.empty() || chs.back() != ctx->chunk_cap()) chs.push_back(ctx->chunk_cap());
-    for (int ch : chs) {
-      if (ch > trial_steps && ch != chs.front()) continue;   // a chunk longer than the trial says nothing
-      ctx->chunk_steps = ch;
-      st = snapshot_restore(ctx);
-      if (st != WG_OK) break;
-      cudaEventRecord(e0, ctx->stream);
-      st = wg_run_steps(ctx, doy0, fday0, ndays, t_begin, t_begin + trial_steps);
-      cudaEventRecord(e1, ctx->stream);
-      if (st != WG_OK) break;
-      st = wg_synchronize(ctx);
-      if (st != WG_OK) break;
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      ++trials;
-      if (ms < best) {
-        best = ms;
-        best_th = th;
-        best_ch = ch;
-        best_va = ctx->layout.va_warps;
+    const int full_blocks = ctx->blocks_fused;
+    for (const Ov &ov : ovs) {
+      ctx->ens_overlap = ov.on;
+      ctx->blocks_fused = std::max(1, full_blocks * ov.num / 4);
+      std::vector<int> chs;   // chunk lengths 8 .. the longest this shape allows
+      for (int c = 8; c <= ctx->chunk_cap(); c *= 2) chs.push_back(c);
+      if (chs.empty() || chs.back() != ctx->chunk_cap()) chs.push_back(ctx->chunk_cap());
+      for (int ch : chs) {
+        if (ch > trial_steps && ch != chs.front()) continue;   // a chunk longer than the trial says nothing
+        ctx->chunk_steps = ch;
+        st = snapshot_restore(ctx);
+        if (st != WG_OK) break;
+        cudaEventRecord(e0, ctx->stream);
+        st = wg_run_steps(ctx, doy0, fday0, ndays, t_begin, t_begin + trial_steps);
+        cudaEventRecord(e1, ctx->stream);
+        if (st != WG_OK) break;
+        st = wg_synchronize(ctx);
+        if (st != WG_OK) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ++trials;
+        if (ms < best) {
+          best = ms;
+          best_th = th;
+          best_ch = ch;
+          best_va = ctx->layout.va_warps;
+          best_eo = ov.on;
+          best_blocks = ctx->blocks_fused;
+        }
       }
+      if (st != WG_OK) break;
     }
+    ctx->blocks_fused = full_blocks;
     if (st != WG_OK) break;
   }
   cudaEventDestroy(e0);
@@ -251,6 +278,7 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
   if (st == WG_OK) st = wg_synchronize(ctx);
   if (st != WG_OK || trials == 0) {
     restore_shape0();
+    ctx->ens_overlap = eo0;
     ctx->chunk_steps = ch0;
     return st != WG_OK ? st : WG_ERR_UNSUPPORTED;
   }
@@ -260,6 +288,8 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
   } else {
     wg_launch_shape(ctx, best_th, 0);
   }
+  ctx->ens_overlap = best_eo;
+  if (ctx->members > 1) ctx->blocks_fused = best_blocks;
   ctx->chunk_steps = best_ch;
   out->threads = ctx->threads;
   int32_t mb = 0;
