@@ -421,12 +421,31 @@ wg_status wg_set_step_sync(wg_ctx *ctx, int32_t flags);
  * output day 0 (wg_get_discharge's day 0) is day-of-year doy_day0; 0 months
  * switches them off.  Enabling (again) zeroes them. */
 wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0);
-/* which: 0 river availability [km3/month] (sum of the daily transported volume),
+/* The vertical balance's monthly output grids as well (daily.cpp:1281-1386, the
+ * reference's grid_store = 2 with grid_store_TypeForStorages = 0), on the calendar
+ * of wg_monthly_outputs: FP64, one member, without water temperature or water use
+ * (WG_ERR_UNSUPPORTED otherwise); accumulated by the wavefront's kernels, so the
+ * per-day wg_step_vertical refuses while they are on (the deferred per-day calls
+ * of wg_set_deferred run through the wavefront).  enable 0 switches them off. */
+wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable);
+/* which: 0 river availability [km3/month] (sum of the daily transported volume
+ * outside inland sinks, routing.cpp:4010-4011),
  * 1 sum of the day-end surface-water + groundwater storage [km3 x days],
- * 2 smallest and 3 largest daily transported volume [km3/day],
+ * 2 smallest and 3 largest daily transported volume [km3/day] (outside inland
+ * sinks; 0 where the month has no routed day and in sinks, as the reference),
  * 4 cell runoff: transported volume minus upstream inflow (routing.cpp:3933-3939;
  * in inland sinks minus the inflow) [km3/month],
  * 5 sum of the daily river velocity [m/s x days];
+ * 6 + k: field k of the vertical balance's grids (wg_monthly_outputs_vertical):
+ * 0 G_monthlyPrecipitation [mm], 1 Temperature [degC x days], 2 ExtRad, 3 ShortUpRad,
+ * 4 ShortDownRad, 5 NetShortRad, 6 NetLongRad, 7 NetRadiation [W/m2 x days],
+ * 8 OpenWaterPET, 9 PET, 10 AET, 11 LandAET, 12 LandAET_uncorr, 13 LAI [x days],
+ * 14 Albedo [x days], 15 Interception, 16 canopyWaterContent, 17
+ * maxcanopyWaterContent, 18 SnowFall, 19 RainFall, 20 SnowMelt, 21 SnowEvap,
+ * 22 SWE, 23 SnowCoverAvg [x days], 24 SoilWaterAvg, 25 Runoff, 26 UrbanRunoff,
+ * 27 SurfaceRunoff, 28 GwRecharge [mm, water terms weighted by the land share of
+ * the continental area], 29 CanopyStorage, 30 SnowStorage, 31 SoilStorage at
+ * the month's end [km3];
  * out [nm][ncell][members], cell order. */
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out);
 

@@ -72,8 +72,21 @@ WT_FIELDS = ["wt_river", "wt_loclake", "wt_locwetl", "wt_glolake", "wt_res", "wt
              "ice_river", "ice_loclake", "ice_locwetl", "ice_glolake", "ice_res", "ice_glowetl", "river_avail"]
 
 
+# the monthly output grids the harness dumps with outputs=True (in its order):
+# the vertical balance's (daily.cpp:1281-1386; storages at the month's end) and routing's
+# (routing.cpp:3964-4040, storages at the month's end 4725-4737)
+MONTHLY_VERTICAL = ["prec", "temp", "ext_rad", "short_up_rad", "short_down_rad", "net_short_rad", "net_long_rad",
+                    "net_rad", "open_water_pet", "pet", "aet", "land_aet", "land_aet_uncorr", "lai", "albedo",
+                    "interception", "canopy_wc", "max_canopy_wc", "snowfall", "rainfall", "snowmelt", "snow_evap",
+                    "swe", "snow_cover", "soil_wc", "runoff", "urban_runoff", "surface_runoff", "gw_recharge",
+                    "canopy_storage", "snow_storage", "soil_storage"]
+MONTHLY_ROUTING = ["river_avail", "min_river_avail", "max_river_avail", "cell_runoff", "velocity", "loclake_storage",
+                   "locwetl_storage", "glolake_storage", "glowetl_storage", "res_storage", "river_storage",
+                   "gw_storage"]
+
+
 def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000, wtemp=None, wuse=None,
-               delayed=False, glwd_unit=None):
+               delayed=False, glwd_unit=None, outputs=False):
     n = region.ncell
     if n > NG:
         raise ValueError("region larger than the reference grid")
@@ -164,6 +177,8 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
     np.ascontiguousarray(P, np.float32).tofile(f"{d}/f_prec.bin")
     np.ascontiguousarray(T, np.float32).tofile(f"{d}/f_temp.bin")
     np.ascontiguousarray(S, np.float32).tofile(f"{d}/f_swrad.bin")
+    if outputs:   # read by dailyWaterBalanceClass::init with grid_store 2 (daily.cpp:1558)
+        _unf(f"{d}/G_ALBEDO_CYCLE.12.UNF0", np.zeros(NG * 12, np.float32), np.float32)
     if wtemp is not None:   # (longwave [ndays, ncell], groundwater temperature [ncell])
         from watergap2_gb300.region import inflow_cells
         lw, gwt = wtemp
@@ -190,13 +205,13 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
         f.write(f"{n} {P.shape[0]} {doy0} {year0} {resopt} {region.river_velo_opt} {len(stations)} {len(snapshots)} "
                 f"{0 if wtemp is None else 1} {int(getattr(region, 'frac_routing', 0))} "
                 f"{0 if wuse is None else (2 if delayed else 1) + (0 if glwd_unit is None else 2)} "
-                f"{int(getattr(region, 'statcorr_opt', 0))}\n")
+                f"{int(getattr(region, 'statcorr_opt', 0))} {int(bool(outputs))}\n")
     with open(f"{d}/snapshots.txt", "w") as f:
         f.write(" ".join(str(int(s)) for s in snapshots) + "\n")
 
 
 def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wtemp=None, wuse=None, delayed=False,
-        threads=1, glwd_unit=None):
+        threads=1, glwd_unit=None, outputs=False):
     """Run the reference harness; returns dict(lai_a, lai_b, bottom_width, snapshots=[{field: array}],
     discharge=[ndays, nstation], stations=..., timing=dict(threads, vertical_s, routing_s)): the vertical
     pass on `threads` OpenMP threads, routing serial, as integrate_wghm_ runs them."""
@@ -211,7 +226,7 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
     snapshots = list(snapshots or [ndays])
     tmp = workdir or tempfile.mkdtemp(prefix="wg_ref_")
     write_case(region, tmp, P, T, S, doy0, stations, snapshots, wtemp=wtemp, wuse=wuse, delayed=delayed,
-               glwd_unit=glwd_unit)
+               glwd_unit=glwd_unit, outputs=outputs)
     out = os.path.join(tmp, "out.bin")
     env = dict(os.environ, WG_REF_THREADS=str(int(threads)))
     subprocess.run([HARNESS, tmp, out], check=True, stdout=subprocess.DEVNULL, env=env)
@@ -241,6 +256,11 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
     if wtemp is not None:
         res["river_temp"] = raw[o:o + ndays * len(stations)].reshape(ndays, len(stations)).copy()
         o += ndays * len(stations)
+    if outputs:   # the year's monthly grids [12][ncell] per field
+        res["monthly"] = {}
+        for f in MONTHLY_VERTICAL + MONTHLY_ROUTING:
+            res["monthly"][f] = raw[o:o + 12 * n].reshape(12, n).copy()
+            o += 12 * n
     assert o == raw.size, (o, raw.size)
     res["stations"] = stations
     with open(os.path.join(tmp, "timing.txt")) as f:

@@ -59,6 +59,7 @@ int main(int argc, char **argv) {
   if (argc < 3) { fprintf(stderr, "usage: %s <case dir> <out file>\n", argv[0]); return 1; }
   std::string dir = argv[1];
   int ncase, ndays, doy0, year0, resopt, velo, nstation, nsnap, wtemp = 0, frac = 0, wuse = 0, statcorr = 0;
+  int outputs = 0;
   {
     std::ifstream m(dir + "/meta.txt");
     m >> ncase >> ndays >> doy0 >> year0 >> resopt >> velo >> nstation >> nsnap;
@@ -69,6 +70,7 @@ int main(int argc, char **argv) {
                                     // (2: delayed satisfaction), 3/4 the same with the NUs of global
                                     // lakes' riparian cells aggregated (aggrNUsGloLakResOpt = 1)
     if (!(m >> statcorr)) statcorr = 0;   // optional: options.statcorrOpt
+    if (!(m >> outputs)) outputs = 0;     // optional: the monthly output grids (grid_store = 2)
   }
   std::vector<int> snap_days(nsnap);
   {
@@ -95,6 +97,10 @@ int main(int argc, char **argv) {
   if (wuse) options.subtract_use = 2;
   if (wuse == 2 || wuse == 4) options.delayedUseSatisfaction = 1;   // unmet demand carried to the next day
   if (wuse >= 3) options.aggrNUsGloLakResOpt = 1;   // GLWD units from <case>/GLWDunits.UNF4
+  if (outputs) {   // monthly output grids, storages at the month's end (grid_store_TypeForStorages 0)
+    options.grid_store = 2;
+    options.outMinMaxRiverAvail = 1;
+  }
   options.glacierOpt = 0; options.calc_wtemp = wtemp; options.start_year = year0; options.end_year = year0;
   options.init_years = 0; options.time_step = 1; options.outLAImax = 0;
 
@@ -308,6 +314,32 @@ int main(int argc, char **argv) {
   }
   write_raw(out, q.data(), q.size());
   if (wtemp) write_raw(out, wt_daily.data(), wt_daily.size());
+  if (outputs) {   // the year's monthly grids [field][month][cell]: daily.cpp:1281-1386, routing.cpp:3964-4040, 4725-4737
+    auto &w = dailyWaterBalance;
+    const MonthlyGrid<false> *vert[] = {
+        &w.G_monthlyPrecipitation, &w.G_monthlyTemperature, &w.G_monthlyExtRad, &w.G_monthlyShortUpRad,
+        &w.G_monthlyShortDownRad, &w.G_monthlyNetShortRad, &w.G_monthlyNetLongRad, &w.G_monthlyNetRadiation,
+        &w.G_monthlyOpenWaterPET, &w.G_monthlyPET, &w.G_monthlyAET, &w.G_monthlyLandAET, &w.G_monthlyLandAET_uncorr,
+        &w.G_monthlyLAI, &w.G_monthlyAlbedo, &w.G_monthlyInterception, &w.G_monthlycanopyWaterContent,
+        &w.G_monthlymaxcanopyWaterContent, &w.G_monthlySnowFall, &w.G_monthlyRainFall, &w.G_monthlySnowMelt,
+        &w.G_monthlySnowEvap, &w.G_monthlySWE, &w.G_monthlySnowCoverAvg, &w.G_monthlySoilWaterAvg,
+        &w.G_monthlyRunoff, &w.G_monthlyUrbanRunoff, &w.G_monthlySurfaceRunoff, &w.G_monthlyGwRecharge};
+    const MonthlyGrid<> *vstor[] = {&w.G_monthlyCanopyStorage, &w.G_monthlySnowStorage, &w.G_monthlySoilStorage};
+    const MonthlyGrid<false> *rout[] = {
+        &routing.G_monthlyRiverAvail, &routing.G_monthlyMinRiverAvail, &routing.G_monthlyMaxRiverAvail,
+        &routing.G_monthlyCellRunoff, &routing.G_monthlyVelocity, &routing.G_monthlyLocLakeStorage,
+        &routing.G_monthlyLocWetlStorage, &routing.G_monthlyGloLakeStorage, &routing.G_monthlyGloWetlStorage,
+        &routing.G_monthlyResStorage, &routing.G_monthlyRiverStorage, &routing.G_monthlyGwStorage};
+    std::vector<double> buf((size_t)12 * ncase);
+    auto dump = [&](auto *g) {
+      for (int m = 0; m < 12; m++)
+        for (int n = 0; n < ncase; n++) buf[(size_t)m * ncase + n] = (*g)(n, m);
+      write_raw(out, buf.data(), buf.size());
+    };
+    for (auto *g : vert) dump(g);
+    for (auto *g : vstor) dump(g);
+    for (auto *g : rout) dump(g);
+  }
   fclose(out);
   if (FILE *tf = fopen((dir + "/timing.txt").c_str(), "w")) {
     fprintf(tf, "%d %.9f %.9f %d %d\n", nthreads, t_vert, t_rout, ndays, ncase);

@@ -68,18 +68,24 @@ def main(names=None):
         res = ref_case.run(region, P, T, S, doy0=doy0, stations=stations, snapshots=snaps)
         extra = dict(P=P, T=T, S=S, doy0=np.array(doy0), stations=res["stations"], snap_days=np.array(snaps),
                      discharge=res["discharge"])
-        rep = ref_case.REF_BANDS // region.nband
-        for i, snap in enumerate(res["snapshots"]):
-            bands = snap.pop("snow_band")
-            # replicated bands must agree with each other; keep one per band
-            b = bands.reshape(region.ncell, region.nband, rep)
-            assert np.array_equal(b, np.repeat(b[:, :, :1], rep, axis=2))
-            extra[f"s{i}_snow_band"] = b[:, :, 0].copy()
-            for k, v in snap.items():
-                extra[f"s{i}_{k}"] = v
+        _put_snapshots(region, res, extra)
         path = os.path.join(HERE, f"{name}.npz")
         save_npz(region, path, **extra)
         print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
+
+
+def _put_snapshots(region, res, extra):
+    """The reference's state at each snapshot day as s<i>_<field>, one snow band
+    of each replicated group."""
+    rep = ref_case.REF_BANDS // region.nband
+    for i, snap in enumerate(res["snapshots"]):
+        bands = snap.pop("snow_band")
+        # replicated bands must agree with each other; keep one per band
+        b = bands.reshape(region.ncell, region.nband, rep)
+        assert np.array_equal(b, np.repeat(b[:, :, :1], rep, axis=2))
+        extra[f"s{i}_snow_band"] = b[:, :, 0].copy()
+        for k, v in snap.items():
+            extra[f"s{i}_{k}"] = v
 
 
 def wtemp_region(seed=21):
@@ -226,6 +232,30 @@ def main_wuse_glwd(names=None):
         print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+def main_outputs(names=None, name="swb_outputs_365d"):
+    """The monthly output grids (grid_store = 2, storages at the month's end) of the
+    vertical balance and routing over one calendar year, on the water-body region
+    with inland sinks."""
+    if names and name not in names:
+        return
+    if not ref_case.available():
+        if not ref_case.build(REF_SOURCE):
+            raise SystemExit("reference sources not found; cannot regenerate fixtures")
+    region = sy.region_small_swb(seed=21, ny=16, nx=32, block_at=(100, 300))
+    nd = 365
+    P, T, S = sy.forcing(region, nd, doy0=1)
+    outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+    res = ref_case.run(region, P, T, S, doy0=1, stations=outl[:24], snapshots=[nd], outputs=True)
+    extra = dict(P=P, T=T, S=S, doy0=np.array(1), stations=res["stations"], snap_days=np.array([nd]),
+                 discharge=res["discharge"])
+    _put_snapshots(region, res, extra)
+    for k, v in res["monthly"].items():
+        extra[f"m_{k}"] = v
+    path = os.path.join(HERE, f"{name}.npz")
+    save_npz(region, path, **extra)
+    print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 def main_wtemp_wuse(names=None, name="swb_wtemp_wuse_120d"):
     """Water use together with the water temperature (calc_wtemp = 1, subtract_use
     = 2): the water-temperature region and a cold season across a year end."""
@@ -351,4 +381,5 @@ if __name__ == "__main__":
     main_wtemp(sys.argv[1:])
     main_wuse(sys.argv[1:])
     main_wuse_glwd(sys.argv[1:])
+    main_outputs(sys.argv[1:])
     main_wtemp_wuse(sys.argv[1:])

@@ -127,3 +127,19 @@ def test_station_correction_fixture_changes_discharge():
     o = Oracle(region.with_options(statcorr_opt=0).with_bands(100))
     q, _ = o.run(int(ex["doy0"]), ex["P"], ex["T"], ex["S"], discharge=True)
     assert not np.allclose(q[:, ex["stations"]], ex["discharge"], rtol=1e-6)
+
+
+def test_monthly_output_fixture_pinned_to_its_inputs():
+    """The reference's monthly grids in swb_outputs_365d are its month sums in
+    cell order (grid_store = 2 divides the means only when it writes): monthly
+    precipitation and temperature equal the sums of the fixture's daily forcing
+    exactly, and the month-end storages at December's end equal the state of
+    the same run's day-365 snapshot."""
+    region, ex = load_npz(os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_365d.npz"))
+    b = np.r_[0, np.cumsum([31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31])]
+    for f, field in (("prec", "P"), ("temp", "T")):
+        x = ex[field].astype(np.float64)
+        sums = np.array([x[b[k]:b[k + 1]].sum(axis=0) for k in range(12)])
+        assert np.array_equal(sums, ex[f"m_{f}"]), f
+    for f in ("loclake", "locwetl", "glolake", "glowetl", "res", "river", "gw"):
+        assert np.array_equal(ex[f"m_{f}_storage"][11], ex[f"s0_{f}"]), f

@@ -289,7 +289,8 @@ struct HostConsts {
 #define WG_RFIELDS(X)                                                                                            \
   X(cfa) X(inv_cfa) X(mprec) X(alpha) X(pet_mxdy) X(mnetrad) X(mcwh) X(t_snowfz) X(t_snowmt) X(pcritgwa) X(gamma) \
   X(albedo) X(albedo_snow) X(ddf_m) X(lai_min) X(lai_max) X(smax) X(inv_smax) X(fg) X(rgmax) X(built_up)         \
-  X(t_gradnt) X(elev0) X(area) X(area_f) X(gw_e) X(gw_ik) X(gw_ome) X(sw_k) X(sw_e) X(sw_ik) X(sw_ome) X(evx)    \
+  X(t_gradnt) X(elev0) X(contfreq) X(area) X(area_f) X(gw_e) X(gw_ik) X(gw_ome) X(sw_k) X(sw_e) X(sw_ik)        \
+  X(sw_ome) X(evx)                                                                                               \
   X(a6) X(ll100) X(maxs_ll) X(inv_maxs_ll) X(lw100) X(maxs_lw) X(inv_maxs_lw) X(la6) X(maxs_gl) X(inv_maxs_gl)  \
   X(ra6) X(rcap) X(rcap01) X(c_ratio) X(c4) X(one_m_c4) X(prov_rel) X(gw100)                                   \
   X(maxs_gw) X(inv_maxs_gw) X(bw) X(inv_mr) X(sqrt_slope) X(inv_len) X(rlen) X(fcatch)
@@ -1050,6 +1051,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     h.flags[i] = f;
     const double ar = r->area_km2[i];
     h.area[i] = ar;
+    h.contfreq[i] = r->contfreq[i];
     h.area_f[i] = ar * 1e-8;
     h.a6[i] = ar / 1000000.;
     h.albedo[i] = r->lct_albedo[lct - 1];
@@ -1702,7 +1704,7 @@ static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevSta
     auto va = [&](int a, int b) {
       ctx->launches++;
       return launch_vertical_ahead(c, s, ctx->forcing, ctx->mem, ctx->balance, ring, doy0, fday0, ndays, a, b,
-                                   ctx->blocks_va, ctx->threads, ctx->va_stream);
+                                   ctx->blocks_va, ctx->threads, ctx->va_stream, ctx->mon, oday0);
     };
     cudaError_t e = cudaEventRecord(ctx->ev_fork, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->va_stream, ctx->ev_fork, 0);
@@ -1738,7 +1740,7 @@ static wg_status run_steps_impl(wg_ctx *ctx, const DevCellsT<R> &c, const DevSta
     cudaError_t e = cudaSuccess;
     if (!ov || a == t_b) {
       e = launch_vertical_ahead(c, s, ctx->forcing, ctx->mem, ctx->balance, ring, doy0, fday0, ndays, a, b,
-                                ctx->blocks_fused, ctx->threads, ctx->stream);
+                                ctx->blocks_fused, ctx->threads, ctx->stream, ctx->mon, oday0);
       ctx->launches++;
     }
     if (ev) cudaEventRecord(ev[1], ctx->stream);
@@ -1770,6 +1772,7 @@ static wg_status run_steps_at(wg_ctx *ctx, int doy0, int fday0, int oday0, int n
 }
 
 static wg_status vertical_now(wg_ctx *ctx, int doy, int fday) {
+  if (ctx->mon.vert) return WG_ERR_UNSUPPORTED;   // the per-day kernel has no monthly grids: wg_set_deferred
   cudaSetDevice(ctx->device);
   join_uploads(ctx);
   ctx->launches++;
@@ -2037,6 +2040,10 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
     cudaFree(ctx->mon_buf);
     ctx->mon_buf = nullptr;
   }
+  if (ctx->mon_vbuf) {
+    cudaFree(ctx->mon_vbuf);
+    ctx->mon_vbuf = nullptr;
+  }
   {   // the daily storage record is kept
     double *ds = ctx->mon.daily_storage;
     const int dd = ctx->mon.daily_days;
@@ -2064,21 +2071,41 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
   e = cudaMemsetAsync(ctx->mon_buf, 0, 6 * per * sizeof(double), ctx->stream);
   if (e == cudaSuccess) e = launch_fill(m.min_avail, per, INFINITY, ctx->stream);
   if (e == cudaSuccess) e = launch_fill(m.max_avail, per, -INFINITY, ctx->stream);
+  if (e == cudaSuccess && ctx->mon_vert_on) {   // the vertical balance's grids, on the same calendar
+    e = cudaMalloc((void **)&ctx->mon_vbuf, (size_t)wg::VOUT_FIELDS * per * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->mon_vbuf, 0, (size_t)wg::VOUT_FIELDS * per * sizeof(double), ctx->stream);
+    if (e == cudaSuccess) m.vert = ctx->mon_vbuf;
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return cuda_fail(ctx, e, "monthly_outputs");
 }
 
+wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable) {
+  if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
+  if (enable && (ctx->precision != 0 || ctx->members != 1 || ctx->wt.enabled || ctx->wu.enabled))
+    return WG_ERR_UNSUPPORTED;
+  ctx->mon_vert_on = enable != 0;
+  if (!ctx->mon.enabled) return WG_OK;   // takes effect with wg_monthly_outputs
+  return wg_monthly_outputs(ctx, ctx->mon.nmonths, ctx->mon.doy_day0);
+}
+
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out) {
-  if (!ctx || !out || which < 0 || which > 5 || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths) return WG_ERR_INVALID;
+  if (!ctx || !out || which < 0 || which >= 6 + wg::VOUT_FIELDS || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths)
+    return WG_ERR_INVALID;
+  if (which >= 6 && !ctx->mon.vert) return WG_ERR_UNSUPPORTED;
   WG_FLUSH(ctx);
   wg_status st = wg_synchronize(ctx);
   if (st != WG_OK) return st;
   const size_t N = ctx->nstate(), per = (size_t)ctx->mon.nmonths * N;
   const int M = ctx->members;
   std::vector<double> buf((size_t)nm * N);
-  cudaError_t e = cudaMemcpy(buf.data(), ctx->mon_buf + which * per + (size_t)m0 * N, buf.size() * sizeof(double),
-                             cudaMemcpyDeviceToHost);
+  const double *src = which < 6 ? ctx->mon_buf + which * per : ctx->mon_vbuf + (size_t)(which - 6) * per;
+  cudaError_t e = cudaMemcpy(buf.data(), src + (size_t)m0 * N, buf.size() * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "get_monthly");
+  if (which == 2 || which == 3)   // no day in the month, or an inland sink: 0, as the reference's reset grids
+    for (double &v : buf)
+      if (std::isinf(v)) v = 0.;
   const auto &c2s = ctx->topo.cell_of_slot;
   for (int k = 0; k < nm; ++k)
     for (int sl = 0; sl < ctx->n; ++sl)

@@ -69,6 +69,8 @@ struct wg_ctx {
   DevSync sync{};
   DevMonthly mon{};                        // wg_monthly_outputs
   double *mon_buf = nullptr;
+  double *mon_vbuf = nullptr;              // the vertical balance's monthly grids (wg_monthly_outputs_vertical)
+  bool mon_vert_on = false;
   double *daily_storage_buf = nullptr;     // wg_record_daily_storages (context allocation)
   double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
   float *staging = nullptr;
@@ -139,6 +141,7 @@ struct wg_ctx {
   ~wg_ctx() {
     release_tools();
     if (mon_buf) cudaFree(mon_buf);
+    if (mon_vbuf) cudaFree(mon_vbuf);
     for (void *p : allocs) cudaFree(p);
     if (own_stream && stream) cudaStreamDestroy(stream);
     if (copy_stream) cudaStreamDestroy(copy_stream);

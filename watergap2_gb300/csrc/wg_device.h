@@ -55,6 +55,7 @@ struct DevCellsT {
   const R *cfa, *inv_cfa, *mprec, *alpha, *pet_mxdy, *mnetrad, *mcwh, *t_snowfz, *t_snowmt, *pcritgwa, *gamma;
   const R *albedo, *albedo_snow, *ddf_m, *lai_min, *lai_max, *smax, *inv_smax, *fg, *rgmax, *built_up;
   const R *t_gradnt, *elev0;
+  const R *contfreq;            // continental share of the cell [%] (the monthly output grids)
   const R *band_dt;             // [nband][n] (elev_b - elev_0) * P_T_GRADNT
   const float *snow_thr;        // FP32 paths: [nband][n] the largest float temperature at which the
                                 // band gets snowfall as the FP64 path decides it (null in FP64)
@@ -118,6 +119,20 @@ constexpr int WG_BALANCE_ARRAYS = 14;
 // G_monthlyMin/MaxRiverAvail, monthly storage), [nmonths][n*members] each; month m
 // of the output calendar = year * 12 + month - month0 of output day od, the
 // calendar starting at day-of-year doy_day0 for output day 0.
+// The vertical balance's monthly output grids (daily.cpp:1281-1386, grid_store 2),
+// field k at vert[k * nmonths * N + month * N + state]: 0 precipitation [mm],
+// 1 temperature [degC], 2-7 radiation [W/m2 x days]: extraterrestrial, reflected
+// and incoming shortwave, net shortwave, net longwave, net, 8 open-water PET,
+// 9 PET, 10 AET of the soil, 11 land AET (cell-corrected), 12 land AET
+// uncorrected, 13 LAI, 14 albedo, 15 interception, 16 canopy water content,
+// 17 its capacity, 18 snowfall, 19 rainfall, 20 snowmelt, 21 snow evaporation,
+// 22 snow water equivalent, 23 snow-covered fraction, 24 soil water, 25 total
+// runoff, 26 urban runoff, 27 surface runoff, 28 groundwater recharge [mm
+// (x days for states), per day's land share of the continental area where the
+// reference weighs it so]; 29-31 canopy, snow and soil storage at the month's
+// end [km3].
+constexpr int VOUT_FIELDS = 32;
+
 struct DevMonthly {
   double *river_avail;   // sum of the day's transported volume [km3/month]   (G_monthlyRiverAvail)
   double *storage;       // sum of the day-end surface-water + groundwater storage [km3 x days]
@@ -125,6 +140,7 @@ struct DevMonthly {
   double *cell_runoff;   // sum of transported minus upstream inflow [km3/month] (G_monthlyCellRunoff)
   double *velocity;      // sum of the river velocity [m/s x days]                (G_monthlyVelocity)
   int32_t nmonths, doy_day0, month0, enabled;
+  double *vert;          // null, or the vertical balance's grids [VOUT_FIELDS][nmonths][N]
   // the day-end routing storages of every cell and output day, [day][7][n*members]
   // in the order the reference writes them into its state file (routing.cpp:5001-5020):
   // local lake, local wetland, global lake, global wetland, reservoir, river,

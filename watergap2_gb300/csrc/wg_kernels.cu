@@ -180,13 +180,18 @@ __device__ __forceinline__ void store_rstate(const DevStateT<R> &s, size_t i, co
 template <class R>
 __device__ __forceinline__ void vertical_at(const DevCellsT<R> &c, const DevStateT<R> &st, size_t N, int s,
                                             size_t si, int doy, R Pin, R gamma_soil, float Tf, float SWf, R laf,
-                                            R prev, VOut<R> &o) {
+                                            R prev, VOut<R> &o, double *mo = nullptr, size_t mos = 0) {
   const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
   const R ext = c.ext_rad[ti], inv_s0 = c.inv_s0[ti];
   R canopy = st.canopy[si], soil = st.soil[si], gsnow = st.snow[si], psum = st.lai_precsum[si];
   int days = st.lai_days[si], status = st.lai_status[si];
-  vertical_cell<R>(c, s, gamma_soil, canopy, soil, gsnow, st.snow_band + si, N, days, status, psum, laf, prev, Pin,
-                   Tf, SWf, ext, inv_s0, o);
+  if (mo)   // the monthly output grids (FP64 single member)
+    vertical_cell<R, std::is_same<R, double>::value>(c, s, gamma_soil, canopy, soil, gsnow, st.snow_band + si, N,
+                                                      days, status, psum, laf, prev, Pin, Tf, SWf, ext, inv_s0, o, mo,
+                                                      mos);
+  else
+    vertical_cell<R>(c, s, gamma_soil, canopy, soil, gsnow, st.snow_band + si, N, days, status, psum, laf, prev, Pin,
+                     Tf, SWf, ext, inv_s0, o);
   st.canopy[si] = canopy; st.soil[si] = soil; st.snow[si] = gsnow; st.lai_precsum[si] = psum;
   st.lai_days[si] = days; st.lai_status[si] = status;
 }
@@ -215,10 +220,22 @@ __global__ void __launch_bounds__(256) k_vertical(DevCellsT<R> c, DevStateT<R> s
 // One (cell, member) state index i of the vertical balance run ahead: the days
 // the wavefront steps [t_b, t_e) will route, vertical state in registers, surface
 // runoff and recharge into the ring; balance terms into arrays 0, 1 and 10.
+// The entry of state si in the vertical balance's monthly output grids for output
+// day od (the month of the output calendar, as the routing aggregates count it),
+// or null when the grids are off or the day is outside them.
+__device__ __forceinline__ double *vert_month(const DevMonthly &mon, int od, size_t si, size_t N) {
+  if (!mon.vert) return nullptr;
+  const int yd = mon.doy_day0 - 1 + od;
+  const int mi = (yd / 365) * 12 + month_of(yd % 365 + 1) - mon.month0;
+  if (mi < 0 || mi >= mon.nmonths) return nullptr;
+  return mon.vert + (size_t)mi * N + si;
+}
+
 template <class R, bool ENS>
 __device__ __forceinline__ void va_cell(const DevCellsT<R> &c, const DevStateT<R> &st, const DevForcing &f,
                                         const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring,
-                                        int doy0, int fday0, int ndays, int t_b, int t_e, size_t i, size_t N) {
+                                        int doy0, int fday0, int ndays, int t_b, int t_e, size_t i, size_t N,
+                                        const DevMonthly *mon = nullptr, int oday0 = 0) {
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const int s = ENS ? (int)(i / M) : (int)i;
@@ -243,8 +260,15 @@ __device__ __forceinline__ void va_cell(const DevCellsT<R> &c, const DevStateT<R
     const size_t fo = (size_t)(fday0 + d) * n + s;
     const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
     VOut<R> o;
-    vertical_cell<R>(c, s, gam, canopy, soil, gsnow, st.snow_band + i, N, days, status, psum, laf, laf,
-                     R(f.prec[fo]) * pf, f.temp[fo], f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o);
+    double *mo = (!ENS && mon) ? vert_month(*mon, oday0 + d, i, N) : nullptr;
+    if (mo)   // the monthly output grids (FP64 single member)
+      vertical_cell<R, std::is_same<R, double>::value>(c, s, gam, canopy, soil, gsnow, st.snow_band + i, N, days,
+                                                        status, psum, laf, laf, R(f.prec[fo]) * pf, f.temp[fo],
+                                                        f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o, mo,
+                                                        (size_t)mon->nmonths * N);
+    else
+      vertical_cell<R>(c, s, gam, canopy, soil, gsnow, st.snow_band + i, N, days, status, psum, laf, laf,
+                       R(f.prec[fo]) * pf, f.temp[fo], f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o);
     const size_t ri = (size_t)(d % ring.ring_days) * N + i;
     ring.rs[ri] = o.rs;
     ring.gwr[ri] = o.gwr;
@@ -273,18 +297,21 @@ __device__ __forceinline__ void va_cell(const DevCellsT<R> &c, const DevStateT<R
 // the vertical state in registers, and leaves surface runoff and recharge in the
 // ring buffer.  Results equal the in-wavefront computation: the vertical balance of
 // such a cell reads nothing routing writes.
-template <class R, bool ENS>
+// OUT: the vertical balance's monthly output grids too (DevMonthly::vert, FP64 single member).
+template <class R, bool ENS, bool OUT = false>
 __global__ void __launch_bounds__(VaBounds<R, ENS>::threads, VaBounds<R, ENS>::min_blocks) k_vertical_ahead(DevCellsT<R> c, DevStateT<R> st, DevForcing f,
                                                         DevMembers mem, DevBalance b, DevRingT<R> ring, int doy0,
-                                                        int fday0, int ndays, int t_b, int t_e) {
+                                                        int fday0, int ndays, int t_b, int t_e, DevMonthly mon,
+                                                        int oday0) {
   const size_t N = (size_t)c.n * (ENS ? mem.members : 1);
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
-    va_cell<R, ENS>(c, st, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e, i, N);
+    va_cell<R, ENS>(c, st, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e, i, N, OUT ? &mon : nullptr, oday0);
 }
 
 // X: what each cell computes after its routing, bit 0 the water temperature,
 // bit 1 the water use, bit 2 (with bit 1) the water use of GLWD units' riparian
-// cells met by their outflow cell.
+// cells met by their outflow cell, bit 3 the vertical balance's monthly output
+// grids (FP64 single member, alone).
 template <class R, bool FUSED, bool ENS, bool VAW, int X>
 __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R, ENS, VAW>::min_blocks) k_pipeline(DevCellsT<R> c, DevStateT<R> st, DevVertT<R> v, DevForcing f,
                                                   DevMembers mem, DevBalance b, DevRingT<R> ring, DevSync sync,
@@ -294,6 +321,7 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
   constexpr bool WT = (X & 1) != 0;
   constexpr bool WU = (X & 2) != 0;
   constexpr bool GL = (X & 4) != 0;   // water use with GLWD units (aggrNUsGloLakResOpt = 1)
+  constexpr bool VO = (X & 8) != 0;   // the vertical balance's monthly output grids
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const size_t N = (size_t)n * M;
@@ -308,7 +336,8 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
       g = __shfl_sync(0xffffffffu, g, 0);
       if (g >= (unsigned)vw.nitems) break;
       const size_t i = (size_t)g * 32 + lane;
-      if (i < N) va_cell<R, ENS>(c, st, f, mem, b, ring, doy0, fday0, ndays, vw.t_b, vw.t_e, i, N);
+      if (i < N) va_cell<R, ENS>(c, st, f, mem, b, ring, doy0, fday0, ndays, vw.t_b, vw.t_e, i, N, VO ? &mon : nullptr,
+                                 oday0);
     }
     return;
   }
@@ -403,8 +432,9 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
               gam *= R(mem.gamma_factor[mm]);
             }
             const int started = st.laf_started[si];
+            double *mo = VO ? vert_month(mon, oday0 + d, si, N) : nullptr;
             vertical_at<R>(c, st, N, s, si, doy, Pin, gam, f.temp[fo], f.swrad[fo], laf,
-                           started == 1 ? laf_prev : laf, o);   // daily.cpp:159-169
+                           started == 1 ? laf_prev : laf, o, mo, (size_t)mon.nmonths * N);   // daily.cpp:159-169
           } else {
             o.rs = v.rs[s]; o.gwr = v.gwr[s]; o.transfer = v.transfer[s]; o.owp = v.owp[s]; o.owpet = v.owpet[s];
             o.land_in = v.land_in[s]; o.land_evap = v.land_evap[s]; o.land_leak = v.land_leak[s];
@@ -482,9 +512,11 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
             if (mi >= 0 && mi < mon.nmonths) {
               const size_t k = (size_t)mi * N + si;
               const double q = (double)tv;
-              mon.river_avail[k] += q;
-              mon.min_avail[k] = fmin(mon.min_avail[k], q);
-              mon.max_avail[k] = fmax(mon.max_avail[k], q);
+              if (!(fl & F_SINK)) {   // outside inland sinks (routing.cpp:4010-4037)
+                mon.river_avail[k] += q;
+                mon.min_avail[k] = fmin(mon.min_avail[k], q);
+                mon.max_avail[k] = fmax(mon.max_avail[k], q);
+              }
               mon.storage[k] += (double)rs.gw + (double)rs.river + (double)rs.loclake + (double)rs.locwetl +
                                 (double)rs.glolake + (double)rs.glowetl + (double)rs.res;
               // CellRunoff (routing.cpp:3933-3939): in inland sinks the transported
@@ -668,11 +700,17 @@ cudaError_t launch_vertical(const DevCellsT<R> &c, const DevStateT<R> &s, const 
 template <class R>
 cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, const DevForcing &f,
                                   const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring, int doy0,
-                                  int fday0, int ndays, int t_b, int t_e, int blocks, int threads, cudaStream_t st) {
+                                  int fday0, int ndays, int t_b, int t_e, int blocks, int threads, cudaStream_t st,
+                                  const DevMonthly &mon, int oday0) {
   if (mem.members > 1)
-    k_vertical_ahead<R, true><<<blocks, threads, 0, st>>>(c, s, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e);
+    k_vertical_ahead<R, true><<<blocks, threads, 0, st>>>(c, s, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e, mon,
+                                                          oday0);
+  else if (mon.vert && std::is_same<R, double>::value)
+    k_vertical_ahead<R, false, true><<<blocks, threads, 0, st>>>(c, s, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e,
+                                                                 mon, oday0);
   else
-    k_vertical_ahead<R, false><<<blocks, threads, 0, st>>>(c, s, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e);
+    k_vertical_ahead<R, false><<<blocks, threads, 0, st>>>(c, s, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e, mon,
+                                                           oday0);
   return cudaGetLastError();
 }
 
@@ -684,8 +722,13 @@ static const void *pipeline_fn_x(bool fused, bool vaw) {
 }
 
 template <class R>
-static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false, bool gl = false) {
+static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false, bool gl = false,
+                               bool vo = false) {
   if (gl && (ens || wt || !wu || !std::is_same<R, double>::value)) return nullptr;   // GLWD units: FP64, one member
+  if (vo) {   // the vertical balance's monthly output grids: FP64, one member, alone
+    if (ens || wt || wu || !std::is_same<R, double>::value) return nullptr;
+    return pipeline_fn_x<R, 8>(fused, vaw);
+  }
   if (ens) return wt ? nullptr
                      : (wu ? (const void *)k_pipeline<R, true, true, false, 2> : (const void *)k_pipeline<R, true, true, false, 0>);
   if constexpr (std::is_same<R, double>::value) {   // FP64 single member only
@@ -747,7 +790,8 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
                   (void *)&oday0, (void *)&ndays, (void *)&t_b, (void *)&t_e, (void *)&cell_warps,
                   (void *)&idle_warp, (void *)&mon, (void *)&vwk, (void *)&wtp, (void *)&wu};
   const bool ens = mem.members > 1;
-  const void *fn = pipeline_fn<R>(fused, ens, vaw, wtp.enabled != 0, wu.enabled != 0, wu.enabled && wu.glwd);
+  const void *fn = pipeline_fn<R>(fused, ens, vaw, wtp.enabled != 0, wu.enabled != 0, wu.enabled && wu.glwd,
+                                  mon.vert != nullptr);
   if (!fn) return cudaErrorInvalidConfiguration;
   if (vaw) threads += 32 * vw.warps;
   // cooperative (all blocks resident, or the launch fails) through the launch
@@ -796,7 +840,8 @@ cudaError_t launch_balance_sum(const DevCellsT<R> &c, const DevStateT<R> &s, int
                                           cudaStream_t);                                                          \
   template cudaError_t launch_vertical_ahead<R>(const DevCellsT<R> &, const DevStateT<R> &, const DevForcing &,   \
                                                 const DevMembers &, const DevBalance &, const DevRingT<R> &, int,  \
-                                                int, int, int, int, int, int, cudaStream_t);                       \
+                                                int, int, int, int, int, int, cudaStream_t, const DevMonthly &,   \
+                                                int);                                                              \
   template cudaError_t launch_volume<R>(const DevCellsT<R> &, const DevStateT<R> &, int, double *, cudaStream_t); \
   template cudaError_t launch_balance_sum<R>(const DevCellsT<R> &, const DevStateT<R> &, int, const DevBalance &,  \
                                              const double *, double *, int *, cudaStream_t);

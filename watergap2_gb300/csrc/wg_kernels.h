@@ -62,7 +62,8 @@ cudaError_t launch_fill(double *p, size_t n, double v, cudaStream_t st);
 template <class R>
 cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, const DevForcing &f,
                                   const DevMembers &mem, const DevBalance &b, const DevRingT<R> &ring, int doy0,
-                                  int fday0, int ndays, int t_b, int t_e, int blocks, int threads, cudaStream_t st);
+                                  int fday0, int ndays, int t_b, int t_e, int blocks, int threads, cudaStream_t st,
+                                  const DevMonthly &mon, int oday0);
 template <class R>
 cudaError_t launch_volume(const DevCellsT<R> &c, const DevStateT<R> &s, int M, double *vol, cudaStream_t st);
 template <class R>

@@ -185,11 +185,13 @@ __device__ __forceinline__ R lai_nogrowing(int &days, int init, int &status, R l
 //   canopy ...  : the cell's state, read and written through references
 //   band        : the cell's snow bands, band[e * bstride]
 //   Pin         : precipitation (times a member's factor in an ensemble)
-template <class R>
+//   OUT, mo, mos: the monthly output grids (FP64): the cell's entry of the day's
+//               month of field k at mo[k * mos] (DevMonthly::vert)
+template <class R, bool OUT = false>
 __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R gamma_soil, R &canopy, R &soil,
                                               R &gsnow, R *band, size_t bstride, int &days, int &status, R &psum,
                                               R landAreaFrac, R prevLAF, R Pin, float Tf, float SWf, R ext_rad,
-                                              R inv_s0, VOut<R> &o) {
+                                              R inv_s0, VOut<R> &o, double *mo = nullptr, size_t mos = 0) {
   typedef M<R> m;
   const int B = c.nband;
   const R invB = c.invB;
@@ -246,6 +248,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   const bool rescale = !cmp::is_one(ratio);
 
   // interception (daily.cpp:825-895)
+  [[maybe_unused]] R out_maxcs = R(0);   // max_canopy_storage, 0 without leaves (daily.cpp:789, 847)
   if (!land) {
     transfer = canopy;
     canopy = R(0);
@@ -255,6 +258,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
     initialStorage = canopy;
     if (cmp::gt_c(dailyLai, R(0.00001))) {
       const R maxcs = c.mcwh[s] * dailyLai;
+      if constexpr (OUT) out_maxcs = maxcs;
       const R deficiency = maxcs - canopy;
       if (cmp::lt(dailyPrec, deficiency)) {
         canopy += dailyPrec;
@@ -288,6 +292,9 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   // rounding of temp_elev never moves a band's precipitation between snow and rain.
   constexpr bool fp32 = sizeof(R) == 4;
   R snowChange = R(0), gs = R(0);
+  // the monthly outputs' band sums: snowfall and rainfall above the canopy, melt,
+  // snow-covered bands (daily.cpp:983, 998, 1032-1041)
+  [[maybe_unused]] R out_snowfall = R(0), out_rainfall = R(0), out_melt = R(0), out_cover = R(0);
   bool above0 = cmp::gt(R(0), c.t_snowfz[s]);   // band 0 above freezing: the soil runs (daily.cpp:1076)
   int thresh = 0;
   const R t_snowfz = c.t_snowfz[s], t_snowmt = c.t_snowmt[s], ddf_m = c.ddf_m[s];
@@ -301,6 +308,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
       // the band's arithmetic and store
       if (e == 0) above0 = true;
       effPrec += prec_to_soil;
+      if constexpr (OUT) out_rainfall += dailyPrec;
       continue;
     }
     if (!land) {
@@ -354,6 +362,12 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
       if (e == 0) above0 = !snowfall;
       gs += sb;
       effPrec += effBefore + melt;
+      if constexpr (OUT) {
+        if (snowfall) out_snowfall += dailyPrec;
+        else out_rainfall += dailyPrec;
+        out_melt += melt;
+        if (cmp::gt0(sb)) out_cover += R(1);
+      }
     }
     band[e * bstride] = sb;
   }
@@ -448,6 +462,59 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   o.land_in = dailyPrec;
   o.land_evap = cellAET;
   o.land_leak = leak;
+  if (OUT && mo) {
+    // the monthly output grids (daily.cpp:1281-1386, grid_store 2): sums over the
+    // month's days; radiation in W/m2 (lat_heat / 0.0864 per mm/day), land terms
+    // weighted by the day's land share of the continental area; the storages at
+    // the month's end (grid_store_TypeForStorages 0)
+    const double conv = (double)lat_heat / 0.0864;
+    const double ns = (double)solar_rad * (1. - (double)albedo);
+    mo[0] += (double)dailyPrec;
+    mo[mos] += (double)T;
+    mo[2 * mos] += (double)ext_rad * conv;
+    mo[3 * mos] += ((double)solar_rad - ns) * conv;
+    mo[4 * mos] += (double)solar_rad * conv;
+    mo[5 * mos] += ns * conv;
+    mo[6 * mos] += (double)net_lw * conv;
+    mo[7 * mos] += (double)net_rad * conv;
+    mo[8 * mos] += (double)owPET;
+    mo[9 * mos] += (double)dailyPET;
+    const double cf = (double)c.contfreq[s];
+    if (cf < 0.000001) {   // no continental area (geo.cpp:52-60): the land terms are zero
+      for (int k = 10; k < 29; ++k) mo[(size_t)k * mos] = 0.;
+    } else {
+      const double lf = (double)landAreaFrac;
+      double snowfall = (double)out_snowfall, rainfall = (double)out_rainfall, melt = (double)out_melt;
+      if (land) {
+        snowfall = snowfall * (double)invB;
+        rainfall = rainfall * (double)invB;
+        melt = melt * (double)invB;
+      }
+      mo[10 * mos] += (double)dailyAET * lf / cf;
+      mo[11 * mos] += (double)cellAET * lf / cf;
+      mo[12 * mos] += ((double)dailyAET + (double)canopyEvapo + (double)snowEvapo) * lf / cf;
+      mo[13 * mos] += (double)dailyLai;
+      mo[14 * mos] += (double)albedo * (lf / 100.) + 0.08 * (1. - (lf / 100.));
+      mo[15 * mos] += (double)canopyEvapo * lf / cf;
+      mo[16 * mos] += (double)canopy * lf / cf;
+      mo[17 * mos] += (double)out_maxcs * lf / cf;
+      mo[18 * mos] += snowfall * lf / cf;
+      mo[19 * mos] += rainfall * lf / cf;
+      mo[20 * mos] += melt * lf / cf;
+      mo[21 * mos] += (double)snowEvapo * lf / cf;
+      mo[22 * mos] += (double)gsnow * lf / cf;
+      mo[23 * mos] += (double)out_cover * (double)invB * lf / cf;
+      mo[24 * mos] += (double)soil * lf / cf;
+      mo[25 * mos] += (double)total * lf / cf;
+      mo[26 * mos] += (double)immediate;
+      mo[27 * mos] += ((double)total - (double)gwr) * lf / cf;
+      mo[28 * mos] += (double)gwr * lf / cf;
+      const double a = (double)c.area[s];
+      mo[29 * mos] = (double)canopy * a / 1000000.0 * lf / 100.0;
+      mo[30 * mos] = (double)gsnow * a / 1000000.0 * lf / 100.0;
+      mo[31 * mos] = (double)soil * a / 1000000.0 * lf / 100.0;
+    }
+  }
 }
 
 template <class R>

@@ -38,7 +38,8 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_upload_forcing_unf", "wg_read_unf", "wg_monthly_outputs", "wg_get_monthly", "wg_set_step_sync",
            "wg_upload_water_use", "wg_set_water_use_inputs", "wg_get_water_use", "wg_set_water_use",
            "wg_model_options_default", "wg_get_member_discharge", "wg_set_deferred",
-           "wg_record_daily_storages", "wg_get_daily_storages", "wg_upload_forcing_cells")
+           "wg_record_daily_storages", "wg_get_daily_storages", "wg_upload_forcing_cells",
+           "wg_monthly_outputs_vertical")
 
 
 class WgError(RuntimeError):
@@ -138,6 +139,8 @@ def load_library(path: str = LIB_PATH):
     lib.wg_set_active_cells.argtypes = [vp, vp]
     lib.wg_upload_forcing_unf.argtypes = [vp, i32, i32, i32, i32, vp, vp, vp, i32]
     lib.wg_monthly_outputs.argtypes = [vp, i32, i32]
+    lib.wg_monthly_outputs_vertical.argtypes = [vp, i32]
+    lib.wg_monthly_outputs_vertical.restype = i32
     lib.wg_set_step_sync.argtypes = [vp, i32]
     lib.wg_get_monthly.argtypes = [vp, i32, i32, i32, vp]
     lib.wg_read_unf.argtypes = [ctypes.c_char_p, vp, i64]
@@ -484,11 +487,22 @@ class Model:
         self._check(self.lib.wg_set_step_sync(self.h, int(flags)), "set_step_sync")
 
     MONTHLY = {"river_avail": 0, "storage": 1, "min_avail": 2, "max_avail": 3, "cell_runoff": 4, "velocity": 5}
+    # the vertical balance's monthly grids (wg_monthly_outputs_vertical), which = 6 + index
+    MONTHLY_VERTICAL = ["prec", "temp", "ext_rad", "short_up_rad", "short_down_rad", "net_short_rad", "net_long_rad",
+                        "net_rad", "open_water_pet", "pet", "aet", "land_aet", "land_aet_uncorr", "lai", "albedo",
+                        "interception", "canopy_wc", "max_canopy_wc", "snowfall", "rainfall", "snowmelt",
+                        "snow_evap", "swe", "snow_cover", "soil_wc", "runoff", "urban_runoff", "surface_runoff",
+                        "gw_recharge", "canopy_storage", "snow_storage", "soil_storage"]
+    MONTHLY.update({k: 6 + i for i, k in enumerate(MONTHLY_VERTICAL)})
 
     def monthly_outputs(self, nmonths: int, doy_day0: int = 1):
         """wg_monthly_outputs: accumulate monthly aggregates for nmonths months."""
         self._check(self.lib.wg_monthly_outputs(self.h, int(nmonths), int(doy_day0)), "monthly_outputs")
         self.nmonths = int(nmonths)
+
+    def monthly_outputs_vertical(self, enable: bool = True):
+        """wg_monthly_outputs_vertical: the vertical balance's monthly grids too."""
+        self._check(self.lib.wg_monthly_outputs_vertical(self.h, int(bool(enable))), "monthly_outputs_vertical")
 
     def monthly(self, name: str, m0: int = 0, nm: int | None = None) -> np.ndarray:
         """[nm, ncell] (or [nm, ncell, members]) monthly aggregate, cell order."""
