@@ -315,6 +315,43 @@ def run_water_use(region, P, T, S, stream, local):
     return out
 
 
+def run_outputs(region, P, T, S, stream, local):
+    """The global grid with the monthly output grids against the plain run:
+    routing's grids only (wg_monthly_outputs: river availability with its
+    minimum and maximum, cell runoff, velocity, storage), and routing's with the
+    vertical balance's 32 grids (wg_monthly_outputs_vertical; the reference's
+    grid_store = 2 sums).  Four years in one wavefront, the fourth timed with
+    CUDA events (the first three fill the wavefront)."""
+    import torch
+    from watergap2_gb300.gpu import Model
+    nd = 4 * DAYS_PER_STEP
+    out = {}
+    for name, grids in (("routing_grids", 1), ("all_grids", 2), ("without", 0)):
+        m = Model(region, max_days=nd, device=local, stream=stream.cuda_stream, days_per_step=WAVEFRONT_DAYS)
+        if grids:
+            m.monthly_outputs(48, doy_day0=1)
+            m.monthly_outputs_vertical(grids == 2)
+        m.upload_forcing(0, P[:nd], T[:nd], S[:nd])
+        assert 3 * WSTEPS_PER_YEAR >= m.num_levels - 1
+        m.run_steps(1, 0, nd, 0, 3 * WSTEPS_PER_YEAR)
+        m.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        m.run_steps(1, 0, nd, 3 * WSTEPS_PER_YEAR, 4 * WSTEPS_PER_YEAR)
+        e1.record(stream)
+        m.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[name] = {"cell_days_per_s": region.ncell * DAYS_PER_STEP / (ms / 1000.0), "ms_per_year": ms}
+        if grids == 2:   # a sanity figure: the first year's mean monthly precipitation sum [mm]
+            # (every cell has finished the first year; the wavefront's upstream
+            # cells have not finished the fourth when the timed steps end)
+            out[name]["mean_monthly_prec_mm"] = float(np.mean(m.monthly("prec", 0, 12)))
+        del m
+    for name in ("routing_grids", "all_grids"):
+        out[name]["cost_vs_plain"] = out["without"]["cell_days_per_s"] / out[name]["cell_days_per_s"]
+    return out
+
+
 # algorithmic HBM bytes per member-cell-day of the ensemble (FP32 state, the
 # forcing and static parameters shared by the members of one cell in a block):
 # per member state r+w 72, perturbed gamma 4, outputs 8; per block of members
@@ -610,6 +647,9 @@ def run_gpu(args, rank, world):
     water_use = None
     if rank == 0 and not os.environ.get("WG_BENCH_NO_WUSE"):
         water_use = run_water_use(region, P, T, S, stream, local)
+    outputs = None
+    if rank == 0 and not os.environ.get("WG_BENCH_NO_OUTPUTS"):
+        outputs = run_outputs(region, P, T, S, stream, local)
     # the other configurations, bounded: one simulated year of the 5-arc-minute
     # grid in both precisions, and the learned-calibration workload
     fine = None
@@ -693,6 +733,7 @@ def run_gpu(args, rank, world):
         "ensemble": ensemble,
         "water_temp": water_temp,
         "water_use": water_use,
+        "outputs": outputs,
         "fine_5min": fine,
         "calibration": calibration,
         "cpu_baseline": {"value": cpu_val, "unit": "cell-days/s", "cores": cpu_threads, "kind": "port",
@@ -705,7 +746,7 @@ def run_gpu(args, rank, world):
         dist.destroy_process_group()
 
 
-def run_profile_case(steps: int = 24, warm_steps: int = 200):
+def run_profile_case(steps: int = 24, warm_steps: int = 200, outputs: bool = False):
     """A short, self-contained case for ncu: the global grid as the bench runs it
     (WAVEFRONT_DAYS days per wavefront step, default chunks of 4 steps, vertical
     overlap), a warm-up call of warm_steps steps that fills the day-pipelined
@@ -715,13 +756,18 @@ def run_profile_case(steps: int = 24, warm_steps: int = 200):
     with its vertical-ahead launch (51) and wavefront launches that carry the
     next chunk's vertical balance (52, 53, ...).  One kernel per capture:
       ncu --set full --clock-control none -k regex:k_pipeline -s 50 -c 2 -o prof python bench.py --profile
-      ncu --set full --clock-control none -k regex:k_vertical_ahead -s 1 -c 1 -o prof python bench.py --profile"""
+      ncu --set full --clock-control none -k regex:k_vertical_ahead -s 1 -c 1 -o prof python bench.py --profile
+    With outputs (--profile-outputs) the run fills routing's and the vertical
+    balance's monthly grids (the same launches, their output variants)."""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global()
     nd = (warm_steps + steps) * WAVEFRONT_DAYS
     P, T, S = sy.forcing(region, nd, seed=2, doy0=1)
     m = Model(region, max_days=nd, days_per_step=WAVEFRONT_DAYS)
+    if outputs:
+        m.monthly_outputs(nd // 28 + 1, doy_day0=1)
+        m.monthly_outputs_vertical(True)
     m.upload_forcing(0, P, T, S)
     m.run_steps(1, 0, nd, 0, warm_steps)
     m.synchronize()
@@ -731,7 +777,8 @@ def run_profile_case(steps: int = 24, warm_steps: int = 200):
     dt = time.perf_counter() - t0
     m.run_steps(1, 0, nd, warm_steps + steps, m.num_steps(nd))
     m.synchronize()
-    print(json.dumps({"profile_case": "global grid, steady-state wavefront", "ncell": region.ncell, "steps": steps,
+    print(json.dumps({"profile_case": "global grid, steady-state wavefront" + (", monthly grids" if outputs else ""),
+                      "ncell": region.ncell, "steps": steps,
                       "days_per_step": WAVEFRONT_DAYS, "seconds": dt,
                       "cell_days_per_s": region.ncell * steps * WAVEFRONT_DAYS / dt, "chunk_steps": m.chunk_steps(),
                       "vertical_overlap_warps": m.vertical_overlap(), "vinline_fraction": m.vinline_fraction()}))
@@ -936,6 +983,8 @@ def main():
     ap.add_argument("--profile-ensemble", action="store_true", help="run the short ensemble ncu case and exit")
     ap.add_argument("--profile-wtemp", action="store_true", help="run the short water-temperature ncu case and exit")
     ap.add_argument("--profile-wuse", action="store_true", help="run the short water-use ncu case and exit")
+    ap.add_argument("--profile-outputs", action="store_true",
+                    help="run the short ncu case with the monthly output grids and exit")
     ap.add_argument("--fine", action="store_true",
                     help="the 5-arc-minute mixed-precision run: FP32 vs FP64 errors at every outlet")
     ap.add_argument("--calibration", action="store_true",
@@ -947,8 +996,8 @@ def main():
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    if args.profile:
-        run_profile_case()
+    if args.profile or args.profile_outputs:
+        run_profile_case(outputs=args.profile_outputs)
         return
     if args.calibration:
         run_calibration()

@@ -90,6 +90,10 @@ class Context {
   void monthly_outputs(int nmonths, int doy_day0) {
     check(wg_monthly_outputs(ctx_, nmonths, doy_day0), "wg_monthly_outputs");
   }
+  // the vertical balance's 32 monthly grids as well (which 6..37 of monthly())
+  void monthly_outputs_vertical(bool enable) {
+    check(wg_monthly_outputs_vertical(ctx_, enable ? 1 : 0), "wg_monthly_outputs_vertical");
+  }
   void monthly(int which, int m0, int nm, double *out) {
     check(wg_get_monthly(ctx_, which, m0, nm, out), "wg_get_monthly");
   }

@@ -236,6 +236,42 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   const R owPET = cmp::le0(ow_net_rad) ? R(0) : apet * ow_net_rad;
   o.owp = dailyPrec;
   o.owpet = owPET;
+  // the monthly output grids (daily.cpp:1281-1386, grid_store 2): sums over the
+  // month's days, each term filed as soon as it is known so that none stays live
+  // to the end of the cell-day.  Radiation in W/m2 (lat_heat / 0.0864 per
+  // mm/day); the land terms (fields 10-28) weighted by the day's land share of
+  // the continental area, zero without continental area (geo.cpp:52-60); the
+  // storages at the month's end (grid_store_TypeForStorages 0).  The reference
+  // divides each land term by contfreq; here one refined reciprocal of contfreq
+  // per cell-day and products with constants give the same values to a few ulp
+  // (a correctly rounded FP64 division costs about ten FP64-pipe operations, and
+  // the FP64 pipe bounds the step).
+  [[maybe_unused]] bool mcont = false;   // the cell has continental area
+  [[maybe_unused]] double mw = 0.;       // landAreaFrac / contfreq
+  if constexpr (OUT) {
+    if (mo) {
+      const double conv = (double)lat_heat * (1.0 / 0.0864);
+      const double ns = (double)solar_rad * (1. - (double)albedo);
+      mo[0] += (double)dailyPrec;
+      mo[mos] += (double)T;
+      mo[2 * mos] += (double)ext_rad * conv;
+      mo[3 * mos] += ((double)solar_rad - ns) * conv;
+      mo[4 * mos] += (double)solar_rad * conv;
+      mo[5 * mos] += ns * conv;
+      mo[6 * mos] += (double)net_lw * conv;
+      mo[7 * mos] += (double)net_rad * conv;
+      mo[8 * mos] += (double)owPET;
+      mo[9 * mos] += (double)dailyPET;
+      const double cf = (double)c.contfreq[s];
+      mcont = !(cf < 0.000001);
+      if (mcont) {
+        const double lf = (double)landAreaFrac, lf100 = lf * 0.01;
+        mw = lf * fm::rcp_pos(cf);
+        mo[13 * mos] += (double)dailyLai;
+        mo[14 * mos] += (double)albedo * lf100 + 0.08 * (1. - lf100);
+      }
+    }
+  }
 
   R lsc = R(0), initialStorage = R(0);
   R canopyEvapo = R(0), prec_to_soil = R(0), soilPET = R(0), snowEvapo = R(0), effPrec = R(0);
@@ -284,6 +320,13 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
     lsc += canopy - initialStorage;
   }
   if (cmp::lt0(soilPET)) soilPET = R(0);
+  if constexpr (OUT) {
+    if (mo && mcont) {   // the canopy's terms: its state does not change after this
+      mo[15 * mos] += (double)canopyEvapo * mw;
+      mo[16 * mos] += (double)canopy * mw;
+      mo[17 * mos] += (double)out_maxcs * mw;
+    }
+  }
 
   // snow in elevation bands (daily.cpp:897-1062).  Whether a band gets snowfall
   // (temp_elev <= P_T_SNOWFZ, daily.cpp:982) decides where the day's precipitation
@@ -292,9 +335,11 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   // rounding of temp_elev never moves a band's precipitation between snow and rain.
   constexpr bool fp32 = sizeof(R) == 4;
   R snowChange = R(0), gs = R(0);
-  // the monthly outputs' band sums: snowfall and rainfall above the canopy, melt,
-  // snow-covered bands (daily.cpp:983, 998, 1032-1041)
-  [[maybe_unused]] R out_snowfall = R(0), out_rainfall = R(0), out_melt = R(0), out_cover = R(0);
+  // the monthly outputs' band sums (daily.cpp:983, 998, 1032-1041): the bands with
+  // snowfall and with rain (each adds the day's precipitation above the canopy;
+  // counted on the integer pipe and multiplied once), melt, snow-covered bands
+  [[maybe_unused]] int n_snowfall = 0, n_rainfall = 0, n_cover = 0;
+  [[maybe_unused]] R out_melt = R(0);
   bool above0 = cmp::gt(R(0), c.t_snowfz[s]);   // band 0 above freezing: the soil runs (daily.cpp:1076)
   int thresh = 0;
   const R t_snowfz = c.t_snowfz[s], t_snowmt = c.t_snowmt[s], ddf_m = c.ddf_m[s];
@@ -308,7 +353,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
       // the band's arithmetic and store
       if (e == 0) above0 = true;
       effPrec += prec_to_soil;
-      if constexpr (OUT) out_rainfall += dailyPrec;
+      if constexpr (OUT) ++n_rainfall;
       continue;
     }
     if (!land) {
@@ -363,10 +408,10 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
       gs += sb;
       effPrec += effBefore + melt;
       if constexpr (OUT) {
-        if (snowfall) out_snowfall += dailyPrec;
-        else out_rainfall += dailyPrec;
+        if (snowfall) ++n_snowfall;
+        else ++n_rainfall;
         out_melt += melt;
-        if (cmp::gt0(sb)) out_cover += R(1);
+        if (cmp::gt0(sb)) ++n_cover;
       }
     }
     band[e * bstride] = sb;
@@ -379,6 +424,18 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
     lsc += snowChange;
   }
   gsnow = gs;
+  if constexpr (OUT) {
+    if (mo && mcont) {   // the snow's terms
+      // per band of the cell's land (1 / bands), without land the sums are 0
+      const double pb = (double)dailyPrec * (double)invB * mw, bw = (double)invB * mw;
+      mo[18 * mos] += (double)n_snowfall * pb;
+      mo[19 * mos] += (double)n_rainfall * pb;
+      mo[20 * mos] += (double)out_melt * bw;
+      mo[21 * mos] += (double)snowEvapo * mw;
+      mo[22 * mos] += (double)gsnow * mw;
+      mo[23 * mos] += (double)n_cover * bw;
+    }
+  }
 
   // immediate runoff from built-up area (daily.cpp:1068-1071)
   if (cmp::gt0(c.built_up[s])) {
@@ -462,57 +519,22 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   o.land_in = dailyPrec;
   o.land_evap = cellAET;
   o.land_leak = leak;
-  if (OUT && mo) {
-    // the monthly output grids (daily.cpp:1281-1386, grid_store 2): sums over the
-    // month's days; radiation in W/m2 (lat_heat / 0.0864 per mm/day), land terms
-    // weighted by the day's land share of the continental area; the storages at
-    // the month's end (grid_store_TypeForStorages 0)
-    const double conv = (double)lat_heat / 0.0864;
-    const double ns = (double)solar_rad * (1. - (double)albedo);
-    mo[0] += (double)dailyPrec;
-    mo[mos] += (double)T;
-    mo[2 * mos] += (double)ext_rad * conv;
-    mo[3 * mos] += ((double)solar_rad - ns) * conv;
-    mo[4 * mos] += (double)solar_rad * conv;
-    mo[5 * mos] += ns * conv;
-    mo[6 * mos] += (double)net_lw * conv;
-    mo[7 * mos] += (double)net_rad * conv;
-    mo[8 * mos] += (double)owPET;
-    mo[9 * mos] += (double)dailyPET;
-    const double cf = (double)c.contfreq[s];
-    if (cf < 0.000001) {   // no continental area (geo.cpp:52-60): the land terms are zero
+  if constexpr (OUT) {
+    if (mo && !mcont) {
       for (int k = 10; k < 29; ++k) mo[(size_t)k * mos] = 0.;
-    } else {
-      const double lf = (double)landAreaFrac;
-      double snowfall = (double)out_snowfall, rainfall = (double)out_rainfall, melt = (double)out_melt;
-      if (land) {
-        snowfall = snowfall * (double)invB;
-        rainfall = rainfall * (double)invB;
-        melt = melt * (double)invB;
-      }
-      mo[10 * mos] += (double)dailyAET * lf / cf;
-      mo[11 * mos] += (double)cellAET * lf / cf;
-      mo[12 * mos] += ((double)dailyAET + (double)canopyEvapo + (double)snowEvapo) * lf / cf;
-      mo[13 * mos] += (double)dailyLai;
-      mo[14 * mos] += (double)albedo * (lf / 100.) + 0.08 * (1. - (lf / 100.));
-      mo[15 * mos] += (double)canopyEvapo * lf / cf;
-      mo[16 * mos] += (double)canopy * lf / cf;
-      mo[17 * mos] += (double)out_maxcs * lf / cf;
-      mo[18 * mos] += snowfall * lf / cf;
-      mo[19 * mos] += rainfall * lf / cf;
-      mo[20 * mos] += melt * lf / cf;
-      mo[21 * mos] += (double)snowEvapo * lf / cf;
-      mo[22 * mos] += (double)gsnow * lf / cf;
-      mo[23 * mos] += (double)out_cover * (double)invB * lf / cf;
-      mo[24 * mos] += (double)soil * lf / cf;
-      mo[25 * mos] += (double)total * lf / cf;
+    } else if (mo) {   // the soil's terms and the storages at the month's end
+      mo[10 * mos] += (double)dailyAET * mw;
+      mo[11 * mos] += (double)cellAET * mw;
+      mo[12 * mos] += ((double)dailyAET + (double)canopyEvapo + (double)snowEvapo) * mw;
+      mo[24 * mos] += (double)soil * mw;
+      mo[25 * mos] += (double)total * mw;
       mo[26 * mos] += (double)immediate;
-      mo[27 * mos] += ((double)total - (double)gwr) * lf / cf;
-      mo[28 * mos] += (double)gwr * lf / cf;
-      const double a = (double)c.area[s];
-      mo[29 * mos] = (double)canopy * a / 1000000.0 * lf / 100.0;
-      mo[30 * mos] = (double)gsnow * a / 1000000.0 * lf / 100.0;
-      mo[31 * mos] = (double)soil * a / 1000000.0 * lf / 100.0;
+      mo[27 * mos] += ((double)total - (double)gwr) * mw;
+      mo[28 * mos] += (double)gwr * mw;
+      const double a = (double)c.area[s] * (double)landAreaFrac * 1e-8;   // area [km2] / 1e6 * landAreaFrac / 100
+      mo[29 * mos] = (double)canopy * a;
+      mo[30 * mos] = (double)gsnow * a;
+      mo[31 * mos] = (double)soil * a;
     }
   }
 }
