@@ -66,7 +66,14 @@ typedef struct wg_region {
   const double *lct_albedo, *lct_albedo_snow, *lct_ddf;        /* [18] LCT_22.DAT    */
   const float *lct_lai_a, *lct_lai_b;                           /* [18] laiClass      */
   const int16_t *lct_initial_days;                              /* [18] LAI_22.DAT    */
-  const double *area_km2, *lat_deg, *contfreq;
+  const double *area_km2, *lat_deg;
+  const double *contfreq;   /* GCONTFREQ [%] as read; the library raises it to the cell's
+                               local-lake + global-lake + reservoir share as geo.init does
+                               (geo.cpp:25-45), and cells whose share stays below 1e-6 %
+                               (the Caspian Sea in the standard land mask) run neither the
+                               vertical balance nor routing (integrateWGHM.cpp:770-780,
+                               routing.cpp:1878-4518): their storages stay, their outflow
+                               is 0, their inflow leaves the system                     */
   const uint8_t *lct;
   const float *built_up, *smax, *lai_max, *gw_factor;
   const int16_t *rg_max;
@@ -77,7 +84,10 @@ typedef struct wg_region {
   const double *loc_lake, *loc_wetl, *glo_wetl, *glo_lake, *glo_res;   /* [%]         */
   const double *lake_area, *res_area, *stor_cap, *mean_outflow, *mean_demand;
   const int8_t *res_type, *start_month;
-  const double *river_length, *river_slope, *roughness, *bankfull;
+  const double *river_length;  /* G_riverLength as routing.init leaves it: the file's length
+                                  times the raised continental share / 100
+                                  (routing.cpp:476-482)                                 */
+  const double *river_slope, *roughness, *bankfull;
   const int32_t *downstream;   /* 0-based downstream cell, -1 at outlets and sinks   */
   const int32_t *rout_order;   /* reference routing order (G_routingCell - 1)          */
   const int32_t *glwd_unit;    /* G_glwdUnit (GLWDunits.UNF4, 0: none), or NULL; used with

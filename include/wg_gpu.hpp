@@ -180,6 +180,16 @@ class DropInCore {
  public:
   DropInCore(Context &c, const wg_region &r) : ctx(c), n(r.ncell), nband(r.nband), area(r.area_km2, r.area_km2 + r.ncell),
                                               contfreq(r.contfreq, r.contfreq + r.ncell) {
+    // the continental share as geo.init leaves it (geo.cpp:25-45): at least the
+    // share of local lakes, global lakes, local reservoirs (none) and reservoirs
+    for (int i = 0; i < n; ++i) {
+      double fw = 0.;
+      fw += r.loc_lake[i];
+      fw += r.glo_lake[i];
+      fw += 0.;
+      fw += r.glo_res[i];
+      if (fw > contfreq[i]) contfreq[i] = fw;
+    }
     ctx.check(wg_set_deferred(ctx.get(), 1), "wg_set_deferred");
     ctx.check(wg_record_daily_storages(ctx.get(), 1), "wg_record_daily_storages");
     canopy.resize(n); soil.resize(n); snow.resize(n); snow_band.resize((size_t)n * nband); laf.resize(n);

@@ -124,6 +124,18 @@ static double lai_nogrowing(int *days, short init, int *status, char lct, int ar
   }
 }
 
+/* The continental share as geo.init leaves it (geo.cpp:25-45): at least the cell's
+   share of local lakes, global lakes, local reservoirs (none here) and reservoirs,
+   summed in that order. */
+static double cont_share(const wgo_static *s, int n) {
+  double fw = 0.;
+  fw += s->loc_lake[n];
+  fw += s->glo_lake[n];
+  fw += 0.;
+  fw += s->glo_res[n];
+  return fw > s->contfreq[n] ? fw : s->contfreq[n];
+}
+
 int wgo_init_state(const wgo_static *s, wgo_state *st) {
   const int N = s->ncell, B = s->nband;
   for (int n = 0; n < N; n++) {
@@ -149,7 +161,7 @@ int wgo_init_state(const wgo_static *s, wgo_state *st) {
     st->fswb_next[n] = s->loc_lake[n] / 100. + s->loc_wetl[n] / 100. + s->glo_wetl[n] / 100.;
     st->laf_started[n] = 0;
     /* annualInit, first year (routing.cpp:1174-1205) */
-    double laf = (s->contfreq[n] - (s->glo_lake[n] + s->glo_wetl[n] + s->loc_lake[n] + s->loc_wetl[n] + s->glo_res[n]));
+    double laf = (cont_share(s, n) - (s->glo_lake[n] + s->glo_wetl[n] + s->loc_lake[n] + s->loc_wetl[n] + s->glo_res[n]));
     if (laf < 0.) laf = 0.;
     st->laf[n] = laf;
     st->laf_prev[n] = 0.;
@@ -815,7 +827,9 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
                     wgo_wt_io *wt, wgo_wu_io *wu) {
   const int N = s->ncell;
   if (s->nband <= 0 || N <= 0) return -1;
-  vout *vo = (vout *)malloc(sizeof(vout) * (size_t)N);
+  /* zero: the terms of cells without continental area, which the vertical pass
+     never writes (the reference's zero-initialised grids, daily.cpp:1670-1676) */
+  vout *vo = (vout *)calloc((size_t)N, sizeof(vout));
   double *inflow_up = (double *)calloc((size_t)N, sizeof(double));
   double *bw = (double *)malloc(sizeof(double) * (size_t)N);
   if (!vo || !inflow_up || !bw) return -2;
@@ -844,10 +858,13 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
     int month = 0;
     while (month < 11 && day >= first_day_in_month[month + 1]) month++;
     const float *P = prec + (size_t)d * N, *T = temp + (size_t)d * N, *SW = swrad + (size_t)d * N;
-    /* vertical pass: the reference's OpenMP cell loop (integrateWGHM.cpp:767-783) */
+    /* vertical pass: the reference's OpenMP cell loop over continental cells
+       (integrateWGHM.cpp:767-783; G_contcell, geo.cpp:50-60) */
     const double w0 = wall_now();
 #pragma omp parallel for schedule(static) if (nthreads > 1)
-    for (int n = 0; n < N; n++) vertical_cell(s, st, n, day, (double)P[n], (double)T[n], (double)SW[n], &vo[n]);
+    for (int n = 0; n < N; n++)
+      if (!(cont_share(s, n) < WGO_LIMIT_CONTCELL_PCT))
+        vertical_cell(s, st, n, day, (double)P[n], (double)T[n], (double)SW[n], &vo[n]);
     const double w1 = wall_now();
     g_time_vertical += w1 - w0;
 
@@ -864,6 +881,16 @@ static int run_impl(const wgo_static *s, wgo_state *st, int doy0, int ndays, con
     for (int n = 0; n < N; n++) inflow_up[n] = 0.;
     for (int rc = 0; rc < N; rc++) {
       const int n = s->rout_order[rc];
+      if (cont_share(s, n) < WGO_LIMIT_CONTCELL_PCT) {
+        /* only continental cells are routed (routing.cpp:1878-4518): the storages
+           stay, nothing flows on, the inflow stays behind in G_riverInflow and so
+           leaves the system (a negative leak); the water temperature keeps its
+           start value */
+        if (discharge) discharge[(size_t)d * N + n] = 0.;
+        if (wt && wt->daily_temp) wt->daily_temp[(size_t)d * N + n] = wt->temp[n];
+        if (balance) b_leak -= inflow_up[n];
+        continue;
+      }
       const double cellArea = s->area_km2[n];
       const double cfa = PAR(s, WGO_P_CFA, n);
       const double laf = st->laf[n];

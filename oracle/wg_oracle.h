@@ -31,6 +31,11 @@
 extern "C" {
 #endif
 
+/* A cell is continental when its continental share is at least this many per cent
+   (limit_contcell_pct, geo.h:32; geo.cpp:50-60); only continental cells run the
+   vertical balance (integrateWGHM.cpp:770-780). */
+#define WGO_LIMIT_CONTCELL_PCT 0.000001
+
 /* Calibration parameters, in the order of eCalibParam (source/calib_param.h:72-101). */
 enum {
   WGO_P_GAMRUN_C = 0, WGO_P_CFA, WGO_P_CFS, WGO_M_ROOT_D, WGO_M_RIVRGH_C, WGO_P_LAK_D,

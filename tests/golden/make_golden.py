@@ -12,6 +12,7 @@ The water-temperature case (WT_CASES) adds longwave radiation, groundwater
 temperature and the reference's inflow-direction table to the inputs; the
 water-use case (WU_CASES) adds three years of monthly net abstractions.
 """
+import dataclasses
 import os
 import sys
 
@@ -40,6 +41,8 @@ CASES = {
                       150, 60, [75, 150]),
     # station correction (options.statcorrOpt = 1): outflow x P_CFS (routing.cpp:3929-3931)
     "swb_statcorr_120d": (lambda: statcorr_region(seed=22), 120, 150, [60, 120]),
+    # cells without continental area (G_contcell = 0, geo.cpp:50-60): no vertical balance
+    "swb_nocont_150d": (lambda: nocont_region(seed=23), 150, 100, [75, 150]),
 }
 
 
@@ -86,6 +89,34 @@ def _put_snapshots(region, res, extra):
         extra[f"s{i}_snow_band"] = b[:, :, 0].copy()
         for k, v in snap.items():
             extra[f"s{i}_{k}"] = v
+
+
+def nocont_region(seed=23):
+    """A region with every water-body type in which five cells have a continental
+    share below the reference's limit (1e-6 %), as the Caspian Sea's cells in the
+    standard land mask: two global lakes, a local wetland and a cell without water
+    bodies at 0 %, and one cell without water bodies at 5e-7 %.  The reference runs
+    no vertical balance in them (integrateWGHM.cpp:770-780)."""
+    region = sy.region_small_swb(seed=seed, block_at=(90, 260))
+    a = region.arrays
+    plain = (a["lake_area"] == 0) & (a["res_area"] == 0) & (a["loc_lake"] == 0) & (a["loc_wetl"] == 0) & \
+        (a["glo_wetl"] == 0)
+    pick = [np.nonzero(a["lake_area"] > 0)[0][:2], np.nonzero((a["loc_wetl"] > 0) & (a["lake_area"] == 0))[0][:1],
+            np.nonzero(plain)[0][:2]]
+    cf = a["contfreq"].copy()
+    cf[np.concatenate(pick[:2] + [pick[2][:1]])] = 0.0
+    cf[pick[2][1]] = float(np.float32(5e-7))   # the reference reads the share as float
+    arrays = dict(a)
+    arrays["contfreq"] = cf
+    # the river length scaled by the continental share as geo.init raises it to the
+    # lake and reservoir share (routing.cpp:476-482, geo.cpp:25-45)
+    share = np.maximum(cf, ((a["loc_lake"] + a["glo_lake"]) + 0.0) + a["glo_res"])
+    arrays["river_length"] = region.extras["river_length_file"] * (share / 100.)
+    out = dataclasses.replace(region, arrays=arrays)
+    for k in ("lct_tables", "extras"):
+        if k in region.__dict__:
+            out.__dict__[k] = region.__dict__[k]
+    return out
 
 
 def wtemp_region(seed=21):

@@ -156,6 +156,23 @@ def test_mass_balance_closes_every_cell():
     assert worst <= 1e-12, worst
 
 
+def test_mass_balance_closes_without_continental_area():
+    """Cells whose continental share is below the reference's limit run neither
+    the vertical balance nor routing; their inflow leaves the system as a
+    negative leak and the balance closes."""
+    from watergap2_gb300.region import load_npz
+    region, ex = load_npz(os.path.join(os.path.dirname(__file__), "golden", "swb_nocont_150d.npz"))
+    P, T, S = ex["P"], ex["T"], ex["S"]
+    m = _model(region, max_days=P.shape[0], record_balance=True)
+    s0 = m.balance()[0]
+    m.run(int(ex["doy0"]), P, T, S)
+    total, pin, evap, out, leak, worst = m.balance()
+    resid = (total - s0) - (pin - evap - out + leak)
+    assert leak < 0.
+    assert abs(resid) <= 1e-12 * max(total, pin), (resid, total, pin)
+    assert worst <= 1e-12, worst
+
+
 def test_split_steps_equal_one_launch():
     """A run split into several wg_run_steps calls (wavefront not drained between
     them) equals one wg_run_days call bit for bit."""

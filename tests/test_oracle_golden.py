@@ -70,6 +70,17 @@ def test_oracle_mass_balance_closes(path):
     assert np.max(resid / b[:, 0]) < 1e-12
 
 
+def test_oracle_balance_closes_without_continental_area():
+    """Cells without continental area (swb_nocont_150d) route nothing: the inflow
+    they receive leaves the system as a negative leak, and the balance still
+    closes every day."""
+    region, ex = load_npz(os.path.join(os.path.dirname(__file__), "golden", "swb_nocont_150d.npz"))
+    o = Oracle(region)
+    _, b = o.run(int(ex["doy0"]), ex["P"], ex["T"], ex["S"], balance=True)
+    assert np.max(np.abs(b[:, 5]) / b[:, 0]) < 1e-12
+    assert np.sum(b[:, 4]) < 0.   # inflow into the cells without continental area
+
+
 def _regen_module():
     import importlib.util
     path = os.path.join(os.path.dirname(__file__), "golden", "make_golden.py")

@@ -257,6 +257,18 @@ wg_status build_topology(int n, const int32_t *down, const int32_t *rout_order, 
   return WG_OK;
 }
 
+// The continental share of cell i as geo.init leaves it (geo.cpp:25-45): at least
+// the cell's share of local lakes, global lakes, local reservoirs (none) and
+// reservoirs, summed in that order.
+double cont_share(const wg_region *r, int i) {
+  double fw = 0.;
+  fw += r->loc_lake[i];
+  fw += r->glo_lake[i];
+  fw += 0.;
+  fw += r->glo_res[i];
+  return fw > r->contfreq[i] ? fw : r->contfreq[i];
+}
+
 // Water-body flags of cell i and F_VINLINE (the vertical balance runs inside the
 // wavefront: a water body, or no land left outside the water bodies).
 uint32_t water_flags(const wg_region *r, int i) {
@@ -266,9 +278,10 @@ uint32_t water_flags(const wg_region *r, int i) {
   if (r->lake_area[i] > 0.) f |= F_GLOLAKE;
   if (r->res_area[i] > 0.) f |= F_RES;
   if (r->glo_wetl[i] > 0) f |= F_GLOWETL;
-  const double l0 =
-      (r->contfreq[i] - (r->glo_lake[i] + r->glo_wetl[i] + r->loc_lake[i] + r->loc_wetl[i] + r->glo_res[i]));
+  const double cf = cont_share(r, i);
+  const double l0 = (cf - (r->glo_lake[i] + r->glo_wetl[i] + r->loc_lake[i] + r->loc_wetl[i] + r->glo_res[i]));
   if (f || !(l0 > 0.)) f |= F_VINLINE;
+  if (cf < 0.000001) f |= F_NOCONT | F_VINLINE;   // limit_contcell_pct (geo.h:32)
   return f;
 }
 
@@ -1051,7 +1064,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     h.flags[i] = f;
     const double ar = r->area_km2[i];
     h.area[i] = ar;
-    h.contfreq[i] = r->contfreq[i];
+    h.contfreq[i] = cont_share(r, i);
     h.area_f[i] = ar * 1e-8;
     h.a6[i] = ar / 1000000.;
     h.albedo[i] = r->lct_albedo[lct - 1];
@@ -1240,7 +1253,7 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     glowetl[i] = (r->glo_wetl[i] / 100.) * ar * wetlDepth;
     resv[i] = (r->res_area[i] > 0.) ? r->stor_cap[i] : 0.;
     fswb[i] = r->loc_lake[i] / 100. + r->loc_wetl[i] / 100. + r->glo_wetl[i] / 100.;
-    double l = (r->contfreq[i] - (r->glo_lake[i] + r->glo_wetl[i] + r->loc_lake[i] + r->loc_wetl[i] + r->glo_res[i]));
+    double l = (cont_share(r, i) - (r->glo_lake[i] + r->glo_wetl[i] + r->loc_lake[i] + r->loc_wetl[i] + r->glo_res[i]));
     laf[i] = l < 0. ? 0. : l;
     if (r->river_velo_opt == 2) {   // setStoragesToZero starts from G_riverStorageMax (routing.cpp:807-812)
       double bf = r->bankfull[i] < 0.05 ? 0.05 : r->bankfull[i];

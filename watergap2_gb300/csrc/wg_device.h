@@ -34,6 +34,9 @@ enum : uint32_t {
   F_VINLINE = 1u << 12,   // vertical balance runs inside the routing wavefront: the cell has a
                           // water body (its land fraction or open-water fluxes depend on routing)
                           // or no land; all other cells run their vertical balance ahead
+  F_NOCONT = 1u << 13,    // continental share below limit_contcell_pct (geo.cpp:50-60): the
+                          // reference runs no vertical balance there (integrateWGHM.cpp:770-780),
+                          // its daily terms stay 0; always with F_VINLINE
 };
 
 template <class R>

@@ -181,6 +181,11 @@ template <class R>
 __device__ __forceinline__ void vertical_at(const DevCellsT<R> &c, const DevStateT<R> &st, size_t N, int s,
                                             size_t si, int doy, R Pin, R gamma_soil, float Tf, float SWf, R laf,
                                             R prev, VOut<R> &o, double *mo = nullptr, size_t mos = 0) {
+  if (c.flags[s] & F_NOCONT) {   // no vertical balance: the terms stay 0, the state as it is
+    o.rs = R(0); o.gwr = R(0); o.transfer = R(0); o.owp = R(0); o.owpet = R(0);
+    o.land_in = R(0); o.land_evap = R(0); o.land_leak = R(0);
+    return;
+  }
   const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
   const R ext = c.ext_rad[ti], inv_s0 = c.inv_s0[ti];
   R canopy = st.canopy[si], soil = st.soil[si], gsnow = st.snow[si], psum = st.lai_precsum[si];
@@ -462,13 +467,24 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
                       (double)c.area[s], g < 0.f ? 0. : (double)g, up, e_up);
           }
           const size_t wrow = WU ? (size_t)wu.row_of_fday[fday0 + d] * WU_FIELDS * (size_t)n : 0;
-          const R tv = routing_cell<R, WT, WU, GL>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtd, &wu, wrow, si,
-                                                   N);
-          store_rstate(st, si, rs, fl);
+          R tv;
+          const bool nocont = (fl & F_NOCONT) != 0;
+          if (nocont) {
+            // the reference routes only continental cells (routing.cpp:1878-4518): the
+            // storages stay, nothing flows on, and the inflow stays behind in
+            // G_riverInflow, i.e. leaves the system (a negative leak: the leak
+            // counts water the model adds)
+            tv = R(0);
+            rt.p_ow = R(0); rt.e_ow = R(0); rt.leak = R(-up); rt.velocity = R(0);
+          } else {
+            tv = routing_cell<R, WT, WU, GL>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtd, &wu, wrow, si, N);
+            store_rstate(st, si, rs, fl);
+          }
           q_now[si] = (double)tv;
           if constexpr (WT) {
-            const double tr = wtd.river((double)rs.river, (double)c.bw[s], (double)c.rlen[s], (double)c.cfa[s],
-                                        (double)o.owpet);
+            // a cell without continental area keeps the reference's initial 15 degrees (routing.cpp:174)
+            const double tr = nocont ? 15. : wtd.river((double)rs.river, (double)c.bw[s], (double)c.rlen[s],
+                                                       (double)c.cfa[s], (double)o.owpet);
             t_now0[(size_t)kk * N + si] = tr;
             const int stw = c.station[s];
             if (stw >= 0) wtp.qst_t[(size_t)(oday0 + d) * c.nstation + stw] = tr;
@@ -512,17 +528,21 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
             if (mi >= 0 && mi < mon.nmonths) {
               const size_t k = (size_t)mi * N + si;
               const double q = (double)tv;
-              if (!(fl & F_SINK)) {   // outside inland sinks (routing.cpp:4010-4037)
+              // the flux grids of continental cells (routing.cpp:1878-4518), river
+              // availability outside inland sinks (routing.cpp:4010-4037)
+              if (!(fl & (F_SINK | F_NOCONT))) {
                 mon.river_avail[k] += q;
                 mon.min_avail[k] = fmin(mon.min_avail[k], q);
                 mon.max_avail[k] = fmax(mon.max_avail[k], q);
               }
               mon.storage[k] += (double)rs.gw + (double)rs.river + (double)rs.loclake + (double)rs.locwetl +
                                 (double)rs.glolake + (double)rs.glowetl + (double)rs.res;
-              // CellRunoff (routing.cpp:3933-3939): in inland sinks the transported
-              // volume leaves the cell as evaporation
-              mon.cell_runoff[k] += ((fl & F_SINK) ? 0. : q) - up;
-              mon.velocity[k] += (double)rt.velocity / 86.4;   // km/d -> m/s
+              if (!(fl & F_NOCONT)) {
+                // CellRunoff (routing.cpp:3933-3939): in inland sinks the transported
+                // volume leaves the cell as evaporation
+                mon.cell_runoff[k] += ((fl & F_SINK) ? 0. : q) - up;
+                mon.velocity[k] += (double)rt.velocity / 86.4;   // km/d -> m/s
+              }
             }
           }
          }   // cells of the unit

@@ -466,11 +466,14 @@ class Model:
 
     def vinline_fraction(self) -> float:
         """Fraction of cells whose vertical balance runs inside the wavefront (a water
-        body, or no land outside the water bodies) -- the rule of wg_create."""
+        body, or no land outside the water bodies, or no continental area) -- the
+        rule of wg_create, on the continental share as geo.init raises it to the
+        lake and reservoir share (geo.cpp:25-45)."""
         r = self.region
         wb = (r.loc_lake > 0) | (r.loc_wetl > 0) | (r.lake_area > 0) | (r.res_area > 0) | (r.glo_wetl > 0)
-        l0 = r.contfreq - (r.glo_lake + r.glo_wetl + r.loc_lake + r.loc_wetl + r.glo_res)
-        return float(np.mean(wb | ~(l0 > 0)))
+        cf = np.maximum(r.contfreq, ((r.loc_lake + r.glo_lake) + 0.0) + r.glo_res)
+        l0 = cf - (r.glo_lake + r.glo_wetl + r.loc_lake + r.loc_wetl + r.glo_res)
+        return float(np.mean(wb | ~(l0 > 0) | (cf < 1e-6)))
 
     def kernel_timing(self, enable: bool = True):
         self._check(self.lib.wg_kernel_timing(self.h, int(bool(enable))), "kernel_timing")
