@@ -95,6 +95,9 @@ typedef struct wg_region {
                                   global lake or reservoir outflow cell has a unit > 0,
                                   one outflow cell per unit, and the cells of a unit do
                                   not drain out of it and back in                     */
+  const double *lct_kc_min, *lct_kc_max;   /* [18] LAI_22.DAT crop coefficients, or NULL;
+                                              needed by wg_daily_outputs_vertical (Kc,
+                                              laiClass::getDailyKc, lai.cpp:295-306)  */
 } wg_region;
 
 /* Host view of the dynamic state (caller-owned arrays, length ncell unless noted;
@@ -455,9 +458,30 @@ wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable);
  * 22 SWE, 23 SnowCoverAvg [x days], 24 SoilWaterAvg, 25 Runoff, 26 UrbanRunoff,
  * 27 SurfaceRunoff, 28 GwRecharge [mm, water terms weighted by the land share of
  * the continental area], 29 CanopyStorage, 30 SnowStorage, 31 SoilStorage at
- * the month's end [km3];
+ * the month's end [km3], 32 TotalPET [mm] (daily.cpp:1303: PET over the land
+ * and open-water PET over the freshwater share of the continental area);
  * out [nm][ncell][members], cell order. */
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out);
+
+/* The vertical balance's daily grids (daily.cpp:1388-1399, 1472-1540: the
+ * reference's grid_store 5/6 with the daily output options on) for output days
+ * 0 .. ndays-1 (wg_get_discharge's days), kept on the device; 0 days switches
+ * them off.  Same conditions as wg_monthly_outputs_vertical, and the region's
+ * lct_kc_min / lct_kc_max are needed (WG_ERR_INVALID without them).  Enabling
+ * (again) zeroes them; a cell without continental area keeps 0, as the
+ * reference, which runs no vertical balance there.  Total PET's freshwater share
+ * starts from the state at the call (the first year's shares before the first
+ * routed day) and follows the local lakes at each year's start as
+ * routing.annualInit does (routing.cpp:1205-1262). */
+wg_status wg_daily_outputs_vertical(wg_ctx *ctx, int32_t ndays);
+/* field: 0 G_daily365Precip [mm], 1 temp [degC], 2 PET, 3 TotalPET, 4 LAI, 5 Kc,
+ * 6 Albedo, 7 Interception, 8 canopyWaterContent, 9 maxcanopyWaterContent,
+ * 10 SnowFall, 11 SnowMelt, 12 SWE, 13 SnowCoverAvg, 14 SoilWaterAvg,
+ * 15 SurfaceRunoff, 16 GwRecharge [mm, water terms weighted by the land share of
+ * the continental area], 17 ExtRad, 18 ShortDownRad, 19 ShortUpRad,
+ * 20 NetShortRad, 21 NetLongRad, 22 NetRadiation [W/m2], 23 CanopyStorage,
+ * 24 SnowStorage, 25 SoilStorage [km3]; out [nd][ncell], cell order. */
+wg_status wg_get_daily_vertical(wg_ctx *ctx, int32_t field, int32_t day0, int32_t nd, double *out);
 
 /* Cells the day step runs (cell order, nonzero = run; NULL = all).  A skipped
  * cell keeps its state and produces no outflow, so skip whole basins only (a

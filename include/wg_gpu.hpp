@@ -97,6 +97,13 @@ class Context {
   void monthly(int which, int m0, int nm, double *out) {
     check(wg_get_monthly(ctx_, which, m0, nm, out), "wg_get_monthly");
   }
+  // the vertical balance's daily grids for output days 0 .. ndays-1 (0: off)
+  void daily_outputs_vertical(int ndays) {
+    check(wg_daily_outputs_vertical(ctx_, ndays), "wg_daily_outputs_vertical");
+  }
+  void daily_vertical(int field, int day0, int nd, double *out) {
+    check(wg_get_daily_vertical(ctx_, field, day0, nd, out), "wg_get_daily_vertical");
+  }
   // water temperature (wg_options.water_temp = 1)
   void upload_longwave(int day0, int ndays, const float *longwave) {
     check(wg_upload_longwave(ctx_, day0, ndays, longwave), "wg_upload_longwave");

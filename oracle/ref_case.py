@@ -72,21 +72,27 @@ WT_FIELDS = ["wt_river", "wt_loclake", "wt_locwetl", "wt_glolake", "wt_res", "wt
              "ice_river", "ice_loclake", "ice_locwetl", "ice_glolake", "ice_res", "ice_glowetl", "river_avail"]
 
 
-# the monthly output grids the harness dumps with outputs=True (in its order):
-# the vertical balance's (daily.cpp:1281-1386; storages at the month's end) and routing's
-# (routing.cpp:3964-4040, storages at the month's end 4725-4737)
+# the monthly output grids the harness dumps with outputs=1 or 2 (in its order):
+# the vertical balance's (daily.cpp:1281-1386; storages at the month's end; total PET
+# daily.cpp:1303) and routing's (routing.cpp:3964-4040, storages at the month's end
+# 4725-4737)
 MONTHLY_VERTICAL = ["prec", "temp", "ext_rad", "short_up_rad", "short_down_rad", "net_short_rad", "net_long_rad",
                     "net_rad", "open_water_pet", "pet", "aet", "land_aet", "land_aet_uncorr", "lai", "albedo",
                     "interception", "canopy_wc", "max_canopy_wc", "snowfall", "rainfall", "snowmelt", "snow_evap",
                     "swe", "snow_cover", "soil_wc", "runoff", "urban_runoff", "surface_runoff", "gw_recharge",
-                    "canopy_storage", "snow_storage", "soil_storage"]
+                    "canopy_storage", "snow_storage", "soil_storage", "total_pet"]
+# the daily 365 grids of the vertical balance the harness dumps with outputs=2
+DAILY_VERTICAL = ["prec", "temp", "pet", "total_pet", "lai", "kc", "albedo", "interception", "canopy_wc",
+                  "max_canopy_wc", "snowfall", "snowmelt", "swe", "snow_cover", "soil_wc", "surface_runoff",
+                  "gw_recharge", "ext_rad", "short_down_rad", "short_up_rad", "net_short_rad", "net_long_rad",
+                  "net_rad", "canopy_storage", "snow_storage", "soil_storage"]
 MONTHLY_ROUTING = ["river_avail", "min_river_avail", "max_river_avail", "cell_runoff", "velocity", "loclake_storage",
                    "locwetl_storage", "glolake_storage", "glowetl_storage", "res_storage", "river_storage",
                    "gw_storage"]
 
 
 def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000, wtemp=None, wuse=None,
-               delayed=False, glwd_unit=None, outputs=False):
+               delayed=False, glwd_unit=None, outputs=0):
     n = region.ncell
     if n > NG:
         raise ValueError("region larger than the reference grid")
@@ -205,13 +211,13 @@ def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: i
         f.write(f"{n} {P.shape[0]} {doy0} {year0} {resopt} {region.river_velo_opt} {len(stations)} {len(snapshots)} "
                 f"{0 if wtemp is None else 1} {int(getattr(region, 'frac_routing', 0))} "
                 f"{0 if wuse is None else (2 if delayed else 1) + (0 if glwd_unit is None else 2)} "
-                f"{int(getattr(region, 'statcorr_opt', 0))} {int(bool(outputs))}\n")
+                f"{int(getattr(region, 'statcorr_opt', 0))} {int(outputs)}\n")
     with open(f"{d}/snapshots.txt", "w") as f:
         f.write(" ".join(str(int(s)) for s in snapshots) + "\n")
 
 
 def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wtemp=None, wuse=None, delayed=False,
-        threads=1, glwd_unit=None, outputs=False):
+        threads=1, glwd_unit=None, outputs=0):
     """Run the reference harness; returns dict(lai_a, lai_b, bottom_width, snapshots=[{field: array}],
     discharge=[ndays, nstation], stations=..., timing=dict(threads, vertical_s, routing_s)): the vertical
     pass on `threads` OpenMP threads, routing serial, as integrate_wghm_ runs them."""
@@ -261,6 +267,11 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
         for f in MONTHLY_VERTICAL + MONTHLY_ROUTING:
             res["monthly"][f] = raw[o:o + 12 * n].reshape(12, n).copy()
             o += 12 * n
+    if outputs == 2:   # the year's daily grids [365][ncell] per field
+        res["daily"] = {}
+        for f in DAILY_VERTICAL:
+            res["daily"][f] = raw[o:o + 365 * n].reshape(365, n).copy()
+            o += 365 * n
     assert o == raw.size, (o, raw.size)
     res["stations"] = stations
     with open(os.path.join(tmp, "timing.txt")) as f:

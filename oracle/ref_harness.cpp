@@ -70,7 +70,8 @@ int main(int argc, char **argv) {
                                     // (2: delayed satisfaction), 3/4 the same with the NUs of global
                                     // lakes' riparian cells aggregated (aggrNUsGloLakResOpt = 1)
     if (!(m >> statcorr)) statcorr = 0;   // optional: options.statcorrOpt
-    if (!(m >> outputs)) outputs = 0;     // optional: the monthly output grids (grid_store = 2)
+    if (!(m >> outputs)) outputs = 0;     // optional: the monthly output grids (1: grid_store = 2),
+                                          // and the daily 365 grids as well (2: grid_store = 6)
   }
   std::vector<int> snap_days(nsnap);
   {
@@ -100,6 +101,17 @@ int main(int argc, char **argv) {
   if (outputs) {   // monthly output grids, storages at the month's end (grid_store_TypeForStorages 0)
     options.grid_store = 2;
     options.outMinMaxRiverAvail = 1;
+  }
+  if (outputs == 2) {   // and the vertical balance's daily 365 grids (daily.cpp:1388-1399, 1472-1540)
+    options.grid_store = 6;
+    options.outPrecDaily = 1; options.outTemp = 1; options.outPETDaily = 1; options.outTotalPETDaily = 1;
+    options.outLAIDaily = 1; options.outAlbedoDaily = 1; options.outInterceptionDaily = 1;
+    options.outCanopyWaterDaily = 1; options.outmaxCanopyWaterDaily = 1; options.outSnowFallDaily = 1;
+    options.outSnowMeltDaily = 1; options.outSWEDaily = 1; options.outSnowCoverDaily = 1;
+    options.outSoilWaterDaily = 1; options.outSurfaceRunoffDaily = 1; options.outGWRechargeDaily = 1;
+    options.outExtRadiationDaily = 1; options.outShortDownRadiationDaily = 1; options.outShortUpRadiationDaily = 1;
+    options.outNetShortWaveRadiationDaily = 1; options.outNetLongWaveRadiationDaily = 1;
+    options.outNetRadiationDaily = 1; options.outSingleStoragesDaily = 1;
   }
   options.glacierOpt = 0; options.calc_wtemp = wtemp; options.start_year = year0; options.end_year = year0;
   options.init_years = 0; options.time_step = 1; options.outLAImax = 0;
@@ -325,6 +337,7 @@ int main(int argc, char **argv) {
         &w.G_monthlySnowEvap, &w.G_monthlySWE, &w.G_monthlySnowCoverAvg, &w.G_monthlySoilWaterAvg,
         &w.G_monthlyRunoff, &w.G_monthlyUrbanRunoff, &w.G_monthlySurfaceRunoff, &w.G_monthlyGwRecharge};
     const MonthlyGrid<> *vstor[] = {&w.G_monthlyCanopyStorage, &w.G_monthlySnowStorage, &w.G_monthlySoilStorage};
+    const MonthlyGrid<false> *vlate[] = {&w.G_monthlyTotalPET};   // daily.cpp:1303
     const MonthlyGrid<false> *rout[] = {
         &routing.G_monthlyRiverAvail, &routing.G_monthlyMinRiverAvail, &routing.G_monthlyMaxRiverAvail,
         &routing.G_monthlyCellRunoff, &routing.G_monthlyVelocity, &routing.G_monthlyLocLakeStorage,
@@ -338,7 +351,25 @@ int main(int argc, char **argv) {
     };
     for (auto *g : vert) dump(g);
     for (auto *g : vstor) dump(g);
+    for (auto *g : vlate) dump(g);
     for (auto *g : rout) dump(g);
+  }
+  if (outputs == 2) {   // the year's daily grids [field][day][cell] (daily.cpp:1388-1399, 1472-1540)
+    auto &w = dailyWaterBalance;
+    const DailyGrid<false> *dvert[] = {
+        &w.G_daily365Precip, &w.G_daily365temp, &w.G_daily365PET, &w.G_daily365TotalPET, &w.G_daily365LAI,
+        &w.G_daily365Kc, &w.G_daily365Albedo, &w.G_daily365Interception, &w.G_daily365canopyWaterContent,
+        &w.G_daily365maxcanopyWaterContent, &w.G_daily365SnowFall, &w.G_daily365SnowMelt, &w.G_daily365SWE,
+        &w.G_daily365SnowCoverAvg, &w.G_daily365SoilWaterAvg, &w.G_daily365SurfaceRunoff, &w.G_daily365GwRecharge,
+        &w.G_daily365ExtRad, &w.G_daily365ShortDownRad, &w.G_daily365ShortUpRad, &w.G_daily365NetShortRad,
+        &w.G_daily365NetLongRad, &w.G_daily365NetRadiation, &w.G_daily365CanopyStorage, &w.G_daily365SnowStorage,
+        &w.G_daily365SoilStorage};
+    std::vector<double> buf((size_t)365 * ncase);
+    for (auto *g : dvert) {
+      for (int d = 0; d < 365; d++)
+        for (int n = 0; n < ncase; n++) buf[(size_t)d * ncase + n] = (*g)(n, d);
+      write_raw(out, buf.data(), buf.size());
+    }
   }
   fclose(out);
   if (FILE *tf = fopen((dir + "/timing.txt").c_str(), "w")) {

@@ -263,25 +263,33 @@ def main_wuse_glwd(names=None):
         print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
 
 
-def main_outputs(names=None, name="swb_outputs_365d"):
-    """The monthly output grids (grid_store = 2, storages at the month's end) of the
-    vertical balance and routing over one calendar year, on the water-body region
-    with inland sinks."""
+def main_outputs(names=None, name="swb_outputs_730d"):
+    """The monthly output grids (grid_store = 6: monthly, storages at the month's
+    end) of the vertical balance and routing, and the vertical balance's daily 365
+    grids, on the water-body region with inland sinks over two calendar years: the
+    grids hold the second year (annualInit resets them; total PET's freshwater
+    share is then the local lakes' share at the year's start, routing.cpp:1249-1259)."""
     if names and name not in names:
         return
     if not ref_case.available():
         if not ref_case.build(REF_SOURCE):
             raise SystemExit("reference sources not found; cannot regenerate fixtures")
     region = sy.region_small_swb(seed=21, ny=16, nx=32, block_at=(100, 300))
-    nd = 365
+    nd = 730
     P, T, S = sy.forcing(region, nd, doy0=1)
     outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
-    res = ref_case.run(region, P, T, S, doy0=1, stations=outl[:24], snapshots=[nd], outputs=True)
+    res = ref_case.run(region, P, T, S, doy0=1, stations=outl[:24], snapshots=[nd], outputs=2)
     extra = dict(P=P, T=T, S=S, doy0=np.array(1), stations=res["stations"], snap_days=np.array([nd]),
                  discharge=res["discharge"])
     _put_snapshots(region, res, extra)
     for k, v in res["monthly"].items():
         extra[f"m_{k}"] = v
+    # the daily grids on a sample of days (the first days of January and February,
+    # every 13th day, the last day), to keep the fixture small
+    days = np.unique(np.r_[0:3, 31:34, np.arange(0, 365, 13), 364])
+    extra["daily_days"] = days
+    for k, v in res["daily"].items():
+        extra[f"d_{k}"] = v[days]
     path = os.path.join(HERE, f"{name}.npz")
     save_npz(region, path, **extra)
     print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")

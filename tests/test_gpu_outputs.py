@@ -1,13 +1,14 @@
-"""Monthly output grids on the GPU against the reference's own grids.
+"""Monthly and daily output grids on the GPU against the reference's own grids.
 
-The fixture swb_outputs_365d holds the reference's monthly grids (options
-grid_store = 2, storages at the month's end, outMinMaxRiverAvail = 1) of one
-calendar year on a 281-cell region with every water-body type and inland
-sinks: the vertical balance's 29 sums and means (daily.cpp:1281-1386) plus its
-canopy, snow and soil storages at the month's end, and routing's river
-availability with its minimum and maximum, cell runoff and velocity
-(routing.cpp:3964-4040) plus every routing storage at the month's end
-(routing.cpp:4725-4737).
+The fixture swb_outputs_730d holds the reference's grids (options grid_store = 6,
+storages at the month's end, outMinMaxRiverAvail = 1, the daily output options
+on) of the second of two calendar years on a 281-cell region with every
+water-body type and inland sinks: the vertical balance's 29 monthly sums and
+means (daily.cpp:1281-1386) with total PET (1303) and its canopy, snow and soil
+storages at the month's end; routing's river availability with its minimum and
+maximum, cell runoff and velocity (routing.cpp:3964-4040) and every routing
+storage at the month's end (routing.cpp:4725-4737); and the vertical balance's
+26 daily grids (daily.cpp:1388-1399, 1472-1540) on a sample of days.
 
 Tolerance (FP64): 1e-10 relative to each grid's values, elements below 1e-6 of
 the grid's largest value compared against that floor (helpers.max_rel_err).
@@ -21,7 +22,8 @@ from helpers import max_rel_err
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-10
-PATH = os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_365d.npz")
+PATH = os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_730d.npz")
+Y2 = 365   # the grids are the second year's
 # Model.monthly name -> the reference's grid
 ROUTING = {"river_avail": "river_avail", "min_avail": "min_river_avail", "max_avail": "max_river_avail",
            "cell_runoff": "cell_runoff", "velocity": "velocity"}
@@ -37,50 +39,68 @@ def _built():
         build.build()
 
 
-def _year(days_per_step=0, deferred=False):
+def _two_years(days_per_step=0, deferred=False):
     from watergap2_gb300.gpu import Model
     from watergap2_gb300.region import load_npz
     region, ex = load_npz(PATH)
     P, T, S = ex["P"], ex["T"], ex["S"]
     nd = P.shape[0]
     m = Model(region, max_days=nd, stations=ex["stations"], days_per_step=days_per_step)
-    m.monthly_outputs(12, doy_day0=1)
+    m.monthly_outputs(24, doy_day0=1)
     m.monthly_outputs_vertical(True)
+    m.daily_outputs_vertical(nd)
     m.record_daily_storages(True)
     m.upload_forcing(0, P, T, S)
     if deferred:                                       # per-day calls, queued into day-pipelined runs
         m.set_deferred(True)
         for d in range(nd):
-            m.step_vertical(d + 1, d)
-            m.step_routing(d + 1, d)
+            doy = d % 365 + 1
+            m.step_vertical(doy, d)
+            m.step_routing(doy, d)
     else:
         m.run_days(1, 0, nd)
-    grids = {k: m.monthly(k) for k in m.MONTHLY_VERTICAL + list(ROUTING)}
+    grids = {k: m.monthly(k, 12, 12) for k in m.MONTHLY_VERTICAL + list(ROUTING)}
+    grids.update({"d_" + k: m.daily_vertical(k, Y2, 365) for k in m.DAILY_VERTICAL})
     return m, ex, grids
 
 
 @pytest.mark.parametrize("dps", [1, 5])
-def test_monthly_grids_match_reference_year(dps):
-    m, ex, grids = _year(days_per_step=dps)
+def test_output_grids_match_reference(dps):
+    m, ex, grids = _two_years(days_per_step=dps)
     errs = {k: max_rel_err(grids[k], ex["m_" + k]) for k in m.MONTHLY_VERTICAL}
     errs.update({k: max_rel_err(grids[k], ex["m_" + r]) for k, r in ROUTING.items()})
-    ds = m.daily_storages(0, 365)
+    ds = m.daily_storages(Y2, 365)
     for i, f in enumerate(STORAGES):
         errs[f + "_storage"] = max_rel_err(ds[MONTH_END, i], ex[f"m_{f}_storage"])
+    days = ex["daily_days"]
+    for k in m.DAILY_VERTICAL:
+        errs["d_" + k] = max_rel_err(grids["d_" + k][days], ex["d_" + k])
     bad = {k: v for k, v in errs.items() if not v <= RTOL}
     assert not bad, bad
-    q = m.discharge(0, 365)
+    q = m.discharge(0, 730)
     assert max_rel_err(q, ex["discharge"]) <= RTOL
 
 
-def test_monthly_grids_deferred_per_day_calls_same_bits():
+def test_output_grids_deferred_per_day_calls_same_bits():
     """The per-day entry points, queued (wg_set_deferred), give the grids of one
     run bit for bit; without the queue the per-day vertical call is refused
     while the vertical grids are on."""
-    _, _, a = _year(deferred=False)
-    _, _, b = _year(deferred=True)
+    _, _, a = _two_years(deferred=False)
+    _, _, b = _two_years(deferred=True)
     for k in a:
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_daily_grids_refused_without_kc():
+    from watergap2_gb300.gpu import Model, WgError
+    from watergap2_gb300.region import load_npz
+    region, ex = load_npz(PATH)
+    region.lct_tables = {k: v for k, v in region.lct_tables.items() if k not in ("kc_min", "kc_max")}
+    m = Model(region, max_days=4)
+    with pytest.raises(WgError):
+        m.daily_outputs_vertical(4)
+    m.monthly_outputs(1, doy_day0=1)
+    m.monthly_outputs_vertical(True)                   # the monthly grids need no Kc
 
 
 def test_per_day_vertical_refused_with_vertical_grids():
@@ -94,5 +114,9 @@ def test_per_day_vertical_refused_with_vertical_grids():
     with pytest.raises(WgError):
         m.step_vertical(1, 0)
     m.monthly_outputs_vertical(False)                  # grids off: the per-day call runs
+    m.daily_outputs_vertical(4)
+    with pytest.raises(WgError):                       # the daily grids refuse it too
+        m.step_vertical(1, 0)
+    m.daily_outputs_vertical(0)
     m.step_vertical(1, 0)
     m.step_routing(1, 0)

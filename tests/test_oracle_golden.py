@@ -140,17 +140,20 @@ def test_station_correction_fixture_changes_discharge():
     assert not np.allclose(q[:, ex["stations"]], ex["discharge"], rtol=1e-6)
 
 
-def test_monthly_output_fixture_pinned_to_its_inputs():
-    """The reference's monthly grids in swb_outputs_365d are its month sums in
-    cell order (grid_store = 2 divides the means only when it writes): monthly
-    precipitation and temperature equal the sums of the fixture's daily forcing
-    exactly, and the month-end storages at December's end equal the state of
-    the same run's day-365 snapshot."""
-    region, ex = load_npz(os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_365d.npz"))
-    b = np.r_[0, np.cumsum([31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31])]
+def test_output_fixture_pinned_to_its_inputs():
+    """The reference's grids in swb_outputs_730d are its second year's month sums
+    and day values in cell order (grid_store = 6 divides the means only when it
+    writes): monthly precipitation and temperature equal the sums of the
+    fixture's daily forcing exactly, the daily ones the forcing itself, and the
+    month-end storages at December's end equal the state of the same run's
+    day-730 snapshot."""
+    region, ex = load_npz(os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_730d.npz"))
+    b = 365 + np.r_[0, np.cumsum([31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31])]
+    days = ex["daily_days"]
     for f, field in (("prec", "P"), ("temp", "T")):
         x = ex[field].astype(np.float64)
         sums = np.array([x[b[k]:b[k + 1]].sum(axis=0) for k in range(12)])
         assert np.array_equal(sums, ex[f"m_{f}"]), f
+        assert np.array_equal(x[365 + days], ex[f"d_{f}"]), f
     for f in ("loclake", "locwetl", "glolake", "glowetl", "res", "river", "gw"):
         assert np.array_equal(ex[f"m_{f}_storage"][11], ex[f"s0_{f}"]), f

@@ -969,7 +969,9 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
       if (r->res_type[i] != 1 && r->res_type[i] != 2) return WG_ERR_INVALID;
       if (!(r->mean_outflow[i] > 0.) || r->start_month[i] < 1 || r->start_month[i] > 12) return WG_ERR_INVALID;
     }
-    if (!(r->river_length[i] > 0.)) return WG_ERR_INVALID;
+    // a river needs a length; cells without continental area are not routed, and
+    // their length (scaled by the share) may be 0
+    if (!(r->river_length[i] > 0.) && !(cont_share(r, i) < 0.000001)) return WG_ERR_INVALID;
   }
   wg_ctx::Glwd glwd;   // GLWD units, checked before any device is touched
   if (aggr) {
@@ -1041,6 +1043,8 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
          PTC_ARI = 11, PET_MXDY = 12, MCWH = 13, T_SNOWFZ = 15, T_SNOWMT = 16, DEGDAY = 17, T_GRADNT = 18,
          PCRITGWA = 21, GWOUTF = 22, PREC = 25 };
   HostConsts h;
+  ctx->has_kc = r->lct_kc_min && r->lct_kc_max;
+  ctx->vstatic.assign((size_t)(wg::VCONST_FIELDS + 1) * n, 0.);
   h.flags.resize(n); h.ext_row.resize(n); h.station.assign(n, -1); h.init_days.resize(n); h.start_month.resize(n);
 #define X(f) h.f.assign(n, 0.);
   WG_RFIELDS(X)
@@ -1073,6 +1077,22 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
     const float lmin = r->lct_lai_a[lct - 1] + r->lct_lai_b[lct - 1] * r->lai_max[i];   // lai.cpp:154 (float)
     h.lai_min[i] = lmin;
     h.lai_max[i] = r->lai_max[i];
+    {   // the output grids' constants: Kc (lai.cpp:295-306, LAImin in float as there),
+        // the first year's freshwater share (routing.cpp:1213), the global-lake and
+        // reservoir shares, G_loc_lake / 100
+      double *v = ctx->vstatic.data();
+      if (ctx->has_kc) {
+        const double kmin = r->lct_kc_min[lct - 1], kmax = r->lct_kc_max[lct - 1];
+        const double den = (double)r->lai_max[i] - (double)lmin;
+        v[i] = kmin;
+        v[(size_t)n + i] = den == 0. ? 0. : (kmax - kmin) / den;
+      }
+      v[2 * (size_t)n + i] = lmin;
+      v[3 * (size_t)n + i] = r->glo_lake[i] + r->loc_lake[i] + r->glo_res[i];
+      v[4 * (size_t)n + i] = r->glo_lake[i];
+      v[5 * (size_t)n + i] = r->glo_res[i];
+      v[6 * (size_t)n + i] = r->loc_lake[i] / 100.;
+    }
     h.init_days[i] = r->lct_initial_days[lct - 1];
     h.mprec[i] = P(PREC, i);
     h.alpha[i] = (r->aindex[i] == 1) ? P(PTC_ARI, i) : P(PTC_HUM, i);
@@ -1785,7 +1805,8 @@ static wg_status run_steps_at(wg_ctx *ctx, int doy0, int fday0, int oday0, int n
 }
 
 static wg_status vertical_now(wg_ctx *ctx, int doy, int fday) {
-  if (ctx->mon.vert) return WG_ERR_UNSUPPORTED;   // the per-day kernel has no monthly grids: wg_set_deferred
+  // the per-day kernel fills no output grids: wg_set_deferred runs the per-day calls through the wavefront
+  if (ctx->mon.vert || ctx->mon.dvert) return WG_ERR_UNSUPPORTED;
   cudaSetDevice(ctx->device);
   join_uploads(ctx);
   ctx->launches++;
@@ -2043,6 +2064,8 @@ wg_status wg_set_step_sync(wg_ctx *ctx, int32_t flags) {
   return WG_OK;
 }
 
+static cudaError_t vconst_upload(wg_ctx *ctx);
+
 wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
   if (!ctx || nmonths < 0 || doy_day0 < 1 || doy_day0 > 365) return WG_ERR_INVALID;
   WG_FLUSH(ctx);
@@ -2057,12 +2080,14 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
     cudaFree(ctx->mon_vbuf);
     ctx->mon_vbuf = nullptr;
   }
-  {   // the daily storage record is kept
-    double *ds = ctx->mon.daily_storage;
-    const int dd = ctx->mon.daily_days;
+  {   // the daily storage record and the daily grids are kept
+    const DevMonthly keep = ctx->mon;
     ctx->mon = DevMonthly{};
-    ctx->mon.daily_storage = ds;
-    ctx->mon.daily_days = dd;
+    ctx->mon.daily_storage = keep.daily_storage;
+    ctx->mon.daily_days = keep.daily_days;
+    ctx->mon.dvert = keep.dvert;
+    ctx->mon.dvert_days = keep.dvert_days;
+    ctx->mon.vconst = keep.vconst;
   }
   if (nmonths == 0) return WG_OK;
   const size_t per = (size_t)nmonths * ctx->nstate();
@@ -2087,10 +2112,89 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
   if (e == cudaSuccess && ctx->mon_vert_on) {   // the vertical balance's grids, on the same calendar
     e = cudaMalloc((void **)&ctx->mon_vbuf, (size_t)wg::VOUT_FIELDS * per * sizeof(double));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->mon_vbuf, 0, (size_t)wg::VOUT_FIELDS * per * sizeof(double), ctx->stream);
+    if (e == cudaSuccess) e = vconst_upload(ctx);
     if (e == cudaSuccess) m.vert = ctx->mon_vbuf;
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return cuda_fail(ctx, e, "monthly_outputs");
+}
+
+// The output grids' constants on the device (DevMonthly::vconst), in slot order:
+// those of wg_create, and for the cells routed already the freshwater share of
+// the current local lakes, as routing.annualInit takes it after the first year
+// (routing.cpp:1249-1259, 5045-5048).
+static cudaError_t vconst_upload(wg_ctx *ctx) {
+  const int n = ctx->n;
+  const size_t nn = (size_t)n;
+  cudaError_t e = cudaSuccess;
+  if (!ctx->mon_vconst) e = cudaMalloc((void **)&ctx->mon_vconst, (size_t)wg::VCONST_FIELDS * nn * sizeof(double));
+  if (e != cudaSuccess) return e;
+  std::vector<int32_t> started(nn);
+  std::vector<double> rf(nn), v((size_t)wg::VCONST_FIELDS * nn);
+  e = cudaMemcpy(started.data(), ctx->sd.laf_started, nn * sizeof(int32_t), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(rf.data(), ctx->sd.rf_loclake, nn * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return e;
+  const double *vs = ctx->vstatic.data();
+  for (int sl = 0; sl < n; ++sl) {
+    const size_t c = (size_t)ctx->topo.cell_of_slot[sl];
+    for (int k = 0; k < wg::VCONST_FIELDS; ++k) v[k * nn + sl] = vs[k * nn + c];
+    if (started[sl] == 1) {
+      const double ll = vs[6 * nn + c];
+      const double fll = (ll > 0. && rf[sl] > 0.) ? rf[sl] * ll : 0.;
+      v[3 * nn + sl] = v[4 * nn + sl] + fll * 100. + v[5 * nn + sl];
+    }
+  }
+  e = cudaMemcpy(ctx->mon_vconst, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) ctx->mon.vconst = ctx->mon_vconst;
+  return e;
+}
+
+wg_status wg_daily_outputs_vertical(wg_ctx *ctx, int32_t ndays) {
+  if (!ctx || ndays < 0) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
+  if (ndays > 0 && (ctx->precision != 0 || ctx->members != 1 || ctx->wt.enabled || ctx->wu.enabled))
+    return WG_ERR_UNSUPPORTED;
+  if (ndays > 0 && !ctx->has_kc) {
+    ctx->err = "the daily grids need the region's lct_kc_min and lct_kc_max (Kc)";
+    return WG_ERR_INVALID;
+  }
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "daily_outputs_vertical");
+  if (ctx->mon_dbuf) {
+    cudaFree(ctx->mon_dbuf);
+    ctx->mon_dbuf = nullptr;
+  }
+  ctx->mon.dvert = nullptr;
+  ctx->mon.dvert_days = 0;
+  if (ndays == 0) return WG_OK;
+  const size_t bytes = (size_t)wg::DOUT_FIELDS * ndays * (size_t)ctx->n * sizeof(double);
+  e = cudaMalloc((void **)&ctx->mon_dbuf, bytes);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->mon_dbuf, 0, bytes, ctx->stream);
+  if (e == cudaSuccess) e = vconst_upload(ctx);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "daily_outputs_vertical");
+  ctx->mon.dvert = ctx->mon_dbuf;
+  ctx->mon.dvert_days = ndays;
+  return WG_OK;
+}
+
+wg_status wg_get_daily_vertical(wg_ctx *ctx, int32_t field, int32_t day0, int32_t nd, double *out) {
+  if (!ctx || !out || field < 0 || field >= wg::DOUT_FIELDS || day0 < 0 || nd < 0 ||
+      day0 + nd > ctx->mon.dvert_days)
+    return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  const size_t N = (size_t)ctx->n;
+  std::vector<double> buf((size_t)nd * N);
+  const double *src = ctx->mon_dbuf + ((size_t)field * ctx->mon.dvert_days + day0) * N;
+  cudaError_t e = cudaMemcpy(buf.data(), src, buf.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "get_daily_vertical");
+  const auto &c2s = ctx->topo.cell_of_slot;
+  for (int d = 0; d < nd; ++d)
+    for (size_t sl = 0; sl < N; ++sl) out[(size_t)d * N + c2s[sl]] = buf[(size_t)d * N + sl];
+  return WG_OK;
 }
 
 wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable) {

@@ -71,6 +71,12 @@ struct wg_ctx {
   double *mon_buf = nullptr;
   double *mon_vbuf = nullptr;              // the vertical balance's monthly grids (wg_monthly_outputs_vertical)
   bool mon_vert_on = false;
+  double *mon_dbuf = nullptr;              // its daily grids (wg_daily_outputs_vertical)
+  double *mon_vconst = nullptr;            // their constants (DevMonthly::vconst)
+  // [7][n] cell order, from wg_create: the grids' constants (DevMonthly::vconst,
+  // the first year's freshwater share) and G_loc_lake / 100
+  std::vector<double> vstatic;
+  bool has_kc = false;                     // the region gave the LCT crop coefficients
   double *daily_storage_buf = nullptr;     // wg_record_daily_storages (context allocation)
   double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
   float *staging = nullptr;
@@ -142,6 +148,8 @@ struct wg_ctx {
     release_tools();
     if (mon_buf) cudaFree(mon_buf);
     if (mon_vbuf) cudaFree(mon_vbuf);
+    if (mon_dbuf) cudaFree(mon_dbuf);
+    if (mon_vconst) cudaFree(mon_vconst);
     for (void *p : allocs) cudaFree(p);
     if (own_stream && stream) cudaStreamDestroy(stream);
     if (copy_stream) cudaStreamDestroy(copy_stream);

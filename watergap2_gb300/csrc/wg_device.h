@@ -133,8 +133,25 @@ constexpr int WG_BALANCE_ARRAYS = 14;
 // runoff, 26 urban runoff, 27 surface runoff, 28 groundwater recharge [mm
 // (x days for states), per day's land share of the continental area where the
 // reference weighs it so]; 29-31 canopy, snow and soil storage at the month's
-// end [km3].
-constexpr int VOUT_FIELDS = 32;
+// end [km3]; 32 total PET over land and fresh water (daily.cpp:1303) [mm].
+constexpr int VOUT_FIELDS = 33;
+
+// The vertical balance's daily grids (daily.cpp:1388-1399, 1472-1540, grid_store
+// 5/6), field k at dvert[k * dvert_days * N + day * N + state]: 0 precipitation,
+// 1 temperature, 2 PET, 3 total PET, 4 LAI, 5 crop coefficient Kc, 6 albedo,
+// 7 interception, 8 canopy water content, 9 its capacity, 10 snowfall,
+// 11 snowmelt, 12 snow water equivalent, 13 snow-covered fraction, 14 soil water,
+// 15 surface runoff, 16 groundwater recharge, 17-22 radiation [W/m2]:
+// extraterrestrial, incoming and reflected shortwave, net shortwave, net
+// longwave, net, 23-25 canopy, snow and soil storage [km3].
+constexpr int DOUT_FIELDS = 26;
+// Per state index, for the grids' Kc and total PET: [0] Kc at LAImin
+// (kc_min), [1] (kc_max - kc_min) / (LAImax - LAImin) (0 where they are equal),
+// [2] LAImin, [3] the freshwater share of the cell for total PET [%]
+// (G_fwaterfreq, routing.cpp:1205-1262: updated on the first day of each year
+// after the first by the thread that routes the cell), [4] its global-lake and
+// [5] its reservoir share [%].
+constexpr int VCONST_FIELDS = 6;
 
 struct DevMonthly {
   double *river_avail;   // sum of the day's transported volume [km3/month]   (G_monthlyRiverAvail)
@@ -144,6 +161,9 @@ struct DevMonthly {
   double *velocity;      // sum of the river velocity [m/s x days]                (G_monthlyVelocity)
   int32_t nmonths, doy_day0, month0, enabled;
   double *vert;          // null, or the vertical balance's grids [VOUT_FIELDS][nmonths][N]
+  double *dvert;         // null, or the vertical balance's daily grids [DOUT_FIELDS][dvert_days][N]
+  int32_t dvert_days;
+  double *vconst;        // with vert or dvert: [VCONST_FIELDS][N]
   // the day-end routing storages of every cell and output day, [day][7][n*members]
   // in the order the reference writes them into its state file (routing.cpp:5001-5020):
   // local lake, local wetland, global lake, global wetland, reservoir, river,

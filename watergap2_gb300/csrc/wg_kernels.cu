@@ -180,7 +180,7 @@ __device__ __forceinline__ void store_rstate(const DevStateT<R> &s, size_t i, co
 template <class R>
 __device__ __forceinline__ void vertical_at(const DevCellsT<R> &c, const DevStateT<R> &st, size_t N, int s,
                                             size_t si, int doy, R Pin, R gamma_soil, float Tf, float SWf, R laf,
-                                            R prev, VOut<R> &o, double *mo = nullptr, size_t mos = 0) {
+                                            R prev, VOut<R> &o, const VSink *vs = nullptr) {
   if (c.flags[s] & F_NOCONT) {   // no vertical balance: the terms stay 0, the state as it is
     o.rs = R(0); o.gwr = R(0); o.transfer = R(0); o.owp = R(0); o.owpet = R(0);
     o.land_in = R(0); o.land_evap = R(0); o.land_leak = R(0);
@@ -190,10 +190,9 @@ __device__ __forceinline__ void vertical_at(const DevCellsT<R> &c, const DevStat
   const R ext = c.ext_rad[ti], inv_s0 = c.inv_s0[ti];
   R canopy = st.canopy[si], soil = st.soil[si], gsnow = st.snow[si], psum = st.lai_precsum[si];
   int days = st.lai_days[si], status = st.lai_status[si];
-  if (mo)   // the monthly output grids (FP64 single member)
+  if (vs)   // the output grids (FP64 single member)
     vertical_cell<R, std::is_same<R, double>::value>(c, s, gamma_soil, canopy, soil, gsnow, st.snow_band + si, N,
-                                                      days, status, psum, laf, prev, Pin, Tf, SWf, ext, inv_s0, o, mo,
-                                                      mos);
+                                                      days, status, psum, laf, prev, Pin, Tf, SWf, ext, inv_s0, o, vs);
   else
     vertical_cell<R>(c, s, gamma_soil, canopy, soil, gsnow, st.snow_band + si, N, days, status, psum, laf, prev, Pin,
                      Tf, SWf, ext, inv_s0, o);
@@ -225,15 +224,24 @@ __global__ void __launch_bounds__(256) k_vertical(DevCellsT<R> c, DevStateT<R> s
 // One (cell, member) state index i of the vertical balance run ahead: the days
 // the wavefront steps [t_b, t_e) will route, vertical state in registers, surface
 // runoff and recharge into the ring; balance terms into arrays 0, 1 and 10.
-// The entry of state si in the vertical balance's monthly output grids for output
-// day od (the month of the output calendar, as the routing aggregates count it),
-// or null when the grids are off or the day is outside them.
-__device__ __forceinline__ double *vert_month(const DevMonthly &mon, int od, size_t si, size_t N) {
-  if (!mon.vert) return nullptr;
-  const int yd = mon.doy_day0 - 1 + od;
-  const int mi = (yd / 365) * 12 + month_of(yd % 365 + 1) - mon.month0;
-  if (mi < 0 || mi >= mon.nmonths) return nullptr;
-  return mon.vert + (size_t)mi * N + si;
+// The output grids of state si for output day od: its entry in the vertical
+// balance's monthly grids (the month of the output calendar, as the routing
+// aggregates count it) and in the daily grids, each null when the grids are off
+// or the day is outside them.  False: no grid takes the day.
+__device__ __forceinline__ bool vert_sink(const DevMonthly &mon, int od, size_t si, size_t N, VSink &vs) {
+  vs.mo = nullptr;
+  vs.dd = nullptr;
+  if (mon.vert) {
+    const int yd = mon.doy_day0 - 1 + od;
+    const int mi = (yd / 365) * 12 + month_of(yd % 365 + 1) - mon.month0;
+    if (mi >= 0 && mi < mon.nmonths) vs.mo = mon.vert + (size_t)mi * N + si;
+  }
+  if (mon.dvert && od >= 0 && od < mon.dvert_days) vs.dd = mon.dvert + (size_t)od * N + si;
+  vs.mos = (size_t)mon.nmonths * N;
+  vs.dds = (size_t)mon.dvert_days * N;
+  vs.vk = mon.vconst + si;
+  vs.vks = N;
+  return vs.mo || vs.dd;
 }
 
 template <class R, bool ENS>
@@ -265,12 +273,11 @@ __device__ __forceinline__ void va_cell(const DevCellsT<R> &c, const DevStateT<R
     const size_t fo = (size_t)(fday0 + d) * n + s;
     const size_t ti = (size_t)(doy - 1) * c.nrow + c.ext_row[s];
     VOut<R> o;
-    double *mo = (!ENS && mon) ? vert_month(*mon, oday0 + d, i, N) : nullptr;
-    if (mo)   // the monthly output grids (FP64 single member)
+    VSink vs;
+    if (!ENS && mon && vert_sink(*mon, oday0 + d, i, N, vs))   // the output grids (FP64 single member)
       vertical_cell<R, std::is_same<R, double>::value>(c, s, gam, canopy, soil, gsnow, st.snow_band + i, N, days,
                                                         status, psum, laf, laf, R(f.prec[fo]) * pf, f.temp[fo],
-                                                        f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o, mo,
-                                                        (size_t)mon->nmonths * N);
+                                                        f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o, &vs);
     else
       vertical_cell<R>(c, s, gam, canopy, soil, gsnow, st.snow_band + i, N, days, status, psum, laf, laf,
                        R(f.prec[fo]) * pf, f.temp[fo], f.swrad[fo], c.ext_rad[ti], c.inv_s0[ti], o);
@@ -437,9 +444,18 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
               gam *= R(mem.gamma_factor[mm]);
             }
             const int started = st.laf_started[si];
-            double *mo = VO ? vert_month(mon, oday0 + d, si, N) : nullptr;
+            VSink vs;
+            const bool vo = VO && vert_sink(mon, oday0 + d, si, N, vs);
+            if (VO && doy == 1 && started == 1 && (fl & F_LOCLAKE) && mon.vconst) {
+              // total PET's freshwater share after the first year: the local lakes'
+              // share at the year's start (routing.cpp:1249-1259, 5045-5048)
+              double *vk = mon.vconst + si;
+              const double rf = (double)st.rf_loclake[si], ll = (double)c.ll100[s];   // G_loc_lake / 100
+              const double fll = (ll > 0. && rf > 0.) ? rf * ll : 0.;              // G_fLocLake
+              vk[3 * N] = vk[4 * N] + fll * 100. + vk[5 * N];
+            }
             vertical_at<R>(c, st, N, s, si, doy, Pin, gam, f.temp[fo], f.swrad[fo], laf,
-                           started == 1 ? laf_prev : laf, o, mo, (size_t)mon.nmonths * N);   // daily.cpp:159-169
+                           started == 1 ? laf_prev : laf, o, vo ? &vs : nullptr);   // daily.cpp:159-169
           } else {
             o.rs = v.rs[s]; o.gwr = v.gwr[s]; o.transfer = v.transfer[s]; o.owp = v.owp[s]; o.owpet = v.owpet[s];
             o.land_in = v.land_in[s]; o.land_evap = v.land_evap[s]; o.land_leak = v.land_leak[s];
@@ -725,7 +741,7 @@ cudaError_t launch_vertical_ahead(const DevCellsT<R> &c, const DevStateT<R> &s, 
   if (mem.members > 1)
     k_vertical_ahead<R, true><<<blocks, threads, 0, st>>>(c, s, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e, mon,
                                                           oday0);
-  else if (mon.vert && std::is_same<R, double>::value)
+  else if ((mon.vert || mon.dvert) && std::is_same<R, double>::value)
     k_vertical_ahead<R, false, true><<<blocks, threads, 0, st>>>(c, s, f, mem, b, ring, doy0, fday0, ndays, t_b, t_e,
                                                                  mon, oday0);
   else
@@ -811,7 +827,7 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
                   (void *)&idle_warp, (void *)&mon, (void *)&vwk, (void *)&wtp, (void *)&wu};
   const bool ens = mem.members > 1;
   const void *fn = pipeline_fn<R>(fused, ens, vaw, wtp.enabled != 0, wu.enabled != 0, wu.enabled && wu.glwd,
-                                  mon.vert != nullptr);
+                                  mon.vert != nullptr || mon.dvert != nullptr);
   if (!fn) return cudaErrorInvalidConfiguration;
   if (vaw) threads += 32 * vw.warps;
   // cooperative (all blocks resident, or the launch fails) through the launch

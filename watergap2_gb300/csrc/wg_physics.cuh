@@ -179,19 +179,31 @@ __device__ __forceinline__ R lai_nogrowing(int &days, int init, int &status, R l
   return lmax;
 }
 
+// Where one cell-day's output terms go (FP64): the sums of the day's month, field
+// k at mo[k * mos] (DevMonthly::vert; null: none), the day's values, field k at
+// dd[k * dds] (DevMonthly::dvert; null: none), and the cell's constants for Kc and
+// total PET, field k at vk[k * vks] (DevMonthly::vconst).
+struct VSink {
+  double *mo;
+  size_t mos;
+  double *dd;
+  size_t dds;
+  const double *vk;
+  size_t vks;
+};
+
 // dailyWaterBalanceClass::calcNewDay for one cell (daily.cpp:94-1257).
 //   c, s        : per-cell constants and the cell's slot
 //   gamma_soil  : runoff exponent (P_GAMRUN_C, times a member's factor in an ensemble)
 //   canopy ...  : the cell's state, read and written through references
 //   band        : the cell's snow bands, band[e * bstride]
 //   Pin         : precipitation (times a member's factor in an ensemble)
-//   OUT, mo, mos: the monthly output grids (FP64): the cell's entry of the day's
-//               month of field k at mo[k * mos] (DevMonthly::vert)
+//   OUT, vs     : the output grids (monthly and daily) of the cell-day
 template <class R, bool OUT = false>
 __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R gamma_soil, R &canopy, R &soil,
                                               R &gsnow, R *band, size_t bstride, int &days, int &status, R &psum,
                                               R landAreaFrac, R prevLAF, R Pin, float Tf, float SWf, R ext_rad,
-                                              R inv_s0, VOut<R> &o, double *mo = nullptr, size_t mos = 0) {
+                                              R inv_s0, VOut<R> &o, const VSink *vs = nullptr) {
   typedef M<R> m;
   const int B = c.nband;
   const R invB = c.invB;
@@ -236,39 +248,61 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   const R owPET = cmp::le0(ow_net_rad) ? R(0) : apet * ow_net_rad;
   o.owp = dailyPrec;
   o.owpet = owPET;
-  // the monthly output grids (daily.cpp:1281-1386, grid_store 2): sums over the
-  // month's days, each term filed as soon as it is known so that none stays live
-  // to the end of the cell-day.  Radiation in W/m2 (lat_heat / 0.0864 per
-  // mm/day); the land terms (fields 10-28) weighted by the day's land share of
-  // the continental area, zero without continental area (geo.cpp:52-60); the
-  // storages at the month's end (grid_store_TypeForStorages 0).  The reference
-  // divides each land term by contfreq; here one refined reciprocal of contfreq
-  // per cell-day and products with constants give the same values to a few ulp
-  // (a correctly rounded FP64 division costs about ten FP64-pipe operations, and
-  // the FP64 pipe bounds the step).
-  [[maybe_unused]] bool mcont = false;   // the cell has continental area
+  // the output grids: the monthly sums (daily.cpp:1281-1386, grid_store 2) and the
+  // day's values (daily.cpp:1388-1399, 1472-1540, grid_store 5/6), each term filed
+  // as soon as it is known so that none stays live to the end of the cell-day.
+  // Radiation in W/m2 (lat_heat / 0.0864 per mm/day); the land terms weighted by
+  // the day's land share of the continental area; the storages at the day's (the
+  // month's) end.  Only continental cells run this (cells without continental
+  // area run no vertical balance).  The reference divides each land term by
+  // contfreq; here one refined reciprocal of contfreq per cell-day and products
+  // with constants give the same values to a few ulp (a correctly rounded FP64
+  // division costs about ten FP64-pipe operations, and the FP64 pipe bounds the
+  // step).
   [[maybe_unused]] double mw = 0.;       // landAreaFrac / contfreq
   if constexpr (OUT) {
-    if (mo) {
+    if (vs) {
       const double conv = (double)lat_heat * (1.0 / 0.0864);
       const double ns = (double)solar_rad * (1. - (double)albedo);
-      mo[0] += (double)dailyPrec;
-      mo[mos] += (double)T;
-      mo[2 * mos] += (double)ext_rad * conv;
-      mo[3 * mos] += ((double)solar_rad - ns) * conv;
-      mo[4 * mos] += (double)solar_rad * conv;
-      mo[5 * mos] += ns * conv;
-      mo[6 * mos] += (double)net_lw * conv;
-      mo[7 * mos] += (double)net_rad * conv;
-      mo[8 * mos] += (double)owPET;
-      mo[9 * mos] += (double)dailyPET;
-      const double cf = (double)c.contfreq[s];
-      mcont = !(cf < 0.000001);
-      if (mcont) {
-        const double lf = (double)landAreaFrac, lf100 = lf * 0.01;
-        mw = lf * fm::rcp_pos(cf);
-        mo[13 * mos] += (double)dailyLai;
-        mo[14 * mos] += (double)albedo * lf100 + 0.08 * (1. - lf100);
+      const double cf = (double)c.contfreq[s], rcf = fm::rcp_pos(cf);
+      const double lf = (double)landAreaFrac, lf100 = lf * 0.01;
+      mw = lf * rcf;
+      // total PET over land and fresh water (daily.cpp:1303, 1484)
+      const double fw = vs->vk[3 * vs->vks];
+      const double tpet = ((cf - fw) * (double)dailyPET + fw * (double)owPET) * rcf;
+      const double alb = (double)albedo * lf100 + 0.08 * (1. - lf100);
+      if (double *m = vs->mo) {
+        const size_t k = vs->mos;
+        m[0] += (double)dailyPrec;
+        m[k] += (double)T;
+        m[2 * k] += (double)ext_rad * conv;
+        m[3 * k] += ((double)solar_rad - ns) * conv;
+        m[4 * k] += (double)solar_rad * conv;
+        m[5 * k] += ns * conv;
+        m[6 * k] += (double)net_lw * conv;
+        m[7 * k] += (double)net_rad * conv;
+        m[8 * k] += (double)owPET;
+        m[9 * k] += (double)dailyPET;
+        m[13 * k] += (double)dailyLai;
+        m[14 * k] += alb;
+        m[32 * k] += tpet;
+      }
+      if (double *dd = vs->dd) {
+        const size_t k = vs->dds;
+        const double *vk = vs->vk;
+        dd[0] = (double)dailyPrec;
+        dd[k] = (double)T;
+        dd[2 * k] = (double)dailyPET;
+        dd[3 * k] = tpet;
+        dd[4 * k] = (double)dailyLai;
+        dd[5 * k] = vk[0] + vk[vs->vks] * ((double)dailyLai - vk[2 * vs->vks]);   // lai.cpp:295-306
+        dd[6 * k] = alb;
+        dd[17 * k] = (double)ext_rad * conv;
+        dd[18 * k] = (double)solar_rad * conv;
+        dd[19 * k] = ((double)solar_rad - ns) * conv;
+        dd[20 * k] = ns * conv;
+        dd[21 * k] = (double)net_lw * conv;
+        dd[22 * k] = (double)net_rad * conv;
       }
     }
   }
@@ -321,10 +355,18 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   }
   if (cmp::lt0(soilPET)) soilPET = R(0);
   if constexpr (OUT) {
-    if (mo && mcont) {   // the canopy's terms: its state does not change after this
-      mo[15 * mos] += (double)canopyEvapo * mw;
-      mo[16 * mos] += (double)canopy * mw;
-      mo[17 * mos] += (double)out_maxcs * mw;
+    if (vs) {   // the canopy's terms: its state does not change after this
+      const double ic = (double)canopyEvapo * mw, cw = (double)canopy * mw, mx = (double)out_maxcs * mw;
+      if (double *m = vs->mo) {
+        m[15 * vs->mos] += ic;
+        m[16 * vs->mos] += cw;
+        m[17 * vs->mos] += mx;
+      }
+      if (double *dd = vs->dd) {
+        dd[7 * vs->dds] = ic;
+        dd[8 * vs->dds] = cw;
+        dd[9 * vs->dds] = mx;
+      }
     }
   }
 
@@ -425,15 +467,27 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   }
   gsnow = gs;
   if constexpr (OUT) {
-    if (mo && mcont) {   // the snow's terms
+    if (vs) {   // the snow's terms
       // per band of the cell's land (1 / bands), without land the sums are 0
       const double pb = (double)dailyPrec * (double)invB * mw, bw = (double)invB * mw;
-      mo[18 * mos] += (double)n_snowfall * pb;
-      mo[19 * mos] += (double)n_rainfall * pb;
-      mo[20 * mos] += (double)out_melt * bw;
-      mo[21 * mos] += (double)snowEvapo * mw;
-      mo[22 * mos] += (double)gsnow * mw;
-      mo[23 * mos] += (double)n_cover * bw;
+      const double sf = (double)n_snowfall * pb, sm = (double)out_melt * bw, swe = (double)gsnow * mw;
+      const double cov = (double)n_cover * bw;
+      if (double *m = vs->mo) {
+        const size_t k = vs->mos;
+        m[18 * k] += sf;
+        m[19 * k] += (double)n_rainfall * pb;
+        m[20 * k] += sm;
+        m[21 * k] += (double)snowEvapo * mw;
+        m[22 * k] += swe;
+        m[23 * k] += cov;
+      }
+      if (double *dd = vs->dd) {
+        const size_t k = vs->dds;
+        dd[10 * k] = sf;
+        dd[11 * k] = sm;
+        dd[12 * k] = swe;
+        dd[13 * k] = cov;
+      }
     }
   }
 
@@ -520,21 +574,33 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
   o.land_evap = cellAET;
   o.land_leak = leak;
   if constexpr (OUT) {
-    if (mo && !mcont) {
-      for (int k = 10; k < 29; ++k) mo[(size_t)k * mos] = 0.;
-    } else if (mo) {   // the soil's terms and the storages at the month's end
-      mo[10 * mos] += (double)dailyAET * mw;
-      mo[11 * mos] += (double)cellAET * mw;
-      mo[12 * mos] += ((double)dailyAET + (double)canopyEvapo + (double)snowEvapo) * mw;
-      mo[24 * mos] += (double)soil * mw;
-      mo[25 * mos] += (double)total * mw;
-      mo[26 * mos] += (double)immediate;
-      mo[27 * mos] += ((double)total - (double)gwr) * mw;
-      mo[28 * mos] += (double)gwr * mw;
+    if (vs) {   // the soil's terms and the storages at the day's end
+      const double sw = (double)soil * mw, sr = ((double)total - (double)gwr) * mw, gr = (double)gwr * mw;
       const double a = (double)c.area[s] * (double)landAreaFrac * 1e-8;   // area [km2] / 1e6 * landAreaFrac / 100
-      mo[29 * mos] = (double)canopy * a;
-      mo[30 * mos] = (double)gsnow * a;
-      mo[31 * mos] = (double)soil * a;
+      const double cs = (double)canopy * a, ss = (double)gsnow * a, ls = (double)soil * a;
+      if (double *m = vs->mo) {
+        const size_t k = vs->mos;
+        m[10 * k] += (double)dailyAET * mw;
+        m[11 * k] += (double)cellAET * mw;
+        m[12 * k] += ((double)dailyAET + (double)canopyEvapo + (double)snowEvapo) * mw;
+        m[24 * k] += sw;
+        m[25 * k] += (double)total * mw;
+        m[26 * k] += (double)immediate;
+        m[27 * k] += sr;
+        m[28 * k] += gr;
+        m[29 * k] = cs;
+        m[30 * k] = ss;
+        m[31 * k] = ls;
+      }
+      if (double *dd = vs->dd) {
+        const size_t k = vs->dds;
+        dd[14 * k] = sw;
+        dd[15 * k] = sr;
+        dd[16 * k] = gr;
+        dd[23 * k] = cs;
+        dd[24 * k] = ss;
+        dd[25 * k] = ls;
+      }
     }
   }
 }

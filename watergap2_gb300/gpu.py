@@ -39,7 +39,7 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_upload_water_use", "wg_set_water_use_inputs", "wg_get_water_use", "wg_set_water_use",
            "wg_model_options_default", "wg_get_member_discharge", "wg_set_deferred",
            "wg_record_daily_storages", "wg_get_daily_storages", "wg_upload_forcing_cells",
-           "wg_monthly_outputs_vertical")
+           "wg_monthly_outputs_vertical", "wg_daily_outputs_vertical", "wg_get_daily_vertical")
 
 
 class WgError(RuntimeError):
@@ -49,7 +49,9 @@ class WgError(RuntimeError):
 class _Region(ctypes.Structure):
     _fields_ = [("ncell", ctypes.c_int32), ("nband", ctypes.c_int32), ("river_velo_opt", ctypes.c_int32),
                 ("frac_routing", ctypes.c_int32), ("default_velocity", ctypes.c_double)] + \
-               [(name, ctypes.c_void_p) for name, _, _ in FIELDS] + [("glwd_unit", ctypes.c_void_p)]
+               [(name, ctypes.c_void_p) for name, _, _ in FIELDS] + [("glwd_unit", ctypes.c_void_p),
+                                                                      ("lct_kc_min", ctypes.c_void_p),
+                                                                      ("lct_kc_max", ctypes.c_void_p)]
 
 
 class _StateView(ctypes.Structure):
@@ -141,6 +143,10 @@ def load_library(path: str = LIB_PATH):
     lib.wg_monthly_outputs.argtypes = [vp, i32, i32]
     lib.wg_monthly_outputs_vertical.argtypes = [vp, i32]
     lib.wg_monthly_outputs_vertical.restype = i32
+    lib.wg_daily_outputs_vertical.argtypes = [vp, i32]
+    lib.wg_daily_outputs_vertical.restype = i32
+    lib.wg_get_daily_vertical.argtypes = [vp, i32, i32, i32, vp]
+    lib.wg_get_daily_vertical.restype = i32
     lib.wg_set_step_sync.argtypes = [vp, i32]
     lib.wg_get_monthly.argtypes = [vp, i32, i32, i32, vp]
     lib.wg_read_unf.argtypes = [ctypes.c_char_p, vp, i64]
@@ -255,6 +261,13 @@ class Model:
                 raise ValueError("glwd_unit is one unit per cell")
             self._keep.append(u)
             r.glwd_unit = u.ctypes.data
+        # the land covers' crop coefficients (LAI_22.DAT), for the daily grids' Kc
+        tabs = getattr(region, "lct_tables", None) or {}
+        if "kc_min" in tabs and "kc_max" in tabs:
+            for name in ("kc_min", "kc_max"):
+                t = np.ascontiguousarray(tabs[name], np.float64)
+                self._keep.append(t)
+                setattr(r, "lct_" + name, t.ctypes.data)
         self.stations = np.ascontiguousarray(
             np.nonzero(region.downstream < 0)[0] if stations is None else stations, np.int32)
         o = _Options()
@@ -495,8 +508,27 @@ class Model:
                         "net_rad", "open_water_pet", "pet", "aet", "land_aet", "land_aet_uncorr", "lai", "albedo",
                         "interception", "canopy_wc", "max_canopy_wc", "snowfall", "rainfall", "snowmelt",
                         "snow_evap", "swe", "snow_cover", "soil_wc", "runoff", "urban_runoff", "surface_runoff",
-                        "gw_recharge", "canopy_storage", "snow_storage", "soil_storage"]
+                        "gw_recharge", "canopy_storage", "snow_storage", "soil_storage", "total_pet"]
     MONTHLY.update({k: 6 + i for i, k in enumerate(MONTHLY_VERTICAL)})
+    # the vertical balance's daily grids (wg_daily_outputs_vertical), field = index
+    DAILY_VERTICAL = ["prec", "temp", "pet", "total_pet", "lai", "kc", "albedo", "interception", "canopy_wc",
+                      "max_canopy_wc", "snowfall", "snowmelt", "swe", "snow_cover", "soil_wc", "surface_runoff",
+                      "gw_recharge", "ext_rad", "short_down_rad", "short_up_rad", "net_short_rad", "net_long_rad",
+                      "net_rad", "canopy_storage", "snow_storage", "soil_storage"]
+
+    def daily_outputs_vertical(self, ndays: int):
+        """wg_daily_outputs_vertical: the vertical balance's daily grids for output
+        days 0 .. ndays-1 (0: off)."""
+        self._check(self.lib.wg_daily_outputs_vertical(self.h, int(ndays)), "daily_outputs_vertical")
+        self.daily_days = int(ndays)
+
+    def daily_vertical(self, name: str, day0: int = 0, nd: int | None = None) -> np.ndarray:
+        """[nd, ncell] daily grid, cell order."""
+        nd = self.daily_days - day0 if nd is None else nd
+        out = np.zeros((nd, self.region.ncell))
+        self._check(self.lib.wg_get_daily_vertical(self.h, self.DAILY_VERTICAL.index(name), int(day0), int(nd),
+                                                   _ptr(out)), "get_daily_vertical")
+        return out
 
     def monthly_outputs(self, nmonths: int, doy_day0: int = 1):
         """wg_monthly_outputs: accumulate monthly aggregates for nmonths months."""
