@@ -460,8 +460,31 @@ wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable);
  * the continental area], 29 CanopyStorage, 30 SnowStorage, 31 SoilStorage at
  * the month's end [km3], 32 TotalPET [mm] (daily.cpp:1303: PET over the land
  * and open-water PET over the freshwater share of the continental area);
+ * 39 + k: field k of routing's further grids (wg_monthly_outputs_routing):
+ * 0 G_monthlyOpenWaterEvap [mm], 1 CellSurfaceRunoff [mm], 2 GwRunoff [km3],
+ * 3 LandAreaFrac [% x days], 4 LocWetlExtent and 5 GloWetlExtent [km2 x days],
+ * 6 ResInflow and 7 ResOutflow [km3] (twice the month's flows, as the reference
+ * adds them twice a day, routing.cpp:4049-4050 and 4653-4655), 8 ConsistentPrecip
+ * [km3], 9 SurfStor at the
+ * month's end [km3]; 49 CellAET [mm] and 50 CellAETWCa [km3] (routing.cpp:
+ * 4572-4580; both sets of grids needed);
  * out [nm][ncell][members], cell order. */
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out);
+/* Routing's further monthly grids (routing.cpp:3964-4238, 4525-4737, 5183-5186,
+ * grid_store = 2), on the calendar of wg_monthly_outputs: the same conditions as
+ * wg_monthly_outputs_vertical, and without fractional routing
+ * (WG_ERR_UNSUPPORTED).  enable 0 switches them off. */
+wg_status wg_monthly_outputs_routing(wg_ctx *ctx, int32_t enable);
+/* Routing's daily grids (routing.cpp:4113-4210, 4620-4634, grid_store 5/6) for
+ * output days 0 .. ndays-1; conditions as wg_monthly_outputs_routing; 0 days
+ * switches them off.  A cell without continental area keeps 0. */
+wg_status wg_daily_outputs_routing(wg_ctx *ctx, int32_t ndays);
+/* field: 0 G_daily365RiverAvail [km3] (0 in inland sinks), 1 Velocity [m/s],
+ * 2 CellRunoff [km3], 3 CellRunoff_mm, 4 CellSurfaceRunoff [mm], 5 GwRunoff [km3],
+ * 6 LandAreaFrac [%], 7 ConsistentPrecip [km3], 8 the open-water evaporation
+ * [mm], 9 CellAET [mm] (field 8 plus the vertical balance's daily land AET:
+ * wg_daily_outputs_vertical needed); out [nd][ncell], cell order. */
+wg_status wg_get_daily_routing(wg_ctx *ctx, int32_t field, int32_t day0, int32_t nd, double *out);
 
 /* The vertical balance's daily grids (daily.cpp:1388-1399, 1472-1540: the
  * reference's grid_store 5/6 with the daily output options on) for output days
@@ -480,7 +503,9 @@ wg_status wg_daily_outputs_vertical(wg_ctx *ctx, int32_t ndays);
  * 15 SurfaceRunoff, 16 GwRecharge [mm, water terms weighted by the land share of
  * the continental area], 17 ExtRad, 18 ShortDownRad, 19 ShortUpRad,
  * 20 NetShortRad, 21 NetLongRad, 22 NetRadiation [W/m2], 23 CanopyStorage,
- * 24 SnowStorage, 25 SoilStorage [km3]; out [nd][ncell], cell order. */
+ * 24 SnowStorage, 25 SoilStorage [km3], 26 land AET [mm] (dailyCellLandAET times
+ * the land share of the continental area: the land part of routing's cell AET);
+ * out [nd][ncell], cell order. */
 wg_status wg_get_daily_vertical(wg_ctx *ctx, int32_t field, int32_t day0, int32_t nd, double *out);
 
 /* Cells the day step runs (cell order, nonzero = run; NULL = all).  A skipped

@@ -90,7 +90,7 @@ class Context {
   void monthly_outputs(int nmonths, int doy_day0) {
     check(wg_monthly_outputs(ctx_, nmonths, doy_day0), "wg_monthly_outputs");
   }
-  // the vertical balance's 32 monthly grids as well (which 6..37 of monthly())
+  // the vertical balance's 33 monthly grids as well (which 6..38 of monthly())
   void monthly_outputs_vertical(bool enable) {
     check(wg_monthly_outputs_vertical(ctx_, enable ? 1 : 0), "wg_monthly_outputs_vertical");
   }
@@ -103,6 +103,14 @@ class Context {
   }
   void daily_vertical(int field, int day0, int nd, double *out) {
     check(wg_get_daily_vertical(ctx_, field, day0, nd, out), "wg_get_daily_vertical");
+  }
+  // routing's further monthly grids (which 39..50 of monthly()) and its daily grids
+  void monthly_outputs_routing(bool enable) {
+    check(wg_monthly_outputs_routing(ctx_, enable ? 1 : 0), "wg_monthly_outputs_routing");
+  }
+  void daily_outputs_routing(int ndays) { check(wg_daily_outputs_routing(ctx_, ndays), "wg_daily_outputs_routing"); }
+  void daily_routing(int field, int day0, int nd, double *out) {
+    check(wg_get_daily_routing(ctx_, field, day0, nd, out), "wg_get_daily_routing");
   }
   // water temperature (wg_options.water_temp = 1)
   void upload_longwave(int day0, int ndays, const float *longwave) {

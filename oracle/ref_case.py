@@ -88,7 +88,12 @@ DAILY_VERTICAL = ["prec", "temp", "pet", "total_pet", "lai", "kc", "albedo", "in
                   "net_rad", "canopy_storage", "snow_storage", "soil_storage"]
 MONTHLY_ROUTING = ["river_avail", "min_river_avail", "max_river_avail", "cell_runoff", "velocity", "loclake_storage",
                    "locwetl_storage", "glolake_storage", "glowetl_storage", "res_storage", "river_storage",
-                   "gw_storage"]
+                   "gw_storage", "open_water_evap", "cell_surface_runoff", "gw_runoff", "land_area_frac",
+                   "loc_wetl_extent", "glo_wetl_extent", "res_inflow", "res_outflow", "consistent_precip",
+                   "surf_storage", "cell_aet", "cell_aet_wca"]
+# routing's daily 365 grids the harness dumps with outputs=2
+DAILY_ROUTING = ["river_avail", "velocity", "cell_runoff", "cell_runoff_mm", "cell_surface_runoff", "gw_runoff",
+                 "land_area_frac", "consistent_precip", "cell_aet"]
 
 
 def write_case(region, d: str, P, T, S, doy0: int, stations, snapshots, year0: int = 2000, wtemp=None, wuse=None,
@@ -269,7 +274,7 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
             o += 12 * n
     if outputs == 2:   # the year's daily grids [365][ncell] per field
         res["daily"] = {}
-        for f in DAILY_VERTICAL:
+        for f in DAILY_VERTICAL + ["r_" + k for k in DAILY_ROUTING]:
             res["daily"][f] = raw[o:o + 365 * n].reshape(365, n).copy()
             o += 365 * n
     assert o == raw.size, (o, raw.size)

@@ -112,6 +112,10 @@ int main(int argc, char **argv) {
     options.outExtRadiationDaily = 1; options.outShortDownRadiationDaily = 1; options.outShortUpRadiationDaily = 1;
     options.outNetShortWaveRadiationDaily = 1; options.outNetLongWaveRadiationDaily = 1;
     options.outNetRadiationDaily = 1; options.outSingleStoragesDaily = 1;
+    // and routing's daily grids (routing.cpp:4113-4210, 4620-4634)
+    options.outRiverAvailDaily = 1; options.outRiverVeloDaily = 1; options.outCellRunoffDaily = 1;
+    options.outCellSurfaceDaily = 1; options.outGWRunoffDaily = 1; options.outLandAreaFracDaily = 1;
+    options.outCellAETDaily = 1;
   }
   options.glacierOpt = 0; options.calc_wtemp = wtemp; options.start_year = year0; options.end_year = year0;
   options.init_years = 0; options.time_step = 1; options.outLAImax = 0;
@@ -342,7 +346,12 @@ int main(int argc, char **argv) {
         &routing.G_monthlyRiverAvail, &routing.G_monthlyMinRiverAvail, &routing.G_monthlyMaxRiverAvail,
         &routing.G_monthlyCellRunoff, &routing.G_monthlyVelocity, &routing.G_monthlyLocLakeStorage,
         &routing.G_monthlyLocWetlStorage, &routing.G_monthlyGloLakeStorage, &routing.G_monthlyGloWetlStorage,
-        &routing.G_monthlyResStorage, &routing.G_monthlyRiverStorage, &routing.G_monthlyGwStorage};
+        &routing.G_monthlyResStorage, &routing.G_monthlyRiverStorage, &routing.G_monthlyGwStorage,
+        // routing's further grids (routing.cpp:3964-4238, 4525-4737, 5183-5186)
+        &routing.G_monthlyOpenWaterEvap, &routing.G_monthlyCellSurfaceRunoff, &routing.G_monthlyGwRunoff,
+        &routing.G_monthlyLandAreaFrac, &routing.G_monthlyLocWetlExtent, &routing.G_monthlyGloWetlExtent,
+        &routing.G_monthlyResInflow, &routing.G_monthlyResOutflow, &routing.G_monthlyConsistentPrecip,
+        &routing.G_monthlySurfStor, &routing.G_monthlyCellAET, &routing.G_monthlyCellAETWCa};
     std::vector<double> buf((size_t)12 * ncase);
     auto dump = [&](auto *g) {
       for (int m = 0; m < 12; m++)
@@ -364,12 +373,18 @@ int main(int argc, char **argv) {
         &w.G_daily365ExtRad, &w.G_daily365ShortDownRad, &w.G_daily365ShortUpRad, &w.G_daily365NetShortRad,
         &w.G_daily365NetLongRad, &w.G_daily365NetRadiation, &w.G_daily365CanopyStorage, &w.G_daily365SnowStorage,
         &w.G_daily365SoilStorage};
+    const DailyGrid<false> *drout[] = {
+        &routing.G_daily365RiverAvail, &routing.G_daily365Velocity, &routing.G_daily365CellRunoff,
+        &routing.G_daily365CellRunoff_mm, &routing.G_daily365CellSurfaceRunoff, &routing.G_daily365GwRunoff,
+        &routing.G_daily365LandAreaFrac, &routing.G_daily365ConsistentPrecip, &routing.G_daily365CellAET};
     std::vector<double> buf((size_t)365 * ncase);
-    for (auto *g : dvert) {
+    auto dump_day = [&](const DailyGrid<false> *g) {
       for (int d = 0; d < 365; d++)
         for (int n = 0; n < ncase; n++) buf[(size_t)d * ncase + n] = (*g)(n, d);
       write_raw(out, buf.data(), buf.size());
-    }
+    };
+    for (auto *g : dvert) dump_day(g);
+    for (auto *g : drout) dump_day(g);
   }
   fclose(out);
   if (FILE *tf = fopen((dir + "/timing.txt").c_str(), "w")) {

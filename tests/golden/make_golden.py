@@ -288,7 +288,7 @@ def main_outputs(names=None, name="swb_outputs_730d"):
     # every 13th day, the last day), to keep the fixture small
     days = np.unique(np.r_[0:3, 31:34, np.arange(0, 365, 13), 364])
     extra["daily_days"] = days
-    for k, v in res["daily"].items():
+    for k, v in res["daily"].items():   # the vertical balance's as d_<field>, routing's as d_r_<field>
         extra[f"d_{k}"] = v[days]
     path = os.path.join(HERE, f"{name}.npz")
     save_npz(region, path, **extra)

@@ -7,8 +7,12 @@ water-body type and inland sinks: the vertical balance's 29 monthly sums and
 means (daily.cpp:1281-1386) with total PET (1303) and its canopy, snow and soil
 storages at the month's end; routing's river availability with its minimum and
 maximum, cell runoff and velocity (routing.cpp:3964-4040) and every routing
-storage at the month's end (routing.cpp:4725-4737); and the vertical balance's
-26 daily grids (daily.cpp:1388-1399, 1472-1540) on a sample of days.
+storage at the month's end (routing.cpp:4725-4737) and routing's further grids
+(open-water evaporation, cell surface runoff, groundwater runoff, land-area
+fraction, wetland extents, reservoir inflow and outflow, consistent
+precipitation, surface storage, cell AET); and the daily grids of both
+(daily.cpp:1388-1399, 1472-1540; routing.cpp:4113-4210, 4620-4634) on a sample
+of days.
 
 Tolerance (FP64): 1e-10 relative to each grid's values, elements below 1e-6 of
 the grid's largest value compared against that floor (helpers.max_rel_err).
@@ -39,7 +43,7 @@ def _built():
         build.build()
 
 
-def _two_years(days_per_step=0, deferred=False):
+def _two_years(days_per_step=0, deferred=False, routing=True):
     from watergap2_gb300.gpu import Model
     from watergap2_gb300.region import load_npz
     region, ex = load_npz(PATH)
@@ -49,6 +53,9 @@ def _two_years(days_per_step=0, deferred=False):
     m.monthly_outputs(24, doy_day0=1)
     m.monthly_outputs_vertical(True)
     m.daily_outputs_vertical(nd)
+    if routing:
+        m.monthly_outputs_routing(True)
+        m.daily_outputs_routing(nd)
     m.record_daily_storages(True)
     m.upload_forcing(0, P, T, S)
     if deferred:                                       # per-day calls, queued into day-pipelined runs
@@ -61,12 +68,18 @@ def _two_years(days_per_step=0, deferred=False):
         m.run_days(1, 0, nd)
     grids = {k: m.monthly(k, 12, 12) for k in m.MONTHLY_VERTICAL + list(ROUTING)}
     grids.update({"d_" + k: m.daily_vertical(k, Y2, 365) for k in m.DAILY_VERTICAL})
+    if routing:
+        grids.update({k: m.monthly(k, 12, 12) for k in m.MONTHLY_ROUTING + ["cell_aet", "cell_aet_wca"]})
+        grids.update({"d_r_" + k: m.daily_routing(k, Y2, 365) for k in m.DAILY_ROUTING})
     return m, ex, grids
 
 
-@pytest.mark.parametrize("dps", [1, 5])
-def test_output_grids_match_reference(dps):
-    m, ex, grids = _two_years(days_per_step=dps)
+@pytest.mark.parametrize("dps,routing", [(1, True), (5, True), (5, False)])
+def test_output_grids_match_reference(dps, routing):
+    """All grids (routing's further grids with the vertical balance's: the
+    wavefront's variant with both), and the vertical balance's grids alone (its
+    variant without routing's further terms)."""
+    m, ex, grids = _two_years(days_per_step=dps, routing=routing)
     errs = {k: max_rel_err(grids[k], ex["m_" + k]) for k in m.MONTHLY_VERTICAL}
     errs.update({k: max_rel_err(grids[k], ex["m_" + r]) for k, r in ROUTING.items()})
     ds = m.daily_storages(Y2, 365)
@@ -74,7 +87,14 @@ def test_output_grids_match_reference(dps):
         errs[f + "_storage"] = max_rel_err(ds[MONTH_END, i], ex[f"m_{f}_storage"])
     days = ex["daily_days"]
     for k in m.DAILY_VERTICAL:
-        errs["d_" + k] = max_rel_err(grids["d_" + k][days], ex["d_" + k])
+        if k != "land_aet":   # not a grid of the reference's
+            errs["d_" + k] = max_rel_err(grids["d_" + k][days], ex["d_" + k])
+    if routing:
+        for k in m.MONTHLY_ROUTING + ["cell_aet", "cell_aet_wca"]:
+            errs[k] = max_rel_err(grids[k], ex["m_" + k])
+        for k in m.DAILY_ROUTING:
+            if k != "open_water_evap":   # not a grid of the reference's
+                errs["d_r_" + k] = max_rel_err(grids["d_r_" + k][days], ex["d_r_" + k])
     bad = {k: v for k, v in errs.items() if not v <= RTOL}
     assert not bad, bad
     q = m.discharge(0, 730)
@@ -89,6 +109,18 @@ def test_output_grids_deferred_per_day_calls_same_bits():
     _, _, b = _two_years(deferred=True)
     for k in a:
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_routing_grids_refused_with_fractional_routing():
+    from watergap2_gb300.gpu import Model, WgError
+    from watergap2_gb300.region import load_npz
+    region, _ = load_npz(PATH)
+    m = Model(region.with_options(frac_routing=1), max_days=4)
+    with pytest.raises(WgError):
+        m.monthly_outputs_routing(True)
+    with pytest.raises(WgError):
+        m.daily_outputs_routing(4)
+    m.monthly_outputs_vertical(True)                   # the vertical balance's grids run with it
 
 
 def test_daily_grids_refused_without_kc():

@@ -1044,6 +1044,9 @@ wg_status wg_create(const wg_region *r, const wg_options *opt, wg_ctx **out) {
          PCRITGWA = 21, GWOUTF = 22, PREC = 25 };
   HostConsts h;
   ctx->has_kc = r->lct_kc_min && r->lct_kc_max;
+  ctx->cell_area.assign(r->area_km2, r->area_km2 + n);
+  ctx->cell_cont.resize(n);
+  for (int i = 0; i < n; ++i) ctx->cell_cont[i] = cont_share(r, i);
   ctx->vstatic.assign((size_t)(wg::VCONST_FIELDS + 1) * n, 0.);
   h.flags.resize(n); h.ext_row.resize(n); h.station.assign(n, -1); h.init_days.resize(n); h.start_month.resize(n);
 #define X(f) h.f.assign(n, 0.);
@@ -2080,6 +2083,10 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
     cudaFree(ctx->mon_vbuf);
     ctx->mon_vbuf = nullptr;
   }
+  if (ctx->mon_rbuf) {
+    cudaFree(ctx->mon_rbuf);
+    ctx->mon_rbuf = nullptr;
+  }
   {   // the daily storage record and the daily grids are kept
     const DevMonthly keep = ctx->mon;
     ctx->mon = DevMonthly{};
@@ -2088,6 +2095,8 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
     ctx->mon.dvert = keep.dvert;
     ctx->mon.dvert_days = keep.dvert_days;
     ctx->mon.vconst = keep.vconst;
+    ctx->mon.drout = keep.drout;
+    ctx->mon.drout_days = keep.drout_days;
   }
   if (nmonths == 0) return WG_OK;
   const size_t per = (size_t)nmonths * ctx->nstate();
@@ -2115,8 +2124,91 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
     if (e == cudaSuccess) e = vconst_upload(ctx);
     if (e == cudaSuccess) m.vert = ctx->mon_vbuf;
   }
+  if (e == cudaSuccess && ctx->mon_rout_on) {   // routing's further grids, on the same calendar
+    const size_t b = (size_t)wg::ROUT_FIELDS * per * sizeof(double);
+    e = cudaMalloc((void **)&ctx->mon_rbuf, b);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->mon_rbuf, 0, b, ctx->stream);
+    if (e == cudaSuccess) e = vconst_upload(ctx);
+    if (e == cudaSuccess) m.rext = ctx->mon_rbuf;
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return cuda_fail(ctx, e, "monthly_outputs");
+}
+
+// the output grids' conditions: FP64, one member, without water temperature or
+// water use; routing's further grids also without fractional routing (its
+// groundwater runoff splits between the river and the water bodies)
+static wg_status outputs_supported(const wg_ctx *ctx, bool routing) {
+  if (ctx->precision != 0 || ctx->members != 1 || ctx->wt.enabled || ctx->wu.enabled) return WG_ERR_UNSUPPORTED;
+  if (routing && ctx->frac_routing) return WG_ERR_UNSUPPORTED;
+  return WG_OK;
+}
+
+wg_status wg_monthly_outputs_routing(wg_ctx *ctx, int32_t enable) {
+  if (!ctx) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
+  if (enable) {
+    const wg_status st = outputs_supported(ctx, true);
+    if (st != WG_OK) return st;
+  }
+  ctx->mon_rout_on = enable != 0;
+  if (!ctx->mon.enabled) return WG_OK;   // takes effect with wg_monthly_outputs
+  return wg_monthly_outputs(ctx, ctx->mon.nmonths, ctx->mon.doy_day0);
+}
+
+wg_status wg_daily_outputs_routing(wg_ctx *ctx, int32_t ndays) {
+  if (!ctx || ndays < 0) return WG_ERR_INVALID;
+  WG_FLUSH(ctx);
+  if (ndays > 0) {
+    const wg_status st = outputs_supported(ctx, true);
+    if (st != WG_OK) return st;
+  }
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "daily_outputs_routing");
+  if (ctx->mon_drbuf) {
+    cudaFree(ctx->mon_drbuf);
+    ctx->mon_drbuf = nullptr;
+  }
+  ctx->mon.drout = nullptr;
+  ctx->mon.drout_days = 0;
+  if (ndays == 0) return WG_OK;
+  const size_t bytes = (size_t)wg::DROUT_FIELDS * ndays * (size_t)ctx->n * sizeof(double);
+  e = cudaMalloc((void **)&ctx->mon_drbuf, bytes);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->mon_drbuf, 0, bytes, ctx->stream);
+  if (e == cudaSuccess) e = vconst_upload(ctx);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "daily_outputs_routing");
+  ctx->mon.drout = ctx->mon_drbuf;
+  ctx->mon.drout_days = ndays;
+  return WG_OK;
+}
+
+wg_status wg_get_daily_routing(wg_ctx *ctx, int32_t field, int32_t day0, int32_t nd, double *out) {
+  if (!ctx || !out || field < 0 || field > wg::DROUT_FIELDS || day0 < 0 || nd < 0 || day0 + nd > ctx->mon.drout_days)
+    return WG_ERR_INVALID;
+  // the cell AET (field DROUT_FIELDS) adds the land part from the vertical balance's daily grids
+  if (field == wg::DROUT_FIELDS && (!ctx->mon.dvert || day0 + nd > ctx->mon.dvert_days)) return WG_ERR_UNSUPPORTED;
+  WG_FLUSH(ctx);
+  wg_status st = wg_synchronize(ctx);
+  if (st != WG_OK) return st;
+  const size_t N = (size_t)ctx->n;
+  std::vector<double> buf((size_t)nd * N), land;
+  const int f = field == wg::DROUT_FIELDS ? 8 : field;
+  cudaError_t e = cudaMemcpy(buf.data(), ctx->mon_drbuf + ((size_t)f * ctx->mon.drout_days + day0) * N,
+                             buf.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && field == wg::DROUT_FIELDS) {
+    land.resize(buf.size());
+    e = cudaMemcpy(land.data(), ctx->mon_dbuf + ((size_t)26 * ctx->mon.dvert_days + day0) * N,
+                   land.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+      for (size_t k = 0; k < buf.size(); ++k) buf[k] += land[k];
+  }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "get_daily_routing");
+  const auto &c2s = ctx->topo.cell_of_slot;
+  for (int d = 0; d < nd; ++d)
+    for (size_t sl = 0; sl < N; ++sl) out[(size_t)d * N + c2s[sl]] = buf[(size_t)d * N + sl];
+  return WG_OK;
 }
 
 // The output grids' constants on the device (DevMonthly::vconst), in slot order:
@@ -2152,8 +2244,10 @@ static cudaError_t vconst_upload(wg_ctx *ctx) {
 wg_status wg_daily_outputs_vertical(wg_ctx *ctx, int32_t ndays) {
   if (!ctx || ndays < 0) return WG_ERR_INVALID;
   WG_FLUSH(ctx);
-  if (ndays > 0 && (ctx->precision != 0 || ctx->members != 1 || ctx->wt.enabled || ctx->wu.enabled))
-    return WG_ERR_UNSUPPORTED;
+  if (ndays > 0) {
+    const wg_status st = outputs_supported(ctx, false);
+    if (st != WG_OK) return st;
+  }
   if (ndays > 0 && !ctx->has_kc) {
     ctx->err = "the daily grids need the region's lct_kc_min and lct_kc_max (Kc)";
     return WG_ERR_INVALID;
@@ -2200,25 +2294,48 @@ wg_status wg_get_daily_vertical(wg_ctx *ctx, int32_t field, int32_t day0, int32_
 wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable) {
   if (!ctx) return WG_ERR_INVALID;
   WG_FLUSH(ctx);
-  if (enable && (ctx->precision != 0 || ctx->members != 1 || ctx->wt.enabled || ctx->wu.enabled))
-    return WG_ERR_UNSUPPORTED;
+  if (enable) {
+    const wg_status st = outputs_supported(ctx, false);
+    if (st != WG_OK) return st;
+  }
   ctx->mon_vert_on = enable != 0;
   if (!ctx->mon.enabled) return WG_OK;   // takes effect with wg_monthly_outputs
   return wg_monthly_outputs(ctx, ctx->mon.nmonths, ctx->mon.doy_day0);
 }
 
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out) {
-  if (!ctx || !out || which < 0 || which >= 6 + wg::VOUT_FIELDS || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths)
+  constexpr int V0 = 6, R0 = V0 + wg::VOUT_FIELDS, AET = R0 + wg::ROUT_FIELDS;   // 6, 39, 49
+  if (!ctx || !out || which < 0 || which > AET + 1 || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths)
     return WG_ERR_INVALID;
-  if (which >= 6 && !ctx->mon.vert) return WG_ERR_UNSUPPORTED;
+  if (which >= V0 && which < R0 && !ctx->mon.vert) return WG_ERR_UNSUPPORTED;
+  if (which >= R0 && !ctx->mon.rext) return WG_ERR_UNSUPPORTED;
+  if (which >= AET && !ctx->mon.vert) return WG_ERR_UNSUPPORTED;   // cell AET: land AET + open-water evaporation
   WG_FLUSH(ctx);
   wg_status st = wg_synchronize(ctx);
   if (st != WG_OK) return st;
   const size_t N = ctx->nstate(), per = (size_t)ctx->mon.nmonths * N;
   const int M = ctx->members;
   std::vector<double> buf((size_t)nm * N);
-  const double *src = which < 6 ? ctx->mon_buf + which * per : ctx->mon_vbuf + (size_t)(which - 6) * per;
+  auto grid = [&](int w) -> const double * {
+    return w < V0 ? ctx->mon_buf + w * per
+                  : (w < R0 ? ctx->mon_vbuf + (size_t)(w - V0) * per : ctx->mon_rbuf + (size_t)(w - R0) * per);
+  };
+  const double *src = grid(which >= AET ? R0 : which);
   cudaError_t e = cudaMemcpy(buf.data(), src + (size_t)m0 * N, buf.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && which >= AET) {
+    // G_monthlyCellAET [mm] (routing.cpp:4572-4580): the land AET grid (field 11)
+    // plus the open-water evaporation; G_monthlyCellAETWCa [km3] the same over
+    // the continental area
+    std::vector<double> land(buf.size());
+    e = cudaMemcpy(land.data(), grid(V0 + 11) + (size_t)m0 * N, land.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    for (size_t k = 0; k < buf.size(); ++k) buf[k] += land[k];
+    if (which == AET + 1)
+      for (int k = 0; k < nm; ++k)
+        for (int sl = 0; sl < ctx->n; ++sl) {
+          const int c = ctx->topo.cell_of_slot[sl];
+          buf[(size_t)k * N + sl] *= ctx->cell_area[c] * ctx->cell_cont[c] * 1e-8;
+        }
+  }
   if (e != cudaSuccess) return cuda_fail(ctx, e, "get_monthly");
   if (which == 2 || which == 3)   // no day in the month, or an inland sink: 0, as the reference's reset grids
     for (double &v : buf)

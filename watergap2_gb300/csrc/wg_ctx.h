@@ -72,11 +72,15 @@ struct wg_ctx {
   double *mon_vbuf = nullptr;              // the vertical balance's monthly grids (wg_monthly_outputs_vertical)
   bool mon_vert_on = false;
   double *mon_dbuf = nullptr;              // its daily grids (wg_daily_outputs_vertical)
+  double *mon_rbuf = nullptr;              // routing's further monthly grids (wg_monthly_outputs_routing)
+  bool mon_rout_on = false;
+  double *mon_drbuf = nullptr;             // routing's daily grids (wg_daily_outputs_routing)
   double *mon_vconst = nullptr;            // their constants (DevMonthly::vconst)
   // [7][n] cell order, from wg_create: the grids' constants (DevMonthly::vconst,
   // the first year's freshwater share) and G_loc_lake / 100
   std::vector<double> vstatic;
   bool has_kc = false;                     // the region gave the LCT crop coefficients
+  std::vector<double> cell_area, cell_cont;   // cell order: area [km2], continental share [%] as raised
   double *daily_storage_buf = nullptr;     // wg_record_daily_storages (context allocation)
   double *outq = nullptr, *qst = nullptr, *vol0 = nullptr, *partial = nullptr;
   float *staging = nullptr;
@@ -149,6 +153,8 @@ struct wg_ctx {
     if (mon_buf) cudaFree(mon_buf);
     if (mon_vbuf) cudaFree(mon_vbuf);
     if (mon_dbuf) cudaFree(mon_dbuf);
+    if (mon_rbuf) cudaFree(mon_rbuf);
+    if (mon_drbuf) cudaFree(mon_drbuf);
     if (mon_vconst) cudaFree(mon_vconst);
     for (void *p : allocs) cudaFree(p);
     if (own_stream && stream) cudaStreamDestroy(stream);

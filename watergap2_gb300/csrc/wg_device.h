@@ -143,8 +143,29 @@ constexpr int VOUT_FIELDS = 33;
 // 11 snowmelt, 12 snow water equivalent, 13 snow-covered fraction, 14 soil water,
 // 15 surface runoff, 16 groundwater recharge, 17-22 radiation [W/m2]:
 // extraterrestrial, incoming and reflected shortwave, net shortwave, net
-// longwave, net, 23-25 canopy, snow and soil storage [km3].
-constexpr int DOUT_FIELDS = 26;
+// longwave, net, 23-25 canopy, snow and soil storage [km3], 26 land AET
+// (dailyCellLandAET weighted by the land share of the continental area [mm]:
+// the land part of routing's daily cell AET, routing.cpp:4533-4634).
+constexpr int DOUT_FIELDS = 27;
+
+// Routing's further monthly grids (routing.cpp:3964-4238, 4525-4737, 5183-5186),
+// field k at rext[k * nmonths * N + month * N + state]: 0 open-water evaporation
+// [mm] (G_monthlyOpenWaterEvap), 1 cell surface runoff [mm]
+// (G_monthlyCellSurfaceRunoff), 2 groundwater runoff [km3] (G_monthlyGwRunoff),
+// 3 land-area fraction [% x days] (G_monthlyLandAreaFrac), 4 local and 5 global
+// wetland extent [km2 x days], 6 reservoir inflow and 7 outflow [km3] (twice
+// the month's flows, as the reference adds them twice a day, routing.cpp:4049-4050
+// and 4653-4655),
+// 8 consistent precipitation [km3] (G_monthlyConsistentPrecip), 9 surface-water
+// storage at the month's end [km3] (G_monthlySurfStor).
+constexpr int ROUT_FIELDS = 10;
+// Routing's daily grids (routing.cpp:4113-4210, 4620-4634), field k at
+// drout[k * drout_days * N + day * N + state]: 0 river availability [km3]
+// (outside inland sinks), 1 velocity [m/s], 2 cell runoff [km3] and 3 [mm],
+// 4 cell surface runoff [mm], 5 groundwater runoff [km3], 6 land-area fraction
+// [%], 7 consistent precipitation [km3], 8 open-water evaporation [mm] (the
+// open-water part of G_daily365CellAET).
+constexpr int DROUT_FIELDS = 9;
 // Per state index, for the grids' Kc and total PET: [0] Kc at LAImin
 // (kc_min), [1] (kc_max - kc_min) / (LAImax - LAImin) (0 where they are equal),
 // [2] LAImin, [3] the freshwater share of the cell for total PET [%]
@@ -163,7 +184,10 @@ struct DevMonthly {
   double *vert;          // null, or the vertical balance's grids [VOUT_FIELDS][nmonths][N]
   double *dvert;         // null, or the vertical balance's daily grids [DOUT_FIELDS][dvert_days][N]
   int32_t dvert_days;
-  double *vconst;        // with vert or dvert: [VCONST_FIELDS][N]
+  double *vconst;        // with any of vert, dvert, rext, drout: [VCONST_FIELDS][N]
+  double *rext;          // null, or routing's further monthly grids [ROUT_FIELDS][nmonths][N]
+  double *drout;         // null, or routing's daily grids [DROUT_FIELDS][drout_days][N]
+  int32_t drout_days;
   // the day-end routing storages of every cell and output day, [day][7][n*members]
   // in the order the reference writes them into its state file (routing.cpp:5001-5020):
   // local lake, local wetland, global lake, global wetland, reservoir, river,

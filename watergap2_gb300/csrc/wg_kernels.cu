@@ -333,7 +333,8 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
   constexpr bool WT = (X & 1) != 0;
   constexpr bool WU = (X & 2) != 0;
   constexpr bool GL = (X & 4) != 0;   // water use with GLWD units (aggrNUsGloLakResOpt = 1)
-  constexpr bool VO = (X & 8) != 0;   // the vertical balance's monthly output grids
+  constexpr bool VO = (X & 8) != 0;   // the vertical balance's output grids
+  constexpr bool RO = (X & 16) != 0;  // routing's further output grids (always with VO)
   const int n = c.n;
   const int M = ENS ? mem.members : 1;
   const size_t N = (size_t)n * M;
@@ -484,6 +485,7 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
           }
           const size_t wrow = WU ? (size_t)wu.row_of_fday[fday0 + d] * WU_FIELDS * (size_t)n : 0;
           R tv;
+          [[maybe_unused]] RoutOut ro;   // the output grids' routing terms (RO)
           const bool nocont = (fl & F_NOCONT) != 0;
           if (nocont) {
             // the reference routes only continental cells (routing.cpp:1878-4518): the
@@ -493,7 +495,8 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
             tv = R(0);
             rt.p_ow = R(0); rt.e_ow = R(0); rt.leak = R(-up); rt.velocity = R(0);
           } else {
-            tv = routing_cell<R, WT, WU, GL>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtd, &wu, wrow, si, N);
+            tv = routing_cell<R, WT, WU, GL, RO>(c, s, rs, doy, month, laf, laf_prev, o, up, rt, &wtd, &wu, wrow, si,
+                                                 N, &ro);
             store_rstate(st, si, rs, fl);
           }
           q_now[si] = (double)tv;
@@ -559,6 +562,63 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
                 mon.cell_runoff[k] += ((fl & F_SINK) ? 0. : q) - up;
                 mon.velocity[k] += (double)rt.velocity / 86.4;   // km/d -> m/s
               }
+            }
+          }
+          if constexpr (RO) {
+            // routing's further output grids (routing.cpp:3964-4238, 4525-4737,
+            // 5183-5186); the flux terms of continental cells only (routing.cpp:1878-4518)
+            const int od = oday0 + d;
+            const double q = (double)tv;
+            const double cr = ((fl & F_SINK) ? 0. : q) - up;   // CellRunoff [km3]
+            double owe = 0., csr = 0., crmm = 0., cp = 0.;
+            if (!nocont && (mon.rext || mon.drout)) {
+              const double cf = (double)c.contfreq[s], area = (double)c.area[s];
+              const double rc = 1e8 * fm::rcp_pos(area * cf);   // km3 -> mm over the continental area
+              // open-water evaporation, with an inland sink's transported volume (routing.cpp:4549-4560)
+              owe = (ro.owe + ((fl & F_SINK) ? q : 0.)) * rc;
+              csr = (cr - ro.gw_runoff) * rc;                  // routing.cpp:3998-4001
+              crmm = cr * rc;
+              const double *vk = mon.vconst + si;
+              double lwe = cf - vk[4 * N] - vk[5 * N];          // G_landWaterExclGloLakAreaFrac (routing.cpp:1187-1196)
+              if (lwe < 0.) lwe = 0.;
+              const double owp = (double)(c.mprec[s] * R(f.prec[(size_t)(fday0 + d) * n + s]));
+              cp = owp * lwe * area * 1e-8 + ro.p_lake;       // consistent precipitation (routing.cpp:3973-3977)
+            }
+            if (mon.rext) {
+              const int yd = mon.doy_day0 - 1 + od;
+              const int mi = (yd / 365) * 12 + month_of(yd % 365 + 1) - mon.month0;
+              if (mi >= 0 && mi < mon.nmonths) {
+                double *r = mon.rext + (size_t)mi * N + si;
+                const size_t k = (size_t)mon.nmonths * N;
+                if (!nocont) {
+                  r[0] += owe;
+                  r[k] += csr;
+                  r[2 * k] += ro.gw_runoff;
+                  r[4 * k] += ro.lw_ext;
+                  r[5 * k] += ro.gw_ext;
+                  // the reference adds the reservoir's flows twice a day, in the cell
+                  // loop and after it (routing.cpp:4049-4050, 4653-4655)
+                  r[6 * k] += 2. * ro.res_in;
+                  r[7 * k] += 2. * ro.res_out;
+                  r[8 * k] += cp;
+                }
+                r[3 * k] += (double)laf;
+                r[9 * k] = (double)rs.loclake + (double)rs.locwetl + (double)rs.glolake + (double)rs.glowetl +
+                           (double)rs.river + (double)rs.res;
+              }
+            }
+            if (mon.drout && !nocont && od < mon.drout_days) {
+              double *r = mon.drout + (size_t)od * N + si;
+              const size_t k = (size_t)mon.drout_days * N;
+              r[0] = (fl & F_SINK) ? 0. : q;
+              r[k] = (double)rt.velocity / 86.4;
+              r[2 * k] = cr;
+              r[3 * k] = crmm;
+              r[4 * k] = csr;
+              r[5 * k] = ro.gw_runoff;
+              r[6 * k] = (double)laf;
+              r[7 * k] = cp;
+              r[8 * k] = owe;
             }
           }
          }   // cells of the unit
@@ -759,11 +819,11 @@ static const void *pipeline_fn_x(bool fused, bool vaw) {
 
 template <class R>
 static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false, bool gl = false,
-                               bool vo = false) {
+                               bool vo = false, bool ro = false) {
   if (gl && (ens || wt || !wu || !std::is_same<R, double>::value)) return nullptr;   // GLWD units: FP64, one member
-  if (vo) {   // the vertical balance's monthly output grids: FP64, one member, alone
+  if (vo || ro) {   // the output grids: FP64, one member, alone
     if (ens || wt || wu || !std::is_same<R, double>::value) return nullptr;
-    return pipeline_fn_x<R, 8>(fused, vaw);
+    return ro ? pipeline_fn_x<R, 24>(fused, vaw) : pipeline_fn_x<R, 8>(fused, vaw);
   }
   if (ens) return wt ? nullptr
                      : (wu ? (const void *)k_pipeline<R, true, true, false, 2> : (const void *)k_pipeline<R, true, true, false, 0>);
@@ -827,7 +887,8 @@ cudaError_t launch_pipeline(bool fused, const DevCellsT<R> &c, const DevStateT<R
                   (void *)&idle_warp, (void *)&mon, (void *)&vwk, (void *)&wtp, (void *)&wu};
   const bool ens = mem.members > 1;
   const void *fn = pipeline_fn<R>(fused, ens, vaw, wtp.enabled != 0, wu.enabled != 0, wu.enabled && wu.glwd,
-                                  mon.vert != nullptr || mon.dvert != nullptr);
+                                  mon.vert != nullptr || mon.dvert != nullptr,
+                                  mon.rext != nullptr || mon.drout != nullptr);
   if (!fn) return cudaErrorInvalidConfiguration;
   if (vaw) threads += 32 * vw.warps;
   // cooperative (all blocks resident, or the launch fails) through the launch

@@ -600,10 +600,22 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
         dd[23 * k] = cs;
         dd[24 * k] = ss;
         dd[25 * k] = ls;
+        dd[26 * k] = (double)cellAET * mw;   // the land part of routing's cell AET
       }
     }
   }
 }
+
+// Routing terms of one cell-day for the output grids (routing.cpp:3964-4238,
+// 4525-4660): the open-water evaporation of the cell's water bodies [km3] (the
+// reference's dailyOpenWaterEvap_km3 without the inland sink's transported
+// volume: each body's evaporation in mm, reduced where the storage limits it,
+// times its area), the groundwater runoff [km3], the wetlands' extents [km2], the
+// reservoir's inflow and outflow [km3] and the precipitation on the global lake
+// and the reservoir [km3].
+struct RoutOut {
+  double owe, gw_runoff, lw_ext, gw_ext, res_in, res_out, p_lake;
+};
 
 template <class R>
 struct RTerms {
@@ -723,11 +735,12 @@ __device__ __forceinline__ void wu_year_end(double *w, size_t N) {
 // factor and outflow, and the local runoff).  WU: water use (subtract_use = 2, satisfied in the cell):
 // wu points at the tables (per cell: slot s, stride c.n) and the state (per
 // member: state index si, stride NN), wrow is the offset of the day's table row.
-template <class R, bool WT = false, bool WU = false, bool GL = false>
+// RO: the terms of routing's output grids into *ro.
+template <class R, bool WT = false, bool WU = false, bool GL = false, bool RO = false>
 __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R> &st, int doy, int month, R laf,
                                           R laf_prev, const VOut<R> &v, double inflow_up, RTerms<R> &rt,
                                           wt::WtDay *wtd = nullptr, const DevWaterUse *wu = nullptr, size_t wrow = 0,
-                                          size_t si = 0, size_t NN = 0) {
+                                          size_t si = 0, size_t NN = 0, RoutOut *ro = nullptr) {
   typedef M<R> m;
   const uint32_t fl = c.flags[s];
   const R cfa = c.cfa[s];
@@ -776,6 +789,10 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (cmp::abs_le_c(gw, R(WG_MIN_STOR_VOL))) gw = R(0);
   }
   st.gw = gw;
+  if constexpr (RO) {
+    ro->owe = 0.; ro->gw_runoff = (double)gw_runoff; ro->lw_ext = 0.; ro->gw_ext = 0.;
+    ro->res_in = 0.; ro->res_out = 0.; ro->p_lake = 0.;
+  }
   R inflow = dlsr + gw_runoff;
   R into_river = R(0), gw_into_river = R(0), local_gw = gw_runoff;
   if (c.frac_routing && !(fl & F_SINK)) {
@@ -813,7 +830,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (PETgwr > PETgwrMax) {
       S = -maxS;
       rt.e_ow += avail;
-      if constexpr (WT) evapo *= PETgwrMax / PETgwr;
+      if constexpr (WT || RO) evapo *= PETgwrMax / PETgwr;   // routing.cpp:2400-2404
     } else {
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
@@ -832,6 +849,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     }
     inflow = outflow;
     if constexpr (WT) wtd->loclake((double)S0 + (double)maxS, evapo, rf, outflow);
+    if constexpr (RO) ro->owe += (double)evapo * (double)a6 * (double)c.ll100[s];
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * (R(0.5) * c.inv_maxs_ll[s]), c.evx[s]);
     st.loclake = S;
     st.rf_loclake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -848,7 +866,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (PETgwr > PETgwrMax) {
       S = R(0);
       rt.e_ow += PETgwrMax;
-      if constexpr (WT) evapo *= PETgwrMax / PETgwr;
+      if constexpr (WT || RO) evapo *= PETgwrMax / PETgwr;
     } else {
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
@@ -866,6 +884,10 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     }
     inflow = outflow;
     if constexpr (WT) wtd->locwetl(S0, evapo, rf, outflow);
+    if constexpr (RO) {   // routing.cpp:2509-2524
+      ro->owe += (double)evapo * (double)a6 * (double)c.lw100[s];
+      ro->lw_ext = (double)rf * (double)c.area[s] * (double)c.lw100[s];
+    }
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_maxs_lw[s], c.evx[s]);
     st.locwetl = S;
     st.rf_locwetl = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -892,7 +914,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = -maxS;
       outflow = R(0);
       rt.e_ow += PUmax;
-      if constexpr (WT) evapo *= PUmax / PU;
+      if constexpr (WT || RO) evapo *= PUmax / PU;
       if constexpr (WU) remUseGL = (remUseGL > R(0)) ? remUseGL - remUseGL * PUmax / PU : R(0);
     } else {
       if constexpr (WU) remUseGL = R(0);
@@ -912,6 +934,10 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     inflow = outflow;
     if constexpr (WU) dailyActualUse = remGL0 - remUseGL;   // routing.cpp:2788
     if constexpr (WT) wtd->glolake((double)S0 + (double)maxS, evapo, outflow);
+    if constexpr (RO) {   // routing.cpp:2648-2664
+      ro->owe += (double)evapo * (double)c.la6[s];
+      ro->p_lake += (double)pin;
+    }
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * (R(0.5) * c.inv_maxs_gl[s]), c.evx[s]);
     st.glolake = S;
     st.rf_glolake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -932,10 +958,14 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       remRes0 = remUseRes;
     }
     R S;
+    if constexpr (RO) {   // routing.cpp:2826, 2853-2854
+      ro->res_in = (double)inflow;
+      ro->p_lake += (double)pin;
+    }
     if (PETgwr > PETgwrMax) {
       S = S0 + TI - PETgwrMax;
       rt.e_ow += PETgwrMax;
-      if constexpr (WT) evapo *= PETgwrMax / PETgwr;
+      if constexpr (WT || RO) evapo *= PETgwrMax / PETgwr;
     } else {
       S = S0 + TI - PETgwr;
       rt.e_ow += PETgwr;
@@ -988,6 +1018,10 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     inflow = outflow;
     if constexpr (WU) dailyActualUse += remRes0 - remUseRes;   // routing.cpp:3068
     if constexpr (WT) wtd->res(S0, evapo, outflow);
+    if constexpr (RO) {   // routing.cpp:2837-2844, 3040
+      ro->owe += (double)evapo * (double)c.ra6[s];
+      ro->res_out = (double)outflow;
+    }
     R r = R(1.) - m::pow(x::div(m::fabs_(S - maxS), maxS), R(2.81383));   // routing.cpp:3071-3072
     st.res = S;
     st.rf_res = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
@@ -1049,7 +1083,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       S = R(0);
       outflow = R(0);
       rt.e_ow += PETgwrMax;
-      if constexpr (WT) evapo *= PETgwrMax / PETgwr;
+      if constexpr (WT || RO) evapo *= PETgwrMax / PETgwr;
     } else {
       S = S0 * c.sw_e[s] + c.sw_ik[s] * (TI - PETgwr) * c.sw_ome[s];
       outflow = TI + S0 - S - PETgwr;
@@ -1062,6 +1096,10 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (m::fabs_(S) <= R(WG_MIN_STOR_VOL)) S = R(0);
     inflow = outflow;
     if constexpr (WT) wtd->glowetl(S0, evapo, rf, outflow);
+    if constexpr (RO) {   // routing.cpp:3194-3210
+      ro->owe += (double)evapo * (double)a6 * (double)c.gw100[s];
+      ro->gw_ext = (double)rf * (double)c.area[s] * (double)c.gw100[s];
+    }
     R r = R(1.) - m::pow(m::fabs_(S - maxS) * c.inv_maxs_gw[s], c.evx[s]);
     st.glowetl = S;
     st.rf_glowetl = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);

@@ -39,7 +39,8 @@ SYMBOLS = ("wg_create", "wg_destroy", "wg_set_state", "wg_get_state", "wg_set_me
            "wg_upload_water_use", "wg_set_water_use_inputs", "wg_get_water_use", "wg_set_water_use",
            "wg_model_options_default", "wg_get_member_discharge", "wg_set_deferred",
            "wg_record_daily_storages", "wg_get_daily_storages", "wg_upload_forcing_cells",
-           "wg_monthly_outputs_vertical", "wg_daily_outputs_vertical", "wg_get_daily_vertical")
+           "wg_monthly_outputs_vertical", "wg_daily_outputs_vertical", "wg_get_daily_vertical",
+           "wg_monthly_outputs_routing", "wg_daily_outputs_routing", "wg_get_daily_routing")
 
 
 class WgError(RuntimeError):
@@ -147,6 +148,12 @@ def load_library(path: str = LIB_PATH):
     lib.wg_daily_outputs_vertical.restype = i32
     lib.wg_get_daily_vertical.argtypes = [vp, i32, i32, i32, vp]
     lib.wg_get_daily_vertical.restype = i32
+    lib.wg_monthly_outputs_routing.argtypes = [vp, i32]
+    lib.wg_monthly_outputs_routing.restype = i32
+    lib.wg_daily_outputs_routing.argtypes = [vp, i32]
+    lib.wg_daily_outputs_routing.restype = i32
+    lib.wg_get_daily_routing.argtypes = [vp, i32, i32, i32, vp]
+    lib.wg_get_daily_routing.restype = i32
     lib.wg_set_step_sync.argtypes = [vp, i32]
     lib.wg_get_monthly.argtypes = [vp, i32, i32, i32, vp]
     lib.wg_read_unf.argtypes = [ctypes.c_char_p, vp, i64]
@@ -514,7 +521,33 @@ class Model:
     DAILY_VERTICAL = ["prec", "temp", "pet", "total_pet", "lai", "kc", "albedo", "interception", "canopy_wc",
                       "max_canopy_wc", "snowfall", "snowmelt", "swe", "snow_cover", "soil_wc", "surface_runoff",
                       "gw_recharge", "ext_rad", "short_down_rad", "short_up_rad", "net_short_rad", "net_long_rad",
-                      "net_rad", "canopy_storage", "snow_storage", "soil_storage"]
+                      "net_rad", "canopy_storage", "snow_storage", "soil_storage", "land_aet"]
+    # routing's further monthly grids (wg_monthly_outputs_routing), which = 39 + index,
+    # and the cell AET grids assembled from both sets
+    MONTHLY_ROUTING = ["open_water_evap", "cell_surface_runoff", "gw_runoff", "land_area_frac", "loc_wetl_extent",
+                       "glo_wetl_extent", "res_inflow", "res_outflow", "consistent_precip", "surf_storage"]
+    MONTHLY.update({k: 6 + 33 + i for i, k in enumerate(MONTHLY_ROUTING)})
+    MONTHLY.update({"cell_aet": 49, "cell_aet_wca": 50})
+    # routing's daily grids (wg_daily_outputs_routing), field = index
+    DAILY_ROUTING = ["river_avail", "velocity", "cell_runoff", "cell_runoff_mm", "cell_surface_runoff", "gw_runoff",
+                     "land_area_frac", "consistent_precip", "open_water_evap", "cell_aet"]
+
+    def monthly_outputs_routing(self, enable: bool = True):
+        """wg_monthly_outputs_routing: routing's further monthly grids too."""
+        self._check(self.lib.wg_monthly_outputs_routing(self.h, int(bool(enable))), "monthly_outputs_routing")
+
+    def daily_outputs_routing(self, ndays: int):
+        """wg_daily_outputs_routing: routing's daily grids for output days 0 .. ndays-1 (0: off)."""
+        self._check(self.lib.wg_daily_outputs_routing(self.h, int(ndays)), "daily_outputs_routing")
+        self.droute_days = int(ndays)
+
+    def daily_routing(self, name: str, day0: int = 0, nd: int | None = None) -> np.ndarray:
+        """[nd, ncell] daily routing grid, cell order."""
+        nd = self.droute_days - day0 if nd is None else nd
+        out = np.zeros((nd, self.region.ncell))
+        self._check(self.lib.wg_get_daily_routing(self.h, self.DAILY_ROUTING.index(name), int(day0), int(nd),
+                                                  _ptr(out)), "get_daily_routing")
+        return out
 
     def daily_outputs_vertical(self, ndays: int):
         """wg_daily_outputs_vertical: the vertical balance's daily grids for output
