@@ -316,21 +316,32 @@ def run_water_use(region, P, T, S, stream, local):
 
 
 def run_outputs(region, P, T, S, stream, local):
-    """The global grid with the monthly output grids against the plain run:
-    routing's grids only (wg_monthly_outputs: river availability with its
-    minimum and maximum, cell runoff, velocity, storage), and routing's with the
-    vertical balance's 32 grids (wg_monthly_outputs_vertical; the reference's
-    grid_store = 2 sums).  Four years in one wavefront, the fourth timed with
-    CUDA events (the first three fill the wavefront)."""
+    """The global grid with the output grids against the plain run: routing's
+    monthly aggregates only (wg_monthly_outputs: river availability with its
+    minimum and maximum, cell runoff, velocity, storage); with the vertical
+    balance's 33 monthly grids (wg_monthly_outputs_vertical; the reference's
+    grid_store = 2 sums); with routing's further 10 monthly grids as well
+    (wg_monthly_outputs_routing); and with every daily grid too (27 of the
+    vertical balance, 9 of routing, kept on the device for all four years:
+    grid_store = 6).  Four years in one wavefront, the fourth timed with CUDA
+    events (the first three fill the wavefront)."""
     import torch
     from watergap2_gb300.gpu import Model
     nd = 4 * DAYS_PER_STEP
     out = {}
-    for name, grids in (("routing_grids", 1), ("all_grids", 2), ("without", 0)):
+    # grids: 1 routing's monthly aggregates, 2 and the vertical balance's monthly
+    # grids, 3 and routing's further monthly grids, 4 all of them and every daily
+    # grid (vertical balance and routing) for the four years
+    for name, grids in (("routing_grids", 1), ("all_grids", 2), ("all_monthly_grids", 3),
+                        ("monthly_and_daily_grids", 4), ("without", 0)):
         m = Model(region, max_days=nd, device=local, stream=stream.cuda_stream, days_per_step=WAVEFRONT_DAYS)
         if grids:
             m.monthly_outputs(48, doy_day0=1)
-            m.monthly_outputs_vertical(grids == 2)
+            m.monthly_outputs_vertical(grids >= 2)
+            m.monthly_outputs_routing(grids >= 3)
+        if grids == 4:
+            m.daily_outputs_vertical(nd)
+            m.daily_outputs_routing(nd)
         m.upload_forcing(0, P[:nd], T[:nd], S[:nd])
         assert 3 * WSTEPS_PER_YEAR >= m.num_levels - 1
         m.run_steps(1, 0, nd, 0, 3 * WSTEPS_PER_YEAR)
@@ -347,7 +358,7 @@ def run_outputs(region, P, T, S, stream, local):
             # cells have not finished the fourth when the timed steps end)
             out[name]["mean_monthly_prec_mm"] = float(np.mean(m.monthly("prec", 0, 12)))
         del m
-    for name in ("routing_grids", "all_grids"):
+    for name in ("routing_grids", "all_grids", "all_monthly_grids", "monthly_and_daily_grids"):
         out[name]["cost_vs_plain"] = out["without"]["cell_days_per_s"] / out[name]["cell_days_per_s"]
     return out
 
