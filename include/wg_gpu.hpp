@@ -104,7 +104,7 @@ class Context {
   void daily_vertical(int field, int day0, int nd, double *out) {
     check(wg_get_daily_vertical(ctx_, field, day0, nd, out), "wg_get_daily_vertical");
   }
-  // routing's further monthly grids (which 39..50 of monthly()) and its daily grids
+  // routing's further monthly grids (which 39..52 of monthly()) and its daily grids
   void monthly_outputs_routing(bool enable) {
     check(wg_monthly_outputs_routing(ctx_, enable ? 1 : 0), "wg_monthly_outputs_routing");
   }

@@ -90,7 +90,7 @@ MONTHLY_ROUTING = ["river_avail", "min_river_avail", "max_river_avail", "cell_ru
                    "locwetl_storage", "glolake_storage", "glowetl_storage", "res_storage", "river_storage",
                    "gw_storage", "open_water_evap", "cell_surface_runoff", "gw_runoff", "land_area_frac",
                    "loc_wetl_extent", "glo_wetl_extent", "res_inflow", "res_outflow", "consistent_precip",
-                   "surf_storage", "cell_aet", "cell_aet_wca"]
+                   "surf_storage", "actual_use", "nug", "cell_aet", "cell_aet_wca"]
 # routing's daily 365 grids the harness dumps with outputs=2
 DAILY_ROUTING = ["river_avail", "velocity", "cell_runoff", "cell_runoff_mm", "cell_surface_runoff", "gw_runoff",
                  "land_area_frac", "consistent_precip", "cell_aet"]

@@ -351,7 +351,8 @@ int main(int argc, char **argv) {
         &routing.G_monthlyOpenWaterEvap, &routing.G_monthlyCellSurfaceRunoff, &routing.G_monthlyGwRunoff,
         &routing.G_monthlyLandAreaFrac, &routing.G_monthlyLocWetlExtent, &routing.G_monthlyGloWetlExtent,
         &routing.G_monthlyResInflow, &routing.G_monthlyResOutflow, &routing.G_monthlyConsistentPrecip,
-        &routing.G_monthlySurfStor, &routing.G_monthlyCellAET, &routing.G_monthlyCellAETWCa};
+        &routing.G_monthlySurfStor, &routing.G_monthlyActualUse, &routing.G_monthlyNUg, &routing.G_monthlyCellAET,
+        &routing.G_monthlyCellAETWCa};
     std::vector<double> buf((size_t)12 * ncase);
     auto dump = [&](auto *g) {
       for (int m = 0; m < 12; m++)

@@ -295,6 +295,37 @@ def main_outputs(names=None, name="swb_outputs_730d"):
     print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+def main_outputs_wuse(names=None, name="swb_outputs_wuse_730d"):
+    """The output grids of main_outputs with water use met in the cell
+    (subtract_use = 2): the same region, two calendar years, the water-use inputs
+    of swb_wuse_420d; the grids hold the second year, among them the monthly
+    actual use and NUg (routing.cpp:3744-3747)."""
+    if names and name not in names:
+        return
+    if not ref_case.available():
+        if not ref_case.build(REF_SOURCE):
+            raise SystemExit("reference sources not found; cannot regenerate fixtures")
+    region = sy.region_small_swb(seed=21, ny=16, nx=32, block_at=(100, 300))
+    nd = 730
+    P, T, S = sy.forcing(region, nd, doy0=1)
+    nus, nug, wdr, cons, frgi = sy.water_use_inputs(region, 3, seed=13)
+    outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+    res = ref_case.run(region, P, T, S, doy0=1, stations=outl[:24], snapshots=[nd], outputs=2,
+                       wuse=(nus, nug, wdr, cons, frgi))
+    extra = dict(P=P, T=T, S=S, NUS=nus, NUG=nug, WDR=wdr, CONS=cons, FRGI=frgi, doy0=np.array(1),
+                 delayed=np.array(0), stations=res["stations"], snap_days=np.array([nd]),
+                 discharge=res["discharge"])
+    for k, v in res["monthly"].items():
+        extra[f"m_{k}"] = v
+    days = np.unique(np.r_[0:3, 31:34, np.arange(0, 365, 13), 364])
+    extra["daily_days"] = days
+    for k, v in res["daily"].items():
+        extra[f"d_{k}"] = v[days]
+    path = os.path.join(HERE, f"{name}.npz")
+    save_npz(region, path, **extra)
+    print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 def main_wtemp_wuse(names=None, name="swb_wtemp_wuse_120d"):
     """Water use together with the water temperature (calc_wtemp = 1, subtract_use
     = 2): the water-temperature region and a cold season across a year end."""
@@ -421,4 +452,5 @@ if __name__ == "__main__":
     main_wuse(sys.argv[1:])
     main_wuse_glwd(sys.argv[1:])
     main_outputs(sys.argv[1:])
+    main_outputs_wuse(sys.argv[1:])
     main_wtemp_wuse(sys.argv[1:])

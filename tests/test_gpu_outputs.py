@@ -27,7 +27,16 @@ from helpers import max_rel_err
 pytestmark = pytest.mark.gpu
 RTOL = 1e-10
 PATH = os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_730d.npz")
+# the same grids with water use met in the cell (subtract_use = 2)
+PATH_WU = os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_wuse_730d.npz")
 Y2 = 365   # the grids are the second year's
+# with water use, routing's flux grids against a floor of 1 % of each grid's largest value
+RTOL_WU = 1e-7
+FLUX_WU = ["river_avail", "min_avail", "max_avail", "cell_runoff", "velocity", "cell_surface_runoff",
+           "open_water_evap", "cell_aet", "cell_aet_wca", "res_inflow", "res_outflow", "actual_use", "nug",
+           "consistent_precip", "surf_storage", "gw_runoff",
+           "d_r_river_avail", "d_r_velocity", "d_r_cell_runoff", "d_r_cell_runoff_mm", "d_r_cell_surface_runoff",
+           "d_r_gw_runoff", "d_r_cell_aet", "d_r_consistent_precip"]
 # Model.monthly name -> the reference's grid
 ROUTING = {"river_avail": "river_avail", "min_avail": "min_river_avail", "max_avail": "max_river_avail",
            "cell_runoff": "cell_runoff", "velocity": "velocity"}
@@ -43,13 +52,16 @@ def _built():
         build.build()
 
 
-def _two_years(days_per_step=0, deferred=False, routing=True):
+def _two_years(days_per_step=0, deferred=False, routing=True, wuse=False):
     from watergap2_gb300.gpu import Model
     from watergap2_gb300.region import load_npz
-    region, ex = load_npz(PATH)
+    region, ex = load_npz(PATH_WU if wuse else PATH)
     P, T, S = ex["P"], ex["T"], ex["S"]
     nd = P.shape[0]
-    m = Model(region, max_days=nd, stations=ex["stations"], days_per_step=days_per_step)
+    m = Model(region, max_days=nd, stations=ex["stations"], days_per_step=days_per_step, water_use=wuse)
+    if wuse:
+        m.set_water_use_inputs(ex["FRGI"])
+        m.upload_water_use_run(0, 1, nd, (ex["NUS"], ex["NUG"], ex["WDR"], ex["CONS"]))
     m.monthly_outputs(24, doy_day0=1)
     m.monthly_outputs_vertical(True)
     m.daily_outputs_vertical(nd)
@@ -74,17 +86,21 @@ def _two_years(days_per_step=0, deferred=False, routing=True):
     return m, ex, grids
 
 
-@pytest.mark.parametrize("dps,routing", [(1, True), (5, True), (5, False)])
-def test_output_grids_match_reference(dps, routing):
+@pytest.mark.parametrize("dps,routing,wuse", [(1, True, False), (5, True, False), (5, False, False),
+                                              (1, True, True), (5, True, True)])
+def test_output_grids_match_reference(dps, routing, wuse):
     """All grids (routing's further grids with the vertical balance's: the
-    wavefront's variant with both), and the vertical balance's grids alone (its
-    variant without routing's further terms)."""
-    m, ex, grids = _two_years(days_per_step=dps, routing=routing)
+    wavefront's variant with both), the vertical balance's grids alone (its
+    variant without routing's further terms), and all grids with water use."""
+    m, ex, grids = _two_years(days_per_step=dps, routing=routing, wuse=wuse)
     errs = {k: max_rel_err(grids[k], ex["m_" + k]) for k in m.MONTHLY_VERTICAL}
     errs.update({k: max_rel_err(grids[k], ex["m_" + r]) for k, r in ROUTING.items()})
     ds = m.daily_storages(Y2, 365)
     for i, f in enumerate(STORAGES):
         errs[f + "_storage"] = max_rel_err(ds[MONTH_END, i], ex[f"m_{f}_storage"])
+        if wuse and f == "river":   # where the use's remainder stays (see below)
+            e = max_rel_err(ds[MONTH_END, i], ex[f"m_{f}_storage"], floor_frac=1e-2)
+            errs[f + "_storage"] = 0. if e <= RTOL_WU else e
     days = ex["daily_days"]
     for k in m.DAILY_VERTICAL:
         if k != "land_aet":   # not a grid of the reference's
@@ -92,13 +108,34 @@ def test_output_grids_match_reference(dps, routing):
     if routing:
         for k in m.MONTHLY_ROUTING + ["cell_aet", "cell_aet_wca"]:
             errs[k] = max_rel_err(grids[k], ex["m_" + k])
+        if wuse:   # the water use grids are exercised
+            assert np.abs(ex["m_actual_use"]).max() > 0 and np.abs(ex["m_nug"]).max() > 0
         for k in m.DAILY_ROUTING:
             if k != "open_water_evap":   # not a grid of the reference's
                 errs["d_r_" + k] = max_rel_err(grids["d_r_" + k][days], ex["d_r_" + k])
+    if wuse:
+        # routing's flux grids with water use: the net abstraction from groundwater
+        # can leave a cell's groundwater runoff as a difference of equal terms,
+        # zero in the reference and +1e-20 km3 here (or the reverse); the river
+        # velocity is not smooth at zero inflow (depth ~ Q^0.341, a floor of 1e-5
+        # km/d, routing.cpp:7274-7297), so the day's release differs (cell 149 of
+        # this fixture, day 312: 7.5e-8 against 1.3e-9 km3) and the water leaves
+        # on the following days instead; every storage and the water-use state
+        # agree with the oracle to 1e-14 at the end.  Against a floor of 1 % of each
+        # grid's largest value the grids' largest such error is 1.3e-8
+        for k in FLUX_WU:
+            g = grids[k] if not k.startswith("d_") else grids[k][days]
+            r = ex["m_" + ROUTING.get(k, k)] if not k.startswith("d_") else ex[k]
+            e = max_rel_err(g, r, floor_frac=1e-2)
+            errs[k] = 0. if e <= RTOL_WU else e   # reported (and failing) above RTOL_WU
     bad = {k: v for k, v in errs.items() if not v <= RTOL}
     assert not bad, bad
     q = m.discharge(0, 730)
-    assert max_rel_err(q, ex["discharge"]) <= RTOL
+    if wuse:   # the same transients reach the stations: 2.1e-7 of 1 % of a station's peak
+        from test_wuse_oracle import discharge_err
+        assert discharge_err(q, ex["discharge"]) <= 1e-6
+    else:
+        assert max_rel_err(q, ex["discharge"]) <= RTOL
 
 
 def test_output_grids_deferred_per_day_calls_same_bits():

@@ -2135,11 +2135,12 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
   return cuda_fail(ctx, e, "monthly_outputs");
 }
 
-// the output grids' conditions: FP64, one member, without water temperature or
-// water use; routing's further grids also without fractional routing (its
+// the output grids' conditions: FP64, one member, without the water temperature
+// or GLWD units; routing's further grids also without fractional routing (its
 // groundwater runoff splits between the river and the water bodies)
 static wg_status outputs_supported(const wg_ctx *ctx, bool routing) {
-  if (ctx->precision != 0 || ctx->members != 1 || ctx->wt.enabled || ctx->wu.enabled) return WG_ERR_UNSUPPORTED;
+  if (ctx->precision != 0 || ctx->members != 1 || ctx->wt.enabled || (ctx->wu.enabled && ctx->wu.glwd))
+    return WG_ERR_UNSUPPORTED;
   if (routing && ctx->frac_routing) return WG_ERR_UNSUPPORTED;
   return WG_OK;
 }
@@ -2304,7 +2305,7 @@ wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable) {
 }
 
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out) {
-  constexpr int V0 = 6, R0 = V0 + wg::VOUT_FIELDS, AET = R0 + wg::ROUT_FIELDS;   // 6, 39, 49
+  constexpr int V0 = 6, R0 = V0 + wg::VOUT_FIELDS, AET = R0 + wg::ROUT_FIELDS;   // 6, 39, 51
   if (!ctx || !out || which < 0 || which > AET + 1 || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths)
     return WG_ERR_INVALID;
   if (which >= V0 && which < R0 && !ctx->mon.vert) return WG_ERR_UNSUPPORTED;

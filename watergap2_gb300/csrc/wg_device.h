@@ -157,8 +157,10 @@ constexpr int DOUT_FIELDS = 27;
 // the month's flows, as the reference adds them twice a day, routing.cpp:4049-4050
 // and 4653-4655),
 // 8 consistent precipitation [km3] (G_monthlyConsistentPrecip), 9 surface-water
-// storage at the month's end [km3] (G_monthlySurfStor).
-constexpr int ROUT_FIELDS = 10;
+// storage at the month's end [km3] (G_monthlySurfStor); with water use 10 the
+// actual use from surface water [km3] (G_monthlyActualUse) and 11 the net
+// abstraction from groundwater [km3] (G_monthlyNUg), routing.cpp:3744-3747.
+constexpr int ROUT_FIELDS = 12;
 // Routing's daily grids (routing.cpp:4113-4210, 4620-4634), field k at
 // drout[k * drout_days * N + day * N + state]: 0 river availability [km3]
 // (outside inland sinks), 1 velocity [m/s], 2 cell runoff [km3] and 3 [mm],

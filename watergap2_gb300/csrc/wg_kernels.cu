@@ -605,6 +605,12 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
                 r[3 * k] += (double)laf;
                 r[9 * k] = (double)rs.loclake + (double)rs.locwetl + (double)rs.glolake + (double)rs.glowetl +
                            (double)rs.river + (double)rs.res;
+                if constexpr (WU) {
+                  if (!nocont) {   // routing.cpp:3744-3747
+                    r[10 * k] += ro.actual_use;
+                    r[11 * k] += ro.nug;
+                  }
+                }
               }
             }
             if (mon.drout && !nocont && od < mon.drout_days) {
@@ -821,8 +827,9 @@ template <class R>
 static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false, bool gl = false,
                                bool vo = false, bool ro = false) {
   if (gl && (ens || wt || !wu || !std::is_same<R, double>::value)) return nullptr;   // GLWD units: FP64, one member
-  if (vo || ro) {   // the output grids: FP64, one member, alone
-    if (ens || wt || wu || !std::is_same<R, double>::value) return nullptr;
+  if (vo || ro) {   // the output grids: FP64, one member, without the water temperature or GLWD units
+    if (ens || wt || gl || !std::is_same<R, double>::value) return nullptr;
+    if (wu) return pipeline_fn_x<R, 26>(fused, vaw);   // with water use: all outputs in one variant
     return ro ? pipeline_fn_x<R, 24>(fused, vaw) : pipeline_fn_x<R, 8>(fused, vaw);
   }
   if (ens) return wt ? nullptr

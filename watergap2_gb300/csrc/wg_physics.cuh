@@ -615,6 +615,7 @@ __device__ __forceinline__ void vertical_cell(const DevCellsT<R> &c, int s, R ga
 // and the reservoir [km3].
 struct RoutOut {
   double owe, gw_runoff, lw_ext, gw_ext, res_in, res_out, p_lake;
+  double actual_use, nug;   // water use: the day's actual use from surface water, NUg [km3]
 };
 
 template <class R>
@@ -745,6 +746,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
   const uint32_t fl = c.flags[s];
   const R cfa = c.cfa[s];
   rt.p_ow = R(0); rt.e_ow = R(0); rt.leak = R(0);
+  if constexpr (RO) *ro = RoutOut{};
   R remainingUse = R(0), dailyActualUse = R(0), remUseGL = R(0), remUseRes = R(0);
   double prevTotalUnsat = 0.;
   double *W = nullptr;
@@ -765,6 +767,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     const size_t tn = (size_t)c.n;
     double nug = wu->tab[wrow + tn + s];
     if (W[0] != 0.) nug = wu_update_nag(W, NN, nug, wu->frgi[s]);
+    if constexpr (RO) ro->nug = nug;   // G_dailydailyNUg (routing.cpp:3747)
     netGWin -= R(nug);
     rt.e_ow += R(nug);
     remainingUse = R(wu->tab[wrow + s]);   // routing.cpp:2225-2290
@@ -789,10 +792,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
     if (cmp::abs_le_c(gw, R(WG_MIN_STOR_VOL))) gw = R(0);
   }
   st.gw = gw;
-  if constexpr (RO) {
-    ro->owe = 0.; ro->gw_runoff = (double)gw_runoff; ro->lw_ext = 0.; ro->gw_ext = 0.;
-    ro->res_in = 0.; ro->res_out = 0.; ro->p_lake = 0.;
-  }
+  if constexpr (RO) ro->gw_runoff = (double)gw_runoff;
   R inflow = dlsr + gw_runoff;
   R into_river = R(0), gw_into_river = R(0), local_gw = gw_runoff;
   if (c.frac_routing && !(fl & F_SINK)) {
@@ -1167,6 +1167,7 @@ __device__ __forceinline__ R routing_cell(const DevCellsT<R> &c, int s, RState<R
       st.rf_loclake = r < R(0) ? R(0) : (r > R(1) ? R(1) : r);
     }
     dailyActualUse += remRiver0 - remainingUse;
+    if constexpr (RO) ro->actual_use = (double)dailyActualUse;   // routing.cpp:3746
     // the cell's bookkeeping (routing.cpp:3736, 3906-3919)
     W[11 * NN] += (double)dailyActualUse;
     if (wu->delayed) {   // routing.cpp:3900-3905

@@ -525,9 +525,11 @@ class Model:
     # routing's further monthly grids (wg_monthly_outputs_routing), which = 39 + index,
     # and the cell AET grids assembled from both sets
     MONTHLY_ROUTING = ["open_water_evap", "cell_surface_runoff", "gw_runoff", "land_area_frac", "loc_wetl_extent",
-                       "glo_wetl_extent", "res_inflow", "res_outflow", "consistent_precip", "surf_storage"]
-    MONTHLY.update({k: 6 + 33 + i for i, k in enumerate(MONTHLY_ROUTING)})
-    MONTHLY.update({"cell_aet": 49, "cell_aet_wca": 50})
+                       "glo_wetl_extent", "res_inflow", "res_outflow", "consistent_precip", "surf_storage",
+                       "actual_use", "nug"]
+    MONTHLY.update({k: i for i, k in enumerate(MONTHLY_ROUTING, 6 + len(MONTHLY_VERTICAL))})
+    MONTHLY.update({"cell_aet": 6 + len(MONTHLY_VERTICAL) + len(MONTHLY_ROUTING),
+                    "cell_aet_wca": 7 + len(MONTHLY_VERTICAL) + len(MONTHLY_ROUTING)})
     # routing's daily grids (wg_daily_outputs_routing), field = index
     DAILY_ROUTING = ["river_avail", "velocity", "cell_runoff", "cell_runoff_mm", "cell_surface_runoff", "gw_runoff",
                      "land_area_frac", "consistent_precip", "open_water_evap", "cell_aet"]
