@@ -233,6 +233,27 @@ class DropInCore {
   }
   // km3 -> mm over the continental area, as the reference writes its state file
   double to_mm(int i, double km3) const { return km3 / ((area[i] * (contfreq[i] / 100.)) / 1000000.); }
+  // The reference's output grids (grid_store 2 and 5/6) from the device's, for its
+  // own writers (daily.cpp:1969-2392, routing.cpp:6066-6834): a grid with
+  // g(cell, month) of the 12 months from output month m0 (wg_get_monthly's which),
+  // and with g(cell, day) of the 365 days from output day d0 (the vertical
+  // balance's or routing's daily field).  The context's grids must be on
+  // (Context::monthly_outputs and the others).
+  template <class MonthlyGrid>
+  void monthly_grid(int which, int m0, MonthlyGrid &g) {
+    std::vector<double> v((size_t)12 * n);
+    ctx.monthly(which, m0, 12, v.data());
+    for (int m = 0; m < 12; ++m)
+      for (int i = 0; i < n; ++i) g(i, m) = v[(size_t)m * n + i];
+  }
+  template <class DailyGrid>
+  void daily_grid(bool routing, int field, int d0, DailyGrid &g) {
+    std::vector<double> v((size_t)365 * n);
+    if (routing) ctx.daily_routing(field, d0, 365, v.data());
+    else ctx.daily_vertical(field, d0, 365, v.data());
+    for (int d = 0; d < 365; ++d)
+      for (int i = 0; i < n; ++i) g(i, d) = v[(size_t)d * n + i];
+  }
   // band of the reference's 100 (1..100) -> this region's band
   double band_of_ref(int i, int elev) const {
     if (elev < 1 || elev > 100) return 0.;
@@ -273,6 +294,11 @@ class DailyWaterBalanceGpu {
     }
   }
 
+  // the reference's monthly and daily grids of the vertical balance (DropInCore::monthly_grid)
+  template <class MonthlyGrid>
+  void monthly_grid(int which, int m0, MonthlyGrid &g) { core.monthly_grid(which, m0, g); }
+  template <class DailyGrid>
+  void daily_grid(int field, int d0, DailyGrid &g) { core.daily_grid(false, field, d0, g); }
   // the calibration parameters are read again at the next calcNewDay call
   void reload_calib_param() { core.params_loaded = false; }
   void set_slot_offset(int slot0) { core.slot_offset = slot0; }
@@ -325,6 +351,11 @@ class RoutingGpu {
     core_.month_slots.push_back(slot);
     if (day == last_day_in_month + 1) month_end(wghmState, additionalOutIn);
   }
+  // the reference's monthly and daily grids of routing (DropInCore::monthly_grid)
+  template <class MonthlyGrid>
+  void monthly_grid(int which, int m0, MonthlyGrid &g) { core_.monthly_grid(which, m0, g); }
+  template <class DailyGrid>
+  void daily_grid(int field, int d0, DailyGrid &g) { core_.daily_grid(true, field, d0, g); }
   // the land-area-fraction update is part of the queued routing (routing.cpp:5034-5188)
   template <class AdditionalOutputInputFile>
   void updateLandAreaFrac(AdditionalOutputInputFile &) {}

@@ -6,8 +6,19 @@
 #include "additionalOutputInputFile.h"
 #include "calib_param.h"
 #include "snowInElevationFile.h"
+#include "grid.h"
 #include "wghmStateFile.h"
 #include "wg_gpu.hpp"
+
+// the reference's own grid types filled from the device's output grids, for its writers
+void output_grids(wg::DailyWaterBalanceGpu &dailyWaterBalance, wg::RoutingGpu &routing, MonthlyGrid<false> &mg,
+                  MonthlyGrid<> &mg_storage, DailyGrid<false> &dg) {
+  dailyWaterBalance.monthly_grid(6, 0, mg);            // G_monthlyPrecipitation
+  dailyWaterBalance.monthly_grid(6 + 29, 0, mg_storage);   // G_monthlyCanopyStorage
+  dailyWaterBalance.daily_grid(0, 0, dg);              // G_daily365Precip
+  routing.monthly_grid(0, 0, mg);                      // G_monthlyRiverAvail
+  routing.daily_grid(0, 0, dg);                        // G_daily365RiverAvail
+}
 
 void day_loop(wg::DailyWaterBalanceGpu &dailyWaterBalance, wg::RoutingGpu &routing, WghmStateFile &wghmState,
               AdditionalOutputInputFile &additionalOutIn, SnowInElevationFile &snow_in_elevation,
