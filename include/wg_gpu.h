@@ -436,8 +436,8 @@ wg_status wg_set_step_sync(wg_ctx *ctx, int32_t flags);
 wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0);
 /* The vertical balance's monthly output grids as well (daily.cpp:1281-1386, the
  * reference's grid_store = 2 with grid_store_TypeForStorages = 0), on the calendar
- * of wg_monthly_outputs: FP64, one member, without the water temperature or GLWD
- * units (WG_ERR_UNSUPPORTED otherwise); accumulated by the wavefront's kernels, so the
+ * of wg_monthly_outputs: FP64, one member, without GLWD units, and not with both
+ * the water temperature and water use (WG_ERR_UNSUPPORTED otherwise); accumulated by the wavefront's kernels, so the
  * per-day wg_step_vertical refuses while they are on (the deferred per-day calls
  * of wg_set_deferred run through the wavefront).  enable 0 switches them off. */
 wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable);
@@ -468,7 +468,10 @@ wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable);
  * [km3], 9 SurfStor at the
  * month's end [km3], with water use 10 ActualUse and 11 NUg [km3]
  * (routing.cpp:3744-3747); 51 CellAET [mm] and 52 CellAETWCa [km3]
- * (routing.cpp:4572-4580; both sets of grids needed);
+ * (routing.cpp:4572-4580; both sets of grids needed); with the water
+ * temperature 53-58 G_monthlyMeanWaterTempRiver, -LocLake, -LocWetl, -GloLake,
+ * -Reservoir, -GloWetl [degC]: the mean over the month's days with a computed
+ * temperature, -9999 without one (routing.cpp:4375-4458);
  * out [nm][ncell][members], cell order. */
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out);
 /* Routing's further monthly grids (routing.cpp:3964-4238, 4525-4737, 5183-5186,

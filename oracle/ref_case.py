@@ -91,6 +91,9 @@ MONTHLY_ROUTING = ["river_avail", "min_river_avail", "max_river_avail", "cell_ru
                    "gw_storage", "open_water_evap", "cell_surface_runoff", "gw_runoff", "land_area_frac",
                    "loc_wetl_extent", "glo_wetl_extent", "res_inflow", "res_outflow", "consistent_precip",
                    "surf_storage", "actual_use", "nug", "cell_aet", "cell_aet_wca"]
+# with the water temperature, the monthly mean temperatures of the river and the
+# five kinds of water body (routing.cpp:4375-4458; -9999 without a computed day)
+MONTHLY_WTEMP = ["wt_river", "wt_loclake", "wt_locwetl", "wt_glolake", "wt_res", "wt_glowetl"]
 # routing's daily 365 grids the harness dumps with outputs=2
 DAILY_ROUTING = ["river_avail", "velocity", "cell_runoff", "cell_runoff_mm", "cell_surface_runoff", "gw_runoff",
                  "land_area_frac", "consistent_precip", "cell_aet"]
@@ -269,7 +272,7 @@ def run(region, P, T, S, doy0=1, stations=None, snapshots=None, workdir=None, wt
         o += ndays * len(stations)
     if outputs:   # the year's monthly grids [12][ncell] per field
         res["monthly"] = {}
-        for f in MONTHLY_VERTICAL + MONTHLY_ROUTING:
+        for f in MONTHLY_VERTICAL + MONTHLY_ROUTING + (MONTHLY_WTEMP if wtemp is not None else []):
             res["monthly"][f] = raw[o:o + 12 * n].reshape(12, n).copy()
             o += 12 * n
     if outputs == 2:   # the year's daily grids [365][ncell] per field

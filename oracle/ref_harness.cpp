@@ -101,6 +101,7 @@ int main(int argc, char **argv) {
   if (outputs) {   // monthly output grids, storages at the month's end (grid_store_TypeForStorages 0)
     options.grid_store = 2;
     options.outMinMaxRiverAvail = 1;
+    if (wtemp) { options.outWaterTempMonthly = 1; options.outWaterTempMonthlyAllSWB = 1; }   // routing.cpp:4375-4458
   }
   if (outputs == 2) {   // and the vertical balance's daily 365 grids (daily.cpp:1388-1399, 1472-1540)
     options.grid_store = 6;
@@ -363,6 +364,13 @@ int main(int argc, char **argv) {
     for (auto *g : vstor) dump(g);
     for (auto *g : vlate) dump(g);
     for (auto *g : rout) dump(g);
+    if (wtemp) {   // the monthly mean water temperatures (routing.cpp:4375-4458)
+      const MonthlyGrid<false> *wt[] = {
+          &routing.G_monthlyMeanWaterTempRiver, &routing.G_monthlyMeanWaterTempLocLake,
+          &routing.G_monthlyMeanWaterTempLocWetl, &routing.G_monthlyMeanWaterTempGloLake,
+          &routing.G_monthlyMeanWaterTempReservoir, &routing.G_monthlyMeanWaterTempGloWetl};
+      for (auto *g : wt) dump(g);
+    }
   }
   if (outputs == 2) {   // the year's daily grids [field][day][cell] (daily.cpp:1388-1399, 1472-1540)
     auto &w = dailyWaterBalance;

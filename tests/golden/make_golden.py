@@ -326,6 +326,31 @@ def main_outputs_wuse(names=None, name="swb_outputs_wuse_730d"):
     print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+def main_outputs_wtemp(names=None, name="swb_outputs_wtemp_365d"):
+    """The monthly output grids with the water temperature (calc_wtemp = 1, and so
+    fractional routing), among them the monthly mean temperatures of the river and
+    every water body, over one calendar year on the water-temperature region."""
+    if names and name not in names:
+        return
+    if not ref_case.available():
+        if not ref_case.build(REF_SOURCE):
+            raise SystemExit("reference sources not found; cannot regenerate fixtures")
+    region = wtemp_region(seed=21)
+    nd = 365
+    P, T, S = sy.forcing(region, nd, doy0=1)
+    T = (T - 9.0).astype(np.float32)     # cold winters: ice forms, grows and breaks up
+    LW, GWT = sy.water_temp_inputs(region, nd, T)
+    outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+    res = ref_case.run(region, P, T, S, doy0=1, stations=outl[:24], snapshots=[nd], wtemp=(LW, GWT), outputs=1)
+    extra = dict(P=P, T=T, S=S, LW=LW, GWT=GWT, doy0=np.array(1), stations=res["stations"],
+                 snap_days=np.array([nd]), discharge=res["discharge"], river_temp=res["river_temp"])
+    for k, v in res["monthly"].items():
+        extra[f"m_{k}"] = v
+    path = os.path.join(HERE, f"{name}.npz")
+    save_npz(region, path, **extra)
+    print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 def main_wtemp_wuse(names=None, name="swb_wtemp_wuse_120d"):
     """Water use together with the water temperature (calc_wtemp = 1, subtract_use
     = 2): the water-temperature region and a cold season across a year end."""
@@ -453,4 +478,5 @@ if __name__ == "__main__":
     main_wuse_glwd(sys.argv[1:])
     main_outputs(sys.argv[1:])
     main_outputs_wuse(sys.argv[1:])
+    main_outputs_wtemp(sys.argv[1:])
     main_wtemp_wuse(sys.argv[1:])

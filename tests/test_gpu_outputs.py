@@ -148,6 +148,44 @@ def test_output_grids_deferred_per_day_calls_same_bits():
         assert np.array_equal(a[k], b[k]), k
 
 
+PATH_WT = os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_wtemp_365d.npz")
+
+
+@pytest.mark.parametrize("dps,vertical", [(1, True), (5, True), (5, False)])
+def test_output_grids_with_water_temperature(dps, vertical):
+    """With the water temperature (and so fractional routing): the monthly mean
+    temperatures of the river and every water body (-9999 without a computed
+    day), routing's aggregates and, in the wavefront's variant with both, the
+    vertical balance's grids, against the reference's over one calendar year."""
+    from watergap2_gb300.gpu import Model
+    from watergap2_gb300.region import load_npz
+    region, ex = load_npz(PATH_WT)
+    P, T, S = ex["P"], ex["T"], ex["S"]
+    nd = P.shape[0]
+    m = Model(region, max_days=nd, stations=ex["stations"], days_per_step=dps, water_temp=True)
+    m.set_water_temp_inputs(ex["GWT"], region.extras["river_length_file"])
+    m.upload_longwave(0, ex["LW"])
+    m.monthly_outputs(12, doy_day0=1)
+    m.monthly_outputs_vertical(vertical)
+    with pytest.raises(Exception):
+        m.monthly_outputs_routing(True)                # routing's further grids: not with the water temperature
+    m.upload_forcing(0, P, T, S)
+    m.run_days(1, 0, nd)
+    errs = {}
+    for k in m.MONTHLY_WTEMP:
+        g, r = m.monthly(k), ex["m_" + k]
+        assert np.array_equal(g == -9999., r == -9999.), k   # the same months without a computed temperature
+        ok = r != -9999.
+        # a temperature is an energy over a heat capacity in K less 273.15: held to
+        # 1e-11 of the absolute temperature, as the water-temperature tests hold it
+        errs[k] = float(np.max(np.abs(g[ok] - r[ok]) / (np.abs(r[ok]) + 273.15) * (RTOL / 1e-11)))
+    errs.update({k: max_rel_err(m.monthly(k), ex["m_" + r]) for k, r in ROUTING.items()})
+    if vertical:
+        errs.update({k: max_rel_err(m.monthly(k), ex["m_" + k]) for k in m.MONTHLY_VERTICAL})
+    bad = {k: v for k, v in errs.items() if not v <= RTOL}
+    assert not bad, bad
+
+
 def test_routing_grids_refused_with_fractional_routing():
     from watergap2_gb300.gpu import Model, WgError
     from watergap2_gb300.region import load_npz

@@ -2087,6 +2087,10 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
     cudaFree(ctx->mon_rbuf);
     ctx->mon_rbuf = nullptr;
   }
+  if (ctx->mon_tbuf) {
+    cudaFree(ctx->mon_tbuf);
+    ctx->mon_tbuf = nullptr;
+  }
   {   // the daily storage record and the daily grids are kept
     const DevMonthly keep = ctx->mon;
     ctx->mon = DevMonthly{};
@@ -2124,6 +2128,12 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
     if (e == cudaSuccess) e = vconst_upload(ctx);
     if (e == cudaSuccess) m.vert = ctx->mon_vbuf;
   }
+  if (e == cudaSuccess && ctx->wt.enabled) {   // the monthly mean water temperatures (sums and day counts)
+    const size_t b = (size_t)12 * per * sizeof(double);
+    e = cudaMalloc((void **)&ctx->mon_tbuf, b);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->mon_tbuf, 0, b, ctx->stream);
+    if (e == cudaSuccess) m.wtemp = ctx->mon_tbuf;
+  }
   if (e == cudaSuccess && ctx->mon_rout_on) {   // routing's further grids, on the same calendar
     const size_t b = (size_t)wg::ROUT_FIELDS * per * sizeof(double);
     e = cudaMalloc((void **)&ctx->mon_rbuf, b);
@@ -2135,12 +2145,13 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
   return cuda_fail(ctx, e, "monthly_outputs");
 }
 
-// the output grids' conditions: FP64, one member, without the water temperature
-// or GLWD units; routing's further grids also without fractional routing (its
-// groundwater runoff splits between the river and the water bodies)
+// the output grids' conditions: FP64, one member, without GLWD units; with the
+// water temperature only the vertical balance's, and not with water use too;
+// routing's further grids also without fractional routing (its groundwater
+// runoff splits between the river and the water bodies)
 static wg_status outputs_supported(const wg_ctx *ctx, bool routing) {
-  if (ctx->precision != 0 || ctx->members != 1 || ctx->wt.enabled || (ctx->wu.enabled && ctx->wu.glwd))
-    return WG_ERR_UNSUPPORTED;
+  if (ctx->precision != 0 || ctx->members != 1 || (ctx->wu.enabled && ctx->wu.glwd)) return WG_ERR_UNSUPPORTED;
+  if (ctx->wt.enabled && (routing || ctx->wu.enabled)) return WG_ERR_UNSUPPORTED;
   if (routing && ctx->frac_routing) return WG_ERR_UNSUPPORTED;
   return WG_OK;
 }
@@ -2305,9 +2316,31 @@ wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable) {
 }
 
 wg_status wg_get_monthly(wg_ctx *ctx, int32_t which, int32_t m0, int32_t nm, double *out) {
-  constexpr int V0 = 6, R0 = V0 + wg::VOUT_FIELDS, AET = R0 + wg::ROUT_FIELDS;   // 6, 39, 51
-  if (!ctx || !out || which < 0 || which > AET + 1 || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths)
+  constexpr int V0 = 6, R0 = V0 + wg::VOUT_FIELDS, AET = R0 + wg::ROUT_FIELDS, WT0 = AET + 2;   // 6, 39, 51, 53
+  if (!ctx || !out || which < 0 || which >= WT0 + 6 || m0 < 0 || nm < 0 || m0 + nm > ctx->mon.nmonths)
     return WG_ERR_INVALID;
+  if (which >= WT0) {   // the monthly mean water temperatures: -9999 without a computed day
+    if (!ctx->mon.wtemp) return WG_ERR_UNSUPPORTED;
+    WG_FLUSH(ctx);
+    wg_status st = wg_synchronize(ctx);
+    if (st != WG_OK) return st;
+    const size_t N = ctx->nstate(), per = (size_t)ctx->mon.nmonths * N;
+    const int k = which - WT0;
+    std::vector<double> sum((size_t)nm * N), cnt((size_t)nm * N);
+    cudaError_t e = cudaMemcpy(sum.data(), ctx->mon_tbuf + k * per + (size_t)m0 * N, sum.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(cnt.data(), ctx->mon_tbuf + (6 + k) * per + (size_t)m0 * N, cnt.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "get_monthly");
+    const auto &c2s = ctx->topo.cell_of_slot;
+    for (int mm = 0; mm < nm; ++mm)
+      for (int sl = 0; sl < ctx->n; ++sl) {
+        const size_t j = (size_t)mm * N + sl;
+        out[(size_t)mm * ctx->n + c2s[sl]] = cnt[j] > 0. ? sum[j] / cnt[j] : -9999.;
+      }
+    return WG_OK;
+  }
   if (which >= V0 && which < R0 && !ctx->mon.vert) return WG_ERR_UNSUPPORTED;
   if (which >= R0 && !ctx->mon.rext) return WG_ERR_UNSUPPORTED;
   if (which >= AET && !ctx->mon.vert) return WG_ERR_UNSUPPORTED;   // cell AET: land AET + open-water evaporation

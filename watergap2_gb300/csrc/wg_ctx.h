@@ -73,6 +73,7 @@ struct wg_ctx {
   bool mon_vert_on = false;
   double *mon_dbuf = nullptr;              // its daily grids (wg_daily_outputs_vertical)
   double *mon_rbuf = nullptr;              // routing's further monthly grids (wg_monthly_outputs_routing)
+  double *mon_tbuf = nullptr;              // the monthly mean water temperatures (with the water temperature)
   bool mon_rout_on = false;
   double *mon_drbuf = nullptr;             // routing's daily grids (wg_daily_outputs_routing)
   double *mon_vconst = nullptr;            // their constants (DevMonthly::vconst)
@@ -154,6 +155,7 @@ struct wg_ctx {
     if (mon_vbuf) cudaFree(mon_vbuf);
     if (mon_dbuf) cudaFree(mon_dbuf);
     if (mon_rbuf) cudaFree(mon_rbuf);
+    if (mon_tbuf) cudaFree(mon_tbuf);
     if (mon_drbuf) cudaFree(mon_drbuf);
     if (mon_vconst) cudaFree(mon_vconst);
     for (void *p : allocs) cudaFree(p);

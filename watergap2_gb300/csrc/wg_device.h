@@ -188,6 +188,10 @@ struct DevMonthly {
   int32_t dvert_days;
   double *vconst;        // with any of vert, dvert, rext, drout: [VCONST_FIELDS][N]
   double *rext;          // null, or routing's further monthly grids [ROUT_FIELDS][nmonths][N]
+  // null, or with the water temperature the monthly mean temperatures' sums
+  // (fields 0-5: the river, local lake, local wetland, global lake, reservoir,
+  // global wetland) and day counts (6-11) [12][nmonths][N]
+  double *wtemp;
   double *drout;         // null, or routing's daily grids [DROUT_FIELDS][drout_days][N]
   int32_t drout_days;
   // the day-end routing storages of every cell and output day, [day][7][n*members]

@@ -482,6 +482,14 @@ __global__ void __launch_bounds__(WaveBounds<R, ENS, VAW>::threads, WaveBounds<R
             const float g = wtp.gwt[s];
             wtd.begin(&wtp, s, si, N, fl, (double)f.temp[fo], (double)f.swrad[fo], (double)wtp.lw[fo], (double)o.owp,
                       (double)c.area[s], g < 0.f ? 0. : (double)g, up, e_up);
+            if (mon.wtemp) {   // the monthly mean temperatures of the day's month
+              const int yd = mon.doy_day0 - 1 + oday0 + d;
+              const int mi = (yd / 365) * 12 + month_of(yd % 365 + 1) - mon.month0;
+              if (mi >= 0 && mi < mon.nmonths) {
+                wtd.msum = mon.wtemp + (size_t)mi * N + si;
+                wtd.ms = (size_t)mon.nmonths * N;
+              }
+            }
           }
           const size_t wrow = WU ? (size_t)wu.row_of_fday[fday0 + d] * WU_FIELDS * (size_t)n : 0;
           R tv;
@@ -827,8 +835,9 @@ template <class R>
 static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false, bool gl = false,
                                bool vo = false, bool ro = false) {
   if (gl && (ens || wt || !wu || !std::is_same<R, double>::value)) return nullptr;   // GLWD units: FP64, one member
-  if (vo || ro) {   // the output grids: FP64, one member, without the water temperature or GLWD units
-    if (ens || wt || gl || !std::is_same<R, double>::value) return nullptr;
+  if (vo || ro) {   // the output grids: FP64, one member, without GLWD units
+    if (ens || gl || !std::is_same<R, double>::value) return nullptr;
+    if (wt) return (wu || ro) ? nullptr : pipeline_fn_x<R, 9>(fused, vaw);   // the vertical balance's with the water temperature
     if (wu) return pipeline_fn_x<R, 26>(fused, vaw);   // with water use: all outputs in one variant
     return ro ? pipeline_fn_x<R, 24>(fused, vaw) : pipeline_fn_x<R, 8>(fused, vaw);
   }

@@ -413,6 +413,16 @@ struct WtDay {
   double loclake_t, locwetl_t, ll_out, lw_out;   // the local bodies' temperatures and outflows
   double mix, chain_in;     // temperature and volume of the next global body's (or the river's) inflow
   double last;              // the temperature calcWTemp reports for the cell (its last water body's)
+  // the monthly mean temperatures (routing.cpp:4375-4458): sums (k) and day
+  // counts (6 + k) of the day's month at msum[k * ms], or null
+  double *msum = nullptr;
+  size_t ms = 0;
+  __device__ __forceinline__ void file(int k, double tk) {
+    if (msum && tk >= 0.) {   // a computed temperature (calcWTempReturns[k] >= 0)
+      msum[k * ms] += tk;
+      msum[(6 + k) * ms] += 1.;
+    }
+  }
 
   // tot_in/e_in: the upstream cells' river outflow of the day, summed, and the
   // energy it carries (sum of volume x rho c (T + 273.15))
@@ -455,6 +465,7 @@ struct WtDay {
     temp(k) = temp_k == WT_NO_TEMP ? keep() : temp_k;
     ice(k) = ice_k;
     last = temp_k;
+    file(k, temp_k);
   }
   // local lake: storage before the day plus capacity, evaporation after any
   // reduction, reduction factor, outflow
@@ -515,6 +526,7 @@ struct WtDay {
                         &ic);
       ice0 = ic;
     }
+    file(0, last);   // the cell's reported temperature (calcWTempReturns[0])
     if (!(fl & F_LOCLAKE)) absent(1);
     if (!(fl & F_LOCWETL)) absent(2);
     if (!(fl & F_GLOLAKE)) absent(3);

@@ -530,6 +530,9 @@ class Model:
     MONTHLY.update({k: i for i, k in enumerate(MONTHLY_ROUTING, 6 + len(MONTHLY_VERTICAL))})
     MONTHLY.update({"cell_aet": 6 + len(MONTHLY_VERTICAL) + len(MONTHLY_ROUTING),
                     "cell_aet_wca": 7 + len(MONTHLY_VERTICAL) + len(MONTHLY_ROUTING)})
+    # with the water temperature: the monthly mean temperatures (-9999 without a computed day)
+    MONTHLY_WTEMP = ["wt_river", "wt_loclake", "wt_locwetl", "wt_glolake", "wt_res", "wt_glowetl"]
+    MONTHLY.update({k: i for i, k in enumerate(MONTHLY_WTEMP, 8 + len(MONTHLY_VERTICAL) + len(MONTHLY_ROUTING))})
     # routing's daily grids (wg_daily_outputs_routing), field = index
     DAILY_ROUTING = ["river_avail", "velocity", "cell_runoff", "cell_runoff_mm", "cell_surface_runoff", "gw_runoff",
                      "land_area_frac", "consistent_precip", "open_water_evap", "cell_aet"]
