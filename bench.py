@@ -768,8 +768,8 @@ def run_profile_case(steps: int = 24, warm_steps: int = 200, outputs: bool = Fal
     next chunk's vertical balance (52, 53, ...).  One kernel per capture:
       ncu --set full --clock-control none -k regex:k_pipeline -s 50 -c 2 -o prof python bench.py --profile
       ncu --set full --clock-control none -k regex:k_vertical_ahead -s 1 -c 1 -o prof python bench.py --profile
-    With outputs (--profile-outputs) the run fills routing's and the vertical
-    balance's monthly grids (the same launches, their output variants)."""
+    With outputs (--profile-outputs) the run fills every monthly grid of routing
+    and the vertical balance (the same launches, their output variants)."""
     from watergap2_gb300 import synthetic as sy
     from watergap2_gb300.gpu import Model
     region = sy.region_global()
@@ -779,6 +779,7 @@ def run_profile_case(steps: int = 24, warm_steps: int = 200, outputs: bool = Fal
     if outputs:
         m.monthly_outputs(nd // 28 + 1, doy_day0=1)
         m.monthly_outputs_vertical(True)
+        m.monthly_outputs_routing(True)
     m.upload_forcing(0, P, T, S)
     m.run_steps(1, 0, nd, 0, warm_steps)
     m.synchronize()
