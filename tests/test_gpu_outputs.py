@@ -227,3 +227,26 @@ def test_per_day_vertical_refused_with_vertical_grids():
     m.daily_outputs_vertical(0)
     m.step_vertical(1, 0)
     m.step_routing(1, 0)
+
+
+def test_autotune_leaves_the_monthly_sums():
+    """The autotuner's trial runs add nothing to the monthly grids: grids after
+    tuning equal those of a run without it."""
+    from watergap2_gb300.gpu import Model
+    from watergap2_gb300.region import load_npz
+    region, ex = load_npz(PATH)
+    nd = 90
+    P, T, S = ex["P"][:nd], ex["T"][:nd], ex["S"][:nd]
+    out = []
+    for tune in (False, True):
+        m = Model(region, max_days=nd, days_per_step=5)
+        m.monthly_outputs(3, doy_day0=1)
+        m.monthly_outputs_vertical(True)
+        m.monthly_outputs_routing(True)
+        m.upload_forcing(0, P, T, S)
+        if tune:
+            assert m.autotune(1, 0, nd, 0, 8)["trials"] > 0
+        m.run_days(1, 0, nd)
+        out.append({k: m.monthly(k) for k in ["river_avail", "prec", "pet", "open_water_evap", "land_area_frac"]})
+    for k in out[0]:
+        assert np.allclose(out[0][k], out[1][k], rtol=1e-12, atol=0), k

@@ -201,6 +201,13 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
   int32_t tmp = 0;
   wg_status st = snapshot_save(ctx);
   if (st != WG_OK) return st;
+  // the trials must not add to the monthly sums (their days run again after the
+  // state is restored); the day's grids they write are written again the same
+  const DevMonthly mon0 = ctx->mon;
+  ctx->mon.enabled = 0;
+  ctx->mon.vert = nullptr;
+  ctx->mon.rext = nullptr;
+  ctx->mon.wtemp = nullptr;
   // candidates: block sizes 64..512 (for ensembles: members of one cell per block,
   // or whole cells per block when a cell has fewer members), chunk lengths 8..ring
   std::vector<int> ths = {64, 128, 256, 512};
@@ -273,6 +280,7 @@ wg_status wg_autotune(wg_ctx *ctx, int32_t doy0, int32_t fday0, int32_t ndays, i
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  ctx->mon = mon0;
   wg_status st2 = snapshot_restore(ctx);
   if (st == WG_OK) st = st2;
   if (st == WG_OK) st = wg_synchronize(ctx);
