@@ -527,8 +527,11 @@ wg_status wg_set_member_factors(wg_ctx *ctx, const float *prec_factor, const flo
  * fractions, the wavefront's outflow buffer and the balance sums): save, and
  * restore as often as needed -- e.g. the start state of each calibration run,
  * or a forecast state of data assimilation.  One snapshot per context; the
- * autotuner uses the same one.  No counterpart in the reference (it re-reads
- * state files). */
+ * autotuner uses the same one (its trial runs leave the monthly output grids
+ * alone).  The output grids and the station discharge are not part of it: days
+ * run again after a restore add to the monthly sums again (switch the grids off,
+ * or on again to zero them).  No counterpart in the reference (it re-reads state
+ * files). */
 wg_status wg_save_snapshot(wg_ctx *ctx);
 wg_status wg_restore_snapshot(wg_ctx *ctx);
 
