@@ -436,8 +436,8 @@ wg_status wg_set_step_sync(wg_ctx *ctx, int32_t flags);
 wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0);
 /* The vertical balance's monthly output grids as well (daily.cpp:1281-1386, the
  * reference's grid_store = 2 with grid_store_TypeForStorages = 0), on the calendar
- * of wg_monthly_outputs: FP64, one member, without GLWD units, and not with both
- * the water temperature and water use (WG_ERR_UNSUPPORTED otherwise); accumulated by the wavefront's kernels, so the
+ * of wg_monthly_outputs: FP64, one member, and not with both the water
+ * temperature and water use (WG_ERR_UNSUPPORTED otherwise); accumulated by the wavefront's kernels, so the
  * per-day wg_step_vertical refuses while they are on (the deferred per-day calls
  * of wg_set_deferred run through the wavefront).  enable 0 switches them off. */
 wg_status wg_monthly_outputs_vertical(wg_ctx *ctx, int32_t enable);

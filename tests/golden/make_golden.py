@@ -295,11 +295,13 @@ def main_outputs(names=None, name="swb_outputs_730d"):
     print(f"{name}: {region.ncell} cells x {nd} days -> {os.path.getsize(path) / 1e6:.2f} MB")
 
 
-def main_outputs_wuse(names=None, name="swb_outputs_wuse_730d"):
+def main_outputs_wuse(names=None, name="swb_outputs_wuse_730d", glwd=False):
     """The output grids of main_outputs with water use met in the cell
     (subtract_use = 2): the same region, two calendar years, the water-use inputs
     of swb_wuse_420d; the grids hold the second year, among them the monthly
-    actual use and NUg (routing.cpp:3744-3747)."""
+    actual use and NUg (routing.cpp:3744-3747).  glwd: the riparian cells' NUs
+    met by their global lake's or reservoir's outflow cell (aggrNUsGloLakResOpt
+    = 1, the units of synthetic.glwd_units)."""
     if names and name not in names:
         return
     if not ref_case.available():
@@ -310,11 +312,14 @@ def main_outputs_wuse(names=None, name="swb_outputs_wuse_730d"):
     P, T, S = sy.forcing(region, nd, doy0=1)
     nus, nug, wdr, cons, frgi = sy.water_use_inputs(region, 3, seed=13)
     outl = np.nonzero((region.downstream < 0) & (region.ldd >= 0))[0]
+    unit = sy.glwd_units(region) if glwd else None
     res = ref_case.run(region, P, T, S, doy0=1, stations=outl[:24], snapshots=[nd], outputs=2,
-                       wuse=(nus, nug, wdr, cons, frgi))
+                       wuse=(nus, nug, wdr, cons, frgi), glwd_unit=unit)
     extra = dict(P=P, T=T, S=S, NUS=nus, NUG=nug, WDR=wdr, CONS=cons, FRGI=frgi, doy0=np.array(1),
                  delayed=np.array(0), stations=res["stations"], snap_days=np.array([nd]),
                  discharge=res["discharge"])
+    if glwd:
+        extra["GLWD"] = unit
     for k, v in res["monthly"].items():
         extra[f"m_{k}"] = v
     days = np.unique(np.r_[0:3, 31:34, np.arange(0, 365, 13), 364])
@@ -478,5 +483,6 @@ if __name__ == "__main__":
     main_wuse_glwd(sys.argv[1:])
     main_outputs(sys.argv[1:])
     main_outputs_wuse(sys.argv[1:])
+    main_outputs_wuse(sys.argv[1:], name="swb_outputs_glwd_730d", glwd=True)
     main_outputs_wtemp(sys.argv[1:])
     main_wtemp_wuse(sys.argv[1:])

@@ -29,6 +29,8 @@ RTOL = 1e-10
 PATH = os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_730d.npz")
 # the same grids with water use met in the cell (subtract_use = 2)
 PATH_WU = os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_wuse_730d.npz")
+# and with the riparian cells' NUs met by their outflow cell (GLWD units)
+PATH_GL = os.path.join(os.path.dirname(__file__), "golden", "swb_outputs_glwd_730d.npz")
 Y2 = 365   # the grids are the second year's
 # with water use, routing's flux grids against a floor of 1 % of each grid's largest value
 RTOL_WU = 1e-7
@@ -55,10 +57,11 @@ def _built():
 def _two_years(days_per_step=0, deferred=False, routing=True, wuse=False):
     from watergap2_gb300.gpu import Model
     from watergap2_gb300.region import load_npz
-    region, ex = load_npz(PATH_WU if wuse else PATH)
+    region, ex = load_npz({False: PATH, True: PATH_WU, "glwd": PATH_GL}[wuse])
     P, T, S = ex["P"], ex["T"], ex["S"]
     nd = P.shape[0]
-    m = Model(region, max_days=nd, stations=ex["stations"], days_per_step=days_per_step, water_use=wuse)
+    kw = {"glwd_unit": ex["GLWD"]} if wuse == "glwd" else {}
+    m = Model(region, max_days=nd, stations=ex["stations"], days_per_step=days_per_step, water_use=bool(wuse), **kw)
     if wuse:
         m.set_water_use_inputs(ex["FRGI"])
         m.upload_water_use_run(0, 1, nd, (ex["NUS"], ex["NUG"], ex["WDR"], ex["CONS"]))
@@ -87,7 +90,7 @@ def _two_years(days_per_step=0, deferred=False, routing=True, wuse=False):
 
 
 @pytest.mark.parametrize("dps,routing,wuse", [(1, True, False), (5, True, False), (5, False, False),
-                                              (1, True, True), (5, True, True)])
+                                              (1, True, True), (5, True, True), (5, True, "glwd")])
 def test_output_grids_match_reference(dps, routing, wuse):
     """All grids (routing's further grids with the vertical balance's: the
     wavefront's variant with both), the vertical balance's grids alone (its

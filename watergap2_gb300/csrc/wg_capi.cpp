@@ -2145,12 +2145,12 @@ wg_status wg_monthly_outputs(wg_ctx *ctx, int32_t nmonths, int32_t doy_day0) {
   return cuda_fail(ctx, e, "monthly_outputs");
 }
 
-// the output grids' conditions: FP64, one member, without GLWD units; with the
-// water temperature only the vertical balance's, and not with water use too;
-// routing's further grids also without fractional routing (its groundwater
-// runoff splits between the river and the water bodies)
+// the output grids' conditions: FP64, one member; with the water temperature
+// only the vertical balance's, and not with water use too; routing's further
+// grids also without fractional routing (its groundwater runoff splits between
+// the river and the water bodies)
 static wg_status outputs_supported(const wg_ctx *ctx, bool routing) {
-  if (ctx->precision != 0 || ctx->members != 1 || (ctx->wu.enabled && ctx->wu.glwd)) return WG_ERR_UNSUPPORTED;
+  if (ctx->precision != 0 || ctx->members != 1) return WG_ERR_UNSUPPORTED;
   if (ctx->wt.enabled && (routing || ctx->wu.enabled)) return WG_ERR_UNSUPPORTED;
   if (routing && ctx->frac_routing) return WG_ERR_UNSUPPORTED;
   return WG_OK;

@@ -835,9 +835,10 @@ template <class R>
 static const void *pipeline_fn(bool fused, bool ens, bool vaw, bool wt = false, bool wu = false, bool gl = false,
                                bool vo = false, bool ro = false) {
   if (gl && (ens || wt || !wu || !std::is_same<R, double>::value)) return nullptr;   // GLWD units: FP64, one member
-  if (vo || ro) {   // the output grids: FP64, one member, without GLWD units
-    if (ens || gl || !std::is_same<R, double>::value) return nullptr;
+  if (vo || ro) {   // the output grids: FP64, one member
+    if (ens || !std::is_same<R, double>::value) return nullptr;
     if (wt) return (wu || ro) ? nullptr : pipeline_fn_x<R, 9>(fused, vaw);   // the vertical balance's with the water temperature
+    if (gl) return pipeline_fn_x<R, 30>(fused, vaw);   // water use over GLWD units: all outputs in one variant
     if (wu) return pipeline_fn_x<R, 26>(fused, vaw);   // with water use: all outputs in one variant
     return ro ? pipeline_fn_x<R, 24>(fused, vaw) : pipeline_fn_x<R, 8>(fused, vaw);
   }
