@@ -21,7 +21,7 @@ from helpers import STATE_KEYS, STORAGES, max_rel_err, state_errors
 pytestmark = pytest.mark.gpu
 RTOL = 1e-10
 FIXTURES = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                  if not ({"wtemp", "wuse"} & set(os.path.basename(p)[:-4].split("_")))
+                  if not ({"wtemp", "wuse", "glwd"} & set(os.path.basename(p)[:-4].split("_")))
                   and not os.path.basename(p).startswith("config"))   # regenerated workloads: own tests   # test_gpu_wtemp.py, test_gpu_wuse.py
 
 

@@ -19,7 +19,7 @@ from oracle import Oracle
 from watergap2_gb300.region import load_npz
 
 FIXTURES = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                  if not ({"wtemp", "wuse"} & set(os.path.basename(p)[:-4].split("_")))
+                  if not ({"wtemp", "wuse", "glwd"} & set(os.path.basename(p)[:-4].split("_")))
                   and not os.path.basename(p).startswith("config"))   # regenerated workloads: own tests   # test_wtemp_oracle.py, test_wuse_oracle.py
 STATE_KEYS = ["canopy", "soil", "snow", "lai_days", "lai_status", "lai_precsum", "gw", "river", "loclake",
               "locwetl", "glolake", "glowetl", "res", "rf_loclake", "rf_locwetl", "rf_glolake", "rf_glowetl",
